@@ -1,0 +1,344 @@
+"""Benchmark: RieCG node-updates/s on one GB300 (and N independent replicas).
+
+Workload (one "step" = one full 3-stage RieCG time step over the whole mesh):
+unit cube with 129^3 nodes (2,146,689 nodes, 12,582,912 tets), interior nodes
+jittered by a seeded U(-0.2h, 0.2h), seeded random input numbering renumbered
+by reverse Cuthill-McKee, smooth density wave rho = 1 + 0.2 sin sin sin,
+u = (1, 0.5, 0.25), p = 1, gamma 1.4, Rusanov flux with MUSCL, symmetry BCs on
+all six faces, CFL 0.5.  Synthetic data: the mesh and state are generated.
+
+  value  node-updates/s = nodes x steps / device time (state resident in HBM)
+  e2e    the same through the C ABI with host buffers: every step uploads U
+         from pinned host memory, advances one step and downloads U
+  roofline  for the dominant kernel (riecg_rhs_update), algorithmic bytes per
+         launch / mean launch time from CUDA events taken inside the timed
+         region, against the measured HBM copy bandwidth
+  cpu_baseline  the oracle (serial C++ restatement of the reference loops) on
+         host cores, on a bounded sample (a 49^3 cube, 30 steps; the per-node
+         work does not depend on the mesh size)
+
+--impl reference runs the reference's CPU arithmetic (the oracle port; the
+reference itself needs Charm++ and cannot be built on the GPU machine) on all host
+cores, one independent mesh partition per core, and prints the same metric.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "RieCG node-updates/s"
+UNIT = "node-updates/s"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------------ clocks
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            for k, nm in enumerate(names):
+                if r[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(self.rows)}
+
+
+# ------------------------------------------------------------------ workload
+
+def wave_state(coord, gamma=1.4):
+    x, y, z = coord
+    r = 1.0 + 0.2 * np.sin(2 * np.pi * x) * np.sin(2 * np.pi * y) * np.sin(2 * np.pi * z)
+    u = np.array([1.0, 0.5, 0.25])
+    U = np.empty((coord.shape[1], 5))
+    U[:, 0] = r
+    U[:, 1:4] = r[:, None] * u[None, :]
+    U[:, 4] = 1.0 / (gamma - 1.0) + 0.5 * r * (u @ u)
+    return U
+
+
+def build_ops(n, seed=0):
+    from xyst_gb300 import mesh, riecg
+
+    m = mesh.cube(n, jitter=0.2, seed=seed, numbering="random", perm_seed=seed + 1)
+    return riecg.operators(m, sym_sets=[1, 2, 3, 4, 5, 6], renumber=True)
+
+
+def kernel_bytes(n, nent, fp32):
+    """Algorithmic (compulsory) bytes per launch: every array the kernel must
+    read or write once; gathered neighbour records are re-reads and excluded."""
+    F = 4 if fp32 else 8
+    Wb, Gb, Db = 8 * F, 16 * F, 4 + 3 * F
+    grad = n * (Wb + 8 + 4 + Gb) + nent * Db
+    rhs12 = n * (Wb + Gb + 8 + 4 + 40 + 40 + Wb) + nent * Db  # stages 1,2
+    rhs0 = rhs12 + n * 80                                       # stage 0: U read, Un write
+    return {"riecg_grad": grad, "riecg_rhs_update": (rhs0 + 2 * rhs12) / 3.0}
+
+
+# ------------------------------------------------------------------ CPU leg
+
+def cpu_sample(n=41, steps=3, procs=1):
+    """Oracle node-updates/s on `procs` independent n^3 cubes, one per process."""
+    code = r"""
+import sys, time, json
+sys.path.insert(0, %r)
+import numpy as np, oracle
+from xyst_gb300 import mesh
+from bench import wave_state
+n, steps = %d, %d
+m = mesh.cube(n, jitter=0.2, seed=0)
+c, ip = m["coord"], m["inpoel"]
+v = oracle.vol(c, ip); e, d = oracle.domint(c, ip)
+tri = np.concatenate([m["bface"][s] for s in sorted(m["bface"])])
+nodes, norms, symset = oracle.sym_bc(c, m["bface"], [1,2,3,4,5,6])
+besym = np.isin(tri, list(symset)).astype(np.uint8)
+o = oracle.RieCG(c, v, e, d, tri, besym)
+o.set_sym(nodes, norms); o.set_state(wave_state(c)); o.bc()
+t0 = time.perf_counter(); o.run(steps); t1 = time.perf_counter()
+print(json.dumps({"n": c.shape[1], "steps": steps, "s": t1 - t0}))
+""" % (ROOT, n, steps)
+    import oracle
+    oracle.build()
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    ps = [subprocess.Popen([sys.executable, "-c", code], stdout=subprocess.PIPE, text=True,
+                           env=env) for _ in range(procs)]
+    res = []
+    for p in ps:
+        out, _ = p.communicate()
+        res.append(json.loads(out.strip().splitlines()[-1]))
+    nodes = res[0]["n"]
+    worst = max(r["s"] for r in res)
+    value = procs * nodes * steps / worst
+    return {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
+            "sample": f"{procs}x independent {n}^3 cube ({nodes} nodes), {steps} steps each, "
+                      f"oracle C++ restatement, 1 thread per process, {worst:.2f} s"}
+
+
+# ------------------------------------------------------------------ GPU leg
+
+def run_gpu(args, rank, world):
+    from xyst_gb300 import lib, riecg
+
+    t_setup = time.perf_counter()
+    ops = build_ops(args.n, seed=rank)
+    n = ops["coord"].shape[1]
+    U0 = wave_state(ops["coord"])
+    ctx = lib.Context(args.device if world == 1 else int(os.environ.get("LOCAL_RANK", 0)))
+    prec = args.precision
+    r = riecg.from_operators(ctx, ops, precision=prec)
+    t_setup = time.perf_counter() - t_setup
+    nent = 2 * ops["edges"].shape[0]
+    r.set_state(U0)
+    r.bc()
+    # warm-up
+    r.run(args.warmup)
+    barrier(world)
+    # timed region: device-resident state, per-kernel events on the ctx stream
+    r.set_state(U0)
+    r.bc()
+    r.profile(True)
+    with Clocks(int(os.environ.get("LOCAL_RANK", args.device))) as ck:
+        barrier(world)
+        dts, ms = r.run(args.steps)
+        barrier(world)
+    r.profile(False)
+    kt = r.kernel_times()
+    # the same step count without events (the headline device time)
+    r.set_state(U0)
+    r.bc()
+    barrier(world)
+    dts2, ms_plain = r.run(args.steps)
+    barrier(world)
+    # e2e through the C ABI with host buffers
+    e2e = e2e_run(r, U0, args.steps, world)
+    out = {"n": n, "nent": nent, "ms": ms_plain, "ms_events": ms, "kt": kt, "clocks": ck.summary(),
+           "e2e_ms": e2e, "setup_s": t_setup, "dts": dts2, "dev_bytes": ctx.device_bytes()}
+    ctx.close()
+    return out
+
+
+def e2e_run(r, U0, steps, world):
+    try:
+        import torch
+        host = torch.empty(U0.shape, dtype=torch.float64, pin_memory=True).numpy()
+    except Exception:
+        host = np.empty_like(U0)
+    host[:] = U0
+    r.set_state(host)
+    r.run(1)
+    r.state()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        r.set_state(host)  # H2D of the step's input state
+        r.run(1)
+        host[:] = r.state()[0]  # D2H of the step's result
+    t1 = time.perf_counter()
+    barrier(world)
+    return (t1 - t0) * 1e3
+
+
+_dist = None
+
+
+def barrier(world):
+    if world > 1 and _dist is not None:
+        _dist.barrier()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="xg", choices=["xg", "reference"])
+    ap.add_argument("--n", type=int, default=129)
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--device", type=int, default=0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    global _dist
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        _dist = dist
+    config = {"workload": f"RieCG Euler, {args.n}^3-node jittered cube (Kuhn 6-tet split), "
+                          "smooth density wave, Rusanov+MUSCL, symmetry BCs, CFL 0.5, 3-stage RK",
+              "nodes": args.n ** 3, "precision": ("FP32 gradients/fluxes, FP64 state/update"
+                                                  if args.precision == "fp32" else "FP64"),
+              "l2": "no flush needed: working set > 129 MB L2",
+              "parallelism": f"replicas x{args.gpus}"}
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        procs = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        for _ in range(args.warmup):
+            pass
+        cb = cpu_sample(n=49, steps=10, procs=procs)
+        line = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": args.n ** 3 / cb["value"] * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": config, "impl": "reference", "cpu_baseline": cb,
+                "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0},
+                "wall_s": time.perf_counter() - t0}
+        print(json.dumps(line))
+        return
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_sample(n=49, steps=30, procs=1)  # before any GPU work in this process
+    res = run_gpu(args, rank, world)
+    # max over ranks
+    ms = res["ms"]
+    e2e_ms = res["e2e_ms"]
+    if world > 1:
+        import torch
+        t = torch.tensor([ms, e2e_ms], dtype=torch.float64)
+        _dist.all_reduce(t, op=_dist.ReduceOp.MAX)
+        ms, e2e_ms = float(t[0]), float(t[1])
+    if rank != 0:
+        return
+    n = res["n"]
+    value = world * n * args.steps / (ms / 1e3)
+    e2e_val = world * n * args.steps / (e2e_ms / 1e3)
+    kb = kernel_bytes(n, res["nent"], args.precision == "fp32")
+    kt = res["kt"]
+    dom = max((k for k in kt if k in kb), key=lambda k: kt[k][0])
+    avg_ms = kt[dom][0] / kt[dom][1]
+    peak, kind = peaks()
+    achieved = kb[dom] / (avg_ms / 1e3) / 1e9
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            traffic = json.load(f).get(f"{dom}:{args.precision}:{args.n}")
+    except Exception:
+        pass
+    launches = int(sum(v[1] for v in kt.values()))
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32" if args.precision == "fp32" else "f64", "data": "synthetic",
+            "config": config,
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                         "peak_kind": kind, "algorithmic_bytes_per_launch": kb[dom],
+                         "mean_launch_ms": avg_ms},
+            "kernels": {k: {"ms_total": v[0], "launches": v[1]} for k, v in kt.items()},
+            "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": n * 5 * 8,
+                    "d2h_bytes_per_step": n * 5 * 8},
+            "gpu_launches": launches,
+            "clocks": res["clocks"],
+            "cpu_baseline": cpu,
+            "setup_s": res["setup_s"], "device_bytes": res["dev_bytes"],
+            "dt_first_last": [float(res["dts"][0]), float(res["dts"][-1])]}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,172 @@
+/*
+ * xg.h -- C ABI of libxg, a single-GPU (sm_103a) implementation of the
+ * node-centred edge-based finite-element hot path of Xyst's Inciter:
+ *
+ *   - RieCG: superedge nodal gradients, MUSCL/Rusanov|HLLC edge and boundary
+ *     residual, low-storage 3-stage RK update, nodal BCs, CFL time step;
+ *   - KozCG: element Taylor-Galerkin residual with flux-corrected transport;
+ *   - ConjugateGradients: CSR matrix-vector product and preconditioned CG.
+ *
+ * Every entry point returns an int status (XG_OK on success) and never throws;
+ * xg_last_error() returns a message for the last failure on a context.  All
+ * arrays are plain host pointers with sizes, laid out exactly like the
+ * reference's containers:
+ *   - tk::Fields (node-major, src/Base/Data.hpp:419-426): U[i*ncomp + c];
+ *   - coordinates as three consecutive arrays x[npoin], y[npoin], z[npoin]
+ *     (std::array<std::vector<tk::real>,3> flattened);
+ *   - ids as uint64_t (std::size_t on LP64), zero based.
+ * One context owns one CUDA stream on one device; a context must be used from
+ * one host thread at a time.
+ */
+#ifndef XG_H
+#define XG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct xg_ctx xg_ctx;
+
+enum xg_status {
+  XG_OK = 0,
+  XG_ERR_ARG = 1,      /* invalid argument (sizes, ids out of range, ...) */
+  XG_ERR_CUDA = 2,     /* a CUDA runtime call failed */
+  XG_ERR_STATE = 3,    /* call out of order (e.g. no operators uploaded) */
+  XG_ERR_BLOWUP = 4,   /* dt below machine epsilon (RieCG::advance blowup) */
+  XG_ERR_NOTCONV = 5,  /* CG stopped without reaching the tolerance */
+  XG_ERR_DEVICE = 6    /* a kernel reported an error status */
+};
+
+enum xg_precision {
+  XG_FP64 = 0,       /* everything in double precision */
+  XG_FP32_FLUX = 1   /* FP32 gradients and fluxes, FP64 state and update */
+};
+
+enum xg_flux { XG_RUSANOV = 0, XG_HLLC = 1 };
+
+/* Physics and numerics settings the reference reads from its global config
+ * (mat.spec_heat_ratio, flux, stab2, stab2coef, cfl, dt). */
+typedef struct xg_riecg_params {
+  double gamma;      /* ratio of specific heats */
+  int flux;          /* enum xg_flux */
+  int stab2;         /* nonzero: artificial viscosity on the edge flux */
+  double stab2coef;  /* its coefficient */
+  double cfl;        /* CFL number (used when const_dt == 0) */
+  double const_dt;   /* constant time step if |const_dt| > eps */
+  int precision;     /* enum xg_precision */
+} xg_riecg_params;
+
+/* ---- context ------------------------------------------------------------ */
+int xg_create(int device, xg_ctx** ctx);
+int xg_destroy(xg_ctx* ctx);
+const char* xg_last_error(const xg_ctx* ctx);
+/* Bytes of device memory the context currently holds. */
+int xg_device_bytes(const xg_ctx* ctx, int64_t* bytes);
+
+/* ---- RieCG -------------------------------------------------------------- */
+
+/* Upload the finite-element operators RieCG builds once per mesh
+ * (RieCG::feop/streamable/domsuped, src/Inciter/RieCG.cpp:247-736): node
+ * coordinates and volumes, the three superedge groups exactly as
+ * RieCG::m_dsupedge/m_dsupint (tets: 4 ids + 6x3 integrals; triangles:
+ * 3 ids + 3x3; edges: 2 ids + 3), the boundary triangles m_triinpoel and
+ * their symmetry flags m_besym.  Counts are in groups.  Replaces the
+ * operator arguments of riemann::grad/rhs (src/Physics/Riemann.hpp:17-39).
+ * Re-upload after any mesh change. */
+int xg_riecg_setup(xg_ctx* ctx, const xg_riecg_params* prm, int64_t npoin,
+                   const double* coord, const double* vol,
+                   int64_t ntet, const uint64_t* dsupedge0, const double* dsupint0,
+                   int64_t ntri, const uint64_t* dsupedge1, const double* dsupint1,
+                   int64_t nedge, const uint64_t* dsupedge2, const double* dsupint2,
+                   int64_t nbtri, const uint64_t* triinpoel, const uint8_t* besym);
+
+/* Nodal boundary conditions as RieCG::setupBC/streamable store them
+ * (src/Inciter/RieCG.cpp:109-245, 527-618), applied by RieCG::BC
+ * (RieCG.cpp:764-785) in the order Dirichlet, symmetry, farfield, pressure:
+ *   sym:  m_symbcnodes / m_symbcnorms (a node may repeat, once per set);
+ *   far:  m_farbcnodes / m_farbcnorms and the farfield state far5 =
+ *         {density, u, v, w, pressure};
+ *   dir:  node ids, 5 mask ints per node (nonzero: component is set) and
+ *         5 values per node (time independent Dirichlet data);
+ *   pre:  m_prebcnodes / m_prebcvals (density, pressure per node).
+ * Any count may be zero. */
+int xg_riecg_set_bc(xg_ctx* ctx,
+                    int64_t nsym, const uint64_t* symnodes, const double* symnorms,
+                    int64_t nfar, const uint64_t* farnodes, const double* farnorms,
+                    const double* far5,
+                    int64_t ndir, const uint64_t* dirnodes, const int32_t* dirmask,
+                    const double* dirvals,
+                    int64_t npre, const uint64_t* prenodes, const double* prevals);
+
+/* Device-resident state U (npoin x 5, node-major), time t. */
+int xg_riecg_set_state(xg_ctx* ctx, const double* U, double t);
+int xg_riecg_get_state(xg_ctx* ctx, double* U, double* t);
+
+/* Drop-in for riemann::grad (src/Physics/Riemann.cpp:229-367): weak nodal
+ * gradients of primitive variables from host U (npoin x 5) into host G
+ * (npoin x 15), not divided by the nodal volume. */
+int xg_riecg_grad(xg_ctx* ctx, const double* U, double* G);
+
+/* Drop-in for riemann::rhs (src/Physics/Riemann.cpp:909-946): right-hand
+ * side R (npoin x 5) from host G (volume-divided, npoin x 15) and U. */
+int xg_riecg_rhs(xg_ctx* ctx, const double* G, const double* U, double* R);
+
+/* Apply the boundary conditions to the device state (RieCG::BC). */
+int xg_riecg_bc(xg_ctx* ctx);
+
+/* CFL time step of the device state (RieCG::dt, src/Inciter/RieCG.cpp:787-852). */
+int xg_riecg_dt(xg_ctx* ctx, double* dt);
+
+/* One RK stage on the device state with a given dt: grad, rhs, update
+ * U = Un - rkcoef[stage]*dt*R/V, BCs (RieCG::grad/rhs/solve,
+ * src/Inciter/RieCG.cpp:871-1057). */
+int xg_riecg_stage(xg_ctx* ctx, int stage, double dt);
+
+/* Advance nstep full time steps (CFL dt, 3 stages) on the device without
+ * host synchronisation.  dts (optional, host, nstep) receives each step's dt;
+ * ms (optional) the device time of the run measured with CUDA events on the
+ * context stream.  Returns XG_ERR_BLOWUP if a dt fell below eps. */
+int xg_riecg_run(xg_ctx* ctx, int64_t nstep, double* dts, float* ms);
+
+/* Per-kernel device time of the last xg_riecg_run with profiling enabled:
+ * enable != 0 brackets every launch with CUDA events (slightly slower).
+ * names/ms/launches receive up to cap entries; *n the number of kernels. */
+int xg_riecg_profile(xg_ctx* ctx, int enable);
+int xg_riecg_kernel_times(xg_ctx* ctx, int cap, const char** names, double* ms,
+                          int64_t* launches, int* n);
+
+/* ---- host operator setup (the caller side of xg_riecg_setup) ------------- */
+
+/* Locality renumbering of mesh nodes (reverse Cuthill-McKee over points
+ * surrounding points; plays the role of the constructor reordering in
+ * RieCG::RieCG, src/Inciter/RieCG.cpp:82-100).  new_of_old[npoin]. */
+int xg_mesh_rcm(int64_t npoin, int64_t nelem, const uint64_t* inpoel, uint64_t* new_of_old);
+
+/* Nodal volumes (Discretization::vol, src/Inciter/Discretization.cpp:619-660).
+ * Fails with XG_ERR_ARG on a non-positive element Jacobian. */
+int xg_mesh_vol(int64_t npoin, const double* coord, int64_t nelem, const uint64_t* inpoel,
+                double* vol);
+
+/* Domain edge integrals (RieCG::domint, src/Inciter/RieCG.cpp:339-382; with
+ * ncoef == 5 also ChoCG's two extra coefficients, src/Inciter/ChoCG.cpp:
+ * 398-445).  Each edge is oriented from the smaller to the larger gid (gid may
+ * be null: identity) and reported with local ids.  Call with cap = 0 to get
+ * *nedge, then again with arrays of that size (edges 2 per edge, dint ncoef
+ * per edge), sorted by (gid, gid). */
+int xg_mesh_edges(int64_t npoin, const double* coord, int64_t nelem, const uint64_t* inpoel,
+                  const uint64_t* gid, int ncoef, int64_t cap, int64_t* nedge,
+                  uint64_t* edges, double* dint);
+
+/* Inverse-distance weighted boundary point normals of one side set
+ * (RieCG::bndint + bnorm, src/Inciter/RieCG.cpp:281-337, 483-525) for the
+ * given nodes, which must lie on faces of the set. */
+int xg_mesh_bnorm(int64_t npoin, const double* coord, int64_t nface, const uint64_t* faces,
+                  int64_t nnode, const uint64_t* nodes, double* norms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* XG_H */

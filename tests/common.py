@@ -1,0 +1,100 @@
+"""Shared test inputs: reference golden fixtures and seeded cube problems."""
+
+from __future__ import annotations
+
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def golden(name):
+    return np.load(os.path.join(GOLDEN, name + ".npz"))
+
+
+def sod_mesh(scheme="RieCG"):
+    d = golden("riecg_sod" if scheme == "RieCG" else "kozcg_sod")
+    bface = {int(k[5:]): d[k] for k in d.files if k.startswith("bface")}
+    return {"coord": d["coord"], "inpoel": d["inpoel"], "bface": bface}, d
+
+
+def sod_ic(coord, gamma=1.4):
+    """Sod shock tube IC (problems::sod::ic, src/Physics/Problems.cpp:371-404)."""
+    x = coord[0]
+    r = np.where(x < 0.5, 1.0, 0.125)
+    p = np.where(x < 0.5, 1.0, 0.1)
+    U = np.zeros((coord.shape[1], 5))
+    U[:, 0] = r
+    U[:, 4] = p / (gamma - 1.0)
+    return U
+
+
+def wave_ic(coord, gamma=1.4):
+    """Smooth density wave rho = 1 + 0.2 sin(2 pi x) sin(2 pi y) sin(2 pi z),
+    u = (1, 0.5, 0.25), p = 1."""
+    x, y, z = coord
+    r = 1.0 + 0.2 * np.sin(2 * np.pi * x) * np.sin(2 * np.pi * y) * np.sin(2 * np.pi * z)
+    u = np.array([1.0, 0.5, 0.25])
+    U = np.zeros((coord.shape[1], 5))
+    U[:, 0] = r
+    U[:, 1:4] = r[:, None] * u[None, :]
+    U[:, 4] = 1.0 / (gamma - 1.0) + 0.5 * r * (u @ u)
+    return U
+
+
+def random_state(n, seed=0):
+    rng = np.random.default_rng(seed)
+    U = np.zeros((n, 5))
+    U[:, 0] = 1.0 + 0.2 * rng.random(n)
+    U[:, 1:4] = 0.2 * rng.standard_normal((n, 3))
+    U[:, 4] = 2.5 + 0.5 * rng.random(n) + 0.5 * (U[:, 1:4] ** 2).sum(1) / U[:, 0]
+    return U
+
+
+def laplacian_14(d):
+    """The positive Laplacian the reference unit tests assemble on their 14-node
+    mesh (tests/unit/LinearSolver/TestCSR.cpp:309-333): A += J/6 grad_a.grad_b
+    with grad = crossdiv(., J), on the psup sparsity; zero-based CSR."""
+    ip = d["inpoel_1based"] - 1
+    X, Y, Z = d["coord"]
+    n = X.size
+    rows = [set([i]) for i in range(n)]
+    for t in ip:
+        for a in t:
+            rows[a].update(t.tolist())
+    ia = np.zeros(n + 1, np.int64)
+    ja = []
+    for i in range(n):
+        c = sorted(rows[i])
+        ja += c
+        ia[i + 1] = ia[i] + len(c)
+    ja = np.array(ja, np.int64)
+    a = np.zeros(ja.size)
+    for N in ip:
+        ba = np.array([X[N[1]] - X[N[0]], Y[N[1]] - Y[N[0]], Z[N[1]] - Z[N[0]]])
+        ca = np.array([X[N[2]] - X[N[0]], Y[N[2]] - Y[N[0]], Z[N[2]] - Z[N[0]]])
+        da = np.array([X[N[3]] - X[N[0]], Y[N[3]] - Y[N[0]], Z[N[3]] - Z[N[0]]])
+        J = ba @ np.cross(ca, da)
+        g = np.zeros((4, 3))
+        g[1] = np.cross(ca, da) / J
+        g[2] = np.cross(da, ba) / J
+        g[3] = np.cross(ba, ca) / J
+        g[0] = -g[1] - g[2] - g[3]
+        for i in range(4):
+            for k in range(3):
+                for j in range(4):
+                    r = N[i]
+                    pos = ia[r] + np.searchsorted(ja[ia[r]:ia[r + 1]], N[j])
+                    a[pos] += J / 6 * g[i][k] * g[j][k]
+    return ia, ja, a
+
+
+def dirichlet_matrix_only(ia, ja, a, i):
+    """tk::CSR::dirichlet with value 0 in serial (src/LinearSolver/CSR.cpp:
+    106-152): zero column i and row i, 1 on the diagonal (b unchanged)."""
+    a = a.copy()
+    a[ja == i] = 0.0
+    for j in range(ia[i], ia[i + 1]):
+        a[j] = 1.0 if ja[j] == i else 0.0
+    return a

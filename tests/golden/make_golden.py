@@ -1,0 +1,119 @@
+"""Extract the reference's own golden vectors for the accelerated path into
+small committed fixtures (tests/golden/*.npz).
+
+Run in a checkout that has the reference sources (default /root/reference):
+
+    python tests/golden/make_golden.py [reference-root]
+
+Sources, all read as data (nothing is executed):
+  * tests/unit/LinearSolver/TestCSR.cpp: the 14-node tet mesh and the
+    expected Laplacian matrix-vector product (test 9);
+  * tests/unit/LinearSolver/TestConjugateGradients.cpp: its 14-node mesh and
+    the expected ||b|| and final residual of the 1-DOF and 3-DOF serial solves
+    (tests 1 and 3);
+  * tests/regression/inciter/RieCG/Sod: the input mesh, the final nodal
+    fields (sod.std.exo) and the per-step diagnostics (diag.std) of the RieCG
+    Sod shock tube (10 steps, CFL 0.5, symmetry on side sets 2,4,5,6);
+  * tests/regression/inciter/KozCG/Sod: the same for KozCG.
+"""
+
+from __future__ import annotations
+
+import os
+import re
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+
+def _block(text: str, start_pat: str) -> str:
+    i = text.index(start_pat)
+    j = text.index("};", i)
+    return text[i + len(start_pat):j]
+
+
+def _numbers(s: str, kind=float):
+    s = re.sub(r"//[^\n]*", "", s)
+    toks = re.findall(r"[-+]?\d+\.?\d*(?:[eE][-+]?\d+)?", s)
+    return np.array([kind(t) if kind is float else int(float(t)) for t in toks])
+
+
+def _mesh14(text: str, test_marker: str):
+    part = text[text.index(test_marker):] if test_marker else text
+    ip = _numbers(_block(part, "inpoel {"), int).reshape(-1, 4)
+    cb = _block(part, "coord {{")
+    rows = re.findall(r"\{\{([^{}]*)\}\}", cb)
+    coord = np.array([_numbers(r) for r in rows[:3]])
+    return ip, coord
+
+
+def csr_fixture(ref: str):
+    t = open(os.path.join(ref, "tests/unit/LinearSolver/TestCSR.cpp")).read()
+    ip, coord = _mesh14(t, "")
+    m = t[t.index("test_name( \"matrix-vector multiply\" )"):]
+    correct = _numbers(_block(m, "std::vector< tk::real > correct{"))
+    return {"inpoel_1based": ip, "coord": coord, "mult_correct": correct,
+            "prec": np.float64(np.finfo(np.float64).eps * 100)}
+
+
+def cg_fixture(ref: str):
+    t = open(os.path.join(ref, "tests/unit/LinearSolver/TestConjugateGradients.cpp")).read()
+    ip, coord = _mesh14(t, "Laplace eq 1DOF 1PE setup")
+
+    def expected(marker):
+        part = t[t.index(marker):]
+        blk = part[part.index("CProxy_CGReceiver::ckNew"):]
+        blk = blk[:blk.index(");")]
+        vals = {}
+        for key in ("maxit", "tol", "normb_ex", "normres_ex"):
+            mm = re.search(r"/\*\s*" + key + r"\s*=\s*\*?\s*\*/\s*([-+0-9.eE]+)", blk)
+            vals[key] = float(mm.group(1))
+        return vals
+
+    e1 = expected("Laplace eq 1DOF 1PE setup")
+    e3 = expected("Laplace eq 3DOF 1PE setup")
+    return {"inpoel_1based": ip, "coord": coord,
+            "dof1": np.array([e1["maxit"], e1["tol"], e1["normb_ex"], e1["normres_ex"]]),
+            "dof3": np.array([e3["maxit"], e3["tol"], e3["normb_ex"], e3["normres_ex"]])}
+
+
+def _diag(path):
+    rows = [ln.split() for ln in open(path) if ln.strip() and not ln.startswith("#")]
+    return np.array([[float(x) for x in r] for r in rows])
+
+
+def sod_fixture(ref: str, scheme: str):
+    from xyst_gb300 import mesh as M
+    from scipy.io import netcdf_file
+
+    base = os.path.join(ref, "tests/regression/inciter", scheme, "Sod")
+    m = M.read_exo(os.path.join(base, "rectangle_01_1.5k.exo"))
+    f = netcdf_file(os.path.join(base, "sod.std.exo"), "r", mmap=False)
+    names = ["".join(c.decode() for c in row if c) for row in f.variables["name_nod_var"][:]]
+    times = np.array(f.variables["time_whole"][:], dtype=np.float64)
+    fields = np.array([np.array(f.variables[f"vals_nod_var{i + 1}"][:][-1], dtype=np.float64)
+                       for i in range(len(names))])
+    ocoord = np.stack([np.asarray(f.variables[k][:], dtype=np.float64)
+                       for k in ("coordx", "coordy", "coordz")])
+    f.close()
+    out = {"coord": m["coord"], "inpoel": m["inpoel"], "final_time": times[-1],
+           "out_coord": ocoord, "out_fields": fields, "out_names": np.array(names),
+           "diag": _diag(os.path.join(base, "diag.std"))}
+    for s, tri in m["bface"].items():
+        out[f"bface{s}"] = tri
+    return out
+
+
+def main(ref: str):
+    np.savez_compressed(os.path.join(HERE, "csr_mult.npz"), **csr_fixture(ref))
+    np.savez_compressed(os.path.join(HERE, "cg_laplace.npz"), **cg_fixture(ref))
+    np.savez_compressed(os.path.join(HERE, "riecg_sod.npz"), **sod_fixture(ref, "RieCG"))
+    np.savez_compressed(os.path.join(HERE, "kozcg_sod.npz"), **sod_fixture(ref, "KozCG"))
+    print("wrote fixtures to", HERE)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -1,0 +1,183 @@
+"""Pins of the oracle restatement (CPU, no GPU):
+
+* against the reference's own compiled functions (oracle/_ref, built from the
+  unmodified reference sources where they are present): bit-for-bit;
+* against the reference's golden vectors committed in tests/golden/ (unit-test
+  known answers and the RieCG/KozCG Sod regression baselines) within the
+  reference's own test tolerances.
+"""
+
+import numpy as np
+import pytest
+
+import oracle
+import oracle.ref as ref
+from common import dirichlet_matrix_only, golden, laplacian_14, random_state, sod_ic, sod_mesh
+from xyst_gb300 import mesh
+
+needs_ref = pytest.mark.skipif(not ref.available(), reason="reference sources not built here")
+
+
+def _cube_ops(n=6, jitter=0.2, seed=1):
+    m = mesh.cube(n, jitter=jitter, seed=seed)
+    coord, inpoel = m["coord"], m["inpoel"]
+    v = oracle.vol(coord, inpoel)
+    e, d = oracle.domint(coord, inpoel)
+    tri = np.concatenate([m["bface"][s] for s in sorted(m["bface"])])
+    nodes, norms, symset = oracle.sym_bc(coord, m["bface"], [1, 2, 3, 4, 5, 6])
+    besym = np.isin(tri, list(symset)).astype(np.uint8)
+    return m, coord, inpoel, v, e, d, tri, besym, nodes, norms
+
+
+@needs_ref
+@pytest.mark.parametrize("flux,stab2", [("rusanov", False), ("rusanov", True), ("hllc", False),
+                                        ("hllc", True)])
+def test_riemann_grad_rhs_bitexact(flux, stab2):
+    m, coord, inpoel, v, e, d, tri, besym, *_ = _cube_ops()
+    U = random_state(coord.shape[1], 3)
+    ref.set_config(flux=flux, stab2=stab2)
+    o = oracle.RieCG(coord, v, e, d, tri, besym, flux=flux, stab2=stab2)
+    G = o.grad(U)
+    assert np.array_equal(G, ref.riemann_grad(coord, [None, None, (e, d)], tri, U))
+    Gv = G / v[:, None]
+    R = o.rhs(Gv, U)
+    assert np.array_equal(R, ref.riemann_rhs(coord, [None, None, (e, d)], tri, besym, Gv, U, v))
+
+
+@needs_ref
+def test_kozak_rhs_bitexact():
+    m, coord, inpoel, v, *_ = _cube_ops(5)
+    U = random_state(coord.shape[1], 4)
+    ref.set_config()
+    k = oracle.KozCG(coord, v, inpoel)
+    assert np.array_equal(k.rhs(U, 1.3e-3), ref.kozak_rhs(coord, inpoel, U, 0.0, 1.3e-3))
+
+
+@needs_ref
+def test_pressure_matrix_and_mult_bitexact():
+    m, coord, inpoel, *_ = _cube_ops(5)
+    ia, ja, a = oracle.pressure_matrix(coord, inpoel)
+    x = np.random.default_rng(0).standard_normal(coord.shape[1])
+    ria, rja, ra, ax, _ = ref.csr_pressure(coord, inpoel, x=x)
+    assert np.array_equal(ria - 1, ia) and np.array_equal(rja - 1, ja)
+    assert np.array_equal(ra, a)
+    assert np.array_equal(ax, oracle.csr_mult(ia, ja, a, x))
+
+
+@needs_ref
+def test_pressure_dirichlet_matches_reference():
+    m, coord, inpoel, *_ = _cube_ops(4)
+    ia, ja, a = oracle.pressure_matrix(coord, inpoel)
+    nodes = np.array([0, 5, 17, 40])
+    vals = np.array([0.5, -1.0, 2.0, 0.25])
+    b = np.zeros(coord.shape[1])
+    a2, b2 = oracle.csr_dirichlet(ia, ja, a, b, nodes, vals)
+    _, _, ra, _, bmod = ref.csr_pressure(coord, inpoel, nodes, vals)
+    assert np.array_equal(a2, ra)
+    expect = -bmod
+    expect[nodes] = vals
+    assert np.allclose(b2, expect, rtol=0, atol=0)
+
+
+@needs_ref
+def test_chorin_grad_reference_callable():
+    # the reference's chorin::grad on an edge list with 5 coefficients runs and
+    # gives a zero gradient for a constant field on a closed surface
+    m, coord, inpoel, *_ = _cube_ops(4, jitter=0.0)
+    e, d5 = oracle.domint(coord, inpoel, ncoef=5)
+    tri = np.concatenate([m["bface"][s] for s in sorted(m["bface"])])
+    G = ref.chorin_grad(coord, e, d5, tri, np.ones(coord.shape[1]))
+    assert np.abs(G).max() < 1e-14
+
+
+def test_csr_mult_golden():
+    d = golden("csr_mult")
+    ia, ja, a = laplacian_14(d)
+    x = np.arange(ia.size - 1, dtype=np.float64)
+    r = oracle.csr_mult(ia, ja, a, x)
+    assert np.allclose(r, d["mult_correct"], rtol=0, atol=float(d["prec"]))
+
+
+@pytest.mark.parametrize("case", ["dof1", "dof3"])
+def test_cg_laplace_golden(case):
+    d = golden("cg_laplace")
+    maxit, tol, normb_ex, normres_ex = d[case]
+    ia, ja, a = laplacian_14(d)
+    n = ia.size - 1
+    a = dirichlet_matrix_only(ia, ja, a, 0)
+    if case == "dof3":  # three decoupled copies, interleaved like tk::CSR(3, psup)
+        import scipy.sparse as sp
+        A = sp.kron(sp.csr_matrix((a, ja, ia), shape=(n, n)), sp.eye(3)).tocsr()
+        A.sort_indices()
+        ia, ja, a = A.indptr.astype(np.int64), A.indices.astype(np.int64), A.data
+        n *= 3
+    b = np.ones(n)
+    x, it, normr, normb, conv = oracle.pcg(ia, ja, a, b, np.zeros(n), int(maxit), tol, pc="none")
+    assert abs(normb - normb_ex) < 1e-12
+    assert abs(normr - normres_ex) < 1e-12
+    assert conv
+
+
+def _sod_oracle(scheme_sets=(2, 4, 5, 6)):
+    m, d = sod_mesh("RieCG")
+    coord, inpoel = m["coord"], m["inpoel"]
+    tri = np.concatenate([m["bface"][s] for s in sorted(m["bface"])])  # all side sets
+    v = oracle.vol(coord, inpoel)
+    e, de = oracle.domint(coord, inpoel)
+    nodes, norms, symset = oracle.sym_bc(coord, m["bface"], list(scheme_sets))
+    besym = np.isin(tri, list(symset)).astype(np.uint8)
+    o = oracle.RieCG(coord, v, e, de, tri, besym, cfl=0.5)
+    o.set_sym(nodes, norms)
+    o.set_state(sod_ic(coord))
+    o.bc()
+    return o, m, d, v
+
+
+def _by_coord(coord, out_coord):
+    from scipy.spatial import cKDTree
+    dist, idx = cKDTree(coord.T).query(out_coord.T)
+    assert dist.max() < 1e-12
+    return idx
+
+
+def _fields(U, gamma=1.4):
+    r = U[:, 0]
+    u, v, w = U[:, 1] / r, U[:, 2] / r, U[:, 3] / r
+    e = U[:, 4] / r
+    p = (gamma - 1.0) * r * (e - 0.5 * (u * u + v * v + w * w))
+    return np.stack([r, u, v, w, e, p])
+
+
+def test_riecg_sod_golden():
+    """10 RieCG steps of the reference's Sod regression: diagnostics within the
+    reference's numdiff tolerances (diag.ndiff.cfg: t, dt, L2 rel 1e-5 / abs
+    2e-4; residual norms rel 1e-7 / abs 3e-4) and final fields within its
+    exodiff tolerances (exodiff.cfg: relative 1e-7 floor 1e-8; velocities
+    absolute 1e-8 floor 1e-7)."""
+    o, m, d, v = _sod_oracle()
+    Vt = v.sum()
+    diag = d["diag"]
+    t = 0.0
+    for k in range(10):
+        Uo = o.state()
+        dt = o.run(1)[0]
+        t += dt
+        U = o.state()
+        l2 = np.sqrt((U ** 2 * v[:, None]).sum(0) / Vt)
+        l2r = np.sqrt(((U - Uo) ** 2 * v[:, None]).sum(0) / Vt)
+        row = np.concatenate([[t, dt], l2, l2r])
+        exp = diag[k, 1:13]
+        tol = np.where(np.arange(12) < 7, np.maximum(2e-4, 1e-5 * np.abs(exp)),
+                       np.maximum(3e-4, 1e-7 * np.abs(exp)))
+        assert np.all(np.abs(row - exp) <= tol), (k, row, exp)
+        assert abs(dt / diag[k, 2] - 1) < 1e-8
+    f = _fields(o.state())[:, _by_coord(m["coord"], d["out_coord"])]
+    ref_f = d["out_fields"]
+    for i in range(6):
+        if i in (1, 2, 3):
+            big = np.abs(ref_f[i]) > 1e-7
+            assert np.all(np.abs(f[i] - ref_f[i])[big] <= 1e-8)
+        else:
+            big = np.abs(ref_f[i]) > 1e-8
+            assert np.all(np.abs(f[i] - ref_f[i])[big] <= 1e-7 * np.abs(ref_f[i][big]))
+    assert abs(t - float(d["final_time"])) < 1e-8

@@ -1,0 +1,188 @@
+"""RieCG on the GPU against the oracle (and the reference's Sod baseline).
+
+Tolerances: the FP64 path must agree with the oracle to 1e-12 relative (the
+only differences are summation order); the FP32-flux path (FP32 gradients and
+fluxes, FP64 state and update) is held to the bound stated in each test."""
+
+import numpy as np
+import pytest
+
+from common import random_state, sod_ic, sod_mesh, wave_ic
+from gpu_util import cube_ops, ctx, pair, relerr
+from xyst_gb300 import riecg
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("flux,stab2", [("rusanov", False), ("hllc", True)])
+def test_dropin_grad_rhs_fp64(flux, stab2):
+    ops = cube_ops(8)
+    d, o = pair(ops, flux=flux, stab2=stab2)
+    U = random_state(ops["coord"].shape[1], 7)
+    G = d.grad(U)
+    Go = o.grad(U)
+    assert relerr(G, Go) < 1e-12
+    Gv = Go / ops["vol"][:, None]
+    R = d.rhs(Gv, U)
+    assert relerr(R, o.rhs(Gv, U)) < 1e-12
+
+
+def test_dropin_fp32_bound():
+    ops = cube_ops(8)
+    d, o = pair(ops, precision="fp32")
+    U = random_state(ops["coord"].shape[1], 8)
+    Go = o.grad(U)
+    assert relerr(d.grad(U), Go) < 2e-6
+    Gv = Go / ops["vol"][:, None]
+    assert relerr(d.rhs(Gv, U), o.rhs(Gv, U)) < 1e-4
+
+
+def test_superedge_groups_expand_like_reference():
+    """Tet and triangle superedge groups are evaluated edge by edge in the
+    reference's orientation; equal to the same edges passed as a plain list."""
+    ops = cube_ops(6)
+    inpoel = ops["inpoel"]
+    e = ops["edges"]
+    key = {(int(a), int(b)): k for k, (a, b) in enumerate(e)}
+    lpoed = [(0, 1), (1, 2), (2, 0), (0, 3), (1, 3), (2, 3)]
+    used = np.zeros(len(e), bool)
+    sup0, int0 = [], []
+    for t in inpoel:
+        ks, sg = [], []
+        for a, b in lpoed:
+            p, q = int(t[a]), int(t[b])
+            k = key.get((p, q), key.get((q, p)))
+            ks.append(k)
+            sg.append(1.0 if (p, q) in key else -1.0)
+        if not any(used[k] for k in ks):
+            for k in ks:
+                used[k] = True
+            sup0.append(t)
+            int0.append(np.concatenate([s * ops["dint"][k] for k, s in zip(ks, sg)]))
+    rest = ~used
+    d = riecg.RieCG(ctx(), ops["coord"], ops["vol"], [np.array(sup0), None, e[rest]],
+                    [np.array(int0), None, ops["dint"][rest]], ops["tri"], ops["besym"])
+    # the same edges, as a plain list with the group orientation
+    ee, dd = [], []
+    for t, it in zip(sup0, int0):
+        for k, (a, b) in enumerate(lpoed):
+            ee.append((t[a], t[b]))
+            dd.append(it[3 * k:3 * k + 3])
+    ee = np.concatenate([np.array(ee), e[rest]])
+    dd = np.concatenate([np.array(dd), ops["dint"][rest]])
+    import oracle
+    o = oracle.RieCG(ops["coord"], ops["vol"], ee, dd, ops["tri"], ops["besym"])
+    U = random_state(ops["coord"].shape[1], 9)
+    Go = o.grad(U)
+    assert relerr(d.grad(U), Go) < 1e-12
+    Gv = Go / ops["vol"][:, None]
+    assert relerr(d.rhs(Gv, U), o.rhs(Gv, U)) < 1e-12
+
+
+@pytest.mark.parametrize("flux", ["rusanov", "hllc"])
+def test_run_fp64_matches_oracle(flux):
+    ops = cube_ops(9)
+    d, o = pair(ops, flux=flux)
+    U0 = wave_ic(ops["coord"])
+    d.set_state(U0)
+    o.set_state(U0)
+    d.bc()
+    o.bc()
+    assert abs(d.dt() / o.dt() - 1) < 1e-14
+    dts, ms = d.run(12)
+    dto = o.run(12)
+    assert np.allclose(dts, dto, rtol=1e-12, atol=0)
+    U, t = d.state()
+    assert relerr(U, o.state()) < 1e-12
+    assert abs(t - dto.sum()) < 1e-15
+
+
+def test_single_stages_match_oracle():
+    ops = cube_ops(7)
+    d, o = pair(ops)
+    U0 = random_state(ops["coord"].shape[1], 2)
+    d.set_state(U0)
+    o.set_state(U0)
+    for st in range(3):
+        d.stage(st, 1.0e-4)
+        o.stage(st, 1.0e-4)
+        assert relerr(d.state()[0], o.state()) < 1e-12
+
+
+def test_run_fp32_bound():
+    """FP32 fluxes and gradients, FP64 state: fields within 1e-5 relative of the
+    FP64 oracle after 12 steps of the smooth wave."""
+    ops = cube_ops(9)
+    d, o = pair(ops, precision="fp32")
+    U0 = wave_ic(ops["coord"])
+    d.set_state(U0)
+    o.set_state(U0)
+    d.bc()
+    o.bc()
+    dts, _ = d.run(12)
+    dto = o.run(12)
+    assert np.allclose(dts, dto, rtol=1e-6)
+    assert relerr(d.state()[0], o.state()) < 1e-5
+
+
+def test_farfield_dirichlet_pressure_bcs():
+    ops = cube_ops(7, sym=(2, 5), far=(1,), dirs=(3,), pres=(6,))
+    d, o = pair(ops, far_state=(1.2, 0.3, 0.0, 0.0, 1.1),
+                dir_vals=lambda x: np.column_stack([np.ones(x.shape[1]), 0.1 * np.ones(x.shape[1]),
+                                                    np.zeros(x.shape[1]), np.zeros(x.shape[1]),
+                                                    2.6 * np.ones(x.shape[1])]),
+                pre_vals=(0.9, 0.95))
+    U0 = wave_ic(ops["coord"])
+    d.set_state(U0)
+    o.set_state(U0)
+    d.bc()
+    o.bc()
+    assert relerr(d.state()[0], o.state()) < 1e-14
+    dts, _ = d.run(6)
+    assert np.allclose(dts, o.run(6), rtol=1e-12)
+    assert relerr(d.state()[0], o.state()) < 1e-12
+
+
+def test_sod_reference_baseline_on_gpu():
+    """The reference's RieCG Sod regression run on the GPU: dt history and final
+    fields within the reference's exodiff/numdiff tolerances."""
+    from test_oracle_pins import _by_coord, _fields
+    m, dd = sod_mesh("RieCG")
+    ops = riecg.operators(m, sym_sets=[2, 4, 5, 6], renumber=True)
+    d, o = pair(ops)
+    U0 = sod_ic(ops["coord"])
+    d.set_state(U0)
+    d.bc()
+    dts, _ = d.run(10)
+    assert np.allclose(dts, dd["diag"][:, 2], rtol=1e-8, atol=0)
+    f = _fields(d.state()[0])[:, _by_coord(ops["coord"], dd["out_coord"])]
+    ref_f = dd["out_fields"]
+    for i in range(6):
+        if i in (1, 2, 3):
+            big = np.abs(ref_f[i]) > 1e-7
+            assert np.all(np.abs(f[i] - ref_f[i])[big] <= 1e-8)
+        else:
+            big = np.abs(ref_f[i]) > 1e-8
+            assert np.all(np.abs(f[i] - ref_f[i])[big] <= 1e-7 * np.abs(ref_f[i][big]))
+
+
+def test_profile_counts_launches():
+    ops = cube_ops(6)
+    d, _ = pair(ops)
+    d.set_state(wave_ic(ops["coord"]))
+    d.profile(True)
+    d.run(3)
+    kt = d.kernel_times()
+    assert kt["riecg_grad"][1] == 9 and kt["riecg_rhs_update"][1] == 9
+    assert kt["riecg_step_begin"][1] == 3
+    d.profile(False)
+
+
+def test_errors_are_status_codes():
+    ops = cube_ops(4)
+    d, _ = pair(ops)
+    with pytest.raises(RuntimeError):
+        d.stage(3, 1e-3)
+    with pytest.raises(RuntimeError):
+        riecg.RieCG(ctx(), ops["coord"], ops["vol"], [None, None, ops["edges"] + 10 ** 6],
+                    [None, None, ops["dint"]], ops["tri"], ops["besym"])

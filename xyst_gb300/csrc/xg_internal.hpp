@@ -1,0 +1,111 @@
+// Internal definitions shared by the libxg translation units: the context,
+// a device arena, error plumbing and the per-solver device state types.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/xg.h"
+
+namespace xg {
+
+// Bump allocator over one cudaMalloc block per solver: every device array of
+// a solver lives in one allocation, 256-byte aligned, released together.
+class Arena {
+ public:
+  Arena() = default;
+  Arena(const Arena&) = delete;
+  Arena& operator=(const Arena&) = delete;
+  ~Arena() { release(); }
+
+  // First pass: record sizes (ptr == nullptr); second pass after reserve().
+  template <class T>
+  void plan(T*& p, size_t count) {
+    size_t bytes = (count * sizeof(T) + 255) & ~size_t(255);
+    if (base_) {
+      p = reinterpret_cast<T*>(base_ + off_);
+      off_ += bytes;
+    } else {
+      p = nullptr;
+      need_ += bytes;
+    }
+  }
+  cudaError_t reserve() {
+    if (need_ == 0) need_ = 256;
+    cudaError_t e = cudaMalloc(&base_, need_);
+    off_ = 0;
+    return e;
+  }
+  void release() {
+    if (base_) cudaFree(base_);
+    base_ = nullptr;
+    need_ = off_ = 0;
+  }
+  size_t bytes() const { return need_; }
+  bool ready() const { return base_ != nullptr; }
+
+ private:
+  char* base_ = nullptr;
+  size_t need_ = 0;
+  size_t off_ = 0;
+};
+
+struct RieCGDev;  // xg_riecg.cu
+struct CGDev;     // xg_cg.cu
+struct KozCGDev;  // xg_kozcg.cu
+
+void destroy_riecg(RieCGDev*);
+void destroy_cg(CGDev*);
+void destroy_kozcg(KozCGDev*);
+size_t bytes_riecg(const RieCGDev*);
+size_t bytes_cg(const CGDev*);
+size_t bytes_kozcg(const KozCGDev*);
+
+}  // namespace xg
+
+struct xg_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  xg::RieCGDev* riecg = nullptr;
+  xg::CGDev* cg = nullptr;
+  xg::KozCGDev* kozcg = nullptr;
+};
+
+namespace xg {
+
+inline int fail(xg_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+#define XG_CUDA(ctx, call)                                                        \
+  do {                                                                            \
+    cudaError_t e_ = (call);                                                      \
+    if (e_ != cudaSuccess)                                                        \
+      return ::xg::fail((ctx), XG_ERR_CUDA,                                       \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));      \
+  } while (0)
+
+#define XG_CHECK_LAUNCH(ctx) XG_CUDA(ctx, cudaGetLastError())
+
+// Grid size for n items at b threads per block, as a multiple of what one
+// wave needs is left to the hardware scheduler: every node kernel is a flat
+// one-thread-per-item launch.
+inline unsigned blocks_for(int64_t n, int b) {
+  return static_cast<unsigned>((n + b - 1) / b);
+}
+
+// Make the context's device current for the calling thread.
+inline int use(xg_ctx* c) {
+  if (!c) return XG_ERR_ARG;
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e != cudaSuccess) return fail(c, XG_ERR_CUDA, cudaGetErrorString(e));
+  return XG_OK;
+}
+
+}  // namespace xg

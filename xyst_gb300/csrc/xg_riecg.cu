@@ -1,0 +1,1551 @@
+// RieCG on one GB300: superedge-equivalent node-gather gradient and residual
+// kernels, fused low-storage RK update, nodal BCs and CFL reduction.
+//
+// Reference path (all paths relative to the reference project root):
+//   riemann::grad   src/Physics/Riemann.cpp:229-367
+//   riemann::rhs    src/Physics/Riemann.cpp:909-946 (advdom :652-766 with
+//                   rusanov :369-478 / hllc :480-650 and muscl :34-143,
+//                   advbnd :768-878)
+//   RieCG::solve    src/Inciter/RieCG.cpp:992-1057 (rkcoef :41)
+//   RieCG::BC       src/Inciter/RieCG.cpp:764-785 -> src/Physics/BC.cpp
+//   RieCG::dt       src/Inciter/RieCG.cpp:787-852
+//
+// Data layout in HBM (n nodes):
+//   U, Un     double SoA [5][n]  conserved state and stage-0 copy
+//   W[0..1]   F [n][8]           (rho, u, v, w, e, x, y, z) records, ping-pong
+//   G         F [n][16]          15 volume-divided gradients + pad
+//   vol       double [n]
+//   adjacency SELL-32: slice s of 32 consecutive nodes holds width[s] entries
+//             per node at off[s] + k*32 + lane: nbr (int32, ~q when the node
+//             is the second end of the canonical edge, PAD for padding) and
+//             the canonical edge integral D (3 x F SoA).
+// Every edge flux is evaluated with the canonical orientation (left = first
+// end), so both ends compute bit-identical fluxes and the sum is the
+// reference's up to summation order.  Each node owns its writes: no atomics
+// except the scalar CFL minimum.
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "xg_internal.hpp"
+
+namespace xg {
+
+namespace {
+
+constexpr int kSlice = 32;
+constexpr int32_t kPad = INT32_MIN;
+constexpr int kBlock = 256;
+
+struct Scalars {
+  double dt;                  // current step size
+  unsigned long long dtmin;   // running minimum of the per-node CFL dt (bits)
+  int32_t blowup;             // set when a dt fell below eps
+  int32_t pad;
+};
+
+}  // namespace
+
+struct RieCGDev {
+  Arena arena;      // mesh-sized arrays
+  Arena bcarena;    // boundary condition program
+  Arena scratch;    // drop-in staging buffers
+  int64_t n = 0, nslice = 0, nent = 0, nbn = 0, nbt = 0, nbent = 0;
+  xg_riecg_params prm{};
+  bool fp32 = false;
+  // node arrays
+  double *U = nullptr, *Un = nullptr, *vol = nullptr;
+  int32_t* bidx = nullptr;  // per node: index into boundary lists or -1
+  void* W[2] = {nullptr, nullptr};
+  void* G = nullptr;
+  // adjacency
+  int32_t *soff = nullptr, *swidth = nullptr, *nbr = nullptr;
+  void *dx = nullptr, *dy = nullptr, *dz = nullptr;
+  // boundary triangles, per boundary node lists of (tri << 2 | position)
+  int32_t *bptr = nullptr, *bent = nullptr, *btri = nullptr;
+  uint8_t* bsym = nullptr;
+  uint8_t* bcflag = nullptr;  // per boundary node: has a nodal BC
+  // BC program: one thread per BC node
+  int64_t nbc = 0;
+  int32_t *bcnode = nullptr, *bcdir = nullptr, *bcsymp = nullptr, *bcfar = nullptr,
+          *bcpre = nullptr, *dirmask = nullptr;
+  double *symn = nullptr, *dirval = nullptr, *farn = nullptr, *preval = nullptr;
+  double far5[5] = {1, 0, 0, 0, 1};
+  // scalars and run bookkeeping
+  Scalars* scal = nullptr;
+  double* dthist = nullptr;
+  int64_t dthist_cap = 0;
+  int cur = 0;
+  double t = 0.0;
+  bool dt_valid = false;
+  // staging for the drop-in entry points
+  double* stage_buf = nullptr;
+  void* stage_W = nullptr;
+  void* stage_G = nullptr;
+  // profiling
+  bool prof = false;
+  struct KT {
+    const char* name;
+    double ms;
+    int64_t launches;
+  };
+  std::vector<KT> ktimes;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+};
+
+void destroy_riecg(RieCGDev* d) {
+  if (!d) return;
+  if (d->dthist) cudaFree(d->dthist);
+  for (auto& p : d->pending) {
+    cudaEventDestroy(p.second.first);
+    cudaEventDestroy(p.second.second);
+  }
+  delete d;
+}
+
+size_t bytes_riecg(const RieCGDev* d) {
+  return d ? d->arena.bytes() + d->bcarena.bytes() + d->scratch.bytes() : 0;
+}
+
+// ---------------------------------------------------------------------------
+// device code
+
+namespace {
+
+__device__ __forceinline__ void load8(const float* p, float o[8]) {
+  float4 a = __ldg(reinterpret_cast<const float4*>(p));
+  float4 b = __ldg(reinterpret_cast<const float4*>(p) + 1);
+  o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+  o[4] = b.x; o[5] = b.y; o[6] = b.z; o[7] = b.w;
+}
+__device__ __forceinline__ void load8(const double* p, double o[8]) {
+  const double2* q = reinterpret_cast<const double2*>(p);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    double2 a = __ldg(q + i);
+    o[2 * i] = a.x;
+    o[2 * i + 1] = a.y;
+  }
+}
+__device__ __forceinline__ void store8(float* p, const float o[8]) {
+  reinterpret_cast<float4*>(p)[0] = make_float4(o[0], o[1], o[2], o[3]);
+  reinterpret_cast<float4*>(p)[1] = make_float4(o[4], o[5], o[6], o[7]);
+}
+__device__ __forceinline__ void store8(double* p, const double o[8]) {
+  double2* q = reinterpret_cast<double2*>(p);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) q[i] = make_double2(o[2 * i], o[2 * i + 1]);
+}
+template <class F>
+__device__ __forceinline__ void load16(const F* p, F o[16]) {
+  load8(p, o);
+  load8(p + 8, o + 8);
+}
+template <class F>
+__device__ __forceinline__ void store16(F* p, const F o[16]) {
+  store8(p, o);
+  store8(p + 8, o + 8);
+}
+
+// Primitive variables from conserved ones (primitive(),
+// src/Physics/Riemann.cpp:211-227), evaluated in double.
+__device__ __forceinline__ void prim5(const double u[5], double w[5]) {
+  w[0] = u[0];
+  w[1] = u[1] / w[0];
+  w[2] = u[2] / w[0];
+  w[3] = u[3] / w[0];
+  w[4] = u[4] / w[0] - 0.5 * (w[1] * w[1] + w[2] * w[2] + w[3] * w[3]);
+}
+
+// Per-node CFL time step (src/Inciter/RieCG.cpp:827-838), before the CFL factor.
+__device__ __forceinline__ double node_dt(const double u[5], double vol, double g) {
+  double r = u[0];
+  double uu = u[1] / r, vv = u[2] / r, ww = u[3] / r;
+  double pr = (u[4] - 0.5 * r * (uu * uu + vv * vv + ww * ww)) * (g - 1.0);
+  double c = sqrt(g * fmax(pr, 0.0) / r);
+  double L = cbrt(vol);
+  double vel = sqrt(uu * uu + vv * vv + ww * ww);
+  return L / fmax(vel + c, 1.0e-8);
+}
+
+// Block-wide minimum of positive doubles folded into *dst with one atomic per
+// block.  Positive IEEE doubles order like their bit patterns.
+__device__ __forceinline__ void block_min_atomic(double v, unsigned long long* dst) {
+  __shared__ double red[32];
+  unsigned long long bits = __double_as_longlong(v);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long other = __shfl_xor_sync(0xffffffffu, bits, o);
+    bits = other < bits ? other : bits;
+  }
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) red[wid] = __longlong_as_double(bits);
+  __syncthreads();
+  if (wid == 0) {
+    int nw = (blockDim.x + 31) >> 5;
+    double x = lane < nw ? red[lane] : DBL_MAX;
+    unsigned long long b = __double_as_longlong(x);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      unsigned long long other = __shfl_xor_sync(0xffffffffu, b, o);
+      b = other < b ? other : b;
+    }
+    if (lane == 0) atomicMin(dst, b);
+  }
+}
+
+// MUSCL reconstruction of the five flow variables on edge L->R
+// (muscl(), src/Physics/Riemann.cpp:34-143).  The double instantiation keeps
+// the reference's operation order; the float one evaluates the same van Leer
+// limiter pair phi(a/b), phi(b/a) = 2|a|/(|a|+|b|), 2|b|/(|a|+|b|) (zero for
+// opposite signs) with one reciprocal instead of four divisions.
+template <class F>
+__device__ __forceinline__ void muscl(const F wl[8], const F wr[8], const F gl[16],
+                                      const F gr[16], F l[5], F r[5]) {
+  const F eps = F(1.0e-9);
+  const F k = F(1.0) / F(3.0);
+  F vw0 = wr[5] - wl[5], vw1 = wr[6] - wl[6], vw2 = wr[7] - wl[7];
+  F d1[5], d3[5];
+#pragma unroll
+  for (int c = 0; c < 5; ++c) {
+    F g1 = gl[c * 3 + 0] * vw0 + gl[c * 3 + 1] * vw1 + gl[c * 3 + 2] * vw2;
+    F g2 = gr[c * 3 + 0] * vw0 + gr[c * 3 + 1] * vw1 + gr[c * 3 + 2] * vw2;
+    F d2 = wr[c] - wl[c];
+    d1[c] = F(2.0) * g1 - d2;
+    d3[c] = F(2.0) * g2 - d2;
+    if constexpr (sizeof(F) == 8) {
+      F rcL = (d2 + eps) / (d1[c] + eps);
+      F rcR = (d2 + eps) / (d3[c] + eps);
+      F rLinv = (d1[c] + eps) / (d2 + eps);
+      F rRinv = (d3[c] + eps) / (d2 + eps);
+      F phiL = (fabs(rcL) + rcL) / (fabs(rcL) + F(1.0));
+      F phiR = (fabs(rcR) + rcR) / (fabs(rcR) + F(1.0));
+      F phiLi = (fabs(rLinv) + rLinv) / (fabs(rLinv) + F(1.0));
+      F phiRi = (fabs(rRinv) + rRinv) / (fabs(rRinv) + F(1.0));
+      l[c] = wl[c] + F(0.25) * (d1[c] * (F(1.0) - k) * phiL + d2 * (F(1.0) + k) * phiLi);
+      r[c] = wr[c] - F(0.25) * (d3[c] * (F(1.0) - k) * phiR + d2 * (F(1.0) + k) * phiRi);
+    } else {
+      float a = d2 + eps, b = d1[c] + eps, e3 = d3[c] + eps;
+      float aa = fabsf(a), ab = fabsf(b), ae = fabsf(e3);
+      float iL = (a * b > 0.f) ? __fdividef(0.5f, aa + ab) : 0.f;
+      float iR = (a * e3 > 0.f) ? __fdividef(0.5f, aa + ae) : 0.f;
+      l[c] = wl[c] + iL * (d1[c] * (1.f - k) * aa + d2 * (1.f + k) * ab);
+      r[c] = wr[c] - iR * (d3[c] * (1.f - k) * aa + d2 * (1.f + k) * ae);
+    }
+  }
+  if (wl[0] < d1[0] || wl[4] < d1[4]) {
+#pragma unroll
+    for (int c = 0; c < 5; ++c) l[c] = wl[c];
+  }
+  if (wr[0] < -d3[0] || wr[4] < -d3[4]) {
+#pragma unroll
+    for (int c = 0; c < 5; ++c) r[c] = wr[c];
+  }
+}
+
+template <class F>
+__device__ __forceinline__ F fsqrt(F x) {
+  return sqrt(x);
+}
+template <>
+__device__ __forceinline__ float fsqrt<float>(float x) {
+  return sqrtf(x);
+}
+template <class F>
+__device__ __forceinline__ F fdiv(F a, F b) {
+  return a / b;
+}
+template <>
+__device__ __forceinline__ float fdiv<float>(float a, float b) {
+  return __fdividef(a, b);
+}
+
+// Rusanov edge flux (rusanov(), src/Physics/Riemann.cpp:369-478).
+template <class F>
+__device__ __forceinline__ void rusanov(const F wl[8], const F wr[8], const F gl[16],
+                                        const F gr[16], F nx, F ny, F nz, F gamma,
+                                        bool stab2, F stab2coef, F f[5]) {
+  F l[5], r[5];
+  muscl(wl, wr, gl, gr, l, r);
+  F pL = l[0] * l[4] * (gamma - F(1.0));
+  F pR = r[0] * r[4] * (gamma - F(1.0));
+  F vnL = l[1] * nx + l[2] * ny + l[3] * nz;
+  F vnR = r[1] * nx + r[2] * ny + r[3] * nz;
+  l[4] = (l[4] + F(0.5) * (l[1] * l[1] + l[2] * l[2] + l[3] * l[3])) * l[0];
+  l[1] *= l[0];
+  l[2] *= l[0];
+  l[3] *= l[0];
+  r[4] = (r[4] + F(0.5) * (r[1] * r[1] + r[2] * r[2] + r[3] * r[3])) * r[0];
+  r[1] *= r[0];
+  r[2] *= r[0];
+  r[3] *= r[0];
+  F len = fsqrt(nx * nx + ny * ny + nz * nz);
+  F sl = fabs(vnL) + fsqrt(fdiv(gamma * pL, l[0])) * len;
+  F sr = fabs(vnR) + fsqrt(fdiv(gamma * pR, r[0])) * len;
+  F fw = sl > sr ? sl : sr;
+  f[0] = l[0] * vnL + r[0] * vnR + fw * (r[0] - l[0]);
+  f[1] = l[1] * vnL + r[1] * vnR + (pL + pR) * nx + fw * (r[1] - l[1]);
+  f[2] = l[2] * vnL + r[2] * vnR + (pL + pR) * ny + fw * (r[2] - l[2]);
+  f[3] = l[3] * vnL + r[3] * vnR + (pL + pR) * nz + fw * (r[3] - l[3]);
+  f[4] = (l[4] + pL) * vnL + (r[4] + pR) * vnR + fw * (r[4] - l[4]);
+  if (stab2) {
+    F fws = stab2coef * fw;
+#pragma unroll
+    for (int c = 0; c < 5; ++c) f[c] -= fws * (l[c] - r[c]);
+  }
+}
+
+// HLLC edge flux (hllc(), src/Physics/Riemann.cpp:480-650).
+template <class F>
+__device__ __forceinline__ void hllc(const F wl[8], const F wr[8], const F gl[16],
+                                     const F gr[16], F dx, F dy, F dz, F gamma, bool stab2,
+                                     F stab2coef, F f[5]) {
+  F l[5], r[5];
+  muscl(wl, wr, gl, gr, l, r);
+  F nx = -dx, ny = -dy, nz = -dz;
+  F len = fsqrt(nx * nx + ny * ny + nz * nz);
+  nx /= len;
+  ny /= len;
+  nz /= len;
+  F qL = l[1] * nx + l[2] * ny + l[3] * nz;
+  F qR = r[1] * nx + r[2] * ny + r[3] * nz;
+  F pL = l[0] * l[4] * (gamma - F(1.0));
+  F pR = r[0] * r[4] * (gamma - F(1.0));
+  l[4] = (l[4] + F(0.5) * (l[1] * l[1] + l[2] * l[2] + l[3] * l[3])) * l[0];
+  l[1] *= l[0];
+  l[2] *= l[0];
+  l[3] *= l[0];
+  r[4] = (r[4] + F(0.5) * (r[1] * r[1] + r[2] * r[2] + r[3] * r[3])) * r[0];
+  r[1] *= r[0];
+  r[2] *= r[0];
+  r[3] *= r[0];
+  F cL = fsqrt(gamma * pL / l[0]);
+  F cR = fsqrt(gamma * pR / r[0]);
+  F sL = fmin(qL - cL, qR - cR);
+  F sR = fmax(qL + cL, qR + cR);
+  F tL = sL - qL;
+  F tR = sR - qR;
+  F sM = (r[0] * qR * tR - l[0] * qL * tL + pL - pR) / (r[0] * tR - l[0] * tL);
+  F pS = pL - l[0] * tL * (qL - sM);
+  F L2 = F(-2.0) * len;
+  if (sL > F(0.0)) {
+    F qL2 = qL * L2;
+    f[0] = l[0] * qL2;
+    f[1] = l[1] * qL2 + pL * (nx * L2);
+    f[2] = l[2] * qL2 + pL * (ny * L2);
+    f[3] = l[3] * qL2 + pL * (nz * L2);
+    f[4] = (l[4] + pL) * qL2;
+  } else if (sL <= F(0.0) && sM > F(0.0)) {
+    F s = sL - sM;
+    F uL0 = tL * l[0] / s;
+    F uL1 = (tL * l[1] + (pS - pL) * nx) / s;
+    F uL2 = (tL * l[2] + (pS - pL) * ny) / s;
+    F uL3 = (tL * l[3] + (pS - pL) * nz) / s;
+    F uL4 = (tL * l[4] - pL * qL + pS * sM) / s;
+    F qL2 = qL * L2, sL2 = sL * L2;
+    f[0] = l[0] * qL2 + sL2 * (uL0 - l[0]);
+    f[1] = l[1] * qL2 + pL * (nx * L2) + sL2 * (uL1 - l[1]);
+    f[2] = l[2] * qL2 + pL * (ny * L2) + sL2 * (uL2 - l[2]);
+    f[3] = l[3] * qL2 + pL * (nz * L2) + sL2 * (uL3 - l[3]);
+    f[4] = (l[4] + pL) * qL2 + sL2 * (uL4 - l[4]);
+  } else if (sM <= F(0.0) && sR >= F(0.0)) {
+    F s = sR - sM;
+    F uR0 = tR * r[0] / s;
+    F uR1 = (tR * r[1] + (pS - pR) * nx) / s;
+    F uR2 = (tR * r[2] + (pS - pR) * ny) / s;
+    F uR3 = (tR * r[3] + (pS - pR) * nz) / s;
+    F uR4 = (tR * r[4] - pR * qR + pS * sM) / s;
+    F qR2 = qR * L2, sR2 = sR * L2;
+    f[0] = r[0] * qR2 + sR2 * (uR0 - r[0]);
+    f[1] = r[1] * qR2 + pR * (nx * L2) + sR2 * (uR1 - r[1]);
+    f[2] = r[2] * qR2 + pR * (ny * L2) + sR2 * (uR2 - r[2]);
+    f[3] = r[3] * qR2 + pR * (nz * L2) + sR2 * (uR3 - r[3]);
+    f[4] = (r[4] + pR) * qR2 + sR2 * (uR4 - r[4]);
+  } else {
+    F qR2 = qR * L2;
+    f[0] = r[0] * qR2;
+    f[1] = r[1] * qR2 + pR * (nx * L2);
+    f[2] = r[2] * qR2 + pR * (ny * L2);
+    f[3] = r[3] * qR2 + pR * (nz * L2);
+    f[4] = (r[4] + pR) * qR2;
+  }
+  if (stab2) {
+    F sl = fabs(qL) + cL;
+    F sr = fabs(qR) + cR;
+    F fws = stab2coef * (sl > sr ? sl : sr) * len;
+#pragma unroll
+    for (int c = 0; c < 5; ++c) f[c] -= fws * (l[c] - r[c]);
+  }
+}
+
+// Node-major (host layout) -> SoA.
+__global__ void k_aos_to_soa(int64_t n, int nc, const double* __restrict__ a,
+                             double* __restrict__ s) {
+  int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= n * nc) return;
+  int64_t p = i / nc;
+  int c = static_cast<int>(i - p * nc);
+  s[c * n + p] = a[i];
+}
+__global__ void k_soa_to_aos(int64_t n, int nc, const double* __restrict__ s,
+                             double* __restrict__ a) {
+  int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= n * nc) return;
+  int64_t p = i / nc;
+  int c = static_cast<int>(i - p * nc);
+  a[i] = s[c * n + p];
+}
+
+// W records from node-major host-layout U (drop-in entry points).
+template <class F>
+__global__ void k_prim_aos(int64_t n, const double* __restrict__ Ua, const F* __restrict__ Wsrc,
+                           F* __restrict__ W) {
+  int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (p >= n) return;
+  double u[5], w[5];
+#pragma unroll
+  for (int c = 0; c < 5; ++c) u[c] = Ua[p * 5 + c];
+  prim5(u, w);
+  F o[8];
+  load8(Wsrc + p * 8, o);
+#pragma unroll
+  for (int c = 0; c < 5; ++c) o[c] = F(w[c]);
+  store8(W + p * 8, o);
+}
+
+// G records <-> node-major 15-wide doubles.
+template <class F>
+__global__ void k_grec_to_aos(int64_t n, const F* __restrict__ G, double* __restrict__ a) {
+  int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= n * 15) return;
+  int64_t p = i / 15;
+  int c = static_cast<int>(i - p * 15);
+  a[i] = double(G[p * 16 + c]);
+}
+template <class F>
+__global__ void k_aos_to_grec(int64_t n, const double* __restrict__ a, F* __restrict__ G) {
+  int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= n * 16) return;
+  int64_t p = i / 16;
+  int c = static_cast<int>(i - p * 16);
+  G[i] = c < 15 ? F(a[p * 15 + c]) : F(0);
+}
+
+struct Adj {
+  const int32_t* soff;
+  const int32_t* swidth;
+  const int32_t* nbr;
+};
+struct Bnd {
+  const int32_t* bidx;
+  const int32_t* bptr;
+  const int32_t* bent;
+  const int32_t* btri;
+  const uint8_t* bsym;
+};
+
+// Nodal gradients of primitive variables (riemann::grad,
+// src/Physics/Riemann.cpp:229-367): sum over the node's edges of
+// -/+ D (u_p + u_q) plus the boundary-triangle term, optionally divided by the
+// nodal volume (RieCG::rhs, src/Inciter/RieCG.cpp:936-939).
+template <class F>
+__global__ void __launch_bounds__(kBlock) k_grad(int64_t n, Adj adj, const F* __restrict__ dx,
+                                                  const F* __restrict__ dy,
+                                                  const F* __restrict__ dz,
+                                                  const F* __restrict__ W, Bnd bnd,
+                                                  const double* __restrict__ vol, int divide,
+                                                  F* __restrict__ G) {
+  int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (p >= n) return;
+  const int lane = static_cast<int>(p & (kSlice - 1));
+  const int64_t s = p >> 5;
+  const int32_t off = __ldg(adj.soff + s), w = __ldg(adj.swidth + s);
+  F wp[8];
+  load8(W + p * 8, wp);
+  F g[15];
+#pragma unroll
+  for (int i = 0; i < 15; ++i) g[i] = F(0);
+  for (int k = 0; k < w; ++k) {
+    const int32_t e = off + k * kSlice + lane;
+    int32_t q = __ldg(adj.nbr + e);
+    if (q == kPad) continue;
+    F d0 = __ldg(dx + e), d1 = __ldg(dy + e), d2 = __ldg(dz + e);
+    if (q >= 0) {  // this node is the first end: G -= f
+      d0 = -d0;
+      d1 = -d1;
+      d2 = -d2;
+    } else {
+      q = ~q;
+    }
+    F wq[8];
+    load8(W + int64_t(q) * 8, wq);
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      F sum = wq[c] + wp[c];
+      g[c * 3 + 0] += d0 * sum;
+      g[c * 3 + 1] += d1 * sum;
+      g[c * 3 + 2] += d2 * sum;
+    }
+  }
+  const int32_t bi = __ldg(bnd.bidx + p);
+  if (bi >= 0) {
+    for (int32_t j = __ldg(bnd.bptr + bi); j < __ldg(bnd.bptr + bi + 1); ++j) {
+      const int32_t t = __ldg(bnd.bent + j) >> 2;
+      const int32_t N0 = __ldg(bnd.btri + 3 * t), N1 = __ldg(bnd.btri + 3 * t + 1),
+                    N2 = __ldg(bnd.btri + 3 * t + 2);
+      F a[8], b[8], c[8];
+      load8(W + int64_t(N0) * 8, a);
+      load8(W + int64_t(N1) * 8, b);
+      load8(W + int64_t(N2) * 8, c);
+      F bax = b[5] - a[5], bay = b[6] - a[6], baz = b[7] - a[7];
+      F cax = c[5] - a[5], cay = c[6] - a[6], caz = c[7] - a[7];
+      F nn[3] = {(bay * caz - cay * baz) / F(12.0), (baz * cax - caz * bax) / F(12.0),
+                 (bax * cay - cax * bay) / F(12.0)};
+#pragma unroll
+      for (int cc = 0; cc < 5; ++cc) {
+        F uab = (a[cc] + b[cc]) / F(4.0);
+        F ubc = (b[cc] + c[cc]) / F(4.0);
+        F uca = (c[cc] + a[cc]) / F(4.0);
+        F gg[3] = {uab + uca + a[cc], uab + ubc + b[cc], ubc + uca + c[cc]};
+#pragma unroll
+        for (int j2 = 0; j2 < 3; ++j2) g[cc * 3 + j2] += gg[j2] * nn[j2];
+      }
+    }
+  }
+  F o[16];
+  if (divide) {
+    const F v = F(vol[p]);
+#pragma unroll
+    for (int i = 0; i < 15; ++i) o[i] = g[i] / v;
+  } else {
+#pragma unroll
+    for (int i = 0; i < 15; ++i) o[i] = g[i];
+  }
+  o[15] = F(0);
+  store16(G + p * 16, o);
+}
+
+// Residual plus (optionally) the RK update of one stage:
+// riemann::rhs (advdom + advbnd) and RieCG::solve
+// (src/Inciter/RieCG.cpp:1010-1021): U = Un - rkcoef*dt*R/vol, then the new
+// primitive records and, on the last stage, the CFL minimum for the next
+// step (src/Inciter/RieCG.cpp:827-839) for nodes without a nodal BC (the BC
+// kernel covers those after it has modified them).
+template <class F, int FLUX, int STAGE, bool UPDATE>
+__global__ void __launch_bounds__(kBlock) k_rhs(int64_t n, Adj adj, const F* __restrict__ dx,
+                                                 const F* __restrict__ dy,
+                                                 const F* __restrict__ dz,
+                                                 const F* __restrict__ W,
+                                                 const F* __restrict__ G, Bnd bnd,
+                                                 const uint8_t* __restrict__ bcflag,
+                                                 const double* __restrict__ vol, double gamma_d,
+                                                 int stab2, double stab2coef_d,
+                                                 const Scalars* __restrict__ scal, double* U,
+                                                 double* Un, F* __restrict__ Wout,
+                                                 double* __restrict__ Rout,
+                                                 unsigned long long* dtmin) {
+  int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  const bool active = p < n;
+  const F gamma = F(gamma_d), stab2coef = F(stab2coef_d);
+  double dtp = DBL_MAX;
+  if (active) {
+    const int lane = static_cast<int>(p & (kSlice - 1));
+    const int64_t s = p >> 5;
+    const int32_t off = __ldg(adj.soff + s), w = __ldg(adj.swidth + s);
+    F wp[8], gp[16];
+    load8(W + p * 8, wp);
+    load16(G + p * 16, gp);
+    F R[5] = {F(0), F(0), F(0), F(0), F(0)};
+    for (int k = 0; k < w; ++k) {
+      const int32_t e = off + k * kSlice + lane;
+      int32_t q = __ldg(adj.nbr + e);
+      if (q == kPad) continue;
+      const bool first = q >= 0;
+      if (!first) q = ~q;
+      const F d0 = __ldg(dx + e), d1 = __ldg(dy + e), d2 = __ldg(dz + e);
+      F wq[8], gq[16];
+      load8(W + int64_t(q) * 8, wq);
+      load16(G + int64_t(q) * 16, gq);
+      F wl[8], wr[8], gl[16], gr[16];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        wl[i] = first ? wp[i] : wq[i];
+        wr[i] = first ? wq[i] : wp[i];
+      }
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        gl[i] = first ? gp[i] : gq[i];
+        gr[i] = first ? gq[i] : gp[i];
+      }
+      F f[5];
+      if (FLUX == XG_HLLC)
+        hllc(wl, wr, gl, gr, d0, d1, d2, gamma, stab2 != 0, stab2coef, f);
+      else
+        rusanov(wl, wr, gl, gr, d0, d1, d2, gamma, stab2 != 0, stab2coef, f);
+      if (first) {
+#pragma unroll
+        for (int c = 0; c < 5; ++c) R[c] -= f[c];
+      } else {
+#pragma unroll
+        for (int c = 0; c < 5; ++c) R[c] += f[c];
+      }
+    }
+    // boundary integral (advbnd, src/Physics/Riemann.cpp:768-878)
+    const int32_t bi = __ldg(bnd.bidx + p);
+    if (bi >= 0) {
+      for (int32_t j = __ldg(bnd.bptr + bi); j < __ldg(bnd.bptr + bi + 1); ++j) {
+        const int32_t ent = __ldg(bnd.bent + j);
+        const int32_t t = ent >> 2, pos = ent & 3;
+        F x[3][8];
+        uint8_t sy[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          load8(W + int64_t(__ldg(bnd.btri + 3 * t + a)) * 8, x[a]);
+          sy[a] = __ldg(bnd.bsym + 3 * t + a);
+        }
+        F bax = x[1][5] - x[0][5], bay = x[1][6] - x[0][6], baz = x[1][7] - x[0][7];
+        F cax = x[2][5] - x[0][5], cay = x[2][6] - x[0][6], caz = x[2][7] - x[0][7];
+        F nx = (bay * caz - cay * baz) / F(12.0);
+        F ny = (baz * cax - caz * bax) / F(12.0);
+        F nz = (bax * cay - cax * bay) / F(12.0);
+        F fl[3][5];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          const F r = x[a][0], u = x[a][1], v = x[a][2], ww = x[a][3], ie = x[a][4];
+          const F pr = r * ie * (gamma - F(1.0));
+          const F vn = sy[a] ? F(0) : (nx * u + ny * v + nz * ww);
+          const F re = r * (ie + F(0.5) * (u * u + v * v + ww * ww));
+          fl[a][0] = r * vn;
+          fl[a][1] = r * u * vn + pr * nx;
+          fl[a][2] = r * v * vn + pr * ny;
+          fl[a][3] = r * ww * vn + pr * nz;
+          fl[a][4] = (re + pr) * vn;
+        }
+#pragma unroll
+        for (int c = 0; c < 5; ++c) {
+          // own value, plus the two averages of the pairs containing this node
+          F fa = fl[0][c], fb = fl[1][c], fcc = fl[2][c];
+          F fab = (fa + fb) / F(4.0), fbc = (fb + fcc) / F(4.0), fca = (fcc + fa) / F(4.0);
+          R[c] += pos == 0 ? (fab + fca + fa) : (pos == 1 ? (fab + fbc + fb) : (fbc + fca + fcc));
+        }
+      }
+    }
+    if (!UPDATE) {
+#pragma unroll
+      for (int c = 0; c < 5; ++c) Rout[p * 5 + c] = double(R[c]);
+    } else {
+      constexpr double rk = STAGE == 0 ? 1.0 / 3.0 : (STAGE == 1 ? 0.5 : 1.0);
+      const double dt = scal->dt;
+      const double v = vol[p];
+      double un[5];
+#pragma unroll
+      for (int c = 0; c < 5; ++c) {
+        double uo;
+        if (STAGE == 0) {
+          uo = U[c * n + p];
+          Un[c * n + p] = uo;
+        } else {
+          uo = Un[c * n + p];
+        }
+        un[c] = uo - rk * dt * double(R[c]) / v;
+        U[c * n + p] = un[c];
+      }
+      double pw[5];
+      prim5(un, pw);
+      F o[8] = {F(pw[0]), F(pw[1]), F(pw[2]), F(pw[3]), F(pw[4]), wp[5], wp[6], wp[7]};
+      store8(Wout + p * 8, o);
+      if (STAGE == 2) {
+        const bool hasbc = bi >= 0 && bcflag[bi];
+        if (!hasbc) dtp = node_dt(un, v, gamma_d);
+      }
+    }
+  }
+  if (UPDATE && STAGE == 2) block_min_atomic(dtp, dtmin);
+}
+
+// Nodal BCs, one thread per BC node, in the reference order: Dirichlet,
+// symmetry (one projection per symmetry set containing the node), farfield,
+// pressure (physics::dirbc/symbc/farbc/prebc, src/Physics/BC.cpp:29-241).
+// Refreshes the node's primitive record and, when asked, its CFL dt.
+struct BCProg {
+  int64_t nbc;
+  const int32_t* node;
+  const int32_t* dir;
+  const int32_t* symp;
+  const int32_t* far;
+  const int32_t* pre;
+  const int32_t* dirmask;
+  const double* dirval;
+  const double* symn;
+  const double* farn;
+  const double* preval;
+  double far5[5];
+};
+
+template <class F>
+__global__ void __launch_bounds__(kBlock) k_bc(int64_t n, BCProg bc, double gamma, double* U,
+                                                F* __restrict__ W, const double* __restrict__ vol,
+                                                int want_dt, unsigned long long* dtmin) {
+  int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  double dtp = DBL_MAX;
+  if (i < bc.nbc) {
+    const int64_t p = bc.node[i];
+    double u[5];
+#pragma unroll
+    for (int c = 0; c < 5; ++c) u[c] = U[c * n + p];
+    const int32_t d = bc.dir[i];
+    if (d >= 0) {
+#pragma unroll
+      for (int c = 0; c < 5; ++c)
+        if (bc.dirmask[d * 5 + c]) u[c] = bc.dirval[d * 5 + c];
+    }
+    for (int32_t k = bc.symp[i]; k < bc.symp[i + 1]; ++k) {
+      const double* nn = bc.symn + 3 * k;
+      double vn = u[1] * nn[0] + u[2] * nn[1] + u[3] * nn[2];
+      u[1] -= vn * nn[0];
+      u[2] -= vn * nn[1];
+      u[3] -= vn * nn[2];
+    }
+    const int32_t f = bc.far[i];
+    if (f >= 0) {
+      const double* nn = bc.farn + 3 * f;
+      const double fr = bc.far5[0], fu = bc.far5[1], fv = bc.far5[2], fw = bc.far5[3],
+                   fp = bc.far5[4];
+      double vn = fu * nn[0] + fv * nn[1] + fw * nn[2];
+      double a = sqrt(gamma * fp / fr);
+      double M = vn / a;
+      if (M <= -1.0) {
+        u[0] = fr;
+        u[1] = fr * fu;
+        u[2] = fr * fv;
+        u[3] = fr * fw;
+        u[4] = fp / (gamma - 1.0) + 0.5 * fr * (fu * fu + fv * fv + fw * fw);
+      } else if (M > -1.0 && M < 0.0) {
+        double pr = (u[4] - 0.5 * (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) / u[0]) *
+                    (gamma - 1.0);
+        u[0] = fr;
+        u[1] = fr * fu;
+        u[2] = fr * fv;
+        u[3] = fr * fw;
+        u[4] = pr / (gamma - 1.0) + 0.5 * fr * (fu * fu + fv * fv + fw * fw);
+      } else if (M >= 0.0 && M < 1.0) {
+        double r = u[0], uu = u[1] / r, vv = u[2] / r, ww = u[3] / r;
+        u[4] = fp / (gamma - 1.0) + 0.5 * r * (uu * uu + vv * vv + ww * ww);
+      }
+    }
+    const int32_t pr = bc.pre[i];
+    if (pr >= 0) {
+      u[0] = bc.preval[pr * 2 + 0];
+      double r = u[0], uu = u[1] / r, vv = u[2] / r, ww = u[3] / r;
+      u[4] = bc.preval[pr * 2 + 1] / (gamma - 1.0) + 0.5 * r * (uu * uu + vv * vv + ww * ww);
+    }
+#pragma unroll
+    for (int c = 0; c < 5; ++c) U[c * n + p] = u[c];
+    double w[5];
+    prim5(u, w);
+    F o[8];
+    load8(W + p * 8, o);
+#pragma unroll
+    for (int c = 0; c < 5; ++c) o[c] = F(w[c]);
+    store8(W + p * 8, o);
+    if (want_dt) dtp = node_dt(u, vol[p], gamma);
+  }
+  if (want_dt) block_min_atomic(dtp, dtmin);
+}
+
+// CFL minimum over all nodes of the current state.
+__global__ void __launch_bounds__(kBlock) k_dt(int64_t n, const double* __restrict__ U,
+                                                const double* __restrict__ vol, double gamma,
+                                                unsigned long long* dtmin) {
+  int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  double dtp = DBL_MAX;
+  if (p < n) {
+    double u[5];
+#pragma unroll
+    for (int c = 0; c < 5; ++c) u[c] = U[c * n + p];
+    dtp = node_dt(u, vol[p], gamma);
+  }
+  block_min_atomic(dtp, dtmin);
+}
+
+// Step prologue (RieCG::dt reduction target + RieCG::advance,
+// src/Inciter/RieCG.cpp:839-869): dt = cfl * min, blowup when dt < eps; then
+// reset the running minimum for the next step.
+__global__ void k_step_begin(Scalars* s, double cfl, double const_dt, double* hist, int64_t k) {
+  double dt;
+  if (fabs(const_dt) > DBL_EPSILON)
+    dt = const_dt;
+  else
+    dt = __longlong_as_double(s->dtmin) * cfl;
+  if (dt < DBL_EPSILON) s->blowup = 1;
+  s->dt = dt;
+  s->dtmin = __double_as_longlong(DBL_MAX);
+  if (hist) hist[k] = dt;
+}
+
+__global__ void k_set_dt(Scalars* s, double dt) { s->dt = dt; }
+__global__ void k_reset_min(Scalars* s) { s->dtmin = __double_as_longlong(DBL_MAX); }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host side
+
+namespace {
+
+struct Edge {
+  int64_t a, b;
+  double d[3];
+};
+
+int launch_done(xg_ctx* c, RieCGDev* d, int slot, cudaEvent_t e0) {
+  if (!d->prof) return XG_OK;
+  cudaEvent_t e1;
+  XG_CUDA(c, cudaEventCreate(&e1));
+  XG_CUDA(c, cudaEventRecord(e1, c->stream));
+  d->pending.push_back({slot, {e0, e1}});
+  return XG_OK;
+}
+
+int launch_begin(xg_ctx* c, RieCGDev* d, const char* name, int* slot, cudaEvent_t* e0) {
+  if (!d->prof) return XG_OK;
+  int k = -1;
+  for (size_t i = 0; i < d->ktimes.size(); ++i)
+    if (std::strcmp(d->ktimes[i].name, name) == 0) k = static_cast<int>(i);
+  if (k < 0) {
+    d->ktimes.push_back({name, 0.0, 0});
+    k = static_cast<int>(d->ktimes.size() - 1);
+  }
+  *slot = k;
+  XG_CUDA(c, cudaEventCreate(e0));
+  XG_CUDA(c, cudaEventRecord(*e0, c->stream));
+  return XG_OK;
+}
+
+int flush_profile(xg_ctx* c, RieCGDev* d) {
+  if (d->pending.empty()) return XG_OK;
+  XG_CUDA(c, cudaStreamSynchronize(c->stream));
+  for (auto& p : d->pending) {
+    float ms = 0.f;
+    XG_CUDA(c, cudaEventElapsedTime(&ms, p.second.first, p.second.second));
+    d->ktimes[p.first].ms += ms;
+    d->ktimes[p.first].launches += 1;
+    cudaEventDestroy(p.second.first);
+    cudaEventDestroy(p.second.second);
+  }
+  d->pending.clear();
+  return XG_OK;
+}
+
+#define XG_PROF_LAUNCH(ctx, dev, name, launch)                   \
+  do {                                                           \
+    int slot_ = 0;                                               \
+    cudaEvent_t e0_ = nullptr;                                   \
+    int rc_ = launch_begin(ctx, dev, name, &slot_, &e0_);        \
+    if (rc_) return rc_;                                         \
+    launch;                                                      \
+    XG_CHECK_LAUNCH(ctx);                                        \
+    rc_ = launch_done(ctx, dev, slot_, e0_);                     \
+    if (rc_) return rc_;                                         \
+  } while (0)
+
+template <class F>
+Adj adj_of(RieCGDev* d) {
+  return Adj{d->soff, d->swidth, d->nbr};
+}
+Bnd bnd_of(RieCGDev* d) { return Bnd{d->bidx, d->bptr, d->bent, d->btri, d->bsym}; }
+
+BCProg bcprog_of(RieCGDev* d) {
+  BCProg b;
+  b.nbc = d->nbc;
+  b.node = d->bcnode;
+  b.dir = d->bcdir;
+  b.symp = d->bcsymp;
+  b.far = d->bcfar;
+  b.pre = d->bcpre;
+  b.dirmask = d->dirmask;
+  b.dirval = d->dirval;
+  b.symn = d->symn;
+  b.farn = d->farn;
+  b.preval = d->preval;
+  for (int i = 0; i < 5; ++i) b.far5[i] = d->far5[i];
+  return b;
+}
+
+template <class F>
+int launch_grad(xg_ctx* c, RieCGDev* d, const F* W, F* G, int divide) {
+  XG_PROF_LAUNCH(c, d, "riecg_grad",
+                 (k_grad<F><<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(
+                     d->n, adj_of<F>(d), static_cast<const F*>(d->dx),
+                     static_cast<const F*>(d->dy), static_cast<const F*>(d->dz), W, bnd_of(d),
+                     d->vol, divide, G)));
+  return XG_OK;
+}
+
+template <class F, int FLUX, int STAGE, bool UPDATE>
+int launch_rhs_t(xg_ctx* c, RieCGDev* d, const F* W, const F* G, F* Wout, double* Rout) {
+  XG_PROF_LAUNCH(c, d, "riecg_rhs_update",
+                 (k_rhs<F, FLUX, STAGE, UPDATE><<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(
+                     d->n, adj_of<F>(d), static_cast<const F*>(d->dx),
+                     static_cast<const F*>(d->dy), static_cast<const F*>(d->dz), W, G, bnd_of(d),
+                     d->bcflag, d->vol, d->prm.gamma, d->prm.stab2, d->prm.stab2coef, d->scal,
+                     d->U, d->Un, Wout, Rout, &d->scal->dtmin)));
+  return XG_OK;
+}
+
+template <class F, int FLUX>
+int launch_rhs_f(xg_ctx* c, RieCGDev* d, int stage, bool update, const F* W, const F* G, F* Wout,
+                 double* Rout) {
+  if (!update) return launch_rhs_t<F, FLUX, 0, false>(c, d, W, G, Wout, Rout);
+  if (stage == 0) return launch_rhs_t<F, FLUX, 0, true>(c, d, W, G, Wout, Rout);
+  if (stage == 1) return launch_rhs_t<F, FLUX, 1, true>(c, d, W, G, Wout, Rout);
+  return launch_rhs_t<F, FLUX, 2, true>(c, d, W, G, Wout, Rout);
+}
+
+template <class F>
+int launch_rhs(xg_ctx* c, RieCGDev* d, int stage, bool update, const F* W, const F* G, F* Wout,
+               double* Rout) {
+  if (d->prm.flux == XG_HLLC)
+    return launch_rhs_f<F, XG_HLLC>(c, d, stage, update, W, G, Wout, Rout);
+  return launch_rhs_f<F, XG_RUSANOV>(c, d, stage, update, W, G, Wout, Rout);
+}
+
+template <class F>
+int launch_bc(xg_ctx* c, RieCGDev* d, F* W, int want_dt) {
+  if (d->nbc == 0) return XG_OK;
+  XG_PROF_LAUNCH(c, d, "riecg_bc",
+                 (k_bc<F><<<blocks_for(d->nbc, kBlock), kBlock, 0, c->stream>>>(
+                     d->n, bcprog_of(d), d->prm.gamma, d->U, W, d->vol, want_dt,
+                     &d->scal->dtmin)));
+  return XG_OK;
+}
+
+// One stage on the device state.
+template <class F>
+int do_stage(xg_ctx* c, RieCGDev* d, int stage) {
+  F* Win = static_cast<F*>(d->W[d->cur]);
+  F* Wout = static_cast<F*>(d->W[d->cur ^ 1]);
+  F* G = static_cast<F*>(d->G);
+  int rc = launch_grad<F>(c, d, Win, G, 1);
+  if (rc) return rc;
+  rc = launch_rhs<F>(c, d, stage, true, Win, G, Wout, nullptr);
+  if (rc) return rc;
+  rc = launch_bc<F>(c, d, Wout, stage == 2);
+  if (rc) return rc;
+  d->cur ^= 1;
+  return XG_OK;
+}
+
+int refresh_dt(xg_ctx* c, RieCGDev* d) {
+  k_reset_min<<<1, 1, 0, c->stream>>>(d->scal);
+  XG_CHECK_LAUNCH(c);
+  k_dt<<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(d->n, d->U, d->vol, d->prm.gamma,
+                                                            &d->scal->dtmin);
+  XG_CHECK_LAUNCH(c);
+  d->dt_valid = true;
+  return XG_OK;
+}
+
+template <class F>
+int alloc_and_upload(xg_ctx* c, RieCGDev* d, const double* coord, const double* vol,
+                     const std::vector<int32_t>& soff, const std::vector<int32_t>& swidth,
+                     const std::vector<int32_t>& nbr, const std::vector<double>& ddx,
+                     const std::vector<double>& ddy, const std::vector<double>& ddz,
+                     const std::vector<int32_t>& bidx, const std::vector<int32_t>& bptr,
+                     const std::vector<int32_t>& bent, const std::vector<int32_t>& btri,
+                     const std::vector<uint8_t>& bsym) {
+  const int64_t n = d->n;
+  F *W0, *W1, *G, *dx, *dy, *dz;
+  for (int pass = 0; pass < 2; ++pass) {
+    Arena& A = d->arena;
+    A.plan(d->U, n * 5);
+    A.plan(d->Un, n * 5);
+    A.plan(d->vol, n);
+    A.plan(d->bidx, n);
+    A.plan(W0, n * 8);
+    A.plan(W1, n * 8);
+    A.plan(G, n * 16);
+    A.plan(d->soff, soff.size());
+    A.plan(d->swidth, swidth.size());
+    A.plan(d->nbr, nbr.size());
+    A.plan(dx, nbr.size());
+    A.plan(dy, nbr.size());
+    A.plan(dz, nbr.size());
+    A.plan(d->bptr, bptr.size());
+    A.plan(d->bent, std::max<size_t>(1, bent.size()));
+    A.plan(d->btri, std::max<size_t>(1, btri.size()));
+    A.plan(d->bsym, std::max<size_t>(1, bsym.size()));
+    A.plan(d->bcflag, std::max<int64_t>(1, d->nbn));
+    A.plan(d->scal, 1);
+    if (pass == 0) XG_CUDA(c, A.reserve());
+  }
+  for (int pass = 0; pass < 2; ++pass) {
+    Arena& S = d->scratch;
+    S.plan(d->stage_buf, n * 15);
+    F* sw;
+    F* sg;
+    S.plan(sw, n * 8);
+    S.plan(sg, n * 16);
+    d->stage_W = sw;
+    d->stage_G = sg;
+    if (pass == 0) XG_CUDA(c, S.reserve());
+  }
+  d->W[0] = W0;
+  d->W[1] = W1;
+  d->G = G;
+  d->dx = dx;
+  d->dy = dy;
+  d->dz = dz;
+  cudaStream_t s = c->stream;
+  auto up = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
+    return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s) : cudaSuccess;
+  };
+  XG_CUDA(c, up(d->vol, vol, n * sizeof(double)));
+  XG_CUDA(c, up(d->bidx, bidx.data(), n * sizeof(int32_t)));
+  XG_CUDA(c, up(d->soff, soff.data(), soff.size() * 4));
+  XG_CUDA(c, up(d->swidth, swidth.data(), swidth.size() * 4));
+  XG_CUDA(c, up(d->nbr, nbr.data(), nbr.size() * 4));
+  {
+    std::vector<F> t(nbr.size());
+    for (size_t i = 0; i < t.size(); ++i) t[i] = F(ddx[i]);
+    XG_CUDA(c, cudaMemcpy(dx, t.data(), t.size() * sizeof(F), cudaMemcpyHostToDevice));
+    for (size_t i = 0; i < t.size(); ++i) t[i] = F(ddy[i]);
+    XG_CUDA(c, cudaMemcpy(dy, t.data(), t.size() * sizeof(F), cudaMemcpyHostToDevice));
+    for (size_t i = 0; i < t.size(); ++i) t[i] = F(ddz[i]);
+    XG_CUDA(c, cudaMemcpy(dz, t.data(), t.size() * sizeof(F), cudaMemcpyHostToDevice));
+  }
+  XG_CUDA(c, up(d->bptr, bptr.data(), bptr.size() * 4));
+  XG_CUDA(c, up(d->bent, bent.data(), bent.size() * 4));
+  XG_CUDA(c, up(d->btri, btri.data(), btri.size() * 4));
+  XG_CUDA(c, up(d->bsym, bsym.data(), bsym.size()));
+  XG_CUDA(c, cudaMemsetAsync(d->bcflag, 0, std::max<int64_t>(1, d->nbn), s));
+  XG_CUDA(c, cudaMemsetAsync(d->U, 0, n * 5 * sizeof(double), s));
+  XG_CUDA(c, cudaMemsetAsync(d->Un, 0, n * 5 * sizeof(double), s));
+  XG_CUDA(c, cudaMemsetAsync(G, 0, n * 16 * sizeof(F), s));
+  {
+    // W records: zero primitives, coordinates in slots 5..7
+    std::vector<F> w(n * 8, F(0));
+    for (int64_t p = 0; p < n; ++p) {
+      w[p * 8 + 5] = F(coord[p]);
+      w[p * 8 + 6] = F(coord[n + p]);
+      w[p * 8 + 7] = F(coord[2 * n + p]);
+    }
+    XG_CUDA(c, cudaMemcpy(W0, w.data(), w.size() * sizeof(F), cudaMemcpyHostToDevice));
+    XG_CUDA(c, cudaMemcpy(W1, w.data(), w.size() * sizeof(F), cudaMemcpyHostToDevice));
+    XG_CUDA(c, cudaMemcpy(d->stage_W, w.data(), w.size() * sizeof(F), cudaMemcpyHostToDevice));
+  }
+  Scalars s0{0.0, 0ull, 0, 0};
+  double big = DBL_MAX;
+  std::memcpy(&s0.dtmin, &big, sizeof(double));
+  XG_CUDA(c, cudaMemcpy(d->scal, &s0, sizeof(s0), cudaMemcpyHostToDevice));
+  XG_CUDA(c, cudaStreamSynchronize(s));
+  return XG_OK;
+}
+
+}  // namespace
+
+}  // namespace xg
+
+using namespace xg;
+
+extern "C" {
+
+int xg_riecg_setup(xg_ctx* c, const xg_riecg_params* prm, int64_t npoin, const double* coord,
+                   const double* vol, int64_t ntet, const uint64_t* dsupedge0,
+                   const double* dsupint0, int64_t ntri, const uint64_t* dsupedge1,
+                   const double* dsupint1, int64_t nedge, const uint64_t* dsupedge2,
+                   const double* dsupint2, int64_t nbtri, const uint64_t* triinpoel,
+                   const uint8_t* besym) {
+  int rc = use(c);
+  if (rc) return rc;
+  if (!prm || npoin <= 0 || !coord || !vol) return fail(c, XG_ERR_ARG, "riecg_setup: bad mesh");
+  if (npoin >= (int64_t(1) << 31) - 64) return fail(c, XG_ERR_ARG, "riecg_setup: too many nodes");
+  if (prm->flux != XG_RUSANOV && prm->flux != XG_HLLC)
+    return fail(c, XG_ERR_ARG, "Flux not configured");
+  if (prm->precision != XG_FP64 && prm->precision != XG_FP32_FLUX)
+    return fail(c, XG_ERR_ARG, "riecg_setup: unknown precision");
+  if ((ntet && (!dsupedge0 || !dsupint0)) || (ntri && (!dsupedge1 || !dsupint1)) ||
+      (nedge && (!dsupedge2 || !dsupint2)) || (nbtri && (!triinpoel || !besym)))
+    return fail(c, XG_ERR_ARG, "riecg_setup: null superedge or boundary array");
+  // Expand superedges into edges in the orientation RieCG evaluates them
+  // (tet group: lpoed order (0,1),(1,2),(2,0),(0,3),(1,3),(2,3); triangle
+  // group: (0,1),(1,2),(2,0); src/Physics/Riemann.cpp:706-753).
+  std::vector<Edge> E;
+  E.reserve(static_cast<size_t>(ntet * 6 + ntri * 3 + nedge));
+  static const int tp[6][2] = {{0, 1}, {1, 2}, {2, 0}, {0, 3}, {1, 3}, {2, 3}};
+  static const int rp[3][2] = {{0, 1}, {1, 2}, {2, 0}};
+  auto bad = [&](uint64_t id) { return id >= static_cast<uint64_t>(npoin); };
+  for (int64_t e = 0; e < ntet; ++e) {
+    const uint64_t* N = dsupedge0 + e * 4;
+    for (int k = 0; k < 6; ++k) {
+      if (bad(N[tp[k][0]]) || bad(N[tp[k][1]])) return fail(c, XG_ERR_ARG, "tet superedge id");
+      const double* dd = dsupint0 + (e * 6 + k) * 3;
+      E.push_back({int64_t(N[tp[k][0]]), int64_t(N[tp[k][1]]), {dd[0], dd[1], dd[2]}});
+    }
+  }
+  for (int64_t e = 0; e < ntri; ++e) {
+    const uint64_t* N = dsupedge1 + e * 3;
+    for (int k = 0; k < 3; ++k) {
+      if (bad(N[rp[k][0]]) || bad(N[rp[k][1]])) return fail(c, XG_ERR_ARG, "tri superedge id");
+      const double* dd = dsupint1 + (e * 3 + k) * 3;
+      E.push_back({int64_t(N[rp[k][0]]), int64_t(N[rp[k][1]]), {dd[0], dd[1], dd[2]}});
+    }
+  }
+  for (int64_t e = 0; e < nedge; ++e) {
+    const uint64_t* N = dsupedge2 + e * 2;
+    if (bad(N[0]) || bad(N[1])) return fail(c, XG_ERR_ARG, "edge id");
+    const double* dd = dsupint2 + e * 3;
+    E.push_back({int64_t(N[0]), int64_t(N[1]), {dd[0], dd[1], dd[2]}});
+  }
+  const int64_t n = npoin;
+  // per node degree, then entries sorted by neighbour id
+  std::vector<int64_t> deg(n + 1, 0);
+  for (auto& e : E) {
+    if (e.a == e.b) return fail(c, XG_ERR_ARG, "degenerate edge");
+    ++deg[e.a + 1];
+    ++deg[e.b + 1];
+  }
+  std::vector<int64_t> start(deg);
+  for (int64_t i = 0; i < n; ++i) start[i + 1] += start[i];
+  struct Ent {
+    int64_t q;
+    int64_t eid;
+    bool first;
+  };
+  std::vector<Ent> ent(static_cast<size_t>(start[n]));
+  {
+    std::vector<int64_t> fill(start.begin(), start.end() - 1);
+    for (size_t k = 0; k < E.size(); ++k) {
+      ent[fill[E[k].a]++] = {E[k].b, int64_t(k), true};
+      ent[fill[E[k].b]++] = {E[k].a, int64_t(k), false};
+    }
+  }
+  for (int64_t p = 0; p < n; ++p)
+    std::sort(ent.begin() + start[p], ent.begin() + start[p + 1],
+              [](const Ent& x, const Ent& y) { return x.q < y.q || (x.q == y.q && x.eid < y.eid); });
+  // SELL-32 slices
+  const int64_t nslice = (n + kSlice - 1) / kSlice;
+  std::vector<int32_t> soff(nslice + 1), swidth(nslice);
+  int64_t total = 0;
+  for (int64_t s = 0; s < nslice; ++s) {
+    int64_t w = 0;
+    for (int64_t p = s * kSlice; p < std::min(n, (s + 1) * kSlice); ++p)
+      w = std::max<int64_t>(w, start[p + 1] - start[p]);
+    swidth[s] = static_cast<int32_t>(w);
+    soff[s] = static_cast<int32_t>(total);
+    total += w * kSlice;
+    if (total >= (int64_t(1) << 31)) return fail(c, XG_ERR_ARG, "adjacency too large");
+  }
+  soff[nslice] = static_cast<int32_t>(total);
+  std::vector<int32_t> nbr(static_cast<size_t>(total), kPad);
+  std::vector<double> ddx(nbr.size(), 0.0), ddy(nbr.size(), 0.0), ddz(nbr.size(), 0.0);
+  for (int64_t p = 0; p < n; ++p) {
+    const int64_t s = p / kSlice, lane = p % kSlice;
+    for (int64_t k = 0; k < start[p + 1] - start[p]; ++k) {
+      const Ent& en = ent[start[p] + k];
+      const int64_t idx = soff[s] + k * kSlice + lane;
+      nbr[idx] = en.first ? static_cast<int32_t>(en.q) : ~static_cast<int32_t>(en.q);
+      ddx[idx] = E[en.eid].d[0];
+      ddy[idx] = E[en.eid].d[1];
+      ddz[idx] = E[en.eid].d[2];
+    }
+  }
+  // boundary triangles: per boundary node, the (tri, position) pairs
+  std::vector<int32_t> bidx(n, -1), btri(nbtri * 3);
+  std::vector<uint8_t> bsym(nbtri * 3);
+  std::vector<int64_t> bcount;
+  int64_t nbn = 0;
+  for (int64_t t = 0; t < nbtri; ++t)
+    for (int a = 0; a < 3; ++a) {
+      uint64_t p = triinpoel[t * 3 + a];
+      if (bad(p)) return fail(c, XG_ERR_ARG, "triinpoel id");
+      btri[t * 3 + a] = static_cast<int32_t>(p);
+      bsym[t * 3 + a] = besym[t * 3 + a] ? 1 : 0;
+      if (bidx[p] < 0) {
+        bidx[p] = static_cast<int32_t>(nbn++);
+        bcount.push_back(0);
+      }
+      ++bcount[bidx[p]];
+    }
+  std::vector<int32_t> bptr(nbn + 1, 0), bent(nbtri * 3);
+  for (int64_t i = 0; i < nbn; ++i) bptr[i + 1] = bptr[i] + static_cast<int32_t>(bcount[i]);
+  {
+    std::vector<int32_t> fill(bptr.begin(), bptr.end() - 1);
+    for (int64_t t = 0; t < nbtri; ++t)
+      for (int a = 0; a < 3; ++a) {
+        int32_t bi = bidx[triinpoel[t * 3 + a]];
+        bent[fill[bi]++] = static_cast<int32_t>(t * 4 + a);
+      }
+  }
+  // (re)create the device state
+  if (c->riecg) {
+    XG_CUDA(c, cudaStreamSynchronize(c->stream));
+    destroy_riecg(c->riecg);
+    c->riecg = nullptr;
+  }
+  auto* d = new RieCGDev;
+  c->riecg = d;
+  d->n = n;
+  d->prm = *prm;
+  d->fp32 = prm->precision == XG_FP32_FLUX;
+  d->nslice = nslice;
+  d->nent = total;
+  d->nbn = nbn;
+  d->nbt = nbtri;
+  d->nbent = nbtri * 3;
+  if (d->fp32)
+    rc = alloc_and_upload<float>(c, d, coord, vol, soff, swidth, nbr, ddx, ddy, ddz, bidx, bptr,
+                                 bent, btri, bsym);
+  else
+    rc = alloc_and_upload<double>(c, d, coord, vol, soff, swidth, nbr, ddx, ddy, ddz, bidx, bptr,
+                                  bent, btri, bsym);
+  if (rc) {
+    destroy_riecg(d);
+    c->riecg = nullptr;
+    return rc;
+  }
+  // bidx is also needed on the host to set BC flags later
+  return XG_OK;
+}
+
+int xg_riecg_set_bc(xg_ctx* c, int64_t nsym, const uint64_t* symnodes, const double* symnorms,
+                    int64_t nfar, const uint64_t* farnodes, const double* farnorms,
+                    const double* far5, int64_t ndir, const uint64_t* dirnodes,
+                    const int32_t* dirmask, const double* dirvals, int64_t npre,
+                    const uint64_t* prenodes, const double* prevals) {
+  int rc = use(c);
+  if (rc) return rc;
+  RieCGDev* d = c->riecg;
+  if (!d) return fail(c, XG_ERR_STATE, "riecg_set_bc before riecg_setup");
+  const int64_t n = d->n;
+  auto chk = [&](int64_t cnt, const uint64_t* ids) {
+    for (int64_t i = 0; i < cnt; ++i)
+      if (ids[i] >= static_cast<uint64_t>(n)) return false;
+    return true;
+  };
+  if ((nsym && (!symnodes || !symnorms)) || (nfar && (!farnodes || !farnorms || !far5)) ||
+      (ndir && (!dirnodes || !dirmask || !dirvals)) || (npre && (!prenodes || !prevals)))
+    return fail(c, XG_ERR_ARG, "riecg_set_bc: null array");
+  if (!chk(nsym, symnodes) || !chk(nfar, farnodes) || !chk(ndir, dirnodes) || !chk(npre, prenodes))
+    return fail(c, XG_ERR_ARG, "riecg_set_bc: node id out of range");
+  // unique BC nodes in increasing id order, each with its ops
+  std::vector<int64_t> ids;
+  ids.insert(ids.end(), symnodes, symnodes + nsym);
+  ids.insert(ids.end(), farnodes, farnodes + nfar);
+  ids.insert(ids.end(), dirnodes, dirnodes + ndir);
+  ids.insert(ids.end(), prenodes, prenodes + npre);
+  std::sort(ids.begin(), ids.end());
+  ids.erase(std::unique(ids.begin(), ids.end()), ids.end());
+  const int64_t nbc = static_cast<int64_t>(ids.size());
+  std::vector<int32_t> node(nbc), dir(nbc, -1), far(nbc, -1), pre(nbc, -1), symp(nbc + 1, 0);
+  auto pos = [&](uint64_t p) {
+    return static_cast<int64_t>(std::lower_bound(ids.begin(), ids.end(), int64_t(p)) - ids.begin());
+  };
+  for (int64_t i = 0; i < nbc; ++i) node[i] = static_cast<int32_t>(ids[i]);
+  for (int64_t k = 0; k < ndir; ++k) dir[pos(dirnodes[k])] = static_cast<int32_t>(k);
+  for (int64_t k = 0; k < nfar; ++k) far[pos(farnodes[k])] = static_cast<int32_t>(k);
+  for (int64_t k = 0; k < npre; ++k) pre[pos(prenodes[k])] = static_cast<int32_t>(k);
+  // symmetry normals grouped per node, keeping the given order within a node
+  std::vector<int64_t> cnt(nbc, 0);
+  for (int64_t k = 0; k < nsym; ++k) ++cnt[pos(symnodes[k])];
+  for (int64_t i = 0; i < nbc; ++i) symp[i + 1] = symp[i] + static_cast<int32_t>(cnt[i]);
+  std::vector<double> symn(std::max<int64_t>(1, nsym) * 3, 0.0);
+  {
+    std::vector<int32_t> fill(symp.begin(), symp.end() - 1);
+    for (int64_t k = 0; k < nsym; ++k) {
+      int32_t j = fill[pos(symnodes[k])]++;
+      for (int a = 0; a < 3; ++a) symn[j * 3 + a] = symnorms[k * 3 + a];
+    }
+  }
+  // per boundary node flag "has a nodal BC" (for the CFL reduction split)
+  std::vector<int32_t> hbidx(n);
+  XG_CUDA(c, cudaMemcpy(hbidx.data(), d->bidx, n * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  std::vector<uint8_t> flag(std::max<int64_t>(1, d->nbn), 0);
+  for (int64_t i = 0; i < nbc; ++i) {
+    int32_t bi = hbidx[ids[i]];
+    if (bi < 0)
+      return fail(c, XG_ERR_ARG, "riecg_set_bc: BC node not on a boundary triangle");
+    flag[bi] = 1;
+  }
+  XG_CUDA(c, cudaStreamSynchronize(c->stream));
+  d->bcarena.release();
+  for (int pass = 0; pass < 2; ++pass) {
+    Arena& A = d->bcarena;
+    A.plan(d->bcnode, std::max<int64_t>(1, nbc));
+    A.plan(d->bcdir, std::max<int64_t>(1, nbc));
+    A.plan(d->bcfar, std::max<int64_t>(1, nbc));
+    A.plan(d->bcpre, std::max<int64_t>(1, nbc));
+    A.plan(d->bcsymp, nbc + 1);
+    A.plan(d->symn, symn.size());
+    A.plan(d->dirmask, std::max<int64_t>(1, ndir) * 5);
+    A.plan(d->dirval, std::max<int64_t>(1, ndir) * 5);
+    A.plan(d->farn, std::max<int64_t>(1, nfar) * 3);
+    A.plan(d->preval, std::max<int64_t>(1, npre) * 2);
+    if (pass == 0) XG_CUDA(c, A.reserve());
+  }
+  auto up = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
+    return bytes ? cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice) : cudaSuccess;
+  };
+  XG_CUDA(c, up(d->bcnode, node.data(), nbc * 4));
+  XG_CUDA(c, up(d->bcdir, dir.data(), nbc * 4));
+  XG_CUDA(c, up(d->bcfar, far.data(), nbc * 4));
+  XG_CUDA(c, up(d->bcpre, pre.data(), nbc * 4));
+  XG_CUDA(c, up(d->bcsymp, symp.data(), (nbc + 1) * 4));
+  XG_CUDA(c, up(d->symn, symn.data(), symn.size() * 8));
+  XG_CUDA(c, up(d->dirmask, dirmask, ndir * 5 * 4));
+  XG_CUDA(c, up(d->dirval, dirvals, ndir * 5 * 8));
+  XG_CUDA(c, up(d->farn, farnorms, nfar * 3 * 8));
+  XG_CUDA(c, up(d->preval, prevals, npre * 2 * 8));
+  XG_CUDA(c, up(d->bcflag, flag.data(), flag.size()));
+  if (far5)
+    for (int i = 0; i < 5; ++i) d->far5[i] = far5[i];
+  d->nbc = nbc;
+  d->dt_valid = false;
+  return XG_OK;
+}
+
+int xg_riecg_set_state(xg_ctx* c, const double* U, double t) {
+  int rc = use(c);
+  if (rc) return rc;
+  RieCGDev* d = c->riecg;
+  if (!d) return fail(c, XG_ERR_STATE, "riecg_set_state before riecg_setup");
+  if (!U) return fail(c, XG_ERR_ARG, "riecg_set_state: null U");
+  XG_CUDA(c, cudaMemcpyAsync(d->stage_buf, U, d->n * 5 * sizeof(double), cudaMemcpyHostToDevice,
+                             c->stream));
+  k_aos_to_soa<<<blocks_for(d->n * 5, kBlock), kBlock, 0, c->stream>>>(d->n, 5, d->stage_buf,
+                                                                        d->U);
+  XG_CHECK_LAUNCH(c);
+  if (d->fp32) {
+    float* W = static_cast<float*>(d->W[d->cur]);
+    k_prim_aos<float><<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(d->n, d->stage_buf, W, W);
+  } else {
+    double* W = static_cast<double*>(d->W[d->cur]);
+    k_prim_aos<double><<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(d->n, d->stage_buf, W, W);
+  }
+  XG_CHECK_LAUNCH(c);
+  d->t = t;
+  rc = refresh_dt(c, d);
+  if (rc) return rc;
+  XG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return XG_OK;
+}
+
+int xg_riecg_get_state(xg_ctx* c, double* U, double* t) {
+  int rc = use(c);
+  if (rc) return rc;
+  RieCGDev* d = c->riecg;
+  if (!d) return fail(c, XG_ERR_STATE, "riecg_get_state before riecg_setup");
+  if (U) {
+    k_soa_to_aos<<<blocks_for(d->n * 5, kBlock), kBlock, 0, c->stream>>>(d->n, 5, d->U,
+                                                                          d->stage_buf);
+    XG_CHECK_LAUNCH(c);
+    XG_CUDA(c, cudaMemcpyAsync(U, d->stage_buf, d->n * 5 * sizeof(double), cudaMemcpyDeviceToHost,
+                               c->stream));
+  }
+  XG_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (t) *t = d->t;
+  return XG_OK;
+}
+
+}  // extern "C"
+
+namespace {
+template <class F>
+int grad_dropin(xg_ctx* c, RieCGDev* d, const double* U, double* G) {
+  F* W = static_cast<F*>(d->stage_W);
+  F* Gr = static_cast<F*>(d->stage_G);
+  XG_CUDA(c, cudaMemcpyAsync(d->stage_buf, U, d->n * 5 * sizeof(double), cudaMemcpyHostToDevice,
+                             c->stream));
+  k_prim_aos<F><<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(d->n, d->stage_buf, W, W);
+  XG_CHECK_LAUNCH(c);
+  int rc = launch_grad<F>(c, d, W, Gr, 0);
+  if (rc) return rc;
+  k_grec_to_aos<F><<<blocks_for(d->n * 15, kBlock), kBlock, 0, c->stream>>>(d->n, Gr, d->stage_buf);
+  XG_CHECK_LAUNCH(c);
+  XG_CUDA(c, cudaMemcpyAsync(G, d->stage_buf, d->n * 15 * sizeof(double), cudaMemcpyDeviceToHost,
+                             c->stream));
+  XG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return XG_OK;
+}
+
+template <class F>
+int rhs_dropin(xg_ctx* c, RieCGDev* d, const double* G, const double* U, double* R) {
+  F* W = static_cast<F*>(d->stage_W);
+  F* Gr = static_cast<F*>(d->stage_G);
+  XG_CUDA(c, cudaMemcpyAsync(d->stage_buf, G, d->n * 15 * sizeof(double), cudaMemcpyHostToDevice,
+                             c->stream));
+  k_aos_to_grec<F><<<blocks_for(d->n * 16, kBlock), kBlock, 0, c->stream>>>(d->n, d->stage_buf, Gr);
+  XG_CHECK_LAUNCH(c);
+  XG_CUDA(c, cudaMemcpyAsync(d->stage_buf, U, d->n * 5 * sizeof(double), cudaMemcpyHostToDevice,
+                             c->stream));
+  k_prim_aos<F><<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(d->n, d->stage_buf, W, W);
+  XG_CHECK_LAUNCH(c);
+  int rc = launch_rhs<F>(c, d, 0, false, W, Gr, nullptr, d->stage_buf);
+  if (rc) return rc;
+  XG_CUDA(c, cudaMemcpyAsync(R, d->stage_buf, d->n * 5 * sizeof(double), cudaMemcpyDeviceToHost,
+                             c->stream));
+  XG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return XG_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int xg_riecg_grad(xg_ctx* c, const double* U, double* G) {
+  int rc = use(c);
+  if (rc) return rc;
+  RieCGDev* d = c->riecg;
+  if (!d) return fail(c, XG_ERR_STATE, "riecg_grad before riecg_setup");
+  if (!U || !G) return fail(c, XG_ERR_ARG, "riecg_grad: null array");
+  return d->fp32 ? grad_dropin<float>(c, d, U, G) : grad_dropin<double>(c, d, U, G);
+}
+
+int xg_riecg_rhs(xg_ctx* c, const double* G, const double* U, double* R) {
+  int rc = use(c);
+  if (rc) return rc;
+  RieCGDev* d = c->riecg;
+  if (!d) return fail(c, XG_ERR_STATE, "riecg_rhs before riecg_setup");
+  if (!U || !G || !R) return fail(c, XG_ERR_ARG, "riecg_rhs: null array");
+  return d->fp32 ? rhs_dropin<float>(c, d, G, U, R) : rhs_dropin<double>(c, d, G, U, R);
+}
+
+int xg_riecg_bc(xg_ctx* c) {
+  int rc = use(c);
+  if (rc) return rc;
+  RieCGDev* d = c->riecg;
+  if (!d) return fail(c, XG_ERR_STATE, "riecg_bc before riecg_setup");
+  if (d->fp32)
+    rc = launch_bc<float>(c, d, static_cast<float*>(d->W[d->cur]), 0);
+  else
+    rc = launch_bc<double>(c, d, static_cast<double*>(d->W[d->cur]), 0);
+  if (rc) return rc;
+  rc = refresh_dt(c, d);
+  if (rc) return rc;
+  XG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return XG_OK;
+}
+
+int xg_riecg_dt(xg_ctx* c, double* dt) {
+  int rc = use(c);
+  if (rc) return rc;
+  RieCGDev* d = c->riecg;
+  if (!d) return fail(c, XG_ERR_STATE, "riecg_dt before riecg_setup");
+  if (!dt) return fail(c, XG_ERR_ARG, "riecg_dt: null dt");
+  if (!d->dt_valid) {
+    rc = refresh_dt(c, d);
+    if (rc) return rc;
+  }
+  Scalars s;
+  XG_CUDA(c, cudaMemcpyAsync(&s, d->scal, sizeof(s), cudaMemcpyDeviceToHost, c->stream));
+  XG_CUDA(c, cudaStreamSynchronize(c->stream));
+  double m;
+  std::memcpy(&m, &s.dtmin, sizeof(double));
+  if (std::fabs(d->prm.const_dt) > std::numeric_limits<double>::epsilon())
+    *dt = d->prm.const_dt;
+  else
+    *dt = m * d->prm.cfl;
+  return XG_OK;
+}
+
+int xg_riecg_stage(xg_ctx* c, int stage, double dt) {
+  int rc = use(c);
+  if (rc) return rc;
+  RieCGDev* d = c->riecg;
+  if (!d) return fail(c, XG_ERR_STATE, "riecg_stage before riecg_setup");
+  if (stage < 0 || stage > 2) return fail(c, XG_ERR_ARG, "riecg_stage: stage must be 0..2");
+  k_set_dt<<<1, 1, 0, c->stream>>>(d->scal, dt);
+  XG_CHECK_LAUNCH(c);
+  if (stage == 2) {
+    k_reset_min<<<1, 1, 0, c->stream>>>(d->scal);
+    XG_CHECK_LAUNCH(c);
+  }
+  rc = d->fp32 ? do_stage<float>(c, d, stage) : do_stage<double>(c, d, stage);
+  if (rc) return rc;
+  d->dt_valid = stage == 2;
+  rc = flush_profile(c, d);
+  if (rc) return rc;
+  XG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return XG_OK;
+}
+
+int xg_riecg_run(xg_ctx* c, int64_t nstep, double* dts, float* ms) {
+  int rc = use(c);
+  if (rc) return rc;
+  RieCGDev* d = c->riecg;
+  if (!d) return fail(c, XG_ERR_STATE, "riecg_run before riecg_setup");
+  if (nstep < 0) return fail(c, XG_ERR_ARG, "riecg_run: negative step count");
+  if (nstep == 0) {
+    if (ms) *ms = 0.f;
+    return XG_OK;
+  }
+  if (!d->dt_valid) {
+    rc = refresh_dt(c, d);
+    if (rc) return rc;
+  }
+  if (d->dthist_cap < nstep) {
+    XG_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (d->dthist) cudaFree(d->dthist);
+    d->dthist = nullptr;
+    XG_CUDA(c, cudaMalloc(&d->dthist, nstep * sizeof(double)));
+    d->dthist_cap = nstep;
+  }
+  cudaEvent_t e0, e1;
+  XG_CUDA(c, cudaEventCreate(&e0));
+  XG_CUDA(c, cudaEventCreate(&e1));
+  XG_CUDA(c, cudaEventRecord(e0, c->stream));
+  for (int64_t k = 0; k < nstep; ++k) {
+    XG_PROF_LAUNCH(c, d, "riecg_step_begin",
+                   (k_step_begin<<<1, 1, 0, c->stream>>>(d->scal, d->prm.cfl, d->prm.const_dt,
+                                                         d->dthist, k)));
+    for (int st = 0; st < 3; ++st) {
+      rc = d->fp32 ? do_stage<float>(c, d, st) : do_stage<double>(c, d, st);
+      if (rc) return rc;
+    }
+  }
+  XG_CUDA(c, cudaEventRecord(e1, c->stream));
+  XG_CUDA(c, cudaEventSynchronize(e1));
+  float el = 0.f;
+  XG_CUDA(c, cudaEventElapsedTime(&el, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (ms) *ms = el;
+  rc = flush_profile(c, d);
+  if (rc) return rc;
+  std::vector<double> h(nstep);
+  XG_CUDA(c, cudaMemcpy(h.data(), d->dthist, nstep * sizeof(double), cudaMemcpyDeviceToHost));
+  for (double v : h) d->t += v;
+  if (dts) std::memcpy(dts, h.data(), nstep * sizeof(double));
+  d->dt_valid = true;
+  Scalars s;
+  XG_CUDA(c, cudaMemcpy(&s, d->scal, sizeof(s), cudaMemcpyDeviceToHost));
+  if (s.blowup) return fail(c, XG_ERR_BLOWUP, "dt below machine epsilon");
+  return XG_OK;
+}
+
+int xg_riecg_profile(xg_ctx* c, int enable) {
+  if (!c || !c->riecg) return fail(c, XG_ERR_STATE, "riecg_profile before riecg_setup");
+  c->riecg->prof = enable != 0;
+  c->riecg->ktimes.clear();
+  return XG_OK;
+}
+
+int xg_riecg_kernel_times(xg_ctx* c, int cap, const char** names, double* ms, int64_t* launches,
+                          int* n) {
+  if (!c || !c->riecg) return fail(c, XG_ERR_STATE, "riecg_kernel_times before riecg_setup");
+  auto& kt = c->riecg->ktimes;
+  if (n) *n = static_cast<int>(kt.size());
+  for (int i = 0; i < cap && i < static_cast<int>(kt.size()); ++i) {
+    if (names) names[i] = kt[i].name;
+    if (ms) ms[i] = kt[i].ms;
+    if (launches) launches[i] = kt[i].launches;
+  }
+  return XG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,247 @@
+// Host-side operator setup: the caller side of xg_riecg_setup.  Builds, from
+// a tetrahedron mesh, the arrays RieCG computes once per mesh (nodal
+// volumes, domain edge integrals, boundary point normals) and a locality
+// renumbering.  Plain C++; linear or n log n in the mesh size.
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <numeric>
+#include <queue>
+#include <string>
+#include <vector>
+
+#include "../../include/xg.h"
+
+namespace {
+
+// Points surrounding points as CSR (sorted, unique, no self) from tets.
+void psup(int64_t n, int64_t nelem, const uint64_t* inpoel, std::vector<int64_t>& ptr,
+          std::vector<int64_t>& adj) {
+  std::vector<int64_t> cnt(n + 1, 0);
+  for (int64_t e = 0; e < nelem; ++e)
+    for (int a = 0; a < 4; ++a) cnt[inpoel[e * 4 + a] + 1] += 3;
+  for (int64_t i = 0; i < n; ++i) cnt[i + 1] += cnt[i];
+  std::vector<int64_t> tmp(cnt[n]);
+  std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
+  for (int64_t e = 0; e < nelem; ++e)
+    for (int a = 0; a < 4; ++a)
+      for (int b = 0; b < 4; ++b)
+        if (a != b) tmp[fill[inpoel[e * 4 + a]]++] = static_cast<int64_t>(inpoel[e * 4 + b]);
+  ptr.assign(n + 1, 0);
+  adj.clear();
+  adj.reserve(tmp.size() / 3);
+  for (int64_t i = 0; i < n; ++i) {
+    auto b = tmp.begin() + cnt[i], en = tmp.begin() + cnt[i + 1];
+    std::sort(b, en);
+    auto u = std::unique(b, en);
+    adj.insert(adj.end(), b, u);
+    ptr[i + 1] = static_cast<int64_t>(adj.size());
+  }
+}
+
+inline void cross(double ax, double ay, double az, double bx, double by, double bz, double& rx,
+                  double& ry, double& rz) {
+  rx = ay * bz - by * az;
+  ry = az * bx - bz * ax;
+  rz = ax * by - bx * ay;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Reverse Cuthill-McKee: BFS from a minimum-degree node of each connected
+// component, visiting neighbours in increasing degree, then reversed.
+int xg_mesh_rcm(int64_t npoin, int64_t nelem, const uint64_t* inpoel, uint64_t* new_of_old) {
+  if (npoin <= 0 || nelem < 0 || !inpoel || !new_of_old) return XG_ERR_ARG;
+  for (int64_t i = 0; i < nelem * 4; ++i)
+    if (inpoel[i] >= static_cast<uint64_t>(npoin)) return XG_ERR_ARG;
+  std::vector<int64_t> ptr, adj;
+  psup(npoin, nelem, inpoel, ptr, adj);
+  std::vector<int64_t> deg(npoin);
+  for (int64_t i = 0; i < npoin; ++i) deg[i] = ptr[i + 1] - ptr[i];
+  std::vector<int64_t> order;
+  order.reserve(npoin);
+  std::vector<char> seen(npoin, 0);
+  std::vector<int64_t> byDeg(npoin);
+  std::iota(byDeg.begin(), byDeg.end(), 0);
+  std::stable_sort(byDeg.begin(), byDeg.end(),
+                   [&](int64_t a, int64_t b) { return deg[a] < deg[b]; });
+  std::vector<int64_t> nb;
+  for (int64_t root : byDeg) {
+    if (seen[root]) continue;
+    size_t head = order.size();
+    order.push_back(root);
+    seen[root] = 1;
+    while (head < order.size()) {
+      int64_t p = order[head++];
+      nb.clear();
+      for (int64_t j = ptr[p]; j < ptr[p + 1]; ++j)
+        if (!seen[adj[j]]) nb.push_back(adj[j]);
+      std::stable_sort(nb.begin(), nb.end(),
+                       [&](int64_t a, int64_t b) { return deg[a] < deg[b]; });
+      for (int64_t q : nb) {
+        seen[q] = 1;
+        order.push_back(q);
+      }
+    }
+  }
+  for (int64_t k = 0; k < npoin; ++k)
+    new_of_old[order[k]] = static_cast<uint64_t>(npoin - 1 - k);
+  return XG_OK;
+}
+
+int xg_mesh_vol(int64_t npoin, const double* coord, int64_t nelem, const uint64_t* inpoel,
+                double* vol) {
+  if (npoin <= 0 || !coord || !inpoel || !vol) return XG_ERR_ARG;
+  const double *x = coord, *y = coord + npoin, *z = coord + 2 * npoin;
+  std::fill(vol, vol + npoin, 0.0);
+  for (int64_t e = 0; e < nelem; ++e) {
+    const uint64_t* N = inpoel + e * 4;
+    for (int a = 0; a < 4; ++a)
+      if (N[a] >= static_cast<uint64_t>(npoin)) return XG_ERR_ARG;
+    double ba[3] = {x[N[1]] - x[N[0]], y[N[1]] - y[N[0]], z[N[1]] - z[N[0]]};
+    double ca[3] = {x[N[2]] - x[N[0]], y[N[2]] - y[N[0]], z[N[2]] - z[N[0]]};
+    double da[3] = {x[N[3]] - x[N[0]], y[N[3]] - y[N[0]], z[N[3]] - z[N[0]]};
+    double cx, cy, cz;
+    cross(ca[0], ca[1], ca[2], da[0], da[1], da[2], cx, cy, cz);
+    double J = (ba[0] * cx + ba[1] * cy + ba[2] * cz) / 24.0;
+    if (!(J > 0)) return XG_ERR_ARG;
+    for (int a = 0; a < 4; ++a) vol[N[a]] += J;
+  }
+  return XG_OK;
+}
+
+int xg_mesh_edges(int64_t npoin, const double* coord, int64_t nelem, const uint64_t* inpoel,
+                  const uint64_t* gid, int ncoef, int64_t cap, int64_t* nedge, uint64_t* edges,
+                  double* dint) {
+  if (npoin <= 0 || !coord || !inpoel || !nedge || (ncoef != 3 && ncoef != 5)) return XG_ERR_ARG;
+  const double *x = coord, *y = coord + npoin, *z = coord + 2 * npoin;
+  auto G = [&](uint64_t p) { return gid ? gid[p] : p; };
+  // rows keyed by the smaller-gid end, holding the larger-gid ends
+  std::vector<int64_t> cnt(npoin + 1, 0);
+  static const int lpoed[6][2] = {{0, 1}, {1, 2}, {2, 0}, {0, 3}, {1, 3}, {2, 3}};
+  for (int64_t e = 0; e < nelem; ++e)
+    for (int k = 0; k < 6; ++k) {
+      uint64_t a = inpoel[e * 4 + lpoed[k][0]], b = inpoel[e * 4 + lpoed[k][1]];
+      if (a >= uint64_t(npoin) || b >= uint64_t(npoin)) return XG_ERR_ARG;
+      ++cnt[(G(a) < G(b) ? a : b) + 1];
+    }
+  for (int64_t i = 0; i < npoin; ++i) cnt[i + 1] += cnt[i];
+  std::vector<uint64_t> col(cnt[npoin]);
+  {
+    std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
+    for (int64_t e = 0; e < nelem; ++e)
+      for (int k = 0; k < 6; ++k) {
+        uint64_t a = inpoel[e * 4 + lpoed[k][0]], b = inpoel[e * 4 + lpoed[k][1]];
+        if (G(a) < G(b))
+          col[fill[a]++] = b;
+        else
+          col[fill[b]++] = a;
+      }
+  }
+  std::vector<int64_t> rptr(npoin + 1, 0);
+  std::vector<uint64_t> rcol;
+  rcol.reserve(col.size() / 4);
+  for (int64_t i = 0; i < npoin; ++i) {
+    auto b = col.begin() + cnt[i], en = col.begin() + cnt[i + 1];
+    std::sort(b, en, [&](uint64_t p, uint64_t q) { return G(p) < G(q); });
+    auto u = std::unique(b, en);
+    rcol.insert(rcol.end(), b, u);
+    rptr[i + 1] = static_cast<int64_t>(rcol.size());
+  }
+  const int64_t ne = static_cast<int64_t>(rcol.size());
+  *nedge = ne;
+  if (cap < ne) return XG_OK;
+  if (!edges || !dint) return XG_ERR_ARG;
+  std::vector<double> D(static_cast<size_t>(ne) * ncoef, 0.0);
+  for (int64_t e = 0; e < nelem; ++e) {
+    const uint64_t* N = inpoel + e * 4;
+    double ba[3] = {x[N[1]] - x[N[0]], y[N[1]] - y[N[0]], z[N[1]] - z[N[0]]};
+    double ca[3] = {x[N[2]] - x[N[0]], y[N[2]] - y[N[0]], z[N[2]] - z[N[0]]};
+    double da[3] = {x[N[3]] - x[N[0]], y[N[3]] - y[N[0]], z[N[3]] - z[N[0]]};
+    double g[4][3];
+    cross(ca[0], ca[1], ca[2], da[0], da[1], da[2], g[1][0], g[1][1], g[1][2]);
+    cross(da[0], da[1], da[2], ba[0], ba[1], ba[2], g[2][0], g[2][1], g[2][2]);
+    cross(ba[0], ba[1], ba[2], ca[0], ca[1], ca[2], g[3][0], g[3][1], g[3][2]);
+    for (int i = 0; i < 3; ++i) g[0][i] = -g[1][i] - g[2][i] - g[3][i];
+    double J = ba[0] * g[1][0] + ba[1] * g[1][1] + ba[2] * g[1][2];
+    for (int k = 0; k < 6; ++k) {
+      int p = lpoed[k][0], q = lpoed[k][1];
+      uint64_t a = N[p], b = N[q];
+      double sig = 1.0;
+      if (G(a) > G(b)) {
+        std::swap(a, b);
+        sig = -1.0;
+      }
+      auto beg = rcol.begin() + rptr[a], en = rcol.begin() + rptr[a + 1];
+      auto it = std::lower_bound(beg, en, b, [&](uint64_t u, uint64_t v) { return G(u) < G(v); });
+      double* n = &D[static_cast<size_t>(it - rcol.begin()) * ncoef];
+      n[0] += sig * (g[p][0] - g[q][0]) / 48.0;
+      n[1] += sig * (g[p][1] - g[q][1]) / 48.0;
+      n[2] += sig * (g[p][2] - g[q][2]) / 48.0;
+      if (ncoef == 5) {
+        n[3] += J / 120.0;
+        n[4] += (g[p][0] * g[q][0] + g[p][1] * g[q][1] + g[p][2] * g[q][2]) / J / 6.0;
+      }
+    }
+  }
+  // emit in (gid, gid) order
+  std::vector<int64_t> rows(npoin);
+  std::iota(rows.begin(), rows.end(), 0);
+  if (gid) std::sort(rows.begin(), rows.end(), [&](int64_t a, int64_t b) { return gid[a] < gid[b]; });
+  int64_t k = 0;
+  for (int64_t a : rows)
+    for (int64_t j = rptr[a]; j < rptr[a + 1]; ++j) {
+      edges[k * 2 + 0] = static_cast<uint64_t>(a);
+      edges[k * 2 + 1] = rcol[j];
+      std::memcpy(dint + k * ncoef, &D[static_cast<size_t>(j) * ncoef], sizeof(double) * ncoef);
+      ++k;
+    }
+  return XG_OK;
+}
+
+int xg_mesh_bnorm(int64_t npoin, const double* coord, int64_t nface, const uint64_t* faces,
+                  int64_t nnode, const uint64_t* nodes, double* norms) {
+  if (npoin <= 0 || !coord || (nface && !faces) || (nnode && (!nodes || !norms)))
+    return XG_ERR_ARG;
+  const double *x = coord, *y = coord + npoin, *z = coord + 2 * npoin;
+  std::vector<double> acc(static_cast<size_t>(npoin) * 4, 0.0);
+  std::vector<char> on(npoin, 0);
+  for (int64_t f = 0; f < nface; ++f) {
+    const uint64_t* N = faces + f * 3;
+    for (int a = 0; a < 3; ++a)
+      if (N[a] >= uint64_t(npoin)) return XG_ERR_ARG;
+    double ba[3] = {x[N[1]] - x[N[0]], y[N[1]] - y[N[0]], z[N[1]] - z[N[0]]};
+    double ca[3] = {x[N[2]] - x[N[0]], y[N[2]] - y[N[0]], z[N[2]] - z[N[0]]};
+    double n[3];
+    cross(ba[0], ba[1], ba[2], ca[0], ca[1], ca[2], n[0], n[1], n[2]);
+    double A2 = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    n[0] /= A2;
+    n[1] /= A2;
+    n[2] /= A2;
+    double c[3] = {(x[N[0]] + x[N[1]] + x[N[2]]) / 3.0, (y[N[0]] + y[N[1]] + y[N[2]]) / 3.0,
+                   (z[N[0]] + z[N[1]] + z[N[2]]) / 3.0};
+    for (int i = 0; i < 3; ++i) {
+      uint64_t p = N[i];
+      double r = 1.0 / ((c[0] - x[p]) * (c[0] - x[p]) + (c[1] - y[p]) * (c[1] - y[p]) +
+                        (c[2] - z[p]) * (c[2] - z[p]));
+      double* v = &acc[p * 4];
+      v[0] += r * n[0];
+      v[1] += r * n[1];
+      v[2] += r * n[2];
+      v[3] += r;
+      on[p] = 1;
+    }
+  }
+  for (int64_t i = 0; i < nnode; ++i) {
+    uint64_t p = nodes[i];
+    if (p >= uint64_t(npoin) || !on[p]) return XG_ERR_ARG;
+    for (int j = 0; j < 3; ++j) norms[i * 3 + j] = acc[p * 4 + j] / acc[p * 4 + 3];
+  }
+  return XG_OK;
+}
+
+}  // extern "C"

@@ -127,7 +127,7 @@ def cube(n: int, jitter: float = 0.0, seed: int = 0, numbering: str = "lex",
         d = rng.uniform(-jitter * h, jitter * h, size=(3, int(interior.sum())))
         coord[:, interior] += d
     inpoel = _orient_positive(coord, _kuhn_cells(m))
-    bface = _cube_faces(n)
+    bface = faces_from_tets(inpoel, _cube_faces(n))
     mesh = {"coord": coord, "inpoel": inpoel, "bface": bface, "h": h}
     if numbering == "lex":
         return mesh
@@ -206,7 +206,38 @@ def read_exo(path: str) -> dict:
                 tri[t] = conn[row][_EXO_TET_SIDE[s]]
         bface[int(sid)] = tri
     f.close()
-    return {"coord": coord, "inpoel": inpoel, "bface": bface}
+    return {"coord": coord, "inpoel": inpoel, "bface": faces_from_tets(inpoel, bface)}
+
+
+def faces_from_tets(inpoel: np.ndarray, bface: dict) -> dict:
+    """Re-derive side-set triangles from the tetrahedra, as the reference's
+    partitioner does (src/Inciter/Partitioner.cpp:578-587): every tet, in
+    order, offers its faces {t0,t2,t1}, {t0,t1,t3}, {t0,t3,t2}, {t1,t2,t3}
+    (outward for positive tets); a face found (in any node order) in a side
+    set is appended to that set with the tet's node order.  The triangle node
+    order matters: the boundary term of the gradient pairs node j's value with
+    normal component j (src/Physics/Riemann.cpp:347-358)."""
+    inpoel = np.asarray(inpoel, dtype=np.int64)
+    key_of = {}
+    for s in sorted(bface):
+        for f in np.asarray(bface[s], dtype=np.int64):
+            key_of[tuple(sorted(f.tolist()))] = s
+    local = np.array([[0, 2, 1], [0, 1, 3], [0, 3, 2], [1, 2, 3]])
+    faces = inpoel[:, local]  # (T, 4, 3)
+    skey = np.sort(faces, axis=2).reshape(-1, 3)
+    flat = faces.reshape(-1, 3)
+    out = {s: [] for s in bface}
+    # only boundary candidates: faces whose sorted key is in the side sets
+    keys = np.array(list(key_of.keys()), dtype=np.int64) if key_of else np.zeros((0, 3), np.int64)
+    if keys.size:
+        big = int(max(inpoel.max(), keys.max())) + 1
+        enc = (skey[:, 0] * big + skey[:, 1]) * big + skey[:, 2]
+        kenc = (keys[:, 0] * big + keys[:, 1]) * big + keys[:, 2]
+        hit = np.nonzero(np.isin(enc, kenc))[0]
+        for i in hit:
+            s = key_of[tuple(skey[i].tolist())]
+            out[s].append(flat[i])
+    return {s: (np.array(v, dtype=np.int64).reshape(-1, 3)) for s, v in out.items()}
 
 
 def counts(n: int) -> dict:
