@@ -137,6 +137,50 @@ int xg_riecg_profile(xg_ctx* ctx, int enable);
 int xg_riecg_kernel_times(xg_ctx* ctx, int cap, const char** names, double* ms,
                           int64_t* launches, int* n);
 
+/* ---- ConjugateGradients ---------------------------------------------------- */
+
+/* Upload a scalar sparse matrix in the layout of tk::CSR with one degree of
+ * freedom per node (src/LinearSolver/CSR.hpp:98-103): row pointers ia[nrow+1],
+ * column ids ja[nnz], values a[nnz], rows sorted by column, every row holding
+ * its diagonal.  base is 1 for the reference's one-based ia/ja, 0 for
+ * zero-based arrays.  The matrix is kept unmodified on the device; Dirichlet
+ * elimination works on a copy at every xg_cg_init(apply != 0). */
+int xg_cg_setup(xg_ctx* ctx, int64_t nrow, const uint64_t* ia, const uint64_t* ja,
+                const double* a, int base);
+
+/* Drop-in for tk::CSR::mult (src/LinearSolver/CSR.cpp:154-172): y = A x. */
+int xg_cg_mult(xg_ctx* ctx, const double* x, double* y);
+
+/* ConjugateGradients::init (src/LinearSolver/ConjugateGradients.cpp:335-427):
+ * x (nrow, optional: null keeps the previous solution as the initial guess),
+ * b (nrow, optional: null keeps the previous rhs), neubc (optional Neumann
+ * contributions added to b), Dirichlet nodes and values applied symmetrically
+ * when apply != 0 (as ConjugateGradients::apply/r), pc 0 = "none",
+ * 1 = "jacobi".  Computes the initial residual, ||b|| and (r,z) (setup/initres). */
+int xg_cg_init(xg_ctx* ctx, const double* x, const double* b, const double* neubc,
+               int64_t ndir, const uint64_t* dirnodes, const double* dirvals, int apply,
+               int pc);
+
+/* ConjugateGradients::solve (ConjugateGradients.cpp:558-823): PCG until
+ * ||r|| < tol * ||b|| (||b|| floored at 1e-14 -> 1), maxit iterations or a
+ * (p,q) = 0 breakdown, at least one iteration.  Reports the iteration count,
+ * the final ||r||, ||b|| and whether it converged (ConjugateGradients::it(),
+ * converged()).  The solution stays on the device (xg_cg_solution). */
+int xg_cg_solve(xg_ctx* ctx, int64_t maxit, double tol, int64_t* it, double* normr,
+                double* normb, int* converged);
+
+/* Mixed-precision variant of xg_cg_solve: iterative refinement with the FP64
+ * residual r = b - A x and FP32 inner PCG solves of A e = r (FP32 matrix and
+ * vectors, FP64 dot products) to inner_tol * ||r||, x += e, until
+ * ||r|| < tol * ||b|| or maxit refinements.  Reports refinement steps, total
+ * inner iterations, final FP64 ||r|| and ||b||. */
+int xg_cg_solve_mixed(xg_ctx* ctx, int64_t maxit, double tol, double inner_tol,
+                      int64_t inner_maxit, int64_t* outer, int64_t* inner, double* normr,
+                      double* normb, int* converged);
+
+/* ConjugateGradients::solution(): copy the device solution to x (nrow). */
+int xg_cg_solution(xg_ctx* ctx, double* x);
+
 /* ---- host operator setup (the caller side of xg_riecg_setup) ------------- */
 
 /* Locality renumbering of mesh nodes (reverse Cuthill-McKee over points
@@ -164,6 +208,14 @@ int xg_mesh_edges(int64_t npoin, const double* coord, int64_t nelem, const uint6
  * given nodes, which must lie on faces of the set. */
 int xg_mesh_bnorm(int64_t npoin, const double* coord, int64_t nface, const uint64_t* faces,
                   int64_t nnode, const uint64_t* nodes, double* norms);
+
+/* Pressure-Poisson matrix of ChoCG::prelhs (src/Inciter/ChoCG.cpp:146-188):
+ * A(a,b) -= grad_a.grad_b / (6J) over tets, on the points-surrounding-points
+ * sparsity plus the diagonal, zero-based, rows sorted by column.  Call with
+ * cap = 0 to get *nnz, then with ia[npoin+1], ja[nnz], a[nnz]. */
+int xg_mesh_pressure_matrix(int64_t npoin, const double* coord, int64_t nelem,
+                            const uint64_t* inpoel, int64_t cap, int64_t* nnz, uint64_t* ia,
+                            uint64_t* ja, double* a);
 
 #ifdef __cplusplus
 }

@@ -30,7 +30,7 @@ def test_library_exports_all_declared_symbols():
     assert len(syms) >= 20
     missing = [s for s in syms if not hasattr(L, s)]
     assert not missing, missing
-    assert set(syms) <= set(lib.SIGNATURES) | {"xg_cg_solve_static"} | set(syms)
+    assert set(syms) <= set(lib.SIGNATURES)
 
 
 def test_no_gpu_create_fails_cleanly():
@@ -47,14 +47,14 @@ def test_host_setup_matches_oracle(numbering):
     ops = riecg.operators(m, sym_sets=[1, 2, 3, 4, 5, 6], renumber=True)
     coord, inpoel = ops["coord"], ops["inpoel"]
     assert np.array_equal(oracle.vol(coord, inpoel), ops["vol"])
-    e2, d2 = oracle.domint(coord, inpoel)
+    e2, d2 = oracle.domint(coord, inpoel, gid=ops["gid"])
     assert np.array_equal(e2, ops["edges"]) and np.array_equal(d2, ops["dint"])
     n2, nn2, ss = oracle.sym_bc(coord, ops["bface"], [1, 2, 3, 4, 5, 6])
     assert np.array_equal(n2, ops["sym"][0]) and np.array_equal(nn2, ops["sym"][1])
     assert ss == ops["symset"]
     # ChoCG coefficients
-    e5, d5 = riecg.edges(coord, inpoel, ncoef=5)
-    o5, od5 = oracle.domint(coord, inpoel, ncoef=5)
+    e5, d5 = riecg.edges(coord, inpoel, gid=ops["gid"], ncoef=5)
+    o5, od5 = oracle.domint(coord, inpoel, gid=ops["gid"], ncoef=5)
     assert np.array_equal(e5, o5) and np.array_equal(d5, od5)
 
 
@@ -80,3 +80,11 @@ def test_boundary_sets_short_circuit():
     assert riecg.boundary_sets(bface, {2}) == [1, 2, 3]
     assert riecg.boundary_sets(bface, {7}) == []
     assert riecg.boundary_sets(bface, set()) == []
+
+
+def test_pressure_matrix_matches_oracle():
+    from xyst_gb300 import cg
+    m = mesh.cube(6, jitter=0.2, seed=4, numbering="random", perm_seed=3)
+    ia, ja, a = cg.pressure_matrix(m["coord"], m["inpoel"])
+    oia, oja, oa = oracle.pressure_matrix(m["coord"], m["inpoel"])
+    assert np.array_equal(ia, oia) and np.array_equal(ja, oja) and np.array_equal(a, oa)

@@ -1,0 +1,108 @@
+"""ConjugateGradients on the GPU against the oracle and the reference's
+unit-test known answers."""
+
+import numpy as np
+import pytest
+
+import oracle
+from common import dirichlet_matrix_only, golden, laplacian_14
+from gpu_util import ctx, relerr
+from xyst_gb300 import cg, mesh
+
+pytestmark = pytest.mark.gpu
+
+
+def _system(n=9, seed=2, ndir_face=1):
+    m = mesh.cube(n, jitter=0.2, seed=seed, numbering="random", perm_seed=seed)
+    ia, ja, a = cg.pressure_matrix(m["coord"], m["inpoel"])
+    dn = np.unique(m["bface"][ndir_face])
+    rng = np.random.default_rng(seed)
+    dv = rng.standard_normal(dn.size) * 0.1
+    b = rng.standard_normal(ia.size - 1)
+    return m, ia, ja, a, dn, dv, b
+
+
+def test_mult_matches_oracle():
+    m, ia, ja, a, *_ = _system()
+    A = cg.ConjugateGradients(ctx(), ia, ja, a)
+    x = np.random.default_rng(1).standard_normal(ia.size - 1)
+    assert relerr(A.mult(x), oracle.csr_mult(ia, ja, a, x)) < 1e-14
+
+
+def test_onebased_reference_layout():
+    m, ia, ja, a, *_ = _system(6)
+    A = cg.ConjugateGradients(ctx(), ia + 1, ja + 1, a, base=1)
+    x = np.arange(ia.size - 1, dtype=np.float64)
+    assert relerr(A.mult(x), oracle.csr_mult(ia, ja, a, x)) < 1e-14
+
+
+@pytest.mark.parametrize("case", ["dof1", "dof3"])
+def test_laplace_golden(case):
+    d = golden("cg_laplace")
+    maxit, tol, normb_ex, normres_ex = d[case]
+    ia, ja, a = laplacian_14(d)
+    n = ia.size - 1
+    a = dirichlet_matrix_only(ia, ja, a, 0)
+    if case == "dof3":
+        import scipy.sparse as sp
+        A = sp.kron(sp.csr_matrix((a, ja, ia), shape=(n, n)), sp.eye(3)).tocsr()
+        A.sort_indices()
+        ia, ja, a = A.indptr.astype(np.int64), A.indices.astype(np.int64), A.data
+        n *= 3
+    s = cg.ConjugateGradients(ctx(), ia, ja, a)
+    s.init(x=np.zeros(n), b=np.ones(n), pc="none")
+    s.solve(int(maxit), float(tol))
+    assert abs(s.normb - normb_ex) < 1e-12
+    assert abs(s.normr - normres_ex) < 1e-12
+    assert s.converged()
+
+
+@pytest.mark.parametrize("pc", ["jacobi", "none"])
+def test_pcg_dirichlet_matches_oracle(pc):
+    m, ia, ja, a, dn, dv, b = _system()
+    n = ia.size - 1
+    a2, b2 = oracle.csr_dirichlet(ia, ja, a, b, dn, dv)
+    x0 = np.zeros(n)
+    xo, ito, nro, nbo, co = oracle.pcg(ia, ja, a2, b2, x0, 2000, 1e-10, pc=pc)
+    s = cg.ConjugateGradients(ctx(), ia, ja, a)
+    s.init(x=x0, b=b, dirbc=(dn, dv), apply=True, pc=pc)
+    s.solve(2000, 1e-10)
+    assert s.converged() and co
+    assert abs(s.it() - ito) <= 1
+    assert abs(s.normb / nbo - 1) < 1e-13
+    x = s.solution()
+    assert relerr(x, xo) < 1e-8
+    # residual of the eliminated system, evaluated by the oracle
+    res = b2 - oracle.csr_mult(ia, ja, a2, x)
+    assert np.linalg.norm(res) < 1e-10 * nbo
+    # the stored matrix is restored: plain products are unaffected
+    assert relerr(s.mult(x), oracle.csr_mult(ia, ja, a, x)) < 1e-14
+
+
+def test_warm_start_and_maxit():
+    m, ia, ja, a, dn, dv, b = _system()
+    n = ia.size - 1
+    s = cg.ConjugateGradients(ctx(), ia, ja, a)
+    s.init(x=np.zeros(n), b=b, dirbc=(dn, dv), apply=True)
+    s.solve(5, 1e-12)
+    assert s.it() == 5 and not s.converged()
+    a2, b2 = oracle.csr_dirichlet(ia, ja, a, b, dn, dv)
+    xo, ito, *_ = oracle.pcg(ia, ja, a2, b2, np.zeros(n), 5, 1e-12)
+    assert relerr(s.solution(), xo) < 1e-10
+    # warm start from the previous solution (x omitted), as ChoCG does
+    s.init(b=b, dirbc=(dn, dv), apply=True)
+    s.solve(2000, 1e-10)
+    assert s.converged()
+
+
+def test_mixed_precision_refinement():
+    m, ia, ja, a, dn, dv, b = _system(11)
+    n = ia.size - 1
+    a2, b2 = oracle.csr_dirichlet(ia, ja, a, b, dn, dv)
+    s = cg.ConjugateGradients(ctx(), ia, ja, a)
+    s.init(x=np.zeros(n), b=b, dirbc=(dn, dv), apply=True)
+    s.solve_mixed(50, 1e-8, inner_tol=1e-3)
+    assert s.converged() and s.outer >= 2
+    x = s.solution()
+    res = b2 - oracle.csr_mult(ia, ja, a2, x)
+    assert np.linalg.norm(res) < 1e-8 * np.linalg.norm(b2)

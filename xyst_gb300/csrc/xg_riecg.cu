@@ -1531,7 +1531,7 @@ int xg_riecg_run(xg_ctx* c, int64_t nstep, double* dts, float* ms) {
 int xg_riecg_profile(xg_ctx* c, int enable) {
   if (!c || !c->riecg) return fail(c, XG_ERR_STATE, "riecg_profile before riecg_setup");
   c->riecg->prof = enable != 0;
-  c->riecg->ktimes.clear();
+  if (enable) c->riecg->ktimes.clear();
   return XG_OK;
 }
 

@@ -244,4 +244,58 @@ int xg_mesh_bnorm(int64_t npoin, const double* coord, int64_t nface, const uint6
   return XG_OK;
 }
 
+// Pressure-Poisson matrix of ChoCG::prelhs (src/Inciter/ChoCG.cpp:146-188):
+// A(a,b) -= grad_a.grad_b / (6 J) summed over tets on the sparsity of points
+// surrounding points plus the diagonal; zero-based rows sorted by column.
+// Call with cap = 0 for *nnz, then with arrays of that size.
+int xg_mesh_pressure_matrix(int64_t npoin, const double* coord, int64_t nelem,
+                            const uint64_t* inpoel, int64_t cap, int64_t* nnz, uint64_t* ia,
+                            uint64_t* ja, double* a) {
+  if (npoin <= 0 || !coord || !inpoel || !nnz) return XG_ERR_ARG;
+  for (int64_t i = 0; i < nelem * 4; ++i)
+    if (inpoel[i] >= static_cast<uint64_t>(npoin)) return XG_ERR_ARG;
+  std::vector<int64_t> ptr, adj;
+  psup(npoin, nelem, inpoel, ptr, adj);
+  const int64_t total = static_cast<int64_t>(adj.size()) + npoin;
+  *nnz = total;
+  if (cap < total) return XG_OK;
+  if (!ia || !ja || !a) return XG_ERR_ARG;
+  ia[0] = 0;
+  int64_t k = 0;
+  for (int64_t i = 0; i < npoin; ++i) {
+    bool diag = false;
+    for (int64_t j = ptr[i]; j < ptr[i + 1]; ++j) {
+      if (!diag && adj[j] > i) {
+        ja[k++] = static_cast<uint64_t>(i);
+        diag = true;
+      }
+      ja[k++] = static_cast<uint64_t>(adj[j]);
+    }
+    if (!diag) ja[k++] = static_cast<uint64_t>(i);
+    ia[i + 1] = static_cast<uint64_t>(k);
+  }
+  std::fill(a, a + total, 0.0);
+  const double *x = coord, *y = coord + npoin, *z = coord + 2 * npoin;
+  for (int64_t e = 0; e < nelem; ++e) {
+    const uint64_t* N = inpoel + e * 4;
+    double ba[3] = {x[N[1]] - x[N[0]], y[N[1]] - y[N[0]], z[N[1]] - z[N[0]]};
+    double ca[3] = {x[N[2]] - x[N[0]], y[N[2]] - y[N[0]], z[N[2]] - z[N[0]]};
+    double da[3] = {x[N[3]] - x[N[0]], y[N[3]] - y[N[0]], z[N[3]] - z[N[0]]};
+    double g[4][3];
+    cross(ca[0], ca[1], ca[2], da[0], da[1], da[2], g[1][0], g[1][1], g[1][2]);
+    cross(da[0], da[1], da[2], ba[0], ba[1], ba[2], g[2][0], g[2][1], g[2][2]);
+    cross(ba[0], ba[1], ba[2], ca[0], ca[1], ca[2], g[3][0], g[3][1], g[3][2]);
+    for (int i = 0; i < 3; ++i) g[0][i] = -g[1][i] - g[2][i] - g[3][i];
+    const double J = (ba[0] * g[1][0] + ba[1] * g[1][1] + ba[2] * g[1][2]) * 6.0;
+    for (int p = 0; p < 4; ++p)
+      for (int q = 0; q < 4; ++q) {
+        const uint64_t* beg = ja + ia[N[p]];
+        const uint64_t* en = ja + ia[N[p] + 1];
+        const uint64_t* pos = std::lower_bound(beg, en, N[q]);
+        a[pos - ja] -= (g[p][0] * g[q][0] + g[p][1] * g[q][1] + g[p][2] * g[q][2]) / J;
+      }
+  }
+  return XG_OK;
+}
+
 }  // extern "C"

@@ -56,10 +56,17 @@ SIGNATURES = {
     "xg_riecg_run": (_int, [_vp, _i64, _vp, _vp]),
     "xg_riecg_profile": (_int, [_vp, _int]),
     "xg_riecg_kernel_times": (_int, [_vp, _int, _vp, _vp, _vp, _vp]),
+    "xg_cg_setup": (_int, [_vp, _i64, _vp, _vp, _vp, _int]),
+    "xg_cg_mult": (_int, [_vp, _vp, _vp]),
+    "xg_cg_init": (_int, [_vp, _vp, _vp, _vp, _i64, _vp, _vp, _int, _int]),
+    "xg_cg_solve": (_int, [_vp, _i64, _dbl, _vp, _vp, _vp, _vp]),
+    "xg_cg_solve_mixed": (_int, [_vp, _i64, _dbl, _dbl, _i64, _vp, _vp, _vp, _vp, _vp]),
+    "xg_cg_solution": (_int, [_vp, _vp]),
     "xg_mesh_rcm": (_int, [_i64, _i64, _vp, _vp]),
     "xg_mesh_vol": (_int, [_i64, _vp, _i64, _vp, _vp]),
     "xg_mesh_edges": (_int, [_i64, _vp, _i64, _vp, _vp, _int, _i64, _vp, _vp, _vp]),
     "xg_mesh_bnorm": (_int, [_i64, _vp, _i64, _vp, _i64, _vp, _vp]),
+    "xg_mesh_pressure_matrix": (_int, [_i64, _vp, _i64, _vp, _i64, _vp, _vp, _vp, _vp]),
 }
 
 _lib = None

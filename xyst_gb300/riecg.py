@@ -98,14 +98,16 @@ def operators(mesh, sym_sets=(), far_sets=(), dir_sets=(), pre_sets=(), extra_se
 
     Boundary triangles come from the side sets :func:`boundary_sets` selects.
     Returns a dict with the (possibly renumbered) mesh and: vol, edges, dint,
-    tri, besym, sym (nodes, norms), far (nodes, norms), dirnodes, prenodes and
-    new_of_old (None without renumbering).
+    tri, besym, sym (nodes, norms), far (nodes, norms), dirnodes, prenodes,
+    new_of_old and gid (the input id of each local node; None without
+    renumbering).
     """
     coord = f64(mesh["coord"])
     inpoel = np.asarray(mesh["inpoel"], dtype=np.int64)
     bface = dict(mesh["bface"])
     npoin = coord.shape[1]
     new_of_old = None
+    gid = None
     if renumber:
         new_of_old = rcm(inpoel, npoin)
         c2 = np.empty_like(coord)
@@ -113,11 +115,15 @@ def operators(mesh, sym_sets=(), far_sets=(), dir_sets=(), pre_sets=(), extra_se
         coord = c2
         inpoel = new_of_old[inpoel]
         bface = {s: new_of_old[f] for s, f in bface.items()}
+        gid = np.empty(npoin, np.int64)  # caller's (global) id of each local node
+        gid[new_of_old] = np.arange(npoin)
     used = set(sym_sets) | set(far_sets) | set(dir_sets) | set(pre_sets) | set(extra_sets)
     kept = boundary_sets(bface, used)
     tri = (np.concatenate([bface[s] for s in kept]) if kept else np.zeros((0, 3), np.int64))
     vol = volumes(coord, inpoel)
-    e, d = edges(coord, inpoel)
+    # edges are oriented from the smaller to the larger global id, as the
+    # reference keys its edge integrals (src/Inciter/RieCG.cpp:369-380)
+    e, d = edges(coord, inpoel, gid=gid)
 
     def nodes_of(sets):
         out = set()
@@ -157,7 +163,7 @@ def operators(mesh, sym_sets=(), far_sets=(), dir_sets=(), pre_sets=(), extra_se
             "far": entries(far, far_sets),
             "dirnodes": np.array(sorted(nodes_of(dir_sets)), dtype=np.int64),
             "prenodes": np.array(sorted(nodes_of(pre_sets)), dtype=np.int64),
-            "new_of_old": new_of_old, "symset": sym}
+            "new_of_old": new_of_old, "gid": gid, "symset": sym}
 
 
 # ---------------------------------------------------------------- device path
