@@ -137,6 +137,59 @@ def kernel_bytes(n, nent, fp32):
     return {"riecg_grad": grad, "riecg_rhs_update": (rhs0 + 2 * rhs12) / 3.0}
 
 
+def pressure_system(ops):
+    """ChoCG pressure-Poisson system on the same mesh: the prelhs matrix,
+    the rhs from the edge divergence of a Taylor-Green velocity field on
+    [0, 2 pi]^3 mapped to the unit cube (unstabilised chorin::div,
+    src/Physics/Chorin.cpp:58-62), Dirichlet p = 0 on side set 4 (x = 1)."""
+    from xyst_gb300 import cg
+
+    coord, inpoel = ops["coord"], ops["inpoel"]
+    ia, ja, a = cg.pressure_matrix(coord, inpoel)
+    X, Y, Z = 2 * np.pi * coord
+    u = np.stack([np.sin(X) * np.cos(Y) * np.cos(Z), -np.cos(X) * np.sin(Y) * np.cos(Z),
+                  np.zeros_like(X)], axis=1)
+    e, d = ops["edges"], ops["dint"]
+    f = (d * (u[e[:, 0]] + u[e[:, 1]])).sum(1)
+    b = np.zeros(coord.shape[1])
+    np.add.at(b, e[:, 0], -f)
+    np.add.at(b, e[:, 1], f)
+    dn = np.unique(ops["bface"][4])
+    # scale to unit RMS: the solver's (p,q) breakdown guard is an absolute
+    # epsilon (src/LinearSolver/ConjugateGradients.cpp:681-690), as ChoCG's
+    # division of the divergence by dt keeps its rhs far from it
+    b *= np.sqrt(b.size) / np.linalg.norm(b)
+    return ia, ja, a, b, dn, np.zeros(dn.size)
+
+
+def run_pcg(ctx, ops, tol=1e-8, maxit=20000):
+    from xyst_gb300 import cg
+
+    ia, ja, a, b, dn, dv = pressure_system(ops)
+    s = cg.ConjugateGradients(ctx, ia, ja, a)
+    n = ia.size - 1
+    out = {"tol": tol, "rows": n, "nnz": int(ja.size), "dirichlet": "p=0 on x=1 face"}
+    for mode in ("fp64", "mixed"):
+        best = None
+        for rep in range(2):
+            s.init(x=np.zeros(n), b=b, dirbc=(dn, dv), apply=True, pc="jacobi")
+            t0 = time.perf_counter()
+            if mode == "fp64":
+                s.solve(maxit, tol)
+            else:
+                s.solve_mixed(200, tol, inner_tol=1e-2, inner_maxit=maxit)
+            t1 = time.perf_counter()
+            if best is None or t1 - t0 < best["s"]:
+                best = {"s": t1 - t0, "iterations": s.it(), "converged": s.converged(),
+                        "rel_residual": s.normr / s.normb}
+                if mode == "mixed":
+                    best["refinements"] = s.outer
+        out[mode] = best
+    it = out["fp64"]["iterations"]
+    out["fp64"]["GBps_per_iteration"] = ((12 * ja.size + 96 * n) * it / out["fp64"]["s"]) / 1e9
+    return out
+
+
 # ------------------------------------------------------------------ CPU leg
 
 def cpu_sample(n=41, steps=3, procs=1):
@@ -213,7 +266,8 @@ def run_gpu(args, rank, world):
     barrier(world)
     # e2e through the C ABI with host buffers
     e2e = e2e_run(r, U0, args.steps, world)
-    out = {"n": n, "nent": nent, "ms": ms_plain, "ms_events": ms, "kt": kt, "clocks": ck.summary(),
+    pcg = run_pcg(ctx, ops) if (rank == 0 and not args.no_pcg) else None
+    out = {"pcg": pcg, "n": n, "nent": nent, "ms": ms_plain, "ms_events": ms, "kt": kt, "clocks": ck.summary(),
            "e2e_ms": e2e, "setup_s": t_setup, "dts": dts2, "dev_bytes": ctx.device_bytes()}
     ctx.close()
     return out
@@ -258,6 +312,7 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-pcg", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -336,7 +391,8 @@ def main():
             "clocks": res["clocks"],
             "cpu_baseline": cpu,
             "setup_s": res["setup_s"], "device_bytes": res["dev_bytes"],
-            "dt_first_last": [float(res["dts"][0]), float(res["dts"][-1])]}
+            "dt_first_last": [float(res["dts"][0]), float(res["dts"][-1])],
+            "chocg_pressure_solve": res["pcg"]}
     print(json.dumps(line))
 
 
