@@ -137,6 +137,47 @@ int xg_riecg_profile(xg_ctx* ctx, int enable);
 int xg_riecg_kernel_times(xg_ctx* ctx, int cap, const char** names, double* ms,
                           int64_t* launches, int* n);
 
+/* ---- KozCG ---------------------------------------------------------------- */
+
+/* KozCG settings (mat.spec_heat_ratio, cfl, dt, fct, fctdif, fctclip, fctsys). */
+typedef struct xg_kozcg_params {
+  double gamma;
+  double cfl;
+  double const_dt;
+  int fct;       /* nonzero: flux-corrected transport (the reference default) */
+  double ctau;   /* fctdif: antidiffusion coefficient */
+  int fctclip;   /* nonzero: limits from the low-order solution only */
+  int fctsys;    /* bit c set: component c is limited as part of the system */
+} xg_kozcg_params;
+
+/* Mesh of KozCG: coordinates, nodal volumes and tetrahedra (Discretization
+ * Coord()/Vol()/Inpoel()), FP64. */
+int xg_kozcg_setup(xg_ctx* ctx, const xg_kozcg_params* prm, int64_t npoin, const double* coord,
+                   const double* vol, int64_t nelem, const uint64_t* inpoel);
+
+/* Symmetry (m_symbcnodes / m_symbcnorms) and Dirichlet (nodes, 5 mask ints,
+ * 5 values per node) BCs applied by KozCG::BC (src/Inciter/KozCG.cpp:590-611). */
+int xg_kozcg_set_bc(xg_ctx* ctx, int64_t nsym, const uint64_t* symnodes, const double* symnorms,
+                    int64_t ndir, const uint64_t* dirnodes, const int32_t* dirmask,
+                    const double* dirvals);
+
+int xg_kozcg_set_state(xg_ctx* ctx, const double* U, double t);
+int xg_kozcg_get_state(xg_ctx* ctx, double* U, double* t);
+
+/* Drop-in for kozak::rhs (src/Physics/Kozak.cpp:29-180): two-step
+ * Taylor-Galerkin residual R (npoin x 5) of host U with time step dt. */
+int xg_kozcg_rhs(xg_ctx* ctx, const double* U, double dt, double* R);
+
+/* Apply the BCs to the device state (KozCG::BC). */
+int xg_kozcg_bc(xg_ctx* ctx);
+
+/* CFL time step of the device state (KozCG::dt, src/Inciter/KozCG.cpp:613-688). */
+int xg_kozcg_dt(xg_ctx* ctx, double* dt);
+
+/* Advance nstep KozCG steps on the device (dt, rhs, FCT aec/alw/lim/solve,
+ * BCs; src/Inciter/KozCG.cpp:613-1197); dts and ms as in xg_riecg_run. */
+int xg_kozcg_run(xg_ctx* ctx, int64_t nstep, double* dts, float* ms);
+
 /* ---- ConjugateGradients ---------------------------------------------------- */
 
 /* Upload a scalar sparse matrix in the layout of tk::CSR with one degree of

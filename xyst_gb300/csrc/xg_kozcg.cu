@@ -1,10 +1,789 @@
-// KozCG element kernels (filled in below).
+// KozCG on one GB300: element Taylor-Galerkin residual and flux-corrected
+// transport, FP64.
+//
+// Reference path (paths relative to the reference project root):
+//   kozak::rhs      src/Physics/Kozak.cpp:29-180
+//   KozCG::dt       src/Inciter/KozCG.cpp:613-688
+//   KozCG::aec      src/Inciter/KozCG.cpp:772-843
+//   KozCG::alw      src/Inciter/KozCG.cpp:865-948
+//   KozCG::lim      src/Inciter/KozCG.cpp:978-1097
+//   KozCG::solve    src/Inciter/KozCG.cpp:1119-1197
+//   KozCG::BC       src/Inciter/KozCG.cpp:590-611 (Dirichlet and symmetry)
+//
+// Layout: node arrays SoA [ncomp][n] (U, R = rhs then low-order solution,
+// P = antidiffusive sums +/- per component, A = limited contributions),
+// elements as int32 [T][4].  Element kernels (one thread per tet) scatter to
+// their four nodes with FP64 atomic adds; the allowed limits Q+/- are
+// maxima/minima kept as order-preserving 64-bit keys so that atomicMax /
+// atomicMin on integers implement them exactly and deterministically.  Node
+// kernels (one thread per node) do the per-node algebra between the element
+// passes.  One step is:
+//   step_begin -> zero -> elem_rhs_aec -> bc_p -> node_lo -> elem_alw ->
+//   node_lim -> elem_lim -> node_solve -> bc (+ CFL minimum for the next step)
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <vector>
+
 #include "xg_internal.hpp"
 
 namespace xg {
+
+namespace {
+constexpr int kBlock = 256;
+
+struct KScalars {
+  double dt;
+  unsigned long long dtmin;
+  int32_t blowup;
+  int32_t pad;
+};
+}  // namespace
+
 struct KozCGDev {
   Arena arena;
+  Arena bcarena;
+  int64_t n = 0, ne = 0;
+  xg_kozcg_params prm{};
+  int32_t* inpoel = nullptr;
+  double *xyz = nullptr, *vol = nullptr;
+  double *U = nullptr, *R = nullptr, *P = nullptr, *A = nullptr;
+  unsigned long long* Q = nullptr;
+  double* stage = nullptr;
+  // BC program: one thread per BC node
+  int64_t nbc = 0;
+  int32_t *bcnode = nullptr, *bcdir = nullptr, *bcsymp = nullptr, *dirmask = nullptr;
+  double *symn = nullptr, *dirval = nullptr;
+  uint8_t* isbc = nullptr;  // per node
+  KScalars* scal = nullptr;
+  double* dthist = nullptr;
+  int64_t dthist_cap = 0;
+  double t = 0.0;
+  bool dt_valid = false;
 };
-void destroy_kozcg(KozCGDev* d) { delete d; }
-size_t bytes_kozcg(const KozCGDev* d) { return d ? d->arena.bytes() : 0; }
+
+void destroy_kozcg(KozCGDev* d) {
+  if (!d) return;
+  if (d->dthist) cudaFree(d->dthist);
+  delete d;
+}
+size_t bytes_kozcg(const KozCGDev* d) { return d ? d->arena.bytes() + d->bcarena.bytes() : 0; }
+
+namespace {
+
+// order-preserving map of doubles to unsigned 64-bit keys
+__device__ __forceinline__ unsigned long long dkey(double v) {
+  unsigned long long b = __double_as_longlong(v);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double dval(unsigned long long k) {
+  unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+  return __longlong_as_double(b);
+}
+
+__device__ __forceinline__ double node_dt(const double u[5], double vol, double g) {
+  double r = u[0];
+  double uu = u[1] / r, vv = u[2] / r, ww = u[3] / r;
+  double pr = (u[4] - 0.5 * r * (uu * uu + vv * vv + ww * ww)) * (g - 1.0);
+  double c = sqrt(g * fmax(pr, 0.0) / r);
+  double L = cbrt(vol);
+  double vel = sqrt(uu * uu + vv * vv + ww * ww);
+  return L / fmax(vel + c, 1.0e-8);
+}
+
+__device__ __forceinline__ void block_min_atomic(double v, unsigned long long* dst) {
+  __shared__ double red[32];
+  unsigned long long bits = __double_as_longlong(v);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long other = __shfl_xor_sync(0xffffffffu, bits, o);
+    bits = other < bits ? other : bits;
+  }
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) red[wid] = __longlong_as_double(bits);
+  __syncthreads();
+  if (wid == 0) {
+    int nw = (blockDim.x + 31) >> 5;
+    double x = lane < nw ? red[lane] : DBL_MAX;
+    unsigned long long b = __double_as_longlong(x);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      unsigned long long other = __shfl_xor_sync(0xffffffffu, b, o);
+      b = other < b ? other : b;
+    }
+    if (lane == 0) atomicMin(dst, b);
+  }
+}
+
+struct Geo {
+  double J;
+  double g[4][3];
+};
+
+__device__ __forceinline__ Geo tetgeo(const double* xyz, int64_t n, const int32_t N[4]) {
+  const double* x = xyz;
+  const double* y = xyz + n;
+  const double* z = xyz + 2 * n;
+  double ba[3] = {x[N[1]] - x[N[0]], y[N[1]] - y[N[0]], z[N[1]] - z[N[0]]};
+  double ca[3] = {x[N[2]] - x[N[0]], y[N[2]] - y[N[0]], z[N[2]] - z[N[0]]};
+  double da[3] = {x[N[3]] - x[N[0]], y[N[3]] - y[N[0]], z[N[3]] - z[N[0]]};
+  Geo t;
+  t.g[1][0] = ca[1] * da[2] - da[1] * ca[2];
+  t.g[1][1] = ca[2] * da[0] - da[2] * ca[0];
+  t.g[1][2] = ca[0] * da[1] - da[0] * ca[1];
+  t.g[2][0] = da[1] * ba[2] - ba[1] * da[2];
+  t.g[2][1] = da[2] * ba[0] - ba[2] * da[0];
+  t.g[2][2] = da[0] * ba[1] - ba[0] * da[1];
+  t.g[3][0] = ba[1] * ca[2] - ca[1] * ba[2];
+  t.g[3][1] = ba[2] * ca[0] - ca[2] * ba[0];
+  t.g[3][2] = ba[0] * ca[1] - ca[0] * ba[1];
+  for (int i = 0; i < 3; ++i) t.g[0][i] = -t.g[1][i] - t.g[2][i] - t.g[3][i];
+  t.J = ba[0] * t.g[1][0] + ba[1] * t.g[1][1] + ba[2] * t.g[1][2];
+  return t;
+}
+
+// kozak::rhs for one tet (Kozak.cpp:73-173) plus the antidiffusive element
+// contributions of KozCG::aec (KozCG.cpp:794-814), scattered to the nodes.
+__global__ void __launch_bounds__(kBlock) k_elem_rhs_aec(int64_t n, int64_t ne,
+                                                          const int32_t* __restrict__ inpoel,
+                                                          const double* __restrict__ xyz,
+                                                          const double* __restrict__ U,
+                                                          const KScalars* __restrict__ sc,
+                                                          double gamma, double ctau, int fct,
+                                                          double* R, double* P) {
+  int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (e >= ne) return;
+  int32_t N[4];
+  for (int a = 0; a < 4; ++a) N[a] = inpoel[e * 4 + a];
+  const Geo t = tetgeo(xyz, n, N);
+  double u[4][5];
+  for (int a = 0; a < 4; ++a)
+    for (int c = 0; c < 5; ++c) u[a][c] = U[c * n + N[a]];
+  const double dt = sc->dt;
+  double p[4];
+  for (int a = 0; a < 4; ++a)
+    p[a] = (gamma - 1.0) *
+           (u[a][4] - 0.5 * (u[a][1] * u[a][1] + u[a][2] * u[a][2] + u[a][3] * u[a][3]) / u[a][0]);
+  double ue[5];
+  for (int c = 0; c < 5; ++c) ue[c] = (u[0][c] + u[1][c] + u[2][c] + u[3][c]) / 4.0;
+  double coef = dt / t.J / 2.0;
+  for (int j = 0; j < 3; ++j)
+    for (int a = 0; a < 4; ++a) {
+      const double cg = coef * t.g[a][j];
+      const double uj = u[a][j + 1] / u[a][0];
+      ue[0] -= cg * u[a][j + 1];
+      ue[1] -= cg * u[a][1] * uj;
+      ue[2] -= cg * u[a][2] * uj;
+      ue[3] -= cg * u[a][3] * uj;
+      ue[j + 1] -= cg * p[a];
+      ue[4] -= cg * (u[a][4] + p[a]) * uj;
+    }
+  const double pr =
+      (gamma - 1.0) * (ue[4] - 0.5 * (ue[1] * ue[1] + ue[2] * ue[2] + ue[3] * ue[3]) / ue[0]);
+  double r[4][5];
+  for (int a = 0; a < 4; ++a)
+    for (int c = 0; c < 5; ++c) r[a][c] = 0.0;
+  coef = 1.0 / 6.0;
+  for (int j = 0; j < 3; ++j) {
+    const double uj = ue[j + 1] / ue[0];
+    for (int a = 0; a < 4; ++a) {
+      const double cg = coef * t.g[a][j];
+      r[a][0] += cg * ue[j + 1];
+      r[a][1] += cg * ue[1] * uj;
+      r[a][2] += cg * ue[2] * uj;
+      r[a][3] += cg * ue[3] * uj;
+      r[a][j + 1] += cg * pr;
+      r[a][4] += cg * (ue[4] + pr) * uj;
+    }
+  }
+  for (int a = 0; a < 4; ++a)
+    for (int c = 0; c < 5; ++c) atomicAdd(R + c * n + N[a], r[a][c]);
+  if (!fct) return;
+  for (int c = 0; c < 5; ++c)
+    for (int a = 0; a < 4; ++a) {
+      double aec = 0.0;
+      for (int b = 0; b < 4; ++b) {
+        const double m = t.J / 120.0 * ((a == b) ? 3.0 : -1.0);
+        aec += m * ctau * u[b][c];
+      }
+      if (aec > 0.0)
+        atomicAdd(P + (c * 2 + 0) * n + N[a], aec);
+      else if (aec < 0.0)
+        atomicAdd(P + (c * 2 + 1) * n + N[a], aec);
+    }
+}
+
+struct KBC {
+  int64_t nbc;
+  const int32_t* node;
+  const int32_t* dir;
+  const int32_t* symp;
+  const int32_t* dirmask;
+  const double* dirval;
+  const double* symn;
+};
+
+// Symmetry projection of the momentum antidiffusive sums (KozCG.cpp:816-830).
+__global__ void k_bc_p(int64_t n, KBC bc, double* P) {
+  int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= bc.nbc) return;
+  const int64_t p = bc.node[i];
+  for (int32_t k = bc.symp[i]; k < bc.symp[i + 1]; ++k) {
+    const double nx = bc.symn[3 * k], ny = bc.symn[3 * k + 1], nz = bc.symn[3 * k + 2];
+    double* P2 = P + 2 * n + p;  // comp 1 (+)
+    double* P3 = P + 3 * n + p;  // comp 1 (-)
+    double* P4 = P + 4 * n + p;
+    double* P5 = P + 5 * n + p;
+    double* P6 = P + 6 * n + p;
+    double* P7 = P + 7 * n + p;
+    const double rvnp = *P2 * nx + *P4 * ny + *P6 * nz;
+    const double rvnn = *P3 * nx + *P5 * ny + *P7 * nz;
+    *P2 -= rvnp * nx;
+    *P3 -= rvnn * nx;
+    *P4 -= rvnp * ny;
+    *P5 -= rvnn * ny;
+    *P6 -= rvnp * nz;
+    *P7 -= rvnn * nz;
+  }
+}
+
+// KozCG::alw node part (KozCG.cpp:887-912): P /= vol, low-order solution
+// R <- U + dt R/vol - P+ - P-, Q keys reset to (-large, +large).  Without FCT
+// the update of KozCG::solve (KozCG.cpp:1151-1160) goes straight to A.
+__global__ void k_node_lo(int64_t n, const double* __restrict__ vol, const double* __restrict__ U,
+                          const KScalars* __restrict__ sc, int fct, double* R, double* P,
+                          unsigned long long* Q, double* A) {
+  int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= n) return;
+  const double dt = sc->dt;
+  const double v = vol[i];
+  for (int c = 0; c < 5; ++c) {
+    if (fct) {
+      double pp = P[(c * 2 + 0) * n + i] / v;
+      double pn = P[(c * 2 + 1) * n + i] / v;
+      P[(c * 2 + 0) * n + i] = pp;
+      P[(c * 2 + 1) * n + i] = pn;
+      R[c * n + i] = U[c * n + i] + dt * R[c * n + i] / v - pp - pn;
+      Q[(c * 2 + 0) * n + i] = dkey(-DBL_MAX);
+      Q[(c * 2 + 1) * n + i] = dkey(DBL_MAX);
+    } else {
+      A[c * n + i] = U[c * n + i] + dt * R[c * n + i] / v;
+    }
+  }
+}
+
+// KozCG::alw element part (KozCG.cpp:914-935): allowed limits.
+__global__ void __launch_bounds__(kBlock) k_elem_alw(int64_t n, int64_t ne,
+                                                      const int32_t* __restrict__ inpoel,
+                                                      const double* __restrict__ U,
+                                                      const double* __restrict__ R, int clip,
+                                                      unsigned long long* Q) {
+  int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (e >= ne) return;
+  int32_t N[4];
+  for (int a = 0; a < 4; ++a) N[a] = inpoel[e * 4 + a];
+  for (int c = 0; c < 5; ++c) {
+    double alwp = -DBL_MAX, alwn = DBL_MAX;
+    for (int a = 0; a < 4; ++a) {
+      const double lo = R[c * n + N[a]];
+      if (clip) {
+        alwp = fmax(alwp, lo);
+        alwn = fmin(alwn, lo);
+      } else {
+        const double uo = U[c * n + N[a]];
+        alwp = fmax(alwp, fmax(lo, uo));
+        alwn = fmin(alwn, fmin(lo, uo));
+      }
+    }
+    const unsigned long long kp = dkey(alwp), kn = dkey(alwn);
+    for (int a = 0; a < 4; ++a) {
+      atomicMax(Q + (c * 2 + 0) * n + N[a], kp);
+      atomicMin(Q + (c * 2 + 1) * n + N[a], kn);
+    }
+  }
+}
+
+// KozCG::lim node part (KozCG.cpp:1004-1024): Q -= low-order solution, limit
+// coefficients C+/- stored back into Q as plain doubles (reinterpreted).
+__global__ void k_node_lim(int64_t n, const double* __restrict__ R, const double* __restrict__ P,
+                           unsigned long long* Q) {
+  int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= n) return;
+  const double eps = DBL_EPSILON;
+  for (int c = 0; c < 5; ++c) {
+    double qp = dval(Q[(c * 2 + 0) * n + i]) - R[c * n + i];
+    double qn = dval(Q[(c * 2 + 1) * n + i]) - R[c * n + i];
+    const double pp = P[(c * 2 + 0) * n + i], pn = P[(c * 2 + 1) * n + i];
+    qp = pp < eps ? 0.0 : fmin(1.0, qp / pp);
+    qn = pn > -eps ? 0.0 : fmin(1.0, qn / pn);
+    Q[(c * 2 + 0) * n + i] = __double_as_longlong(qp);
+    Q[(c * 2 + 1) * n + i] = __double_as_longlong(qn);
+  }
+}
+
+// KozCG::lim element part (KozCG.cpp:1049-1078): limited antidiffusive
+// element contributions, system-limited over the components in sysmask.
+__global__ void __launch_bounds__(kBlock) k_elem_lim(int64_t n, int64_t ne,
+                                                      const int32_t* __restrict__ inpoel,
+                                                      const double* __restrict__ xyz,
+                                                      const double* __restrict__ U,
+                                                      const unsigned long long* __restrict__ Q,
+                                                      double ctau, int sysmask, double* A) {
+  int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (e >= ne) return;
+  int32_t N[4];
+  for (int a = 0; a < 4; ++a) N[a] = inpoel[e * 4 + a];
+  const Geo t = tetgeo(xyz, n, N);
+  double coef[5], aec[5][4];
+  for (int c = 0; c < 5; ++c) {
+    coef[c] = 1.0;
+    for (int a = 0; a < 4; ++a) {
+      double s = 0.0;
+      for (int b = 0; b < 4; ++b) {
+        const double m = t.J / 120.0 * ((a == b) ? 3.0 : -1.0);
+        s += m * ctau * U[c * n + N[b]];
+      }
+      aec[c][a] = s;
+      const double lim = __longlong_as_double(Q[(c * 2 + (s > 0.0 ? 0 : 1)) * n + N[a]]);
+      coef[c] = fmin(coef[c], lim);
+    }
+  }
+  double cs = 1.0;
+  for (int c = 0; c < 5; ++c)
+    if (sysmask & (1 << c)) cs = fmin(cs, coef[c]);
+  for (int c = 0; c < 5; ++c)
+    if (sysmask & (1 << c)) coef[c] = cs;
+  for (int c = 0; c < 5; ++c)
+    for (int a = 0; a < 4; ++a) atomicAdd(A + c * n + N[a], coef[c] * aec[c][a]);
+}
+
+// KozCG::solve (KozCG.cpp:1144-1150): A = low-order + A/vol, then U = A and
+// the CFL minimum of the new state for nodes without BCs.
+__global__ void __launch_bounds__(kBlock) k_node_solve(int64_t n, const double* __restrict__ vol,
+                                                        const double* __restrict__ R,
+                                                        const double* __restrict__ A, int fct,
+                                                        const uint8_t* __restrict__ isbc,
+                                                        double gamma, double* U,
+                                                        unsigned long long* dtmin) {
+  int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  double dtp = DBL_MAX;
+  if (i < n) {
+    double u[5];
+    for (int c = 0; c < 5; ++c) {
+      u[c] = fct ? R[c * n + i] + A[c * n + i] / vol[i] : A[c * n + i];
+      U[c * n + i] = u[c];
+    }
+    if (!isbc[i]) dtp = node_dt(u, vol[i], gamma);
+  }
+  block_min_atomic(dtp, dtmin);
+}
+
+// KozCG::BC: Dirichlet then symmetry (physics::dirbc/symbc), one thread per
+// BC node, with the node's CFL dt.
+__global__ void __launch_bounds__(kBlock) k_bc(int64_t n, KBC bc, double gamma, double* U,
+                                                const double* __restrict__ vol, int want_dt,
+                                                unsigned long long* dtmin) {
+  int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  double dtp = DBL_MAX;
+  if (i < bc.nbc) {
+    const int64_t p = bc.node[i];
+    double u[5];
+    for (int c = 0; c < 5; ++c) u[c] = U[c * n + p];
+    const int32_t d = bc.dir[i];
+    if (d >= 0)
+      for (int c = 0; c < 5; ++c)
+        if (bc.dirmask[d * 5 + c]) u[c] = bc.dirval[d * 5 + c];
+    for (int32_t k = bc.symp[i]; k < bc.symp[i + 1]; ++k) {
+      const double* nn = bc.symn + 3 * k;
+      double vn = u[1] * nn[0] + u[2] * nn[1] + u[3] * nn[2];
+      u[1] -= vn * nn[0];
+      u[2] -= vn * nn[1];
+      u[3] -= vn * nn[2];
+    }
+    for (int c = 0; c < 5; ++c) U[c * n + p] = u[c];
+    if (want_dt) dtp = node_dt(u, vol[p], gamma);
+  }
+  if (want_dt) block_min_atomic(dtp, dtmin);
+}
+
+__global__ void k_dt(int64_t n, const double* __restrict__ U, const double* __restrict__ vol,
+                     double gamma, unsigned long long* dtmin) {
+  int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  double dtp = DBL_MAX;
+  if (p < n) {
+    double u[5];
+    for (int c = 0; c < 5; ++c) u[c] = U[c * n + p];
+    dtp = node_dt(u, vol[p], gamma);
+  }
+  block_min_atomic(dtp, dtmin);
+}
+
+__global__ void k_step_begin(KScalars* s, double cfl, double const_dt, double* hist, int64_t k) {
+  double dt;
+  if (fabs(const_dt) > DBL_EPSILON)
+    dt = const_dt;
+  else
+    dt = __longlong_as_double(s->dtmin) * cfl;
+  if (dt < DBL_EPSILON) s->blowup = 1;
+  s->dt = dt;
+  s->dtmin = __double_as_longlong(DBL_MAX);
+  if (hist) hist[k] = dt;
+}
+
+__global__ void k_reset_min(KScalars* s) { s->dtmin = __double_as_longlong(DBL_MAX); }
+__global__ void k_set_dt(KScalars* s, double dt) { s->dt = dt; }
+
+__global__ void k_aos_to_soa(int64_t n, int nc, const double* __restrict__ a,
+                             double* __restrict__ s) {
+  int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= n * nc) return;
+  int64_t p = i / nc;
+  int c = static_cast<int>(i - p * nc);
+  s[c * n + p] = a[i];
+}
+__global__ void k_soa_to_aos(int64_t n, int nc, const double* __restrict__ s,
+                             double* __restrict__ a) {
+  int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= n * nc) return;
+  int64_t p = i / nc;
+  int c = static_cast<int>(i - p * nc);
+  a[i] = s[c * n + p];
+}
+
+KBC kbc_of(KozCGDev* d) {
+  return KBC{d->nbc, d->bcnode, d->bcdir, d->bcsymp, d->dirmask, d->dirval, d->symn};
+}
+
+int refresh_dt(xg_ctx* c, KozCGDev* d) {
+  k_reset_min<<<1, 1, 0, c->stream>>>(d->scal);
+  XG_CHECK_LAUNCH(c);
+  k_dt<<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(d->n, d->U, d->vol, d->prm.gamma,
+                                                            &d->scal->dtmin);
+  XG_CHECK_LAUNCH(c);
+  d->dt_valid = true;
+  return XG_OK;
+}
+
+// One KozCG step with the dt already in the device scalars.
+int step(xg_ctx* c, KozCGDev* d) {
+  cudaStream_t s = c->stream;
+  const int64_t n = d->n, ne = d->ne;
+  const int fct = d->prm.fct;
+  XG_CUDA(c, cudaMemsetAsync(d->R, 0, n * 5 * 8, s));
+  if (fct) {
+    XG_CUDA(c, cudaMemsetAsync(d->P, 0, n * 10 * 8, s));
+    XG_CUDA(c, cudaMemsetAsync(d->A, 0, n * 5 * 8, s));
+  }
+  k_elem_rhs_aec<<<blocks_for(ne, kBlock), kBlock, 0, s>>>(n, ne, d->inpoel, d->xyz, d->U,
+                                                            d->scal, d->prm.gamma, d->prm.ctau,
+                                                            fct, d->R, d->P);
+  XG_CHECK_LAUNCH(c);
+  if (fct && d->nbc) {
+    k_bc_p<<<blocks_for(d->nbc, kBlock), kBlock, 0, s>>>(n, kbc_of(d), d->P);
+    XG_CHECK_LAUNCH(c);
+  }
+  k_node_lo<<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, d->vol, d->U, d->scal, fct, d->R, d->P,
+                                                      d->Q, d->A);
+  XG_CHECK_LAUNCH(c);
+  if (fct) {
+    k_elem_alw<<<blocks_for(ne, kBlock), kBlock, 0, s>>>(n, ne, d->inpoel, d->U, d->R,
+                                                          d->prm.fctclip, d->Q);
+    XG_CHECK_LAUNCH(c);
+    k_node_lim<<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, d->R, d->P, d->Q);
+    XG_CHECK_LAUNCH(c);
+    k_elem_lim<<<blocks_for(ne, kBlock), kBlock, 0, s>>>(n, ne, d->inpoel, d->xyz, d->U, d->Q,
+                                                          d->prm.ctau, d->prm.fctsys, d->A);
+    XG_CHECK_LAUNCH(c);
+  }
+  k_node_solve<<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, d->vol, d->R, d->A, fct, d->isbc,
+                                                         d->prm.gamma, d->U, &d->scal->dtmin);
+  XG_CHECK_LAUNCH(c);
+  if (d->nbc) {
+    k_bc<<<blocks_for(d->nbc, kBlock), kBlock, 0, s>>>(n, kbc_of(d), d->prm.gamma, d->U, d->vol,
+                                                        1, &d->scal->dtmin);
+    XG_CHECK_LAUNCH(c);
+  }
+  return XG_OK;
+}
+
+}  // namespace
 }  // namespace xg
+
+using namespace xg;
+
+extern "C" {
+
+int xg_kozcg_setup(xg_ctx* c, const xg_kozcg_params* prm, int64_t npoin, const double* coord,
+                   const double* vol, int64_t nelem, const uint64_t* inpoel) {
+  int rc = use(c);
+  if (rc) return rc;
+  if (!prm || npoin <= 0 || nelem <= 0 || !coord || !vol || !inpoel)
+    return fail(c, XG_ERR_ARG, "kozcg_setup: bad mesh");
+  if (npoin >= (int64_t(1) << 31) - 64) return fail(c, XG_ERR_ARG, "kozcg_setup: too many nodes");
+  if (prm->fctsys & ~31) return fail(c, XG_ERR_ARG, "kozcg_setup: fctsys mask beyond 5 components");
+  std::vector<int32_t> ip(nelem * 4);
+  for (int64_t i = 0; i < nelem * 4; ++i) {
+    if (inpoel[i] >= static_cast<uint64_t>(npoin))
+      return fail(c, XG_ERR_ARG, "kozcg_setup: element node id out of range");
+    ip[i] = static_cast<int32_t>(inpoel[i]);
+  }
+  if (c->kozcg) {
+    XG_CUDA(c, cudaStreamSynchronize(c->stream));
+    destroy_kozcg(c->kozcg);
+    c->kozcg = nullptr;
+  }
+  auto* d = new KozCGDev;
+  c->kozcg = d;
+  d->n = npoin;
+  d->ne = nelem;
+  d->prm = *prm;
+  for (int pass = 0; pass < 2; ++pass) {
+    Arena& A = d->arena;
+    A.plan(d->inpoel, nelem * 4);
+    A.plan(d->xyz, npoin * 3);
+    A.plan(d->vol, npoin);
+    A.plan(d->U, npoin * 5);
+    A.plan(d->R, npoin * 5);
+    A.plan(d->P, npoin * 10);
+    A.plan(d->Q, npoin * 10);
+    A.plan(d->A, npoin * 5);
+    A.plan(d->stage, npoin * 5);
+    A.plan(d->isbc, npoin);
+    A.plan(d->scal, 1);
+    if (pass == 0) {
+      cudaError_t e = A.reserve();
+      if (e != cudaSuccess) {
+        destroy_kozcg(d);
+        c->kozcg = nullptr;
+        return fail(c, XG_ERR_CUDA, std::string("kozcg_setup: ") + cudaGetErrorString(e));
+      }
+    }
+  }
+  cudaStream_t s = c->stream;
+  XG_CUDA(c, cudaMemcpy(d->inpoel, ip.data(), ip.size() * 4, cudaMemcpyHostToDevice));
+  XG_CUDA(c, cudaMemcpy(d->xyz, coord, npoin * 3 * 8, cudaMemcpyHostToDevice));
+  XG_CUDA(c, cudaMemcpy(d->vol, vol, npoin * 8, cudaMemcpyHostToDevice));
+  XG_CUDA(c, cudaMemsetAsync(d->U, 0, npoin * 5 * 8, s));
+  XG_CUDA(c, cudaMemsetAsync(d->isbc, 0, npoin, s));
+  KScalars k0{0.0, 0ull, 0, 0};
+  double big = DBL_MAX;
+  std::memcpy(&k0.dtmin, &big, sizeof(double));
+  XG_CUDA(c, cudaMemcpyAsync(d->scal, &k0, sizeof(k0), cudaMemcpyHostToDevice, s));
+  XG_CUDA(c, cudaStreamSynchronize(s));
+  return XG_OK;
+}
+
+int xg_kozcg_set_bc(xg_ctx* c, int64_t nsym, const uint64_t* symnodes, const double* symnorms,
+                    int64_t ndir, const uint64_t* dirnodes, const int32_t* dirmask,
+                    const double* dirvals) {
+  int rc = use(c);
+  if (rc) return rc;
+  KozCGDev* d = c->kozcg;
+  if (!d) return fail(c, XG_ERR_STATE, "kozcg_set_bc before kozcg_setup");
+  if ((nsym && (!symnodes || !symnorms)) || (ndir && (!dirnodes || !dirmask || !dirvals)))
+    return fail(c, XG_ERR_ARG, "kozcg_set_bc: null array");
+  const int64_t n = d->n;
+  std::vector<int64_t> ids;
+  for (int64_t i = 0; i < nsym; ++i) {
+    if (symnodes[i] >= uint64_t(n)) return fail(c, XG_ERR_ARG, "kozcg_set_bc: node id");
+    ids.push_back(int64_t(symnodes[i]));
+  }
+  for (int64_t i = 0; i < ndir; ++i) {
+    if (dirnodes[i] >= uint64_t(n)) return fail(c, XG_ERR_ARG, "kozcg_set_bc: node id");
+    ids.push_back(int64_t(dirnodes[i]));
+  }
+  std::sort(ids.begin(), ids.end());
+  ids.erase(std::unique(ids.begin(), ids.end()), ids.end());
+  const int64_t nbc = static_cast<int64_t>(ids.size());
+  auto pos = [&](uint64_t p) {
+    return static_cast<int64_t>(std::lower_bound(ids.begin(), ids.end(), int64_t(p)) - ids.begin());
+  };
+  std::vector<int32_t> node(nbc), dir(nbc, -1), symp(nbc + 1, 0);
+  for (int64_t i = 0; i < nbc; ++i) node[i] = static_cast<int32_t>(ids[i]);
+  for (int64_t k = 0; k < ndir; ++k) dir[pos(dirnodes[k])] = static_cast<int32_t>(k);
+  std::vector<int64_t> cnt(nbc, 0);
+  for (int64_t k = 0; k < nsym; ++k) ++cnt[pos(symnodes[k])];
+  for (int64_t i = 0; i < nbc; ++i) symp[i + 1] = symp[i] + static_cast<int32_t>(cnt[i]);
+  std::vector<double> symn(std::max<int64_t>(1, nsym) * 3, 0.0);
+  {
+    std::vector<int32_t> fill(symp.begin(), symp.end() - 1);
+    for (int64_t k = 0; k < nsym; ++k) {
+      int32_t j = fill[pos(symnodes[k])]++;
+      for (int a = 0; a < 3; ++a) symn[j * 3 + a] = symnorms[k * 3 + a];
+    }
+  }
+  std::vector<uint8_t> isbc(n, 0);
+  for (auto p : ids) isbc[p] = 1;
+  XG_CUDA(c, cudaStreamSynchronize(c->stream));
+  d->bcarena.release();
+  for (int pass = 0; pass < 2; ++pass) {
+    Arena& A = d->bcarena;
+    A.plan(d->bcnode, std::max<int64_t>(1, nbc));
+    A.plan(d->bcdir, std::max<int64_t>(1, nbc));
+    A.plan(d->bcsymp, nbc + 1);
+    A.plan(d->symn, symn.size());
+    A.plan(d->dirmask, std::max<int64_t>(1, ndir) * 5);
+    A.plan(d->dirval, std::max<int64_t>(1, ndir) * 5);
+    if (pass == 0) XG_CUDA(c, A.reserve());
+  }
+  auto up = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
+    return bytes ? cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice) : cudaSuccess;
+  };
+  XG_CUDA(c, up(d->bcnode, node.data(), nbc * 4));
+  XG_CUDA(c, up(d->bcdir, dir.data(), nbc * 4));
+  XG_CUDA(c, up(d->bcsymp, symp.data(), (nbc + 1) * 4));
+  XG_CUDA(c, up(d->symn, symn.data(), symn.size() * 8));
+  XG_CUDA(c, up(d->dirmask, dirmask, ndir * 5 * 4));
+  XG_CUDA(c, up(d->dirval, dirvals, ndir * 5 * 8));
+  XG_CUDA(c, up(d->isbc, isbc.data(), n));
+  d->nbc = nbc;
+  d->dt_valid = false;
+  return XG_OK;
+}
+
+int xg_kozcg_set_state(xg_ctx* c, const double* U, double t) {
+  int rc = use(c);
+  if (rc) return rc;
+  KozCGDev* d = c->kozcg;
+  if (!d) return fail(c, XG_ERR_STATE, "kozcg_set_state before kozcg_setup");
+  if (!U) return fail(c, XG_ERR_ARG, "kozcg_set_state: null U");
+  XG_CUDA(c, cudaMemcpyAsync(d->stage, U, d->n * 5 * 8, cudaMemcpyHostToDevice, c->stream));
+  k_aos_to_soa<<<blocks_for(d->n * 5, kBlock), kBlock, 0, c->stream>>>(d->n, 5, d->stage, d->U);
+  XG_CHECK_LAUNCH(c);
+  d->t = t;
+  rc = refresh_dt(c, d);
+  if (rc) return rc;
+  XG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return XG_OK;
+}
+
+int xg_kozcg_get_state(xg_ctx* c, double* U, double* t) {
+  int rc = use(c);
+  if (rc) return rc;
+  KozCGDev* d = c->kozcg;
+  if (!d) return fail(c, XG_ERR_STATE, "kozcg_get_state before kozcg_setup");
+  if (U) {
+    k_soa_to_aos<<<blocks_for(d->n * 5, kBlock), kBlock, 0, c->stream>>>(d->n, 5, d->U, d->stage);
+    XG_CHECK_LAUNCH(c);
+    XG_CUDA(c, cudaMemcpyAsync(U, d->stage, d->n * 5 * 8, cudaMemcpyDeviceToHost, c->stream));
+  }
+  XG_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (t) *t = d->t;
+  return XG_OK;
+}
+
+int xg_kozcg_rhs(xg_ctx* c, const double* U, double dt, double* R) {
+  int rc = use(c);
+  if (rc) return rc;
+  KozCGDev* d = c->kozcg;
+  if (!d) return fail(c, XG_ERR_STATE, "kozcg_rhs before kozcg_setup");
+  if (!U || !R) return fail(c, XG_ERR_ARG, "kozcg_rhs: null array");
+  cudaStream_t s = c->stream;
+  // use A as scratch for the caller's state so the device state is untouched
+  XG_CUDA(c, cudaMemcpyAsync(d->stage, U, d->n * 5 * 8, cudaMemcpyHostToDevice, s));
+  k_aos_to_soa<<<blocks_for(d->n * 5, kBlock), kBlock, 0, s>>>(d->n, 5, d->stage, d->A);
+  XG_CHECK_LAUNCH(c);
+  k_set_dt<<<1, 1, 0, s>>>(d->scal, dt);
+  XG_CHECK_LAUNCH(c);
+  XG_CUDA(c, cudaMemsetAsync(d->R, 0, d->n * 5 * 8, s));
+  k_elem_rhs_aec<<<blocks_for(d->ne, kBlock), kBlock, 0, s>>>(d->n, d->ne, d->inpoel, d->xyz, d->A,
+                                                               d->scal, d->prm.gamma, d->prm.ctau,
+                                                               0, d->R, d->P);
+  XG_CHECK_LAUNCH(c);
+  k_soa_to_aos<<<blocks_for(d->n * 5, kBlock), kBlock, 0, s>>>(d->n, 5, d->R, d->stage);
+  XG_CHECK_LAUNCH(c);
+  XG_CUDA(c, cudaMemcpyAsync(R, d->stage, d->n * 5 * 8, cudaMemcpyDeviceToHost, s));
+  XG_CUDA(c, cudaStreamSynchronize(s));
+  d->dt_valid = false;
+  return XG_OK;
+}
+
+int xg_kozcg_dt(xg_ctx* c, double* dt) {
+  int rc = use(c);
+  if (rc) return rc;
+  KozCGDev* d = c->kozcg;
+  if (!d) return fail(c, XG_ERR_STATE, "kozcg_dt before kozcg_setup");
+  if (!dt) return fail(c, XG_ERR_ARG, "kozcg_dt: null dt");
+  if (!d->dt_valid) {
+    rc = refresh_dt(c, d);
+    if (rc) return rc;
+  }
+  KScalars h;
+  XG_CUDA(c, cudaMemcpyAsync(&h, d->scal, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  XG_CUDA(c, cudaStreamSynchronize(c->stream));
+  double m;
+  std::memcpy(&m, &h.dtmin, sizeof(double));
+  *dt = std::fabs(d->prm.const_dt) > std::numeric_limits<double>::epsilon() ? d->prm.const_dt
+                                                                             : m * d->prm.cfl;
+  return XG_OK;
+}
+
+int xg_kozcg_bc(xg_ctx* c) {
+  int rc = use(c);
+  if (rc) return rc;
+  KozCGDev* d = c->kozcg;
+  if (!d) return fail(c, XG_ERR_STATE, "kozcg_bc before kozcg_setup");
+  if (d->nbc) {
+    k_bc<<<blocks_for(d->nbc, kBlock), kBlock, 0, c->stream>>>(d->n, kbc_of(d), d->prm.gamma,
+                                                                d->U, d->vol, 0, &d->scal->dtmin);
+    XG_CHECK_LAUNCH(c);
+  }
+  rc = refresh_dt(c, d);
+  if (rc) return rc;
+  XG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return XG_OK;
+}
+
+int xg_kozcg_run(xg_ctx* c, int64_t nstep, double* dts, float* ms) {
+  int rc = use(c);
+  if (rc) return rc;
+  KozCGDev* d = c->kozcg;
+  if (!d) return fail(c, XG_ERR_STATE, "kozcg_run before kozcg_setup");
+  if (nstep < 0) return fail(c, XG_ERR_ARG, "kozcg_run: negative step count");
+  if (nstep == 0) {
+    if (ms) *ms = 0.f;
+    return XG_OK;
+  }
+  if (!d->dt_valid) {
+    rc = refresh_dt(c, d);
+    if (rc) return rc;
+  }
+  if (d->dthist_cap < nstep) {
+    XG_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (d->dthist) cudaFree(d->dthist);
+    d->dthist = nullptr;
+    XG_CUDA(c, cudaMalloc(&d->dthist, nstep * sizeof(double)));
+    d->dthist_cap = nstep;
+  }
+  cudaEvent_t e0, e1;
+  XG_CUDA(c, cudaEventCreate(&e0));
+  XG_CUDA(c, cudaEventCreate(&e1));
+  XG_CUDA(c, cudaEventRecord(e0, c->stream));
+  for (int64_t k = 0; k < nstep; ++k) {
+    k_step_begin<<<1, 1, 0, c->stream>>>(d->scal, d->prm.cfl, d->prm.const_dt, d->dthist, k);
+    XG_CHECK_LAUNCH(c);
+    rc = step(c, d);
+    if (rc) return rc;
+  }
+  XG_CUDA(c, cudaEventRecord(e1, c->stream));
+  XG_CUDA(c, cudaEventSynchronize(e1));
+  float el = 0.f;
+  XG_CUDA(c, cudaEventElapsedTime(&el, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (ms) *ms = el;
+  std::vector<double> h(nstep);
+  XG_CUDA(c, cudaMemcpy(h.data(), d->dthist, nstep * 8, cudaMemcpyDeviceToHost));
+  for (double v : h) d->t += v;
+  if (dts) std::memcpy(dts, h.data(), nstep * 8);
+  d->dt_valid = true;
+  KScalars s;
+  XG_CUDA(c, cudaMemcpy(&s, d->scal, sizeof(s), cudaMemcpyDeviceToHost));
+  if (s.blowup) return fail(c, XG_ERR_BLOWUP, "dt below machine epsilon");
+  return XG_OK;
+}
+
+}  // extern "C"

@@ -36,6 +36,11 @@ class RiecgParams(C.Structure):
                 ("cfl", _dbl), ("const_dt", _dbl), ("precision", _int)]
 
 
+class KozcgParams(C.Structure):
+    _fields_ = [("gamma", _dbl), ("cfl", _dbl), ("const_dt", _dbl), ("fct", _int),
+                ("ctau", _dbl), ("fctclip", _int), ("fctsys", _int)]
+
+
 # name -> (restype, argtypes); every function of include/xg.h
 SIGNATURES = {
     "xg_create": (_int, [_int, C.POINTER(_vp)]),
@@ -56,6 +61,14 @@ SIGNATURES = {
     "xg_riecg_run": (_int, [_vp, _i64, _vp, _vp]),
     "xg_riecg_profile": (_int, [_vp, _int]),
     "xg_riecg_kernel_times": (_int, [_vp, _int, _vp, _vp, _vp, _vp]),
+    "xg_kozcg_setup": (_int, [_vp, C.POINTER(KozcgParams), _i64, _vp, _vp, _i64, _vp]),
+    "xg_kozcg_set_bc": (_int, [_vp, _i64, _vp, _vp, _i64, _vp, _vp, _vp]),
+    "xg_kozcg_set_state": (_int, [_vp, _vp, _dbl]),
+    "xg_kozcg_get_state": (_int, [_vp, _vp, _vp]),
+    "xg_kozcg_rhs": (_int, [_vp, _vp, _dbl, _vp]),
+    "xg_kozcg_bc": (_int, [_vp]),
+    "xg_kozcg_dt": (_int, [_vp, _vp]),
+    "xg_kozcg_run": (_int, [_vp, _i64, _vp, _vp]),
     "xg_cg_setup": (_int, [_vp, _i64, _vp, _vp, _vp, _int]),
     "xg_cg_mult": (_int, [_vp, _vp, _vp]),
     "xg_cg_init": (_int, [_vp, _vp, _vp, _vp, _i64, _vp, _vp, _int, _int]),
