@@ -17,8 +17,10 @@ def _system(n=9, seed=2, ndir_face=1):
     ia, ja, a = cg.pressure_matrix(m["coord"], m["inpoel"])
     dn = np.unique(m["bface"][ndir_face])
     rng = np.random.default_rng(seed)
-    dv = rng.standard_normal(dn.size) * 0.1
-    b = rng.standard_normal(ia.size - 1)
+    # scaled well above the solver's absolute (p,q) breakdown guard
+    # (src/LinearSolver/ConjugateGradients.cpp:681-690)
+    dv = rng.standard_normal(dn.size) * 1e3
+    b = rng.standard_normal(ia.size - 1) * 1e4
     return m, ia, ja, a, dn, dv, b
 
 
