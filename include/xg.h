@@ -137,6 +137,22 @@ int xg_riecg_profile(xg_ctx* ctx, int enable);
 int xg_riecg_kernel_times(xg_ctx* ctx, int cap, const char** names, double* ms,
                           int64_t* launches, int* n);
 
+/* Allocation-free CFL time step.  No counterpart in the reference: this is
+ * for callers that cannot allocate device memory (their own pool already owns
+ * the device's memory, or they run where cudaMalloc is not allowed) and that
+ * hold RieCG's state on the device themselves.  U (npoin x 5, node-major)
+ * and vol (npoin) are device pointers; dt (host) receives cfl * min over
+ * nodes of cbrt(vol)/max(|u|+c, 1e-8), as xg_riecg_dt, or const_dt when
+ * |const_dt| > eps.  Work is issued on stream (a cudaStream_t, null for the
+ * default stream) on the calling thread's current device, then synchronised.
+ * The scratch is a fixed 512 KiB device array inside the library, shared by
+ * all calls on a device: npoin is limited to 16,777,216 nodes (XG_ERR_ARG
+ * beyond), and calls that overlap on the GPU race.  The first call on each
+ * device looks the array up (device set-up); make it before any stream
+ * capture. */
+int xg_riecg_dt_noalloc(const double* U, const double* vol, int64_t npoin, double gamma,
+                        double cfl, double const_dt, void* stream, double* dt);
+
 /* ---- KozCG ---------------------------------------------------------------- */
 
 /* KozCG settings (mat.spec_heat_ratio, cfl, dt, fct, fctdif, fctclip, fctsys). */

@@ -61,6 +61,7 @@ SIGNATURES = {
     "xg_riecg_run": (_int, [_vp, _i64, _vp, _vp]),
     "xg_riecg_profile": (_int, [_vp, _int]),
     "xg_riecg_kernel_times": (_int, [_vp, _int, _vp, _vp, _vp, _vp]),
+    "xg_riecg_dt_noalloc": (_int, [_vp, _vp, _i64, _dbl, _dbl, _dbl, _vp, _vp]),
     "xg_kozcg_setup": (_int, [_vp, C.POINTER(KozcgParams), _i64, _vp, _vp, _i64, _vp]),
     "xg_kozcg_set_bc": (_int, [_vp, _i64, _vp, _vp, _i64, _vp, _vp, _vp]),
     "xg_kozcg_set_state": (_int, [_vp, _vp, _dbl]),
