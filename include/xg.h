@@ -28,6 +28,7 @@ extern "C" {
 #endif
 
 typedef struct xg_ctx xg_ctx;
+typedef struct xg_lpc xg_lpc;  /* learned preconditioner model (xg_lpc_*) */
 
 enum xg_status {
   XG_OK = 0,
@@ -235,8 +236,44 @@ int xg_cg_solve_mixed(xg_ctx* ctx, int64_t maxit, double tol, double inner_tol,
                       int64_t inner_maxit, int64_t* outer, int64_t* inner, double* normr,
                       double* normb, int* converged);
 
+/* Factored approximate-inverse preconditioner (pc = 2 in xg_cg_init; no
+ * counterpart in the reference, whose preconditioners are "none" and
+ * "jacobi"): M^-1 = -S (I+N)(I+N)^T S on the non-Dirichlet rows, identity on
+ * Dirichlet rows, S = diag(1/sqrt|a_ii|), N strictly lower on A's sparsity.
+ * With model == null, N = scale * e with e_ij = a_ij s_i s_j (scale 0 is
+ * Jacobi); otherwise the model's network emits N.  The factor is rebuilt at
+ * every xg_cg_init(pc = 2), after the Dirichlet elimination. */
+int xg_cg_set_factor(xg_ctx* ctx, xg_lpc* model, double scale);
+
+/* z = M^-1 r with the preconditioner of the last xg_cg_init (host vectors). */
+int xg_cg_precondition(xg_ctx* ctx, const double* r, double* z);
+
 /* ConjugateGradients::solution(): copy the device solution to x (nrow). */
 int xg_cg_solution(xg_ctx* ctx, double* x);
+
+/* ---- learned preconditioner (no counterpart in the reference) ----------
+ * A message-passing network on the matrix graph (3 layers, hidden width 64)
+ * that emits the factor N of xg_cg_set_factor.  The model lives on the
+ * device of the context it is created with; precision 0 runs its dense
+ * layers in FP32, 1 as BF16 tensor-core GEMMs with FP32 accumulation.
+ * Parameters are one flat FP32 vector of xg_lpc_nparams() values in the
+ * order W0 (4x64) b0 W1 (128x64) b1 W2 b2 W3 b3 Wo (64x128) c d w ob. */
+int64_t xg_lpc_nparams(void);
+int xg_lpc_create(xg_ctx* ctx, int precision, xg_lpc** model);
+int xg_lpc_destroy(xg_lpc* model);
+int xg_lpc_set_params(xg_lpc* model, const float* theta); /* also resets Adam */
+int xg_lpc_get_params(xg_lpc* model, float* theta);
+int xg_lpc_zero_grads(xg_lpc* model);
+int xg_lpc_get_grads(xg_lpc* model, float* grad);
+/* Adds d loss / d theta for the matrix of the CG system of `system`
+ * (after xg_cg_init, Dirichlet rows eliminated) to the model's gradient.
+ * loss = (tr(L^T A^ L) - n) / n with A^ = -S A S and L = I + N: Kaporin's
+ * trace functional of the factorised approximate inverse (no solve needed).
+ * Calls on one model must not overlap. */
+int xg_lpc_grad(xg_lpc* model, xg_ctx* system, double* loss);
+const char* xg_lpc_last_error(xg_lpc* model);
+/* One Adam step on the accumulated gradient. */
+int xg_lpc_adam(xg_lpc* model, double lr, double beta1, double beta2, double eps);
 
 /* ---- host operator setup (the caller side of xg_riecg_setup) ------------- */
 

@@ -11,7 +11,9 @@ import numpy as np
 
 from .lib import Context, f64, load, p, u64
 
-PC = {"none": 0, "jacobi": 1}
+# "factor": M^-1 = -S (I+N)(I+N)^T S with N from set_factor (no counterpart
+# in the reference, whose ConjugateGradients offers "none" and "jacobi")
+PC = {"none": 0, "jacobi": 1, "factor": 2}
 
 
 class ConjugateGradients:
@@ -77,6 +79,20 @@ class ConjugateGradients:
         self.normr, self.normb = nr.value, nb.value
         self.outer = o.value
         return self.normr
+
+    def set_factor(self, model=None, scale=1.0):
+        """Source of N for pc="factor": a LearnedPreconditioner, or None for
+        N = scale * e (scale 1: the first-order factor, 0: Jacobi)."""
+        self._model = model  # keep the model alive while it is attached
+        h = None if model is None else model.h
+        self.ctx.check(self.lib.xg_cg_set_factor(self.ctx.h, h, float(scale)))
+
+    def precondition(self, r):
+        """z = M^-1 r with the preconditioner of the last init."""
+        r = f64(r)
+        z = np.zeros(self.n)
+        self.ctx.check(self.lib.xg_cg_precondition(self.ctx.h, p(r), p(z)))
+        return z
 
     def solution(self):
         x = np.zeros(self.n)

@@ -76,6 +76,20 @@ struct CGDev {
   double last_normr = 0, last_normb = 0;
   int last_conv = 0;
   int64_t inner_its = 0;
+  // factored approximate inverse M^-1 = -S (I+N)(I+N)^T S (pc 2): lower and
+  // upper triangles of the matrix graph as SELL-32, the factor values, the
+  // row scales s = 1/sqrt|a_ii| and the normalised couplings e_ij = a_ij s_i s_j
+  int64_t nentL = 0, nentU = 0;
+  int32_t *soffL = nullptr, *swL = nullptr, *colL = nullptr, *posL = nullptr, *tposU = nullptr;
+  int32_t *soffU = nullptr, *swU = nullptr, *colU = nullptr;
+  float *nvL = nullptr, *nvU = nullptr, *srow = nullptr, *eL = nullptr, *eU = nullptr;
+  float* eF = nullptr;  // e_ij in the full layout (0 on the diagonal and at Dirichlet nodes)
+  bool geom_set = false;
+  double *u = nullptr, *t = nullptr;  // t: output of xg_cg_precondition
+  float* u32 = nullptr;
+  bool factor_set = false;
+  xg_lpc* factor_model = nullptr;  // network emitting N, or null: N = factor_c * e
+  double factor_c = 1.0;
 };
 
 void destroy_cg(CGDev* d) { delete d; }
@@ -304,6 +318,7 @@ __global__ void __launch_bounds__(kBlock) k_iter_a(int64_t n, const int32_t* __r
 }
 
 // pq + rz + x (ConjugateGradients.cpp:671-823), fused.
+template <bool FACTOR>
 __global__ void __launch_bounds__(kBlock) k_iter_b(int64_t n, const double* __restrict__ q,
                                                     const double* __restrict__ d,
                                                     const double* __restrict__ p,
@@ -316,18 +331,20 @@ __global__ void __launch_bounds__(kBlock) k_iter_b(int64_t n, const double* __re
   double v[2] = {0.0, 0.0};
   if (i < n) {
     const double ri = r[i] - alpha * q[i];
-    const double zi = ri / d[i];
     r[i] = ri;
-    z[i] = zi;
     x[i] += alpha * p[i];
-    v[0] = ri * zi;
+    if (!FACTOR) {  // Jacobi / none; the factored inverse follows in two passes
+      const double zi = ri / d[i];
+      z[i] = zi;
+      v[0] = ri * zi;
+    }
     v[1] = ri * ri;
   }
   if (block_partials<2>(v, partial, nblk, &sc->ticket[2])) {
     double rz = sum_partials(partial, nblk, 0);
     double rr = sum_partials(partial, nblk, 1);
     if (threadIdx.x == 0) {
-      sc->rho = rz;
+      if (!FACTOR) sc->rho = rz;
       sc->rr = rr;
       sc->it += 1;
       const double nb = sc->normb > 1.0e-14 ? sc->normb : 1.0;
@@ -438,6 +455,7 @@ __global__ void __launch_bounds__(kBlock) k_in_a(int64_t n, const int32_t* __res
 
 // inner stop: ||r_inner|| < tol * ||r_outer|| (tol in sc->tol, ||r_outer||^2
 // kept in sc->normb as the reference norm of this inner solve)
+template <bool FACTOR>
 __global__ void __launch_bounds__(kBlock) k_in_b(int64_t n, const float* __restrict__ q,
                                                   const float* __restrict__ d,
                                                   const float* __restrict__ p,
@@ -450,24 +468,32 @@ __global__ void __launch_bounds__(kBlock) k_in_b(int64_t n, const float* __restr
   double v[2] = {0.0, 0.0};
   if (i < n) {
     const float ri = r[i] - alpha * q[i];
-    const float zi = ri / d[i];
     r[i] = ri;
-    z[i] = zi;
     e[i] += alpha * p[i];
-    v[0] = double(ri) * double(zi);
+    if (!FACTOR) {
+      const float zi = ri / d[i];
+      z[i] = zi;
+      v[0] = double(ri) * double(zi);
+    }
     v[1] = double(ri) * double(ri);
   }
   if (block_partials<2>(v, partial, nblk, &sc->ticket[2])) {
     double rz = sum_partials(partial, nblk, 0);
     double rr = sum_partials(partial, nblk, 1);
     if (threadIdx.x == 0) {
-      sc->rho = rz;
+      if (!FACTOR) sc->rho = rz;
       sc->it += 1;
       const double nr = sqrt(rr);
       if (sc->finished || nr < sc->tol * sc->normb || sc->it >= sc->maxit) sc->done = 1;
       sc->ticket[2] = 0;
     }
   }
+}
+
+__global__ void k_jacobi_apply(int64_t n, const double* __restrict__ r, const double* __restrict__ d,
+                               double* __restrict__ z) {
+  int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i < n) z[i] = r[i] / d[i];
 }
 
 __global__ void k_add_correction(int64_t n, const float* __restrict__ e, double* __restrict__ x) {
@@ -481,6 +507,193 @@ __global__ void k_set_inner(CGScalars* sc, double tol, int64_t maxit) {
   sc->maxit = maxit;
 }
 
+// ---- factored approximate inverse (pc 2)
+
+struct Tri {
+  const int32_t* soff;
+  const int32_t* sw;
+  const int32_t* col;
+};
+
+// Row scales and normalised lower couplings of the working matrix:
+// s_i = 1/sqrt|a_ii|, e_ij = a_ij s_i s_j (0 when i or j is a Dirichlet node).
+__global__ void k_factor_geom(int64_t n, const double* __restrict__ a,
+                              const int32_t* __restrict__ diagpos, const uint8_t* __restrict__ mask,
+                              float* __restrict__ srow) {
+  int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= n) return;
+  srow[i] = float(1.0 / sqrt(fabs(a[diagpos[i]])));
+}
+__global__ void k_factor_e(int64_t n, Tri L, const int32_t* __restrict__ posL,
+                           const int32_t* __restrict__ tposU, const double* __restrict__ a,
+                           const float* __restrict__ srow, const uint8_t* __restrict__ mask,
+                           float* __restrict__ eL, float* __restrict__ eU) {
+  int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= n) return;
+  const int lane = int(i & 31);
+  const int32_t off = L.soff[i >> 5], w = L.sw[i >> 5];
+  for (int k = 0; k < w; ++k) {
+    const int32_t e = off + k * kSlice + lane;
+    const int32_t j = L.col[e];
+    if (j < 0) continue;
+    const float v = (mask[i] || mask[j]) ? 0.f : float(a[posL[e]]) * srow[i] * srow[j];
+    eL[e] = v;
+    eU[tposU[e]] = v;
+  }
+}
+__global__ void k_factor_efull(int64_t n, const int32_t* __restrict__ soff,
+                               const int32_t* __restrict__ sw, const int32_t* __restrict__ col,
+                               const double* __restrict__ a, const float* __restrict__ srow,
+                               const uint8_t* __restrict__ mask, float* __restrict__ eF) {
+  int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= n) return;
+  const int lane = int(i & 31);
+  const int32_t off = soff[i >> 5], w = sw[i >> 5];
+  for (int k = 0; k < w; ++k) {
+    const int32_t e = off + k * kSlice + lane;
+    const int32_t j = col[e];
+    eF[e] = (j < 0 || j == i || mask[i] || mask[j]) ? 0.f : float(a[e]) * srow[i] * srow[j];
+  }
+}
+// N_ij = c e_ij (the first-order factor, c = 1, or any uniform scaling).
+__global__ void k_factor_scaled(int64_t n, Tri L, const int32_t* __restrict__ tposU,
+                                const float* __restrict__ eL, const float* __restrict__ srow,
+                                float c, float* __restrict__ nvL, float* __restrict__ nvU) {
+  int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= n) return;
+  const int lane = int(i & 31);
+  const int32_t off = L.soff[i >> 5], w = L.sw[i >> 5];
+  for (int k = 0; k < w; ++k) {
+    const int32_t e = off + k * kSlice + lane;
+    const int32_t j = L.col[e];
+    if (j < 0) continue;
+    const float v = c * eL[e];
+    nvL[e] = v;
+    nvU[tposU[e]] = v * srow[i];  // the upper copy (row j, column i) carries s_i
+  }
+}
+
+// u = (I+N)^T S r: u_i = s_i r_i + sum_{j>i} N_ji s_j r_j.
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_pc_upper(int64_t n, Tri U, const float* __restrict__ nvU,
+                                                      const float* __restrict__ srow,
+                                                      const T* __restrict__ r, T* __restrict__ u,
+                                                      const CGScalars* __restrict__ sc) {
+  if (sc->done) return;
+  int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= n) return;
+  const int lane = int(i & 31);
+  const int32_t off = U.soff[i >> 5], w = U.sw[i >> 5];
+  T acc = T(srow[i]) * r[i];
+  for (int k = 0; k < w; ++k) {
+    const int32_t e = off + k * kSlice + lane;
+    const int32_t j = __ldg(U.col + e);
+    if (j < 0) continue;
+    acc += T(__ldg(nvU + e)) * __ldg(r + j);
+  }
+  u[i] = acc;
+}
+
+// z = -S (I+N) u (Dirichlet rows: z = r), partial (r,z); the last block
+// stores rho = (r,z).  With SETP the search direction starts as p = z.
+template <class T, bool SETP>
+__global__ void __launch_bounds__(kBlock) k_pc_lower(int64_t n, Tri L, const float* __restrict__ nvL,
+                                                      const float* __restrict__ srow,
+                                                      const uint8_t* __restrict__ mask,
+                                                      const T* __restrict__ u, const T* __restrict__ r,
+                                                      T* __restrict__ z, T* __restrict__ p,
+                                                      double* partial, int64_t nblk, CGScalars* sc) {
+  if (sc->done) return;
+  int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  double v[1] = {0.0};
+  if (i < n) {
+    const int lane = int(i & 31);
+    const int32_t off = L.soff[i >> 5], w = L.sw[i >> 5];
+    T acc = u[i];
+    for (int k = 0; k < w; ++k) {
+      const int32_t e = off + k * kSlice + lane;
+      const int32_t j = __ldg(L.col + e);
+      if (j < 0) continue;
+      acc += T(__ldg(nvL + e)) * __ldg(u + j);
+    }
+    const T ri = r[i];
+    const T zi = mask[i] ? ri : -T(srow[i]) * acc;
+    z[i] = zi;
+    if (SETP) p[i] = zi;
+    v[0] = double(ri) * double(zi);
+  }
+  if (block_partials<1>(v, partial, nblk, &sc->ticket[3])) {
+    double rz = sum_partials(partial, nblk, 0);
+    if (threadIdx.x == 0) {
+      sc->rho = rz;
+      sc->ticket[3] = 0;
+    }
+  }
+}
+
+Tri tri_l(const CGDev* d) { return Tri{d->soffL, d->swL, d->colL}; }
+Tri tri_u(const CGDev* d) { return Tri{d->soffU, d->swU, d->colU}; }
+
+// Row scales and normalised couplings of the current working matrix.
+int build_geom(xg_ctx* c, CGDev* d) {
+  cudaStream_t s = c->stream;
+  const unsigned nb = blocks_for(d->n, kBlock);
+  k_factor_geom<<<nb, kBlock, 0, s>>>(d->n, d->a, d->diagpos, d->bcmask, d->srow);
+  XG_CHECK_LAUNCH(c);
+  k_factor_e<<<nb, kBlock, 0, s>>>(d->n, tri_l(d), d->posL, d->tposU, d->a, d->srow, d->bcmask,
+                                   d->eL, d->eU);
+  XG_CHECK_LAUNCH(c);
+  k_factor_efull<<<nb, kBlock, 0, s>>>(d->n, d->soff, d->swidth, d->col, d->a, d->srow, d->bcmask,
+                                       d->eF);
+  XG_CHECK_LAUNCH(c);
+  d->geom_set = true;
+  return XG_OK;
+}
+
+LpcGraph graph_of(const CGDev* d) {
+  LpcGraph g;
+  g.n = d->n;
+  g.nslice = d->nslice;
+  g.soff = d->soff;
+  g.sw = d->swidth;
+  g.col = d->col;
+  g.eF = d->eF;
+  g.soffL = d->soffL;
+  g.swL = d->swL;
+  g.colL = d->colL;
+  g.eL = d->eL;
+  g.tposU = d->tposU;
+  g.soffU = d->soffU;
+  g.swU = d->swU;
+  g.colU = d->colU;
+  g.eU = d->eU;
+  g.srow = d->srow;
+  g.mask = d->bcmask;
+  g.nentL = d->nentL;
+  g.nentU = d->nentU;
+  return g;
+}
+
+// Scales, couplings and factor values of the current working matrix.
+int build_factor(xg_ctx* c, CGDev* d) {
+  cudaStream_t s = c->stream;
+  const unsigned nb = blocks_for(d->n, kBlock);
+  if (!d->geom_set) {
+    int rg = build_geom(c, d);
+    if (rg) return rg;
+  }
+  if (d->factor_model) {
+    int rc = lpc_factor(c, d->factor_model, graph_of(d), d->nvL, d->nvU);
+    if (rc) return rc;
+  } else {
+    k_factor_scaled<<<nb, kBlock, 0, s>>>(d->n, tri_l(d), d->tposU, d->eL, d->srow,
+                                          float(d->factor_c), d->nvL, d->nvU);
+    XG_CHECK_LAUNCH(c);
+  }
+  d->factor_set = true;
+  return XG_OK;
+}
+
 int read_scal(xg_ctx* c, CGDev* d, CGScalars* h) {
   XG_CUDA(c, cudaMemcpyAsync(h, d->scal, sizeof(CGScalars), cudaMemcpyDeviceToHost, c->stream));
   XG_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -488,6 +701,17 @@ int read_scal(xg_ctx* c, CGDev* d, CGScalars* h) {
 }
 
 }  // namespace
+
+int cg_graph(xg_ctx* c, LpcGraph* g) {
+  CGDev* d = c->cg;
+  if (!d || !d->ready) return fail(c, XG_ERR_STATE, "learned preconditioner: no initialised CG system");
+  if (!d->geom_set) {
+    int rc = build_geom(c, d);
+    if (rc) return rc;
+  }
+  *g = graph_of(d);
+  return XG_OK;
+}
 
 }  // namespace xg
 
@@ -539,6 +763,76 @@ int xg_cg_setup(xg_ctx* c, int64_t nrow, const uint64_t* ia, const uint64_t* ja,
     }
     dpos[i] = static_cast<int32_t>(soff[s] + int64_t(diagk[i]) * kSlice + lane);
   }
+  // lower / upper triangles (off-diagonal) as SELL-32, rows sorted by column;
+  // posL: the full-layout index of each lower entry; tposU: the upper-layout
+  // index of its transposed entry (j,i)
+  std::vector<int32_t> soffL(nslice + 1), swL(nslice), soffU(nslice + 1), swU(nslice);
+  int64_t totL = 0, totU = 0;
+  for (int64_t s2 = 0; s2 < nslice; ++s2) {
+    int64_t wl = 0, wu = 0;
+    for (int64_t i = s2 * kSlice; i < std::min(nrow, (s2 + 1) * kSlice); ++i) {
+      int64_t nl = 0, nu = 0;
+      for (uint64_t j = ia[i]; j < ia[i + 1]; ++j) {
+        const int64_t cc = int64_t(ja[j - b0] - b0);
+        if (cc < i) ++nl;
+        if (cc > i) ++nu;
+      }
+      wl = std::max(wl, nl);
+      wu = std::max(wu, nu);
+    }
+    swL[s2] = int32_t(wl);
+    swU[s2] = int32_t(wu);
+    soffL[s2] = int32_t(totL);
+    soffU[s2] = int32_t(totU);
+    totL += wl * kSlice;
+    totU += wu * kSlice;
+  }
+  soffL[nslice] = int32_t(totL);
+  soffU[nslice] = int32_t(totU);
+  std::vector<int32_t> colL(std::max<int64_t>(1, totL), kPad), posL(std::max<int64_t>(1, totL), 0),
+      colU(std::max<int64_t>(1, totU), kPad), tposU(std::max<int64_t>(1, totL), 0);
+  std::vector<int64_t> rowU(nrow + 1, 0);  // for locating (j,i) in row j's upper list
+  for (int64_t i = 0; i < nrow; ++i) {
+    const int64_t s2 = i / kSlice, lane = i % kSlice;
+    int64_t kl = 0, ku = 0;
+    for (uint64_t j = ia[i]; j < ia[i + 1]; ++j) {
+      const int64_t cc = int64_t(ja[j - b0] - b0);
+      const int64_t kfull = int64_t(j - ia[i]);
+      if (cc < i) {
+        const int64_t e = soffL[s2] + kl * kSlice + lane;
+        colL[e] = int32_t(cc);
+        posL[e] = int32_t(soff[s2] + kfull * kSlice + lane);
+        ++kl;
+      } else if (cc > i) {
+        colU[soffU[s2] + ku * kSlice + lane] = int32_t(cc);
+        ++ku;
+      }
+    }
+  }
+  for (int64_t i = 0; i < nrow; ++i) {
+    const int64_t s2 = i / kSlice, lane = i % kSlice;
+    int64_t kl = 0;
+    for (uint64_t j = ia[i]; j < ia[i + 1]; ++j) {
+      const int64_t cc = int64_t(ja[j - b0] - b0);
+      if (cc >= i) continue;
+      // position of column i in row cc's upper list (rows sorted by column)
+      const int64_t s3 = cc / kSlice, lane3 = cc % kSlice;
+      int64_t ku = 0;
+      bool found = false;
+      for (uint64_t jj = ia[cc]; jj < ia[cc + 1]; ++jj) {
+        const int64_t c3 = int64_t(ja[jj - b0] - b0);
+        if (c3 <= cc) continue;
+        if (c3 == i) {
+          found = true;
+          break;
+        }
+        ++ku;
+      }
+      if (!found) return fail(c, XG_ERR_ARG, "cg_setup: matrix graph is not symmetric");
+      tposU[soffL[s2] + kl * kSlice + lane] = int32_t(soffU[s3] + ku * kSlice + lane3);
+      ++kl;
+    }
+  }
   if (c->cg) {
     XG_CUDA(c, cudaStreamSynchronize(c->stream));
     destroy_cg(c->cg);
@@ -578,6 +872,23 @@ int xg_cg_setup(xg_ctx* c, int64_t nrow, const uint64_t* ia, const uint64_t* ja,
     A.plan(d->p32[1], nrow);
     A.plan(d->partial, 3 * d->nblk);
     A.plan(d->scal, 1);
+    A.plan(d->soffL, nslice + 1);
+    A.plan(d->swL, nslice);
+    A.plan(d->colL, colL.size());
+    A.plan(d->posL, posL.size());
+    A.plan(d->tposU, tposU.size());
+    A.plan(d->soffU, nslice + 1);
+    A.plan(d->swU, nslice);
+    A.plan(d->colU, colU.size());
+    A.plan(d->nvL, colL.size());
+    A.plan(d->nvU, colU.size());
+    A.plan(d->eL, colL.size());
+    A.plan(d->eU, colU.size());
+    A.plan(d->eF, tot);
+    A.plan(d->srow, nrow);
+    A.plan(d->u, nrow);
+    A.plan(d->t, nrow);
+    A.plan(d->u32, nrow);
     if (pass == 0) {
       cudaError_t e = A.reserve();
       if (e != cudaSuccess) {
@@ -593,6 +904,19 @@ int xg_cg_setup(xg_ctx* c, int64_t nrow, const uint64_t* ia, const uint64_t* ja,
   XG_CUDA(c, cudaMemcpyAsync(d->col, col.data(), col.size() * 4, cudaMemcpyHostToDevice, s));
   XG_CUDA(c, cudaMemcpyAsync(d->a0, val.data(), val.size() * 8, cudaMemcpyHostToDevice, s));
   XG_CUDA(c, cudaMemcpyAsync(d->diagpos, dpos.data(), dpos.size() * 4, cudaMemcpyHostToDevice, s));
+  d->nentL = totL;
+  d->nentU = totU;
+  XG_CUDA(c, cudaMemcpyAsync(d->soffL, soffL.data(), soffL.size() * 4, cudaMemcpyHostToDevice, s));
+  XG_CUDA(c, cudaMemcpyAsync(d->swL, swL.data(), swL.size() * 4, cudaMemcpyHostToDevice, s));
+  XG_CUDA(c, cudaMemcpyAsync(d->colL, colL.data(), colL.size() * 4, cudaMemcpyHostToDevice, s));
+  XG_CUDA(c, cudaMemcpyAsync(d->posL, posL.data(), posL.size() * 4, cudaMemcpyHostToDevice, s));
+  XG_CUDA(c, cudaMemcpyAsync(d->tposU, tposU.data(), tposU.size() * 4, cudaMemcpyHostToDevice, s));
+  XG_CUDA(c, cudaMemcpyAsync(d->soffU, soffU.data(), soffU.size() * 4, cudaMemcpyHostToDevice, s));
+  XG_CUDA(c, cudaMemcpyAsync(d->swU, swU.data(), swU.size() * 4, cudaMemcpyHostToDevice, s));
+  XG_CUDA(c, cudaMemcpyAsync(d->colU, colU.data(), colU.size() * 4, cudaMemcpyHostToDevice, s));
+  XG_CUDA(c, cudaMemsetAsync(d->nvL, 0, colL.size() * 4, s));
+  XG_CUDA(c, cudaMemsetAsync(d->nvU, 0, colU.size() * 4, s));
+  XG_CUDA(c, cudaMemsetAsync(d->eU, 0, colU.size() * 4, s));
   XG_CUDA(c, cudaMemsetAsync(d->x, 0, nrow * 8, s));
   XG_CUDA(c, cudaMemsetAsync(d->b, 0, nrow * 8, s));
   XG_CUDA(c, cudaMemsetAsync(d->bcmask, 0, nrow, s));
@@ -624,7 +948,7 @@ int xg_cg_init(xg_ctx* c, const double* x, const double* b, const double* neubc,
   if (rc) return rc;
   CGDev* d = c->cg;
   if (!d) return fail(c, XG_ERR_STATE, "cg_init before cg_setup");
-  if (pc != 0 && pc != 1) return fail(c, XG_ERR_ARG, "cg_init: unknown preconditioner");
+  if (pc != 0 && pc != 1 && pc != 2) return fail(c, XG_ERR_ARG, "cg_init: unknown preconditioner");
   if (ndir && (!dirnodes || !dirvals)) return fail(c, XG_ERR_ARG, "cg_init: null Dirichlet data");
   cudaStream_t s = c->stream;
   const int64_t n = d->n;
@@ -632,6 +956,8 @@ int xg_cg_init(xg_ctx* c, const double* x, const double* b, const double* neubc,
   if (b) XG_CUDA(c, cudaMemcpyAsync(d->b, b, n * 8, cudaMemcpyHostToDevice, s));
   d->pc = pc;
   d->apply = apply != 0;
+  d->geom_set = false;
+  d->factor_set = false;
   if (d->apply) {
     std::vector<uint8_t> mask(n, 0);
     std::vector<double> val(n, 0.0);
@@ -653,6 +979,7 @@ int xg_cg_init(xg_ctx* c, const double* x, const double* b, const double* neubc,
                                                          d->b);
     XG_CHECK_LAUNCH(c);
   } else {
+    XG_CUDA(c, cudaMemsetAsync(d->bcmask, 0, n, s));
     k_copy_values<<<blocks_for(d->nent, kBlock), kBlock, 0, s>>>(d->nent, d->a0, d->a, d->a32);
     XG_CHECK_LAUNCH(c);
   }
@@ -663,6 +990,16 @@ int xg_cg_init(xg_ctx* c, const double* x, const double* b, const double* neubc,
                                                     d->x, d->b, d->r, d->d, d->z, d->p[0], d->d32,
                                                     d->partial, d->nblk, d->scal);
   XG_CHECK_LAUNCH(c);
+  if (pc == 2) {
+    int rf = build_factor(c, d);
+    if (rf) return rf;
+    const unsigned nb = blocks_for(n, kBlock);
+    k_pc_upper<double><<<nb, kBlock, 0, s>>>(n, tri_u(d), d->nvU, d->srow, d->r, d->u, d->scal);
+    k_pc_lower<double, false><<<nb, kBlock, 0, s>>>(n, tri_l(d), d->nvL, d->srow, d->bcmask, d->u,
+                                                    d->r, d->z, nullptr, d->partial, d->nblk,
+                                                    d->scal);
+    XG_CHECK_LAUNCH(c);
+  }
   d->cur = 0;
   XG_CUDA(c, cudaStreamSynchronize(s));
   d->ready = true;
@@ -682,8 +1019,18 @@ int cg_iterate(xg_ctx* c, CGDev* d, int64_t maxit, double tol, CGScalars* h) {
       double* pnew = d->p[d->cur ^ 1];
       k_iter_a<<<nb, kBlock, 0, s>>>(d->n, d->soff, d->swidth, d->col, d->a, d->z, pold, pnew,
                                      d->q, d->partial, d->nblk, d->scal);
-      k_iter_b<<<nb, kBlock, 0, s>>>(d->n, d->q, d->d, pnew, d->r, d->z, d->x, d->partial,
-                                     d->nblk, d->scal);
+      if (d->pc == 2) {
+        k_iter_b<true><<<nb, kBlock, 0, s>>>(d->n, d->q, d->d, pnew, d->r, d->z, d->x, d->partial,
+                                             d->nblk, d->scal);
+        k_pc_upper<double><<<nb, kBlock, 0, s>>>(d->n, tri_u(d), d->nvU, d->srow, d->r, d->u,
+                                                 d->scal);
+        k_pc_lower<double, false><<<nb, kBlock, 0, s>>>(d->n, tri_l(d), d->nvL, d->srow,
+                                                        d->bcmask, d->u, d->r, d->z, nullptr,
+                                                        d->partial, d->nblk, d->scal);
+      } else {
+        k_iter_b<false><<<nb, kBlock, 0, s>>>(d->n, d->q, d->d, pnew, d->r, d->z, d->x,
+                                              d->partial, d->nblk, d->scal);
+      }
       d->cur ^= 1;
     }
     XG_CHECK_LAUNCH(c);
@@ -741,6 +1088,14 @@ int xg_cg_solve_mixed(xg_ctx* c, int64_t maxit, double tol, double inner_tol,
                                       d->r32, d->z32, d->p32[0], d->e32, d->partial, d->nblk,
                                       d->scal);
     XG_CHECK_LAUNCH(c);
+    if (d->pc == 2) {
+      k_pc_upper<float><<<nb, kBlock, 0, s>>>(d->n, tri_u(d), d->nvU, d->srow, d->r32, d->u32,
+                                              d->scal);
+      k_pc_lower<float, false><<<nb, kBlock, 0, s>>>(d->n, tri_l(d), d->nvL, d->srow, d->bcmask,
+                                                     d->u32, d->r32, d->z32, nullptr, d->partial,
+                                                     d->nblk, d->scal);
+      XG_CHECK_LAUNCH(c);
+    }
     rc = read_scal(c, d, &h);
     if (rc) return rc;
     nr = std::sqrt(h.rr);
@@ -757,8 +1112,18 @@ int xg_cg_solve_mixed(xg_ctx* c, int64_t maxit, double tol, double inner_tol,
         k_in_a<<<nb, kBlock, 0, s>>>(d->n, d->soff, d->swidth, d->col, d->a32, d->z32,
                                      d->p32[cur], d->p32[cur ^ 1], d->q32, d->partial, d->nblk,
                                      d->scal);
-        k_in_b<<<nb, kBlock, 0, s>>>(d->n, d->q32, d->d32, d->p32[cur ^ 1], d->r32, d->z32,
-                                     d->e32, d->partial, d->nblk, d->scal);
+        if (d->pc == 2) {
+          k_in_b<true><<<nb, kBlock, 0, s>>>(d->n, d->q32, d->d32, d->p32[cur ^ 1], d->r32,
+                                             d->z32, d->e32, d->partial, d->nblk, d->scal);
+          k_pc_upper<float><<<nb, kBlock, 0, s>>>(d->n, tri_u(d), d->nvU, d->srow, d->r32,
+                                                  d->u32, d->scal);
+          k_pc_lower<float, false><<<nb, kBlock, 0, s>>>(d->n, tri_l(d), d->nvL, d->srow,
+                                                         d->bcmask, d->u32, d->r32, d->z32,
+                                                         nullptr, d->partial, d->nblk, d->scal);
+        } else {
+          k_in_b<false><<<nb, kBlock, 0, s>>>(d->n, d->q32, d->d32, d->p32[cur ^ 1], d->r32,
+                                              d->z32, d->e32, d->partial, d->nblk, d->scal);
+        }
         cur ^= 1;
       }
       XG_CHECK_LAUNCH(c);
@@ -781,6 +1146,52 @@ int xg_cg_solve_mixed(xg_ctx* c, int64_t maxit, double tol, double inner_tol,
   if (normr) *normr = nr;
   if (normb) *normb = nb0;
   if (converged) *converged = conv ? 1 : 0;
+  return XG_OK;
+}
+
+int xg_cg_set_factor(xg_ctx* c, xg_lpc* model, double scale) {
+  int rc = use(c);
+  if (rc) return rc;
+  CGDev* d = c->cg;
+  if (!d) return fail(c, XG_ERR_STATE, "cg_set_factor before cg_setup");
+  d->factor_model = model;
+  d->factor_c = scale;
+  d->factor_set = false;
+  return XG_OK;
+}
+
+int xg_cg_precondition(xg_ctx* c, const double* r, double* z) {
+  int rc = use(c);
+  if (rc) return rc;
+  CGDev* d = c->cg;
+  if (!d || !d->ready) return fail(c, XG_ERR_STATE, "cg_precondition before cg_init");
+  if (!r || !z) return fail(c, XG_ERR_ARG, "cg_precondition: null vector");
+  cudaStream_t s = c->stream;
+  const unsigned nb = blocks_for(d->n, kBlock);
+  XG_CUDA(c, cudaMemcpyAsync(d->q, r, d->n * 8, cudaMemcpyHostToDevice, s));
+  // a scratch copy of the scalars with done = 0 so the passes run
+  CGScalars h{};
+  CGScalars* sc = d->scal + 0;
+  XG_CUDA(c, cudaMemcpyAsync(&h, sc, sizeof(h), cudaMemcpyDeviceToHost, s));
+  XG_CUDA(c, cudaStreamSynchronize(s));
+  int32_t zero = 0;
+  XG_CUDA(c, cudaMemcpyAsync(&sc->done, &zero, sizeof(int32_t), cudaMemcpyHostToDevice, s));
+  if (d->pc == 2) {
+    if (!d->factor_set) {
+      rc = build_factor(c, d);
+      if (rc) return rc;
+    }
+    k_pc_upper<double><<<nb, kBlock, 0, s>>>(d->n, tri_u(d), d->nvU, d->srow, d->q, d->u, sc);
+    k_pc_lower<double, false><<<nb, kBlock, 0, s>>>(d->n, tri_l(d), d->nvL, d->srow, d->bcmask,
+                                                    d->u, d->q, d->t, nullptr, d->partial,
+                                                    d->nblk, sc);
+  } else {
+    k_jacobi_apply<<<nb, kBlock, 0, s>>>(d->n, d->q, d->d, d->t);
+  }
+  XG_CHECK_LAUNCH(c);
+  XG_CUDA(c, cudaMemcpyAsync(sc, &h, sizeof(h), cudaMemcpyHostToDevice, s));
+  XG_CUDA(c, cudaMemcpyAsync(z, d->t, d->n * 8, cudaMemcpyDeviceToHost, s));
+  XG_CUDA(c, cudaStreamSynchronize(s));
   return XG_OK;
 }
 

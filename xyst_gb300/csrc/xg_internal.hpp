@@ -58,6 +58,29 @@ struct RieCGDev;  // xg_riecg.cu
 struct CGDev;     // xg_cg.cu
 struct KozCGDev;  // xg_kozcg.cu
 
+// Matrix graph of a CG system as the learned preconditioner sees it: the full
+// rows, the strictly lower and strictly upper triangles (SELL-32 each, slice
+// offsets / widths / columns, PAD < 0), the normalised couplings
+// e_ij = a_ij s_i s_j in each layout, the row scales s_i = 1/sqrt|a_ii|, the
+// Dirichlet mask and tposU (upper-layout index of the transpose of each
+// lower entry).
+struct LpcGraph {
+  int64_t n = 0, nslice = 0, nentL = 0, nentU = 0;
+  const int32_t *soff = nullptr, *sw = nullptr, *col = nullptr;
+  const int32_t *soffL = nullptr, *swL = nullptr, *colL = nullptr;
+  const int32_t *soffU = nullptr, *swU = nullptr, *colU = nullptr;
+  const int32_t* tposU = nullptr;
+  const float *eF = nullptr, *eL = nullptr, *eU = nullptr, *srow = nullptr;
+  const uint8_t* mask = nullptr;
+};
+
+// The context's CG system (xg_cg.cu), geometry computed on first use.
+int cg_graph(xg_ctx* c, LpcGraph* g);
+
+// Learned factor (xg_learn.cu): runs the network on g and writes the factor
+// values, lower layout N_ij (nvL) and upper layout N_ij s_i (nvU).
+int lpc_factor(xg_ctx* c, xg_lpc* m, const LpcGraph& g, float* nvL, float* nvU);
+
 void destroy_riecg(RieCGDev*);
 void destroy_cg(CGDev*);
 void destroy_kozcg(KozCGDev*);

@@ -76,6 +76,18 @@ SIGNATURES = {
     "xg_cg_solve": (_int, [_vp, _i64, _dbl, _vp, _vp, _vp, _vp]),
     "xg_cg_solve_mixed": (_int, [_vp, _i64, _dbl, _dbl, _i64, _vp, _vp, _vp, _vp, _vp]),
     "xg_cg_solution": (_int, [_vp, _vp]),
+    "xg_cg_set_factor": (_int, [_vp, _vp, _dbl]),
+    "xg_cg_precondition": (_int, [_vp, _vp, _vp]),
+    "xg_lpc_nparams": (_i64, []),
+    "xg_lpc_create": (_int, [_vp, _int, C.POINTER(_vp)]),
+    "xg_lpc_destroy": (_int, [_vp]),
+    "xg_lpc_set_params": (_int, [_vp, _vp]),
+    "xg_lpc_get_params": (_int, [_vp, _vp]),
+    "xg_lpc_zero_grads": (_int, [_vp]),
+    "xg_lpc_get_grads": (_int, [_vp, _vp]),
+    "xg_lpc_grad": (_int, [_vp, _vp, _vp]),
+    "xg_lpc_adam": (_int, [_vp, _dbl, _dbl, _dbl, _dbl]),
+    "xg_lpc_last_error": (C.c_char_p, [_vp]),
     "xg_mesh_rcm": (_int, [_i64, _i64, _vp, _vp]),
     "xg_mesh_vol": (_int, [_i64, _vp, _i64, _vp, _vp]),
     "xg_mesh_edges": (_int, [_i64, _vp, _i64, _vp, _vp, _int, _i64, _vp, _vp, _vp]),
@@ -139,6 +151,7 @@ class Context:
         if rc != XG_OK:
             raise XgError(rc, f"xg_create({device}) failed (no CUDA device?)")
         self.h = h
+        self.device = device
 
     def check(self, rc: int):
         if rc != XG_OK:
