@@ -165,31 +165,65 @@ def pressure_system(ops):
     return ia, ja, a, b, dn, np.zeros(dn.size)
 
 
-def run_pcg(ctx, ops, tol=1e-8, maxit=20000):
+def train_lpc(ctx, steps=300, lr=1e-3):
+    """The learned preconditioner, trained on the device on four small
+    ChoCG-like pressure systems (13^3-21^3 jittered cubes, p = 0 on x = 1)."""
+    from xyst_gb300 import lpc
+
+    t0 = time.perf_counter()
+    systems = [lpc.training_system(ctx, lpc.pressure_system(ctx, m, seed))
+               for m, seed in ((13, 1), (17, 2), (21, 3), (15, 4))]
+    model = lpc.LearnedPreconditioner(ctx, precision="bf16", seed=0)
+    hist = model.train(systems, steps, lr=lr)
+    return model, {"train_s": time.perf_counter() - t0, "steps": steps,
+                   "loss_first_last": [hist[0], hist[-1]],
+                   "systems": "13^3, 17^3, 21^3, 15^3 jittered cubes"}
+
+
+def run_pcg(ctx, ops, tol=1e-8, maxit=20000, reps=3):
+    """ChoCG pressure solve per time step: init (host rhs, BCs) + solve +
+    solution download, FP64 Jacobi PCG (the reference's algorithm) against
+    the learned factor with the FP32 reliable-update solver."""
     from xyst_gb300 import cg
 
     ia, ja, a, b, dn, dv = pressure_system(ops)
     s = cg.ConjugateGradients(ctx, ia, ja, a)
     n = ia.size - 1
     out = {"tol": tol, "rows": n, "nnz": int(ja.size), "dirichlet": "p=0 on x=1 face"}
-    for mode in ("fp64", "mixed"):
-        best = None
-        for rep in range(2):
-            s.init(x=np.zeros(n), b=b, dirbc=(dn, dv), apply=True, pc="jacobi")
+    model, tr = train_lpc(ctx)
+    out["training"] = tr
+    modes = {"fp64_jacobi": ("jacobi", None, False), "fp64_first_order": ("factor", None, False),
+             "mixed_jacobi": ("jacobi", None, True), "mixed_first_order": ("factor", None, True),
+             "fp64_learned": ("factor", model, False), "mixed_learned": ("factor", model, True)}
+    for name, (pc, mdl, mixed) in modes.items():
+        if pc == "factor":
+            s.set_factor(mdl, 1.0)
             t0 = time.perf_counter()
-            if mode == "fp64":
-                s.solve(maxit, tol)
-            else:
+            s.init(x=np.zeros(n), b=b, dirbc=(dn, dv), apply=True, pc=pc)
+            build_s = time.perf_counter() - t0  # factor (and network inference) built here
+        best = None
+        for rep in range(reps):
+            t0 = time.perf_counter()
+            s.init(x=np.zeros(n), b=b, dirbc=(dn, dv), apply=True, pc=pc)
+            if mixed:
                 s.solve_mixed(200, tol, inner_tol=1e-2, inner_maxit=maxit)
+            else:
+                s.solve(maxit, tol)
+            x = s.solution()
             t1 = time.perf_counter()
             if best is None or t1 - t0 < best["s"]:
                 best = {"s": t1 - t0, "iterations": s.it(), "converged": s.converged(),
                         "rel_residual": s.normr / s.normb}
-                if mode == "mixed":
-                    best["refinements"] = s.outer
-        out[mode] = best
-    it = out["fp64"]["iterations"]
-    out["fp64"]["GBps_per_iteration"] = ((12 * ja.size + 96 * n) * it / out["fp64"]["s"]) / 1e9
+                if mixed:
+                    best["replacements"] = s.outer
+        if pc == "factor":
+            best["factor_build_s"] = build_s
+        out[name] = best
+    model.close()
+    it = out["fp64_jacobi"]["iterations"]
+    out["fp64_jacobi"]["GBps_per_iteration"] = ((12 * ja.size + 96 * n) * it /
+                                                out["fp64_jacobi"]["s"]) / 1e9
+    out["speedup_mixed_learned_vs_fp64_jacobi"] = out["fp64_jacobi"]["s"] / out["mixed_learned"]["s"]
     return out
 
 

@@ -241,8 +241,10 @@ int xg_cg_solve_mixed(xg_ctx* ctx, int64_t maxit, double tol, double inner_tol,
  * "jacobi"): M^-1 = -S (I+N)(I+N)^T S on the non-Dirichlet rows, identity on
  * Dirichlet rows, S = diag(1/sqrt|a_ii|), N strictly lower on A's sparsity.
  * With model == null, N = scale * e with e_ij = a_ij s_i s_j (scale 0 is
- * Jacobi); otherwise the model's network emits N.  The factor is rebuilt at
- * every xg_cg_init(pc = 2), after the Dirichlet elimination. */
+ * Jacobi); otherwise the model's network emits N.  The factor is built at
+ * xg_cg_init(pc = 2) after the Dirichlet elimination and kept while later
+ * inits use the same Dirichlet node set and no xg_cg_set_factor intervenes
+ * (call it again after changing the model's parameters). */
 int xg_cg_set_factor(xg_ctx* ctx, xg_lpc* model, double scale);
 
 /* z = M^-1 r with the preconditioner of the last xg_cg_init (host vectors). */
@@ -257,7 +259,7 @@ int xg_cg_solution(xg_ctx* ctx, double* x);
  * device of the context it is created with; precision 0 runs its dense
  * layers in FP32, 1 as BF16 tensor-core GEMMs with FP32 accumulation.
  * Parameters are one flat FP32 vector of xg_lpc_nparams() values in the
- * order W0 (4x64) b0 W1 (128x64) b1 W2 b2 W3 b3 Wo (64x128) c d w ob. */
+ * order W0 (4x64) b0 W1 (128x64) b1 W2 b2 W3 b3 Wo (64x128) c c2 d w ob. */
 int64_t xg_lpc_nparams(void);
 int xg_lpc_create(xg_ctx* ctx, int precision, xg_lpc** model);
 int xg_lpc_destroy(xg_lpc* model);

@@ -10,18 +10,20 @@ The preconditioned system.  For a matrix A with Dirichlet rows eliminated
 (identity rows, decoupled) and a negative-definite remainder (ChoCG's
 -K), let s_i = 1/sqrt|a_ii| and, off the diagonal and away from Dirichlet
 nodes, e_ij = a_ij s_i s_j, so that A_hat = I - E = -S A S is the SPD
-Jacobi-scaled matrix.  The network emits, for every lower edge (i > j),
-n_ij = e_ij * (1 + 2 tanh(o_ij)); with L = I + N (strictly lower N),
+Jacobi-scaled matrix.  With t_ij = sum_{k > j, k != i} e_ik e_kj (the
+second-order term of the factorised sparse approximate inverse on A's lower
+pattern), the network emits, for every lower edge (i > j),
+n_ij = (e_ij + t_ij) * (1 + tanh(o_ij)); with L = I + N (strictly lower N),
 
     z = M^-1 r:  z_i = r_i (Dirichlet), z_i = -s_i (L L^T (s o r))_i (others),
 
 which is Jacobi for N = 0 and symmetric (negative definite on the -K block)
 for any N.
 
-The network.  Node features x_i = [1, dirichlet_i, sum_j e_ij, degree_i/16];
-h0 = relu(x W0 + b0); three message-passing layers
+The network.  Node features x_i = [dirichlet_i, sum_j e_ij, sum_j e_ij^2,
+degree_i/16]; h0 = relu(x W0 + b0); three message-passing layers
 h_l = relu([h_{l-1}, E h_{l-1}] W_l + b_l) (64 wide); a = h3 P, b = h3 Q;
-per lower edge z = relu(a_i + b_j + c e_ij + d), o_ij = w . z + ob.
+per lower edge z = relu(a_i + b_j + c e_ij + c2 t_ij + d), o_ij = w . z + ob.
 
 The loss is Kaporin's trace functional of the factorised approximate inverse
 (the objective that factorised sparse approximate inverses minimise): with
@@ -44,7 +46,8 @@ H = 64
 
 SHAPES = [("W0", (4, H)), ("b0", (H,)), ("W1", (2 * H, H)), ("b1", (H,)),
           ("W2", (2 * H, H)), ("b2", (H,)), ("W3", (2 * H, H)), ("b3", (H,)),
-          ("Wo", (H, 2 * H)), ("c", (H,)), ("d", (H,)), ("w", (H,)), ("ob", (1,))]
+          ("Wo", (H, 2 * H)), ("c", (H,)), ("c2", (H,)), ("d", (H,)), ("w", (H,)),
+          ("ob", (1,))]
 
 
 def nparams():
@@ -72,7 +75,7 @@ def init_params(seed=0):
             d[name] = rng.standard_normal(shp) * np.sqrt(2.0 / shp[0])
         else:
             d[name] = np.zeros(shp)
-    d["w"] = np.zeros(H)  # o = 0 at start: n = e (first-order factor)
+    d["w"] = np.zeros(H)  # o = 0 at start: n = e + t (second-order factor)
     return flatten(d)
 
 
@@ -96,6 +99,16 @@ class Graph:
         self.li, self.lj, self.le = self.r[lo], self.c[lo], self.e[lo]
         self.deg = np.bincount(rows[off], minlength=n).astype(np.float64)
         del diag
+        self.lt = self.cross(self.le)
+
+    def cross(self, nval):
+        """sum_{k != i} e_ik n_kj at every lower edge (i, j), N strictly lower."""
+        import scipy.sparse as sp
+        n = self.n
+        N = sp.csr_matrix((nval, (self.li, self.lj)), shape=(n, n))
+        E = sp.csr_matrix((self.e, (self.r, self.c)), shape=(n, n))
+        EN = (E @ N).tocsr()
+        return np.asarray(EN[self.li, self.lj]).ravel()
 
     def E(self, v):
         out = np.zeros((self.n,) + v.shape[1:])
@@ -105,7 +118,9 @@ class Graph:
     def features(self):
         rs = np.zeros(self.n)
         np.add.at(rs, self.r, self.e)
-        return np.stack([np.ones(self.n), self.dir.astype(np.float64), rs, self.deg / 16.0], axis=1)
+        r2 = np.zeros(self.n)
+        np.add.at(r2, self.r, self.e * self.e)
+        return np.stack([self.dir.astype(np.float64), rs, r2, self.deg / 16.0], axis=1)
 
 
 def relu(x):
@@ -126,11 +141,11 @@ def forward(theta, g):
         cache[f"h{l}"] = h
     ab = h @ p["Wo"]
     a, b = ab[:, :H], ab[:, H:]
-    z = a[g.li] + b[g.lj] + np.outer(g.le, p["c"]) + p["d"]
+    z = a[g.li] + b[g.lj] + np.outer(g.le, p["c"]) + np.outer(g.lt, p["c2"]) + p["d"]
     zr = relu(z)
     o = zr @ p["w"] + p["ob"][0]
     t = np.tanh(o)
-    nval = g.le * (1.0 + 2.0 * t)
+    nval = (g.le + g.lt) * (1.0 + t)
     cache.update(a=a, b=b, z=z, zr=zr, t=t)
     return nval, cache
 
@@ -162,12 +177,8 @@ def precondition(g, nval, r):
 
 def kaporin(g, nval):
     """Trace loss and its derivative with respect to each lower n_ij."""
-    import scipy.sparse as sp
     n = g.n
-    N = sp.csr_matrix((nval, (g.li, g.lj)), shape=(n, n))
-    E = sp.csr_matrix((g.e, (g.r, g.c)), shape=(n, n))
-    EN = (E @ N).tocsr()
-    cross = np.asarray(EN[g.li, g.lj]).ravel()
+    cross = g.cross(nval)
     loss = float(-2.0 * nval @ g.le + nval @ nval - nval @ cross) / n
     dn = 2.0 * (nval - g.le - cross) / n
     return loss, dn
@@ -179,11 +190,12 @@ def loss_grad(theta, g):
     nval, cache = forward(theta, g)
     loss, dn = kaporin(g, nval)
     grads = {k: np.zeros_like(v) for k, v in p.items()}
-    do = dn * 2.0 * g.le * (1.0 - cache["t"] ** 2)
+    do = dn * (g.le + g.lt) * (1.0 - cache["t"] ** 2)
     grads["ob"][0] = do.sum()
     grads["w"] = cache["zr"].T @ do
     dz = np.outer(do, p["w"]) * (cache["z"] > 0)
     grads["c"] = dz.T @ g.le
+    grads["c2"] = dz.T @ g.lt
     grads["d"] = dz.sum(0)
     da = np.zeros((g.n, H))
     db = np.zeros((g.n, H))

@@ -126,5 +126,5 @@ def test_training_lowers_loss_and_beats_first_order():
     itl, cl = lpc.iterations(s, test, "factor", model=model)
     assert cj and cf and cl
     assert itl < 0.6 * itj
-    assert itl <= itf
+    assert itl < itf  # better than the first-order factor N = e
     model.close()

@@ -9,22 +9,36 @@
 //
 // Layout: the matrix is stored as SELL-32 (slices of 32 rows, each padded to
 // the slice's longest row; entry k of row i at off[s] + k*32 + lane) with
-// int32 columns and FP64 values, plus an FP32 copy for the mixed-precision
-// inner solver.  Dirichlet elimination never rewrites the host matrix: a
-// device pass builds the working values from the original ones and the
-// Dirichlet mask, which is what the reference's sequential elimination
-// produces (rows and columns of Dirichlet nodes zeroed, 1 on their
-// diagonal), and the right-hand side correction sum_i a_ji * val_i is summed
-// per row in the reference's order (decreasing node id).
+// int32 columns and FP64 values.  Dirichlet elimination never rewrites the
+// host matrix: a device pass builds the working values from the original
+// ones and the Dirichlet mask, which is what the reference's sequential
+// elimination produces (rows and columns of Dirichlet nodes zeroed, 1 on
+// their diagonal), and the right-hand side correction sum_i a_ji * val_i is
+// summed per row in the reference's order (decreasing node id).
 //
-// One PCG iteration is two kernels:
-//   k_iter_a: p' = z + beta p (beta = rho/rho0), q = A p', partial (p', q)
-//   k_iter_b: alpha = rho/(p,q); r -= alpha q; z = M^-1 r; x += alpha p';
-//             partial (r,z), (r,r); convergence test
-// Block partial sums go to a scratch array; the last block to finish (an
-// atomic ticket, no spinning) adds them in block order, so every reduction is
+// One PCG iteration (the reference's FP64 algorithm) is two kernels:
+//   k_cg_a: p' = z + beta p (beta = rho/rho0), q = A p', partial (p', q)
+//   k_cg_b: alpha = rho/(p,q); r -= alpha q; x += alpha p'; z = r/d (Jacobi);
+//           partial (r,z), (r,r); convergence test
+// plus, for the factored preconditioner (pc 2, no reference counterpart),
+// z = -S (I+N)(I+N)^T S r in two passes over the lower and upper triangles.
+// Kernels loop over rows with a grid of one wave of resident blocks, so a
+// reduction has one partial per block; the last block to finish (an atomic
+// ticket, no spinning) adds them in block order, so every reduction is
 // deterministic.  Kernels return at once when the solve is done, so the host
 // launches iterations in batches and reads the done flag once per batch.
+//
+// Mixed precision (xg_cg_solve_mixed): the same iteration in FP32 on an FP32
+// copy of the working matrix, its columns stored as 16-bit offsets from the
+// row (when every |j - i| < 32768) and the factor values in FP16, with FP64
+// dot products and reliable updates: the FP32 correction e = sum alpha p' is
+// folded into the FP64 x and the FP32 residual replaced by the true FP64
+// residual b - A x whenever the recursive residual has fallen by the factor
+// `inner_tol` since the last replacement.  The search direction is kept
+// across replacements, so the FP32 iteration follows the FP64 one instead of
+// restarting.
+
+#include <cuda_fp16.h>
 
 #include <algorithm>
 #include <cfloat>
@@ -40,11 +54,12 @@ namespace xg {
 namespace {
 constexpr int kSlice = 32;
 constexpr int32_t kPad = -1;
+constexpr int16_t kPad16 = std::numeric_limits<int16_t>::min();
 constexpr int kBlock = 256;
 constexpr int kBatch = 16;
 
 struct CGScalars {
-  double rho, rho0, pq, alpha, rr, normb, tol;
+  double rho, rho0, pq, alpha, rr, normb, tol, delta, rlast;
   double pad0;
   int64_t it, maxit;
   int32_t done, finished, converged, pc;
@@ -54,9 +69,11 @@ struct CGScalars {
 
 struct CGDev {
   Arena arena;
-  int64_t n = 0, nslice = 0, nent = 0, nblk = 0;
+  int64_t n = 0, nslice = 0, nent = 0, maxgrid = 0;
   int32_t *soff = nullptr, *swidth = nullptr, *col = nullptr;
-  double *a0 = nullptr, *a = nullptr;  // original and working values
+  int16_t* col16 = nullptr;            // column - row, kPad16 for padding
+  double* a0 = nullptr;                // original values (SELL order)
+  double* a = nullptr;                 // working values (after Dirichlet elimination)
   float* a32 = nullptr;
   int32_t* diagpos = nullptr;          // SELL index of each row's diagonal
   uint8_t* bcmask = nullptr;
@@ -65,29 +82,31 @@ struct CGDev {
   double* p[2] = {nullptr, nullptr};
   float *r32 = nullptr, *q32 = nullptr, *z32 = nullptr, *d32 = nullptr, *e32 = nullptr;
   float* p32[2] = {nullptr, nullptr};
-  double* partial = nullptr;  // 3 * nblk
+  double* partial = nullptr;  // 3 * maxgrid
   CGScalars* scal = nullptr;
-  int cur = 0;
   bool apply = false;
-  bool have_bc = false;
   bool ready = false;
+  bool use16 = false;  // every |j - i| fits a 16-bit offset
   int pc = 1;
   int64_t last_it = 0;
   double last_normr = 0, last_normb = 0;
   int last_conv = 0;
-  int64_t inner_its = 0;
   // factored approximate inverse M^-1 = -S (I+N)(I+N)^T S (pc 2): lower and
-  // upper triangles of the matrix graph as SELL-32, the factor values, the
-  // row scales s = 1/sqrt|a_ii| and the normalised couplings e_ij = a_ij s_i s_j
+  // upper triangles of the matrix graph as SELL-32, the factor values (FP32,
+  // and FP16 for the mixed solver), the row scales s = 1/sqrt|a_ii| and the
+  // normalised couplings e_ij = a_ij s_i s_j
   int64_t nentL = 0, nentU = 0;
   int32_t *soffL = nullptr, *swL = nullptr, *colL = nullptr, *posL = nullptr, *tposU = nullptr;
   int32_t *soffU = nullptr, *swU = nullptr, *colU = nullptr;
+  int16_t *colL16 = nullptr, *colU16 = nullptr;
   float *nvL = nullptr, *nvU = nullptr, *srow = nullptr, *eL = nullptr, *eU = nullptr;
+  __half *hvL = nullptr, *hvU = nullptr;
   float* eF = nullptr;  // e_ij in the full layout (0 on the diagonal and at Dirichlet nodes)
+  double *v = nullptr, *u = nullptr, *t = nullptr;  // S r, (I+N)^T S r; t: xg_cg_precondition
+  float *v32 = nullptr, *u32 = nullptr;
   bool geom_set = false;
-  double *u = nullptr, *t = nullptr;  // t: output of xg_cg_precondition
-  float* u32 = nullptr;
   bool factor_set = false;
+  uint64_t bc_key = 0;  // hash of the Dirichlet mask the geometry was built for
   xg_lpc* factor_model = nullptr;  // network emitting N, or null: N = factor_c * e
   double factor_c = 1.0;
 };
@@ -99,11 +118,12 @@ namespace {
 
 // ---------------------------------------------------------------- reductions
 
-// Sum of one value per thread into partial[blockIdx.x]; returns true in the
-// block that completes last (its threads then see every partial).
+// Sum of one value per thread into partial[k * gridDim.x + blockIdx.x];
+// returns true in the block that completes last (its threads then see every
+// partial).
 template <int K>
 __device__ __forceinline__ bool block_partials(const double (&v)[K], double* partial,
-                                               int64_t nblk, unsigned int* ticket) {
+                                               unsigned int* ticket) {
   __shared__ double sm[K][32];
   __shared__ bool last;
   double s[K];
@@ -123,7 +143,7 @@ __device__ __forceinline__ bool block_partials(const double (&v)[K], double* par
     for (int k = 0; k < K; ++k) {
       double t = 0.0;
       for (int w = 0; w < nw; ++w) t += sm[k][w];
-      partial[k * nblk + blockIdx.x] = t;
+      partial[k * gridDim.x + blockIdx.x] = t;
     }
     __threadfence();
     unsigned int prev = atomicAdd(ticket, 1u);
@@ -133,14 +153,23 @@ __device__ __forceinline__ bool block_partials(const double (&v)[K], double* par
   return last;
 }
 
-// In the last block: deterministic sum of the partials of component k, by
-// lane-strided chunks then a fixed-order tree.
-__device__ double sum_partials(const double* partial, int64_t nblk, int k) {
+// In the last block: deterministic sum of the partials of component k, four
+// independent lane-strided chains, then a fixed-order tree.
+__device__ double sum_partials(const double* partial, int k) {
   __shared__ double red[kBlock];
   __threadfence();
-  double t = 0.0;
-  for (int64_t i = threadIdx.x; i < nblk; i += blockDim.x) t += __ldcg(partial + k * nblk + i);
-  red[threadIdx.x] = t;
+  const int64_t nb = gridDim.x;
+  const double* base = partial + k * nb;
+  double t0 = 0.0, t1 = 0.0, t2 = 0.0, t3 = 0.0;
+  int64_t i = threadIdx.x;
+  for (; i + 3 * kBlock < nb; i += 4 * kBlock) {
+    t0 += __ldcg(base + i);
+    t1 += __ldcg(base + i + kBlock);
+    t2 += __ldcg(base + i + 2 * kBlock);
+    t3 += __ldcg(base + i + 3 * kBlock);
+  }
+  for (; i < nb; i += kBlock) t0 += __ldcg(base + i);
+  red[threadIdx.x] = (t0 + t1) + (t2 + t3);
   __syncthreads();
   for (int s = blockDim.x / 2; s > 0; s >>= 1) {
     if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
@@ -151,24 +180,87 @@ __device__ double sum_partials(const double* partial, int64_t nblk, int k) {
   return r;
 }
 
+// ---------------------------------------------------------------- row access
+
+// Column of SELL entry e of row i (or -1 for padding), from int32 columns or
+// 16-bit offsets.
+struct Cols32 {
+  const int32_t* c;
+  __device__ __forceinline__ int32_t at(int32_t e, int32_t) const { return __ldg(c + e); }
+};
+struct Cols16 {
+  const int16_t* c;
+  __device__ __forceinline__ int32_t at(int32_t e, int32_t i) const {
+    const int16_t dlt = __ldg(c + e);
+    return dlt == kPad16 ? -1 : i + int32_t(dlt);
+  }
+};
+
+__device__ __forceinline__ float ldv(const __half* p) { return __half2float(p[0]); }
+__device__ __forceinline__ float ldv(const float* p) { return __ldg(p); }
+__device__ __forceinline__ double ldv(const double* p) { return __ldg(p); }
+
+// sum_k val[e_k] * g(col[e_k]) over row i of a SELL-32 layout, in entry
+// order, issued in groups of U entries so that U column / value loads and
+// then U gathers are in flight at once (padding reads the row's own entry
+// with weight 0).
+template <int U, class T, class CI, class V, class G>
+__device__ __forceinline__ T sell_row(CI ci, const V* __restrict__ val, int32_t off, int w,
+                                      int lane, int32_t i, G g) {
+  T s = T(0);
+  int k = 0;
+  for (; k + U <= w; k += U) {
+    int32_t cc[U];
+    T vv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int32_t e = off + (k + u) * kSlice + lane;
+      const int32_t c = ci.at(e, i);
+      vv[u] = c < 0 ? T(0) : T(ldv(val + e));
+      cc[u] = c < 0 ? i : c;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) s += vv[u] * g(cc[u]);
+  }
+  for (; k < w; ++k) {
+    const int32_t e = off + k * kSlice + lane;
+    const int32_t c = ci.at(e, i);
+    if (c >= 0) s += T(ldv(val + e)) * g(c);
+  }
+  return s;
+}
+
+// One wave of resident blocks of kernel K for n rows.
+int g_nsm = 0;
+template <auto K>
+unsigned pgrid(int64_t n) {
+  static const int per_sm = [] {
+    int v = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, K, kBlock, 0) != cudaSuccess) v = 1;
+    return v < 1 ? 1 : v;
+  }();
+  const int64_t want = (n + kBlock - 1) / kBlock;
+  return static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>(want, int64_t(per_sm) * g_nsm)));
+}
+
+#define XG_ROWS(i, n) \
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < (n); \
+       i += int64_t(gridDim.x) * blockDim.x)
+
 // ---------------------------------------------------------------- kernels
 
-// CSR::mult on the original (or working) values: y = A x.
-__global__ void k_spmv(int64_t n, const int32_t* __restrict__ soff, const int32_t* __restrict__ sw,
-                       const int32_t* __restrict__ col, const double* __restrict__ a,
-                       const double* __restrict__ x, double* __restrict__ y) {
-  int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  if (i >= n) return;
-  const int lane = int(i & 31);
-  const int32_t off = soff[i >> 5], w = sw[i >> 5];
-  double s = 0.0;
-  for (int k = 0; k < w; ++k) {
-    const int32_t e = off + k * kSlice + lane;
-    const int32_t c = __ldg(col + e);
-    if (c < 0) continue;
-    s += __ldg(a + e) * __ldg(x + c);
+// CSR::mult on the original values: y = A x.
+__global__ void __launch_bounds__(kBlock) k_spmv(int64_t n, const int32_t* __restrict__ soff,
+                                                 const int32_t* __restrict__ sw,
+                                                 const int32_t* __restrict__ col,
+                                                 const double* __restrict__ a,
+                                                 const double* __restrict__ x,
+                                                 double* __restrict__ y) {
+  XG_ROWS(i, n) {
+    const int lane = int(i & 31);
+    y[i] = sell_row<4, double>(Cols32{col}, a, soff[i >> 5], sw[i >> 5], lane, int32_t(i),
+                               [&](int32_t c) { return __ldg(x + c); });
   }
-  y[i] = s;
 }
 
 // Working values from the original ones and the Dirichlet mask; the
@@ -221,7 +313,7 @@ __global__ void k_copy_values(int64_t nent, const double* __restrict__ a0, doubl
 }
 
 // ConjugateGradients::setup + pc + initres (ConjugateGradients.cpp:105-319):
-// r = b - A x, d = diag(A) (Jacobi) or 1 (none), z = r/d, p = r,
+// r = b - A x, d = diag(A) (Jacobi) or 1 (none, factor), z = r/d, p = r,
 // partials of (b,b) and (r,z).
 __global__ void __launch_bounds__(kBlock) k_setup(int64_t n, const int32_t* __restrict__ soff,
                                                    const int32_t* __restrict__ sw,
@@ -233,33 +325,27 @@ __global__ void __launch_bounds__(kBlock) k_setup(int64_t n, const int32_t* __re
                                                    double* __restrict__ r, double* __restrict__ d,
                                                    double* __restrict__ z, double* __restrict__ p,
                                                    float* __restrict__ d32, double* partial,
-                                                   int64_t nblk, CGScalars* sc) {
-  int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+                                                   CGScalars* sc) {
   double v[2] = {0.0, 0.0};
-  if (i < n) {
+  const int pc = sc->pc;
+  XG_ROWS(i, n) {
     const int lane = int(i & 31);
-    const int32_t off = soff[i >> 5], w = sw[i >> 5];
-    double s = 0.0;
-    for (int k = 0; k < w; ++k) {
-      const int32_t e = off + k * kSlice + lane;
-      const int32_t c = col[e];
-      if (c < 0) continue;
-      s += a[e] * x[c];
-    }
+    const double s = sell_row<4, double>(Cols32{col}, a, soff[i >> 5], sw[i >> 5], lane,
+                                         int32_t(i), [&](int32_t c) { return x[c]; });
     const double ri = b[i] - s;
-    const double di = sc->pc == 1 ? a[diagpos[i]] : 1.0;
+    const double di = pc == 1 ? a[diagpos[i]] : 1.0;
     r[i] = ri;
     d[i] = di;
     d32[i] = float(di);
     const double zi = ri / di;
     z[i] = zi;
     p[i] = ri;
-    v[0] = b[i] * b[i];
-    v[1] = ri * zi;
+    v[0] += b[i] * b[i];
+    v[1] += ri * zi;
   }
-  if (block_partials<2>(v, partial, nblk, &sc->ticket[0])) {
-    double bb = sum_partials(partial, nblk, 0);
-    double rz = sum_partials(partial, nblk, 1);
+  if (block_partials<2>(v, partial, &sc->ticket[0])) {
+    double bb = sum_partials(partial, 0);
+    double rz = sum_partials(partial, 1);
     if (threadIdx.x == 0) {
       sc->normb = sqrt(bb);
       sc->rho = rz;
@@ -272,41 +358,42 @@ __global__ void __launch_bounds__(kBlock) k_setup(int64_t n, const int32_t* __re
   }
 }
 
-// next + qAp + q (ConjugateGradients.cpp:584-669), fused.
-__global__ void __launch_bounds__(kBlock) k_iter_a(int64_t n, const int32_t* __restrict__ soff,
-                                                    const int32_t* __restrict__ sw,
-                                                    const int32_t* __restrict__ col,
-                                                    const double* __restrict__ a,
-                                                    const double* __restrict__ z,
-                                                    const double* __restrict__ pold,
-                                                    double* __restrict__ pnew,
-                                                    double* __restrict__ q, double* partial,
-                                                    int64_t nblk, CGScalars* sc) {
+// next + qAp + q (ConjugateGradients.cpp:584-669), fused: p' = z + beta p,
+// q = A p', partial (p', q); the last block sets alpha = rho / (p', q).
+// T is the vector type, V the matrix value type, CI the column encoding.
+// The search direction ping-pongs between p0 and p1 by the parity of the
+// iteration count, which only the iterations that ran advance.
+template <class T, class V, class CI>
+__global__ void __launch_bounds__(kBlock) k_cg_a(int64_t n, const int32_t* __restrict__ soff,
+                                                  const int32_t* __restrict__ sw, CI ci,
+                                                  const V* __restrict__ a,
+                                                  const T* __restrict__ z, T* p0, T* p1,
+                                                  T* __restrict__ q, double* partial,
+                                                  CGScalars* sc) {
   if (sc->done) return;
-  const double beta = sc->it == 0 ? 0.0 : sc->rho / sc->rho0;
-  int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  const int64_t it = sc->it;
+  const T beta = it == 0 ? T(0) : T(sc->rho / sc->rho0);
+  const T* __restrict__ pold = (it & 1) ? p1 : p0;
+  T* __restrict__ pnew = (it & 1) ? p0 : p1;
   double v[1] = {0.0};
-  if (i < n) {
+  XG_ROWS(i, n) {
     const int lane = int(i & 31);
-    const int32_t off = soff[i >> 5], w = sw[i >> 5];
-    double s = 0.0;
-    for (int k = 0; k < w; ++k) {
-      const int32_t e = off + k * kSlice + lane;
-      const int32_t c = __ldg(col + e);
-      if (c < 0) continue;
-      s += __ldg(a + e) * (__ldg(z + c) + beta * __ldg(pold + c));
-    }
-    const double pi = z[i] + beta * pold[i];
+    const T s = sell_row<4, T>(ci, a, soff[i >> 5], sw[i >> 5], lane, int32_t(i),
+                               [&](int32_t c) { return __ldg(z + c) + beta * __ldg(pold + c); });
+    const T pi = z[i] + beta * pold[i];
     pnew[i] = pi;
     q[i] = s;
-    v[0] = pi * s;
+    v[0] += double(pi) * double(s);
   }
-  if (block_partials<1>(v, partial, nblk, &sc->ticket[1])) {
-    double pq = sum_partials(partial, nblk, 0);
+  if (block_partials<1>(v, partial, &sc->ticket[1])) {
+    double pq = sum_partials(partial, 0);
     if (threadIdx.x == 0) {
       sc->rho0 = sc->rho;
       sc->pq = pq;
-      if (fabs(pq) < DBL_EPSILON) {
+      // the reference's breakdown guard is an absolute epsilon
+      // (ConjugateGradients.cpp:681-690); the FP32 solver guards underflow only
+      const double eps = sizeof(T) == 8 ? DBL_EPSILON : DBL_MIN;
+      if (fabs(pq) < eps) {
         sc->finished = 1;
         sc->alpha = 0.0;
       } else {
@@ -317,51 +404,123 @@ __global__ void __launch_bounds__(kBlock) k_iter_a(int64_t n, const int32_t* __r
   }
 }
 
-// pq + rz + x (ConjugateGradients.cpp:671-823), fused.
-template <bool FACTOR>
-__global__ void __launch_bounds__(kBlock) k_iter_b(int64_t n, const double* __restrict__ q,
-                                                    const double* __restrict__ d,
-                                                    const double* __restrict__ p,
-                                                    double* __restrict__ r, double* __restrict__ z,
-                                                    double* __restrict__ x, double* partial,
-                                                    int64_t nblk, CGScalars* sc) {
+// pq + rz + x (ConjugateGradients.cpp:671-823), fused: r -= alpha q,
+// x += alpha p'; Jacobi z = r / d and rho = (r, z), or (FACTOR) v = S r for
+// the factor passes that follow; (r, r) and the stopping test:
+//   FP64: ||r|| < tol ||b||, or maxit iterations (the reference's test);
+//   MIXED: ||r|| < max(tol ||b||, delta * rlast) asks for a residual
+//   replacement (rlast: the last true residual norm), as does maxit.
+template <class T, bool FACTOR, bool MIXED>
+__global__ void __launch_bounds__(kBlock) k_cg_b(int64_t n, const T* __restrict__ q,
+                                                  const T* __restrict__ d, const T* p0,
+                                                  const T* p1, const float* __restrict__ srow,
+                                                  T* __restrict__ r, T* __restrict__ z,
+                                                  T* __restrict__ vs, T* __restrict__ x,
+                                                  double* partial, CGScalars* sc) {
   if (sc->done) return;
-  const double alpha = sc->alpha;
-  int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  const T alpha = T(sc->alpha);
+  // the p' of this iteration (k_cg_a wrote it; the count advances below)
+  const T* __restrict__ p = (sc->it & 1) ? p0 : p1;
   double v[2] = {0.0, 0.0};
-  if (i < n) {
-    const double ri = r[i] - alpha * q[i];
+  XG_ROWS(i, n) {
+    const T ri = r[i] - alpha * q[i];
     r[i] = ri;
     x[i] += alpha * p[i];
-    if (!FACTOR) {  // Jacobi / none; the factored inverse follows in two passes
-      const double zi = ri / d[i];
+    if (FACTOR) {
+      vs[i] = T(srow[i]) * ri;
+    } else {
+      const T zi = ri / d[i];
       z[i] = zi;
-      v[0] = ri * zi;
+      v[0] += double(ri) * double(zi);
     }
-    v[1] = ri * ri;
+    v[1] += double(ri) * double(ri);
   }
-  if (block_partials<2>(v, partial, nblk, &sc->ticket[2])) {
-    double rz = sum_partials(partial, nblk, 0);
-    double rr = sum_partials(partial, nblk, 1);
+  if (block_partials<2>(v, partial, &sc->ticket[2])) {
+    double rz = sum_partials(partial, 0);
+    double rr = sum_partials(partial, 1);
     if (threadIdx.x == 0) {
       if (!FACTOR) sc->rho = rz;
       sc->rr = rr;
       sc->it += 1;
-      const double nb = sc->normb > 1.0e-14 ? sc->normb : 1.0;
       const double nr = sqrt(rr);
-      if (sc->finished || nr < sc->tol * nb || sc->it >= sc->maxit) {
-        sc->done = 1;
-        sc->converged = nr > sc->tol * nb ? 0 : 1;
+      const double nb = sc->normb > 1.0e-14 ? sc->normb : 1.0;
+      if (MIXED) {
+        const double lim = fmax(sc->tol * nb, sc->delta * sc->rlast);
+        if (sc->finished || nr < lim || sc->it >= sc->maxit) sc->done = 1;
+      } else {
+        if (sc->finished || nr < sc->tol * nb || sc->it >= sc->maxit) {
+          sc->done = 1;
+          sc->converged = nr > sc->tol * nb ? 0 : 1;
+        }
       }
       sc->ticket[2] = 0;
     }
   }
 }
 
-// ---- mixed precision: FP32 inner PCG on A e = r (x untouched), FP64 dots.
+// ---- factored approximate inverse (pc 2)
 
-// r = b - A x in FP64, r32 = r, e32 = 0, z32 = r/d, p32 = z32; partials
-// (r,r) and (r32,z32).
+// u = (I+N)^T v: u_i = v_i + sum_{j>i} N_ji v_j (upper layout of N).
+template <class T, class V, class CI>
+__global__ void __launch_bounds__(kBlock) k_pc_upper(int64_t n, const int32_t* __restrict__ soffU,
+                                                      const int32_t* __restrict__ swU, CI ci,
+                                                      const V* __restrict__ nvU,
+                                                      const T* __restrict__ vs,
+                                                      T* __restrict__ u,
+                                                      const CGScalars* __restrict__ sc) {
+  if (sc->done) return;
+  XG_ROWS(i, n) {
+    const int lane = int(i & 31);
+    u[i] = vs[i] + sell_row<4, T>(ci, nvU, soffU[i >> 5], swU[i >> 5], lane, int32_t(i),
+                                  [&](int32_t c) { return __ldg(vs + c); });
+  }
+}
+
+// z = -S (I+N) u (Dirichlet rows: z = r), partial (r,z); the last block
+// stores rho = (r,z).
+template <class T, class V, class CI>
+__global__ void __launch_bounds__(kBlock) k_pc_lower(int64_t n, const int32_t* __restrict__ soffL,
+                                                      const int32_t* __restrict__ swL, CI ci,
+                                                      const V* __restrict__ nvL,
+                                                      const float* __restrict__ srow,
+                                                      const uint8_t* __restrict__ mask,
+                                                      const T* __restrict__ u,
+                                                      const T* __restrict__ r, T* __restrict__ z,
+                                                      double* partial, CGScalars* sc) {
+  if (sc->done) return;
+  double v[1] = {0.0};
+  XG_ROWS(i, n) {
+    const int lane = int(i & 31);
+    const T acc = u[i] + sell_row<4, T>(ci, nvL, soffL[i >> 5], swL[i >> 5], lane, int32_t(i),
+                                        [&](int32_t c) { return __ldg(u + c); });
+    const T ri = r[i];
+    const T zi = mask[i] ? ri : -T(srow[i]) * acc;
+    z[i] = zi;
+    v[0] += double(ri) * double(zi);
+  }
+  if (block_partials<1>(v, partial, &sc->ticket[3])) {
+    double rz = sum_partials(partial, 0);
+    if (threadIdx.x == 0) {
+      sc->rho = rz;
+      sc->ticket[3] = 0;
+    }
+  }
+}
+
+// v = S r
+template <class T>
+__global__ void k_scale(int64_t n, const float* __restrict__ srow, const T* __restrict__ r,
+                        T* __restrict__ v) {
+  int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i < n) v[i] = T(srow[i]) * r[i];
+}
+
+// ---- mixed precision: residual replacement
+
+// r = b - A x in FP64 (true residual), r32 = r; Jacobi: z32 = r32 / d32 and
+// rho = (r32, z32); factor (srow given): v32 = S r32.  Partial (r,r) -> rr.
+// FIRST starts the FP32 iteration (it = 0, so beta = 0); otherwise it
+// continues with the kept search direction.
 __global__ void __launch_bounds__(kBlock) k_outer_res(int64_t n, const int32_t* __restrict__ soff,
                                                        const int32_t* __restrict__ sw,
                                                        const int32_t* __restrict__ col,
@@ -369,40 +528,35 @@ __global__ void __launch_bounds__(kBlock) k_outer_res(int64_t n, const int32_t* 
                                                        const double* __restrict__ x,
                                                        const double* __restrict__ b,
                                                        const float* __restrict__ d32,
+                                                       const float* __restrict__ srow,
                                                        float* __restrict__ r32,
                                                        float* __restrict__ z32,
-                                                       float* __restrict__ p32,
-                                                       float* __restrict__ e32, double* partial,
-                                                       int64_t nblk, CGScalars* sc) {
-  int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+                                                       float* __restrict__ v32, int first,
+                                                       double* partial, CGScalars* sc) {
   double v[2] = {0.0, 0.0};
-  if (i < n) {
+  XG_ROWS(i, n) {
     const int lane = int(i & 31);
-    const int32_t off = soff[i >> 5], w = sw[i >> 5];
-    double s = 0.0;
-    for (int k = 0; k < w; ++k) {
-      const int32_t e = off + k * kSlice + lane;
-      const int32_t c = col[e];
-      if (c < 0) continue;
-      s += a[e] * x[c];
-    }
+    const double s = sell_row<4, double>(Cols32{col}, a, soff[i >> 5], sw[i >> 5], lane,
+                                         int32_t(i), [&](int32_t c) { return __ldg(x + c); });
     const double ri = b[i] - s;
     const float rf = float(ri);
-    const float zf = rf / d32[i];
     r32[i] = rf;
-    z32[i] = zf;
-    p32[i] = zf;
-    e32[i] = 0.f;
-    v[0] = ri * ri;
-    v[1] = double(rf) * double(zf);
+    if (srow) {
+      v32[i] = srow[i] * rf;
+    } else {
+      const float zf = rf / d32[i];
+      z32[i] = zf;
+      v[1] += double(rf) * double(zf);
+    }
+    v[0] += ri * ri;
   }
-  if (block_partials<2>(v, partial, nblk, &sc->ticket[0])) {
-    double rr = sum_partials(partial, nblk, 0);
-    double rz = sum_partials(partial, nblk, 1);
+  if (block_partials<2>(v, partial, &sc->ticket[0])) {
+    double rr = sum_partials(partial, 0);
+    double rz = sum_partials(partial, 1);
     if (threadIdx.x == 0) {
       sc->rr = rr;
-      sc->rho = rz;
-      sc->it = 0;
+      if (!srow) sc->rho = rz;
+      if (first) sc->it = 0;
       sc->done = 0;
       sc->finished = 0;
       sc->ticket[0] = 0;
@@ -410,83 +564,12 @@ __global__ void __launch_bounds__(kBlock) k_outer_res(int64_t n, const int32_t* 
   }
 }
 
-__global__ void __launch_bounds__(kBlock) k_in_a(int64_t n, const int32_t* __restrict__ soff,
-                                                  const int32_t* __restrict__ sw,
-                                                  const int32_t* __restrict__ col,
-                                                  const float* __restrict__ a,
-                                                  const float* __restrict__ z,
-                                                  const float* __restrict__ pold,
-                                                  float* __restrict__ pnew, float* __restrict__ q,
-                                                  double* partial, int64_t nblk, CGScalars* sc) {
-  if (sc->done) return;
-  const float beta = sc->it == 0 ? 0.f : float(sc->rho / sc->rho0);
+// x += e, e = 0
+__global__ void k_add_correction(int64_t n, float* __restrict__ e, double* __restrict__ x) {
   int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  double v[1] = {0.0};
   if (i < n) {
-    const int lane = int(i & 31);
-    const int32_t off = soff[i >> 5], w = sw[i >> 5];
-    float s = 0.f;
-    for (int k = 0; k < w; ++k) {
-      const int32_t e = off + k * kSlice + lane;
-      const int32_t c = __ldg(col + e);
-      if (c < 0) continue;
-      s += __ldg(a + e) * (__ldg(z + c) + beta * __ldg(pold + c));
-    }
-    const float pi = z[i] + beta * pold[i];
-    pnew[i] = pi;
-    q[i] = s;
-    v[0] = double(pi) * double(s);
-  }
-  if (block_partials<1>(v, partial, nblk, &sc->ticket[1])) {
-    double pq = sum_partials(partial, nblk, 0);
-    if (threadIdx.x == 0) {
-      sc->rho0 = sc->rho;
-      sc->pq = pq;
-      if (fabs(pq) < DBL_MIN) {
-        sc->finished = 1;
-        sc->alpha = 0.0;
-      } else {
-        sc->alpha = sc->rho / pq;
-      }
-      sc->ticket[1] = 0;
-    }
-  }
-}
-
-// inner stop: ||r_inner|| < tol * ||r_outer|| (tol in sc->tol, ||r_outer||^2
-// kept in sc->normb as the reference norm of this inner solve)
-template <bool FACTOR>
-__global__ void __launch_bounds__(kBlock) k_in_b(int64_t n, const float* __restrict__ q,
-                                                  const float* __restrict__ d,
-                                                  const float* __restrict__ p,
-                                                  float* __restrict__ r, float* __restrict__ z,
-                                                  float* __restrict__ e, double* partial,
-                                                  int64_t nblk, CGScalars* sc) {
-  if (sc->done) return;
-  const float alpha = float(sc->alpha);
-  int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  double v[2] = {0.0, 0.0};
-  if (i < n) {
-    const float ri = r[i] - alpha * q[i];
-    r[i] = ri;
-    e[i] += alpha * p[i];
-    if (!FACTOR) {
-      const float zi = ri / d[i];
-      z[i] = zi;
-      v[0] = double(ri) * double(zi);
-    }
-    v[1] = double(ri) * double(ri);
-  }
-  if (block_partials<2>(v, partial, nblk, &sc->ticket[2])) {
-    double rz = sum_partials(partial, nblk, 0);
-    double rr = sum_partials(partial, nblk, 1);
-    if (threadIdx.x == 0) {
-      if (!FACTOR) sc->rho = rz;
-      sc->it += 1;
-      const double nr = sqrt(rr);
-      if (sc->finished || nr < sc->tol * sc->normb || sc->it >= sc->maxit) sc->done = 1;
-      sc->ticket[2] = 0;
-    }
+    x[i] += double(e[i]);
+    e[i] = 0.f;
   }
 }
 
@@ -496,51 +579,37 @@ __global__ void k_jacobi_apply(int64_t n, const double* __restrict__ r, const do
   if (i < n) z[i] = r[i] / d[i];
 }
 
-__global__ void k_add_correction(int64_t n, const float* __restrict__ e, double* __restrict__ x) {
-  int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  if (i < n) x[i] += double(e[i]);
-}
+// ---- factor construction
 
-__global__ void k_set_inner(CGScalars* sc, double tol, int64_t maxit) {
-  sc->normb = sqrt(sc->rr);
-  sc->tol = tol;
-  sc->maxit = maxit;
-}
-
-// ---- factored approximate inverse (pc 2)
-
-struct Tri {
-  const int32_t* soff;
-  const int32_t* sw;
-  const int32_t* col;
-};
-
-// Row scales and normalised lower couplings of the working matrix:
-// s_i = 1/sqrt|a_ii|, e_ij = a_ij s_i s_j (0 when i or j is a Dirichlet node).
+// Row scales s_i = 1/sqrt|a_ii| of the working matrix.
 __global__ void k_factor_geom(int64_t n, const double* __restrict__ a,
-                              const int32_t* __restrict__ diagpos, const uint8_t* __restrict__ mask,
-                              float* __restrict__ srow) {
+                              const int32_t* __restrict__ diagpos, float* __restrict__ srow) {
   int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (i >= n) return;
   srow[i] = float(1.0 / sqrt(fabs(a[diagpos[i]])));
 }
-__global__ void k_factor_e(int64_t n, Tri L, const int32_t* __restrict__ posL,
-                           const int32_t* __restrict__ tposU, const double* __restrict__ a,
-                           const float* __restrict__ srow, const uint8_t* __restrict__ mask,
-                           float* __restrict__ eL, float* __restrict__ eU) {
+// e_ij = a_ij s_i s_j (0 when i or j is a Dirichlet node) in the lower and
+// upper layouts.
+__global__ void k_factor_e(int64_t n, const int32_t* __restrict__ soffL,
+                           const int32_t* __restrict__ swL, const int32_t* __restrict__ colL,
+                           const int32_t* __restrict__ posL, const int32_t* __restrict__ tposU,
+                           const double* __restrict__ a, const float* __restrict__ srow,
+                           const uint8_t* __restrict__ mask, float* __restrict__ eL,
+                           float* __restrict__ eU) {
   int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (i >= n) return;
   const int lane = int(i & 31);
-  const int32_t off = L.soff[i >> 5], w = L.sw[i >> 5];
+  const int32_t off = soffL[i >> 5], w = swL[i >> 5];
   for (int k = 0; k < w; ++k) {
     const int32_t e = off + k * kSlice + lane;
-    const int32_t j = L.col[e];
+    const int32_t j = colL[e];
     if (j < 0) continue;
     const float v = (mask[i] || mask[j]) ? 0.f : float(a[posL[e]]) * srow[i] * srow[j];
     eL[e] = v;
     eU[tposU[e]] = v;
   }
 }
+// e_ij in the full layout.
 __global__ void k_factor_efull(int64_t n, const int32_t* __restrict__ soff,
                                const int32_t* __restrict__ sw, const int32_t* __restrict__ col,
                                const double* __restrict__ a, const float* __restrict__ srow,
@@ -555,93 +624,52 @@ __global__ void k_factor_efull(int64_t n, const int32_t* __restrict__ soff,
     eF[e] = (j < 0 || j == i || mask[i] || mask[j]) ? 0.f : float(a[e]) * srow[i] * srow[j];
   }
 }
-// N_ij = c e_ij (the first-order factor, c = 1, or any uniform scaling).
-__global__ void k_factor_scaled(int64_t n, Tri L, const int32_t* __restrict__ tposU,
-                                const float* __restrict__ eL, const float* __restrict__ srow,
+// N_ij = c e_ij (the first-order factor, c = 1, or any uniform scaling), in
+// the lower layout and, transposed, the upper one.
+__global__ void k_factor_scaled(int64_t n, const int32_t* __restrict__ soffL,
+                                const int32_t* __restrict__ swL, const int32_t* __restrict__ colL,
+                                const int32_t* __restrict__ tposU, const float* __restrict__ eL,
                                 float c, float* __restrict__ nvL, float* __restrict__ nvU) {
   int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (i >= n) return;
   const int lane = int(i & 31);
-  const int32_t off = L.soff[i >> 5], w = L.sw[i >> 5];
+  const int32_t off = soffL[i >> 5], w = swL[i >> 5];
   for (int k = 0; k < w; ++k) {
     const int32_t e = off + k * kSlice + lane;
-    const int32_t j = L.col[e];
+    const int32_t j = colL[e];
     if (j < 0) continue;
     const float v = c * eL[e];
     nvL[e] = v;
-    nvU[tposU[e]] = v * srow[i];  // the upper copy (row j, column i) carries s_i
+    nvU[tposU[e]] = v;
   }
 }
-
-// u = (I+N)^T S r: u_i = s_i r_i + sum_{j>i} N_ji s_j r_j.
-template <class T>
-__global__ void __launch_bounds__(kBlock) k_pc_upper(int64_t n, Tri U, const float* __restrict__ nvU,
-                                                      const float* __restrict__ srow,
-                                                      const T* __restrict__ r, T* __restrict__ u,
-                                                      const CGScalars* __restrict__ sc) {
-  if (sc->done) return;
-  int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  if (i >= n) return;
-  const int lane = int(i & 31);
-  const int32_t off = U.soff[i >> 5], w = U.sw[i >> 5];
-  T acc = T(srow[i]) * r[i];
-  for (int k = 0; k < w; ++k) {
-    const int32_t e = off + k * kSlice + lane;
-    const int32_t j = __ldg(U.col + e);
-    if (j < 0) continue;
-    acc += T(__ldg(nvU + e)) * __ldg(r + j);
-  }
-  u[i] = acc;
+__global__ void k_to_half(int64_t m, const float* __restrict__ a, __half* __restrict__ h) {
+  int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (e < m) h[e] = __float2half_rn(a[e]);
 }
 
-// z = -S (I+N) u (Dirichlet rows: z = r), partial (r,z); the last block
-// stores rho = (r,z).  With SETP the search direction starts as p = z.
-template <class T, bool SETP>
-__global__ void __launch_bounds__(kBlock) k_pc_lower(int64_t n, Tri L, const float* __restrict__ nvL,
-                                                      const float* __restrict__ srow,
-                                                      const uint8_t* __restrict__ mask,
-                                                      const T* __restrict__ u, const T* __restrict__ r,
-                                                      T* __restrict__ z, T* __restrict__ p,
-                                                      double* partial, int64_t nblk, CGScalars* sc) {
-  if (sc->done) return;
-  int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  double v[1] = {0.0};
-  if (i < n) {
-    const int lane = int(i & 31);
-    const int32_t off = L.soff[i >> 5], w = L.sw[i >> 5];
-    T acc = u[i];
-    for (int k = 0; k < w; ++k) {
-      const int32_t e = off + k * kSlice + lane;
-      const int32_t j = __ldg(L.col + e);
-      if (j < 0) continue;
-      acc += T(__ldg(nvL + e)) * __ldg(u + j);
-    }
-    const T ri = r[i];
-    const T zi = mask[i] ? ri : -T(srow[i]) * acc;
-    z[i] = zi;
-    if (SETP) p[i] = zi;
-    v[0] = double(ri) * double(zi);
-  }
-  if (block_partials<1>(v, partial, nblk, &sc->ticket[3])) {
-    double rz = sum_partials(partial, nblk, 0);
-    if (threadIdx.x == 0) {
-      sc->rho = rz;
-      sc->ticket[3] = 0;
-    }
-  }
-}
+// ---------------------------------------------------------------- host helpers
 
-Tri tri_l(const CGDev* d) { return Tri{d->soffL, d->swL, d->colL}; }
-Tri tri_u(const CGDev* d) { return Tri{d->soffU, d->swU, d->colU}; }
+int read_scal(xg_ctx* c, CGDev* d, CGScalars* h) {
+  XG_CUDA(c, cudaMemcpyAsync(h, d->scal, sizeof(CGScalars), cudaMemcpyDeviceToHost, c->stream));
+  XG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return XG_OK;
+}
+int write_scal(xg_ctx* c, CGDev* d, const CGScalars* h) {
+  XG_CUDA(c, cudaMemcpyAsync(d->scal, h, sizeof(CGScalars), cudaMemcpyHostToDevice, c->stream));
+  // h lives on the caller's stack frame: complete the copy before returning
+  XG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return XG_OK;
+}
 
 // Row scales and normalised couplings of the current working matrix.
 int build_geom(xg_ctx* c, CGDev* d) {
   cudaStream_t s = c->stream;
   const unsigned nb = blocks_for(d->n, kBlock);
-  k_factor_geom<<<nb, kBlock, 0, s>>>(d->n, d->a, d->diagpos, d->bcmask, d->srow);
+  k_factor_geom<<<nb, kBlock, 0, s>>>(d->n, d->a, d->diagpos, d->srow);
   XG_CHECK_LAUNCH(c);
-  k_factor_e<<<nb, kBlock, 0, s>>>(d->n, tri_l(d), d->posL, d->tposU, d->a, d->srow, d->bcmask,
-                                   d->eL, d->eU);
+  k_factor_e<<<nb, kBlock, 0, s>>>(d->n, d->soffL, d->swL, d->colL, d->posL, d->tposU, d->a,
+                                   d->srow, d->bcmask, d->eL, d->eU);
   XG_CHECK_LAUNCH(c);
   k_factor_efull<<<nb, kBlock, 0, s>>>(d->n, d->soff, d->swidth, d->col, d->a, d->srow, d->bcmask,
                                        d->eF);
@@ -674,7 +702,8 @@ LpcGraph graph_of(const CGDev* d) {
   return g;
 }
 
-// Scales, couplings and factor values of the current working matrix.
+// Scales, couplings and factor values (FP32 and FP16) of the current
+// working matrix.
 int build_factor(xg_ctx* c, CGDev* d) {
   cudaStream_t s = c->stream;
   const unsigned nb = blocks_for(d->n, kBlock);
@@ -686,17 +715,121 @@ int build_factor(xg_ctx* c, CGDev* d) {
     int rc = lpc_factor(c, d->factor_model, graph_of(d), d->nvL, d->nvU);
     if (rc) return rc;
   } else {
-    k_factor_scaled<<<nb, kBlock, 0, s>>>(d->n, tri_l(d), d->tposU, d->eL, d->srow,
+    k_factor_scaled<<<nb, kBlock, 0, s>>>(d->n, d->soffL, d->swL, d->colL, d->tposU, d->eL,
                                           float(d->factor_c), d->nvL, d->nvU);
     XG_CHECK_LAUNCH(c);
   }
+  k_to_half<<<blocks_for(std::max<int64_t>(1, d->nentL), kBlock), kBlock, 0, s>>>(d->nentL, d->nvL,
+                                                                                  d->hvL);
+  k_to_half<<<blocks_for(std::max<int64_t>(1, d->nentU), kBlock), kBlock, 0, s>>>(d->nentU, d->nvU,
+                                                                                  d->hvU);
+  XG_CHECK_LAUNCH(c);
   d->factor_set = true;
   return XG_OK;
 }
 
-int read_scal(xg_ctx* c, CGDev* d, CGScalars* h) {
-  XG_CUDA(c, cudaMemcpyAsync(h, d->scal, sizeof(CGScalars), cudaMemcpyDeviceToHost, c->stream));
-  XG_CUDA(c, cudaStreamSynchronize(c->stream));
+// z = M^-1 r with the factor in FP64 vectors (FP32 values): v = S r, then the
+// two passes; rho = (r, z).
+int factor_apply64(xg_ctx* c, CGDev* d, const double* r, double* z) {
+  cudaStream_t s = c->stream;
+  const int64_t n = d->n;
+  k_scale<double><<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, d->srow, r, d->v);
+  k_pc_upper<double, float, Cols32>
+      <<<pgrid<k_pc_upper<double, float, Cols32>>(n), kBlock, 0, s>>>(
+          n, d->soffU, d->swU, Cols32{d->colU}, d->nvU, d->v, d->u, d->scal);
+  k_pc_lower<double, float, Cols32>
+      <<<pgrid<k_pc_lower<double, float, Cols32>>(n), kBlock, 0, s>>>(
+          n, d->soffL, d->swL, Cols32{d->colL}, d->nvL, d->srow, d->bcmask, d->u, r, z,
+          d->partial, d->scal);
+  XG_CHECK_LAUNCH(c);
+  return XG_OK;
+}
+
+// The FP32 factor passes on v32 = S r32 (already written): z32, rho.
+template <class CI>
+void factor_passes32(xg_ctx* c, CGDev* d, CI cu, CI cl) {
+  cudaStream_t s = c->stream;
+  const int64_t n = d->n;
+  k_pc_upper<float, __half, CI><<<pgrid<k_pc_upper<float, __half, CI>>(n), kBlock, 0, s>>>(
+      n, d->soffU, d->swU, cu, d->hvU, d->v32, d->u32, d->scal);
+  k_pc_lower<float, __half, CI><<<pgrid<k_pc_lower<float, __half, CI>>(n), kBlock, 0, s>>>(
+      n, d->soffL, d->swL, cl, d->hvL, d->srow, d->bcmask, d->u32, d->r32, d->z32, d->partial,
+      d->scal);
+}
+
+int cg_iterate(xg_ctx* c, CGDev* d, int64_t maxit, double tol, CGScalars* h) {
+  cudaStream_t s = c->stream;
+  // tol and maxit into the device scalars without touching the rest
+  XG_CUDA(c, cudaMemcpyAsync(&d->scal->tol, &tol, sizeof(double), cudaMemcpyHostToDevice, s));
+  XG_CUDA(c, cudaMemcpyAsync(&d->scal->maxit, &maxit, sizeof(int64_t), cudaMemcpyHostToDevice, s));
+  const int64_t n = d->n;
+  for (;;) {
+    for (int k = 0; k < kBatch; ++k) {
+      double *p0 = d->p[0], *p1 = d->p[1];
+      k_cg_a<double, double, Cols32><<<pgrid<k_cg_a<double, double, Cols32>>(n), kBlock, 0, s>>>(
+          n, d->soff, d->swidth, Cols32{d->col}, d->a, d->z, p0, p1, d->q, d->partial, d->scal);
+      if (d->pc == 2) {
+        k_cg_b<double, true, false><<<pgrid<k_cg_b<double, true, false>>(n), kBlock, 0, s>>>(
+            n, d->q, d->d, p0, p1, d->srow, d->r, d->z, d->v, d->x, d->partial, d->scal);
+        k_pc_upper<double, float, Cols32>
+            <<<pgrid<k_pc_upper<double, float, Cols32>>(n), kBlock, 0, s>>>(
+                n, d->soffU, d->swU, Cols32{d->colU}, d->nvU, d->v, d->u, d->scal);
+        k_pc_lower<double, float, Cols32>
+            <<<pgrid<k_pc_lower<double, float, Cols32>>(n), kBlock, 0, s>>>(
+                n, d->soffL, d->swL, Cols32{d->colL}, d->nvL, d->srow, d->bcmask, d->u, d->r,
+                d->z, d->partial, d->scal);
+      } else {
+        k_cg_b<double, false, false><<<pgrid<k_cg_b<double, false, false>>(n), kBlock, 0, s>>>(
+            n, d->q, d->d, p0, p1, d->srow, d->r, d->z, d->v, d->x, d->partial, d->scal);
+      }
+    }
+    XG_CHECK_LAUNCH(c);
+    int rc = read_scal(c, d, h);
+    if (rc) return rc;
+    if (h->done) break;
+  }
+  return XG_OK;
+}
+
+// A batch of FP32 iterations with column encoding CI.
+template <class CI>
+int mixed_batch(xg_ctx* c, CGDev* d, CI ca, CI cu, CI cl) {
+  cudaStream_t s = c->stream;
+  const int64_t n = d->n;
+  for (int k = 0; k < kBatch; ++k) {
+    float *p0 = d->p32[0], *p1 = d->p32[1];
+    k_cg_a<float, float, CI><<<pgrid<k_cg_a<float, float, CI>>(n), kBlock, 0, s>>>(
+        n, d->soff, d->swidth, ca, d->a32, d->z32, p0, p1, d->q32, d->partial, d->scal);
+    if (d->pc == 2) {
+      k_cg_b<float, true, true><<<pgrid<k_cg_b<float, true, true>>(n), kBlock, 0, s>>>(
+          n, d->q32, d->d32, p0, p1, d->srow, d->r32, d->z32, d->v32, d->e32, d->partial,
+          d->scal);
+      factor_passes32<CI>(c, d, cu, cl);
+    } else {
+      k_cg_b<float, false, true><<<pgrid<k_cg_b<float, false, true>>(n), kBlock, 0, s>>>(
+          n, d->q32, d->d32, p0, p1, d->srow, d->r32, d->z32, d->v32, d->e32, d->partial,
+          d->scal);
+    }
+  }
+  XG_CHECK_LAUNCH(c);
+  return XG_OK;
+}
+
+// True residual into the FP32 iteration (and the factor passes for z32).
+int replace_residual(xg_ctx* c, CGDev* d, int first) {
+  cudaStream_t s = c->stream;
+  const int64_t n = d->n;
+  k_outer_res<<<pgrid<k_outer_res>(n), kBlock, 0, s>>>(
+      n, d->soff, d->swidth, d->col, d->a, d->x, d->b, d->d32, d->pc == 2 ? d->srow : nullptr,
+      d->r32, d->z32, d->v32, first, d->partial, d->scal);
+  XG_CHECK_LAUNCH(c);
+  if (d->pc == 2) {
+    if (d->use16)
+      factor_passes32<Cols16>(c, d, Cols16{d->colU16}, Cols16{d->colL16});
+    else
+      factor_passes32<Cols32>(c, d, Cols32{d->colU}, Cols32{d->colL});
+    XG_CHECK_LAUNCH(c);
+  }
   return XG_OK;
 }
 
@@ -729,14 +862,24 @@ int xg_cg_setup(xg_ctx* c, int64_t nrow, const uint64_t* ia, const uint64_t* ja,
   const uint64_t b0 = static_cast<uint64_t>(base);
   if (ia[0] != b0) return fail(c, XG_ERR_ARG, "cg_setup: ia[0] must equal the index base");
   std::vector<int32_t> diagk(nrow, -1);
+  bool fits16 = true;
   for (int64_t i = 0; i < nrow; ++i) {
     if (ia[i + 1] < ia[i]) return fail(c, XG_ERR_ARG, "cg_setup: ia not monotonic");
     for (uint64_t j = ia[i]; j < ia[i + 1]; ++j) {
       uint64_t cc = ja[j - b0] - b0;
       if (cc >= static_cast<uint64_t>(nrow)) return fail(c, XG_ERR_ARG, "cg_setup: column id");
       if (static_cast<int64_t>(cc) == i) diagk[i] = static_cast<int32_t>(j - ia[i]);
+      const int64_t dl = static_cast<int64_t>(cc) - i;
+      if (dl <= int64_t(kPad16) || dl > int64_t(std::numeric_limits<int16_t>::max()))
+        fits16 = false;
     }
     if (diagk[i] < 0) return fail(c, XG_ERR_ARG, "cg_setup: row without diagonal entry");
+  }
+  if (g_nsm == 0) {
+    int dev = 0, nsm = 0;
+    XG_CUDA(c, cudaGetDevice(&dev));
+    XG_CUDA(c, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    g_nsm = nsm > 0 ? nsm : 1;
   }
   const int64_t nslice = (nrow + kSlice - 1) / kSlice;
   std::vector<int32_t> soff(nslice + 1), sw(nslice);
@@ -752,6 +895,7 @@ int xg_cg_setup(xg_ctx* c, int64_t nrow, const uint64_t* ia, const uint64_t* ja,
   }
   soff[nslice] = static_cast<int32_t>(tot);
   std::vector<int32_t> col(tot, kPad), dpos(nrow);
+  std::vector<int16_t> col16(fits16 ? tot : 0, kPad16);
   std::vector<double> val(tot, 0.0);
   for (int64_t i = 0; i < nrow; ++i) {
     const int64_t s = i / kSlice, lane = i % kSlice;
@@ -759,6 +903,7 @@ int xg_cg_setup(xg_ctx* c, int64_t nrow, const uint64_t* ia, const uint64_t* ja,
       const int64_t k = int64_t(j - ia[i]);
       const int64_t e = soff[s] + k * kSlice + lane;
       col[e] = static_cast<int32_t>(ja[j - b0] - b0);
+      if (fits16) col16[e] = static_cast<int16_t>(col[e] - i);
       val[e] = a[j - b0];
     }
     dpos[i] = static_cast<int32_t>(soff[s] + int64_t(diagk[i]) * kSlice + lane);
@@ -791,7 +936,8 @@ int xg_cg_setup(xg_ctx* c, int64_t nrow, const uint64_t* ia, const uint64_t* ja,
   soffU[nslice] = int32_t(totU);
   std::vector<int32_t> colL(std::max<int64_t>(1, totL), kPad), posL(std::max<int64_t>(1, totL), 0),
       colU(std::max<int64_t>(1, totU), kPad), tposU(std::max<int64_t>(1, totL), 0);
-  std::vector<int64_t> rowU(nrow + 1, 0);  // for locating (j,i) in row j's upper list
+  std::vector<int16_t> colL16(fits16 ? colL.size() : 0, kPad16),
+      colU16(fits16 ? colU.size() : 0, kPad16);
   for (int64_t i = 0; i < nrow; ++i) {
     const int64_t s2 = i / kSlice, lane = i % kSlice;
     int64_t kl = 0, ku = 0;
@@ -801,10 +947,13 @@ int xg_cg_setup(xg_ctx* c, int64_t nrow, const uint64_t* ia, const uint64_t* ja,
       if (cc < i) {
         const int64_t e = soffL[s2] + kl * kSlice + lane;
         colL[e] = int32_t(cc);
+        if (fits16) colL16[e] = int16_t(cc - i);
         posL[e] = int32_t(soff[s2] + kfull * kSlice + lane);
         ++kl;
       } else if (cc > i) {
-        colU[soffU[s2] + ku * kSlice + lane] = int32_t(cc);
+        const int64_t e = soffU[s2] + ku * kSlice + lane;
+        colU[e] = int32_t(cc);
+        if (fits16) colU16[e] = int16_t(cc - i);
         ++ku;
       }
     }
@@ -843,12 +992,14 @@ int xg_cg_setup(xg_ctx* c, int64_t nrow, const uint64_t* ia, const uint64_t* ja,
   d->n = nrow;
   d->nslice = nslice;
   d->nent = tot;
-  d->nblk = (nrow + kBlock - 1) / kBlock;
+  d->use16 = fits16;
+  d->maxgrid = int64_t(g_nsm) * (2048 / kBlock);
   for (int pass = 0; pass < 2; ++pass) {
     Arena& A = d->arena;
     A.plan(d->soff, nslice + 1);
     A.plan(d->swidth, nslice);
     A.plan(d->col, tot);
+    A.plan(d->col16, fits16 ? tot : 1);
     A.plan(d->a0, tot);
     A.plan(d->a, tot);
     A.plan(d->a32, tot);
@@ -870,24 +1021,30 @@ int xg_cg_setup(xg_ctx* c, int64_t nrow, const uint64_t* ia, const uint64_t* ja,
     A.plan(d->e32, nrow);
     A.plan(d->p32[0], nrow);
     A.plan(d->p32[1], nrow);
-    A.plan(d->partial, 3 * d->nblk);
+    A.plan(d->partial, 3 * d->maxgrid);
     A.plan(d->scal, 1);
     A.plan(d->soffL, nslice + 1);
     A.plan(d->swL, nslice);
     A.plan(d->colL, colL.size());
+    A.plan(d->colL16, fits16 ? colL.size() : 1);
     A.plan(d->posL, posL.size());
     A.plan(d->tposU, tposU.size());
     A.plan(d->soffU, nslice + 1);
     A.plan(d->swU, nslice);
     A.plan(d->colU, colU.size());
+    A.plan(d->colU16, fits16 ? colU.size() : 1);
     A.plan(d->nvL, colL.size());
     A.plan(d->nvU, colU.size());
+    A.plan(d->hvL, colL.size());
+    A.plan(d->hvU, colU.size());
     A.plan(d->eL, colL.size());
     A.plan(d->eU, colU.size());
     A.plan(d->eF, tot);
     A.plan(d->srow, nrow);
+    A.plan(d->v, nrow);
     A.plan(d->u, nrow);
     A.plan(d->t, nrow);
+    A.plan(d->v32, nrow);
     A.plan(d->u32, nrow);
     if (pass == 0) {
       cudaError_t e = A.reserve();
@@ -902,6 +1059,8 @@ int xg_cg_setup(xg_ctx* c, int64_t nrow, const uint64_t* ia, const uint64_t* ja,
   XG_CUDA(c, cudaMemcpyAsync(d->soff, soff.data(), soff.size() * 4, cudaMemcpyHostToDevice, s));
   XG_CUDA(c, cudaMemcpyAsync(d->swidth, sw.data(), sw.size() * 4, cudaMemcpyHostToDevice, s));
   XG_CUDA(c, cudaMemcpyAsync(d->col, col.data(), col.size() * 4, cudaMemcpyHostToDevice, s));
+  if (fits16)
+    XG_CUDA(c, cudaMemcpyAsync(d->col16, col16.data(), col16.size() * 2, cudaMemcpyHostToDevice, s));
   XG_CUDA(c, cudaMemcpyAsync(d->a0, val.data(), val.size() * 8, cudaMemcpyHostToDevice, s));
   XG_CUDA(c, cudaMemcpyAsync(d->diagpos, dpos.data(), dpos.size() * 4, cudaMemcpyHostToDevice, s));
   d->nentL = totL;
@@ -914,8 +1073,16 @@ int xg_cg_setup(xg_ctx* c, int64_t nrow, const uint64_t* ia, const uint64_t* ja,
   XG_CUDA(c, cudaMemcpyAsync(d->soffU, soffU.data(), soffU.size() * 4, cudaMemcpyHostToDevice, s));
   XG_CUDA(c, cudaMemcpyAsync(d->swU, swU.data(), swU.size() * 4, cudaMemcpyHostToDevice, s));
   XG_CUDA(c, cudaMemcpyAsync(d->colU, colU.data(), colU.size() * 4, cudaMemcpyHostToDevice, s));
+  if (fits16) {
+    XG_CUDA(c, cudaMemcpyAsync(d->colL16, colL16.data(), colL16.size() * 2, cudaMemcpyHostToDevice,
+                               s));
+    XG_CUDA(c, cudaMemcpyAsync(d->colU16, colU16.data(), colU16.size() * 2, cudaMemcpyHostToDevice,
+                               s));
+  }
   XG_CUDA(c, cudaMemsetAsync(d->nvL, 0, colL.size() * 4, s));
   XG_CUDA(c, cudaMemsetAsync(d->nvU, 0, colU.size() * 4, s));
+  XG_CUDA(c, cudaMemsetAsync(d->hvL, 0, colL.size() * 2, s));
+  XG_CUDA(c, cudaMemsetAsync(d->hvU, 0, colU.size() * 2, s));
   XG_CUDA(c, cudaMemsetAsync(d->eU, 0, colU.size() * 4, s));
   XG_CUDA(c, cudaMemsetAsync(d->x, 0, nrow * 8, s));
   XG_CUDA(c, cudaMemsetAsync(d->b, 0, nrow * 8, s));
@@ -934,8 +1101,8 @@ int xg_cg_mult(xg_ctx* c, const double* x, double* y) {
   if (!d) return fail(c, XG_ERR_STATE, "cg_mult before cg_setup");
   if (!x || !y) return fail(c, XG_ERR_ARG, "cg_mult: null vector");
   XG_CUDA(c, cudaMemcpyAsync(d->r, x, d->n * 8, cudaMemcpyHostToDevice, c->stream));
-  k_spmv<<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(d->n, d->soff, d->swidth, d->col,
-                                                              d->a0, d->r, d->q);
+  k_spmv<<<pgrid<k_spmv>(d->n), kBlock, 0, c->stream>>>(d->n, d->soff, d->swidth, d->col, d->a0,
+                                                        d->r, d->q);
   XG_CHECK_LAUNCH(c);
   XG_CUDA(c, cudaMemcpyAsync(y, d->q, d->n * 8, cudaMemcpyDeviceToHost, c->stream));
   XG_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -956,8 +1123,10 @@ int xg_cg_init(xg_ctx* c, const double* x, const double* b, const double* neubc,
   if (b) XG_CUDA(c, cudaMemcpyAsync(d->b, b, n * 8, cudaMemcpyHostToDevice, s));
   d->pc = pc;
   d->apply = apply != 0;
-  d->geom_set = false;
-  d->factor_set = false;
+  // the working matrix depends on the Dirichlet node set only: its scales,
+  // couplings and factor survive re-initialisations with the same set (a
+  // pressure solve per time step)
+  uint64_t key = 1469598103934665603ull;  // FNV-1a over the mask, 0 without BCs
   if (d->apply) {
     std::vector<uint8_t> mask(n, 0);
     std::vector<double> val(n, 0.0);
@@ -967,6 +1136,7 @@ int xg_cg_init(xg_ctx* c, const double* x, const double* b, const double* neubc,
       mask[dirnodes[k]] = 1;
       val[dirnodes[k]] = dirvals[k];
     }
+    for (int64_t i = 0; i < n; ++i) key = (key ^ mask[i]) * 1099511628211ull;
     XG_CUDA(c, cudaMemcpyAsync(d->bcmask, mask.data(), n, cudaMemcpyHostToDevice, s));
     XG_CUDA(c, cudaMemcpyAsync(d->bcval, val.data(), n * 8, cudaMemcpyHostToDevice, s));
     double* neu = nullptr;
@@ -978,71 +1148,36 @@ int xg_cg_init(xg_ctx* c, const double* x, const double* b, const double* neubc,
                                                          d->a, d->a32, d->bcmask, d->bcval, neu,
                                                          d->b);
     XG_CHECK_LAUNCH(c);
+    // mask and val are host vectors of this frame: complete their copies
+    XG_CUDA(c, cudaStreamSynchronize(s));
   } else {
+    key = 0;
     XG_CUDA(c, cudaMemsetAsync(d->bcmask, 0, n, s));
     k_copy_values<<<blocks_for(d->nent, kBlock), kBlock, 0, s>>>(d->nent, d->a0, d->a, d->a32);
     XG_CHECK_LAUNCH(c);
   }
+  if (key != d->bc_key || !d->ready) {
+    d->geom_set = false;
+    d->factor_set = false;
+  }
+  d->bc_key = key;
   CGScalars h{};
   h.pc = pc;
   XG_CUDA(c, cudaMemcpyAsync(d->scal, &h, sizeof(h), cudaMemcpyHostToDevice, s));
-  k_setup<<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, d->soff, d->swidth, d->col, d->a, d->diagpos,
-                                                    d->x, d->b, d->r, d->d, d->z, d->p[0], d->d32,
-                                                    d->partial, d->nblk, d->scal);
+  k_setup<<<pgrid<k_setup>(n), kBlock, 0, s>>>(n, d->soff, d->swidth, d->col, d->a, d->diagpos,
+                                               d->x, d->b, d->r, d->d, d->z, d->p[0], d->d32,
+                                               d->partial, d->scal);
   XG_CHECK_LAUNCH(c);
   if (pc == 2) {
-    int rf = build_factor(c, d);
+    int rf = d->factor_set ? XG_OK : build_factor(c, d);
     if (rf) return rf;
-    const unsigned nb = blocks_for(n, kBlock);
-    k_pc_upper<double><<<nb, kBlock, 0, s>>>(n, tri_u(d), d->nvU, d->srow, d->r, d->u, d->scal);
-    k_pc_lower<double, false><<<nb, kBlock, 0, s>>>(n, tri_l(d), d->nvL, d->srow, d->bcmask, d->u,
-                                                    d->r, d->z, nullptr, d->partial, d->nblk,
-                                                    d->scal);
-    XG_CHECK_LAUNCH(c);
+    rf = factor_apply64(c, d, d->r, d->z);
+    if (rf) return rf;
   }
-  d->cur = 0;
   XG_CUDA(c, cudaStreamSynchronize(s));
   d->ready = true;
   return XG_OK;
 }
-
-namespace {
-int cg_iterate(xg_ctx* c, CGDev* d, int64_t maxit, double tol, CGScalars* h) {
-  cudaStream_t s = c->stream;
-  // tol and maxit into the device scalars without touching the rest
-  XG_CUDA(c, cudaMemcpyAsync(&d->scal->tol, &tol, sizeof(double), cudaMemcpyHostToDevice, s));
-  XG_CUDA(c, cudaMemcpyAsync(&d->scal->maxit, &maxit, sizeof(int64_t), cudaMemcpyHostToDevice, s));
-  const unsigned nb = static_cast<unsigned>(d->nblk);
-  for (;;) {
-    for (int k = 0; k < kBatch; ++k) {
-      double* pold = d->p[d->cur];
-      double* pnew = d->p[d->cur ^ 1];
-      k_iter_a<<<nb, kBlock, 0, s>>>(d->n, d->soff, d->swidth, d->col, d->a, d->z, pold, pnew,
-                                     d->q, d->partial, d->nblk, d->scal);
-      if (d->pc == 2) {
-        k_iter_b<true><<<nb, kBlock, 0, s>>>(d->n, d->q, d->d, pnew, d->r, d->z, d->x, d->partial,
-                                             d->nblk, d->scal);
-        k_pc_upper<double><<<nb, kBlock, 0, s>>>(d->n, tri_u(d), d->nvU, d->srow, d->r, d->u,
-                                                 d->scal);
-        k_pc_lower<double, false><<<nb, kBlock, 0, s>>>(d->n, tri_l(d), d->nvL, d->srow,
-                                                        d->bcmask, d->u, d->r, d->z, nullptr,
-                                                        d->partial, d->nblk, d->scal);
-      } else {
-        k_iter_b<false><<<nb, kBlock, 0, s>>>(d->n, d->q, d->d, pnew, d->r, d->z, d->x,
-                                              d->partial, d->nblk, d->scal);
-      }
-      d->cur ^= 1;
-    }
-    XG_CHECK_LAUNCH(c);
-    int rc = read_scal(c, d, h);
-    if (rc) return rc;
-    if (h->done) break;
-  }
-  // the parity of p buffers only matters while iterating; a finished solve
-  // leaves p unused
-  return XG_OK;
-}
-}  // namespace
 
 int xg_cg_solve(xg_ctx* c, int64_t maxit, double tol, int64_t* it, double* normr,
                 double* normb, int* converged) {
@@ -1072,77 +1207,59 @@ int xg_cg_solve_mixed(xg_ctx* c, int64_t maxit, double tol, double inner_tol,
   if (rc) return rc;
   CGDev* d = c->cg;
   if (!d || !d->ready) return fail(c, XG_ERR_STATE, "cg_solve_mixed before cg_init");
-  if (maxit <= 0 || inner_maxit <= 0 || !(tol >= 0) || !(inner_tol > 0))
+  if (maxit <= 0 || inner_maxit <= 0 || !(tol >= 0) || !(inner_tol > 0) || !(inner_tol < 1))
     return fail(c, XG_ERR_ARG, "cg_solve_mixed: bad limits");
   cudaStream_t s = c->stream;
-  const unsigned nb = static_cast<unsigned>(d->nblk);
   CGScalars h{};
   rc = read_scal(c, d, &h);
   if (rc) return rc;
   const double nb0 = h.normb > 1.0e-14 ? h.normb : 1.0;
-  int64_t nout = 0, nin = 0;
-  double nr = 0.0;
-  bool conv = false;
-  for (;;) {
-    k_outer_res<<<nb, kBlock, 0, s>>>(d->n, d->soff, d->swidth, d->col, d->a, d->x, d->b, d->d32,
-                                      d->r32, d->z32, d->p32[0], d->e32, d->partial, d->nblk,
-                                      d->scal);
-    XG_CHECK_LAUNCH(c);
-    if (d->pc == 2) {
-      k_pc_upper<float><<<nb, kBlock, 0, s>>>(d->n, tri_u(d), d->nvU, d->srow, d->r32, d->u32,
-                                              d->scal);
-      k_pc_lower<float, false><<<nb, kBlock, 0, s>>>(d->n, tri_l(d), d->nvL, d->srow, d->bcmask,
-                                                     d->u32, d->r32, d->z32, nullptr, d->partial,
-                                                     d->nblk, d->scal);
-      XG_CHECK_LAUNCH(c);
-    }
-    rc = read_scal(c, d, &h);
+  XG_CUDA(c, cudaMemsetAsync(d->e32, 0, d->n * 4, s));
+  // the first FP32 iteration reads p with weight beta = 0: make it finite
+  XG_CUDA(c, cudaMemsetAsync(d->p32[0], 0, d->n * 4, s));
+  XG_CUDA(c, cudaMemsetAsync(d->p32[1], 0, d->n * 4, s));
+  rc = replace_residual(c, d, 1);
+  if (rc) return rc;
+  rc = read_scal(c, d, &h);
+  if (rc) return rc;
+  double nr = std::sqrt(h.rr);
+  int64_t nout = 0;
+  bool conv = nr < tol * nb0;
+  int breakdown = 0;
+  while (!conv && nout < maxit && h.it < inner_maxit && !breakdown) {
+    h.tol = tol;
+    h.delta = inner_tol;
+    h.rlast = nr;
+    h.maxit = inner_maxit;
+    h.done = 0;
+    rc = write_scal(c, d, &h);
     if (rc) return rc;
-    nr = std::sqrt(h.rr);
-    if (nr < tol * nb0) {
-      conv = true;
-      break;
-    }
-    if (nout >= maxit || nin >= maxit * inner_maxit) break;
-    k_set_inner<<<1, 1, 0, s>>>(d->scal, inner_tol, inner_maxit);
-    XG_CHECK_LAUNCH(c);
-    int cur = 0;
     for (;;) {
-      for (int k = 0; k < kBatch; ++k) {
-        k_in_a<<<nb, kBlock, 0, s>>>(d->n, d->soff, d->swidth, d->col, d->a32, d->z32,
-                                     d->p32[cur], d->p32[cur ^ 1], d->q32, d->partial, d->nblk,
-                                     d->scal);
-        if (d->pc == 2) {
-          k_in_b<true><<<nb, kBlock, 0, s>>>(d->n, d->q32, d->d32, d->p32[cur ^ 1], d->r32,
-                                             d->z32, d->e32, d->partial, d->nblk, d->scal);
-          k_pc_upper<float><<<nb, kBlock, 0, s>>>(d->n, tri_u(d), d->nvU, d->srow, d->r32,
-                                                  d->u32, d->scal);
-          k_pc_lower<float, false><<<nb, kBlock, 0, s>>>(d->n, tri_l(d), d->nvL, d->srow,
-                                                         d->bcmask, d->u32, d->r32, d->z32,
-                                                         nullptr, d->partial, d->nblk, d->scal);
-        } else {
-          k_in_b<false><<<nb, kBlock, 0, s>>>(d->n, d->q32, d->d32, d->p32[cur ^ 1], d->r32,
-                                              d->z32, d->e32, d->partial, d->nblk, d->scal);
-        }
-        cur ^= 1;
-      }
-      XG_CHECK_LAUNCH(c);
+      rc = d->use16 ? mixed_batch<Cols16>(c, d, Cols16{d->col16}, Cols16{d->colU16},
+                                          Cols16{d->colL16})
+                    : mixed_batch<Cols32>(c, d, Cols32{d->col}, Cols32{d->colU}, Cols32{d->colL});
+      if (rc) return rc;
       rc = read_scal(c, d, &h);
       if (rc) return rc;
       if (h.done) break;
     }
-    nin += h.it;
+    breakdown = h.finished;
     k_add_correction<<<blocks_for(d->n, kBlock), kBlock, 0, s>>>(d->n, d->e32, d->x);
     XG_CHECK_LAUNCH(c);
+    rc = replace_residual(c, d, 0);
+    if (rc) return rc;
+    rc = read_scal(c, d, &h);
+    if (rc) return rc;
+    nr = std::sqrt(h.rr);
     ++nout;
+    conv = nr < tol * nb0;
   }
-  d->last_it = nin;
-  d->inner_its = nin;
+  d->last_it = h.it;
   d->last_normr = nr;
   d->last_normb = nb0;
   d->last_conv = conv;
   if (outer) *outer = nout;
-  if (inner) *inner = nin;
+  if (inner) *inner = h.it;
   if (normr) *normr = nr;
   if (normb) *normb = nb0;
   if (converged) *converged = conv ? 1 : 0;
@@ -1167,29 +1284,29 @@ int xg_cg_precondition(xg_ctx* c, const double* r, double* z) {
   if (!d || !d->ready) return fail(c, XG_ERR_STATE, "cg_precondition before cg_init");
   if (!r || !z) return fail(c, XG_ERR_ARG, "cg_precondition: null vector");
   cudaStream_t s = c->stream;
-  const unsigned nb = blocks_for(d->n, kBlock);
   XG_CUDA(c, cudaMemcpyAsync(d->q, r, d->n * 8, cudaMemcpyHostToDevice, s));
-  // a scratch copy of the scalars with done = 0 so the passes run
+  // the passes run only while the solve is not done: save the scalars, clear
+  // done, restore them afterwards
   CGScalars h{};
-  CGScalars* sc = d->scal + 0;
-  XG_CUDA(c, cudaMemcpyAsync(&h, sc, sizeof(h), cudaMemcpyDeviceToHost, s));
-  XG_CUDA(c, cudaStreamSynchronize(s));
-  int32_t zero = 0;
-  XG_CUDA(c, cudaMemcpyAsync(&sc->done, &zero, sizeof(int32_t), cudaMemcpyHostToDevice, s));
+  rc = read_scal(c, d, &h);
+  if (rc) return rc;
+  CGScalars run = h;
+  run.done = 0;
+  rc = write_scal(c, d, &run);
+  if (rc) return rc;
   if (d->pc == 2) {
     if (!d->factor_set) {
       rc = build_factor(c, d);
       if (rc) return rc;
     }
-    k_pc_upper<double><<<nb, kBlock, 0, s>>>(d->n, tri_u(d), d->nvU, d->srow, d->q, d->u, sc);
-    k_pc_lower<double, false><<<nb, kBlock, 0, s>>>(d->n, tri_l(d), d->nvL, d->srow, d->bcmask,
-                                                    d->u, d->q, d->t, nullptr, d->partial,
-                                                    d->nblk, sc);
+    rc = factor_apply64(c, d, d->q, d->t);
+    if (rc) return rc;
   } else {
-    k_jacobi_apply<<<nb, kBlock, 0, s>>>(d->n, d->q, d->d, d->t);
+    k_jacobi_apply<<<blocks_for(d->n, kBlock), kBlock, 0, s>>>(d->n, d->q, d->d, d->t);
+    XG_CHECK_LAUNCH(c);
   }
-  XG_CHECK_LAUNCH(c);
-  XG_CUDA(c, cudaMemcpyAsync(sc, &h, sizeof(h), cudaMemcpyHostToDevice, s));
+  rc = write_scal(c, d, &h);
+  if (rc) return rc;
   XG_CUDA(c, cudaMemcpyAsync(z, d->t, d->n * 8, cudaMemcpyDeviceToHost, s));
   XG_CUDA(c, cudaStreamSynchronize(s));
   return XG_OK;

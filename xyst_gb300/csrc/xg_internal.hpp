@@ -78,7 +78,7 @@ struct LpcGraph {
 int cg_graph(xg_ctx* c, LpcGraph* g);
 
 // Learned factor (xg_learn.cu): runs the network on g and writes the factor
-// values, lower layout N_ij (nvL) and upper layout N_ij s_i (nvU).
+// values N_ij in the lower layout (nvL) and, transposed, the upper one (nvU).
 int lpc_factor(xg_ctx* c, xg_lpc* m, const LpcGraph& g, float* nvL, float* nvU);
 
 void destroy_riecg(RieCGDev*);

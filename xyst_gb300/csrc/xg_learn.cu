@@ -58,7 +58,8 @@ constexpr int64_t oW3 = ob2 + H;
 constexpr int64_t ob3 = oW3 + 2 * H * H;
 constexpr int64_t oWo = ob3 + H;
 constexpr int64_t oc = oWo + 2 * H * H;
-constexpr int64_t od = oc + H;
+constexpr int64_t oc2 = oc + H;
+constexpr int64_t od = oc2 + H;
 constexpr int64_t ow = od + H;
 constexpr int64_t oob = ow + H;
 constexpr int64_t kNParams = oob + 1;
@@ -110,18 +111,20 @@ __global__ void k_features(int64_t n, const int32_t* __restrict__ soff,
   if (i >= n) return;
   const int lane = int(i & 31);
   const int32_t off = soff[i >> 5], w = sw[i >> 5];
-  float rs = 0.f;
+  float rs = 0.f, r2 = 0.f;
   int deg = 0;
   for (int k = 0; k < w; ++k) {
     const int32_t p = off + k * kSlice + lane;
     const int32_t j = col[p];
     if (j < 0) continue;
     if (j != i) ++deg;
-    rs += eF[p];
+    const float e = eF[p];
+    rs += e;
+    r2 += e * e;
   }
-  x4[i * 4 + 0] = 1.f;
-  x4[i * 4 + 1] = mask[i] ? 1.f : 0.f;
-  x4[i * 4 + 2] = rs;
+  x4[i * 4 + 0] = mask[i] ? 1.f : 0.f;
+  x4[i * 4 + 1] = rs;
+  x4[i * 4 + 2] = r2;
   x4[i * 4 + 3] = float(deg) / 16.f;
 }
 
@@ -389,110 +392,126 @@ __global__ void k_reduce_parts(const float* __restrict__ part, int nblk, int nou
 
 struct EdgeParams {
   const float* c;
+  const float* c2;
   const float* d;
   const float* w;
   const float* ob;
 };
 
 EdgeParams edge_params(const float* theta) {
-  return EdgeParams{theta + oc, theta + od, theta + ow, theta + oob};
+  return EdgeParams{theta + oc, theta + oc2, theta + od, theta + ow, theta + oob};
 }
 
+// Edge inputs of unit pair (2 lane, 2 lane + 1): c, c2, d, w.
+struct EdgeLane {
+  float2 c, c2, d, w;
+  __device__ EdgeLane(const EdgeParams& P, int lane)
+      : c(reinterpret_cast<const float2*>(P.c)[lane]),
+        c2(reinterpret_cast<const float2*>(P.c2)[lane]),
+        d(reinterpret_cast<const float2*>(P.d)[lane]),
+        w(reinterpret_cast<const float2*>(P.w)[lane]) {}
+  __device__ float2 z(float2 ai, float2 bj, float e, float t) const {
+    return make_float2(ai.x + bj.x + c.x * e + c2.x * t + d.x, ai.y + bj.y + c.y * e + c2.y * t + d.y);
+  }
+};
+
 // Forward over the lower edges (warp per row i, lane = units 2 lane, 2 lane + 1).
-// N_ij = e_ij (1 + 2 tanh o_ij).  Inference writes nvL = N_ij and
-// nvU[tposU] = N_ij s_i; training writes the plain N in both layouts and
-// tanh(o) in tL.
+// N_ij = (e_ij + t_ij) (1 + tanh o_ij), written to the lower layout and,
+// transposed, the upper one; training also keeps tanh(o) in thL.  t_ij is read
+// from the upper layout (tU).
 template <bool TRAIN>
 __global__ void __launch_bounds__(kThreads) k_edge_fwd(int64_t n, const int32_t* __restrict__ soffL,
                                                        const int32_t* __restrict__ swL,
                                                        const int32_t* __restrict__ colL,
                                                        const float* __restrict__ eL,
                                                        const int32_t* __restrict__ tposU,
-                                                       const float* __restrict__ srow,
+                                                       const float* __restrict__ tU,
                                                        const float* __restrict__ A,
                                                        const float* __restrict__ B, EdgeParams P,
                                                        float* __restrict__ nL,
                                                        float* __restrict__ nU,
-                                                       float* __restrict__ tL) {
+                                                       float* __restrict__ thL) {
   const int64_t i = blockIdx.x * int64_t(kRowsPerBlock) + (threadIdx.x >> 5);
   if (i >= n) return;
   const int lane = threadIdx.x & 31;
   const int li = int(i & 31);
   const int32_t off = soffL[i >> 5], w = swL[i >> 5];
   const float2 ai = reinterpret_cast<const float2*>(A + i * H)[lane];
-  const float2 cc = reinterpret_cast<const float2*>(P.c)[lane];
-  const float2 dd = reinterpret_cast<const float2*>(P.d)[lane];
-  const float2 ww = reinterpret_cast<const float2*>(P.w)[lane];
+  const EdgeLane E(P, lane);
   const float ob = *P.ob;
-  const float si = srow[i];
   for (int k = 0; k < w; ++k) {
     const int32_t p = off + k * kSlice + li;
     const int32_t j = __ldg(colL + p);
     if (j < 0) continue;
     const float e = __ldg(eL + p);
-    float nv = 0.f, t = 0.f;
-    if (e != 0.f) {
+    const int32_t pu = tposU[p];
+    const float t = tU[pu];
+    float nv = 0.f, th = 0.f;
+    // e = t = 0 on edges at Dirichlet nodes (N = 0 there); a zero coupling
+    // elsewhere can still carry a second-order term
+    if (e != 0.f || t != 0.f) {
       const float2 bj = __ldg(reinterpret_cast<const float2*>(B + int64_t(j) * H) + lane);
-      const float z0 = ai.x + bj.x + cc.x * e + dd.x;
-      const float z1 = ai.y + bj.y + cc.y * e + dd.y;
-      const float o = warp_sum(ww.x * relu(z0) + ww.y * relu(z1)) + ob;
-      t = tanhf(o);
-      nv = e * (1.f + 2.f * t);
+      const float2 z = E.z(ai, bj, e, t);
+      const float o = warp_sum(E.w.x * relu(z.x) + E.w.y * relu(z.y)) + ob;
+      th = tanhf(o);
+      nv = (e + t) * (1.f + th);
     }
     if (lane == 0) {
       nL[p] = nv;
-      nU[tposU[p]] = TRAIN ? nv : nv * si;
-      if (TRAIN) tL[p] = t;
+      nU[pu] = nv;
+      if (TRAIN) thL[p] = th;
     }
   }
 }
 
 // Backward over the lower edges: d loss / d N_ij (upper layout, from
-// k_kaporin) through tanh and the edge MLP.  da_i (sum over the row's edges) is written
+// k_cross) through tanh and the edge MLP.  da_i (sum over the row's edges) is written
 // per row; do_ij goes to the upper layout for the b_j pass; the gradients of
-// c, d, w, ob leave as per-block partials (fixed order).
+// c, c2, d, w, ob leave as per-block partials (fixed order).
+constexpr int kEdgeParts = 4 * H + 1;
 __global__ void __launch_bounds__(kThreads) k_edge_bwd_lower(
     int64_t n, const int32_t* __restrict__ soffL, const int32_t* __restrict__ swL,
     const int32_t* __restrict__ colL, const float* __restrict__ eL,
-    const int32_t* __restrict__ tposU, const float* __restrict__ tL, const float* __restrict__ A,
-    const float* __restrict__ B, EdgeParams P, const float* __restrict__ dnU,
-    float* __restrict__ da, float* __restrict__ doU, float* __restrict__ part) {
-  constexpr int NOUT = 3 * H + 1;
+    const int32_t* __restrict__ tposU, const float* __restrict__ tU,
+    const float* __restrict__ thL, const float* __restrict__ A, const float* __restrict__ B,
+    EdgeParams P, const float* __restrict__ dnU, float* __restrict__ da, float* __restrict__ doU,
+    float* __restrict__ part) {
+  constexpr int NOUT = kEdgeParts;
   __shared__ float red[kRowsPerBlock][NOUT];
   const int64_t i = blockIdx.x * int64_t(kRowsPerBlock) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  float2 gw = make_float2(0.f, 0.f), gc = gw, gd = gw, dai = gw;
+  float2 gw = make_float2(0.f, 0.f), gc = gw, gc2 = gw, gd = gw, dai = gw;
   float gob = 0.f;
   if (i < n) {
     const int li = int(i & 31);
     const int32_t off = soffL[i >> 5], w = swL[i >> 5];
     const float2 ai = reinterpret_cast<const float2*>(A + i * H)[lane];
-    const float2 cc = reinterpret_cast<const float2*>(P.c)[lane];
-    const float2 dd = reinterpret_cast<const float2*>(P.d)[lane];
-    const float2 ww = reinterpret_cast<const float2*>(P.w)[lane];
+    const EdgeLane E(P, lane);
     for (int k = 0; k < w; ++k) {
       const int32_t p = off + k * kSlice + li;
       const int32_t j = __ldg(colL + p);
       if (j < 0) continue;
       const float e = __ldg(eL + p);
-      if (e == 0.f) {
-        if (lane == 0) doU[tposU[p]] = 0.f;
+      const int32_t pu = tposU[p];
+      const float t = tU[pu];
+      if (e == 0.f && t == 0.f) {
+        if (lane == 0) doU[pu] = 0.f;
         continue;
       }
-      const int32_t pu = tposU[p];
-      const float t = tL[p];
-      const float dov = dnU[pu] * 2.f * e * (1.f - t * t);
+      const float th = thL[p];
+      const float dov = dnU[pu] * (e + t) * (1.f - th * th);
       const float2 bj = __ldg(reinterpret_cast<const float2*>(B + int64_t(j) * H) + lane);
-      const float z0 = ai.x + bj.x + cc.x * e + dd.x;
-      const float z1 = ai.y + bj.y + cc.y * e + dd.y;
-      const float dz0 = z0 > 0.f ? dov * ww.x : 0.f;
-      const float dz1 = z1 > 0.f ? dov * ww.y : 0.f;
+      const float2 z = E.z(ai, bj, e, t);
+      const float dz0 = z.x > 0.f ? dov * E.w.x : 0.f;
+      const float dz1 = z.y > 0.f ? dov * E.w.y : 0.f;
       dai.x += dz0;
       dai.y += dz1;
-      gw.x += dov * relu(z0);
-      gw.y += dov * relu(z1);
+      gw.x += dov * relu(z.x);
+      gw.y += dov * relu(z.y);
       gc.x += dz0 * e;
       gc.y += dz1 * e;
+      gc2.x += dz0 * t;
+      gc2.y += dz1 * t;
       gd.x += dz0;
       gd.y += dz1;
       gob += dov;
@@ -502,11 +521,13 @@ __global__ void __launch_bounds__(kThreads) k_edge_bwd_lower(
   }
   red[wid][2 * lane] = gc.x;
   red[wid][2 * lane + 1] = gc.y;
-  red[wid][H + 2 * lane] = gd.x;
-  red[wid][H + 2 * lane + 1] = gd.y;
-  red[wid][2 * H + 2 * lane] = gw.x;
-  red[wid][2 * H + 2 * lane + 1] = gw.y;
-  if (lane == 0) red[wid][3 * H] = gob;
+  red[wid][H + 2 * lane] = gc2.x;
+  red[wid][H + 2 * lane + 1] = gc2.y;
+  red[wid][2 * H + 2 * lane] = gd.x;
+  red[wid][2 * H + 2 * lane + 1] = gd.y;
+  red[wid][3 * H + 2 * lane] = gw.x;
+  red[wid][3 * H + 2 * lane + 1] = gw.y;
+  if (lane == 0) red[wid][4 * H] = gob;
   __syncthreads();
   for (int k = threadIdx.x; k < NOUT; k += kThreads) {
     float s = 0.f;
@@ -518,18 +539,16 @@ __global__ void __launch_bounds__(kThreads) k_edge_bwd_lower(
 // Backward to b_j: warp per row j over its upper entries (j, i), i > j.
 __global__ void __launch_bounds__(kThreads) k_edge_bwd_upper(
     int64_t n, const int32_t* __restrict__ soffU, const int32_t* __restrict__ swU,
-    const int32_t* __restrict__ colU, const float* __restrict__ eU, const float* __restrict__ doU,
-    const float* __restrict__ A, const float* __restrict__ B, EdgeParams P,
-    float* __restrict__ db) {
+    const int32_t* __restrict__ colU, const float* __restrict__ eU, const float* __restrict__ tU,
+    const float* __restrict__ doU, const float* __restrict__ A, const float* __restrict__ B,
+    EdgeParams P, float* __restrict__ db) {
   const int64_t j = blockIdx.x * int64_t(kRowsPerBlock) + (threadIdx.x >> 5);
   if (j >= n) return;
   const int lane = threadIdx.x & 31;
   const int lj = int(j & 31);
   const int32_t off = soffU[j >> 5], w = swU[j >> 5];
   const float2 bj = reinterpret_cast<const float2*>(B + j * H)[lane];
-  const float2 cc = reinterpret_cast<const float2*>(P.c)[lane];
-  const float2 dd = reinterpret_cast<const float2*>(P.d)[lane];
-  const float2 ww = reinterpret_cast<const float2*>(P.w)[lane];
+  const EdgeLane E(P, lane);
   float2 acc = make_float2(0.f, 0.f);
   for (int k = 0; k < w; ++k) {
     const int32_t p = off + k * kSlice + lj;
@@ -539,10 +558,9 @@ __global__ void __launch_bounds__(kThreads) k_edge_bwd_upper(
     if (dov == 0.f) continue;
     const float e = __ldg(eU + p);
     const float2 ai = __ldg(reinterpret_cast<const float2*>(A + int64_t(i) * H) + lane);
-    const float z0 = ai.x + bj.x + cc.x * e + dd.x;
-    const float z1 = ai.y + bj.y + cc.y * e + dd.y;
-    if (z0 > 0.f) acc.x += dov * ww.x;
-    if (z1 > 0.f) acc.y += dov * ww.y;
+    const float2 z = E.z(ai, bj, e, tU[p]);
+    if (z.x > 0.f) acc.x += dov * E.w.x;
+    if (z.y > 0.f) acc.y += dov * E.w.y;
   }
   reinterpret_cast<float2*>(db + j * H)[lane] = acc;
 }
@@ -551,10 +569,12 @@ __global__ void __launch_bounds__(kThreads) k_edge_bwd_upper(
 
 // Thread per column j (the upper-layout row j lists the lower edges (i, j)):
 // for each of its edges the cross term sum_{k != i} e_ik n_kj, found by
-// walking row i of the full layout and searching row j's sorted upper list;
-// writes d loss / d n_ij (upper layout) and per-block partials of the
-// columns' loss terms (times n).
-__global__ void __launch_bounds__(kThreads) k_kaporin(int64_t n, const int32_t* __restrict__ soff,
+// walking row i of the full layout and searching row j's sorted upper list.
+// LOSS: writes d loss / d n_ij (upper layout) and per-block partials of the
+// columns' loss terms (times n); otherwise writes the cross term itself
+// (with n = e: the edge feature t).
+template <bool LOSS>
+__global__ void __launch_bounds__(kThreads) k_cross(int64_t n, const int32_t* __restrict__ soff,
                                                       const int32_t* __restrict__ sw,
                                                       const int32_t* __restrict__ col,
                                                       const float* __restrict__ eF,
@@ -598,12 +618,18 @@ __global__ void __launch_bounds__(kThreads) k_kaporin(int64_t n, const int32_t* 
         if (lo < wj && colU[offj + lo * kSlice + lane] == c)
           cross += eik * nU[offj + lo * kSlice + lane];
       }
-      dnU[pa] = two_n * (na - ea - cross);
-      lj += double(na) * (-2.0 * double(ea) + double(na) - double(cross));
+      if (LOSS) {
+        dnU[pa] = two_n * (na - ea - cross);
+        lj += double(na) * (-2.0 * double(ea) + double(na) - double(cross));
+      } else {
+        dnU[pa] = cross;
+      }
     }
   }
-  const double t = block_sum(lj);
-  if (threadIdx.x == 0) part[blockIdx.x] = t;
+  if (LOSS) {
+    const double t = block_sum(lj);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+  }
 }
 
 // out[slot] = sum of nblk partials, fixed order.
@@ -650,7 +676,8 @@ struct xg_lpc {
   float *x4 = nullptr, *h[4] = {}, *mh[4] = {}, *A = nullptr, *B = nullptr;
   float *da = nullptr, *db = nullptr, *du = nullptr, *du2 = nullptr, *dih = nullptr,
         *dim = nullptr;
-  float *nL = nullptr, *tL = nullptr, *nU = nullptr, *doU = nullptr, *dnU = nullptr;
+  float *nL = nullptr, *tL = nullptr, *nU = nullptr, *doU = nullptr, *dnU = nullptr,
+        *tU = nullptr;
   double* dpart = nullptr;
   float* epart = nullptr;  // edge-parameter partials, one row per block
 };
@@ -684,8 +711,9 @@ int ensure_work(xg_ctx* c, xg_lpc* m, int64_t n, int64_t nl, int64_t nu) {
     W.plan(m->nU, std::max<int64_t>(1, U));
     W.plan(m->doU, std::max<int64_t>(1, U));
     W.plan(m->dnU, std::max<int64_t>(1, U));
+    W.plan(m->tU, std::max<int64_t>(1, U));
     W.plan(m->dpart, nblk);
-    W.plan(m->epart, nrb * (3 * H + 1));
+    W.plan(m->epart, nrb * kEdgeParts);
     if (pass == 0) {
       cudaError_t e = W.reserve();
       if (e != cudaSuccess) {
@@ -748,6 +776,14 @@ int forward_nodes(xg_ctx* c, xg_lpc* m, const LpcGraph& g) {
   return XG_OK;
 }
 
+// t_ij = sum_{k > j, k != i} e_ik e_kj in the upper layout (m->tU).
+int edge_feature(xg_ctx* c, xg_lpc* m, const LpcGraph& g) {
+  k_cross<false><<<blocks_for(g.n, kThreads), kThreads, 0, c->stream>>>(
+      g.n, g.soff, g.sw, g.col, g.eF, g.soffU, g.swU, g.colU, g.eU, g.eU, m->tU, nullptr);
+  XG_CHECK_LAUNCH(c);
+  return XG_OK;
+}
+
 template <int K1, int K2, int N, bool BIAS>
 int wgrad(xg_ctx* c, xg_lpc* m, int64_t n, const float* X1, const float* X2, const float* dY1,
           const float* dY2, int64_t wofs, int64_t bofs) {
@@ -770,8 +806,10 @@ int lpc_factor(xg_ctx* c, xg_lpc* m, const LpcGraph& g, float* nvL, float* nvU) 
   if (rc) return rc;
   rc = forward_nodes(c, m, g);
   if (rc) return rc;
+  rc = edge_feature(c, m, g);
+  if (rc) return rc;
   k_edge_fwd<false><<<blocks_for(g.n, kRowsPerBlock), kThreads, 0, c->stream>>>(
-      g.n, g.soffL, g.swL, g.colL, g.eL, g.tposU, g.srow, m->A, m->B, edge_params(m->theta), nvL,
+      g.n, g.soffL, g.swL, g.colL, g.eL, g.tposU, m->tU, m->A, m->B, edge_params(m->theta), nvL,
       nvU, nullptr);
   XG_CHECK_LAUNCH(c);
   return XG_OK;
@@ -904,20 +942,23 @@ int xg_lpc_grad(xg_lpc* m, xg_ctx* c, double* loss) {
   const EdgeParams P = edge_params(m->theta);
   rc = forward_nodes(c, m, g);
   if (rc) return rc;
-  k_edge_fwd<true><<<nrb, kThreads, 0, s>>>(n, g.soffL, g.swL, g.colL, g.eL, g.tposU, g.srow,
+  rc = edge_feature(c, m, g);
+  if (rc) return rc;
+  k_edge_fwd<true><<<nrb, kThreads, 0, s>>>(n, g.soffL, g.swL, g.colL, g.eL, g.tposU, m->tU,
                                             m->A, m->B, P, m->nL, m->nU, m->tL);
   XG_CHECK_LAUNCH(c);
   // trace loss and d loss / d N
-  k_kaporin<<<nb, kThreads, 0, s>>>(n, g.soff, g.sw, g.col, g.eF, g.soffU, g.swU, g.colU, g.eU,
-                                    m->nU, m->dnU, m->dpart);
+  k_cross<true><<<nb, kThreads, 0, s>>>(n, g.soff, g.sw, g.col, g.eF, g.soffU, g.swU, g.colU,
+                                        g.eU, m->nU, m->dnU, m->dpart);
   k_sum_parts<<<1, kThreads, 0, s>>>(m->dpart, nb, m->lossv, 0);
   XG_CHECK_LAUNCH(c);
   // edge backward
-  k_edge_bwd_lower<<<nrb, kThreads, 0, s>>>(n, g.soffL, g.swL, g.colL, g.eL, g.tposU, m->tL,
-                                            m->A, m->B, P, m->dnU, m->da, m->doU, m->epart);
-  k_reduce_parts<<<1, 256, 0, s>>>(m->epart, int(nrb), 3 * H + 1, 3 * H + 1, oc, 0, m->grad);
-  k_edge_bwd_upper<<<nrb, kThreads, 0, s>>>(n, g.soffU, g.swU, g.colU, g.eU, m->doU, m->A, m->B,
-                                            P, m->db);
+  k_edge_bwd_lower<<<nrb, kThreads, 0, s>>>(n, g.soffL, g.swL, g.colL, g.eL, g.tposU, m->tU,
+                                            m->tL, m->A, m->B, P, m->dnU, m->da, m->doU,
+                                            m->epart);
+  k_reduce_parts<<<1, 512, 0, s>>>(m->epart, int(nrb), kEdgeParts, kEdgeParts, oc, 0, m->grad);
+  k_edge_bwd_upper<<<nrb, kThreads, 0, s>>>(n, g.soffU, g.swU, g.colU, g.eU, m->tU, m->doU, m->A,
+                                            m->B, P, m->db);
   XG_CHECK_LAUNCH(c);
   // output layer: dWo = h3^T [da | db]; du3 = ([da | db] Wo^T) o [h3 > 0]
   const unsigned ngemm = static_cast<unsigned>(std::min<int64_t>(blocks_for(n, 32), 4 * 148));

@@ -97,12 +97,13 @@ class LearnedPreconditioner:
 H = 64
 SHAPES = [("W0", (4, H)), ("b0", (H,)), ("W1", (2 * H, H)), ("b1", (H,)),
           ("W2", (2 * H, H)), ("b2", (H,)), ("W3", (2 * H, H)), ("b3", (H,)),
-          ("Wo", (H, 2 * H)), ("c", (H,)), ("d", (H,)), ("w", (H,)), ("ob", (1,))]
+          ("Wo", (H, 2 * H)), ("c", (H,)), ("c2", (H,)), ("d", (H,)), ("w", (H,)),
+          ("ob", (1,))]
 
 
 def init_params(seed=0, wscale=0.0):
     """He-initialised weights, zero biases; w = wscale * N(0, 1/H) (0: the
-    network starts as the first-order factor N = e)."""
+    network starts as the second-order factor N = e + t)."""
     rng = np.random.default_rng(seed)
     out = []
     for name, shp in SHAPES:
