@@ -70,18 +70,19 @@ struct RieCGDev {
   // adjacency
   int32_t *soff = nullptr, *swidth = nullptr;
   void* ent = nullptr;  // int4 (FP32 mode) or Ent64 (FP64 mode) per entry
-  // half-edge lists of the residual: edges a node is the first end of (with
-  // the flux slot at the entry's own index) and the flux slots of the edges it
-  // is the second end of
+  // half-edge lists of the residual: the edges a node owns (list 1, with
+  // the position of each edge in its other end's list) and the edges its
+  // neighbours own (list 2, whose slots receive those owners' fluxes)
   int64_t nent1 = 0, nent2 = 0;
-  int32_t *soff1 = nullptr, *sw1 = nullptr, *soff2 = nullptr, *sw2 = nullptr, *slot2 = nullptr;
+  int32_t *soff1 = nullptr, *sw1 = nullptr, *soff2 = nullptr, *sw2 = nullptr, *pos1 = nullptr;
   void* ent1 = nullptr;
-  void* fbuf = nullptr;  // F [5][nent1] edge fluxes
+  void* fbuf = nullptr;  // F: [nent2][4] components 0-3, then [nent2] component 4
   void* Rp = nullptr;    // F [5][n] first-end partial residuals
   double* ivol = nullptr;
   float* cbrtv = nullptr;
   // boundary triangles, per boundary node lists of (tri << 2 | position)
-  int32_t *bptr = nullptr, *bent = nullptr, *btri = nullptr;
+  int32_t *bptr = nullptr, *bent = nullptr, *btri = nullptr, *bnode = nullptr;
+  void* Rb = nullptr;  // F [5][nbn] domain residual of the boundary nodes
   uint8_t* bsym = nullptr;
   uint8_t* bcflag = nullptr;  // per boundary node: has a nodal BC
   // BC program: one thread per BC node
@@ -134,29 +135,36 @@ size_t bytes_riecg(const RieCGDev* d) {
 
 namespace {
 
+// Record loads and stores as single 256-bit accesses (one 32-byte sector per
+// lane: half the L1 wavefronts of two 128-bit accesses on scattered rows).
+// Loads use the read-only path: every record read this way is either not
+// written by the kernel or read before the same thread overwrites it.
 __device__ __forceinline__ void load8(const float* p, float o[8]) {
-  float4 a = __ldg(reinterpret_cast<const float4*>(p));
-  float4 b = __ldg(reinterpret_cast<const float4*>(p) + 1);
-  o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
-  o[4] = b.x; o[5] = b.y; o[6] = b.z; o[7] = b.w;
+  asm volatile("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=f"(o[0]), "=f"(o[1]), "=f"(o[2]), "=f"(o[3]), "=f"(o[4]), "=f"(o[5]),
+                 "=f"(o[6]), "=f"(o[7])
+               : "l"(p));
 }
 __device__ __forceinline__ void load8(const double* p, double o[8]) {
-  const double2* q = reinterpret_cast<const double2*>(p);
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    double2 a = __ldg(q + i);
-    o[2 * i] = a.x;
-    o[2 * i + 1] = a.y;
-  }
+  asm volatile("ld.global.nc.v4.f64 {%0,%1,%2,%3}, [%4];"
+               : "=d"(o[0]), "=d"(o[1]), "=d"(o[2]), "=d"(o[3])
+               : "l"(p));
+  asm volatile("ld.global.nc.v4.f64 {%0,%1,%2,%3}, [%4];"
+               : "=d"(o[4]), "=d"(o[5]), "=d"(o[6]), "=d"(o[7])
+               : "l"(p + 4));
 }
 __device__ __forceinline__ void store8(float* p, const float o[8]) {
-  reinterpret_cast<float4*>(p)[0] = make_float4(o[0], o[1], o[2], o[3]);
-  reinterpret_cast<float4*>(p)[1] = make_float4(o[4], o[5], o[6], o[7]);
+  asm volatile("st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(p), "f"(o[0]), "f"(o[1]),
+               "f"(o[2]), "f"(o[3]), "f"(o[4]), "f"(o[5]), "f"(o[6]), "f"(o[7])
+               : "memory");
 }
 __device__ __forceinline__ void store8(double* p, const double o[8]) {
-  double2* q = reinterpret_cast<double2*>(p);
-#pragma unroll
-  for (int i = 0; i < 4; ++i) q[i] = make_double2(o[2 * i], o[2 * i + 1]);
+  asm volatile("st.global.v4.f64 [%0], {%1,%2,%3,%4};" ::"l"(p), "d"(o[0]), "d"(o[1]), "d"(o[2]),
+               "d"(o[3])
+               : "memory");
+  asm volatile("st.global.v4.f64 [%0], {%1,%2,%3,%4};" ::"l"(p + 4), "d"(o[4]), "d"(o[5]),
+               "d"(o[6]), "d"(o[7])
+               : "memory");
 }
 template <class F>
 __device__ __forceinline__ void load16(const F* p, F o[16]) {
@@ -167,6 +175,36 @@ template <class F>
 __device__ __forceinline__ void store16(F* p, const F o[16]) {
   store8(p, o);
   store8(p + 8, o + 8);
+}
+
+// Five primitives of a W record (the coordinates in slots 5-7 are not read).
+__device__ __forceinline__ void load5(const float* p, float o[5]) {
+  const float4 a = __ldg(reinterpret_cast<const float4*>(p));
+  o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+  o[4] = __ldg(p + 4);
+}
+__device__ __forceinline__ void load5(const double* p, double o[5]) {
+  const double2* q = reinterpret_cast<const double2*>(p);
+  const double2 a = __ldg(q), b = __ldg(q + 1);
+  o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
+  o[4] = __ldg(p + 4);
+}
+
+// Asynchronous global -> shared copies (cp.async, 16 bytes, L2 only) with
+// their commit/wait group fences.  The adjacency entries a thread will need
+// are streamed into a per-thread ring in shared memory several iterations
+// ahead, so the coalesced entry stream stays in flight while the thread waits
+// on its gathers.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
 // Primitive variables from conserved ones (primitive(),
@@ -423,6 +461,37 @@ __device__ __forceinline__ void load_ent(const Ent64* ent, int32_t e, int32_t& q
   q = __double2loint(b.y);
 }
 
+// Ring entries: copy one entry into its shared-memory slot, decode a landed one.
+template <class E>
+__device__ __forceinline__ void fetch_ent(E* slot, const E* g) {
+#pragma unroll
+  for (int i = 0; i < int(sizeof(E) / 16); ++i)
+    cp_async16(reinterpret_cast<char*>(slot) + 16 * i, reinterpret_cast<const char*>(g) + 16 * i);
+}
+__device__ __forceinline__ void dec_ent(const int4* slot, int32_t& q, float& d0, float& d1,
+                                        float& d2) {
+  const int4 v = *slot;
+  q = v.x;
+  d0 = __int_as_float(v.y);
+  d1 = __int_as_float(v.z);
+  d2 = __int_as_float(v.w);
+}
+__device__ __forceinline__ void dec_ent(const Ent64* slot, int32_t& q, double& d0, double& d1,
+                                        double& d2) {
+  const double2* p = reinterpret_cast<const double2*>(slot);
+  const double2 a = p[0], b = p[1];
+  d0 = a.x;
+  d1 = a.y;
+  d2 = b.x;
+  q = __double2loint(b.y);
+}
+// Ring depth in entries per thread: 8 x 16 bytes (FP32 entries) or
+// 4 x 32 bytes (FP64 entries), 32 KiB per 256-thread block either way.
+template <class E>
+constexpr int ring_len() {
+  return sizeof(E) == 16 ? 8 : 4;
+}
+
 // Flux slots: components 0-3 as one 16-byte (float) / 32-byte (double)
 // record, component 4 in a separate array, so a gather costs two sectors.
 __device__ __forceinline__ void store_f4(float* a, int64_t i, const float f[5]) {
@@ -516,6 +585,7 @@ struct Adj {
   const typename EntOf<F>::type* ent;
 };
 struct Bnd {
+  const int32_t* bnode;  // node of each boundary index
   const int32_t* bidx;
   const int32_t* bptr;
   const int32_t* bent;
@@ -532,72 +602,18 @@ struct NodeAux {
 // src/Physics/Riemann.cpp:229-367): sum over the node's edges of
 // -/+ D (u_p + u_q) plus the boundary-triangle term, optionally divided by the
 // nodal volume (RieCG::rhs, src/Inciter/RieCG.cpp:936-939).
+//
+// The adjacency entries stream into a per-thread ring in shared memory
+// (cp.async, RG - 1 groups of GU entries ahead); each group's GU neighbour
+// records are gathered together, so GU gathers are in flight per thread while
+// the entry stream runs ahead.  The ring is kept small: shared memory comes
+// out of the L1 capacity that serves the neighbour gathers.
+// Weak gradient to nodal gradient: divide by the nodal volume
+// (RieCG::rhs, src/Inciter/RieCG.cpp:936-939), as 1/vol in FP32 mode.
 template <class F>
-__global__ void __launch_bounds__(kBlock) k_grad(int64_t n, Adj<F> adj, const F* __restrict__ W,
-                                                  Bnd bnd, const double* __restrict__ vol,
-                                                  NodeAux aux, int divide, F* __restrict__ G) {
-  int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  if (p >= n) return;
-  const int lane = static_cast<int>(p & (kSlice - 1));
-  const int64_t s = p >> 5;
-  const int32_t off = __ldg(adj.soff + s), w = __ldg(adj.swidth + s);
-  F wp[8];
-  load8(W + p * 8, wp);
-  F g[15];
-#pragma unroll
-  for (int i = 0; i < 15; ++i) g[i] = F(0);
-  int32_t qn = kPad;
-  F dn0 = F(0), dn1 = F(0), dn2 = F(0);
-  if (w > 0) load_ent(adj.ent, off + lane, qn, dn0, dn1, dn2);
-  for (int k = 0; k < w; ++k) {
-    const int32_t e = off + k * kSlice + lane;
-    int32_t q = qn;
-    F d0 = dn0, d1 = dn1, d2 = dn2;
-    if (k + 1 < w) load_ent(adj.ent, e + kSlice, qn, dn0, dn1, dn2);  // next entry in flight
-    if (q == kPad) continue;
-    if (q >= 0) {  // this node is the first end: G -= f
-      d0 = -d0;
-      d1 = -d1;
-      d2 = -d2;
-    } else {
-      q = ~q;
-    }
-    F wq[8];
-    load8(W + int64_t(q) * 8, wq);
-#pragma unroll
-    for (int c = 0; c < 5; ++c) {
-      F sum = wq[c] + wp[c];
-      g[c * 3 + 0] += d0 * sum;
-      g[c * 3 + 1] += d1 * sum;
-      g[c * 3 + 2] += d2 * sum;
-    }
-  }
-  const int32_t bi = __ldg(bnd.bidx + p);
-  if (bi >= 0) {
-    for (int32_t j = __ldg(bnd.bptr + bi); j < __ldg(bnd.bptr + bi + 1); ++j) {
-      const int32_t t = __ldg(bnd.bent + j) >> 2;
-      const int32_t N0 = __ldg(bnd.btri + 3 * t), N1 = __ldg(bnd.btri + 3 * t + 1),
-                    N2 = __ldg(bnd.btri + 3 * t + 2);
-      F a[8], b[8], c[8];
-      load8(W + int64_t(N0) * 8, a);
-      load8(W + int64_t(N1) * 8, b);
-      load8(W + int64_t(N2) * 8, c);
-      F bax = b[5] - a[5], bay = b[6] - a[6], baz = b[7] - a[7];
-      F cax = c[5] - a[5], cay = c[6] - a[6], caz = c[7] - a[7];
-      F nn[3] = {(bay * caz - cay * baz) / F(12.0), (baz * cax - caz * bax) / F(12.0),
-                 (bax * cay - cax * bay) / F(12.0)};
-#pragma unroll
-      for (int cc = 0; cc < 5; ++cc) {
-        F uab = (a[cc] + b[cc]) / F(4.0);
-        F ubc = (b[cc] + c[cc]) / F(4.0);
-        F uca = (c[cc] + a[cc]) / F(4.0);
-        F gg[3] = {uab + uca + a[cc], uab + ubc + b[cc], ubc + uca + c[cc]};
-#pragma unroll
-        for (int j2 = 0; j2 < 3; ++j2) g[cc * 3 + j2] += gg[j2] * nn[j2];
-      }
-    }
-  }
-  F o[16];
+__device__ __forceinline__ void finish_grad(const F g[15], int divide,
+                                            const double* __restrict__ vol, NodeAux aux,
+                                            int64_t p, F o[16]) {
   if (divide) {
     if constexpr (sizeof(F) == 8) {
       const double v = vol[p];
@@ -612,6 +628,144 @@ __global__ void __launch_bounds__(kBlock) k_grad(int64_t n, Adj<F> adj, const F*
 #pragma unroll
     for (int i = 0; i < 15; ++i) o[i] = g[i];
   }
+}
+
+template <class F>
+struct GradShape {
+  static constexpr int GU = 2;                        // entries per group
+  static constexpr int RG = 2;                        // ring groups per thread
+  static constexpr int BLOCK = 256;
+};
+
+template <class F>
+__global__ void __launch_bounds__(GradShape<F>::BLOCK)
+    k_grad(int64_t n, Adj<F> adj, const F* __restrict__ W, Bnd bnd,
+           const double* __restrict__ vol, NodeAux aux, int divide, F* __restrict__ G) {
+  using EntT = typename EntOf<F>::type;
+  constexpr int GU = GradShape<F>::GU, RG = GradShape<F>::RG, NB = GradShape<F>::BLOCK;
+  static_assert((RG & (RG - 1)) == 0 && RG >= 2, "ring of a power-of-two number of groups");
+  __shared__ EntT ring[GU * RG][NB];
+  int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (p >= n) return;
+  const int tid = threadIdx.x;
+  const int lane = static_cast<int>(p & (kSlice - 1));
+  const int64_t s = p >> 5;
+  const int32_t off = __ldg(adj.soff + s), w = __ldg(adj.swidth + s);
+  const EntT* src = adj.ent + off + lane;
+  // group j holds entries GU*j..GU*j+GU-1; groups 0..RG-2 are requested up
+  // front, group k+RG-1 while group k is processed, into the slots group k-1
+  // freed
+#pragma unroll
+  for (int j = 0; j < RG - 1; ++j) {
+#pragma unroll
+    for (int u = 0; u < GU; ++u)
+      if (GU * j + u < w) fetch_ent(&ring[GU * j + u][tid], src + (GU * j + u) * kSlice);
+    cp_async_commit();
+  }
+  F wp[5];
+  load5(W + p * 8, wp);
+  F g[15];
+#pragma unroll
+  for (int i = 0; i < 15; ++i) g[i] = F(0);
+  const int ng = (w + GU - 1) / GU;
+  for (int kg = 0; kg < ng; ++kg) {
+    cp_async_wait<RG - 2>();
+    const int sl = (kg & (RG - 1)) * GU;
+    int32_t q[GU];
+    F d[GU][3];
+#pragma unroll
+    for (int u = 0; u < GU; ++u) {
+      q[u] = kPad;
+      if (GU * kg + u < w) dec_ent(&ring[sl + u][tid], q[u], d[u][0], d[u][1], d[u][2]);
+    }
+    const int jn = kg + RG - 1;
+    const int sn = (jn & (RG - 1)) * GU;
+#pragma unroll
+    for (int u = 0; u < GU; ++u)
+      if (GU * jn + u < w) fetch_ent(&ring[sn + u][tid], src + (GU * jn + u) * kSlice);
+    cp_async_commit();
+    F wq[GU][5];
+#pragma unroll
+    for (int u = 0; u < GU; ++u) {
+      if (q[u] == kPad) continue;
+      if (q[u] >= 0) {  // this node is the first end: G -= f
+        d[u][0] = -d[u][0];
+        d[u][1] = -d[u][1];
+        d[u][2] = -d[u][2];
+      } else {
+        q[u] = ~q[u];
+      }
+      load5(W + int64_t(q[u]) * 8, wq[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < GU; ++u) {
+      if (q[u] == kPad) continue;
+#pragma unroll
+      for (int c = 0; c < 5; ++c) {
+        F sum = wq[u][c] + wp[c];
+        g[c * 3 + 0] += d[u][0] * sum;
+        g[c * 3 + 1] += d[u][1] * sum;
+        g[c * 3 + 2] += d[u][2] * sum;
+      }
+    }
+  }
+  cp_async_wait<0>();
+  F o[16];
+  if (__ldg(bnd.bidx + p) >= 0) {
+    // boundary node: the domain sum as it stands; k_grad_bnd adds the
+    // boundary integral and divides (the reference's order of summation)
+#pragma unroll
+    for (int i = 0; i < 15; ++i) o[i] = g[i];
+  } else {
+    finish_grad(g, divide, vol, aux, p, o);
+  }
+  o[15] = F(0);
+  store16(G + p * 16, o);
+}
+
+// Boundary-triangle term of riemann::grad (src/Physics/Riemann.cpp:329-364)
+// at boundary node p, added to g in the node's triangle order.
+template <class F>
+__device__ __forceinline__ void grad_bnd_term(const Bnd& bnd, int32_t bi, const F* __restrict__ W,
+                                              F g[15]) {
+  for (int32_t j = __ldg(bnd.bptr + bi); j < __ldg(bnd.bptr + bi + 1); ++j) {
+    const int32_t t = __ldg(bnd.bent + j) >> 2;
+    const int32_t N0 = __ldg(bnd.btri + 3 * t), N1 = __ldg(bnd.btri + 3 * t + 1),
+                  N2 = __ldg(bnd.btri + 3 * t + 2);
+    F a[8], b[8], c[8];
+    load8(W + int64_t(N0) * 8, a);
+    load8(W + int64_t(N1) * 8, b);
+    load8(W + int64_t(N2) * 8, c);
+    F bax = b[5] - a[5], bay = b[6] - a[6], baz = b[7] - a[7];
+    F cax = c[5] - a[5], cay = c[6] - a[6], caz = c[7] - a[7];
+    F nn[3] = {(bay * caz - cay * baz) / F(12.0), (baz * cax - caz * bax) / F(12.0),
+               (bax * cay - cax * bay) / F(12.0)};
+#pragma unroll
+    for (int cc = 0; cc < 5; ++cc) {
+      F uab = (a[cc] + b[cc]) / F(4.0);
+      F ubc = (b[cc] + c[cc]) / F(4.0);
+      F uca = (c[cc] + a[cc]) / F(4.0);
+      F gg[3] = {uab + uca + a[cc], uab + ubc + b[cc], ubc + uca + c[cc]};
+#pragma unroll
+      for (int j2 = 0; j2 < 3; ++j2) g[cc * 3 + j2] += gg[j2] * nn[j2];
+    }
+  }
+}
+
+// Boundary nodes of the gradient pass, one thread per boundary node.
+template <class F>
+__global__ void __launch_bounds__(kBlock) k_grad_bnd(int64_t nbn, Bnd bnd,
+                                                      const F* __restrict__ W,
+                                                      const double* __restrict__ vol,
+                                                      NodeAux aux, int divide, F* G) {
+  const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= nbn) return;
+  const int64_t p = __ldg(bnd.bnode + i);
+  F g[16];
+  load16(G + p * 16, g);
+  grad_bnd_term(bnd, static_cast<int32_t>(i), W, g);
+  F o[16];
+  finish_grad(g, divide, vol, aux, p, o);
   o[15] = F(0);
   store16(G + p * 16, o);
 }
@@ -631,44 +785,58 @@ __device__ __forceinline__ float node_dt_f(const double ud[5], float L, float g)
 
 // Half-edge residual, pass 1: every edge flux once, at the edge's owner end,
 // in the edge's canonical orientation (riemann::rhs advdom,
-// src/Physics/Riemann.cpp:695-759): f is stored in the slot coalesced with the
-// entry and -f (owner is the first end) or +f summed into the node's partial
-// residual.
+// src/Physics/Riemann.cpp:695-759): -f (owner is the first end) or +f is
+// summed into the owner's partial residual and the other end's contribution
+// (+f or -f) is stored into that end's list-2 slot (pos1), so the second pass
+// reads its fluxes as a coalesced stream.
 template <class F>
 struct Half {
   const int32_t* soff1;
   const int32_t* sw1;
   const typename EntOf<F>::type* ent1;
+  const int32_t* pos1;
   const int32_t* soff2;
   const int32_t* sw2;
-  const int32_t* slot2;
-  int64_t nent1;
+  int64_t nent2;
 };
 
 template <class F, int FLUX>
-__global__ void __launch_bounds__(kBlock, sizeof(F) == 4 ? 4 : 1)
+__global__ void __launch_bounds__(kBlock, sizeof(F) == 4 ? 3 : 1)
     k_flux1(int64_t n, Half<F> h, const F* __restrict__ W, const F* __restrict__ G,
             double gamma_d, int stab2, double stab2coef_d, F* __restrict__ fbuf,
             F* __restrict__ Rp) {
+  using EntT = typename EntOf<F>::type;
+  constexpr int RL = ring_len<EntT>();
+  __shared__ EntT ring[RL][kBlock];
   int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (p >= n) return;
+  const int tid = threadIdx.x;
   const F gamma = F(gamma_d), stab2coef = F(stab2coef_d);
   const int lane = static_cast<int>(p & (kSlice - 1));
   const int64_t s = p >> 5;
   const int32_t off = __ldg(h.soff1 + s), w = __ldg(h.sw1 + s);
+  const EntT* src = h.ent1 + off + lane;
+  // entries 0..RL-2 requested up front, entry k+RL-1 while entry k is
+  // processed, into the slot entry k-1 has freed
+#pragma unroll
+  for (int j = 0; j < RL - 1; ++j) {
+    if (j < w) fetch_ent(&ring[j][tid], src + j * kSlice);
+    cp_async_commit();
+  }
   F wp[8], gp[16];
   load8(W + p * 8, wp);
   load16(G + p * 16, gp);
   F R[5] = {F(0), F(0), F(0), F(0), F(0)};
-  int32_t qn = kPad;
-  F dn0 = F(0), dn1 = F(0), dn2 = F(0);
-  if (w > 0) load_ent(h.ent1, off + lane, qn, dn0, dn1, dn2);
   for (int k = 0; k < w; ++k) {
     const int32_t e = off + k * kSlice + lane;
-    int32_t q = qn;
-    const F d0 = dn0, d1 = dn1, d2 = dn2;
-    if (k + 1 < w) load_ent(h.ent1, e + kSlice, qn, dn0, dn1, dn2);  // next entry in flight
+    cp_async_wait<RL - 2>();
+    int32_t q;
+    F d0, d1, d2;
+    dec_ent(&ring[k & (RL - 1)][tid], q, d0, d1, d2);
+    if (k + RL - 1 < w) fetch_ent(&ring[(k + RL - 1) & (RL - 1)][tid], src + (k + RL - 1) * kSlice);
+    cp_async_commit();
     if (q == kPad) continue;
+    const int32_t dst = __ldg(h.pos1 + e);
     const bool first = q >= 0;
     if (!first) q = ~q;
     F wq[8], gq[16];
@@ -691,154 +859,209 @@ __global__ void __launch_bounds__(kBlock, sizeof(F) == 4 ? 4 : 1)
     else
       rusanov(wl, wr, g1, g2, d0, d1, d2, gamma, stab2 != 0, stab2coef, f);
     const F sg = first ? F(-1) : F(1);
+    F fo[5];
 #pragma unroll
-    for (int c = 0; c < 5; ++c) R[c] += sg * f[c];
-    store_f4(fbuf, e, f);
-    fbuf[4 * h.nent1 + e] = f[4];
+    for (int c = 0; c < 5; ++c) {
+      R[c] += sg * f[c];
+      fo[c] = -sg * f[c];
+    }
+    store_f4(fbuf, dst, fo);
+    fbuf[4 * h.nent2 + dst] = fo[4];
   }
+  cp_async_wait<0>();
 #pragma unroll
   for (int c = 0; c < 5; ++c) Rp[c * n + p] = R[c];
 }
 
-// Half-edge residual, pass 2: the fluxes of the edges the other end owns,
-// the boundary integral (advbnd, src/Physics/Riemann.cpp:
-// 768-878), and (optionally) the RK update of one stage (RieCG::solve,
-// src/Inciter/RieCG.cpp:1010-1021) with the new primitive records and, on the
-// last stage, the CFL minimum (src/Inciter/RieCG.cpp:827-839) of nodes without
-// a nodal BC (the BC kernel covers those after modifying them).
+// Boundary integral of riemann::rhs (advbnd, src/Physics/Riemann.cpp:768-878)
+// at the boundary node with index bi, added to R in the node's triangle order.
+template <class F>
+__device__ __forceinline__ void rhs_bnd_term(const Bnd& bnd, int32_t bi, const F* __restrict__ W,
+                                             F gamma, F R[5]) {
+  for (int32_t j = __ldg(bnd.bptr + bi); j < __ldg(bnd.bptr + bi + 1); ++j) {
+    const int32_t ent = __ldg(bnd.bent + j);
+    const int32_t t = ent >> 2, pos = ent & 3;
+    F x[3][8];
+    uint8_t sy[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      load8(W + int64_t(__ldg(bnd.btri + 3 * t + a)) * 8, x[a]);
+      sy[a] = __ldg(bnd.bsym + 3 * t + a);
+    }
+    F bax = x[1][5] - x[0][5], bay = x[1][6] - x[0][6], baz = x[1][7] - x[0][7];
+    F cax = x[2][5] - x[0][5], cay = x[2][6] - x[0][6], caz = x[2][7] - x[0][7];
+    F nx = (bay * caz - cay * baz) / F(12.0);
+    F ny = (baz * cax - caz * bax) / F(12.0);
+    F nz = (bax * cay - cax * bay) / F(12.0);
+    F fl[3][5];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const F r = x[a][0], u = x[a][1], v = x[a][2], ww = x[a][3], ie = x[a][4];
+      const F pr = r * ie * (gamma - F(1.0));
+      const F vn = sy[a] ? F(0) : (nx * u + ny * v + nz * ww);
+      const F re = r * (ie + F(0.5) * (u * u + v * v + ww * ww));
+      fl[a][0] = r * vn;
+      fl[a][1] = r * u * vn + pr * nx;
+      fl[a][2] = r * v * vn + pr * ny;
+      fl[a][3] = r * ww * vn + pr * nz;
+      fl[a][4] = (re + pr) * vn;
+    }
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      // own value, plus the two averages of the pairs containing this node
+      F fa = fl[0][c], fb = fl[1][c], fcc = fl[2][c];
+      F fab = (fa + fb) / F(4.0), fbc = (fb + fcc) / F(4.0), fca = (fcc + fa) / F(4.0);
+      R[c] += pos == 0 ? (fab + fca + fa) : (pos == 1 ? (fab + fbc + fb) : (fbc + fca + fcc));
+    }
+  }
+}
+
+// One node's stage update (RieCG::solve, src/Inciter/RieCG.cpp:1010-1021):
+// U = Un - rkcoef*dt*R/vol from uo (U at stage 0, Un after), the new
+// primitive record and, on the last stage when want_dt, the node's CFL time
+// step (src/Inciter/RieCG.cpp:827-839); DBL_MAX otherwise.
+template <class F, int STAGE>
+__device__ __forceinline__ double update_node(int64_t n, int64_t p, const F R[5],
+                                              const double uo[5], const F wp[8], bool want_dt,
+                                              const double* __restrict__ vol, NodeAux aux,
+                                              double gamma_d, double dt, double* U, double* Un,
+                                              F* __restrict__ Wout) {
+  constexpr double rk = STAGE == 0 ? 1.0 / 3.0 : (STAGE == 1 ? 0.5 : 1.0);
+  double dtp = DBL_MAX;
+  double un[5];
+  if constexpr (sizeof(F) == 8) {
+    // FP64: the reference's expression, Un - rkcoef*dt*R/vol
+    const double v = vol[p];
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      if (STAGE == 0) Un[c * n + p] = uo[c];
+      un[c] = uo[c] - rk * dt * double(R[c]) / v;
+      U[c * n + p] = un[c];
+    }
+    double pw[5];
+    prim5(un, pw);
+    F o[8] = {F(pw[0]), F(pw[1]), F(pw[2]), F(pw[3]), F(pw[4]), wp[5], wp[6], wp[7]};
+    store8(Wout + p * 8, o);
+    if (STAGE == 2 && want_dt) dtp = node_dt(un, v, gamma_d);
+  } else {
+    // FP32 fluxes: the FP64 state update uses 1/vol; primitives and the
+    // CFL estimate are formed in FP32 (no FP64 division per node)
+    const double cf = rk * dt * aux.ivol[p];
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      if (STAGE == 0) Un[c * n + p] = uo[c];
+      un[c] = uo[c] - cf * double(R[c]);
+      U[c * n + p] = un[c];
+    }
+    const float r = float(un[0]);
+    const float ir = __frcp_rn(r);
+    const float uu = float(un[1]) * ir, vv = float(un[2]) * ir, ww = float(un[3]) * ir;
+    const float ie = float(un[4]) * ir - 0.5f * (uu * uu + vv * vv + ww * ww);
+    F o[8] = {r, uu, vv, ww, ie, wp[5], wp[6], wp[7]};
+    store8(Wout + p * 8, o);
+    if (STAGE == 2 && want_dt) dtp = double(node_dt_f(un, aux.cbrtv[p], float(gamma_d)));
+  }
+  return dtp;
+}
+
+// Half-edge residual, pass 2: the fluxes of the edges the other end owns and
+// (optionally) the RK update of one stage with the new primitive records and,
+// on the last stage, the CFL minimum.  Boundary nodes only park their domain
+// residual in Rb: k_rhs_bnd adds their boundary integral and updates them,
+// so no warp here waits on the triangle gathers.
 template <class F, int STAGE, bool UPDATE>
-__global__ void __launch_bounds__(kBlock) k_rhs2(int64_t n, Half<F> h,
-                                                  const F* __restrict__ fbuf,
-                                                  const F* __restrict__ Rp,
-                                                  const F* __restrict__ W, Bnd bnd,
-                                                  const uint8_t* __restrict__ bcflag,
-                                                  const double* __restrict__ vol, NodeAux aux,
-                                                  double gamma_d, const Scalars* __restrict__ scal,
-                                                  double* U, double* Un, F* __restrict__ Wout,
-                                                  double* __restrict__ Rout,
-                                                  unsigned long long* dtmin) {
+__global__ void __launch_bounds__(kBlock, sizeof(F) == 4 ? 4 : 1)
+    k_rhs2(int64_t n, Half<F> h, const F* __restrict__ fbuf, const F* __restrict__ Rp,
+           const F* __restrict__ W, Bnd bnd, int64_t nbn, F* __restrict__ Rb,
+           const double* __restrict__ vol, NodeAux aux, double gamma_d,
+           const Scalars* __restrict__ scal, double* U, double* Un, F* __restrict__ Wout,
+           double* __restrict__ Rout, unsigned long long* dtmin) {
   int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   const bool active = p < n;
-  const F gamma = F(gamma_d);
   double dtp = DBL_MAX;
   if (active) {
     const int lane = static_cast<int>(p & (kSlice - 1));
     const int64_t s = p >> 5;
+    const int32_t off = __ldg(h.soff2 + s), w = __ldg(h.sw2 + s);
+    const int32_t bi = __ldg(bnd.bidx + p);
+    // every per-node load is issued before the flux stream is summed
     F R[5];
 #pragma unroll
     for (int c = 0; c < 5; ++c) R[c] = Rp[c * n + p];
-    const int32_t off = __ldg(h.soff2 + s), w = __ldg(h.sw2 + s);
-#pragma unroll 4
-    for (int k = 0; k < w; ++k) {
-      int32_t slot = __ldg(h.slot2 + off + k * kSlice + lane);
-      if (slot == kPad) continue;
-      const F sg = slot >= 0 ? F(1) : F(-1);
-      if (slot < 0) slot = ~slot;
-      F f[4];
-      load_f4(fbuf, slot, f);
-      const F f4 = __ldg(fbuf + 4 * h.nent1 + slot);
+    double uo[5];
+    if (UPDATE && bi < 0) {
 #pragma unroll
-      for (int c = 0; c < 4; ++c) R[c] += sg * f[c];
-      R[4] += sg * f4;
+      for (int c = 0; c < 5; ++c) uo[c] = STAGE == 0 ? U[c * n + p] : Un[c * n + p];
     }
     F wp[8];
-    load8(W + p * 8, wp);
-    const int32_t bi = __ldg(bnd.bidx + p);
-    if (bi >= 0) {
-      for (int32_t j = __ldg(bnd.bptr + bi); j < __ldg(bnd.bptr + bi + 1); ++j) {
-        const int32_t ent = __ldg(bnd.bent + j);
-        const int32_t t = ent >> 2, pos = ent & 3;
-        F x[3][8];
-        uint8_t sy[3];
+    if (UPDATE && bi < 0) load8(W + p * 8, wp);
+    // the other ends' contributions, a coalesced stream (padding slots hold
+    // 0), four slots per batch with all of a batch's loads in flight
+    for (int k0 = 0; k0 < w; k0 += 4) {
+      F f[4][4], f4[4];
 #pragma unroll
-        for (int a = 0; a < 3; ++a) {
-          load8(W + int64_t(__ldg(bnd.btri + 3 * t + a)) * 8, x[a]);
-          sy[a] = __ldg(bnd.bsym + 3 * t + a);
+      for (int u = 0; u < 4; ++u) {
+        if (k0 + u < w) {
+          const int64_t e = off + (k0 + u) * kSlice + lane;
+          load_f4(fbuf, e, f[u]);
+          f4[u] = __ldg(fbuf + 4 * h.nent2 + e);
         }
-        F bax = x[1][5] - x[0][5], bay = x[1][6] - x[0][6], baz = x[1][7] - x[0][7];
-        F cax = x[2][5] - x[0][5], cay = x[2][6] - x[0][6], caz = x[2][7] - x[0][7];
-        F nx = (bay * caz - cay * baz) / F(12.0);
-        F ny = (baz * cax - caz * bax) / F(12.0);
-        F nz = (bax * cay - cax * bay) / F(12.0);
-        F fl[3][5];
+      }
 #pragma unroll
-        for (int a = 0; a < 3; ++a) {
-          const F r = x[a][0], u = x[a][1], v = x[a][2], ww = x[a][3], ie = x[a][4];
-          const F pr = r * ie * (gamma - F(1.0));
-          const F vn = sy[a] ? F(0) : (nx * u + ny * v + nz * ww);
-          const F re = r * (ie + F(0.5) * (u * u + v * v + ww * ww));
-          fl[a][0] = r * vn;
-          fl[a][1] = r * u * vn + pr * nx;
-          fl[a][2] = r * v * vn + pr * ny;
-          fl[a][3] = r * ww * vn + pr * nz;
-          fl[a][4] = (re + pr) * vn;
-        }
+      for (int u = 0; u < 4; ++u) {
+        if (k0 + u < w) {
 #pragma unroll
-        for (int c = 0; c < 5; ++c) {
-          // own value, plus the two averages of the pairs containing this node
-          F fa = fl[0][c], fb = fl[1][c], fcc = fl[2][c];
-          F fab = (fa + fb) / F(4.0), fbc = (fb + fcc) / F(4.0), fca = (fcc + fa) / F(4.0);
-          R[c] += pos == 0 ? (fab + fca + fa) : (pos == 1 ? (fab + fbc + fb) : (fbc + fca + fcc));
+          for (int c = 0; c < 4; ++c) R[c] += f[u][c];
+          R[4] += f4[u];
         }
       }
     }
+    if (bi >= 0) {
+#pragma unroll
+      for (int c = 0; c < 5; ++c) Rb[c * nbn + bi] = R[c];
+    } else if (!UPDATE) {
+#pragma unroll
+      for (int c = 0; c < 5; ++c) Rout[p * 5 + c] = double(R[c]);
+    } else {
+      dtp = update_node<F, STAGE>(n, p, R, uo, wp, true, vol, aux, gamma_d, scal->dt, U, Un,
+                                  Wout);
+    }
+  }
+  if (UPDATE && STAGE == 2) block_min_atomic(dtp, dtmin);
+}
+
+// Boundary nodes of pass 2, one thread per boundary node: the boundary
+// integral after the domain residual (the reference's order), then the same
+// update; the CFL minimum skips nodes with a nodal BC (the BC kernel covers
+// those after modifying them).
+template <class F, int STAGE, bool UPDATE>
+__global__ void __launch_bounds__(kBlock)
+    k_rhs_bnd(int64_t n, int64_t nbn, Bnd bnd, const F* __restrict__ Rb,
+              const F* __restrict__ W, const uint8_t* __restrict__ bcflag,
+              const double* __restrict__ vol, NodeAux aux, double gamma_d,
+              const Scalars* __restrict__ scal, double* U, double* Un, F* __restrict__ Wout,
+              double* __restrict__ Rout, unsigned long long* dtmin) {
+  const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  double dtp = DBL_MAX;
+  if (i < nbn) {
+    const int64_t p = __ldg(bnd.bnode + i);
+    F R[5];
+#pragma unroll
+    for (int c = 0; c < 5; ++c) R[c] = Rb[c * nbn + i];
+    double uo[5];
+    if (UPDATE) {
+#pragma unroll
+      for (int c = 0; c < 5; ++c) uo[c] = STAGE == 0 ? U[c * n + p] : Un[c * n + p];
+    }
+    F wp[8];
+    load8(W + p * 8, wp);
+    rhs_bnd_term(bnd, static_cast<int32_t>(i), W, F(gamma_d), R);
     if (!UPDATE) {
 #pragma unroll
       for (int c = 0; c < 5; ++c) Rout[p * 5 + c] = double(R[c]);
     } else {
-      constexpr double rk = STAGE == 0 ? 1.0 / 3.0 : (STAGE == 1 ? 0.5 : 1.0);
-      const double dt = scal->dt;
-      double un[5];
-      if constexpr (sizeof(F) == 8) {
-        // FP64: the reference's expression, Un - rkcoef*dt*R/vol
-        const double v = vol[p];
-#pragma unroll
-        for (int c = 0; c < 5; ++c) {
-          double uo;
-          if (STAGE == 0) {
-            uo = U[c * n + p];
-            Un[c * n + p] = uo;
-          } else {
-            uo = Un[c * n + p];
-          }
-          un[c] = uo - rk * dt * double(R[c]) / v;
-          U[c * n + p] = un[c];
-        }
-        double pw[5];
-        prim5(un, pw);
-        F o[8] = {F(pw[0]), F(pw[1]), F(pw[2]), F(pw[3]), F(pw[4]), wp[5], wp[6], wp[7]};
-        store8(Wout + p * 8, o);
-        if (STAGE == 2) {
-          const bool hasbc = bi >= 0 && bcflag[bi];
-          if (!hasbc) dtp = node_dt(un, v, gamma_d);
-        }
-      } else {
-        // FP32 fluxes: the FP64 state update uses 1/vol; primitives and the
-        // CFL estimate are formed in FP32 (no FP64 division per node)
-        const double cf = rk * dt * aux.ivol[p];
-#pragma unroll
-        for (int c = 0; c < 5; ++c) {
-          double uo;
-          if (STAGE == 0) {
-            uo = U[c * n + p];
-            Un[c * n + p] = uo;
-          } else {
-            uo = Un[c * n + p];
-          }
-          un[c] = uo - cf * double(R[c]);
-          U[c * n + p] = un[c];
-        }
-        const float r = float(un[0]);
-        const float ir = __frcp_rn(r);
-        const float uu = float(un[1]) * ir, vv = float(un[2]) * ir, ww = float(un[3]) * ir;
-        const float ie = float(un[4]) * ir - 0.5f * (uu * uu + vv * vv + ww * ww);
-        F o[8] = {r, uu, vv, ww, ie, wp[5], wp[6], wp[7]};
-        store8(Wout + p * 8, o);
-        if (STAGE == 2) {
-          const bool hasbc = bi >= 0 && bcflag[bi];
-          if (!hasbc) dtp = double(node_dt_f(un, aux.cbrtv[p], float(gamma_d)));
-        }
-      }
+      dtp = update_node<F, STAGE>(n, p, R, uo, wp, bcflag[i] == 0, vol, aux, gamma_d, scal->dt,
+                                  U, Un, Wout);
     }
   }
   if (UPDATE && STAGE == 2) block_min_atomic(dtp, dtmin);
@@ -866,7 +1089,8 @@ struct BCProg {
 template <class F>
 __global__ void __launch_bounds__(kBlock) k_bc(int64_t n, BCProg bc, double gamma, double* U,
                                                 F* __restrict__ W, const double* __restrict__ vol,
-                                                int want_dt, unsigned long long* dtmin) {
+                                                NodeAux aux, int want_dt,
+                                                unsigned long long* dtmin) {
   int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   double dtp = DBL_MAX;
   if (i < bc.nbc) {
@@ -922,14 +1146,28 @@ __global__ void __launch_bounds__(kBlock) k_bc(int64_t n, BCProg bc, double gamm
     }
 #pragma unroll
     for (int c = 0; c < 5; ++c) U[c * n + p] = u[c];
-    double w[5];
-    prim5(u, w);
     F o[8];
     load8(W + p * 8, o);
+    if constexpr (sizeof(F) == 8) {
+      double w[5];
+      prim5(u, w);
 #pragma unroll
-    for (int c = 0; c < 5; ++c) o[c] = F(w[c]);
+      for (int c = 0; c < 5; ++c) o[c] = w[c];
+      if (want_dt) dtp = node_dt(u, vol[p], gamma);
+    } else {
+      // FP32 mode: the primitive record and the CFL estimate as the fused
+      // update forms them (no FP64 division per node)
+      const float r = float(u[0]);
+      const float ir = __frcp_rn(r);
+      const float uu = float(u[1]) * ir, vv = float(u[2]) * ir, ww = float(u[3]) * ir;
+      o[0] = r;
+      o[1] = uu;
+      o[2] = vv;
+      o[3] = ww;
+      o[4] = float(u[4]) * ir - 0.5f * (uu * uu + vv * vv + ww * ww);
+      if (want_dt) dtp = double(node_dt_f(u, aux.cbrtv[p], float(gamma)));
+    }
     store8(W + p * 8, o);
-    if (want_dt) dtp = node_dt(u, vol[p], gamma);
   }
   if (want_dt) block_min_atomic(dtp, dtmin);
 }
@@ -982,7 +1220,7 @@ struct Edge {
 };
 
 struct HalfLists {
-  std::vector<int32_t> soff1, sw1, soff2, sw2, q1, slot2;
+  std::vector<int32_t> soff1, sw1, soff2, sw2, q1, pos1;
   std::vector<double> d1;
   int64_t nent1 = 0, nent2 = 0;
 };
@@ -1043,7 +1281,7 @@ Adj<F> adj_of(RieCGDev* d) {
   return Adj<F>{d->soff, d->swidth, static_cast<const typename EntOf<F>::type*>(d->ent)};
 }
 NodeAux aux_of(RieCGDev* d) { return NodeAux{d->ivol, d->cbrtv}; }
-Bnd bnd_of(RieCGDev* d) { return Bnd{d->bidx, d->bptr, d->bent, d->btri, d->bsym}; }
+Bnd bnd_of(RieCGDev* d) { return Bnd{d->bnode, d->bidx, d->bptr, d->bent, d->btri, d->bsym}; }
 
 BCProg bcprog_of(RieCGDev* d) {
   BCProg b;
@@ -1065,15 +1303,20 @@ BCProg bcprog_of(RieCGDev* d) {
 template <class F>
 int launch_grad(xg_ctx* c, RieCGDev* d, const F* W, F* G, int divide) {
   XG_PROF_LAUNCH(c, d, "riecg_grad",
-                 (k_grad<F><<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(
+                 (k_grad<F><<<blocks_for(d->n, GradShape<F>::BLOCK), GradShape<F>::BLOCK, 0,
+                                c->stream>>>(
                      d->n, adj_of<F>(d), W, bnd_of(d), d->vol, aux_of(d), divide, G)));
+  if (d->nbn > 0)
+    XG_PROF_LAUNCH(c, d, "riecg_grad_bnd",
+                   (k_grad_bnd<F><<<blocks_for(d->nbn, kBlock), kBlock, 0, c->stream>>>(
+                       d->nbn, bnd_of(d), W, d->vol, aux_of(d), divide, G)));
   return XG_OK;
 }
 
 template <class F>
 Half<F> half_of(RieCGDev* d) {
   return Half<F>{d->soff1, d->sw1, static_cast<const typename EntOf<F>::type*>(d->ent1),
-                 d->soff2, d->sw2, d->slot2, d->nent1};
+                 d->pos1, d->soff2, d->sw2, d->nent2};
 }
 
 template <class F, int FLUX, int STAGE, bool UPDATE>
@@ -1086,8 +1329,16 @@ int launch_rhs_t(xg_ctx* c, RieCGDev* d, const F* W, const F* G, F* Wout, double
                      fbuf, Rp)));
   XG_PROF_LAUNCH(c, d, "riecg_rhs_update",
                  (k_rhs2<F, STAGE, UPDATE><<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(
-                     d->n, half_of<F>(d), fbuf, Rp, W, bnd_of(d), d->bcflag, d->vol, aux_of(d),
-                     d->prm.gamma, d->scal, d->U, d->Un, Wout, Rout, &d->scal->dtmin)));
+                     d->n, half_of<F>(d), fbuf, Rp, W, bnd_of(d), d->nbn,
+                     static_cast<F*>(d->Rb), d->vol, aux_of(d), d->prm.gamma, d->scal, d->U,
+                     d->Un, Wout, Rout, &d->scal->dtmin)));
+  if (d->nbn > 0)
+    XG_PROF_LAUNCH(c, d, "riecg_rhs_bnd",
+                   (k_rhs_bnd<F, STAGE, UPDATE><<<blocks_for(d->nbn, kBlock), kBlock, 0,
+                                                  c->stream>>>(
+                       d->n, d->nbn, bnd_of(d), static_cast<const F*>(d->Rb), W, d->bcflag,
+                       d->vol, aux_of(d), d->prm.gamma, d->scal, d->U, d->Un, Wout, Rout,
+                       &d->scal->dtmin)));
   return XG_OK;
 }
 
@@ -1113,7 +1364,7 @@ int launch_bc(xg_ctx* c, RieCGDev* d, F* W, int want_dt) {
   if (d->nbc == 0) return XG_OK;
   XG_PROF_LAUNCH(c, d, "riecg_bc",
                  (k_bc<F><<<blocks_for(d->nbc, kBlock), kBlock, 0, c->stream>>>(
-                     d->n, bcprog_of(d), d->prm.gamma, d->U, W, d->vol, want_dt,
+                     d->n, bcprog_of(d), d->prm.gamma, d->U, W, d->vol, aux_of(d), want_dt,
                      &d->scal->dtmin)));
   return XG_OK;
 }
@@ -1154,7 +1405,7 @@ int alloc_and_upload(xg_ctx* c, RieCGDev* d, const double* coord, const double* 
                      const std::vector<uint8_t>& bsym, const HalfLists& hl) {
   const int64_t n = d->n;
   using EntT = typename EntOf<F>::type;
-  F *W0, *W1, *G, *fbuf, *Rp;
+  F *W0, *W1, *G, *fbuf, *Rp, *Rb;
   EntT *ent, *ent1;
   for (int pass = 0; pass < 2; ++pass) {
     Arena& A = d->arena;
@@ -1172,9 +1423,9 @@ int alloc_and_upload(xg_ctx* c, RieCGDev* d, const double* coord, const double* 
     A.plan(d->sw1, hl.sw1.size());
     A.plan(d->soff2, hl.soff2.size());
     A.plan(d->sw2, hl.sw2.size());
-    A.plan(d->slot2, std::max<int64_t>(1, hl.nent2));
+    A.plan(d->pos1, std::max<int64_t>(1, hl.nent1));
     A.plan(ent1, std::max<int64_t>(1, hl.nent1));
-    A.plan(fbuf, std::max<int64_t>(1, hl.nent1) * 5);
+    A.plan(fbuf, std::max<int64_t>(1, hl.nent2) * 5);
     A.plan(Rp, n * 5);
     A.plan(d->ivol, n);
     A.plan(d->cbrtv, n);
@@ -1183,9 +1434,12 @@ int alloc_and_upload(xg_ctx* c, RieCGDev* d, const double* coord, const double* 
     A.plan(d->btri, std::max<size_t>(1, btri.size()));
     A.plan(d->bsym, std::max<size_t>(1, bsym.size()));
     A.plan(d->bcflag, std::max<int64_t>(1, d->nbn));
+    A.plan(d->bnode, std::max<int64_t>(1, d->nbn));
+    A.plan(Rb, std::max<int64_t>(1, d->nbn) * 5);
     A.plan(d->scal, 1);
     if (pass == 0) XG_CUDA(c, A.reserve());
   }
+  d->Rb = Rb;
   for (int pass = 0; pass < 2; ++pass) {
     Arena& S = d->scratch;
     S.plan(d->stage_buf, n * 15);
@@ -1257,7 +1511,9 @@ int alloc_and_upload(xg_ctx* c, RieCGDev* d, const double* coord, const double* 
     XG_CUDA(c, up(d->sw1, hl.sw1.data(), hl.sw1.size() * 4));
     XG_CUDA(c, up(d->soff2, hl.soff2.data(), hl.soff2.size() * 4));
     XG_CUDA(c, up(d->sw2, hl.sw2.data(), hl.sw2.size() * 4));
-    XG_CUDA(c, up(d->slot2, hl.slot2.data(), hl.slot2.size() * 4));
+    XG_CUDA(c, up(d->pos1, hl.pos1.data(), hl.pos1.size() * 4));
+    // list-2 padding slots are never written and must read as zero
+    XG_CUDA(c, cudaMemsetAsync(fbuf, 0, std::max<int64_t>(1, hl.nent2) * 5 * sizeof(F), s));
     XG_CUDA(c, cudaStreamSynchronize(s));
     std::vector<double> iv(n);
     std::vector<float> cv(n);
@@ -1268,6 +1524,10 @@ int alloc_and_upload(xg_ctx* c, RieCGDev* d, const double* coord, const double* 
     XG_CUDA(c, cudaMemcpy(d->ivol, iv.data(), n * sizeof(double), cudaMemcpyHostToDevice));
     XG_CUDA(c, cudaMemcpy(d->cbrtv, cv.data(), n * sizeof(float), cudaMemcpyHostToDevice));
   }
+  std::vector<int32_t> bnode(std::max<int64_t>(1, d->nbn), 0);
+  for (int64_t p = 0; p < n; ++p)
+    if (bidx[p] >= 0) bnode[bidx[p]] = static_cast<int32_t>(p);
+  XG_CUDA(c, cudaMemcpy(d->bnode, bnode.data(), bnode.size() * 4, cudaMemcpyHostToDevice));
   XG_CUDA(c, up(d->bptr, bptr.data(), bptr.size() * 4));
   XG_CUDA(c, up(d->bent, bent.data(), bent.size() * 4));
   XG_CUDA(c, up(d->btri, btri.data(), btri.size() * 4));
@@ -1406,10 +1666,9 @@ int xg_riecg_setup(xg_ctx* c, const xg_riecg_params* prm, int64_t npoin, const d
   }
   // half-edge lists: every edge is owned by its end with the smaller local
   // id (with locality ordering that splits each node's edges about evenly);
-  // the owner's entry holds the other end (~id when the owner is the
-  // canonical second end) and D, and its index is the edge's flux slot; the
-  // other end's entry holds the slot (~slot when that end is the canonical
-  // first end and subtracts the flux)
+  // the owner's entry (list 1) holds the other end (~id when the owner is the
+  // canonical second end), D and the position of the edge in the other end's
+  // list 2, where the owner deposits that end's signed flux
   HalfLists hl;
   {
     std::vector<int64_t> c1(n + 1, 0), c2(n + 1, 0);
@@ -1460,7 +1719,7 @@ int xg_riecg_setup(xg_ctx* c, const xg_riecg_params* prm, int64_t npoin, const d
       return fail(c, XG_ERR_ARG, "adjacency too large");
     hl.q1.assign(hl.nent1, kPad);
     hl.d1.assign(hl.nent1 * 3, 0.0);
-    hl.slot2.assign(hl.nent2, kPad);
+    hl.pos1.assign(hl.nent1, kPad);
     std::vector<int32_t> slot1(E.size(), -1);
     for (int64_t p = 0; p < n; ++p) {
       const int64_t s2 = p / kSlice, lane = p % kSlice;
@@ -1477,8 +1736,7 @@ int xg_riecg_setup(xg_ctx* c, const xg_riecg_params* prm, int64_t npoin, const d
       const int64_t s2 = p / kSlice, lane = p % kSlice;
       for (int64_t k = 0; k < c2[p + 1] - c2[p]; ++k) {
         const int64_t eid = l2[c2[p] + k];
-        const int32_t sl = slot1[eid];
-        hl.slot2[hl.soff2[s2] + k * kSlice + lane] = (E[eid].b == p) ? sl : ~sl;
+        hl.pos1[slot1[eid]] = static_cast<int32_t>(hl.soff2[s2] + k * kSlice + lane);
       }
     }
   }
