@@ -130,12 +130,13 @@ def kernel_bytes(n, nedge, fp32):
     """Algorithmic (compulsory) bytes per launch: every array the kernel must
     read or write once; gathered neighbour records are re-reads and excluded.
     nedge edges, each stored once per end in the gradient adjacency and once
-    in each half-edge list of the residual."""
+    in the owner's half-edge list (neighbour, D and the slot of the edge in
+    the other end's list, where the owner deposits that end's flux)."""
     F = 4 if fp32 else 8
     Wb, Gb, Db = 8 * F, 16 * F, 4 + 3 * F
     grad = n * (Wb + 8 + 4 + Gb) + 2 * nedge * Db
-    flux = n * (Wb + Gb + 5 * F) + nedge * (Db + 5 * F)
-    rhs12 = n * (5 * F + Wb + 8 + 4 + 40 + 40 + Wb) + nedge * (4 + 5 * F)
+    flux = n * (Wb + Gb + 5 * F) + nedge * (Db + 4 + 5 * F)
+    rhs12 = n * (5 * F + Wb + 8 + 4 + 40 + 40 + Wb) + nedge * 5 * F
     rhs0 = rhs12 + n * 80  # stage 0 also reads U and writes Un
     return {"riecg_grad": grad, "riecg_flux": flux, "riecg_rhs_update": (rhs0 + 2 * rhs12) / 3.0}
 

@@ -97,6 +97,23 @@ def lib():
         L.orc_pcg.restype = _i64
         L.orc_pcg.argtypes = [_i64, _vp, _vp, _vp, _vp, _vp, _i64, _dbl, C.c_int, _vp, _vp, _vp]
         L.orc_csr_mult.argtypes = [_i64, _vp, _vp, _vp, _vp, _vp]
+        L.orc_chocg_create.restype = _vp
+        L.orc_chocg_create.argtypes = ([_i64, _vp, _vp, _i64, _vp, _vp, _i64, _vp, _vp, _vp, _vp,
+                                        _dbl, _dbl, _dbl] + [C.c_int] * 3 +
+                                       [_dbl, C.c_int, C.c_int, _dbl, _i64])
+        L.orc_chocg_destroy.argtypes = [_vp]
+        L.orc_chocg_set_bc.argtypes = [_vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp, _i64, _vp, _i64,
+                                       _vp, _vp]
+        L.orc_chocg_set_state.argtypes = [_vp, _vp, _vp, _dbl]
+        L.orc_chocg_get.argtypes = [_vp, C.c_int, _vp]
+        L.orc_chocg_init.argtypes = [_vp]
+        L.orc_chocg_init.restype = _i64
+        L.orc_chocg_step.argtypes = [_vp, _vp]
+        L.orc_chocg_step.restype = _dbl
+        L.orc_chocg_div.argtypes = [_vp, _vp, _vp, _vp, _dbl, C.c_int, _vp]
+        L.orc_chocg_vgrad.argtypes = [_vp, _vp, C.c_int, _vp]
+        L.orc_chocg_flux.argtypes = [_vp, _vp, _vp, _vp]
+        L.orc_chocg_rhs.argtypes = [_vp, _vp, _vp, _vp, _vp]
     return _lib
 
 
@@ -361,3 +378,88 @@ def csr_mult(ia, ja, a, x):
     r = np.zeros(ia.size - 1)
     lib().orc_csr_mult(ia.size - 1, _p(ia), _p(ja), _p(a), _p(x), _p(r))
     return r
+
+
+# ---------------------------------------------------------------- ChoCG
+
+class ChoCG:
+    """Serial ChoCG (src/Inciter/ChoCG.cpp, src/Physics/Chorin.cpp) over plain
+    edges with ChoCG's five integrals per edge; pressure matrix zero-based."""
+
+    def __init__(self, coord, vol, edge, dint5, tri, ia, ja, a, mu=0.0, cfl=0.5, const_dt=0.0,
+                 flux="damp2", stab=True, stab2=False, stab2coef=0.2, rk=1, pc="jacobi",
+                 ptol=1e-3, pmaxit=10):
+        self._k = [_c(coord, np.float64), _c(vol, np.float64), _c(edge, np.int64),
+                   _c(dint5, np.float64), _c(tri, np.int64), _c(ia, np.int64), _c(ja, np.int64),
+                   _c(a, np.float64)]
+        c, v, e, d, t, i, j, aa = self._k
+        self.n = c.shape[1]
+        self.h = lib().orc_chocg_create(self.n, _p(c), _p(v), e.shape[0], _p(e), _p(d),
+                                        t.shape[0], _p(t), _p(i), _p(j), _p(aa), mu, cfl,
+                                        const_dt, 1 if flux == "damp4" else 0, int(stab),
+                                        int(stab2), stab2coef, rk,
+                                        1 if pc == "jacobi" else 0, ptol, pmaxit)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_chocg_destroy(self.h)
+            self.h = None
+
+    def set_bc(self, dir=None, sym=None, noslip=(), pdir=None):
+        """dir: (nodes, mask (n,3), values (n,3)); sym: (nodes, normals);
+        noslip: nodes; pdir: (nodes, values of the initial solves)."""
+        z = np.zeros(0, np.int64)
+        dn, dm, dv = dir if dir is not None else (z, np.zeros((0, 3)), np.zeros((0, 3)))
+        sn, snv = sym if sym is not None else (z, np.zeros((0, 3)))
+        pn, pv = pdir if pdir is not None else (z, np.zeros(0))
+        k = [_c(dn, np.int64), _c(dm, np.int32), _c(dv, np.float64), _c(sn, np.int64),
+             _c(snv, np.float64), _c(np.asarray(noslip), np.int64), _c(pn, np.int64),
+             _c(pv, np.float64)]
+        self._bc = k
+        lib().orc_chocg_set_bc(self.h, k[0].size, _p(k[0]), _p(k[1]), _p(k[2]), k[3].size,
+                               _p(k[3]), _p(k[4]), k[5].size, _p(k[5]), k[6].size, _p(k[6]),
+                               _p(k[7]))
+
+    def set_state(self, u, p=None, t=0.0):
+        u = _c(u, np.float64)
+        pp = None if p is None else _c(p, np.float64)
+        lib().orc_chocg_set_state(self.h, _p(u), _p(pp), t)
+
+    def get(self, what):
+        shape = {0: (self.n, 3), 1: (self.n, 3), 2: (self.n,), 3: (self.n, 3), 4: (self.n, 9),
+                 5: (self.n,), 6: (self.n,)}[what]
+        out = np.zeros(shape)
+        lib().orc_chocg_get(self.h, what, _p(out))
+        return out
+
+    def init(self):
+        return int(lib().orc_chocg_init(self.h))
+
+    def step(self):
+        it = np.zeros(1, np.int64)
+        dt = lib().orc_chocg_step(self.h, _p(it))
+        return dt, int(it[0])
+
+    def div(self, U, P, G, dt, stab):
+        D = np.zeros(self.n)
+        U, P, G = _c(U, np.float64), _c(P, np.float64), _c(G, np.float64)
+        lib().orc_chocg_div(self.h, _p(U), _p(P), _p(G), dt, int(stab), _p(D))
+        return D
+
+    def vgrad(self, U, ncomp):
+        G = np.zeros((self.n, 3 * ncomp))
+        U = _c(U, np.float64)
+        lib().orc_chocg_vgrad(self.h, _p(U), ncomp, _p(G))
+        return G
+
+    def flux(self, U, G):
+        F = np.zeros((self.n, 3))
+        U, G = _c(U, np.float64), _c(G, np.float64)
+        lib().orc_chocg_flux(self.h, _p(U), _p(G), _p(F))
+        return F
+
+    def rhs(self, U, G, P):
+        R = np.zeros((self.n, 3))
+        U, G, P = _c(U, np.float64), _c(G, np.float64), _c(P, np.float64)
+        lib().orc_chocg_rhs(self.h, _p(U), _p(G), _p(P), _p(R))
+        return R

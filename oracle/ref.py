@@ -39,6 +39,11 @@ def lib():
                                         C.c_int, _vp]
         _lib.ref_chorin_grad.argtypes = [_i64, _vp, _i64, _vp, _vp, _i64, _vp, _vp, _vp]
         _lib.ref_genpsup.argtypes = [_i64, _vp, _vp, _vp, _vp, _vp]
+        _lib.ref_set_chorin.argtypes = [_dbl, C.c_int]
+        _lib.ref_chorin_vgrad.argtypes = [_i64, _vp, _i64, _vp, _vp, _i64, _vp, _i64, _vp, _vp]
+        _lib.ref_chorin_flux.argtypes = [_i64, _vp, _i64, _vp, _vp, _i64, _vp, _vp, _vp, _vp]
+        _lib.ref_chorin_rhs.argtypes = [_i64, _vp, _i64, _vp, _vp, _i64, _vp, _vp, _dbl, _vp, _vp,
+                                        _vp, _vp]
         _lib.ref_csr_pressure.argtypes = [_i64, _vp, _i64, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp,
                                           _vp, _vp]
     return _lib
@@ -171,3 +176,41 @@ def csr_pressure(coord, inpoel, dirnodes=(), dirvals=(), x=None):
                                   _p(dv), _p(xx), _p(nnz), _p(ia), _p(ja), _p(a),
                                   _p(ax) if xx is not None else None, _p(bmod)))
     return ia, ja, a, (ax if xx is not None else None), bmod
+
+
+def set_chorin(mu=0.0, stab=True):
+    lib().ref_set_chorin(mu, int(stab))
+
+
+def chorin_vgrad(coord, edge, dedge5, tri, U):
+    coord = _c(coord, np.float64)
+    n = coord.shape[1]
+    edge, dedge5, tri = _c(edge, np.int64), _c(dedge5, np.float64), _c(tri, np.int64)
+    U = _c(U, np.float64)
+    nc = U.shape[1]
+    G = np.zeros((n, 3 * nc))
+    _check(lib().ref_chorin_vgrad(n, _p(coord), edge.shape[0], _p(edge), _p(dedge5),
+                                  tri.shape[0], _p(tri), nc, _p(U), _p(G)))
+    return G
+
+
+def chorin_flux(coord, edge, dedge5, tri, U, G):
+    coord = _c(coord, np.float64)
+    n = coord.shape[1]
+    edge, dedge5, tri = _c(edge, np.int64), _c(dedge5, np.float64), _c(tri, np.int64)
+    U, G = _c(U, np.float64), _c(G, np.float64)
+    F = np.zeros((n, 3))
+    _check(lib().ref_chorin_flux(n, _p(coord), edge.shape[0], _p(edge), _p(dedge5), tri.shape[0],
+                                 _p(tri), _p(U), _p(G), _p(F)))
+    return F
+
+
+def chorin_rhs(coord, edge, dedge5, tri, vol, P, U, G, t=0.0):
+    coord = _c(coord, np.float64)
+    n = coord.shape[1]
+    edge, dedge5, tri = _c(edge, np.int64), _c(dedge5, np.float64), _c(tri, np.int64)
+    vol, P, U, G = _c(vol, np.float64), _c(P, np.float64), _c(U, np.float64), _c(G, np.float64)
+    R = np.zeros((n, 3))
+    _check(lib().ref_chorin_rhs(n, _p(coord), edge.shape[0], _p(edge), _p(dedge5), tri.shape[0],
+                                _p(tri), _p(vol), t, _p(P), _p(U), _p(G), _p(R)))
+    return R

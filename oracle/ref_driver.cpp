@@ -198,6 +198,75 @@ int ref_chorin_grad(int64_t npoin, const double* xyz, int64_t n2, const int64_t*
   return 0;
 }
 
+// The viscosity and advection stabilisation switch chorin::rhs/flux read.
+int ref_set_chorin(double mu, int stab) {
+  g_cfg.get<tag::mat_dyn_viscosity>() = mu;
+  g_cfg.get<tag::stab>() = stab != 0;
+  return 0;
+}
+
+// chorin::vgrad (src/Physics/Chorin.cpp:211-334) over edge groups only.
+int ref_chorin_vgrad(int64_t npoin, const double* xyz, int64_t n2, const int64_t* e2,
+                     const double* i2, int64_t ntri, const int64_t* tri, int64_t ncomp,
+                     const double* U, double* G) {
+  try {
+    std::array<std::vector<std::size_t>, 3> sup{{{}, {}, ids(e2, n2 * 2)}};
+    std::array<std::vector<tk::real>, 3> sint{{{}, {}, std::vector<tk::real>(i2, i2 + n2 * 5)}};
+    auto coord = make_coord(npoin, xyz);
+    auto u = make_fields(npoin, ncomp, U);
+    tk::Fields g(static_cast<std::size_t>(npoin), static_cast<std::size_t>(ncomp * 3));
+    g.fill(0.0);
+    chorin::vgrad(sup, sint, coord, ids(tri, ntri * 3), u, g);
+    read_fields(g, G);
+  } catch (std::exception& e) {
+    g_err = e.what();
+    return 1;
+  }
+  return 0;
+}
+
+// chorin::flux (src/Physics/Chorin.cpp:509-638) over edge groups only.
+int ref_chorin_flux(int64_t npoin, const double* xyz, int64_t n2, const int64_t* e2,
+                    const double* i2, int64_t ntri, const int64_t* tri, const double* U,
+                    const double* G, double* F) {
+  try {
+    std::array<std::vector<std::size_t>, 3> sup{{{}, {}, ids(e2, n2 * 2)}};
+    std::array<std::vector<tk::real>, 3> sint{{{}, {}, std::vector<tk::real>(i2, i2 + n2 * 5)}};
+    auto coord = make_coord(npoin, xyz);
+    auto u = make_fields(npoin, 3, U);
+    auto g = make_fields(npoin, 9, G);
+    tk::Fields f(static_cast<std::size_t>(npoin), 3);
+    f.fill(0.0);
+    chorin::flux(sup, sint, coord, ids(tri, ntri * 3), u, g, f);
+    read_fields(f, F);
+  } catch (std::exception& e) {
+    g_err = e.what();
+    return 1;
+  }
+  return 0;
+}
+
+// chorin::rhs (src/Physics/Chorin.cpp:1010-1044) over edge groups only.
+int ref_chorin_rhs(int64_t npoin, const double* xyz, int64_t n2, const int64_t* e2,
+                   const double* i2, int64_t ntri, const int64_t* tri, const double* vol,
+                   double t, const double* P, const double* U, const double* G, double* R) {
+  try {
+    std::array<std::vector<std::size_t>, 3> sup{{{}, {}, ids(e2, n2 * 2)}};
+    std::array<std::vector<tk::real>, 3> sint{{{}, {}, std::vector<tk::real>(i2, i2 + n2 * 5)}};
+    auto coord = make_coord(npoin, xyz);
+    auto u = make_fields(npoin, 3, U);
+    auto g = make_fields(npoin, 9, G);
+    tk::Fields r(static_cast<std::size_t>(npoin), 3);
+    std::vector<tk::real> v(vol, vol + npoin), p(P, P + npoin);
+    chorin::rhs(sup, sint, coord, ids(tri, ntri * 3), v, t, p, u, g, r);
+    read_fields(r, R);
+  } catch (std::exception& e) {
+    g_err = e.what();
+    return 1;
+  }
+  return 0;
+}
+
 // tk::genPsup (src/Mesh/DerivedData.cpp:132-250): returns sizes first when the
 // output pointers are null.
 int ref_genpsup(int64_t nelem, const int64_t* inpoel, int64_t* n1, int64_t* n2,

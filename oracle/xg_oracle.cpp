@@ -30,6 +30,14 @@
 #include <string>
 #include <vector>
 
+extern "C" {
+void orc_csr_dirichlet(int64_t n, const int64_t* ia, const int64_t* ja, double* a, double* b,
+                       int64_t ndir, const int64_t* nodes, const double* vals);
+int64_t orc_pcg(int64_t n, const int64_t* ia, const int64_t* ja, const double* a,
+                const double* b, double* x, int64_t maxit, double tol, int pc,
+                double* normr_out, double* normb_out, int* converged);
+}
+
 namespace {
 
 using real = double;
@@ -708,6 +716,427 @@ void csr_mult(const CG& A, const real* x, real* r) {
   }
 }
 
+
+// --------------------------------------------------------------------------
+// ChoCG (src/Inciter/ChoCG.cpp, src/Physics/Chorin.cpp) over plain edges:
+// each edge (p,q) carries ChoCG's five integrals d[0..2] (dual-face normal),
+// d[3] = J/120 and d[4] = grad_p.grad_q/J/6 (ChoCG::domint,
+// src/Inciter/ChoCG.cpp:398-445) and contributes -f to p and +f to q, as the
+// edge group of the chorin:: loops does (Chorin.cpp:160-170, 264-277, ...).
+struct ChoCG {
+  int64_t n = 0;
+  std::vector<real> xyz, vol;
+  std::vector<int64_t> edge;  // 2 per edge
+  std::vector<real> dint;     // 5 per edge
+  std::vector<int64_t> tri;   // boundary triangles
+  real mu = 0, cfl = 0.5, const_dt = 0, stab2coef = 0.2;
+  int damp4 = 0, stab = 1, stab2 = 0, rk = 1;
+  // velocity BCs (ChoCG::BC, src/Inciter/ChoCG.cpp:1333-1354)
+  std::vector<int64_t> dirn;
+  std::vector<int32_t> dirmask;  // 3 per node
+  std::vector<real> dirval;      // 3 per node
+  std::vector<int64_t> symn;
+  std::vector<real> symnorm;
+  std::vector<int64_t> noslip;
+  // pressure Dirichlet nodes and the values of the initial solves
+  std::vector<int64_t> pdirn;
+  std::vector<real> pdirval;
+  // pressure system (ChoCG::prelhs) and its solver settings
+  CG A;
+  int pc = 1;
+  real ptol = 1e-3;
+  int64_t pmaxit = 10;
+  // state
+  std::vector<real> u, un, pr, pgrad, vgrad, flx, div, sgrad, rhs, sol;
+  real t = 0, dt = 0;
+  int np = 0;
+  int64_t last_it = 0;
+  real last_normr = 0, last_normb = 0;
+};
+
+inline real cx(const ChoCG& s, int64_t p) { return s.xyz[p]; }
+inline real cy(const ChoCG& s, int64_t p) { return s.xyz[s.n + p]; }
+inline real cz(const ChoCG& s, int64_t p) { return s.xyz[2 * s.n + p]; }
+
+// Boundary-face normal / 6 of triangle e (tk::crossdiv(..., 6.0)).
+inline void cho_tri_normal(const ChoCG& s, int64_t e, real n[3]) {
+  const int64_t* N = &s.tri[e * 3];
+  cross(cx(s, N[1]) - cx(s, N[0]), cy(s, N[1]) - cy(s, N[0]), cz(s, N[1]) - cz(s, N[0]),
+        cx(s, N[2]) - cx(s, N[0]), cy(s, N[2]) - cy(s, N[0]), cz(s, N[2]) - cz(s, N[0]), n[0],
+        n[1], n[2]);
+  n[0] /= 6.0;
+  n[1] /= 6.0;
+  n[2] /= 6.0;
+}
+
+// chorin::div (src/Physics/Chorin.cpp:34-83 per edge, 85-209 loops):
+// divergence of U (3 components) with 4th-order pressure damping when stab.
+void cho_div(const ChoCG& s, const real* U, const real* P, const real* G, real dt, bool stab,
+             real* D) {
+  for (int64_t e = 0; e < static_cast<int64_t>(s.edge.size() / 2); ++e) {
+    const int64_t p = s.edge[2 * e], q = s.edge[2 * e + 1];
+    const real* d = &s.dint[5 * e];
+    real f = d[0] * (U[p * 3 + 0] + U[q * 3 + 0]) + d[1] * (U[p * 3 + 1] + U[q * 3 + 1]) +
+             d[2] * (U[p * 3 + 2] + U[q * 3 + 2]);
+    if (stab) {
+      real dx = cx(s, p) - cx(s, q), dy = cy(s, p) - cy(s, q), dz = cz(s, p) - cz(s, q);
+      real dl = std::sqrt(dx * dx + dy * dy + dz * dz);
+      real p2 = P[q] - P[p];
+      real Dn = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+      real dpx = G[p * 3 + 0] + G[q * 3 + 0];
+      real dpy = G[p * 3 + 1] + G[q * 3 + 1];
+      real dpz = G[p * 3 + 2] + G[q * 3 + 2];
+      real p4 = 0.5 * (dx * dpx + dy * dpy + dz * dpz);
+      f += Dn * dt / dl * (p2 + p4);
+    }
+    D[p] -= f;
+    D[q] += f;
+  }
+  for (int64_t e = 0; e < static_cast<int64_t>(s.tri.size() / 3); ++e) {
+    const int64_t* N = &s.tri[e * 3];
+    real n[3];
+    cho_tri_normal(s, e, n);
+    real uA[3], uB[3], uC[3];
+    for (int c = 0; c < 3; ++c) {
+      uA[c] = U[N[0] * 3 + c];
+      uB[c] = U[N[1] * 3 + c];
+      uC[c] = U[N[2] * 3 + c];
+    }
+    real ux = (6.0 * uA[0] + uB[0] + uC[0]) / 8.0;
+    real uy = (6.0 * uA[1] + uB[1] + uC[1]) / 8.0;
+    real uz = (6.0 * uA[2] + uB[2] + uC[2]) / 8.0;
+    D[N[0]] += ux * n[0] + uy * n[1] + uz * n[2];
+    ux = (uA[0] + 6.0 * uB[0] + uC[0]) / 8.0;
+    uy = (uA[1] + 6.0 * uB[1] + uC[1]) / 8.0;
+    uz = (uA[2] + 6.0 * uB[2] + uC[2]) / 8.0;
+    D[N[1]] += ux * n[0] + uy * n[1] + uz * n[2];
+    ux = (uA[0] + uB[0] + 6.0 * uC[0]) / 8.0;
+    uy = (uA[1] + uB[1] + 6.0 * uC[1]) / 8.0;
+    uz = (uA[2] + uB[2] + 6.0 * uC[2]) / 8.0;
+    D[N[2]] += ux * n[0] + uy * n[1] + uz * n[2];
+  }
+}
+
+// chorin::vgrad (Chorin.cpp:211-334) for ncomp components into G (ncomp*3);
+// chorin::grad (Chorin.cpp:336-449) is the ncomp = 1 case.
+void cho_vgrad(const ChoCG& s, const real* U, int ncomp, real* G) {
+  const int nc3 = ncomp * 3;
+  for (int64_t e = 0; e < static_cast<int64_t>(s.edge.size() / 2); ++e) {
+    const int64_t p = s.edge[2 * e], q = s.edge[2 * e + 1];
+    const real* d = &s.dint[5 * e];
+    for (int i = 0; i < ncomp; ++i) {
+      const real u0 = U[p * ncomp + i], u1 = U[q * ncomp + i];
+      for (int j = 0; j < 3; ++j) {
+        real f = d[j] * (u1 + u0);
+        G[p * nc3 + i * 3 + j] -= f;
+        G[q * nc3 + i * 3 + j] += f;
+      }
+    }
+  }
+  for (int64_t e = 0; e < static_cast<int64_t>(s.tri.size() / 3); ++e) {
+    const int64_t* N = &s.tri[e * 3];
+    real n[3];
+    cho_tri_normal(s, e, n);
+    for (int i = 0; i < ncomp; ++i) {
+      real u[3] = {U[N[0] * ncomp + i], U[N[1] * ncomp + i], U[N[2] * ncomp + i]};
+      real f = (6.0 * u[0] + u[1] + u[2]) / 8.0;
+      for (int j = 0; j < 3; ++j) G[N[0] * nc3 + i * 3 + j] += f * n[j];
+      f = (u[0] + 6.0 * u[1] + u[2]) / 8.0;
+      for (int j = 0; j < 3; ++j) G[N[1] * nc3 + i * 3 + j] += f * n[j];
+      f = (u[0] + u[1] + 6.0 * u[2]) / 8.0;
+      for (int j = 0; j < 3; ++j) G[N[2] * nc3 + i * 3 + j] += f * n[j];
+    }
+  }
+}
+
+// Momentum flux of one tensor component over edge p-q and in point p
+// (chorin flux, Chorin.cpp:451-507).
+inline real cho_flux_e(const ChoCG& s, const real* U, const real* G, int i, int j, int64_t p,
+                       int64_t q) {
+  real inv = U[p * 3 + i] * U[p * 3 + j] + U[q * 3 + i] * U[q * 3 + j];
+  const real eps = std::numeric_limits<real>::epsilon();
+  if (s.mu < eps) return -inv;
+  real vis = G[p * 9 + i * 3 + j] + G[p * 9 + j * 3 + i] + G[q * 9 + i * 3 + j] +
+             G[q * 9 + j * 3 + i];
+  if (i == j)
+    vis -= 2.0 / 3.0 * (G[p * 9 + 0] + G[p * 9 + 4] + G[p * 9 + 8] + G[q * 9 + 0] +
+                        G[q * 9 + 4] + G[q * 9 + 8]);
+  return s.mu * vis - inv;
+}
+inline real cho_flux_p(const ChoCG& s, const real* U, const real* G, int i, int j, int64_t p) {
+  real inv = U[p * 3 + i] * U[p * 3 + j];
+  const real eps = std::numeric_limits<real>::epsilon();
+  if (s.mu < eps) return -inv;
+  real vis = G[p * 9 + i * 3 + j] + G[p * 9 + j * 3 + i];
+  if (i == j) vis -= 2.0 / 3.0 * (G[p * 9 + 0] + G[p * 9 + 4] + G[p * 9 + 8]);
+  return s.mu * vis - inv;
+}
+
+// chorin::flux (Chorin.cpp:509-638): F_i = d[s_ij - u_i u_j]/dx_j.
+void cho_flux(const ChoCG& s, const real* U, const real* G, real* F) {
+  for (int64_t e = 0; e < static_cast<int64_t>(s.edge.size() / 2); ++e) {
+    const int64_t p = s.edge[2 * e], q = s.edge[2 * e + 1];
+    const real* d = &s.dint[5 * e];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        real f = d[j] * cho_flux_e(s, U, G, i, j, q, p);
+        F[p * 3 + i] -= f;
+        F[q * 3 + i] += f;
+      }
+  }
+  for (int64_t e = 0; e < static_cast<int64_t>(s.tri.size() / 3); ++e) {
+    const int64_t* N = &s.tri[e * 3];
+    real n[3];
+    cho_tri_normal(s, e, n);
+    for (int i = 0; i < 3; ++i) {
+      real fxA = cho_flux_p(s, U, G, i, 0, N[0]), fyA = cho_flux_p(s, U, G, i, 1, N[0]),
+           fzA = cho_flux_p(s, U, G, i, 2, N[0]);
+      real fxB = cho_flux_p(s, U, G, i, 0, N[1]), fyB = cho_flux_p(s, U, G, i, 1, N[1]),
+           fzB = cho_flux_p(s, U, G, i, 2, N[1]);
+      real fxC = cho_flux_p(s, U, G, i, 0, N[2]), fyC = cho_flux_p(s, U, G, i, 1, N[2]),
+           fzC = cho_flux_p(s, U, G, i, 2, N[2]);
+      real fx = (6.0 * fxA + fxB + fxC) / 8.0;
+      real fy = (6.0 * fyA + fyB + fyC) / 8.0;
+      real fz = (6.0 * fzA + fzB + fzC) / 8.0;
+      F[N[0] * 3 + i] += fx * n[0] + fy * n[1] + fz * n[2];
+      fx = (fxA + 6.0 * fxB + fxC) / 8.0;
+      fy = (fyA + 6.0 * fyB + fyC) / 8.0;
+      fz = (fzA + 6.0 * fzB + fzC) / 8.0;
+      F[N[1] * 3 + i] += fx * n[0] + fy * n[1] + fz * n[2];
+      fx = (fxA + fxB + 6.0 * fxC) / 8.0;
+      fy = (fyA + fyB + 6.0 * fyC) / 8.0;
+      fz = (fzA + fzB + 6.0 * fzC) / 8.0;
+      F[N[2] * 3 + i] += fx * n[0] + fy * n[1] + fz * n[2];
+    }
+  }
+}
+
+// adv_damp2 / adv_damp4 edge fluxes of the three velocity components
+// (Chorin.cpp:640-709, 711-829), no transported scalars.
+void cho_adv_edge(const ChoCG& s, const real* d, const real* U, const real* G, const real* P,
+                  int64_t p, int64_t q, real f[3]) {
+  real uL[3] = {U[p * 3 + 0], U[p * 3 + 1], U[p * 3 + 2]};
+  real uR[3] = {U[q * 3 + 0], U[q * 3 + 1], U[q * 3 + 2]};
+  if (s.damp4) {
+    const real eps = 1.0e-9, k = 1.0 / 3.0;
+    real dx = cx(s, q) - cx(s, p), dy = cy(s, q) - cy(s, p), dz = cz(s, q) - cz(s, p);
+    for (int c = 0; c < 3; ++c) {
+      real g1 = G[p * 9 + c * 3 + 0] * dx + G[p * 9 + c * 3 + 1] * dy + G[p * 9 + c * 3 + 2] * dz;
+      real g2 = G[q * 9 + c * 3 + 0] * dx + G[q * 9 + c * 3 + 1] * dy + G[q * 9 + c * 3 + 2] * dz;
+      real delta2 = uR[c] - uL[c];
+      real delta1 = 2.0 * g1 - delta2;
+      real delta3 = 2.0 * g2 - delta2;
+      real rL = (delta2 + eps) / (delta1 + eps);
+      real rR = (delta2 + eps) / (delta3 + eps);
+      real rLinv = (delta1 + eps) / (delta2 + eps);
+      real rRinv = (delta3 + eps) / (delta2 + eps);
+      real phiL = (std::abs(rL) + rL) / (std::abs(rL) + 1.0);
+      real phiR = (std::abs(rR) + rR) / (std::abs(rR) + 1.0);
+      real phi_L_inv = (std::abs(rLinv) + rLinv) / (std::abs(rLinv) + 1.0);
+      real phi_R_inv = (std::abs(rRinv) + rRinv) / (std::abs(rRinv) + 1.0);
+      uL[c] += 0.25 * (delta1 * (1.0 - k) * phiL + delta2 * (1.0 + k) * phi_L_inv);
+      uR[c] -= 0.25 * (delta3 * (1.0 - k) * phiR + delta2 * (1.0 + k) * phi_R_inv);
+    }
+  }
+  const real nx = d[0], ny = d[1], nz = d[2];
+  real vnL = uL[0] * nx + uL[1] * ny + uL[2] * nz;
+  real vnR = uR[0] * nx + uR[1] * ny + uR[2] * nz;
+  real aw = 0.0;
+  if (s.stab) aw = std::abs(vnL + vnR) / 2.0;
+  if (s.stab2) {
+    real sl = std::abs(vnL), sr = std::abs(vnR);
+    aw += s.stab2coef * std::max(sl, sr);
+  }
+  real v = d[4] * s.mu;
+  real pf = P[p] + P[q];
+  if (s.damp4) {
+    f[0] = uL[0] * vnL + uR[0] * vnR + pf * nx + aw * (uR[0] - uL[0]) - v * (U[q * 3 + 0] - U[p * 3 + 0]);
+    f[1] = uL[1] * vnL + uR[1] * vnR + pf * ny + aw * (uR[1] - uL[1]) - v * (U[q * 3 + 1] - U[p * 3 + 1]);
+    f[2] = uL[2] * vnL + uR[2] * vnR + pf * nz + aw * (uR[2] - uL[2]) - v * (U[q * 3 + 2] - U[p * 3 + 2]);
+  } else {
+    f[0] = uL[0] * vnL + uR[0] * vnR + pf * nx + (aw - v) * (uR[0] - uL[0]);
+    f[1] = uL[1] * vnL + uR[1] * vnR + pf * ny + (aw - v) * (uR[1] - uL[1]);
+    f[2] = uL[2] * vnL + uR[2] * vnR + pf * nz + (aw - v) * (uR[2] - uL[2]);
+  }
+}
+
+// chorin::rhs = adv (Chorin.cpp:831-982, 1010-1044); no source term.
+void cho_rhs(const ChoCG& s, const real* U, const real* G, const real* P, real* R) {
+  std::fill(R, R + s.n * 3, 0.0);
+  for (int64_t e = 0; e < static_cast<int64_t>(s.edge.size() / 2); ++e) {
+    const int64_t p = s.edge[2 * e], q = s.edge[2 * e + 1];
+    real f[3];
+    cho_adv_edge(s, &s.dint[5 * e], U, G, P, p, q, f);
+    for (int c = 0; c < 3; ++c) {
+      R[p * 3 + c] -= f[c];
+      R[q * 3 + c] += f[c];
+    }
+  }
+  for (int64_t e = 0; e < static_cast<int64_t>(s.tri.size() / 3); ++e) {
+    const int64_t* N = &s.tri[e * 3];
+    real n[3];
+    cho_tri_normal(s, e, n);
+    real f[3][3];
+    for (int a = 0; a < 3; ++a) {
+      real u = U[N[a] * 3 + 0], v = U[N[a] * 3 + 1], w = U[N[a] * 3 + 2], pp = P[N[a]];
+      real vn = n[0] * u + n[1] * v + n[2] * w;
+      f[0][a] = u * vn + pp * n[0];
+      f[1][a] = v * vn + pp * n[1];
+      f[2][a] = w * vn + pp * n[2];
+    }
+    for (int c = 0; c < 3; ++c) {
+      R[N[0] * 3 + c] += (6.0 * f[c][0] + f[c][1] + f[c][2]) / 8.0;
+      R[N[1] * 3 + c] += (f[c][0] + 6.0 * f[c][1] + f[c][2]) / 8.0;
+      R[N[2] * 3 + c] += (f[c][0] + f[c][1] + 6.0 * f[c][2]) / 8.0;
+    }
+  }
+}
+
+// ChoCG::fingrad (src/Inciter/ChoCG.cpp:841-866): divide by the nodal volume.
+void cho_fingrad(const ChoCG& s, real* G, int nprop) {
+  for (int64_t p = 0; p < s.n; ++p)
+    for (int c = 0; c < nprop; ++c) G[p * nprop + c] /= s.vol[p];
+}
+
+// physics::symbc on a 3-component field (src/Physics/BC.cpp:108-132).
+void cho_symbc(const ChoCG& s, real* U) {
+  for (size_t i = 0; i < s.symn.size(); ++i) {
+    const int64_t p = s.symn[i];
+    const real* nn = &s.symnorm[i * 3];
+    real vn = U[p * 3 + 0] * nn[0] + U[p * 3 + 1] * nn[1] + U[p * 3 + 2] * nn[2];
+    U[p * 3 + 0] -= vn * nn[0];
+    U[p * 3 + 1] -= vn * nn[1];
+    U[p * 3 + 2] -= vn * nn[2];
+  }
+}
+
+// ChoCG::BC (src/Inciter/ChoCG.cpp:1333-1354): dirbc (time-independent
+// values per node, src/Physics/BC.cpp:27-70), symbc, noslipbc (BC.cpp:134-145).
+void cho_bc(ChoCG& s, real* U) {
+  for (size_t i = 0; i < s.dirn.size(); ++i) {
+    const int64_t p = s.dirn[i];
+    for (int c = 0; c < 3; ++c)
+      if (s.dirmask[i * 3 + c]) U[p * 3 + c] = s.dirval[i * 3 + c];
+  }
+  cho_symbc(s, U);
+  for (int64_t p : s.noslip) U[p * 3 + 0] = U[p * 3 + 1] = U[p * 3 + 2] = 0.0;
+}
+
+// ChoCG::dt (src/Inciter/ChoCG.cpp:1356-1412), freezeflow 1, no scalars.
+real cho_dt(const ChoCG& s) {
+  const real eps = std::numeric_limits<real>::epsilon();
+  if (std::abs(s.const_dt) > eps) return s.const_dt;
+  real mindt = std::numeric_limits<real>::max();
+  const real large = std::numeric_limits<real>::max();
+  const real dif = s.mu;  // max(mu, diffusivity 0)
+  for (int64_t i = 0; i < s.n; ++i) {
+    real u = s.u[i * 3 + 0], v = s.u[i * 3 + 1], w = s.u[i * 3 + 2];
+    real vel = std::sqrt(u * u + v * v + w * w);
+    real L = std::cbrt(s.vol[i]);
+    real euler_dt = L / std::max(vel, 1.0e-8);
+    mindt = std::min(mindt, euler_dt);
+    real dif_dt = dif > eps ? L * L / dif : large;
+    mindt = std::min(mindt, dif_dt);
+  }
+  return mindt * s.cfl;
+}
+
+// Serial PCG of the pressure system (ConjugateGradients::init with apply =
+// true, then solve; src/LinearSolver/ConjugateGradients.cpp:335-823): the
+// Dirichlet rows and columns of a copy of A are eliminated in decreasing node
+// order (CSR::dirichlet, src/LinearSolver/CSR.cpp:106-152), x warm-starts from
+// the previous solution.
+void cho_psolve(ChoCG& s, const real* b, const std::vector<real>& dval) {
+  std::vector<real> a = s.A.a, bb(b, b + s.n);
+  std::vector<int64_t> nodes = s.pdirn;
+  orc_csr_dirichlet(s.n, s.A.ia.data(), s.A.ja.data(), a.data(), bb.data(),
+                    static_cast<int64_t>(nodes.size()), nodes.data(), dval.data());
+  int conv = 0;
+  s.last_it = orc_pcg(s.n, s.A.ia.data(), s.A.ja.data(), a.data(), bb.data(), s.sol.data(),
+                      s.pmaxit, s.ptol, s.pc, &s.last_normr, &s.last_normb, &conv);
+}
+
+// The initial projection of ChoCG::merge -> div -> pinit -> psolve -> sgrad ->
+// psolved (m_np = 0), then velgrad -> flux -> div -> pinit -> psolve ->
+// psolved (m_np = 1) and pgrad (src/Inciter/ChoCG.cpp:739-764, 868-1281).
+void cho_init(ChoCG& s) {
+  const int64_t n = s.n;
+  s.np = 0;
+  cho_bc(s, s.u.data());
+  // m_np = 0: divergence of u without stabilisation, Dirichlet values as set
+  std::fill(s.div.begin(), s.div.end(), 0.0);
+  cho_div(s, s.u.data(), s.pr.data(), s.pgrad.data(), s.dt, false, s.div.data());
+  cho_psolve(s, s.div.data(), s.pdirval);
+  std::fill(s.sgrad.begin(), s.sgrad.end(), 0.0);
+  cho_vgrad(s, s.sol.data(), 1, s.sgrad.data());
+  cho_fingrad(s, s.sgrad.data(), 3);
+  for (int64_t i = 0; i < n; ++i)
+    for (int c = 0; c < 3; ++c) s.u[i * 3 + c] -= 1.0 * s.sgrad[i * 3 + c];
+  cho_bc(s, s.u.data());
+  // m_np = 1: momentum flux of the projected field as the Poisson rhs
+  s.np = 1;
+  std::fill(s.vgrad.begin(), s.vgrad.end(), 0.0);
+  cho_vgrad(s, s.u.data(), 3, s.vgrad.data());
+  cho_fingrad(s, s.vgrad.data(), 9);
+  std::fill(s.flx.begin(), s.flx.end(), 0.0);
+  cho_flux(s, s.u.data(), s.vgrad.data(), s.flx.data());
+  cho_fingrad(s, s.flx.data(), 3);
+  cho_symbc(s, s.flx.data());
+  std::fill(s.div.begin(), s.div.end(), 0.0);
+  cho_div(s, s.flx.data(), s.pr.data(), s.pgrad.data(), s.dt, false, s.div.data());
+  cho_psolve(s, s.div.data(), s.pdirval);
+  // m_np = 2: initial pressure and its gradient
+  s.np = 2;
+  s.pr = s.sol;
+  std::fill(s.pgrad.begin(), s.pgrad.end(), 0.0);
+  cho_vgrad(s, s.pr.data(), 1, s.pgrad.data());
+  cho_fingrad(s, s.pgrad.data(), 3);
+}
+
+// One time step: dt -> rk stages of rhs/solve/pred(BC, damp4 vgrad) -> div
+// (stabilised) / dt -> pressure-increment solve (Dirichlet values 0) ->
+// sgrad -> projection and BC -> pressure update and pgrad -> t += dt
+// (src/Inciter/ChoCG.cpp:1356-1695, 868-1281).
+real cho_step(ChoCG& s) {
+  static const real rkc[4][4] = {{1.0, 0, 0, 0},
+                                 {1.0 / 2.0, 1.0, 0, 0},
+                                 {1.0 / 3.0, 1.0 / 2.0, 1.0, 0},
+                                 {1.0 / 4.0, 1.0 / 3.0, 1.0 / 2.0, 1.0}};
+  const int64_t n = s.n;
+  s.dt = cho_dt(s);
+  for (int st = 0; st < s.rk; ++st) {
+    cho_rhs(s, s.u.data(), s.vgrad.data(), s.pr.data(), s.rhs.data());
+    if (st == 0) s.un = s.u;
+    const real dtk = rkc[s.rk - 1][st] * s.dt;
+    for (int64_t i = 0; i < n; ++i)
+      for (int c = 0; c < 3; ++c)
+        s.u[i * 3 + c] = s.un[i * 3 + c] - dtk * s.rhs[i * 3 + c] / s.vol[i];
+    cho_bc(s, s.u.data());
+    if (s.damp4) {
+      std::fill(s.vgrad.begin(), s.vgrad.end(), 0.0);
+      cho_vgrad(s, s.u.data(), 3, s.vgrad.data());
+      cho_fingrad(s, s.vgrad.data(), 9);
+    }
+  }
+  std::fill(s.div.begin(), s.div.end(), 0.0);
+  cho_div(s, s.u.data(), s.pr.data(), s.pgrad.data(), s.dt, true, s.div.data());
+  for (auto& d : s.div) d /= s.dt;
+  std::vector<real> zero(s.pdirn.size(), 0.0);
+  cho_psolve(s, s.div.data(), zero);
+  std::fill(s.sgrad.begin(), s.sgrad.end(), 0.0);
+  cho_vgrad(s, s.sol.data(), 1, s.sgrad.data());
+  cho_fingrad(s, s.sgrad.data(), 3);
+  for (int64_t i = 0; i < n; ++i)
+    for (int c = 0; c < 3; ++c) s.u[i * 3 + c] -= s.dt * s.sgrad[i * 3 + c];
+  cho_bc(s, s.u.data());
+  for (int64_t i = 0; i < n; ++i) s.pr[i] += s.sol[i];
+  std::fill(s.pgrad.begin(), s.pgrad.end(), 0.0);
+  cho_vgrad(s, s.pr.data(), 1, s.pgrad.data());
+  cho_fingrad(s, s.pgrad.data(), 3);
+  s.t += s.dt;
+  return s.dt;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1166,6 +1595,135 @@ void orc_csr_mult(int64_t n, const int64_t* ia, const int64_t* ja, const double*
   A.ja.assign(ja, ja + ia[n]);
   A.a.assign(a, a + ia[n]);
   csr_mult(A, x, r);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- ChoCG
+
+extern "C" {
+
+// ChoCG state over plain edges (2 ids + 5 integrals each), boundary triangles
+// and the zero-based pressure matrix of ChoCG::prelhs.  flux: 0 damp2,
+// 1 damp4; pc: 0 none, 1 jacobi.
+void* orc_chocg_create(int64_t npoin, const double* xyz, const double* vol, int64_t nedge,
+                       const int64_t* edges, const double* dint, int64_t ntri, const int64_t* tri,
+                       const int64_t* ia, const int64_t* ja, const double* a, double mu,
+                       double cfl, double const_dt, int damp4, int stab, int stab2,
+                       double stab2coef, int rk, int pc, double ptol, int64_t pmaxit) {
+  auto* s = new ChoCG;
+  s->n = npoin;
+  s->xyz.assign(xyz, xyz + 3 * npoin);
+  s->vol.assign(vol, vol + npoin);
+  s->edge.assign(edges, edges + 2 * nedge);
+  s->dint.assign(dint, dint + 5 * nedge);
+  s->tri.assign(tri, tri + 3 * ntri);
+  s->A.n = npoin;
+  s->A.ia.assign(ia, ia + npoin + 1);
+  s->A.ja.assign(ja, ja + ia[npoin]);
+  s->A.a.assign(a, a + ia[npoin]);
+  s->mu = mu;
+  s->cfl = cfl;
+  s->const_dt = const_dt;
+  s->damp4 = damp4;
+  s->stab = stab;
+  s->stab2 = stab2;
+  s->stab2coef = stab2coef;
+  s->rk = rk;
+  s->pc = pc;
+  s->ptol = ptol;
+  s->pmaxit = pmaxit;
+  const size_t n = static_cast<size_t>(npoin);
+  s->u.assign(3 * n, 0.0);
+  s->un.assign(3 * n, 0.0);
+  s->pr.assign(n, 0.0);
+  s->pgrad.assign(3 * n, 0.0);
+  s->vgrad.assign(9 * n, 0.0);
+  s->flx.assign(3 * n, 0.0);
+  s->div.assign(n, 0.0);
+  s->sgrad.assign(3 * n, 0.0);
+  s->rhs.assign(3 * n, 0.0);
+  s->sol.assign(n, 0.0);
+  return s;
+}
+
+void orc_chocg_destroy(void* h) { delete static_cast<ChoCG*>(h); }
+
+void orc_chocg_set_bc(void* h, int64_t ndir, const int64_t* dirn, const int32_t* dirmask,
+                      const double* dirval, int64_t nsym, const int64_t* symn,
+                      const double* symnorm, int64_t nnoslip, const int64_t* noslip,
+                      int64_t npdir, const int64_t* pdirn, const double* pdirval) {
+  auto* s = static_cast<ChoCG*>(h);
+  s->dirn.assign(dirn, dirn + ndir);
+  s->dirmask.assign(dirmask, dirmask + 3 * ndir);
+  s->dirval.assign(dirval, dirval + 3 * ndir);
+  s->symn.assign(symn, symn + nsym);
+  s->symnorm.assign(symnorm, symnorm + 3 * nsym);
+  s->noslip.assign(noslip, noslip + nnoslip);
+  s->pdirn.assign(pdirn, pdirn + npdir);
+  s->pdirval.assign(pdirval, pdirval + npdir);
+}
+
+void orc_chocg_set_state(void* h, const double* u, const double* p, double t) {
+  auto* s = static_cast<ChoCG*>(h);
+  s->u.assign(u, u + 3 * s->n);
+  if (p) s->pr.assign(p, p + s->n);
+  s->t = t;
+}
+
+// what: 0 u (n x 3), 1 un, 2 pressure, 3 pressure gradient (n x 3),
+// 4 velocity gradient (n x 9), 5 divergence (n), 6 last pressure solution (n).
+void orc_chocg_get(void* h, int what, double* out) {
+  auto* s = static_cast<ChoCG*>(h);
+  const std::vector<real>* v = nullptr;
+  switch (what) {
+    case 0: v = &s->u; break;
+    case 1: v = &s->un; break;
+    case 2: v = &s->pr; break;
+    case 3: v = &s->pgrad; break;
+    case 4: v = &s->vgrad; break;
+    case 5: v = &s->div; break;
+    default: v = &s->sol; break;
+  }
+  std::memcpy(out, v->data(), v->size() * sizeof(double));
+}
+
+// Initial projection and pressure; returns the iterations of the last solve.
+int64_t orc_chocg_init(void* h) {
+  auto* s = static_cast<ChoCG*>(h);
+  cho_init(*s);
+  return s->last_it;
+}
+
+// One time step; returns dt and writes the pressure-solve iterations.
+double orc_chocg_step(void* h, int64_t* it) {
+  auto* s = static_cast<ChoCG*>(h);
+  double dt = cho_step(*s);
+  if (it) *it = s->last_it;
+  return dt;
+}
+
+// Single chorin:: passes on caller arrays (for pinning and drop-in parity):
+// raw weak results, nothing divided by the volume.
+void orc_chocg_div(void* h, const double* U, const double* P, const double* G, double dt,
+                   int stab, double* D) {
+  auto* s = static_cast<ChoCG*>(h);
+  std::fill(D, D + s->n, 0.0);
+  cho_div(*s, U, P, G, dt, stab != 0, D);
+}
+void orc_chocg_vgrad(void* h, const double* U, int ncomp, double* G) {
+  auto* s = static_cast<ChoCG*>(h);
+  std::fill(G, G + s->n * ncomp * 3, 0.0);
+  cho_vgrad(*s, U, ncomp, G);
+}
+void orc_chocg_flux(void* h, const double* U, const double* G, double* F) {
+  auto* s = static_cast<ChoCG*>(h);
+  std::fill(F, F + s->n * 3, 0.0);
+  cho_flux(*s, U, G, F);
+}
+void orc_chocg_rhs(void* h, const double* U, const double* G, const double* P, double* R) {
+  auto* s = static_cast<ChoCG*>(h);
+  cho_rhs(*s, U, G, P, R);
 }
 
 }  // extern "C"

@@ -98,3 +98,44 @@ def dirichlet_matrix_only(ia, ja, a, i):
     for j in range(ia[i], ia[i + 1]):
         a[j] = 1.0 if ja[j] == i else 0.0
     return a
+
+
+def chocg_mesh(name):
+    """ChoCG regression fixture ("lid" or "poiseuille"): mesh dict and data."""
+    d = golden("chocg_" + name)
+    bface = {int(k[5:]): d[k] for k in d.files if k.startswith("bface")}
+    return {"coord": d["coord"], "inpoel": d["inpoel"], "bface": bface}, d
+
+
+def nodes_of(bface, sets):
+    out = [np.unique(bface[s]) for s in sets if s in bface]
+    return np.unique(np.concatenate(out)) if out else np.zeros(0, np.int64)
+
+
+def chocg_regression_setup(name, m):
+    """Boundary conditions and settings of the reference's ChoCG regressions
+    (tests/regression/inciter/ChoCG/Lid/ldc.q and Poiseuille/poiseuille_damp2.q)
+    as per-node lists in the mesh file's numbering: velocity Dirichlet
+    (nodes, mask, values), noslip nodes, pressure Dirichlet (nodes, values of
+    the initial solves), and the solver settings."""
+    bf = m["bface"]
+    if name == "lid":
+        dn = nodes_of(bf, [4])
+        dirbc = (dn, np.ones((dn.size, 3), np.int32), np.tile([1.0, 0.0, 0.0], (dn.size, 1)))
+        noslip = nodes_of(bf, [1, 2, 3, 5, 6])
+        pdir = (np.array([0]), np.array([0.0]))  # hydrostat = 0, userdef pressure IC 0
+        prm = dict(mu=0.01, cfl=0.9, flux="damp4", pc="jacobi", ptol=1e-3, pmaxit=500)
+        nstep = 10
+    else:
+        dn = nodes_of(bf, [1, 5])
+        mask = np.tile([0, 1, 1], (dn.size, 1)).astype(np.int32)
+        dirbc = (dn, mask, np.zeros((dn.size, 3)))  # mask 1: the IC value, 0
+        noslip = nodes_of(bf, [3, 4])
+        p1, p2 = nodes_of(bf, [1]), nodes_of(bf, [2])
+        pn = np.concatenate([p1, p2])
+        pv = np.concatenate([np.full(p1.size, 2.4), np.zeros(p2.size)])
+        order = np.argsort(pn, kind="stable")
+        pdir = (pn[order], pv[order])
+        prm = dict(mu=0.01, cfl=0.05, flux="damp2", pc="jacobi", ptol=1e-3, pmaxit=500)
+        nstep = 20
+    return dirbc, noslip, pdir, prm, nstep

@@ -14,7 +14,14 @@ Sources, all read as data (nothing is executed):
   * tests/regression/inciter/RieCG/Sod: the input mesh, the final nodal
     fields (sod.std.exo) and the per-step diagnostics (diag.std) of the RieCG
     Sod shock tube (10 steps, CFL 0.5, symmetry on side sets 2,4,5,6);
-  * tests/regression/inciter/KozCG/Sod: the same for KozCG.
+  * tests/regression/inciter/KozCG/Sod: the same for KozCG;
+  * tests/regression/inciter/ChoCG/Lid: the lid-driven cavity (damp4, CFL
+    0.9, Re 100, Jacobi PCG to 1e-3, hydrostat node 0, noslip on side sets
+    1,2,3,5,6, lid velocity (1,0,0) on side set 4, 10 steps): input mesh,
+    final nodal fields (ldc.std.exo) and per-step diagnostics (diag_ldc.std);
+  * tests/regression/inciter/ChoCG/Poiseuille: the damp2 Poiseuille flow
+    (CFL 0.05, mu 0.01, pressure 2.4 / 0 on side sets 1 / 2, noslip on 3,4,
+    v = w = 0 on 1 and 5, 20 steps): the same three files.
 """
 
 from __future__ import annotations
@@ -107,11 +114,40 @@ def sod_fixture(ref: str, scheme: str):
     return out
 
 
+def chocg_fixture(ref: str, case: str, meshfile: str, outfile: str, diagfile: str):
+    from xyst_gb300 import mesh as M
+    from scipy.io import netcdf_file
+
+    base = os.path.join(ref, "tests/regression/inciter/ChoCG", case)
+    m = M.read_exo(os.path.join(base, meshfile))
+    f = netcdf_file(os.path.join(base, outfile), "r", mmap=False)
+    names = ["".join(c.decode() for c in row if c) for row in f.variables["name_nod_var"][:]]
+    times = np.array(f.variables["time_whole"][:], dtype=np.float64)
+    fields = np.array([np.array(f.variables[f"vals_nod_var{i + 1}"][:][-1], dtype=np.float64)
+                       for i in range(len(names))])
+    ocoord = np.stack([np.asarray(f.variables[k][:], dtype=np.float64)
+                       for k in ("coordx", "coordy", "coordz")])
+    f.close()
+    out = {"coord": m["coord"], "inpoel": m["inpoel"], "final_time": times[-1],
+           "out_coord": ocoord, "out_fields": fields, "out_names": np.array(names),
+           "diag": _diag(os.path.join(base, diagfile))}
+    for s, tri in m["bface"].items():
+        out[f"bface{s}"] = tri
+    return out
+
+
 def main(ref: str):
     np.savez_compressed(os.path.join(HERE, "csr_mult.npz"), **csr_fixture(ref))
     np.savez_compressed(os.path.join(HERE, "cg_laplace.npz"), **cg_fixture(ref))
     np.savez_compressed(os.path.join(HERE, "riecg_sod.npz"), **sod_fixture(ref, "RieCG"))
     np.savez_compressed(os.path.join(HERE, "kozcg_sod.npz"), **sod_fixture(ref, "KozCG"))
+    np.savez_compressed(os.path.join(HERE, "chocg_lid.npz"),
+                        **chocg_fixture(ref, "Lid", "unitcube_1k.exo", "ldc.std.exo",
+                                        "diag_ldc.std"))
+    np.savez_compressed(os.path.join(HERE, "chocg_poiseuille.npz"),
+                        **chocg_fixture(ref, "Poiseuille", "poiseuille1tetz.exo",
+                                        "poiseuille_damp2.std.exo",
+                                        "diag_poiseuille_damp2.std"))
     print("wrote fixtures to", HERE)
 
 

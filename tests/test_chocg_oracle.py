@@ -1,0 +1,123 @@
+"""Pins of the ChoCG oracle restatement (CPU, no GPU):
+
+* chorin::div/grad/vgrad/flux/rhs of the restatement against the reference's
+  own compiled functions (oracle/_ref), bit for bit, for damp2 and damp4,
+  with and without viscosity and stabilisation;
+* the whole restated ChoCG driver (initial projection, time steps, pressure
+  PCG) against the reference's regression baselines committed in
+  tests/golden/: the lid-driven cavity (damp4, hydrostat, noslip, lid
+  Dirichlet) and the damp2 Poiseuille flow (pressure Dirichlet sets), final
+  fields within the reference's exodiff tolerances and every per-step
+  diagnostic row within its numdiff tolerances.
+"""
+
+import numpy as np
+import pytest
+
+import oracle
+import oracle.ref as ref
+from common import chocg_mesh, chocg_regression_setup
+from xyst_gb300 import mesh
+
+needs_ref = pytest.mark.skipif(not ref.available(), reason="reference sources not built here")
+
+
+def _cube5(n=6, jitter=0.2, seed=1):
+    m = mesh.cube(n, jitter=jitter, seed=seed)
+    coord, inpoel = m["coord"], m["inpoel"]
+    v = oracle.vol(coord, inpoel)
+    e, d = oracle.domint(coord, inpoel, ncoef=5)
+    tri = np.concatenate([m["bface"][s] for s in sorted(m["bface"])])
+    ia, ja, a = oracle.pressure_matrix(coord, inpoel)
+    return m, coord, inpoel, v, e, d, tri, ia, ja, a
+
+
+@needs_ref
+@pytest.mark.parametrize("flux,mu,stab", [("damp2", 0.0, True), ("damp2", 0.01, True),
+                                          ("damp4", 0.01, True), ("damp4", 0.0, False)])
+def test_chorin_bitexact(flux, mu, stab):
+    m, coord, inpoel, v, e, d, tri, ia, ja, a = _cube5()
+    n = coord.shape[1]
+    rng = np.random.default_rng(7)
+    U = rng.standard_normal((n, 3))
+    P = rng.standard_normal(n)
+    PG = rng.standard_normal((n, 3))
+    G = rng.standard_normal((n, 9))
+    ref.set_config(flux=flux)
+    ref.set_chorin(mu, stab)
+    o = oracle.ChoCG(coord, v, e, d, tri, ia, ja, a, mu=mu, flux=flux, stab=stab)
+    for s in (True, False):
+        assert np.array_equal(o.div(U, P, PG, 1.7e-2, s),
+                              ref.chorin_div(coord, e, d, tri, 1.7e-2, P, PG, U, s))
+    assert np.array_equal(o.vgrad(U, 3), ref.chorin_vgrad(coord, e, d, tri, U))
+    assert np.array_equal(o.vgrad(P[:, None], 1), ref.chorin_grad(coord, e, d, tri, P))
+    assert np.array_equal(o.flux(U, G), ref.chorin_flux(coord, e, d, tri, U, G))
+    assert np.array_equal(o.rhs(U, G, P), ref.chorin_rhs(coord, e, d, tri, v, P, U, G))
+
+
+def chocg_oracle(name):
+    m, d = chocg_mesh(name)
+    coord, inpoel = m["coord"], m["inpoel"]
+    v = oracle.vol(coord, inpoel)
+    e, de = oracle.domint(coord, inpoel, ncoef=5)
+    tri = np.concatenate([m["bface"][s] for s in sorted(m["bface"])])  # all side sets
+    ia, ja, a = oracle.pressure_matrix(coord, inpoel)
+    dirbc, noslip, pdir, prm, nstep = chocg_regression_setup(name, m)
+    o = oracle.ChoCG(coord, v, e, de, tri, ia, ja, a, **prm)
+    o.set_bc(dir=dirbc, noslip=noslip, pdir=pdir)
+    o.set_state(np.zeros((coord.shape[1], 3)), np.zeros(coord.shape[1]))
+    return o, m, d, v, nstep
+
+
+def _by_coord(coord, out_coord):
+    from scipy.spatial import cKDTree
+    dist, idx = cKDTree(coord.T).query(out_coord.T)
+    assert dist.max() < 1e-12
+    return idx
+
+
+def chocg_diag_row(o, v, t, dt):
+    """One row of the reference's ChoCG diag file (NodeDiagnostics::precompute,
+    src/Inciter/NodeDiagnostics.cpp:148-246, finished by
+    Transporter::prediagnostics, src/Inciter/Transporter.cpp:1533-1575):
+    t, dt, L2(p), L2(u,v,w), L2(dp), L2(u-un) over the mesh volume."""
+    Vt = v.sum()
+    u, un, p, dp = o.get(0), o.get(1), o.get(2), o.get(6)
+    l2 = [np.sqrt((p * p * v).sum() / Vt)] + list(np.sqrt((u * u * v[:, None]).sum(0) / Vt))
+    l2r = [np.sqrt((dp * dp * v).sum() / Vt)] + list(
+        np.sqrt(((u - un) ** 2 * v[:, None]).sum(0) / Vt))
+    return np.array([t, dt] + l2 + l2r)
+
+
+# exodiff.cfg of both regressions: velocity x/y/z relative 3e-7 / 2e-6 / 3e-7
+# (Lid; Poiseuille uses its own file), others relative 1e-7 floor 1e-8
+FIELD_TOL = {"lid": {"velocityx": 3e-7, "velocityy": 2e-6, "velocityz": 3e-7,
+                     "pressure": 1e-7, "divergence": 1e-7}}
+
+
+@pytest.mark.parametrize("name", ["lid", "poiseuille"])
+def test_chocg_regression_golden(name):
+    o, m, d, v, nstep = chocg_oracle(name)
+    o.init()
+    diag = d["diag"]
+    t = 0.0
+    for k in range(nstep):
+        dt, it = o.step()
+        t += dt
+        row = chocg_diag_row(o, v, t, dt)
+        exp = diag[k, 1:11]
+        # diag.ndiff.cfg: t, dt and every L2 norm abs 1e-7 or rel 1e-7
+        assert np.all(np.abs(row - exp) <= np.maximum(1e-7, 1e-7 * np.abs(exp))), (k, row, exp)
+    assert abs(t - float(d["final_time"])) < 1e-8
+    names = [str(x) for x in d["out_names"]]
+    idx = _by_coord(m["coord"], d["out_coord"])
+    u, p = o.get(0)[idx], o.get(2)[idx]
+    got = {"velocityx": u[:, 0], "velocityy": u[:, 1], "velocityz": u[:, 2], "pressure": p}
+    tol = FIELD_TOL.get(name, {})
+    for fname, val in got.items():
+        exp = d["out_fields"][names.index(fname)]
+        rel = tol.get(fname, 1e-7)
+        big = np.abs(exp) > 1e-8
+        err = np.abs(val - exp)
+        assert np.all(err[big] <= rel * np.abs(exp[big]) + 1e-12), (fname, err.max())
+        assert np.all(err[~big] <= 1e-8), fname
