@@ -5,6 +5,8 @@
  *   - RieCG: superedge nodal gradients, MUSCL/Rusanov|HLLC edge and boundary
  *     residual, low-storage 3-stage RK update, nodal BCs, CFL time step;
  *   - KozCG: element Taylor-Galerkin residual with flux-corrected transport;
+ *   - ChoCG: projection step of incompressible flow (chorin:: edge passes,
+ *     explicit RK momentum prediction, pressure-increment Poisson solve);
  *   - ConjugateGradients: CSR matrix-vector product and preconditioned CG.
  *
  * Every entry point returns an int status (XG_OK on success) and never throws;
@@ -194,6 +196,106 @@ int xg_kozcg_dt(xg_ctx* ctx, double* dt);
 /* Advance nstep KozCG steps on the device (dt, rhs, FCT aec/alw/lim/solve,
  * BCs; src/Inciter/KozCG.cpp:613-1197); dts and ms as in xg_riecg_run. */
 int xg_kozcg_run(xg_ctx* ctx, int64_t nstep, double* dts, float* ms);
+
+/* ---- ChoCG ---------------------------------------------------------------- */
+
+enum xg_chorin_flux { XG_DAMP2 = 0, XG_DAMP4 = 1 };
+
+/* ChoCG settings the reference reads from its global config
+ * (mat_dyn_viscosity, cfl, dt, flux, stab, stab2, stab2coef, rk and the
+ * pressure{iter, tol, pc} block), plus the pressure-solve variants of this
+ * library: ppc 2 is the factored preconditioner of xg_cg_set_factor, pmixed
+ * the mixed-precision solve of xg_cg_solve_mixed. */
+typedef struct xg_chocg_params {
+  double mu;          /* dynamic viscosity */
+  double cfl;         /* CFL number (used when const_dt == 0) */
+  double const_dt;    /* constant time step if |const_dt| > eps */
+  int flux;           /* enum xg_chorin_flux (the reference needs damp2 or damp4) */
+  int stab;           /* nonzero: advective stabilisation |vnL + vnR|/2 */
+  int stab2;          /* nonzero: artificial viscosity stab2coef*max(|vnL|,|vnR|) */
+  double stab2coef;
+  int rk;             /* explicit Runge-Kutta stages, 1..4 */
+  int ppc;            /* pressure preconditioner: 0 none, 1 jacobi, 2 factor */
+  double ptol;        /* pressure solve: relative residual tolerance */
+  int64_t pmaxit;     /* pressure solve: iteration limit */
+  int pmixed;         /* nonzero: mixed-precision refinement (xg_cg_solve_mixed) */
+  double pinner_tol;  /* its inner residual reduction per replacement */
+} xg_chocg_params;
+
+/* Upload the operators ChoCG builds once per mesh (ChoCG::feop/streamable/
+ * domsuped, src/Inciter/ChoCG.cpp:277-813): coordinates, nodal volumes, the
+ * three superedge groups as ChoCG::m_dsupedge/m_dsupint with five integrals
+ * per edge (tets: 4 ids + 6x5; triangles: 3 ids + 3x5; edges: 2 ids + 5) and
+ * the boundary triangles m_triinpoel.  The pressure matrix of ChoCG::prelhs
+ * goes to xg_cg_setup on the same context (as the reference inserts it into
+ * its ConjugateGradients array); xg_chocg_init and xg_chocg_run solve on it. */
+int xg_chocg_setup(xg_ctx* ctx, const xg_chocg_params* prm, int64_t npoin, const double* coord,
+                   const double* vol, int64_t ntet, const uint64_t* dsupedge0,
+                   const double* dsupint0, int64_t ntri, const uint64_t* dsupedge1,
+                   const double* dsupint1, int64_t nedge, const uint64_t* dsupedge2,
+                   const double* dsupint2, int64_t nbtri, const uint64_t* triinpoel);
+
+/* Boundary conditions as ChoCG::setupDirBC/streamable store them and
+ * ChoCG::BC applies them (src/Inciter/ChoCG.cpp:207-275, 1333-1354):
+ *   velocity Dirichlet: nodes, 3 mask ints per node (nonzero: set) and 3
+ *     values per node (time independent);
+ *   symmetry: m_symbcnodes / m_symbcnorms (a node may repeat);
+ *   noslip: m_noslipbcnodes;
+ *   pressure Dirichlet (pressure.bc_dir and the hydrostat node): nodes and
+ *     the values of the initial solves; the time-increment solves use 0
+ *     (ChoCG::pinit, src/Inciter/ChoCG.cpp:1025-1125). */
+int xg_chocg_set_bc(xg_ctx* ctx, int64_t ndir, const uint64_t* dirnodes, const int32_t* dirmask,
+                    const double* dirvals, int64_t nsym, const uint64_t* symnodes,
+                    const double* symnorms, int64_t nnoslip, const uint64_t* noslipnodes,
+                    int64_t npdir, const uint64_t* pdirnodes, const double* pdirvals);
+
+/* Device state: velocity u (npoin x 3, node-major), pressure p (npoin; null
+ * keeps zero on set), time t. */
+int xg_chocg_set_state(xg_ctx* ctx, const double* u, const double* p, double t);
+int xg_chocg_get_state(xg_ctx* ctx, double* u, double* p, double* t);
+
+/* ChoCG's start-up sequence on the device state (ChoCG::merge -> div ->
+ * pinit -> psolve -> sgrad -> psolved, twice, then pgrad;
+ * src/Inciter/ChoCG.cpp:739-764, 868-1281): BCs, projection of the initial
+ * velocity onto divergence-free fields, the initial pressure from the
+ * momentum-flux divergence and its gradient.  *it receives the iterations of
+ * the last pressure solve (negated when that solve stopped short of its
+ * tolerance; the reference carries on in that case, and so does this). */
+int xg_chocg_init(xg_ctx* ctx, int64_t* it);
+
+/* Advance nstep time steps (ChoCG::dt/advance/rhs/solve/pred/corr/div/pinit/
+ * psolve/sgrad/psolved/pgrad, src/Inciter/ChoCG.cpp:1356-1695, 868-1281) on
+ * the device: explicit RK momentum prediction, pressure-increment Poisson
+ * solve, projection.  dts and its (optional, host, nstep) receive each step's
+ * dt and pressure-solve iterations (negated for a solve that stopped short
+ * of its tolerance at the iteration limit or the (p,q) breakdown guard, after
+ * which the step completes as in the reference), ms (optional) the device
+ * time.  Returns XG_ERR_BLOWUP if dt fell below eps. */
+int xg_chocg_run(xg_ctx* ctx, int64_t nstep, double* dts, int64_t* its, float* ms);
+
+/* Diagnostics fields of the device state (NodeDiagnostics::precompute,
+ * src/Inciter/NodeDiagnostics.cpp:148-246): what 0 = u at the start of the
+ * last step (npoin x 3), 1 = pressure gradient (npoin x 3), 2 = velocity
+ * gradient (npoin x 9), 3 = last Poisson right-hand side (npoin), 4 = last
+ * pressure increment (npoin). */
+int xg_chocg_fields(xg_ctx* ctx, int what, double* out);
+
+/* Drop-ins for the chorin:: passes (src/Physics/Chorin.hpp:19-70) on host
+ * arrays with the operators of xg_chocg_setup; outputs are the raw weak
+ * sums (not divided by the nodal volume), like the reference functions:
+ *   div: D (npoin) of U (npoin x 3) with pressure P and its gradient G
+ *        (npoin x 3), stabilised when stab (Chorin.cpp:85-209);
+ *   grad: G (npoin x 3) of the scalar S (Chorin.cpp:336-449);
+ *   vgrad: G (npoin x 9) of U (npoin x 3) (Chorin.cpp:211-334);
+ *   flux: F (npoin x 3) of U with velocity gradients G (npoin x 9)
+ *         (Chorin.cpp:509-638);
+ *   rhs: R (npoin x 3) of P, U and G (npoin x 9) (Chorin.cpp:1010-1044). */
+int xg_chorin_div(xg_ctx* ctx, const double* U, const double* P, const double* G, double dt,
+                  int stab, double* D);
+int xg_chorin_grad(xg_ctx* ctx, const double* S, double* G);
+int xg_chorin_vgrad(xg_ctx* ctx, const double* U, double* G);
+int xg_chorin_flux(xg_ctx* ctx, const double* U, const double* G, double* F);
+int xg_chorin_rhs(xg_ctx* ctx, const double* P, const double* U, const double* G, double* R);
 
 /* ---- ConjugateGradients ---------------------------------------------------- */
 

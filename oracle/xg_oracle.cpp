@@ -1054,6 +1054,7 @@ void cho_psolve(ChoCG& s, const real* b, const std::vector<real>& dval) {
   int conv = 0;
   s.last_it = orc_pcg(s.n, s.A.ia.data(), s.A.ja.data(), a.data(), bb.data(), s.sol.data(),
                       s.pmaxit, s.ptol, s.pc, &s.last_normr, &s.last_normb, &conv);
+  if (!conv) s.last_it = -s.last_it;  // reported, not an error (ConjugateGradients.cpp:792-806)
 }
 
 // The initial projection of ChoCG::merge -> div -> pinit -> psolve -> sgrad ->

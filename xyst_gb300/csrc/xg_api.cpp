@@ -34,6 +34,7 @@ int xg_destroy(xg_ctx* c) {
   xg::destroy_riecg(c->riecg);
   xg::destroy_cg(c->cg);
   xg::destroy_kozcg(c->kozcg);
+  xg::destroy_chocg(c->chocg);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return XG_OK;
@@ -44,7 +45,7 @@ const char* xg_last_error(const xg_ctx* c) { return c ? c->err.c_str() : "null c
 int xg_device_bytes(const xg_ctx* c, int64_t* bytes) {
   if (!c || !bytes) return XG_ERR_ARG;
   *bytes = static_cast<int64_t>(xg::bytes_riecg(c->riecg) + xg::bytes_cg(c->cg) +
-                                xg::bytes_kozcg(c->kozcg));
+                                xg::bytes_kozcg(c->kozcg) + xg::bytes_chocg(c->chocg));
   return XG_OK;
 }
 

@@ -846,6 +846,67 @@ int cg_graph(xg_ctx* c, LpcGraph* g) {
   return XG_OK;
 }
 
+int cg_set_dirichlet(xg_ctx* c, const uint8_t* mask, const double* val) {
+  CGDev* d = c->cg;
+  if (!d) return fail(c, XG_ERR_STATE, "pressure Dirichlet data before cg_setup");
+  const int64_t n = d->n;
+  uint64_t key = 1469598103934665603ull;  // FNV-1a over the mask, as xg_cg_init
+  for (int64_t i = 0; i < n; ++i) key = (key ^ mask[i]) * 1099511628211ull;
+  XG_CUDA(c, cudaMemcpyAsync(d->bcmask, mask, n, cudaMemcpyHostToDevice, c->stream));
+  XG_CUDA(c, cudaMemcpyAsync(d->bcval, val, n * 8, cudaMemcpyHostToDevice, c->stream));
+  XG_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (key != d->bc_key || !d->ready) {
+    d->geom_set = false;
+    d->factor_set = false;
+  }
+  d->bc_key = key;
+  return XG_OK;
+}
+
+int cg_zero_solution(xg_ctx* c) {
+  CGDev* d = c->cg;
+  if (!d) return fail(c, XG_ERR_STATE, "cg_zero_solution before cg_setup");
+  XG_CUDA(c, cudaMemsetAsync(d->x, 0, d->n * 8, c->stream));
+  return XG_OK;
+}
+
+int cg_init_device(xg_ctx* c, const double* b_dev, int zero_values, int pc) {
+  CGDev* d = c->cg;
+  if (!d) return fail(c, XG_ERR_STATE, "cg_init_device before cg_setup");
+  if (pc != 0 && pc != 1 && pc != 2) return fail(c, XG_ERR_ARG, "unknown preconditioner");
+  cudaStream_t s = c->stream;
+  const int64_t n = d->n;
+  XG_CUDA(c, cudaMemcpyAsync(d->b, b_dev, n * 8, cudaMemcpyDeviceToDevice, s));
+  const double* val = d->bcval;
+  if (zero_values) {  // r is free until k_setup writes it
+    XG_CUDA(c, cudaMemsetAsync(d->r, 0, n * 8, s));
+    val = d->r;
+  }
+  d->pc = pc;
+  d->apply = true;
+  k_apply_bc<<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, d->soff, d->swidth, d->col, d->a0, d->a,
+                                                       d->a32, d->bcmask, val, nullptr, d->b);
+  XG_CHECK_LAUNCH(c);
+  CGScalars h{};
+  h.pc = pc;
+  XG_CUDA(c, cudaMemcpyAsync(d->scal, &h, sizeof(h), cudaMemcpyHostToDevice, s));
+  k_setup<<<pgrid<k_setup>(n), kBlock, 0, s>>>(n, d->soff, d->swidth, d->col, d->a, d->diagpos,
+                                               d->x, d->b, d->r, d->d, d->z, d->p[0], d->d32,
+                                               d->partial, d->scal);
+  XG_CHECK_LAUNCH(c);
+  d->ready = true;
+  if (pc == 2) {
+    int rf = d->factor_set ? XG_OK : build_factor(c, d);
+    if (rf) return rf;
+    rf = factor_apply64(c, d, d->r, d->z);
+    if (rf) return rf;
+  }
+  return XG_OK;
+}
+
+const double* cg_solution_device(xg_ctx* c) { return c->cg ? c->cg->x : nullptr; }
+int64_t cg_rows(xg_ctx* c) { return c->cg ? c->cg->n : 0; }
+
 }  // namespace xg
 
 using namespace xg;

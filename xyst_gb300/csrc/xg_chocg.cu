@@ -1,0 +1,1241 @@
+// ChoCG on one GB300: the chorin:: edge passes as node-gather kernels, the
+// explicit RK momentum prediction, nodal BCs, CFL reduction and the
+// pressure-increment projection around the context's CG solver.
+//
+// Reference path (all paths relative to the reference project root):
+//   chorin::div/vgrad/grad/flux/rhs  src/Physics/Chorin.cpp:34-1044
+//   ChoCG::merge/div/pinit/psolve/sgrad/psolved/pgrad
+//                                    src/Inciter/ChoCG.cpp:739-764, 868-1281
+//   ChoCG::BC/dt/advance/rhs/solve/pred/corr
+//                                    src/Inciter/ChoCG.cpp:1333-1695
+//   physics::dirbc/symbc/noslipbc    src/Physics/BC.cpp:27-145
+//
+// Layout in HBM (n nodes), FP64 throughout (the projection scheme is the
+// configuration the reference runs in double precision):
+//   u, u2, un     [3][n]  velocity (ping-pong) and the stage-0 copy
+//   pr, div       [n]     pressure and the Poisson right-hand side
+//   pgrad         [3][n]  pressure gradient
+//   vgrad         [9][n]  velocity gradient (damp4 and the start-up flux)
+//   flx           [3][n]  momentum flux (start-up only)
+//   adjacency     SELL-32 over both ends of every edge, entry (k, lane) of
+//                 slice s at off[s] + 32k + lane: the neighbour (~id when the
+//                 node is the canonical second end) and (d0, d1, d2, d4), the
+//                 dual-face normal and the viscous coefficient of the edge.
+// Every edge term is evaluated in the edge's canonical orientation at both
+// ends, so the two ends see bit-identical values and each node owns its
+// writes (no atomics except the scalar CFL minimum).  A node's neighbours are
+// visited in increasing id, which for an unrenumbered mesh is the order in
+// which the reference's edge loop reaches the node.
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+
+#include "xg_internal.hpp"
+
+namespace xg {
+
+namespace {
+constexpr int kSlice = 32;
+constexpr int32_t kPad = INT32_MIN;
+constexpr int kBlock = 256;
+}  // namespace
+
+// The four edge coefficients of an adjacency entry: d0, d1, d2 (dual-face
+// normal) and d4 (viscous coefficient).
+struct alignas(32) Coef4 {
+  double x, y, z, w;
+};
+
+struct ChoCGDev {
+  Arena arena;    // mesh-sized arrays
+  Arena bcarena;  // boundary condition program
+  int64_t n = 0, nslice = 0, nent = 0, nbn = 0;
+  xg_chocg_params prm{};
+  int32_t *soff = nullptr, *swidth = nullptr, *nbr = nullptr;
+  Coef4* dd = nullptr;
+  int32_t *bidx = nullptr, *bptr = nullptr, *bent = nullptr, *btri = nullptr;
+  double *xyz = nullptr, *vol = nullptr;
+  double *u = nullptr, *u2 = nullptr, *un = nullptr, *pr = nullptr, *pgrad = nullptr,
+         *vgrad = nullptr, *div = nullptr, *flx = nullptr, *stage = nullptr;
+  unsigned long long* dtmin = nullptr;
+  // BC program, one thread per BC node
+  int64_t nbc = 0, nsymbc = 0;
+  int32_t *bcnode = nullptr, *bcdir = nullptr, *bcsymp = nullptr, *bcnoslip = nullptr,
+          *dirmask = nullptr;
+  double *dirval = nullptr, *symn = nullptr;
+  bool pdir_set = false;
+  double t = 0.0;
+  bool ready = false;  // start-up done
+  int64_t last_it = 0;
+};
+
+void destroy_chocg(ChoCGDev* d) { delete d; }
+size_t bytes_chocg(const ChoCGDev* d) { return d ? d->arena.bytes() + d->bcarena.bytes() : 0; }
+
+namespace {
+
+struct ChoAdj {
+  const int32_t* soff;
+  const int32_t* swidth;
+  const int32_t* nbr;
+  const Coef4* dd;
+};
+struct ChoBnd {
+  const int32_t* bidx;
+  const int32_t* bptr;
+  const int32_t* bent;  // (triangle << 2) | position of the node in it
+  const int32_t* btri;
+  const double* xyz;    // SoA coordinates
+};
+
+__device__ __forceinline__ Coef4 ldd4(const Coef4* p) {
+  const double2* q = reinterpret_cast<const double2*>(p);
+  const double2 a = __ldg(q), b = __ldg(q + 1);
+  return Coef4{a.x, a.y, b.x, b.y};
+}
+
+// Boundary-face normal / 6 of triangle t (tk::crossdiv(..., 6.0),
+// src/Base/Vector.hpp:68-77), the same expression at every vertex.
+__device__ __forceinline__ void tri_normal6(const ChoBnd& b, int64_t n, int32_t t, int32_t N[3],
+                                            double nn[3]) {
+  N[0] = __ldg(b.btri + 3 * t);
+  N[1] = __ldg(b.btri + 3 * t + 1);
+  N[2] = __ldg(b.btri + 3 * t + 2);
+  const double* x = b.xyz;
+  const double* y = b.xyz + n;
+  const double* z = b.xyz + 2 * n;
+  const double bax = x[N[1]] - x[N[0]], bay = y[N[1]] - y[N[0]], baz = z[N[1]] - z[N[0]];
+  const double cax = x[N[2]] - x[N[0]], cay = y[N[2]] - y[N[0]], caz = z[N[2]] - z[N[0]];
+  nn[0] = (bay * caz - cay * baz) / 6.0;
+  nn[1] = (baz * cax - caz * bax) / 6.0;
+  nn[2] = (bax * cay - cax * bay) / 6.0;
+}
+
+// (6 f_pos + f_other + f_other)/8 of a triangle's three vertex values, for
+// the vertex at pos (Chorin.cpp:183-205 and the same weights elsewhere).
+__device__ __forceinline__ double wavg(int pos, double a, double b, double c) {
+  return pos == 0 ? (6.0 * a + b + c) / 8.0
+                  : (pos == 1 ? (a + 6.0 * b + c) / 8.0 : (a + b + 6.0 * c) / 8.0);
+}
+
+__device__ __forceinline__ void block_min(double v, unsigned long long* dst) {
+  __shared__ double red[32];
+  unsigned long long bits = __double_as_longlong(v);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long other = __shfl_xor_sync(0xffffffffu, bits, o);
+    bits = other < bits ? other : bits;
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) red[wid] = __longlong_as_double(bits);
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    unsigned long long b = __double_as_longlong(lane < nw ? red[lane] : DBL_MAX);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      unsigned long long other = __shfl_xor_sync(0xffffffffu, b, o);
+      b = other < b ? other : b;
+    }
+    if (lane == 0) atomicMin(dst, b);
+  }
+}
+
+// What the gradient kernel does with a node's gradient g of NC components.
+enum GradOut { GRAD_RAW = 0, GRAD_DIVIDE = 1, GRAD_PROJECT = 2 };
+
+// chorin::vgrad / chorin::grad (Chorin.cpp:211-449): G = sum over edges of
+// -/+ d (u_p + u_q) plus the boundary-triangle term.  GRAD_RAW stores it,
+// GRAD_DIVIDE stores G/vol (ChoCG::fingrad, src/Inciter/ChoCG.cpp:841-866),
+// GRAD_PROJECT (NC = 1, the pressure increment) applies the projection of
+// ChoCG::psolved (src/Inciter/ChoCG.cpp:1204-1216): u -= dt G/vol, and with
+// addp the pressure update pr += increment (src/Inciter/ChoCG.cpp:1246-1250).
+template <int NC, int MODE>
+__global__ void __launch_bounds__(kBlock) k_cgrad(int64_t n, ChoAdj adj, const double* U,
+                                                   ChoBnd bnd, const double* __restrict__ vol,
+                                                   double* __restrict__ G, double dt, int addp,
+                                                   double* u, double* pr) {
+  const int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (p >= n) return;
+  const int lane = static_cast<int>(p & (kSlice - 1));
+  const int64_t s = p >> 5;
+  const int32_t off = __ldg(adj.soff + s), w = __ldg(adj.swidth + s);
+  double up[NC];
+#pragma unroll
+  for (int i = 0; i < NC; ++i) up[i] = U[i * n + p];
+  double g[3 * NC];
+#pragma unroll
+  for (int i = 0; i < 3 * NC; ++i) g[i] = 0.0;
+  for (int k = 0; k < w; ++k) {
+    const int32_t e = off + k * kSlice + lane;
+    int32_t q = __ldg(adj.nbr + e);
+    if (q == kPad) continue;
+    const bool first = q >= 0;
+    if (!first) q = ~q;
+    const Coef4 d = ldd4(adj.dd + e);
+#pragma unroll
+    for (int i = 0; i < NC; ++i) {
+      const double sum = U[i * n + q] + up[i];
+      const double f0 = d.x * sum, f1 = d.y * sum, f2 = d.z * sum;
+      if (first) {
+        g[i * 3 + 0] -= f0;
+        g[i * 3 + 1] -= f1;
+        g[i * 3 + 2] -= f2;
+      } else {
+        g[i * 3 + 0] += f0;
+        g[i * 3 + 1] += f1;
+        g[i * 3 + 2] += f2;
+      }
+    }
+  }
+  const int32_t bi = __ldg(bnd.bidx + p);
+  if (bi >= 0) {
+    for (int32_t j = __ldg(bnd.bptr + bi); j < __ldg(bnd.bptr + bi + 1); ++j) {
+      const int32_t ent = __ldg(bnd.bent + j);
+      const int pos = ent & 3;
+      int32_t N[3];
+      double nn[3];
+      tri_normal6(bnd, n, ent >> 2, N, nn);
+#pragma unroll
+      for (int i = 0; i < NC; ++i) {
+        const double f = wavg(pos, U[i * n + N[0]], U[i * n + N[1]], U[i * n + N[2]]);
+#pragma unroll
+        for (int jj = 0; jj < 3; ++jj) g[i * 3 + jj] += f * nn[jj];
+      }
+    }
+  }
+  if (MODE == GRAD_RAW) {
+#pragma unroll
+    for (int i = 0; i < 3 * NC; ++i) G[i * n + p] = g[i];
+  } else if (MODE == GRAD_DIVIDE) {
+    const double v = vol[p];
+#pragma unroll
+    for (int i = 0; i < 3 * NC; ++i) G[i * n + p] = g[i] / v;
+  } else {
+    const double v = vol[p];
+#pragma unroll
+    for (int jj = 0; jj < 3; ++jj) u[jj * n + p] -= dt * (g[jj] / v);
+    if (addp) pr[p] += up[0];
+  }
+}
+
+// chorin::div (Chorin.cpp:34-209): divergence of the 3-component U with the
+// 4th-order pressure damping when stab, optionally divided by dt
+// (ChoCG::pinit, src/Inciter/ChoCG.cpp:1039).
+__global__ void __launch_bounds__(kBlock) k_cdiv(int64_t n, ChoAdj adj, const double* U,
+                                                  const double* __restrict__ P,
+                                                  const double* __restrict__ PG, ChoBnd bnd,
+                                                  double dt, int stab, int bydt,
+                                                  double* __restrict__ D) {
+  const int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (p >= n) return;
+  const int lane = static_cast<int>(p & (kSlice - 1));
+  const int64_t s = p >> 5;
+  const int32_t off = __ldg(adj.soff + s), w = __ldg(adj.swidth + s);
+  const double* x = bnd.xyz;
+  const double* y = bnd.xyz + n;
+  const double* z = bnd.xyz + 2 * n;
+  double acc = 0.0;
+  for (int k = 0; k < w; ++k) {
+    const int32_t e = off + k * kSlice + lane;
+    int32_t q = __ldg(adj.nbr + e);
+    if (q == kPad) continue;
+    const bool first = q >= 0;
+    if (!first) q = ~q;
+    const Coef4 d = ldd4(adj.dd + e);
+    const int64_t a = first ? p : q, b = first ? q : p;  // canonical ends
+    double f = d.x * (U[a] + U[b]) + d.y * (U[n + a] + U[n + b]) +
+               d.z * (U[2 * n + a] + U[2 * n + b]);
+    if (stab) {
+      const double dx = x[a] - x[b], dy = y[a] - y[b], dz = z[a] - z[b];
+      const double dl = sqrt(dx * dx + dy * dy + dz * dz);
+      const double p2 = P[b] - P[a];
+      const double Dn = sqrt(d.x * d.x + d.y * d.y + d.z * d.z);
+      const double dpx = PG[a] + PG[b], dpy = PG[n + a] + PG[n + b],
+                   dpz = PG[2 * n + a] + PG[2 * n + b];
+      const double p4 = 0.5 * (dx * dpx + dy * dpy + dz * dpz);
+      f += Dn * dt / dl * (p2 + p4);
+    }
+    acc = first ? acc - f : acc + f;
+  }
+  const int32_t bi = __ldg(bnd.bidx + p);
+  if (bi >= 0) {
+    for (int32_t j = __ldg(bnd.bptr + bi); j < __ldg(bnd.bptr + bi + 1); ++j) {
+      const int32_t ent = __ldg(bnd.bent + j);
+      const int pos = ent & 3;
+      int32_t N[3];
+      double nn[3];
+      tri_normal6(bnd, n, ent >> 2, N, nn);
+      const double ux = wavg(pos, U[N[0]], U[N[1]], U[N[2]]);
+      const double uy = wavg(pos, U[n + N[0]], U[n + N[1]], U[n + N[2]]);
+      const double uz = wavg(pos, U[2 * n + N[0]], U[2 * n + N[1]], U[2 * n + N[2]]);
+      acc += ux * nn[0] + uy * nn[1] + uz * nn[2];
+    }
+  }
+  D[p] = bydt ? acc / dt : acc;
+}
+
+// Momentum flux of tensor component (i,j) over an edge and in a point
+// (Chorin.cpp:451-507).  The edge form is called with the canonical second
+// end first, as the reference's loops do.
+__device__ __forceinline__ double mflux_e(const double* U, const double* G, int64_t n, int i,
+                                          int j, int64_t p, int64_t q, double mu) {
+  const double inv = U[i * n + p] * U[j * n + p] + U[i * n + q] * U[j * n + q];
+  if (mu < DBL_EPSILON) return -inv;
+  double vis = G[(i * 3 + j) * n + p] + G[(j * 3 + i) * n + p] + G[(i * 3 + j) * n + q] +
+               G[(j * 3 + i) * n + q];
+  if (i == j)
+    vis -= 2.0 / 3.0 * (G[0 * n + p] + G[4 * n + p] + G[8 * n + p] + G[0 * n + q] +
+                        G[4 * n + q] + G[8 * n + q]);
+  return mu * vis - inv;
+}
+__device__ __forceinline__ double mflux_p(const double* U, const double* G, int64_t n, int i,
+                                          int j, int64_t p, double mu) {
+  const double inv = U[i * n + p] * U[j * n + p];
+  if (mu < DBL_EPSILON) return -inv;
+  double vis = G[(i * 3 + j) * n + p] + G[(j * 3 + i) * n + p];
+  if (i == j) vis -= 2.0 / 3.0 * (G[0 * n + p] + G[4 * n + p] + G[8 * n + p]);
+  return mu * vis - inv;
+}
+
+// chorin::flux (Chorin.cpp:509-638): F_i = d[s_ij - u_i u_j]/dx_j, raw or
+// divided by the volume (ChoCG::div at start-up, src/Inciter/ChoCG.cpp:877).
+__global__ void __launch_bounds__(kBlock) k_cflux(int64_t n, ChoAdj adj, const double* U,
+                                                   const double* G, ChoBnd bnd,
+                                                   const double* __restrict__ vol, double mu,
+                                                   int divide, double* __restrict__ F) {
+  const int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (p >= n) return;
+  const int lane = static_cast<int>(p & (kSlice - 1));
+  const int64_t s = p >> 5;
+  const int32_t off = __ldg(adj.soff + s), w = __ldg(adj.swidth + s);
+  double acc[3] = {0.0, 0.0, 0.0};
+  for (int k = 0; k < w; ++k) {
+    const int32_t e = off + k * kSlice + lane;
+    int32_t q = __ldg(adj.nbr + e);
+    if (q == kPad) continue;
+    const bool first = q >= 0;
+    if (!first) q = ~q;
+    const Coef4 d = ldd4(adj.dd + e);
+    const int64_t a = first ? p : q, b = first ? q : p;
+    const double dj[3] = {d.x, d.y, d.z};
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const double f = dj[j] * mflux_e(U, G, n, i, j, b, a, mu);
+        acc[i] = first ? acc[i] - f : acc[i] + f;
+      }
+  }
+  const int32_t bi = __ldg(bnd.bidx + p);
+  if (bi >= 0) {
+    for (int32_t jb = __ldg(bnd.bptr + bi); jb < __ldg(bnd.bptr + bi + 1); ++jb) {
+      const int32_t ent = __ldg(bnd.bent + jb);
+      const int pos = ent & 3;
+      int32_t N[3];
+      double nn[3];
+      tri_normal6(bnd, n, ent >> 2, N, nn);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        double fv[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+          fv[j] = wavg(pos, mflux_p(U, G, n, i, j, N[0], mu), mflux_p(U, G, n, i, j, N[1], mu),
+                       mflux_p(U, G, n, i, j, N[2], mu));
+        acc[i] += fv[0] * nn[0] + fv[1] * nn[1] + fv[2] * nn[2];
+      }
+    }
+  }
+  const double v = divide ? vol[p] : 1.0;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) F[i * n + p] = divide ? acc[i] / v : acc[i];
+}
+
+struct AdvPrm {
+  double mu, stab2coef;
+  int stab, stab2;
+};
+
+// adv_damp2 / adv_damp4 edge flux of the three velocity components on the
+// canonical edge a -> b (Chorin.cpp:640-829).
+template <bool DAMP4>
+__device__ __forceinline__ void adv_edge(const double* U, const double* G, const double* P,
+                                         const double* xyz, int64_t n, Coef4 d, int64_t a,
+                                         int64_t b, const AdvPrm& ap, double f[3]) {
+  double uL[3] = {U[a], U[n + a], U[2 * n + a]};
+  double uR[3] = {U[b], U[n + b], U[2 * n + b]};
+  if (DAMP4) {
+    const double eps = 1.0e-9, k = 1.0 / 3.0;
+    const double dx = xyz[b] - xyz[a], dy = xyz[n + b] - xyz[n + a],
+                 dz = xyz[2 * n + b] - xyz[2 * n + a];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const double g1 = G[(c * 3 + 0) * n + a] * dx + G[(c * 3 + 1) * n + a] * dy +
+                        G[(c * 3 + 2) * n + a] * dz;
+      const double g2 = G[(c * 3 + 0) * n + b] * dx + G[(c * 3 + 1) * n + b] * dy +
+                        G[(c * 3 + 2) * n + b] * dz;
+      const double delta2 = uR[c] - uL[c];
+      const double delta1 = 2.0 * g1 - delta2;
+      const double delta3 = 2.0 * g2 - delta2;
+      const double rL = (delta2 + eps) / (delta1 + eps);
+      const double rR = (delta2 + eps) / (delta3 + eps);
+      const double rLinv = (delta1 + eps) / (delta2 + eps);
+      const double rRinv = (delta3 + eps) / (delta2 + eps);
+      const double phiL = (fabs(rL) + rL) / (fabs(rL) + 1.0);
+      const double phiR = (fabs(rR) + rR) / (fabs(rR) + 1.0);
+      const double phiLi = (fabs(rLinv) + rLinv) / (fabs(rLinv) + 1.0);
+      const double phiRi = (fabs(rRinv) + rRinv) / (fabs(rRinv) + 1.0);
+      uL[c] += 0.25 * (delta1 * (1.0 - k) * phiL + delta2 * (1.0 + k) * phiLi);
+      uR[c] -= 0.25 * (delta3 * (1.0 - k) * phiR + delta2 * (1.0 + k) * phiRi);
+    }
+  }
+  const double nx = d.x, ny = d.y, nz = d.z;
+  const double vnL = uL[0] * nx + uL[1] * ny + uL[2] * nz;
+  const double vnR = uR[0] * nx + uR[1] * ny + uR[2] * nz;
+  double aw = 0.0;
+  if (ap.stab) aw = fabs(vnL + vnR) / 2.0;
+  if (ap.stab2) aw += ap.stab2coef * fmax(fabs(vnL), fabs(vnR));
+  const double v = d.w * ap.mu;
+  const double pf = P[a] + P[b];
+  const double nv[3] = {nx, ny, nz};
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    if (DAMP4)
+      f[c] = uL[c] * vnL + uR[c] * vnR + pf * nv[c] + aw * (uR[c] - uL[c]) -
+             v * (U[c * n + b] - U[c * n + a]);
+    else
+      f[c] = uL[c] * vnL + uR[c] * vnR + pf * nv[c] + (aw - v) * (uR[c] - uL[c]);
+  }
+}
+
+// chorin::rhs (Chorin.cpp:831-1044) at every node, fused with the explicit
+// stage update of ChoCG::solve (src/Inciter/ChoCG.cpp:1550-1566):
+// u_out = un - dtk R / vol, where un is this stage's input at stage 0.
+// With dtk == 0 and a null u_out only R is written (drop-in).
+template <bool DAMP4>
+__global__ void __launch_bounds__(kBlock) k_crhs(int64_t n, ChoAdj adj, const double* U,
+                                                  const double* G, const double* P, ChoBnd bnd,
+                                                  AdvPrm ap, const double* __restrict__ vol,
+                                                  double dtk, int stage0, double* un,
+                                                  double* __restrict__ uout,
+                                                  double* __restrict__ R) {
+  const int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (p >= n) return;
+  const int lane = static_cast<int>(p & (kSlice - 1));
+  const int64_t s = p >> 5;
+  const int32_t off = __ldg(adj.soff + s), w = __ldg(adj.swidth + s);
+  double acc[3] = {0.0, 0.0, 0.0};
+  for (int k = 0; k < w; ++k) {
+    const int32_t e = off + k * kSlice + lane;
+    int32_t q = __ldg(adj.nbr + e);
+    if (q == kPad) continue;
+    const bool first = q >= 0;
+    if (!first) q = ~q;
+    const Coef4 d = ldd4(adj.dd + e);
+    double f[3];
+    adv_edge<DAMP4>(U, G, P, bnd.xyz, n, d, first ? p : q, first ? q : p, ap, f);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) acc[c] = first ? acc[c] - f[c] : acc[c] + f[c];
+  }
+  const int32_t bi = __ldg(bnd.bidx + p);
+  if (bi >= 0) {
+    for (int32_t j = __ldg(bnd.bptr + bi); j < __ldg(bnd.bptr + bi + 1); ++j) {
+      const int32_t ent = __ldg(bnd.bent + j);
+      const int pos = ent & 3;
+      int32_t N[3];
+      double nn[3];
+      tri_normal6(bnd, n, ent >> 2, N, nn);
+      double fl[3][3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const double uu = U[N[a]], vv = U[n + N[a]], ww = U[2 * n + N[a]], pp = P[N[a]];
+        const double vn = nn[0] * uu + nn[1] * vv + nn[2] * ww;
+        fl[0][a] = uu * vn + pp * nn[0];
+        fl[1][a] = vv * vn + pp * nn[1];
+        fl[2][a] = ww * vn + pp * nn[2];
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) acc[c] += wavg(pos, fl[c][0], fl[c][1], fl[c][2]);
+    }
+  }
+  if (R) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) R[c * n + p] = acc[c];
+  }
+  if (uout) {
+    const double v = vol[p];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      double u0;
+      if (stage0) {
+        u0 = U[c * n + p];
+        un[c * n + p] = u0;
+      } else {
+        u0 = un[c * n + p];
+      }
+      uout[c * n + p] = u0 - dtk * acc[c] / v;
+    }
+  }
+}
+
+// ChoCG::BC (src/Inciter/ChoCG.cpp:1333-1354) per BC node, in the
+// reference's order: Dirichlet components, symmetry projections (one per
+// set holding the node), noslip.  sym_only applies just the symmetry
+// projections (to the start-up momentum flux, ChoCG.cpp:878).
+__global__ void k_cbc(int64_t n, int64_t nbc, const int32_t* __restrict__ node,
+                      const int32_t* __restrict__ dir, const int32_t* __restrict__ symp,
+                      const int32_t* __restrict__ noslip, const int32_t* __restrict__ dirmask,
+                      const double* __restrict__ dirval, const double* __restrict__ symn,
+                      int sym_only, double* U) {
+  const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= nbc) return;
+  const int64_t p = node[i];
+  double u[3] = {U[p], U[n + p], U[2 * n + p]};
+  const int32_t dd = dir[i];
+  if (!sym_only && dd >= 0) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      if (dirmask[dd * 3 + c]) u[c] = dirval[dd * 3 + c];
+  }
+  for (int32_t k = symp[i]; k < symp[i + 1]; ++k) {
+    const double* nn = symn + 3 * k;
+    const double vn = u[0] * nn[0] + u[1] * nn[1] + u[2] * nn[2];
+    u[0] -= vn * nn[0];
+    u[1] -= vn * nn[1];
+    u[2] -= vn * nn[2];
+  }
+  if (!sym_only && noslip[i]) u[0] = u[1] = u[2] = 0.0;
+  U[p] = u[0];
+  U[n + p] = u[1];
+  U[2 * n + p] = u[2];
+}
+
+// ChoCG::dt (src/Inciter/ChoCG.cpp:1356-1412): min over nodes of
+// cbrt(V)/max(|u|, 1e-8) and, with viscosity, V^(2/3)/mu.
+__global__ void __launch_bounds__(kBlock) k_cdt(int64_t n, const double* __restrict__ U,
+                                                 const double* __restrict__ vol, double mu,
+                                                 unsigned long long* dtmin) {
+  const int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  double m = DBL_MAX;
+  if (p < n) {
+    const double u = U[p], v = U[n + p], w = U[2 * n + p];
+    const double vel = sqrt(u * u + v * v + w * w);
+    const double L = cbrt(vol[p]);
+    m = fmin(m, L / fmax(vel, 1.0e-8));
+    if (mu > DBL_EPSILON) m = fmin(m, L * L / mu);
+  }
+  block_min(m, dtmin);
+}
+
+__global__ void k_aos_soa(int64_t n, int nc, const double* __restrict__ a, double* __restrict__ s) {
+  const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= n * nc) return;
+  const int64_t p = i / nc;
+  const int c = static_cast<int>(i - p * nc);
+  s[c * n + p] = a[i];
+}
+__global__ void k_soa_aos(int64_t n, int nc, const double* __restrict__ s, double* __restrict__ a) {
+  const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= n * nc) return;
+  const int64_t p = i / nc;
+  const int c = static_cast<int>(i - p * nc);
+  a[i] = s[c * n + p];
+}
+
+// ---------------------------------------------------------------- host side
+
+ChoAdj adj_of(ChoCGDev* d) { return ChoAdj{d->soff, d->swidth, d->nbr, d->dd}; }
+ChoBnd bnd_of(ChoCGDev* d) { return ChoBnd{d->bidx, d->bptr, d->bent, d->btri, d->xyz}; }
+AdvPrm adv_of(ChoCGDev* d) {
+  return AdvPrm{d->prm.mu, d->prm.stab2coef, d->prm.stab != 0, d->prm.stab2 != 0};
+}
+
+int get_ctx(xg_ctx* c, ChoCGDev** out, bool need_cg) {
+  int rc = use(c);
+  if (rc) return rc;
+  ChoCGDev* d = c->chocg;
+  if (!d) return fail(c, XG_ERR_STATE, "chocg: no operators (xg_chocg_setup)");
+  if (need_cg && cg_rows(c) != d->n)
+    return fail(c, XG_ERR_STATE, "chocg: the context's CG system is not the pressure matrix");
+  *out = d;
+  return XG_OK;
+}
+
+template <int NC, int MODE>
+int launch_grad(xg_ctx* c, ChoCGDev* d, const double* U, double* G, double dt = 0.0,
+                int addp = 0) {
+  k_cgrad<NC, MODE><<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(
+      d->n, adj_of(d), U, bnd_of(d), d->vol, G, dt, addp, d->u, d->pr);
+  XG_CHECK_LAUNCH(c);
+  return XG_OK;
+}
+
+int launch_bc(xg_ctx* c, ChoCGDev* d, double* U, int sym_only) {
+  if (d->nbc == 0) return XG_OK;
+  k_cbc<<<blocks_for(d->nbc, kBlock), kBlock, 0, c->stream>>>(
+      d->n, d->nbc, d->bcnode, d->bcdir, d->bcsymp, d->bcnoslip, d->dirmask, d->dirval, d->symn,
+      sym_only, U);
+  XG_CHECK_LAUNCH(c);
+  return XG_OK;
+}
+
+int launch_div(xg_ctx* c, ChoCGDev* d, const double* U, double dt, int stab, int bydt) {
+  k_cdiv<<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(
+      d->n, adj_of(d), U, d->pr, d->pgrad, bnd_of(d), dt, stab, bydt, d->div);
+  XG_CHECK_LAUNCH(c);
+  return XG_OK;
+}
+
+int launch_rhs(xg_ctx* c, ChoCGDev* d, const double* U, double dtk, int stage0, double* uout,
+               double* R) {
+  const AdvPrm ap = adv_of(d);
+  if (d->prm.flux == XG_DAMP4)
+    k_crhs<true><<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(
+        d->n, adj_of(d), U, d->vgrad, d->pr, bnd_of(d), ap, d->vol, dtk, stage0, d->un, uout, R);
+  else
+    k_crhs<false><<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(
+        d->n, adj_of(d), U, d->vgrad, d->pr, bnd_of(d), ap, d->vol, dtk, stage0, d->un, uout, R);
+  XG_CHECK_LAUNCH(c);
+  return XG_OK;
+}
+
+// One pressure solve of ChoCG::pinit/psolve on the context's CG system with
+// the device right-hand side d->div: Dirichlet values of the first solves or
+// zero, warm start from the previous solution.  As in the reference, a solve
+// that stops short of the tolerance (iteration limit or the (p,q) breakdown
+// guard) does not stop the scheme: last_it is then the negated count.
+int pressure_solve(xg_ctx* c, ChoCGDev* d, int zero_values) {
+  int rc = cg_init_device(c, d->div, zero_values, d->prm.ppc);
+  if (rc) return rc;
+  int64_t it = 0, outer = 0;
+  double normr = 0, normb = 0;
+  int conv = 0;
+  if (d->prm.pmixed)
+    rc = xg_cg_solve_mixed(c, 1000, d->prm.ptol, d->prm.pinner_tol, d->prm.pmaxit, &outer, &it,
+                           &normr, &normb, &conv);
+  else
+    rc = xg_cg_solve(c, d->prm.pmaxit, d->prm.ptol, &it, &normr, &normb, &conv);
+  if (rc && rc != XG_ERR_NOTCONV) return rc;
+  d->last_it = conv ? it : -it;
+  return XG_OK;
+}
+
+// Time step size of the device state (ChoCG::dt): synchronises.
+int step_dt(xg_ctx* c, ChoCGDev* d, double* dt) {
+  if (std::fabs(d->prm.const_dt) > DBL_EPSILON) {
+    *dt = d->prm.const_dt;
+    return XG_OK;
+  }
+  const unsigned long long big = 0x7fefffffffffffffull;  // DBL_MAX bits
+  XG_CUDA(c, cudaMemcpyAsync(d->dtmin, &big, sizeof(big), cudaMemcpyHostToDevice, c->stream));
+  k_cdt<<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(d->n, d->u, d->vol, d->prm.mu,
+                                                             d->dtmin);
+  XG_CHECK_LAUNCH(c);
+  unsigned long long bits = 0;
+  XG_CUDA(c, cudaMemcpyAsync(&bits, d->dtmin, sizeof(bits), cudaMemcpyDeviceToHost, c->stream));
+  XG_CUDA(c, cudaStreamSynchronize(c->stream));
+  double m;
+  std::memcpy(&m, &bits, sizeof(m));
+  *dt = m * d->prm.cfl;
+  return XG_OK;
+}
+
+struct EdgeRec {
+  int64_t a, b;
+  double d[5];
+};
+
+}  // namespace
+
+}  // namespace xg
+
+using namespace xg;
+
+extern "C" {
+
+int xg_chocg_setup(xg_ctx* c, const xg_chocg_params* prm, int64_t npoin, const double* coord,
+                   const double* vol, int64_t ntet, const uint64_t* dsupedge0,
+                   const double* dsupint0, int64_t ntri, const uint64_t* dsupedge1,
+                   const double* dsupint1, int64_t nedge, const uint64_t* dsupedge2,
+                   const double* dsupint2, int64_t nbtri, const uint64_t* triinpoel) {
+  int rc = use(c);
+  if (rc) return rc;
+  if (!prm || npoin <= 0 || !coord || !vol) return fail(c, XG_ERR_ARG, "chocg_setup: bad mesh");
+  if (npoin >= (int64_t(1) << 31) - 64) return fail(c, XG_ERR_ARG, "chocg_setup: too many nodes");
+  if (prm->flux != XG_DAMP2 && prm->flux != XG_DAMP4)
+    return fail(c, XG_ERR_ARG, "Flux not correctly configured");
+  if (prm->rk < 1 || prm->rk > 4) return fail(c, XG_ERR_ARG, "chocg_setup: rk must be 1..4");
+  if (prm->ppc < 0 || prm->ppc > 2) return fail(c, XG_ERR_ARG, "chocg_setup: unknown pressure pc");
+  if (prm->pmaxit <= 0 || !(prm->ptol >= 0))
+    return fail(c, XG_ERR_ARG, "chocg_setup: bad pressure iteration limit or tolerance");
+  if ((ntet && (!dsupedge0 || !dsupint0)) || (ntri && (!dsupedge1 || !dsupint1)) ||
+      (nedge && (!dsupedge2 || !dsupint2)) || (nbtri && !triinpoel))
+    return fail(c, XG_ERR_ARG, "chocg_setup: null superedge or boundary array");
+  const int64_t n = npoin;
+  // superedges -> edges in the orientation chorin:: evaluates them
+  // (Chorin.cpp:122-170: tet group (0,1),(1,2),(2,0),(0,3),(1,3),(2,3),
+  // triangle group (0,1),(1,2),(2,0))
+  std::vector<EdgeRec> E;
+  E.reserve(static_cast<size_t>(ntet * 6 + ntri * 3 + nedge));
+  static const int tp[6][2] = {{0, 1}, {1, 2}, {2, 0}, {0, 3}, {1, 3}, {2, 3}};
+  static const int rp[3][2] = {{0, 1}, {1, 2}, {2, 0}};
+  auto bad = [&](uint64_t id) { return id >= static_cast<uint64_t>(n); };
+  auto push = [&](uint64_t a, uint64_t b, const double* dd) -> bool {
+    if (bad(a) || bad(b) || a == b) return false;
+    EdgeRec r{int64_t(a), int64_t(b), {dd[0], dd[1], dd[2], dd[3], dd[4]}};
+    E.push_back(r);
+    return true;
+  };
+  for (int64_t e = 0; e < ntet; ++e)
+    for (int k = 0; k < 6; ++k)
+      if (!push(dsupedge0[e * 4 + tp[k][0]], dsupedge0[e * 4 + tp[k][1]],
+                dsupint0 + (e * 6 + k) * 5))
+        return fail(c, XG_ERR_ARG, "chocg_setup: tet superedge id");
+  for (int64_t e = 0; e < ntri; ++e)
+    for (int k = 0; k < 3; ++k)
+      if (!push(dsupedge1[e * 3 + rp[k][0]], dsupedge1[e * 3 + rp[k][1]],
+                dsupint1 + (e * 3 + k) * 5))
+        return fail(c, XG_ERR_ARG, "chocg_setup: triangle superedge id");
+  for (int64_t e = 0; e < nedge; ++e)
+    if (!push(dsupedge2[e * 2], dsupedge2[e * 2 + 1], dsupint2 + e * 5))
+      return fail(c, XG_ERR_ARG, "chocg_setup: edge id");
+  // per-node entries sorted by neighbour id
+  std::vector<int64_t> start(n + 1, 0);
+  for (auto& e : E) {
+    ++start[e.a + 1];
+    ++start[e.b + 1];
+  }
+  for (int64_t i = 0; i < n; ++i) start[i + 1] += start[i];
+  struct Ent {
+    int64_t q, eid;
+    bool first;
+  };
+  std::vector<Ent> ent(static_cast<size_t>(start[n]));
+  {
+    std::vector<int64_t> fill(start.begin(), start.end() - 1);
+    for (size_t k = 0; k < E.size(); ++k) {
+      ent[fill[E[k].a]++] = {E[k].b, int64_t(k), true};
+      ent[fill[E[k].b]++] = {E[k].a, int64_t(k), false};
+    }
+  }
+  for (int64_t p = 0; p < n; ++p)
+    std::sort(ent.begin() + start[p], ent.begin() + start[p + 1],
+              [](const Ent& x, const Ent& y) { return x.q < y.q || (x.q == y.q && x.eid < y.eid); });
+  const int64_t nslice = (n + kSlice - 1) / kSlice;
+  std::vector<int32_t> soff(nslice + 1), swidth(nslice);
+  int64_t total = 0;
+  for (int64_t s = 0; s < nslice; ++s) {
+    int64_t w = 0;
+    for (int64_t p = s * kSlice; p < std::min(n, (s + 1) * kSlice); ++p)
+      w = std::max<int64_t>(w, start[p + 1] - start[p]);
+    swidth[s] = static_cast<int32_t>(w);
+    soff[s] = static_cast<int32_t>(total);
+    total += w * kSlice;
+    if (total >= (int64_t(1) << 31)) return fail(c, XG_ERR_ARG, "chocg_setup: adjacency too large");
+  }
+  soff[nslice] = static_cast<int32_t>(total);
+  std::vector<int32_t> nbr(static_cast<size_t>(std::max<int64_t>(1, total)), kPad);
+  std::vector<Coef4> dd(nbr.size(), Coef4{0.0, 0.0, 0.0, 0.0});
+  for (int64_t p = 0; p < n; ++p) {
+    const int64_t s = p / kSlice, lane = p % kSlice;
+    for (int64_t k = 0; k < start[p + 1] - start[p]; ++k) {
+      const Ent& en = ent[start[p] + k];
+      const int64_t idx = soff[s] + k * kSlice + lane;
+      nbr[idx] = en.first ? static_cast<int32_t>(en.q) : ~static_cast<int32_t>(en.q);
+      const double* r = E[en.eid].d;
+      dd[idx] = Coef4{r[0], r[1], r[2], r[4]};
+    }
+  }
+  // boundary triangles, per boundary node the (triangle, position) pairs in
+  // triangle order
+  std::vector<int32_t> bidx(n, -1), btri(std::max<int64_t>(1, nbtri * 3));
+  std::vector<int32_t> bcount;
+  int64_t nbn = 0;
+  for (int64_t t = 0; t < nbtri; ++t)
+    for (int a = 0; a < 3; ++a) {
+      const uint64_t p = triinpoel[t * 3 + a];
+      if (bad(p)) return fail(c, XG_ERR_ARG, "chocg_setup: triinpoel id");
+      btri[t * 3 + a] = static_cast<int32_t>(p);
+      if (bidx[p] < 0) {
+        bidx[p] = static_cast<int32_t>(nbn++);
+        bcount.push_back(0);
+      }
+      ++bcount[bidx[p]];
+    }
+  std::vector<int32_t> bptr(nbn + 1, 0), bent(std::max<int64_t>(1, nbtri * 3));
+  for (int64_t i = 0; i < nbn; ++i) bptr[i + 1] = bptr[i] + bcount[i];
+  {
+    std::vector<int32_t> fill(bptr.begin(), bptr.end() - 1);
+    for (int64_t t = 0; t < nbtri; ++t)
+      for (int a = 0; a < 3; ++a)
+        bent[fill[bidx[triinpoel[t * 3 + a]]]++] = static_cast<int32_t>(t * 4 + a);
+  }
+  if (c->chocg) {
+    XG_CUDA(c, cudaStreamSynchronize(c->stream));
+    destroy_chocg(c->chocg);
+    c->chocg = nullptr;
+  }
+  auto* d = new ChoCGDev;
+  c->chocg = d;
+  d->n = n;
+  d->prm = *prm;
+  d->nslice = nslice;
+  d->nent = total;
+  d->nbn = nbn;
+  for (int pass = 0; pass < 2; ++pass) {
+    Arena& A = d->arena;
+    A.plan(d->soff, soff.size());
+    A.plan(d->swidth, swidth.size());
+    A.plan(d->nbr, nbr.size());
+    A.plan(d->dd, dd.size());
+    A.plan(d->bidx, n);
+    A.plan(d->bptr, bptr.size());
+    A.plan(d->bent, bent.size());
+    A.plan(d->btri, btri.size());
+    A.plan(d->xyz, 3 * n);
+    A.plan(d->vol, n);
+    A.plan(d->u, 3 * n);
+    A.plan(d->u2, 3 * n);
+    A.plan(d->un, 3 * n);
+    A.plan(d->pr, n);
+    A.plan(d->pgrad, 3 * n);
+    A.plan(d->vgrad, 9 * n);
+    A.plan(d->div, n);
+    A.plan(d->flx, 3 * n);
+    A.plan(d->stage, 9 * n);
+    A.plan(d->dtmin, 1);
+    if (pass == 0) {
+      cudaError_t e = A.reserve();
+      if (e != cudaSuccess) {
+        destroy_chocg(d);
+        c->chocg = nullptr;
+        return fail(c, XG_ERR_CUDA, std::string("chocg_setup: ") + cudaGetErrorString(e));
+      }
+    }
+  }
+  auto up = [&](void* dst, const void* src, size_t bytes) {
+    return cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
+  };
+  XG_CUDA(c, up(d->soff, soff.data(), soff.size() * 4));
+  XG_CUDA(c, up(d->swidth, swidth.data(), swidth.size() * 4));
+  XG_CUDA(c, up(d->nbr, nbr.data(), nbr.size() * 4));
+  XG_CUDA(c, up(d->dd, dd.data(), dd.size() * sizeof(Coef4)));
+  XG_CUDA(c, up(d->bidx, bidx.data(), n * 4));
+  XG_CUDA(c, up(d->bptr, bptr.data(), bptr.size() * 4));
+  XG_CUDA(c, up(d->bent, bent.data(), bent.size() * 4));
+  XG_CUDA(c, up(d->btri, btri.data(), btri.size() * 4));
+  XG_CUDA(c, up(d->xyz, coord, 3 * n * 8));
+  XG_CUDA(c, up(d->vol, vol, n * 8));
+  for (double* z : {d->u, d->u2, d->un, d->pr, d->pgrad, d->vgrad, d->div, d->flx})
+    XG_CUDA(c, cudaMemset(z, 0, (z == d->vgrad ? 9 : (z == d->pr || z == d->div ? 1 : 3)) * n * 8));
+  return XG_OK;
+}
+
+int xg_chocg_set_bc(xg_ctx* c, int64_t ndir, const uint64_t* dirnodes, const int32_t* dirmask,
+                    const double* dirvals, int64_t nsym, const uint64_t* symnodes,
+                    const double* symnorms, int64_t nnoslip, const uint64_t* noslipnodes,
+                    int64_t npdir, const uint64_t* pdirnodes, const double* pdirvals) {
+  ChoCGDev* d = nullptr;
+  int rc = get_ctx(c, &d, false);
+  if (rc) return rc;
+  if ((ndir && (!dirnodes || !dirmask || !dirvals)) || (nsym && (!symnodes || !symnorms)) ||
+      (nnoslip && !noslipnodes) || (npdir && (!pdirnodes || !pdirvals)) || ndir < 0 ||
+      nsym < 0 || nnoslip < 0 || npdir < 0)
+    return fail(c, XG_ERR_ARG, "chocg_set_bc: bad BC arrays");
+  const int64_t n = d->n;
+  auto bad = [&](uint64_t id) { return id >= static_cast<uint64_t>(n); };
+  // BC program: one entry per distinct BC node, in node order
+  std::vector<int32_t> dirof(n, -1), noslip(n, 0);
+  std::vector<std::vector<int32_t>> symof;
+  for (int64_t k = 0; k < ndir; ++k) {
+    if (bad(dirnodes[k])) return fail(c, XG_ERR_ARG, "chocg_set_bc: Dirichlet node out of range");
+    dirof[dirnodes[k]] = static_cast<int32_t>(k);
+  }
+  for (int64_t k = 0; k < nnoslip; ++k) {
+    if (bad(noslipnodes[k])) return fail(c, XG_ERR_ARG, "chocg_set_bc: noslip node out of range");
+    noslip[noslipnodes[k]] = 1;
+  }
+  std::vector<int64_t> symcount(n, 0);
+  for (int64_t k = 0; k < nsym; ++k) {
+    if (bad(symnodes[k])) return fail(c, XG_ERR_ARG, "chocg_set_bc: symmetry node out of range");
+    ++symcount[symnodes[k]];
+  }
+  std::vector<int32_t> node, dir, nsl, symp(1, 0);
+  std::vector<double> symn;
+  std::vector<std::vector<int64_t>> symlist(n);
+  for (int64_t k = 0; k < nsym; ++k) symlist[symnodes[k]].push_back(k);
+  for (int64_t p = 0; p < n; ++p) {
+    if (dirof[p] < 0 && !noslip[p] && symcount[p] == 0) continue;
+    node.push_back(static_cast<int32_t>(p));
+    dir.push_back(dirof[p]);
+    nsl.push_back(noslip[p]);
+    for (int64_t k : symlist[p])
+      for (int a = 0; a < 3; ++a) symn.push_back(symnorms[k * 3 + a]);
+    symp.push_back(static_cast<int32_t>(symn.size() / 3));
+  }
+  d->bcarena.release();
+  d->nbc = static_cast<int64_t>(node.size());
+  for (int pass = 0; pass < 2; ++pass) {
+    Arena& A = d->bcarena;
+    A.plan(d->bcnode, std::max<size_t>(1, node.size()));
+    A.plan(d->bcdir, std::max<size_t>(1, dir.size()));
+    A.plan(d->bcnoslip, std::max<size_t>(1, nsl.size()));
+    A.plan(d->bcsymp, symp.size());
+    A.plan(d->symn, std::max<size_t>(1, symn.size()));
+    A.plan(d->dirmask, std::max<int64_t>(1, ndir * 3));
+    A.plan(d->dirval, std::max<int64_t>(1, ndir * 3));
+    if (pass == 0) XG_CUDA(c, A.reserve());
+  }
+  auto up = [&](void* dst, const void* src, size_t bytes) {
+    return bytes ? cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice) : cudaSuccess;
+  };
+  XG_CUDA(c, up(d->bcnode, node.data(), node.size() * 4));
+  XG_CUDA(c, up(d->bcdir, dir.data(), dir.size() * 4));
+  XG_CUDA(c, up(d->bcnoslip, nsl.data(), nsl.size() * 4));
+  XG_CUDA(c, up(d->bcsymp, symp.data(), symp.size() * 4));
+  XG_CUDA(c, up(d->symn, symn.data(), symn.size() * 8));
+  XG_CUDA(c, up(d->dirmask, dirmask, ndir * 3 * 4));
+  XG_CUDA(c, up(d->dirval, dirvals, ndir * 3 * 8));
+  // pressure Dirichlet nodes on the context's CG system
+  if (cg_rows(c) != n)
+    return fail(c, XG_ERR_STATE, "chocg_set_bc: set up the pressure matrix (xg_cg_setup) first");
+  std::vector<uint8_t> mask(n, 0);
+  std::vector<double> val(n, 0.0);
+  for (int64_t k = 0; k < npdir; ++k) {
+    if (bad(pdirnodes[k]))
+      return fail(c, XG_ERR_ARG, "chocg_set_bc: pressure Dirichlet node out of range");
+    mask[pdirnodes[k]] = 1;
+    val[pdirnodes[k]] = pdirvals[k];
+  }
+  rc = cg_set_dirichlet(c, mask.data(), val.data());
+  if (rc) return rc;
+  d->pdir_set = true;
+  return XG_OK;
+}
+
+int xg_chocg_set_state(xg_ctx* c, const double* u, const double* p, double t) {
+  ChoCGDev* d = nullptr;
+  int rc = get_ctx(c, &d, false);
+  if (rc) return rc;
+  if (!u) return fail(c, XG_ERR_ARG, "chocg_set_state: null velocity");
+  const int64_t n = d->n;
+  XG_CUDA(c, cudaMemcpyAsync(d->stage, u, n * 3 * 8, cudaMemcpyHostToDevice, c->stream));
+  k_aos_soa<<<blocks_for(n * 3, kBlock), kBlock, 0, c->stream>>>(n, 3, d->stage, d->u);
+  XG_CHECK_LAUNCH(c);
+  if (p)
+    XG_CUDA(c, cudaMemcpyAsync(d->pr, p, n * 8, cudaMemcpyHostToDevice, c->stream));
+  else
+    XG_CUDA(c, cudaMemsetAsync(d->pr, 0, n * 8, c->stream));
+  XG_CUDA(c, cudaMemsetAsync(d->pgrad, 0, n * 3 * 8, c->stream));
+  XG_CUDA(c, cudaStreamSynchronize(c->stream));
+  d->t = t;
+  d->ready = false;
+  return XG_OK;
+}
+
+int xg_chocg_get_state(xg_ctx* c, double* u, double* p, double* t) {
+  ChoCGDev* d = nullptr;
+  int rc = get_ctx(c, &d, false);
+  if (rc) return rc;
+  const int64_t n = d->n;
+  if (u) {
+    k_soa_aos<<<blocks_for(n * 3, kBlock), kBlock, 0, c->stream>>>(n, 3, d->u, d->stage);
+    XG_CHECK_LAUNCH(c);
+    XG_CUDA(c, cudaMemcpyAsync(u, d->stage, n * 3 * 8, cudaMemcpyDeviceToHost, c->stream));
+  }
+  if (p) XG_CUDA(c, cudaMemcpyAsync(p, d->pr, n * 8, cudaMemcpyDeviceToHost, c->stream));
+  XG_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (t) *t = d->t;
+  return XG_OK;
+}
+
+int xg_chocg_init(xg_ctx* c, int64_t* it) {
+  ChoCGDev* d = nullptr;
+  int rc = get_ctx(c, &d, true);
+  if (rc) return rc;
+  if (!d->pdir_set) return fail(c, XG_ERR_STATE, "chocg_init: no BCs (xg_chocg_set_bc)");
+  // m_np = 0 (ChoCG::merge -> div -> pinit -> psolve -> sgrad -> psolved):
+  // BCs, divergence without stabilisation, projection with dt = 1
+  rc = launch_bc(c, d, d->u, 0);
+  if (rc) return rc;
+  rc = cg_zero_solution(c);
+  if (rc) return rc;
+  rc = launch_div(c, d, d->u, 0.0, 0, 0);
+  if (rc) return rc;
+  rc = pressure_solve(c, d, 0);
+  if (rc) return rc;
+  rc = launch_grad<1, GRAD_PROJECT>(c, d, cg_solution_device(c), nullptr, 1.0, 0);
+  if (rc) return rc;
+  rc = launch_bc(c, d, d->u, 0);
+  if (rc) return rc;
+  // m_np = 1 (velgrad -> flux -> div -> pinit -> psolve -> psolved): the
+  // divergence of the volume-divided momentum flux with symmetry applied
+  rc = launch_grad<3, GRAD_DIVIDE>(c, d, d->u, d->vgrad);
+  if (rc) return rc;
+  k_cflux<<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(
+      d->n, adj_of(d), d->u, d->vgrad, bnd_of(d), d->vol, d->prm.mu, 1, d->flx);
+  XG_CHECK_LAUNCH(c);
+  rc = launch_bc(c, d, d->flx, 1);
+  if (rc) return rc;
+  rc = launch_div(c, d, d->flx, 0.0, 0, 0);
+  if (rc) return rc;
+  rc = pressure_solve(c, d, 0);
+  if (rc) return rc;
+  // m_np = 2: initial pressure and its gradient
+  XG_CUDA(c, cudaMemcpyAsync(d->pr, cg_solution_device(c), d->n * 8, cudaMemcpyDeviceToDevice,
+                             c->stream));
+  rc = launch_grad<1, GRAD_DIVIDE>(c, d, d->pr, d->pgrad);
+  if (rc) return rc;
+  XG_CUDA(c, cudaStreamSynchronize(c->stream));
+  d->ready = true;
+  if (it) *it = d->last_it;
+  return XG_OK;
+}
+
+int xg_chocg_run(xg_ctx* c, int64_t nstep, double* dts, int64_t* its, float* ms) {
+  ChoCGDev* d = nullptr;
+  int rc = get_ctx(c, &d, true);
+  if (rc) return rc;
+  if (!d->ready) return fail(c, XG_ERR_STATE, "chocg_run before chocg_init");
+  static const double rkc[4][4] = {{1.0, 0, 0, 0},
+                                   {1.0 / 2.0, 1.0, 0, 0},
+                                   {1.0 / 3.0, 1.0 / 2.0, 1.0, 0},
+                                   {1.0 / 4.0, 1.0 / 3.0, 1.0 / 2.0, 1.0}};
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (ms) {
+    XG_CUDA(c, cudaEventCreate(&e0));
+    XG_CUDA(c, cudaEventCreate(&e1));
+    XG_CUDA(c, cudaEventRecord(e0, c->stream));
+  }
+  int status = XG_OK;
+  for (int64_t st = 0; st < nstep; ++st) {
+    double dt = 0.0;
+    rc = step_dt(c, d, &dt);
+    if (rc) return rc;
+    if (dt < DBL_EPSILON) {
+      status = XG_ERR_BLOWUP;
+      fail(c, XG_ERR_BLOWUP, "chocg: dt below eps");
+      break;
+    }
+    // momentum prediction (ChoCG::rhs -> solve -> pred -> corr, per stage)
+    for (int k = 0; k < d->prm.rk; ++k) {
+      rc = launch_rhs(c, d, d->u, rkc[d->prm.rk - 1][k] * dt, k == 0, d->u2, nullptr);
+      if (rc) return rc;
+      std::swap(d->u, d->u2);
+      rc = launch_bc(c, d, d->u, 0);
+      if (rc) return rc;
+      if (d->prm.flux == XG_DAMP4) {
+        rc = launch_grad<3, GRAD_DIVIDE>(c, d, d->u, d->vgrad);
+        if (rc) return rc;
+      }
+    }
+    // pressure increment (ChoCG::div -> pinit -> psolve) and projection
+    // (sgrad -> psolved -> pgrad)
+    rc = launch_div(c, d, d->u, dt, 1, 1);
+    if (rc) return rc;
+    rc = pressure_solve(c, d, 1);
+    if (rc) return rc;
+    rc = launch_grad<1, GRAD_PROJECT>(c, d, cg_solution_device(c), nullptr, dt, 1);
+    if (rc) return rc;
+    rc = launch_bc(c, d, d->u, 0);
+    if (rc) return rc;
+    rc = launch_grad<1, GRAD_DIVIDE>(c, d, d->pr, d->pgrad);
+    if (rc) return rc;
+    d->t += dt;
+    if (dts) dts[st] = dt;
+    if (its) its[st] = d->last_it;
+  }
+  if (ms) {
+    XG_CUDA(c, cudaEventRecord(e1, c->stream));
+    XG_CUDA(c, cudaEventSynchronize(e1));
+    XG_CUDA(c, cudaEventElapsedTime(ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+  }
+  XG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return status;
+}
+
+int xg_chocg_fields(xg_ctx* c, int what, double* out) {
+  ChoCGDev* d = nullptr;
+  int rc = get_ctx(c, &d, false);
+  if (rc) return rc;
+  if (!out) return fail(c, XG_ERR_ARG, "chocg_fields: null output");
+  const int64_t n = d->n;
+  const double* src = nullptr;
+  int nc = 1;
+  switch (what) {
+    case 0: src = d->un; nc = 3; break;
+    case 1: src = d->pgrad; nc = 3; break;
+    case 2: src = d->vgrad; nc = 9; break;
+    case 3: src = d->div; break;
+    case 4:
+      src = cg_solution_device(c);
+      if (!src || cg_rows(c) != n) return fail(c, XG_ERR_STATE, "chocg_fields: no pressure solve");
+      break;
+    default: return fail(c, XG_ERR_ARG, "chocg_fields: unknown field");
+  }
+  k_soa_aos<<<blocks_for(n * nc, kBlock), kBlock, 0, c->stream>>>(n, nc, src, d->stage);
+  XG_CHECK_LAUNCH(c);
+  XG_CUDA(c, cudaMemcpyAsync(out, d->stage, n * nc * 8, cudaMemcpyDeviceToHost, c->stream));
+  XG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return XG_OK;
+}
+
+// ---- drop-ins: host node-major arrays through per-call device buffers (the
+// device state of xg_chocg_run is left untouched)
+
+int xg_chorin_div(xg_ctx* c, const double* U, const double* P, const double* G, double dt,
+                  int stab, double* D) {
+  ChoCGDev* d = nullptr;
+  int rc = get_ctx(c, &d, false);
+  if (rc) return rc;
+  if (!U || !P || !G || !D) return fail(c, XG_ERR_ARG, "chorin_div: null array");
+  const int64_t n = d->n;
+  double *u, *p, *g, *out;
+  Arena A;
+  for (int pass = 0; pass < 2; ++pass) {
+    A.plan(u, 3 * n);
+    A.plan(p, n);
+    A.plan(g, 3 * n);
+    A.plan(out, 3 * n);
+    if (pass == 0) XG_CUDA(c, A.reserve());
+  }
+  cudaStream_t s = c->stream;
+  XG_CUDA(c, cudaMemcpyAsync(out, U, n * 24, cudaMemcpyHostToDevice, s));
+  k_aos_soa<<<blocks_for(n * 3, kBlock), kBlock, 0, s>>>(n, 3, out, u);
+  XG_CUDA(c, cudaMemcpyAsync(out, G, n * 24, cudaMemcpyHostToDevice, s));
+  k_aos_soa<<<blocks_for(n * 3, kBlock), kBlock, 0, s>>>(n, 3, out, g);
+  XG_CUDA(c, cudaMemcpyAsync(p, P, n * 8, cudaMemcpyHostToDevice, s));
+  k_cdiv<<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, adj_of(d), u, p, g, bnd_of(d), dt, stab, 0,
+                                                   out);
+  XG_CHECK_LAUNCH(c);
+  XG_CUDA(c, cudaMemcpyAsync(D, out, n * 8, cudaMemcpyDeviceToHost, s));
+  XG_CUDA(c, cudaStreamSynchronize(s));
+  return XG_OK;
+}
+
+int xg_chorin_grad(xg_ctx* c, const double* S, double* Gout) {
+  ChoCGDev* d = nullptr;
+  int rc = get_ctx(c, &d, false);
+  if (rc) return rc;
+  if (!S || !Gout) return fail(c, XG_ERR_ARG, "chorin_grad: null array");
+  const int64_t n = d->n;
+  double *sv, *g, *out;
+  Arena A;
+  for (int pass = 0; pass < 2; ++pass) {
+    A.plan(sv, n);
+    A.plan(g, 3 * n);
+    A.plan(out, 3 * n);
+    if (pass == 0) XG_CUDA(c, A.reserve());
+  }
+  cudaStream_t s = c->stream;
+  XG_CUDA(c, cudaMemcpyAsync(sv, S, n * 8, cudaMemcpyHostToDevice, s));
+  k_cgrad<1, GRAD_RAW><<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, adj_of(d), sv, bnd_of(d),
+                                                                 d->vol, g, 0.0, 0, nullptr,
+                                                                 nullptr);
+  XG_CHECK_LAUNCH(c);
+  k_soa_aos<<<blocks_for(n * 3, kBlock), kBlock, 0, s>>>(n, 3, g, out);
+  XG_CUDA(c, cudaMemcpyAsync(Gout, out, n * 24, cudaMemcpyDeviceToHost, s));
+  XG_CUDA(c, cudaStreamSynchronize(s));
+  return XG_OK;
+}
+
+int xg_chorin_vgrad(xg_ctx* c, const double* U, double* Gout) {
+  ChoCGDev* d = nullptr;
+  int rc = get_ctx(c, &d, false);
+  if (rc) return rc;
+  if (!U || !Gout) return fail(c, XG_ERR_ARG, "chorin_vgrad: null array");
+  const int64_t n = d->n;
+  double *u, *g, *out;
+  Arena A;
+  for (int pass = 0; pass < 2; ++pass) {
+    A.plan(u, 3 * n);
+    A.plan(g, 9 * n);
+    A.plan(out, 9 * n);
+    if (pass == 0) XG_CUDA(c, A.reserve());
+  }
+  cudaStream_t s = c->stream;
+  XG_CUDA(c, cudaMemcpyAsync(out, U, n * 24, cudaMemcpyHostToDevice, s));
+  k_aos_soa<<<blocks_for(n * 3, kBlock), kBlock, 0, s>>>(n, 3, out, u);
+  k_cgrad<3, GRAD_RAW><<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, adj_of(d), u, bnd_of(d),
+                                                                 d->vol, g, 0.0, 0, nullptr,
+                                                                 nullptr);
+  XG_CHECK_LAUNCH(c);
+  k_soa_aos<<<blocks_for(n * 9, kBlock), kBlock, 0, s>>>(n, 9, g, out);
+  XG_CUDA(c, cudaMemcpyAsync(Gout, out, n * 72, cudaMemcpyDeviceToHost, s));
+  XG_CUDA(c, cudaStreamSynchronize(s));
+  return XG_OK;
+}
+
+int xg_chorin_flux(xg_ctx* c, const double* U, const double* G, double* F) {
+  ChoCGDev* d = nullptr;
+  int rc = get_ctx(c, &d, false);
+  if (rc) return rc;
+  if (!U || !G || !F) return fail(c, XG_ERR_ARG, "chorin_flux: null array");
+  const int64_t n = d->n;
+  double *u, *g, *f, *tmp;
+  Arena A;
+  for (int pass = 0; pass < 2; ++pass) {
+    A.plan(u, 3 * n);
+    A.plan(g, 9 * n);
+    A.plan(f, 3 * n);
+    A.plan(tmp, 9 * n);
+    if (pass == 0) XG_CUDA(c, A.reserve());
+  }
+  cudaStream_t s = c->stream;
+  XG_CUDA(c, cudaMemcpyAsync(tmp, U, n * 24, cudaMemcpyHostToDevice, s));
+  k_aos_soa<<<blocks_for(n * 3, kBlock), kBlock, 0, s>>>(n, 3, tmp, u);
+  XG_CUDA(c, cudaMemcpyAsync(tmp, G, n * 72, cudaMemcpyHostToDevice, s));
+  k_aos_soa<<<blocks_for(n * 9, kBlock), kBlock, 0, s>>>(n, 9, tmp, g);
+  k_cflux<<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, adj_of(d), u, g, bnd_of(d), d->vol,
+                                                    d->prm.mu, 0, f);
+  XG_CHECK_LAUNCH(c);
+  k_soa_aos<<<blocks_for(n * 3, kBlock), kBlock, 0, s>>>(n, 3, f, tmp);
+  XG_CUDA(c, cudaMemcpyAsync(F, tmp, n * 24, cudaMemcpyDeviceToHost, s));
+  XG_CUDA(c, cudaStreamSynchronize(s));
+  return XG_OK;
+}
+
+int xg_chorin_rhs(xg_ctx* c, const double* P, const double* U, const double* G, double* R) {
+  ChoCGDev* d = nullptr;
+  int rc = get_ctx(c, &d, false);
+  if (rc) return rc;
+  if (!P || !U || !G || !R) return fail(c, XG_ERR_ARG, "chorin_rhs: null array");
+  const int64_t n = d->n;
+  double *u, *g, *p, *r, *tmp;
+  Arena A;
+  for (int pass = 0; pass < 2; ++pass) {
+    A.plan(u, 3 * n);
+    A.plan(g, 9 * n);
+    A.plan(p, n);
+    A.plan(r, 3 * n);
+    A.plan(tmp, 9 * n);
+    if (pass == 0) XG_CUDA(c, A.reserve());
+  }
+  cudaStream_t s = c->stream;
+  XG_CUDA(c, cudaMemcpyAsync(tmp, U, n * 24, cudaMemcpyHostToDevice, s));
+  k_aos_soa<<<blocks_for(n * 3, kBlock), kBlock, 0, s>>>(n, 3, tmp, u);
+  XG_CUDA(c, cudaMemcpyAsync(tmp, G, n * 72, cudaMemcpyHostToDevice, s));
+  k_aos_soa<<<blocks_for(n * 9, kBlock), kBlock, 0, s>>>(n, 9, tmp, g);
+  XG_CUDA(c, cudaMemcpyAsync(p, P, n * 8, cudaMemcpyHostToDevice, s));
+  const AdvPrm ap = adv_of(d);
+  if (d->prm.flux == XG_DAMP4)
+    k_crhs<true><<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, adj_of(d), u, g, p, bnd_of(d), ap,
+                                                           d->vol, 0.0, 0, nullptr, nullptr, r);
+  else
+    k_crhs<false><<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, adj_of(d), u, g, p, bnd_of(d), ap,
+                                                            d->vol, 0.0, 0, nullptr, nullptr, r);
+  XG_CHECK_LAUNCH(c);
+  k_soa_aos<<<blocks_for(n * 3, kBlock), kBlock, 0, s>>>(n, 3, r, tmp);
+  XG_CUDA(c, cudaMemcpyAsync(R, tmp, n * 24, cudaMemcpyDeviceToHost, s));
+  XG_CUDA(c, cudaStreamSynchronize(s));
+  return XG_OK;
+}
+
+}  // extern "C"

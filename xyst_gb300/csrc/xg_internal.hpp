@@ -57,6 +57,7 @@ class Arena {
 struct RieCGDev;  // xg_riecg.cu
 struct CGDev;     // xg_cg.cu
 struct KozCGDev;  // xg_kozcg.cu
+struct ChoCGDev;  // xg_chocg.cu
 
 // Matrix graph of a CG system as the learned preconditioner sees it: the full
 // rows, the strictly lower and strictly upper triangles (SELL-32 each, slice
@@ -81,9 +82,22 @@ int cg_graph(xg_ctx* c, LpcGraph* g);
 // values N_ij in the lower layout (nvL) and, transposed, the upper one (nvU).
 int lpc_factor(xg_ctx* c, xg_lpc* m, const LpcGraph& g, float* nvL, float* nvU);
 
+// Device-side pressure solves for ChoCG on the context's CG system: the
+// Dirichlet mask and the values of the first solves (host arrays, one per
+// row), a zero initial guess, ConjugateGradients::init with apply and a
+// device right-hand side (values zero when zero_values, the stored ones
+// otherwise), the device solution and the row count.
+int cg_set_dirichlet(xg_ctx* c, const uint8_t* mask, const double* val);
+int cg_zero_solution(xg_ctx* c);
+int cg_init_device(xg_ctx* c, const double* b_dev, int zero_values, int pc);
+const double* cg_solution_device(xg_ctx* c);
+int64_t cg_rows(xg_ctx* c);
+
 void destroy_riecg(RieCGDev*);
 void destroy_cg(CGDev*);
 void destroy_kozcg(KozCGDev*);
+void destroy_chocg(ChoCGDev*);
+size_t bytes_chocg(const ChoCGDev*);
 size_t bytes_riecg(const RieCGDev*);
 size_t bytes_cg(const CGDev*);
 size_t bytes_kozcg(const KozCGDev*);
@@ -97,6 +111,7 @@ struct xg_ctx {
   xg::RieCGDev* riecg = nullptr;
   xg::CGDev* cg = nullptr;
   xg::KozCGDev* kozcg = nullptr;
+  xg::ChoCGDev* chocg = nullptr;
 };
 
 namespace xg {

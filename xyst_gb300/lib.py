@@ -41,6 +41,12 @@ class KozcgParams(C.Structure):
                 ("ctau", _dbl), ("fctclip", _int), ("fctsys", _int)]
 
 
+class ChocgParams(C.Structure):
+    _fields_ = [("mu", _dbl), ("cfl", _dbl), ("const_dt", _dbl), ("flux", _int), ("stab", _int),
+                ("stab2", _int), ("stab2coef", _dbl), ("rk", _int), ("ppc", _int),
+                ("ptol", _dbl), ("pmaxit", _i64), ("pmixed", _int), ("pinner_tol", _dbl)]
+
+
 # name -> (restype, argtypes); every function of include/xg.h
 SIGNATURES = {
     "xg_create": (_int, [_int, C.POINTER(_vp)]),
@@ -70,6 +76,20 @@ SIGNATURES = {
     "xg_kozcg_bc": (_int, [_vp]),
     "xg_kozcg_dt": (_int, [_vp, _vp]),
     "xg_kozcg_run": (_int, [_vp, _i64, _vp, _vp]),
+    "xg_chocg_setup": (_int, [_vp, C.POINTER(ChocgParams), _i64, _vp, _vp, _i64, _vp, _vp,
+                              _i64, _vp, _vp, _i64, _vp, _vp, _i64, _vp]),
+    "xg_chocg_set_bc": (_int, [_vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp, _i64, _vp, _i64, _vp,
+                               _vp]),
+    "xg_chocg_set_state": (_int, [_vp, _vp, _vp, _dbl]),
+    "xg_chocg_get_state": (_int, [_vp, _vp, _vp, _vp]),
+    "xg_chocg_init": (_int, [_vp, _vp]),
+    "xg_chocg_run": (_int, [_vp, _i64, _vp, _vp, _vp]),
+    "xg_chocg_fields": (_int, [_vp, _int, _vp]),
+    "xg_chorin_div": (_int, [_vp, _vp, _vp, _vp, _dbl, _int, _vp]),
+    "xg_chorin_grad": (_int, [_vp, _vp, _vp]),
+    "xg_chorin_vgrad": (_int, [_vp, _vp, _vp]),
+    "xg_chorin_flux": (_int, [_vp, _vp, _vp, _vp]),
+    "xg_chorin_rhs": (_int, [_vp, _vp, _vp, _vp, _vp]),
     "xg_cg_setup": (_int, [_vp, _i64, _vp, _vp, _vp, _int]),
     "xg_cg_mult": (_int, [_vp, _vp, _vp]),
     "xg_cg_init": (_int, [_vp, _vp, _vp, _vp, _i64, _vp, _vp, _int, _int]),
