@@ -10,12 +10,16 @@ all six faces, CFL 0.5.  Synthetic data: the mesh and state are generated.
   value  node-updates/s = nodes x steps / device time (state resident in HBM)
   e2e    the same through the C ABI with host buffers: every step uploads U
          from pinned host memory, advances one step and downloads U
-  roofline  for the dominant kernel (riecg_rhs_update), algorithmic bytes per
-         launch / mean launch time from CUDA events taken inside the timed
-         region, against the measured HBM copy bandwidth
+  roofline  for the dominant kernel (the one with the largest device time),
+         algorithmic bytes per launch / mean launch time from CUDA events
+         taken inside the timed region, against the measured HBM copy
+         bandwidth
   cpu_baseline  the oracle (serial C++ restatement of the reference loops) on
          host cores, on a bounded sample (a 49^3 cube, 30 steps; the per-node
          work does not depend on the mesh size)
+  chocg  the metric's second half: ChoCG s/step on the same cube (Taylor-Green
+         vortex, Re 100), every pressure solve to 1e-8 relative residual, FP64
+         Jacobi PCG against the learned factor with mixed precision
 
 --impl reference runs the reference's CPU arithmetic (the oracle port; the
 reference itself needs Charm++ and cannot be built on the GPU machine) on all host
@@ -141,90 +145,70 @@ def kernel_bytes(n, nedge, fp32):
     return {"riecg_grad": grad, "riecg_flux": flux, "riecg_rhs_update": (rhs0 + 2 * rhs12) / 3.0}
 
 
-def pressure_system(ops):
-    """ChoCG pressure-Poisson system on the same mesh: the prelhs matrix,
-    the rhs from the edge divergence of a Taylor-Green velocity field on
-    [0, 2 pi]^3 mapped to the unit cube (unstabilised chorin::div,
-    src/Physics/Chorin.cpp:58-62), Dirichlet p = 0 on side set 4 (x = 1)."""
-    from xyst_gb300 import cg
+def run_chocg(n=129, steps=5, warm=2, tol=1e-8, train_steps=300, seed=0):
+    """ChoCG s/step on the n^3 jittered cube (Taylor-Green vortex on
+    [0, 2 pi]^3 mapped to the unit cube, mu = 1/Re = 0.01, damp2, CFL 0.5,
+    symmetry on every face, hydrostat node), every pressure-increment solve to
+    tol relative residual: FP64 Jacobi PCG (the reference's algorithm)
+    against the learned factor with the mixed-precision solve, plus the
+    factor without the network; fields after the timed steps compared with
+    the FP64 Jacobi run.  Every solve runs to the tolerance: the reference's
+    absolute (p,q) breakdown test would end these small-rhs increment solves
+    near 1e-6, so the FP64 solver guards underflow only (as the FP32 one)."""
+    from xyst_gb300 import chocg, lib, lpc, mesh
 
-    coord, inpoel = ops["coord"], ops["inpoel"]
-    ia, ja, a = cg.pressure_matrix(coord, inpoel)
-    X, Y, Z = 2 * np.pi * coord
-    u = np.stack([np.sin(X) * np.cos(Y) * np.cos(Z), -np.cos(X) * np.sin(Y) * np.cos(Z),
-                  np.zeros_like(X)], axis=1)
-    e, d = ops["edges"], ops["dint"]
-    f = (d * (u[e[:, 0]] + u[e[:, 1]])).sum(1)
-    b = np.zeros(coord.shape[1])
-    np.add.at(b, e[:, 0], -f)
-    np.add.at(b, e[:, 1], f)
-    dn = np.unique(ops["bface"][4])
-    # scale to unit RMS: the solver's (p,q) breakdown guard is an absolute
-    # epsilon (src/LinearSolver/ConjugateGradients.cpp:681-690), as ChoCG's
-    # division of the divergence by dt keeps its rhs far from it
-    b *= np.sqrt(b.size) / np.linalg.norm(b)
-    return ia, ja, a, b, dn, np.zeros(dn.size)
-
-
-def train_lpc(ctx, steps=300, lr=1e-3):
-    """The learned preconditioner, trained on the device on four small
-    ChoCG-like pressure systems (13^3-21^3 jittered cubes, p = 0 on x = 1)."""
-    from xyst_gb300 import lpc
-
+    t_setup = time.perf_counter()
+    m = mesh.cube(n, jitter=0.2, seed=seed, numbering="random", perm_seed=seed + 1)
+    ops = chocg.operators(m, sym_sets=[1, 2, 3, 4, 5, 6], hydrostat=0)
+    u0 = chocg.taylor_green(ops["coord"])
+    t_setup = time.perf_counter() - t_setup
+    tctx = lib.Context(0)
     t0 = time.perf_counter()
-    systems = [lpc.training_system(ctx, lpc.pressure_system(ctx, m, seed))
-               for m, seed in ((13, 1), (17, 2), (21, 3), (15, 4))]
-    model = lpc.LearnedPreconditioner(ctx, precision="bf16", seed=0)
-    hist = model.train(systems, steps, lr=lr)
-    return model, {"train_s": time.perf_counter() - t0, "steps": steps,
-                   "loss_first_last": [hist[0], hist[-1]],
-                   "systems": "13^3, 17^3, 21^3, 15^3 jittered cubes"}
-
-
-def run_pcg(ctx, ops, tol=1e-8, maxit=20000, reps=3):
-    """ChoCG pressure solve per time step: init (host rhs, BCs) + solve +
-    solution download, FP64 Jacobi PCG (the reference's algorithm) against
-    the learned factor with the FP32 reliable-update solver."""
-    from xyst_gb300 import cg
-
-    ia, ja, a, b, dn, dv = pressure_system(ops)
-    s = cg.ConjugateGradients(ctx, ia, ja, a)
-    n = ia.size - 1
-    out = {"tol": tol, "rows": n, "nnz": int(ja.size), "dirichlet": "p=0 on x=1 face"}
-    model, tr = train_lpc(ctx)
-    out["training"] = tr
-    modes = {"fp64_jacobi": ("jacobi", None, False), "fp64_first_order": ("factor", None, False),
-             "mixed_jacobi": ("jacobi", None, True), "mixed_first_order": ("factor", None, True),
-             "fp64_learned": ("factor", model, False), "mixed_learned": ("factor", model, True)}
+    systems = [lpc.training_system(tctx, lpc.chocg_system(tctx, k, sd))
+               for k, sd in ((13, 1), (17, 2), (21, 3), (25, 4))]
+    model = lpc.LearnedPreconditioner(tctx, precision="bf16", seed=0)
+    hist = model.train(systems, train_steps, lr=1e-3)
+    out = {"workload": f"ChoCG Taylor-Green, {n}^3 jittered cube, Re 100, damp2, CFL 0.5, "
+                       "symmetry on all faces, hydrostat node",
+           "nodes": int(ops["coord"].shape[1]), "tol": tol, "steps_timed": steps,
+           "setup_s": t_setup,
+           "training": {"s": time.perf_counter() - t0, "steps": train_steps,
+                        "loss_first_last": [hist[0], hist[-1]],
+                        "systems": "ChoCG pressure matrices (hydrostat) of 13^3-25^3 cubes"}}
+    modes = {"fp64_jacobi": ("jacobi", None, False),
+             "mixed_first_order": ("factor", "none", True),
+             "mixed_learned": ("factor", model, True)}
+    fields = {}
     for name, (pc, mdl, mixed) in modes.items():
+        ctx = lib.Context(0)
+        d = chocg.ChoCG(ctx, ops, mu=0.01, cfl=0.5, flux="damp2", pc=pc, ptol=tol,
+                        pmaxit=50000, mixed=mixed, inner_tol=1e-2, guard="underflow")
         if pc == "factor":
-            s.set_factor(mdl, 1.0)
-            t0 = time.perf_counter()
-            s.init(x=np.zeros(n), b=b, dirbc=(dn, dv), apply=True, pc=pc)
-            build_s = time.perf_counter() - t0  # factor (and network inference) built here
-        best = None
-        for rep in range(reps):
-            t0 = time.perf_counter()
-            s.init(x=np.zeros(n), b=b, dirbc=(dn, dv), apply=True, pc=pc)
-            if mixed:
-                s.solve_mixed(200, tol, inner_tol=1e-2, inner_maxit=maxit)
-            else:
-                s.solve(maxit, tol)
-            x = s.solution()
-            t1 = time.perf_counter()
-            if best is None or t1 - t0 < best["s"]:
-                best = {"s": t1 - t0, "iterations": s.it(), "converged": s.converged(),
-                        "rel_residual": s.normr / s.normb}
-                if mixed:
-                    best["replacements"] = s.outer
-        if pc == "factor":
-            best["factor_build_s"] = build_s
-        out[name] = best
+            d.cg.set_factor(None if mdl == "none" else mdl, 1.0)
+        d.set_state(u0)
+        init_it = d.init()
+        d.run(warm)
+        t0 = time.perf_counter()
+        dts, its, ms, _ = d.run(steps)
+        wall = time.perf_counter() - t0
+        u, pr, t = d.state()
+        fields[name] = (u, pr)
+        out[name] = {"s_per_step": wall / steps, "device_ms_per_step": ms / steps,
+                     "pressure_iterations": [int(i) for i in its], "init_iterations": init_it,
+                     "dt_last": float(dts[-1])}
+        ctx.close()
+    ref_u, ref_p = fields["fp64_jacobi"]
+    for name in ("mixed_first_order", "mixed_learned"):
+        u, pr = fields[name]
+        out[name]["u_rel_err_vs_fp64"] = float(np.linalg.norm(u - ref_u) / np.linalg.norm(ref_u))
+        out[name]["p_rel_err_vs_fp64"] = float(np.linalg.norm(pr - ref_p) /
+                                               max(np.linalg.norm(ref_p), 1e-300))
+    out["speedup_learned_mixed_vs_fp64_jacobi"] = (out["fp64_jacobi"]["s_per_step"] /
+                                                   out["mixed_learned"]["s_per_step"])
     model.close()
-    it = out["fp64_jacobi"]["iterations"]
-    out["fp64_jacobi"]["GBps_per_iteration"] = ((12 * ja.size + 96 * n) * it /
-                                                out["fp64_jacobi"]["s"]) / 1e9
-    out["speedup_mixed_learned_vs_fp64_jacobi"] = out["fp64_jacobi"]["s"] / out["mixed_learned"]["s"]
+    for s_ in systems:
+        s_.ctx.close()
+    tctx.close()
     return out
 
 
@@ -304,10 +288,12 @@ def run_gpu(args, rank, world):
     barrier(world)
     # e2e through the C ABI with host buffers
     e2e = e2e_run(r, U0, args.steps, world)
-    pcg = run_pcg(ctx, ops) if (rank == 0 and not args.no_pcg) else None
-    out = {"pcg": pcg, "n": n, "nedge": nedge, "ms": ms_plain, "ms_events": ms, "kt": kt, "clocks": ck.summary(),
-           "e2e_ms": e2e, "setup_s": t_setup, "dts": dts2, "dev_bytes": ctx.device_bytes()}
+    dev_bytes = ctx.device_bytes()
     ctx.close()
+    cho = run_chocg(n=args.n) if (rank == 0 and not args.no_pcg) else None
+    out = {"chocg": cho, "n": n, "nedge": nedge, "ms": ms_plain, "ms_events": ms, "kt": kt,
+           "clocks": ck.summary(), "e2e_ms": e2e, "setup_s": t_setup, "dts": dts2,
+           "dev_bytes": dev_bytes}
     return out
 
 
@@ -350,7 +336,7 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--no-pcg", action="store_true")
+    ap.add_argument("--no-pcg", action="store_true", help="skip the ChoCG leg")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -430,7 +416,7 @@ def main():
             "cpu_baseline": cpu,
             "setup_s": res["setup_s"], "device_bytes": res["dev_bytes"],
             "dt_first_last": [float(res["dts"][0]), float(res["dts"][-1])],
-            "chocg_pressure_solve": res["pcg"]}
+            "chocg": res["chocg"]}
     print(json.dumps(line))
 
 

@@ -220,6 +220,7 @@ typedef struct xg_chocg_params {
   int64_t pmaxit;     /* pressure solve: iteration limit */
   int pmixed;         /* nonzero: mixed-precision refinement (xg_cg_solve_mixed) */
   double pinner_tol;  /* its inner residual reduction per replacement */
+  int pguard;         /* FP64 breakdown guard, as xg_cg_set_guard (0: the reference's) */
 } xg_chocg_params;
 
 /* Upload the operators ChoCG builds once per mesh (ChoCG::feop/streamable/
@@ -348,6 +349,15 @@ int xg_cg_solve_mixed(xg_ctx* ctx, int64_t maxit, double tol, double inner_tol,
  * inits use the same Dirichlet node set and no xg_cg_set_factor intervenes
  * (call it again after changing the model's parameters). */
 int xg_cg_set_factor(xg_ctx* ctx, xg_lpc* model, double scale);
+
+/* Breakdown guard of the FP64 solver (no counterpart in the reference):
+ * guard 0 (the default) ends a solve when |(p,q)| < DBL_EPSILON, the
+ * reference's absolute test (ConjugateGradients.cpp:681-690), which stops
+ * well-posed solves early when the right-hand side is small (a pressure
+ * increment on a fine mesh); guard 1 stops only on underflow (|(p,q)| <
+ * DBL_MIN), as the mixed-precision solver does, so the relative tolerance is
+ * what ends the solve.  Applies from the next xg_cg_init. */
+int xg_cg_set_guard(xg_ctx* ctx, int guard);
 
 /* z = M^-1 r with the preconditioner of the last xg_cg_init (host vectors). */
 int xg_cg_precondition(xg_ctx* ctx, const double* r, double* z);

@@ -108,3 +108,24 @@ def test_mixed_precision_refinement():
     x = s.solution()
     res = b2 - oracle.csr_mult(ia, ja, a2, x)
     assert np.linalg.norm(res) < 1e-8 * np.linalg.norm(b2)
+
+
+def test_breakdown_guard_modes():
+    """A small right-hand side (ChoCG's pressure increments on fine meshes):
+    with the reference's absolute (p,q) test the FP64 solve stops short of the
+    tolerance exactly where the oracle does; with the underflow-only guard it
+    runs to the tolerance."""
+    m, ia, ja, a, dn, dv, b = _system(9)
+    b = b * 1e-9
+    dv = np.zeros_like(dv)
+    A = cg.ConjugateGradients(ctx(), ia, ja, a)
+    aa, bb = oracle.csr_dirichlet(ia, ja, a, b, dn, dv)
+    _, ito, _, _, conv_o = oracle.pcg(ia, ja, aa, bb, np.zeros(ia.size - 1), 5000, 1e-10)
+    A.init(x=np.zeros(A.n), b=b, dirbc=(dn, dv), apply=True, pc="jacobi")
+    A.solve(5000, 1e-10)
+    assert not conv_o and not A.converged() and abs(A.it() - ito) <= 1
+    A.set_guard("underflow")
+    A.init(x=np.zeros(A.n), b=b, dirbc=(dn, dv), apply=True, pc="jacobi")
+    A.solve(5000, 1e-10)
+    assert A.converged() and A.normr < 1e-10 * A.normb
+    A.set_guard("reference")

@@ -87,6 +87,12 @@ class ConjugateGradients:
         h = None if model is None else model.h
         self.ctx.check(self.lib.xg_cg_set_factor(self.ctx.h, h, float(scale)))
 
+    def set_guard(self, guard="reference"):
+        """(p,q) breakdown test of the FP64 solver: "reference" (absolute
+        epsilon, ConjugateGradients.cpp:681-690) or "underflow"."""
+        self.ctx.check(self.lib.xg_cg_set_guard(self.ctx.h,
+                                                {"reference": 0, "underflow": 1}[guard]))
+
     def precondition(self, r):
         """z = M^-1 r with the preconditioner of the last init."""
         r = f64(r)

@@ -116,9 +116,11 @@ def operators(mesh, sym_sets=(), noslip_sets=(), dir_bcs=(), pdir_bcs=(), hydros
 class ChoCG:
     def __init__(self, ctx: Context, ops, mu=0.0, cfl=0.5, const_dt=0.0, flux="damp2",
                  stab=True, stab2=False, stab2coef=0.2, rk=1, pc="jacobi", ptol=1e-3,
-                 pmaxit=10, mixed=False, inner_tol=1e-2, matrix=True):
+                 pmaxit=10, mixed=False, inner_tol=1e-2, guard="reference", matrix=True):
         """ops: :func:`operators` output.  The pressure matrix goes to the
-        context's CG system unless matrix is False (already set up)."""
+        context's CG system unless matrix is False (already set up).  guard:
+        "reference" keeps the reference's absolute (p,q) breakdown test,
+        "underflow" lets the FP64 solve run to its relative tolerance."""
         from . import cg as _cg
 
         self.ctx = ctx
@@ -128,7 +130,8 @@ class ChoCG:
         if matrix:
             self.cg = _cg.ConjugateGradients(ctx, *ops["matrix"])
         prm = ChocgParams(mu, cfl, const_dt, FLUX[flux], int(stab), int(stab2), stab2coef, rk,
-                          PC[pc], ptol, pmaxit, int(mixed), inner_tol)
+                          PC[pc], ptol, pmaxit, int(mixed), inner_tol,
+                          {"reference": 0, "underflow": 1}[guard])
         self.prm = prm
         e = u64(ops["edges"]).reshape(-1)
         dd = f64(ops["dint"]).reshape(-1)

@@ -63,6 +63,7 @@ struct CGScalars {
   double pad0;
   int64_t it, maxit;
   int32_t done, finished, converged, pc;
+  int32_t guard, pad1;  // 0: |(p,q)| < DBL_EPSILON ends the solve; 1: underflow only
   unsigned int ticket[4];
 };
 }  // namespace
@@ -107,6 +108,7 @@ struct CGDev {
   bool geom_set = false;
   bool factor_set = false;
   uint64_t bc_key = 0;  // hash of the Dirichlet mask the geometry was built for
+  int guard = 0;        // breakdown guard of the FP64 solver (xg_cg_set_guard)
   xg_lpc* factor_model = nullptr;  // network emitting N, or null: N = factor_c * e
   double factor_c = 1.0;
 };
@@ -391,8 +393,9 @@ __global__ void __launch_bounds__(kBlock) k_cg_a(int64_t n, const int32_t* __res
       sc->rho0 = sc->rho;
       sc->pq = pq;
       // the reference's breakdown guard is an absolute epsilon
-      // (ConjugateGradients.cpp:681-690); the FP32 solver guards underflow only
-      const double eps = sizeof(T) == 8 ? DBL_EPSILON : DBL_MIN;
+      // (ConjugateGradients.cpp:681-690); the FP32 solver, and the FP64 one
+      // with guard 1, guard underflow only
+      const double eps = (sizeof(T) == 8 && sc->guard == 0) ? DBL_EPSILON : DBL_MIN;
       if (fabs(pq) < eps) {
         sc->finished = 1;
         sc->alpha = 0.0;
@@ -889,6 +892,7 @@ int cg_init_device(xg_ctx* c, const double* b_dev, int zero_values, int pc) {
   XG_CHECK_LAUNCH(c);
   CGScalars h{};
   h.pc = pc;
+  h.guard = d->guard;
   XG_CUDA(c, cudaMemcpyAsync(d->scal, &h, sizeof(h), cudaMemcpyHostToDevice, s));
   k_setup<<<pgrid<k_setup>(n), kBlock, 0, s>>>(n, d->soff, d->swidth, d->col, d->a, d->diagpos,
                                                d->x, d->b, d->r, d->d, d->z, d->p[0], d->d32,
@@ -1224,6 +1228,7 @@ int xg_cg_init(xg_ctx* c, const double* x, const double* b, const double* neubc,
   d->bc_key = key;
   CGScalars h{};
   h.pc = pc;
+  h.guard = d->guard;
   XG_CUDA(c, cudaMemcpyAsync(d->scal, &h, sizeof(h), cudaMemcpyHostToDevice, s));
   k_setup<<<pgrid<k_setup>(n), kBlock, 0, s>>>(n, d->soff, d->swidth, d->col, d->a, d->diagpos,
                                                d->x, d->b, d->r, d->d, d->z, d->p[0], d->d32,
@@ -1335,6 +1340,16 @@ int xg_cg_set_factor(xg_ctx* c, xg_lpc* model, double scale) {
   d->factor_model = model;
   d->factor_c = scale;
   d->factor_set = false;
+  return XG_OK;
+}
+
+int xg_cg_set_guard(xg_ctx* c, int guard) {
+  int rc = use(c);
+  if (rc) return rc;
+  CGDev* d = c->cg;
+  if (!d) return fail(c, XG_ERR_STATE, "cg_set_guard before cg_setup");
+  if (guard != 0 && guard != 1) return fail(c, XG_ERR_ARG, "cg_set_guard: guard is 0 or 1");
+  d->guard = guard;
   return XG_OK;
 }
 

@@ -610,7 +610,9 @@ int launch_rhs(xg_ctx* c, ChoCGDev* d, const double* U, double dtk, int stage0, 
 // that stops short of the tolerance (iteration limit or the (p,q) breakdown
 // guard) does not stop the scheme: last_it is then the negated count.
 int pressure_solve(xg_ctx* c, ChoCGDev* d, int zero_values) {
-  int rc = cg_init_device(c, d->div, zero_values, d->prm.ppc);
+  int rc = xg_cg_set_guard(c, d->prm.pguard);
+  if (rc) return rc;
+  rc = cg_init_device(c, d->div, zero_values, d->prm.ppc);
   if (rc) return rc;
   int64_t it = 0, outer = 0;
   double normr = 0, normb = 0;
@@ -671,6 +673,8 @@ int xg_chocg_setup(xg_ctx* c, const xg_chocg_params* prm, int64_t npoin, const d
     return fail(c, XG_ERR_ARG, "Flux not correctly configured");
   if (prm->rk < 1 || prm->rk > 4) return fail(c, XG_ERR_ARG, "chocg_setup: rk must be 1..4");
   if (prm->ppc < 0 || prm->ppc > 2) return fail(c, XG_ERR_ARG, "chocg_setup: unknown pressure pc");
+  if (prm->pguard != 0 && prm->pguard != 1)
+    return fail(c, XG_ERR_ARG, "chocg_setup: pressure guard is 0 or 1");
   if (prm->pmaxit <= 0 || !(prm->ptol >= 0))
     return fail(c, XG_ERR_ARG, "chocg_setup: bad pressure iteration limit or tolerance");
   if ((ntet && (!dsupedge0 || !dsupint0)) || (ntri && (!dsupedge1 || !dsupint1)) ||

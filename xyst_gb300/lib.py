@@ -44,7 +44,8 @@ class KozcgParams(C.Structure):
 class ChocgParams(C.Structure):
     _fields_ = [("mu", _dbl), ("cfl", _dbl), ("const_dt", _dbl), ("flux", _int), ("stab", _int),
                 ("stab2", _int), ("stab2coef", _dbl), ("rk", _int), ("ppc", _int),
-                ("ptol", _dbl), ("pmaxit", _i64), ("pmixed", _int), ("pinner_tol", _dbl)]
+                ("ptol", _dbl), ("pmaxit", _i64), ("pmixed", _int), ("pinner_tol", _dbl),
+                ("pguard", _int)]
 
 
 # name -> (restype, argtypes); every function of include/xg.h
@@ -98,6 +99,7 @@ SIGNATURES = {
     "xg_cg_solution": (_int, [_vp, _vp]),
     "xg_cg_set_factor": (_int, [_vp, _vp, _dbl]),
     "xg_cg_precondition": (_int, [_vp, _vp, _vp]),
+    "xg_cg_set_guard": (_int, [_vp, _int]),
     "xg_lpc_nparams": (_i64, []),
     "xg_lpc_create": (_int, [_vp, _int, C.POINTER(_vp)]),
     "xg_lpc_destroy": (_int, [_vp]),

@@ -143,6 +143,18 @@ def pressure_system(ctx: Context, n: int, seed: int, jitter: float = 0.2, dir_se
     return dict(mesh=m, ia=ia, ja=ja, a=a, dirnodes=dn, dirvals=np.zeros(dn.size), b=b)
 
 
+def chocg_system(ctx: Context, n: int, seed: int, jitter: float = 0.2):
+    """The pressure system ChoCG assembles for the Taylor-Green setup on an
+    n^3 jittered cube (symmetry on every face): the ChoCG::prelhs matrix with
+    the hydrostat node as its only Dirichlet row.  The trace loss reads the
+    matrix only; b is a random right-hand side for iteration counts."""
+    m = mesh.cube(n, jitter=jitter, seed=seed, numbering="rcm", perm_seed=seed + 7)
+    ia, ja, a = cg.pressure_matrix(m["coord"], m["inpoel"])
+    rng = np.random.default_rng(seed + 1000)
+    b = rng.standard_normal(ia.size - 1) * np.abs(a).max() * 1e2
+    return dict(mesh=m, ia=ia, ja=ja, a=a, dirnodes=np.array([0]), dirvals=np.zeros(1), b=b)
+
+
 def training_system(ctx: Context, sysd):
     """A ConjugateGradients holding sysd with its Dirichlet rows eliminated
     (what the trace loss reads), on a context of its own (a context holds
