@@ -18,7 +18,8 @@
 //
 // One PCG iteration (the reference's FP64 algorithm) is two kernels:
 //   k_cg_a: p' = z + beta p (beta = rho/rho0), q = A p', partial (p', q)
-//   k_cg_b: alpha = rho/(p,q); r -= alpha q; x += alpha p'; z = r/d (Jacobi);
+//   k_cg_b: alpha = rho/(p,q); r -= alpha q; x += alpha p'; z = r/d (Jacobi,
+//           as r times the stored inverse diagonal);
 //           partial (r,z), (r,r); convergence test
 // plus, for the factored preconditioner (pc 2, no reference counterpart),
 // z = -S (I+N)(I+N)^T S r in two passes over the lower and upper triangles.
@@ -315,7 +316,7 @@ __global__ void k_copy_values(int64_t nent, const double* __restrict__ a0, doubl
 }
 
 // ConjugateGradients::setup + pc + initres (ConjugateGradients.cpp:105-319):
-// r = b - A x, d = diag(A) (Jacobi) or 1 (none, factor), z = r/d, p = r,
+// r = b - A x, d = 1/diag(A) (Jacobi) or 1 (none, factor), z = r d, p = r,
 // partials of (b,b) and (r,z).
 __global__ void __launch_bounds__(kBlock) k_setup(int64_t n, const int32_t* __restrict__ soff,
                                                    const int32_t* __restrict__ sw,
@@ -335,11 +336,13 @@ __global__ void __launch_bounds__(kBlock) k_setup(int64_t n, const int32_t* __re
     const double s = sell_row<4, double>(Cols32{col}, a, soff[i >> 5], sw[i >> 5], lane,
                                          int32_t(i), [&](int32_t c) { return x[c]; });
     const double ri = b[i] - s;
-    const double di = pc == 1 ? a[diagpos[i]] : 1.0;
+    // the inverse Jacobi diagonal: one multiply per row and iteration in
+    // place of an FP64 division (the slow FP64 pipe of this GPU)
+    const double di = pc == 1 ? 1.0 / a[diagpos[i]] : 1.0;
     r[i] = ri;
     d[i] = di;
     d32[i] = float(di);
-    const double zi = ri / di;
+    const double zi = ri * di;
     z[i] = zi;
     p[i] = ri;
     v[0] += b[i] * b[i];
@@ -408,7 +411,8 @@ __global__ void __launch_bounds__(kBlock) k_cg_a(int64_t n, const int32_t* __res
 }
 
 // pq + rz + x (ConjugateGradients.cpp:671-823), fused: r -= alpha q,
-// x += alpha p'; Jacobi z = r / d and rho = (r, z), or (FACTOR) v = S r for
+// x += alpha p'; Jacobi z = r d (d the inverse diagonal), rho = (r, z), or
+// (FACTOR) v = S r for
 // the factor passes that follow; (r, r) and the stopping test:
 //   FP64: ||r|| < tol ||b||, or maxit iterations (the reference's test);
 //   MIXED: ||r|| < max(tol ||b||, delta * rlast) asks for a residual
@@ -432,7 +436,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_b(int64_t n, const T* __restrict_
     if (FACTOR) {
       vs[i] = T(srow[i]) * ri;
     } else {
-      const T zi = ri / d[i];
+      const T zi = ri * d[i];
       z[i] = zi;
       v[0] += double(ri) * double(zi);
     }
@@ -520,7 +524,7 @@ __global__ void k_scale(int64_t n, const float* __restrict__ srow, const T* __re
 
 // ---- mixed precision: residual replacement
 
-// r = b - A x in FP64 (true residual), r32 = r; Jacobi: z32 = r32 / d32 and
+// r = b - A x in FP64 (true residual), r32 = r; Jacobi: z32 = r32 d32 and
 // rho = (r32, z32); factor (srow given): v32 = S r32.  Partial (r,r) -> rr.
 // FIRST starts the FP32 iteration (it = 0, so beta = 0); otherwise it
 // continues with the kept search direction.
@@ -547,7 +551,7 @@ __global__ void __launch_bounds__(kBlock) k_outer_res(int64_t n, const int32_t* 
     if (srow) {
       v32[i] = srow[i] * rf;
     } else {
-      const float zf = rf / d32[i];
+      const float zf = rf * d32[i];
       z32[i] = zf;
       v[1] += double(rf) * double(zf);
     }
@@ -579,7 +583,7 @@ __global__ void k_add_correction(int64_t n, float* __restrict__ e, double* __res
 __global__ void k_jacobi_apply(int64_t n, const double* __restrict__ r, const double* __restrict__ d,
                                double* __restrict__ z) {
   int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  if (i < n) z[i] = r[i] / d[i];
+  if (i < n) z[i] = r[i] * d[i];
 }
 
 // ---- factor construction
