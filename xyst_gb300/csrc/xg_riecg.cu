@@ -81,10 +81,10 @@ struct RieCGDev {
   double* ivol = nullptr;
   float* cbrtv = nullptr;
   // boundary triangles, per boundary node lists of (tri << 2 | position)
-  int32_t *bptr = nullptr, *bent = nullptr, *btri = nullptr, *bnode = nullptr;
+  int32_t *bptr = nullptr, *bnode = nullptr;
+  int4* bent4 = nullptr;  // per boundary entry: the triangle's 3 nodes, pos | sym flags << 2
   void* Rb = nullptr;  // F [5][nbn] domain residual of the boundary nodes
-  uint8_t* bsym = nullptr;
-  uint8_t* bcflag = nullptr;  // per boundary node: has a nodal BC
+  int32_t* bcof = nullptr;  // per boundary node: its BC program entry or -1
   // BC program: one thread per BC node
   int64_t nbc = 0;
   int32_t *bcnode = nullptr, *bcdir = nullptr, *bcsymp = nullptr, *bcfar = nullptr,
@@ -586,11 +586,10 @@ struct Adj {
 };
 struct Bnd {
   const int32_t* bnode;  // node of each boundary index
-  const int32_t* bidx;
-  const int32_t* bptr;
-  const int32_t* bent;
-  const int32_t* btri;
-  const uint8_t* bsym;
+  const int32_t* bidx;   // boundary index of each node, or -1
+  const int32_t* bptr;   // per boundary node: its range of entries
+  const int4* bent4;     // per entry: triangle nodes N0, N1, N2 and
+                         // pos | symN0 << 2 | symN1 << 3 | symN2 << 4
 };
 // Per-node factors of the FP32-mode epilogue: 1/vol and cbrt(vol).
 struct NodeAux {
@@ -729,13 +728,11 @@ template <class F>
 __device__ __forceinline__ void grad_bnd_term(const Bnd& bnd, int32_t bi, const F* __restrict__ W,
                                               F g[15]) {
   for (int32_t j = __ldg(bnd.bptr + bi); j < __ldg(bnd.bptr + bi + 1); ++j) {
-    const int32_t t = __ldg(bnd.bent + j) >> 2;
-    const int32_t N0 = __ldg(bnd.btri + 3 * t), N1 = __ldg(bnd.btri + 3 * t + 1),
-                  N2 = __ldg(bnd.btri + 3 * t + 2);
+    const int4 te = __ldg(bnd.bent4 + j);
     F a[8], b[8], c[8];
-    load8(W + int64_t(N0) * 8, a);
-    load8(W + int64_t(N1) * 8, b);
-    load8(W + int64_t(N2) * 8, c);
+    load8(W + int64_t(te.x) * 8, a);
+    load8(W + int64_t(te.y) * 8, b);
+    load8(W + int64_t(te.z) * 8, c);
     F bax = b[5] - a[5], bay = b[6] - a[6], baz = b[7] - a[7];
     F cax = c[5] - a[5], cay = c[6] - a[6], caz = c[7] - a[7];
     F nn[3] = {(bay * caz - cay * baz) / F(12.0), (baz * cax - caz * bax) / F(12.0),
@@ -879,15 +876,13 @@ template <class F>
 __device__ __forceinline__ void rhs_bnd_term(const Bnd& bnd, int32_t bi, const F* __restrict__ W,
                                              F gamma, F R[5]) {
   for (int32_t j = __ldg(bnd.bptr + bi); j < __ldg(bnd.bptr + bi + 1); ++j) {
-    const int32_t ent = __ldg(bnd.bent + j);
-    const int32_t t = ent >> 2, pos = ent & 3;
+    const int4 te = __ldg(bnd.bent4 + j);
+    const int32_t pos = te.w & 3;
     F x[3][8];
-    uint8_t sy[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      load8(W + int64_t(__ldg(bnd.btri + 3 * t + a)) * 8, x[a]);
-      sy[a] = __ldg(bnd.bsym + 3 * t + a);
-    }
+    load8(W + int64_t(te.x) * 8, x[0]);
+    load8(W + int64_t(te.y) * 8, x[1]);
+    load8(W + int64_t(te.z) * 8, x[2]);
+    const bool sy[3] = {((te.w >> 2) & 1) != 0, ((te.w >> 3) & 1) != 0, ((te.w >> 4) & 1) != 0};
     F bax = x[1][5] - x[0][5], bay = x[1][6] - x[0][6], baz = x[1][7] - x[0][7];
     F cax = x[2][5] - x[0][5], cay = x[2][6] - x[0][6], caz = x[2][7] - x[0][7];
     F nx = (bay * caz - cay * baz) / F(12.0);
@@ -916,50 +911,128 @@ __device__ __forceinline__ void rhs_bnd_term(const Bnd& bnd, int32_t bi, const F
   }
 }
 
-// One node's stage update (RieCG::solve, src/Inciter/RieCG.cpp:1010-1021):
-// U = Un - rkcoef*dt*R/vol from uo (U at stage 0, Un after), the new
-// primitive record and, on the last stage when want_dt, the node's CFL time
-// step (src/Inciter/RieCG.cpp:827-839); DBL_MAX otherwise.
+// Nodal BC program, one entry per BC node, applied in the reference order:
+// Dirichlet, symmetry (one projection per symmetry set containing the node),
+// farfield, pressure (physics::dirbc/symbc/farbc/prebc,
+// src/Physics/BC.cpp:29-241).
+struct BCProg {
+  int64_t nbc;
+  const int32_t* node;
+  const int32_t* dir;
+  const int32_t* symp;
+  const int32_t* far;
+  const int32_t* pre;
+  const int32_t* dirmask;
+  const double* dirval;
+  const double* symn;
+  const double* farn;
+  const double* preval;
+  double far5[5];
+};
+
+// BC program entry i applied to the conserved state u of its node.
+__device__ __forceinline__ void apply_bc(const BCProg& bc, int64_t i, double gamma,
+                                         double u[5]) {
+  const int32_t d = bc.dir[i];
+  if (d >= 0) {
+#pragma unroll
+    for (int c = 0; c < 5; ++c)
+      if (bc.dirmask[d * 5 + c]) u[c] = bc.dirval[d * 5 + c];
+  }
+  for (int32_t k = bc.symp[i]; k < bc.symp[i + 1]; ++k) {
+    const double* nn = bc.symn + 3 * k;
+    double vn = u[1] * nn[0] + u[2] * nn[1] + u[3] * nn[2];
+    u[1] -= vn * nn[0];
+    u[2] -= vn * nn[1];
+    u[3] -= vn * nn[2];
+  }
+  const int32_t f = bc.far[i];
+  if (f >= 0) {
+    const double* nn = bc.farn + 3 * f;
+    const double fr = bc.far5[0], fu = bc.far5[1], fv = bc.far5[2], fw = bc.far5[3],
+                 fp = bc.far5[4];
+    double vn = fu * nn[0] + fv * nn[1] + fw * nn[2];
+    double a = sqrt(gamma * fp / fr);
+    double M = vn / a;
+    if (M <= -1.0) {
+      u[0] = fr;
+      u[1] = fr * fu;
+      u[2] = fr * fv;
+      u[3] = fr * fw;
+      u[4] = fp / (gamma - 1.0) + 0.5 * fr * (fu * fu + fv * fv + fw * fw);
+    } else if (M > -1.0 && M < 0.0) {
+      double pr = (u[4] - 0.5 * (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) / u[0]) *
+                  (gamma - 1.0);
+      u[0] = fr;
+      u[1] = fr * fu;
+      u[2] = fr * fv;
+      u[3] = fr * fw;
+      u[4] = pr / (gamma - 1.0) + 0.5 * fr * (fu * fu + fv * fv + fw * fw);
+    } else if (M >= 0.0 && M < 1.0) {
+      double r = u[0], uu = u[1] / r, vv = u[2] / r, ww = u[3] / r;
+      u[4] = fp / (gamma - 1.0) + 0.5 * r * (uu * uu + vv * vv + ww * ww);
+    }
+  }
+  const int32_t pr = bc.pre[i];
+  if (pr >= 0) {
+    u[0] = bc.preval[pr * 2 + 0];
+    double r = u[0], uu = u[1] / r, vv = u[2] / r, ww = u[3] / r;
+    u[4] = bc.preval[pr * 2 + 1] / (gamma - 1.0) + 0.5 * r * (uu * uu + vv * vv + ww * ww);
+  }
+}
+
+// One node's stage state (RieCG::solve, src/Inciter/RieCG.cpp:1010-1021):
+// un = Un - rkcoef*dt*R/vol from uo (U at stage 0, copied to Un, and Un
+// after).  The FP64 mode keeps the reference's expression; FP32 mode uses
+// 1/vol (no FP64 division per node).
 template <class F, int STAGE>
-__device__ __forceinline__ double update_node(int64_t n, int64_t p, const F R[5],
-                                              const double uo[5], const F wp[8], bool want_dt,
-                                              const double* __restrict__ vol, NodeAux aux,
-                                              double gamma_d, double dt, double* U, double* Un,
-                                              F* __restrict__ Wout) {
+__device__ __forceinline__ void stage_state(int64_t n, int64_t p, const F R[5],
+                                            const double uo[5],
+                                            const double* __restrict__ vol, NodeAux aux,
+                                            double dt, double* Un, double un[5]) {
   constexpr double rk = STAGE == 0 ? 1.0 / 3.0 : (STAGE == 1 ? 0.5 : 1.0);
-  double dtp = DBL_MAX;
-  double un[5];
   if constexpr (sizeof(F) == 8) {
-    // FP64: the reference's expression, Un - rkcoef*dt*R/vol
     const double v = vol[p];
 #pragma unroll
     for (int c = 0; c < 5; ++c) {
       if (STAGE == 0) Un[c * n + p] = uo[c];
       un[c] = uo[c] - rk * dt * double(R[c]) / v;
-      U[c * n + p] = un[c];
     }
-    double pw[5];
-    prim5(un, pw);
-    F o[8] = {F(pw[0]), F(pw[1]), F(pw[2]), F(pw[3]), F(pw[4]), wp[5], wp[6], wp[7]};
-    store8(Wout + p * 8, o);
-    if (STAGE == 2 && want_dt) dtp = node_dt(un, v, gamma_d);
   } else {
-    // FP32 fluxes: the FP64 state update uses 1/vol; primitives and the
-    // CFL estimate are formed in FP32 (no FP64 division per node)
     const double cf = rk * dt * aux.ivol[p];
 #pragma unroll
     for (int c = 0; c < 5; ++c) {
       if (STAGE == 0) Un[c * n + p] = uo[c];
       un[c] = uo[c] - cf * double(R[c]);
-      U[c * n + p] = un[c];
     }
-    const float r = float(un[0]);
+  }
+}
+
+// Store a node's new state u: U, its primitive record (coordinates from wp)
+// and, when want_dt, its CFL time step (src/Inciter/RieCG.cpp:827-839, the
+// FP32 estimate in FP32 mode); DBL_MAX otherwise.
+template <class F>
+__device__ __forceinline__ double store_node(int64_t n, int64_t p, const double u[5],
+                                             const F wp[8], bool want_dt,
+                                             const double* __restrict__ vol, NodeAux aux,
+                                             double gamma_d, double* U, F* __restrict__ Wout) {
+  double dtp = DBL_MAX;
+#pragma unroll
+  for (int c = 0; c < 5; ++c) U[c * n + p] = u[c];
+  if constexpr (sizeof(F) == 8) {
+    double pw[5];
+    prim5(u, pw);
+    F o[8] = {F(pw[0]), F(pw[1]), F(pw[2]), F(pw[3]), F(pw[4]), wp[5], wp[6], wp[7]};
+    store8(Wout + p * 8, o);
+    if (want_dt) dtp = node_dt(u, vol[p], gamma_d);
+  } else {
+    const float r = float(u[0]);
     const float ir = __frcp_rn(r);
-    const float uu = float(un[1]) * ir, vv = float(un[2]) * ir, ww = float(un[3]) * ir;
-    const float ie = float(un[4]) * ir - 0.5f * (uu * uu + vv * vv + ww * ww);
+    const float uu = float(u[1]) * ir, vv = float(u[2]) * ir, ww = float(u[3]) * ir;
+    const float ie = float(u[4]) * ir - 0.5f * (uu * uu + vv * vv + ww * ww);
     F o[8] = {r, uu, vv, ww, ie, wp[5], wp[6], wp[7]};
     store8(Wout + p * 8, o);
-    if (STAGE == 2 && want_dt) dtp = double(node_dt_f(un, aux.cbrtv[p], float(gamma_d)));
+    if (want_dt) dtp = double(node_dt_f(u, aux.cbrtv[p], float(gamma_d)));
   }
   return dtp;
 }
@@ -1023,21 +1096,23 @@ __global__ void __launch_bounds__(kBlock, sizeof(F) == 4 ? 4 : 1)
 #pragma unroll
       for (int c = 0; c < 5; ++c) Rout[p * 5 + c] = double(R[c]);
     } else {
-      dtp = update_node<F, STAGE>(n, p, R, uo, wp, true, vol, aux, gamma_d, scal->dt, U, Un,
-                                  Wout);
+      double un[5];
+      stage_state<F, STAGE>(n, p, R, uo, vol, aux, scal->dt, Un, un);
+      dtp = store_node<F>(n, p, un, wp, STAGE == 2, vol, aux, gamma_d, U, Wout);
     }
   }
   if (UPDATE && STAGE == 2) block_min_atomic(dtp, dtmin);
 }
 
 // Boundary nodes of pass 2, one thread per boundary node: the boundary
-// integral after the domain residual (the reference's order), then the same
-// update; the CFL minimum skips nodes with a nodal BC (the BC kernel covers
-// those after modifying them).
+// integral after the domain residual (the reference's order), the stage
+// update, then the node's nodal BCs (RieCG::BC after RieCG::solve's update,
+// src/Inciter/RieCG.cpp:1010-1030; every BC node lies on a boundary
+// triangle) and, on the last stage, the CFL time step of the final state.
 template <class F, int STAGE, bool UPDATE>
 __global__ void __launch_bounds__(kBlock)
     k_rhs_bnd(int64_t n, int64_t nbn, Bnd bnd, const F* __restrict__ Rb,
-              const F* __restrict__ W, const uint8_t* __restrict__ bcflag,
+              const F* __restrict__ W, const int32_t* __restrict__ bcof, BCProg bc,
               const double* __restrict__ vol, NodeAux aux, double gamma_d,
               const Scalars* __restrict__ scal, double* U, double* Un, F* __restrict__ Wout,
               double* __restrict__ Rout, unsigned long long* dtmin) {
@@ -1055,37 +1130,23 @@ __global__ void __launch_bounds__(kBlock)
     }
     F wp[8];
     load8(W + p * 8, wp);
+    const int32_t b = UPDATE ? __ldg(bcof + i) : -1;
     rhs_bnd_term(bnd, static_cast<int32_t>(i), W, F(gamma_d), R);
     if (!UPDATE) {
 #pragma unroll
       for (int c = 0; c < 5; ++c) Rout[p * 5 + c] = double(R[c]);
     } else {
-      dtp = update_node<F, STAGE>(n, p, R, uo, wp, bcflag[i] == 0, vol, aux, gamma_d, scal->dt,
-                                  U, Un, Wout);
+      double un[5];
+      stage_state<F, STAGE>(n, p, R, uo, vol, aux, scal->dt, Un, un);
+      if (b >= 0) apply_bc(bc, b, gamma_d, un);
+      dtp = store_node<F>(n, p, un, wp, STAGE == 2, vol, aux, gamma_d, U, Wout);
     }
   }
   if (UPDATE && STAGE == 2) block_min_atomic(dtp, dtmin);
 }
 
-// Nodal BCs, one thread per BC node, in the reference order: Dirichlet,
-// symmetry (one projection per symmetry set containing the node), farfield,
-// pressure (physics::dirbc/symbc/farbc/prebc, src/Physics/BC.cpp:29-241).
-// Refreshes the node's primitive record and, when asked, its CFL dt.
-struct BCProg {
-  int64_t nbc;
-  const int32_t* node;
-  const int32_t* dir;
-  const int32_t* symp;
-  const int32_t* far;
-  const int32_t* pre;
-  const int32_t* dirmask;
-  const double* dirval;
-  const double* symn;
-  const double* farn;
-  const double* preval;
-  double far5[5];
-};
-
+// Nodal BCs on the device state (RieCG::BC), one thread per BC node; refreshes
+// the node's primitive record and, when asked, its CFL dt.
 template <class F>
 __global__ void __launch_bounds__(kBlock) k_bc(int64_t n, BCProg bc, double gamma, double* U,
                                                 F* __restrict__ W, const double* __restrict__ vol,
@@ -1098,76 +1159,10 @@ __global__ void __launch_bounds__(kBlock) k_bc(int64_t n, BCProg bc, double gamm
     double u[5];
 #pragma unroll
     for (int c = 0; c < 5; ++c) u[c] = U[c * n + p];
-    const int32_t d = bc.dir[i];
-    if (d >= 0) {
-#pragma unroll
-      for (int c = 0; c < 5; ++c)
-        if (bc.dirmask[d * 5 + c]) u[c] = bc.dirval[d * 5 + c];
-    }
-    for (int32_t k = bc.symp[i]; k < bc.symp[i + 1]; ++k) {
-      const double* nn = bc.symn + 3 * k;
-      double vn = u[1] * nn[0] + u[2] * nn[1] + u[3] * nn[2];
-      u[1] -= vn * nn[0];
-      u[2] -= vn * nn[1];
-      u[3] -= vn * nn[2];
-    }
-    const int32_t f = bc.far[i];
-    if (f >= 0) {
-      const double* nn = bc.farn + 3 * f;
-      const double fr = bc.far5[0], fu = bc.far5[1], fv = bc.far5[2], fw = bc.far5[3],
-                   fp = bc.far5[4];
-      double vn = fu * nn[0] + fv * nn[1] + fw * nn[2];
-      double a = sqrt(gamma * fp / fr);
-      double M = vn / a;
-      if (M <= -1.0) {
-        u[0] = fr;
-        u[1] = fr * fu;
-        u[2] = fr * fv;
-        u[3] = fr * fw;
-        u[4] = fp / (gamma - 1.0) + 0.5 * fr * (fu * fu + fv * fv + fw * fw);
-      } else if (M > -1.0 && M < 0.0) {
-        double pr = (u[4] - 0.5 * (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) / u[0]) *
-                    (gamma - 1.0);
-        u[0] = fr;
-        u[1] = fr * fu;
-        u[2] = fr * fv;
-        u[3] = fr * fw;
-        u[4] = pr / (gamma - 1.0) + 0.5 * fr * (fu * fu + fv * fv + fw * fw);
-      } else if (M >= 0.0 && M < 1.0) {
-        double r = u[0], uu = u[1] / r, vv = u[2] / r, ww = u[3] / r;
-        u[4] = fp / (gamma - 1.0) + 0.5 * r * (uu * uu + vv * vv + ww * ww);
-      }
-    }
-    const int32_t pr = bc.pre[i];
-    if (pr >= 0) {
-      u[0] = bc.preval[pr * 2 + 0];
-      double r = u[0], uu = u[1] / r, vv = u[2] / r, ww = u[3] / r;
-      u[4] = bc.preval[pr * 2 + 1] / (gamma - 1.0) + 0.5 * r * (uu * uu + vv * vv + ww * ww);
-    }
-#pragma unroll
-    for (int c = 0; c < 5; ++c) U[c * n + p] = u[c];
+    apply_bc(bc, i, gamma, u);
     F o[8];
     load8(W + p * 8, o);
-    if constexpr (sizeof(F) == 8) {
-      double w[5];
-      prim5(u, w);
-#pragma unroll
-      for (int c = 0; c < 5; ++c) o[c] = w[c];
-      if (want_dt) dtp = node_dt(u, vol[p], gamma);
-    } else {
-      // FP32 mode: the primitive record and the CFL estimate as the fused
-      // update forms them (no FP64 division per node)
-      const float r = float(u[0]);
-      const float ir = __frcp_rn(r);
-      const float uu = float(u[1]) * ir, vv = float(u[2]) * ir, ww = float(u[3]) * ir;
-      o[0] = r;
-      o[1] = uu;
-      o[2] = vv;
-      o[3] = ww;
-      o[4] = float(u[4]) * ir - 0.5f * (uu * uu + vv * vv + ww * ww);
-      if (want_dt) dtp = double(node_dt_f(u, aux.cbrtv[p], float(gamma)));
-    }
-    store8(W + p * 8, o);
+    dtp = store_node<F>(n, p, u, o, want_dt != 0, vol, aux, gamma, U, W);
   }
   if (want_dt) block_min_atomic(dtp, dtmin);
 }
@@ -1281,7 +1276,7 @@ Adj<F> adj_of(RieCGDev* d) {
   return Adj<F>{d->soff, d->swidth, static_cast<const typename EntOf<F>::type*>(d->ent)};
 }
 NodeAux aux_of(RieCGDev* d) { return NodeAux{d->ivol, d->cbrtv}; }
-Bnd bnd_of(RieCGDev* d) { return Bnd{d->bnode, d->bidx, d->bptr, d->bent, d->btri, d->bsym}; }
+Bnd bnd_of(RieCGDev* d) { return Bnd{d->bnode, d->bidx, d->bptr, d->bent4}; }
 
 BCProg bcprog_of(RieCGDev* d) {
   BCProg b;
@@ -1336,9 +1331,9 @@ int launch_rhs_t(xg_ctx* c, RieCGDev* d, const F* W, const F* G, F* Wout, double
     XG_PROF_LAUNCH(c, d, "riecg_rhs_bnd",
                    (k_rhs_bnd<F, STAGE, UPDATE><<<blocks_for(d->nbn, kBlock), kBlock, 0,
                                                   c->stream>>>(
-                       d->n, d->nbn, bnd_of(d), static_cast<const F*>(d->Rb), W, d->bcflag,
-                       d->vol, aux_of(d), d->prm.gamma, d->scal, d->U, d->Un, Wout, Rout,
-                       &d->scal->dtmin)));
+                       d->n, d->nbn, bnd_of(d), static_cast<const F*>(d->Rb), W, d->bcof,
+                       bcprog_of(d), d->vol, aux_of(d), d->prm.gamma, d->scal, d->U, d->Un,
+                       Wout, Rout, &d->scal->dtmin)));
   return XG_OK;
 }
 
@@ -1377,9 +1372,9 @@ int do_stage(xg_ctx* c, RieCGDev* d, int stage) {
   F* G = static_cast<F*>(d->G);
   int rc = launch_grad<F>(c, d, Win, G, 1);
   if (rc) return rc;
+  // the residual pass updates every node and applies the nodal BCs of the
+  // boundary nodes (all BC nodes) after their update
   rc = launch_rhs<F>(c, d, stage, true, Win, G, Wout, nullptr);
-  if (rc) return rc;
-  rc = launch_bc<F>(c, d, Wout, stage == 2);
   if (rc) return rc;
   d->cur ^= 1;
   return XG_OK;
@@ -1401,8 +1396,7 @@ int alloc_and_upload(xg_ctx* c, RieCGDev* d, const double* coord, const double* 
                      const std::vector<int32_t>& nbr, const std::vector<double>& ddx,
                      const std::vector<double>& ddy, const std::vector<double>& ddz,
                      const std::vector<int32_t>& bidx, const std::vector<int32_t>& bptr,
-                     const std::vector<int32_t>& bent, const std::vector<int32_t>& btri,
-                     const std::vector<uint8_t>& bsym, const HalfLists& hl) {
+                     const std::vector<int4>& bent4, const HalfLists& hl) {
   const int64_t n = d->n;
   using EntT = typename EntOf<F>::type;
   F *W0, *W1, *G, *fbuf, *Rp, *Rb;
@@ -1430,10 +1424,8 @@ int alloc_and_upload(xg_ctx* c, RieCGDev* d, const double* coord, const double* 
     A.plan(d->ivol, n);
     A.plan(d->cbrtv, n);
     A.plan(d->bptr, bptr.size());
-    A.plan(d->bent, std::max<size_t>(1, bent.size()));
-    A.plan(d->btri, std::max<size_t>(1, btri.size()));
-    A.plan(d->bsym, std::max<size_t>(1, bsym.size()));
-    A.plan(d->bcflag, std::max<int64_t>(1, d->nbn));
+    A.plan(d->bent4, std::max<size_t>(1, bent4.size()));
+    A.plan(d->bcof, std::max<int64_t>(1, d->nbn));
     A.plan(d->bnode, std::max<int64_t>(1, d->nbn));
     A.plan(Rb, std::max<int64_t>(1, d->nbn) * 5);
     A.plan(d->scal, 1);
@@ -1529,10 +1521,8 @@ int alloc_and_upload(xg_ctx* c, RieCGDev* d, const double* coord, const double* 
     if (bidx[p] >= 0) bnode[bidx[p]] = static_cast<int32_t>(p);
   XG_CUDA(c, cudaMemcpy(d->bnode, bnode.data(), bnode.size() * 4, cudaMemcpyHostToDevice));
   XG_CUDA(c, up(d->bptr, bptr.data(), bptr.size() * 4));
-  XG_CUDA(c, up(d->bent, bent.data(), bent.size() * 4));
-  XG_CUDA(c, up(d->btri, btri.data(), btri.size() * 4));
-  XG_CUDA(c, up(d->bsym, bsym.data(), bsym.size()));
-  XG_CUDA(c, cudaMemsetAsync(d->bcflag, 0, std::max<int64_t>(1, d->nbn), s));
+  XG_CUDA(c, up(d->bent4, bent4.data(), bent4.size() * sizeof(int4)));
+  XG_CUDA(c, cudaMemsetAsync(d->bcof, 0xff, std::max<int64_t>(1, d->nbn) * 4, s));  // -1
   XG_CUDA(c, cudaMemsetAsync(d->U, 0, n * 5 * sizeof(double), s));
   XG_CUDA(c, cudaMemsetAsync(d->Un, 0, n * 5 * sizeof(double), s));
   XG_CUDA(c, cudaMemsetAsync(G, 0, n * 16 * sizeof(F), s));
@@ -1757,14 +1747,17 @@ int xg_riecg_setup(xg_ctx* c, const xg_riecg_params* prm, int64_t npoin, const d
       }
       ++bcount[bidx[p]];
     }
-  std::vector<int32_t> bptr(nbn + 1, 0), bent(nbtri * 3);
+  std::vector<int32_t> bptr(nbn + 1, 0);
+  std::vector<int4> bent4(nbtri * 3);
   for (int64_t i = 0; i < nbn; ++i) bptr[i + 1] = bptr[i] + static_cast<int32_t>(bcount[i]);
   {
     std::vector<int32_t> fill(bptr.begin(), bptr.end() - 1);
     for (int64_t t = 0; t < nbtri; ++t)
       for (int a = 0; a < 3; ++a) {
         int32_t bi = bidx[triinpoel[t * 3 + a]];
-        bent[fill[bi]++] = static_cast<int32_t>(t * 4 + a);
+        const int32_t flags = a | (bsym[t * 3] << 2) | (bsym[t * 3 + 1] << 3) |
+                              (bsym[t * 3 + 2] << 4);
+        bent4[fill[bi]++] = make_int4(btri[t * 3], btri[t * 3 + 1], btri[t * 3 + 2], flags);
       }
   }
   // (re)create the device state
@@ -1785,10 +1778,10 @@ int xg_riecg_setup(xg_ctx* c, const xg_riecg_params* prm, int64_t npoin, const d
   d->nbent = nbtri * 3;
   if (d->fp32)
     rc = alloc_and_upload<float>(c, d, coord, vol, soff, swidth, nbr, ddx, ddy, ddz, bidx, bptr,
-                                 bent, btri, bsym, hl);
+                                 bent4, hl);
   else
     rc = alloc_and_upload<double>(c, d, coord, vol, soff, swidth, nbr, ddx, ddy, ddz, bidx, bptr,
-                                  bent, btri, bsym, hl);
+                                  bent4, hl);
   if (rc) {
     destroy_riecg(d);
     c->riecg = nullptr;
@@ -1847,15 +1840,15 @@ int xg_riecg_set_bc(xg_ctx* c, int64_t nsym, const uint64_t* symnodes, const dou
       for (int a = 0; a < 3; ++a) symn[j * 3 + a] = symnorms[k * 3 + a];
     }
   }
-  // per boundary node flag "has a nodal BC" (for the CFL reduction split)
+  // per boundary node: its BC program entry (the residual pass applies it)
   std::vector<int32_t> hbidx(n);
   XG_CUDA(c, cudaMemcpy(hbidx.data(), d->bidx, n * sizeof(int32_t), cudaMemcpyDeviceToHost));
-  std::vector<uint8_t> flag(std::max<int64_t>(1, d->nbn), 0);
+  std::vector<int32_t> bcof(std::max<int64_t>(1, d->nbn), -1);
   for (int64_t i = 0; i < nbc; ++i) {
     int32_t bi = hbidx[ids[i]];
     if (bi < 0)
       return fail(c, XG_ERR_ARG, "riecg_set_bc: BC node not on a boundary triangle");
-    flag[bi] = 1;
+    bcof[bi] = static_cast<int32_t>(i);
   }
   XG_CUDA(c, cudaStreamSynchronize(c->stream));
   d->bcarena.release();
@@ -1886,7 +1879,7 @@ int xg_riecg_set_bc(xg_ctx* c, int64_t nsym, const uint64_t* symnodes, const dou
   XG_CUDA(c, up(d->dirval, dirvals, ndir * 5 * 8));
   XG_CUDA(c, up(d->farn, farnorms, nfar * 3 * 8));
   XG_CUDA(c, up(d->preval, prevals, npre * 2 * 8));
-  XG_CUDA(c, up(d->bcflag, flag.data(), flag.size()));
+  XG_CUDA(c, up(d->bcof, bcof.data(), bcof.size() * 4));
   if (far5)
     for (int i = 0; i < 5; ++i) d->far5[i] = far5[i];
   d->nbc = nbc;
