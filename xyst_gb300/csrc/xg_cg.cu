@@ -410,6 +410,28 @@ __global__ void __launch_bounds__(kBlock) k_cg_a(int64_t n, const int32_t* __res
   }
 }
 
+// The end of an iteration, in the last block: (r,r), the count and the
+// stopping test (ConjugateGradients.cpp:772-823):
+//   FP64: ||r|| < tol ||b||, or maxit iterations (the reference's test);
+//   MIXED: ||r|| < max(tol ||b||, delta * rlast) asks for a residual
+//   replacement (rlast: the last true residual norm), as does maxit.
+template <bool MIXED>
+__device__ __forceinline__ void end_iteration(double rr, CGScalars* sc) {
+  sc->rr = rr;
+  sc->it += 1;
+  const double nr = sqrt(rr);
+  const double nb = sc->normb > 1.0e-14 ? sc->normb : 1.0;
+  if (MIXED) {
+    const double lim = fmax(sc->tol * nb, sc->delta * sc->rlast);
+    if (sc->finished || nr < lim || sc->it >= sc->maxit) sc->done = 1;
+  } else {
+    if (sc->finished || nr < sc->tol * nb || sc->it >= sc->maxit) {
+      sc->done = 1;
+      sc->converged = nr > sc->tol * nb ? 0 : 1;
+    }
+  }
+}
+
 // pq + rz + x (ConjugateGradients.cpp:671-823), fused: r -= alpha q,
 // x += alpha p'; Jacobi z = r d (d the inverse diagonal), rho = (r, z), or
 // (FACTOR) v = S r for
@@ -426,40 +448,36 @@ __global__ void __launch_bounds__(kBlock) k_cg_b(int64_t n, const T* __restrict_
                                                   double* partial, CGScalars* sc) {
   if (sc->done) return;
   const T alpha = T(sc->alpha);
-  // the p' of this iteration (k_cg_a wrote it; the count advances below)
+  // the p' of this iteration (k_cg_a wrote it; the count advances below, or
+  // at the end of the factor passes)
   const T* __restrict__ p = (sc->it & 1) ? p0 : p1;
+  if (FACTOR) {
+    // no reduction here: (r,z), (r,r) and the stopping test close the
+    // iteration in k_pc_lower
+    XG_ROWS(i, n) {
+      const T ri = r[i] - alpha * q[i];
+      r[i] = ri;
+      x[i] += alpha * p[i];
+      vs[i] = T(srow[i]) * ri;
+    }
+    return;
+  }
   double v[2] = {0.0, 0.0};
   XG_ROWS(i, n) {
     const T ri = r[i] - alpha * q[i];
     r[i] = ri;
     x[i] += alpha * p[i];
-    if (FACTOR) {
-      vs[i] = T(srow[i]) * ri;
-    } else {
-      const T zi = ri * d[i];
-      z[i] = zi;
-      v[0] += double(ri) * double(zi);
-    }
+    const T zi = ri * d[i];
+    z[i] = zi;
+    v[0] += double(ri) * double(zi);
     v[1] += double(ri) * double(ri);
   }
   if (block_partials<2>(v, partial, &sc->ticket[2])) {
     double rz = sum_partials(partial, 0);
     double rr = sum_partials(partial, 1);
     if (threadIdx.x == 0) {
-      if (!FACTOR) sc->rho = rz;
-      sc->rr = rr;
-      sc->it += 1;
-      const double nr = sqrt(rr);
-      const double nb = sc->normb > 1.0e-14 ? sc->normb : 1.0;
-      if (MIXED) {
-        const double lim = fmax(sc->tol * nb, sc->delta * sc->rlast);
-        if (sc->finished || nr < lim || sc->it >= sc->maxit) sc->done = 1;
-      } else {
-        if (sc->finished || nr < sc->tol * nb || sc->it >= sc->maxit) {
-          sc->done = 1;
-          sc->converged = nr > sc->tol * nb ? 0 : 1;
-        }
-      }
+      sc->rho = rz;
+      end_iteration<MIXED>(rr, sc);
       sc->ticket[2] = 0;
     }
   }
@@ -484,8 +502,10 @@ __global__ void __launch_bounds__(kBlock) k_pc_upper(int64_t n, const int32_t* _
 }
 
 // z = -S (I+N) u (Dirichlet rows: z = r), partial (r,z); the last block
-// stores rho = (r,z).
-template <class T, class V, class CI>
+// stores rho = (r,z).  MODE 0 applies the preconditioner only; MODE 1 (FP64)
+// and MODE 2 (mixed) also close a CG iteration: partial (r,r), the count and
+// the stopping test.
+template <class T, class V, class CI, int MODE>
 __global__ void __launch_bounds__(kBlock) k_pc_lower(int64_t n, const int32_t* __restrict__ soffL,
                                                       const int32_t* __restrict__ swL, CI ci,
                                                       const V* __restrict__ nvL,
@@ -495,7 +515,7 @@ __global__ void __launch_bounds__(kBlock) k_pc_lower(int64_t n, const int32_t* _
                                                       const T* __restrict__ r, T* __restrict__ z,
                                                       double* partial, CGScalars* sc) {
   if (sc->done) return;
-  double v[1] = {0.0};
+  double v[2] = {0.0, 0.0};
   XG_ROWS(i, n) {
     const int lane = int(i & 31);
     const T acc = u[i] + sell_row<4, T>(ci, nvL, soffL[i >> 5], swL[i >> 5], lane, int32_t(i),
@@ -504,11 +524,23 @@ __global__ void __launch_bounds__(kBlock) k_pc_lower(int64_t n, const int32_t* _
     const T zi = mask[i] ? ri : -T(srow[i]) * acc;
     z[i] = zi;
     v[0] += double(ri) * double(zi);
+    if (MODE > 0) v[1] += double(ri) * double(ri);
   }
-  if (block_partials<1>(v, partial, &sc->ticket[3])) {
+  if (MODE == 0) {
+    double w[1] = {v[0]};
+    if (block_partials<1>(w, partial, &sc->ticket[3])) {
+      double rz = sum_partials(partial, 0);
+      if (threadIdx.x == 0) {
+        sc->rho = rz;
+        sc->ticket[3] = 0;
+      }
+    }
+  } else if (block_partials<2>(v, partial, &sc->ticket[3])) {
     double rz = sum_partials(partial, 0);
+    double rr = sum_partials(partial, 1);
     if (threadIdx.x == 0) {
       sc->rho = rz;
+      end_iteration<MODE == 2>(rr, sc);
       sc->ticket[3] = 0;
     }
   }
@@ -744,24 +776,26 @@ int factor_apply64(xg_ctx* c, CGDev* d, const double* r, double* z) {
   k_pc_upper<double, float, Cols32>
       <<<pgrid<k_pc_upper<double, float, Cols32>>(n), kBlock, 0, s>>>(
           n, d->soffU, d->swU, Cols32{d->colU}, d->nvU, d->v, d->u, d->scal);
-  k_pc_lower<double, float, Cols32>
-      <<<pgrid<k_pc_lower<double, float, Cols32>>(n), kBlock, 0, s>>>(
+  k_pc_lower<double, float, Cols32, 0>
+      <<<pgrid<k_pc_lower<double, float, Cols32, 0>>(n), kBlock, 0, s>>>(
           n, d->soffL, d->swL, Cols32{d->colL}, d->nvL, d->srow, d->bcmask, d->u, r, z,
           d->partial, d->scal);
   XG_CHECK_LAUNCH(c);
   return XG_OK;
 }
 
-// The FP32 factor passes on v32 = S r32 (already written): z32, rho.
-template <class CI>
+// The FP32 factor passes on v32 = S r32 (already written): z32, rho; with
+// MODE 2 they also close a mixed iteration.
+template <class CI, int MODE>
 void factor_passes32(xg_ctx* c, CGDev* d, CI cu, CI cl) {
   cudaStream_t s = c->stream;
   const int64_t n = d->n;
   k_pc_upper<float, __half, CI><<<pgrid<k_pc_upper<float, __half, CI>>(n), kBlock, 0, s>>>(
       n, d->soffU, d->swU, cu, d->hvU, d->v32, d->u32, d->scal);
-  k_pc_lower<float, __half, CI><<<pgrid<k_pc_lower<float, __half, CI>>(n), kBlock, 0, s>>>(
-      n, d->soffL, d->swL, cl, d->hvL, d->srow, d->bcmask, d->u32, d->r32, d->z32, d->partial,
-      d->scal);
+  k_pc_lower<float, __half, CI, MODE>
+      <<<pgrid<k_pc_lower<float, __half, CI, MODE>>(n), kBlock, 0, s>>>(
+          n, d->soffL, d->swL, cl, d->hvL, d->srow, d->bcmask, d->u32, d->r32, d->z32,
+          d->partial, d->scal);
 }
 
 int cg_iterate(xg_ctx* c, CGDev* d, int64_t maxit, double tol, CGScalars* h) {
@@ -781,8 +815,8 @@ int cg_iterate(xg_ctx* c, CGDev* d, int64_t maxit, double tol, CGScalars* h) {
         k_pc_upper<double, float, Cols32>
             <<<pgrid<k_pc_upper<double, float, Cols32>>(n), kBlock, 0, s>>>(
                 n, d->soffU, d->swU, Cols32{d->colU}, d->nvU, d->v, d->u, d->scal);
-        k_pc_lower<double, float, Cols32>
-            <<<pgrid<k_pc_lower<double, float, Cols32>>(n), kBlock, 0, s>>>(
+        k_pc_lower<double, float, Cols32, 1>
+            <<<pgrid<k_pc_lower<double, float, Cols32, 1>>(n), kBlock, 0, s>>>(
                 n, d->soffL, d->swL, Cols32{d->colL}, d->nvL, d->srow, d->bcmask, d->u, d->r,
                 d->z, d->partial, d->scal);
       } else {
@@ -811,7 +845,7 @@ int mixed_batch(xg_ctx* c, CGDev* d, CI ca, CI cu, CI cl) {
       k_cg_b<float, true, true><<<pgrid<k_cg_b<float, true, true>>(n), kBlock, 0, s>>>(
           n, d->q32, d->d32, p0, p1, d->srow, d->r32, d->z32, d->v32, d->e32, d->partial,
           d->scal);
-      factor_passes32<CI>(c, d, cu, cl);
+      factor_passes32<CI, 2>(c, d, cu, cl);
     } else {
       k_cg_b<float, false, true><<<pgrid<k_cg_b<float, false, true>>(n), kBlock, 0, s>>>(
           n, d->q32, d->d32, p0, p1, d->srow, d->r32, d->z32, d->v32, d->e32, d->partial,
@@ -832,9 +866,9 @@ int replace_residual(xg_ctx* c, CGDev* d, int first) {
   XG_CHECK_LAUNCH(c);
   if (d->pc == 2) {
     if (d->use16)
-      factor_passes32<Cols16>(c, d, Cols16{d->colU16}, Cols16{d->colL16});
+      factor_passes32<Cols16, 0>(c, d, Cols16{d->colU16}, Cols16{d->colL16});
     else
-      factor_passes32<Cols32>(c, d, Cols32{d->colU}, Cols32{d->colL});
+      factor_passes32<Cols32, 0>(c, d, Cols32{d->colU}, Cols32{d->colL});
     XG_CHECK_LAUNCH(c);
   }
   return XG_OK;
