@@ -251,6 +251,94 @@ print(json.dumps({"n": c.shape[1], "steps": steps, "s": t1 - t0}))
                       f"oracle C++ restatement, 1 thread per process, {worst:.2f} s"}
 
 
+def _oracle_proc(code):
+    """Run a timing snippet in a fresh single-threaded process; its JSON line."""
+    import oracle
+    oracle.build()
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    out = subprocess.run([sys.executable, "-c", code], stdout=subprocess.PIPE, text=True,
+                         env=env, check=True).stdout
+    return json.loads(out.strip().splitlines()[-1])
+
+
+def cpu_kozcg(n=49, steps=6):
+    """Oracle KozCG (Taylor-Galerkin + FCT) node-updates/s on one core."""
+    code = r"""
+import sys, time, json
+sys.path.insert(0, %r)
+import oracle
+from xyst_gb300 import mesh
+from bench import wave_state
+m = mesh.cube(%d, jitter=0.2, seed=0)
+c, ip = m["coord"], m["inpoel"]
+v = oracle.vol(c, ip)
+nodes, norms, _ = oracle.sym_bc(c, m["bface"], [1,2,3,4,5,6])
+k = oracle.KozCG(c, v, ip)
+k.set_sym(nodes, norms); k.set_state(wave_state(c))
+t0 = time.perf_counter(); k.run(%d); t1 = time.perf_counter()
+print(json.dumps({"n": c.shape[1], "s": t1 - t0}))
+""" % (ROOT, n, steps)
+    r = _oracle_proc(code)
+    return {"value": r["n"] * steps / r["s"], "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{n}^3 cube ({r['n']} nodes), {steps} KozCG steps, oracle C++ "
+                      f"restatement, 1 thread, {r['s']:.2f} s"}
+
+
+def cpu_chocg(n=49, steps=3):
+    """Oracle ChoCG s/step (FP64 Jacobi PCG to 1e-8, the reference's breakdown
+    test) on one core."""
+    code = r"""
+import sys, time, json
+sys.path.insert(0, %r)
+import numpy as np, oracle
+from xyst_gb300 import mesh, chocg
+m = mesh.cube(%d, jitter=0.2, seed=0, numbering="random", perm_seed=1)
+ops = chocg.operators(m, sym_sets=[1, 2, 3, 4, 5, 6], hydrostat=0)
+ia, ja, a = ops["matrix"]
+o = oracle.ChoCG(ops["coord"], ops["vol"], ops["edges"], ops["dint"], ops["tri"], ia, ja, a,
+                 mu=0.01, cfl=0.5, flux="damp2", pc="jacobi", ptol=1e-8, pmaxit=50000)
+o.set_bc(dir=ops["dir"], sym=ops["sym"], noslip=ops["noslip"], pdir=ops["pdir"])
+u0 = chocg.taylor_green(ops["coord"]); o.set_state(u0, np.zeros(u0.shape[0])); o.init()
+its = []
+t0 = time.perf_counter()
+for _ in range(%d): its.append(o.step()[1])
+t1 = time.perf_counter()
+print(json.dumps({"n": u0.shape[0], "s": t1 - t0, "its": its}))
+""" % (ROOT, n, steps)
+    r = _oracle_proc(code)
+    return {"value": r["s"] / steps, "unit": "s/step", "cores": 1, "kind": "port",
+            "sample": f"{n}^3 cube ({r['n']} nodes), {steps} ChoCG steps, FP64 Jacobi PCG to "
+                      f"1e-8 with the reference's breakdown test (iterations {r['its']}, "
+                      "negative: stopped by the test), oracle C++ restatement, 1 thread"}
+
+
+def run_kozcg(n=129, steps=10, warm=2, seed=0):
+    """KozCG (FP64 Taylor-Galerkin + FCT) node-updates/s on the n^3 jittered
+    cube with the smooth density wave and symmetry on every face."""
+    from xyst_gb300 import kozcg, lib, mesh, riecg
+
+    m = mesh.cube(n, jitter=0.2, seed=seed, numbering="random", perm_seed=seed + 1)
+    new_of_old = riecg.rcm(m["inpoel"], m["coord"].shape[1])
+    m = mesh.relabel(m, new_of_old)
+    coord, inpoel = m["coord"], m["inpoel"]
+    v = riecg.volumes(coord, inpoel)
+    ops = riecg.operators(m, sym_sets=[1, 2, 3, 4, 5, 6], renumber=False)
+    ctx = lib.Context(0)
+    k = kozcg.KozCG(ctx, coord, v, inpoel)
+    k.set_bc(sym=ops["sym"])
+    U0 = wave_state(coord)
+    k.set_state(U0)
+    k.run(warm)
+    k.set_state(U0)
+    dts, ms = k.run(steps)
+    ctx.close()
+    nn = coord.shape[1]
+    return {"workload": f"KozCG Euler, {n}^3 jittered cube (RCM), smooth density wave, "
+                        "Taylor-Galerkin + FCT, symmetry on all faces, CFL 0.5, FP64",
+            "nodes": int(nn), "steps": steps, "ms_per_step": ms / steps,
+            "value": nn * steps / (ms / 1e3), "unit": UNIT}
+
+
 # ------------------------------------------------------------------ GPU leg
 
 def run_gpu(args, rank, world):
@@ -291,7 +379,8 @@ def run_gpu(args, rank, world):
     dev_bytes = ctx.device_bytes()
     ctx.close()
     cho = run_chocg(n=args.n) if (rank == 0 and not args.no_pcg) else None
-    out = {"chocg": cho, "n": n, "nedge": nedge, "ms": ms_plain, "ms_events": ms, "kt": kt,
+    koz = run_kozcg(n=args.n) if (rank == 0 and not args.no_pcg) else None
+    out = {"chocg": cho, "kozcg": koz, "n": n, "nedge": nedge, "ms": ms_plain, "ms_events": ms, "kt": kt,
            "clocks": ck.summary(), "e2e_ms": e2e, "setup_s": t_setup, "dts": dts2,
            "dev_bytes": dev_bytes}
     return out
@@ -369,9 +458,12 @@ def main():
                 "wall_s": time.perf_counter() - t0}
         print(json.dumps(line))
         return
-    cpu = None
+    cpu = cpu_koz = cpu_cho = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_sample(n=49, steps=30, procs=1)  # before any GPU work in this process
+        if not args.no_pcg:
+            cpu_koz = cpu_kozcg()
+            cpu_cho = cpu_chocg()
     res = run_gpu(args, rank, world)
     # max over ranks
     ms = res["ms"]
@@ -416,7 +508,11 @@ def main():
             "cpu_baseline": cpu,
             "setup_s": res["setup_s"], "device_bytes": res["dev_bytes"],
             "dt_first_last": [float(res["dts"][0]), float(res["dts"][-1])],
-            "chocg": res["chocg"]}
+            "chocg": res["chocg"], "kozcg": res["kozcg"]}
+    if line["chocg"] is not None:
+        line["chocg"]["cpu_baseline"] = cpu_cho
+    if line["kozcg"] is not None:
+        line["kozcg"]["cpu_baseline"] = cpu_koz
     print(json.dumps(line))
 
 
