@@ -18,7 +18,7 @@
 // atomicMin on integers implement them exactly and deterministically.  Node
 // kernels (one thread per node) do the per-node algebra between the element
 // passes.  One step is:
-//   step_begin -> zero -> elem_rhs_aec -> bc_p -> node_lo -> elem_alw ->
+//   step_begin -> zero -> node_prim -> elem_rhs_aec -> bc_p -> node_lo -> elem_alw ->
 //   node_lim -> elem_lim -> node_solve -> bc (+ CFL minimum for the next step)
 
 #include <algorithm>
@@ -53,6 +53,7 @@ struct KozCGDev {
   double *U = nullptr, *R = nullptr, *P = nullptr, *A = nullptr;
   unsigned long long* Q = nullptr;
   double* stage = nullptr;
+  double* V = nullptr;  // [n][4] velocity and pressure per node
   // BC program: one thread per BC node
   int64_t nbc = 0;
   int32_t *bcnode = nullptr, *bcdir = nullptr, *bcsymp = nullptr, *dirmask = nullptr;
@@ -145,12 +146,34 @@ __device__ __forceinline__ Geo tetgeo(const double* xyz, int64_t n, const int32_
   return t;
 }
 
+// Per-node velocity and pressure (the node-wise quotients kozak::rhs forms
+// for every element holding the node, Kozak.cpp:93-118): computed once per
+// node, the same expressions, so the element pass gathers bit-identical
+// values instead of repeating the FP64 divisions per element.
+__global__ void __launch_bounds__(kBlock) k_node_prim(int64_t n, const double* __restrict__ U,
+                                                       double gamma, double* __restrict__ V) {
+  const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= n) return;
+  double u[5];
+#pragma unroll
+  for (int c = 0; c < 5; ++c) u[c] = U[c * n + i];
+  double o[4];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) o[j] = u[j + 1] / u[0];
+  o[3] = (gamma - 1.0) * (u[4] - 0.5 * (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) / u[0]);
+  double2* q = reinterpret_cast<double2*>(V + i * 4);
+  q[0] = make_double2(o[0], o[1]);
+  q[1] = make_double2(o[2], o[3]);
+}
+
 // kozak::rhs for one tet (Kozak.cpp:73-173) plus the antidiffusive element
 // contributions of KozCG::aec (KozCG.cpp:794-814), scattered to the nodes.
+// V holds each node's velocity and pressure (k_node_prim).
 __global__ void __launch_bounds__(kBlock) k_elem_rhs_aec(int64_t n, int64_t ne,
                                                           const int32_t* __restrict__ inpoel,
                                                           const double* __restrict__ xyz,
                                                           const double* __restrict__ U,
+                                                          const double* __restrict__ V,
                                                           const KScalars* __restrict__ sc,
                                                           double gamma, double ctau, int fct,
                                                           double* R, double* P) {
@@ -159,21 +182,24 @@ __global__ void __launch_bounds__(kBlock) k_elem_rhs_aec(int64_t n, int64_t ne,
   int32_t N[4];
   for (int a = 0; a < 4; ++a) N[a] = inpoel[e * 4 + a];
   const Geo t = tetgeo(xyz, n, N);
-  double u[4][5];
-  for (int a = 0; a < 4; ++a)
+  double u[4][5], vel[4][3], p[4];
+  for (int a = 0; a < 4; ++a) {
     for (int c = 0; c < 5; ++c) u[a][c] = U[c * n + N[a]];
+    const double2* q = reinterpret_cast<const double2*>(V + int64_t(N[a]) * 4);
+    const double2 v01 = __ldg(q), v23 = __ldg(q + 1);
+    vel[a][0] = v01.x;
+    vel[a][1] = v01.y;
+    vel[a][2] = v23.x;
+    p[a] = v23.y;
+  }
   const double dt = sc->dt;
-  double p[4];
-  for (int a = 0; a < 4; ++a)
-    p[a] = (gamma - 1.0) *
-           (u[a][4] - 0.5 * (u[a][1] * u[a][1] + u[a][2] * u[a][2] + u[a][3] * u[a][3]) / u[a][0]);
   double ue[5];
   for (int c = 0; c < 5; ++c) ue[c] = (u[0][c] + u[1][c] + u[2][c] + u[3][c]) / 4.0;
   double coef = dt / t.J / 2.0;
   for (int j = 0; j < 3; ++j)
     for (int a = 0; a < 4; ++a) {
       const double cg = coef * t.g[a][j];
-      const double uj = u[a][j + 1] / u[a][0];
+      const double uj = vel[a][j];
       ue[0] -= cg * u[a][j + 1];
       ue[1] -= cg * u[a][1] * uj;
       ue[2] -= cg * u[a][2] * uj;
@@ -477,7 +503,8 @@ int step(xg_ctx* c, KozCGDev* d) {
     XG_CUDA(c, cudaMemsetAsync(d->P, 0, n * 10 * 8, s));
     XG_CUDA(c, cudaMemsetAsync(d->A, 0, n * 5 * 8, s));
   }
-  k_elem_rhs_aec<<<blocks_for(ne, kBlock), kBlock, 0, s>>>(n, ne, d->inpoel, d->xyz, d->U,
+  k_node_prim<<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, d->U, d->prm.gamma, d->V);
+  k_elem_rhs_aec<<<blocks_for(ne, kBlock), kBlock, 0, s>>>(n, ne, d->inpoel, d->xyz, d->U, d->V,
                                                             d->scal, d->prm.gamma, d->prm.ctau,
                                                             fct, d->R, d->P);
   XG_CHECK_LAUNCH(c);
@@ -551,6 +578,7 @@ int xg_kozcg_setup(xg_ctx* c, const xg_kozcg_params* prm, int64_t npoin, const d
     A.plan(d->Q, npoin * 10);
     A.plan(d->A, npoin * 5);
     A.plan(d->stage, npoin * 5);
+    A.plan(d->V, npoin * 4);
     A.plan(d->isbc, npoin);
     A.plan(d->scal, 1);
     if (pass == 0) {
@@ -689,9 +717,10 @@ int xg_kozcg_rhs(xg_ctx* c, const double* U, double dt, double* R) {
   k_set_dt<<<1, 1, 0, s>>>(d->scal, dt);
   XG_CHECK_LAUNCH(c);
   XG_CUDA(c, cudaMemsetAsync(d->R, 0, d->n * 5 * 8, s));
+  k_node_prim<<<blocks_for(d->n, kBlock), kBlock, 0, s>>>(d->n, d->A, d->prm.gamma, d->V);
   k_elem_rhs_aec<<<blocks_for(d->ne, kBlock), kBlock, 0, s>>>(d->n, d->ne, d->inpoel, d->xyz, d->A,
-                                                               d->scal, d->prm.gamma, d->prm.ctau,
-                                                               0, d->R, d->P);
+                                                               d->V, d->scal, d->prm.gamma,
+                                                               d->prm.ctau, 0, d->R, d->P);
   XG_CHECK_LAUNCH(c);
   k_soa_to_aos<<<blocks_for(d->n * 5, kBlock), kBlock, 0, s>>>(d->n, 5, d->R, d->stage);
   XG_CHECK_LAUNCH(c);
