@@ -324,19 +324,34 @@ def run_kozcg(n=129, steps=10, warm=2, seed=0):
     v = riecg.volumes(coord, inpoel)
     ops = riecg.operators(m, sym_sets=[1, 2, 3, 4, 5, 6], renumber=False)
     ctx = lib.Context(0)
-    k = kozcg.KozCG(ctx, coord, v, inpoel)
-    k.set_bc(sym=ops["sym"])
     U0 = wave_state(coord)
-    k.set_state(U0)
-    k.run(warm)
-    k.set_state(U0)
-    dts, ms = k.run(steps)
-    ctx.close()
     nn = coord.shape[1]
+    res = {}
+    for fct in (True, False):
+        for prec in ("fp64", "fp32"):
+            k = kozcg.KozCG(ctx, coord, v, inpoel, fct=fct, precision=prec)
+            k.set_bc(sym=ops["sym"])
+            k.set_state(U0)
+            k.run(warm)
+            k.set_state(U0)
+            dts, ms = k.run(steps)
+            res[prec, fct] = (ms, k.state()[0])
+            del k
+    ctx.close()
+
+    def dev(fct):
+        a, b = res["fp32", fct][1], res["fp64", fct][1]
+        return float(np.abs(a - b).max() / np.abs(b).max())
+
+    ms, ms32 = res["fp64", True][0], res["fp32", True][0]
     return {"workload": f"KozCG Euler, {n}^3 jittered cube (RCM), smooth density wave, "
                         "Taylor-Galerkin + FCT, symmetry on all faces, CFL 0.5, FP64",
             "nodes": int(nn), "steps": steps, "ms_per_step": ms / steps,
-            "value": nn * steps / (ms / 1e3), "unit": UNIT}
+            "value": nn * steps / (ms / 1e3), "unit": UNIT,
+            "fp32_elements": {"ms_per_step": ms32 / steps,
+                              "value": nn * steps / (ms32 / 1e3), "unit": UNIT,
+                              "max_rel_dev_vs_fp64": dev(True),
+                              "max_rel_dev_vs_fp64_without_fct": dev(False)}}
 
 
 # ------------------------------------------------------------------ GPU leg

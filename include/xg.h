@@ -167,6 +167,9 @@ typedef struct xg_kozcg_params {
   double ctau;   /* fctdif: antidiffusion coefficient */
   int fctclip;   /* nonzero: limits from the low-order solution only */
   int fctsys;    /* bit c set: component c is limited as part of the system */
+  int precision; /* enum xg_precision: XG_FP32_FLUX forms the element terms
+                    (Galerkin residual, antidiffusive and limited element
+                    contributions) in FP32 and sums them into FP64 nodes */
 } xg_kozcg_params;
 
 /* Mesh of KozCG: coordinates, nodal volumes and tetrahedra (Discretization

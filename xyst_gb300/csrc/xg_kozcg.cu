@@ -53,7 +53,7 @@ struct KozCGDev {
   double *U = nullptr, *R = nullptr, *P = nullptr, *A = nullptr;
   unsigned long long* Q = nullptr;
   double* stage = nullptr;
-  double* V = nullptr;  // [n][4] velocity and pressure per node
+  double* V = nullptr;  // [n][4] velocity and pressure per node (FP32 packed in the first half)
   // BC program: one thread per BC node
   int64_t nbc = 0;
   int32_t *bcnode = nullptr, *bcdir = nullptr, *bcsymp = nullptr, *dirmask = nullptr;
@@ -119,19 +119,23 @@ __device__ __forceinline__ void block_min_atomic(double v, unsigned long long* d
   }
 }
 
+template <class F>
 struct Geo {
-  double J;
-  double g[4][3];
+  F J;
+  F g[4][3];
 };
 
-__device__ __forceinline__ Geo tetgeo(const double* xyz, int64_t n, const int32_t N[4]) {
+// Element geometry (Kozak.cpp:76-89): coordinate differences in FP64, the
+// cross products and Jacobian in F.
+template <class F>
+__device__ __forceinline__ Geo<F> tetgeo(const double* xyz, int64_t n, const int32_t N[4]) {
   const double* x = xyz;
   const double* y = xyz + n;
   const double* z = xyz + 2 * n;
-  double ba[3] = {x[N[1]] - x[N[0]], y[N[1]] - y[N[0]], z[N[1]] - z[N[0]]};
-  double ca[3] = {x[N[2]] - x[N[0]], y[N[2]] - y[N[0]], z[N[2]] - z[N[0]]};
-  double da[3] = {x[N[3]] - x[N[0]], y[N[3]] - y[N[0]], z[N[3]] - z[N[0]]};
-  Geo t;
+  const F ba[3] = {F(x[N[1]] - x[N[0]]), F(y[N[1]] - y[N[0]]), F(z[N[1]] - z[N[0]])};
+  const F ca[3] = {F(x[N[2]] - x[N[0]]), F(y[N[2]] - y[N[0]]), F(z[N[2]] - z[N[0]])};
+  const F da[3] = {F(x[N[3]] - x[N[0]]), F(y[N[3]] - y[N[0]]), F(z[N[3]] - z[N[0]])};
+  Geo<F> t;
   t.g[1][0] = ca[1] * da[2] - da[1] * ca[2];
   t.g[1][1] = ca[2] * da[0] - da[2] * ca[0];
   t.g[1][2] = ca[0] * da[1] - da[0] * ca[1];
@@ -150,56 +154,77 @@ __device__ __forceinline__ Geo tetgeo(const double* xyz, int64_t n, const int32_
 // for every element holding the node, Kozak.cpp:93-118): computed once per
 // node, the same expressions, so the element pass gathers bit-identical
 // values instead of repeating the FP64 divisions per element.
+template <class F>
 __global__ void __launch_bounds__(kBlock) k_node_prim(int64_t n, const double* __restrict__ U,
-                                                       double gamma, double* __restrict__ V) {
+                                                       double gamma_d, F* __restrict__ V) {
   const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (i >= n) return;
-  double u[5];
+  const F gamma = F(gamma_d);
+  F u[5];
 #pragma unroll
-  for (int c = 0; c < 5; ++c) u[c] = U[c * n + i];
-  double o[4];
+  for (int c = 0; c < 5; ++c) u[c] = F(U[c * n + i]);
+  F o[4];
 #pragma unroll
   for (int j = 0; j < 3; ++j) o[j] = u[j + 1] / u[0];
-  o[3] = (gamma - 1.0) * (u[4] - 0.5 * (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) / u[0]);
-  double2* q = reinterpret_cast<double2*>(V + i * 4);
-  q[0] = make_double2(o[0], o[1]);
-  q[1] = make_double2(o[2], o[3]);
+  o[3] = (gamma - F(1.0)) * (u[4] - F(0.5) * (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) / u[0]);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) V[i * 4 + k] = o[k];
 }
 
 // kozak::rhs for one tet (Kozak.cpp:73-173) plus the antidiffusive element
 // contributions of KozCG::aec (KozCG.cpp:794-814), scattered to the nodes.
 // V holds each node's velocity and pressure (k_node_prim).
+template <class F>
+__device__ __forceinline__ void load_v4(const F* V, int64_t i, F o[4]) {
+  if constexpr (sizeof(F) == 8) {
+    const double2* q = reinterpret_cast<const double2*>(V + i * 4);
+    const double2 a = __ldg(q), b = __ldg(q + 1);
+    o[0] = a.x;
+    o[1] = a.y;
+    o[2] = b.x;
+    o[3] = b.y;
+  } else {
+    const float4 a = __ldg(reinterpret_cast<const float4*>(V + i * 4));
+    o[0] = a.x;
+    o[1] = a.y;
+    o[2] = a.z;
+    o[3] = a.w;
+  }
+}
+
+template <class F>
 __global__ void __launch_bounds__(kBlock) k_elem_rhs_aec(int64_t n, int64_t ne,
                                                           const int32_t* __restrict__ inpoel,
                                                           const double* __restrict__ xyz,
                                                           const double* __restrict__ U,
-                                                          const double* __restrict__ V,
+                                                          const F* __restrict__ V,
                                                           const KScalars* __restrict__ sc,
-                                                          double gamma, double ctau, int fct,
+                                                          double gamma_d, double ctau_d, int fct,
                                                           double* R, double* P) {
   int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (e >= ne) return;
+  const F gamma = F(gamma_d), ctau = F(ctau_d);
   int32_t N[4];
   for (int a = 0; a < 4; ++a) N[a] = inpoel[e * 4 + a];
-  const Geo t = tetgeo(xyz, n, N);
-  double u[4][5], vel[4][3], p[4];
+  const Geo<F> t = tetgeo<F>(xyz, n, N);
+  F u[4][5], vel[4][3], p[4];
   for (int a = 0; a < 4; ++a) {
-    for (int c = 0; c < 5; ++c) u[a][c] = U[c * n + N[a]];
-    const double2* q = reinterpret_cast<const double2*>(V + int64_t(N[a]) * 4);
-    const double2 v01 = __ldg(q), v23 = __ldg(q + 1);
-    vel[a][0] = v01.x;
-    vel[a][1] = v01.y;
-    vel[a][2] = v23.x;
-    p[a] = v23.y;
+    for (int c = 0; c < 5; ++c) u[a][c] = F(U[c * n + N[a]]);
+    F v4[4];
+    load_v4(V, N[a], v4);
+    vel[a][0] = v4[0];
+    vel[a][1] = v4[1];
+    vel[a][2] = v4[2];
+    p[a] = v4[3];
   }
-  const double dt = sc->dt;
-  double ue[5];
-  for (int c = 0; c < 5; ++c) ue[c] = (u[0][c] + u[1][c] + u[2][c] + u[3][c]) / 4.0;
-  double coef = dt / t.J / 2.0;
+  const F dt = F(sc->dt);
+  F ue[5];
+  for (int c = 0; c < 5; ++c) ue[c] = (u[0][c] + u[1][c] + u[2][c] + u[3][c]) / F(4.0);
+  F coef = dt / t.J / F(2.0);
   for (int j = 0; j < 3; ++j)
     for (int a = 0; a < 4; ++a) {
-      const double cg = coef * t.g[a][j];
-      const double uj = vel[a][j];
+      const F cg = coef * t.g[a][j];
+      const F uj = vel[a][j];
       ue[0] -= cg * u[a][j + 1];
       ue[1] -= cg * u[a][1] * uj;
       ue[2] -= cg * u[a][2] * uj;
@@ -207,16 +232,16 @@ __global__ void __launch_bounds__(kBlock) k_elem_rhs_aec(int64_t n, int64_t ne,
       ue[j + 1] -= cg * p[a];
       ue[4] -= cg * (u[a][4] + p[a]) * uj;
     }
-  const double pr =
-      (gamma - 1.0) * (ue[4] - 0.5 * (ue[1] * ue[1] + ue[2] * ue[2] + ue[3] * ue[3]) / ue[0]);
-  double r[4][5];
+  const F pr =
+      (gamma - F(1.0)) * (ue[4] - F(0.5) * (ue[1] * ue[1] + ue[2] * ue[2] + ue[3] * ue[3]) / ue[0]);
+  F r[4][5];
   for (int a = 0; a < 4; ++a)
-    for (int c = 0; c < 5; ++c) r[a][c] = 0.0;
-  coef = 1.0 / 6.0;
+    for (int c = 0; c < 5; ++c) r[a][c] = F(0.0);
+  coef = F(1.0) / F(6.0);
   for (int j = 0; j < 3; ++j) {
-    const double uj = ue[j + 1] / ue[0];
+    const F uj = ue[j + 1] / ue[0];
     for (int a = 0; a < 4; ++a) {
-      const double cg = coef * t.g[a][j];
+      const F cg = coef * t.g[a][j];
       r[a][0] += cg * ue[j + 1];
       r[a][1] += cg * ue[1] * uj;
       r[a][2] += cg * ue[2] * uj;
@@ -226,19 +251,19 @@ __global__ void __launch_bounds__(kBlock) k_elem_rhs_aec(int64_t n, int64_t ne,
     }
   }
   for (int a = 0; a < 4; ++a)
-    for (int c = 0; c < 5; ++c) atomicAdd(R + c * n + N[a], r[a][c]);
+    for (int c = 0; c < 5; ++c) atomicAdd(R + c * n + N[a], double(r[a][c]));
   if (!fct) return;
   for (int c = 0; c < 5; ++c)
     for (int a = 0; a < 4; ++a) {
-      double aec = 0.0;
+      F aec = F(0.0);
       for (int b = 0; b < 4; ++b) {
-        const double m = t.J / 120.0 * ((a == b) ? 3.0 : -1.0);
+        const F m = t.J / F(120.0) * ((a == b) ? F(3.0) : F(-1.0));
         aec += m * ctau * u[b][c];
       }
-      if (aec > 0.0)
-        atomicAdd(P + (c * 2 + 0) * n + N[a], aec);
-      else if (aec < 0.0)
-        atomicAdd(P + (c * 2 + 1) * n + N[a], aec);
+      if (aec > F(0.0))
+        atomicAdd(P + (c * 2 + 0) * n + N[a], double(aec));
+      else if (aec < F(0.0))
+        atomicAdd(P + (c * 2 + 1) * n + N[a], double(aec));
     }
 }
 
@@ -352,38 +377,40 @@ __global__ void k_node_lim(int64_t n, const double* __restrict__ R, const double
 
 // KozCG::lim element part (KozCG.cpp:1049-1078): limited antidiffusive
 // element contributions, system-limited over the components in sysmask.
+template <class F>
 __global__ void __launch_bounds__(kBlock) k_elem_lim(int64_t n, int64_t ne,
                                                       const int32_t* __restrict__ inpoel,
                                                       const double* __restrict__ xyz,
                                                       const double* __restrict__ U,
                                                       const unsigned long long* __restrict__ Q,
-                                                      double ctau, int sysmask, double* A) {
+                                                      double ctau_d, int sysmask, double* A) {
   int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (e >= ne) return;
+  const F ctau = F(ctau_d);
   int32_t N[4];
   for (int a = 0; a < 4; ++a) N[a] = inpoel[e * 4 + a];
-  const Geo t = tetgeo(xyz, n, N);
-  double coef[5], aec[5][4];
+  const Geo<F> t = tetgeo<F>(xyz, n, N);
+  F coef[5], aec[5][4];
   for (int c = 0; c < 5; ++c) {
-    coef[c] = 1.0;
+    coef[c] = F(1.0);
     for (int a = 0; a < 4; ++a) {
-      double s = 0.0;
+      F s = F(0.0);
       for (int b = 0; b < 4; ++b) {
-        const double m = t.J / 120.0 * ((a == b) ? 3.0 : -1.0);
-        s += m * ctau * U[c * n + N[b]];
+        const F m = t.J / F(120.0) * ((a == b) ? F(3.0) : F(-1.0));
+        s += m * ctau * F(U[c * n + N[b]]);
       }
       aec[c][a] = s;
-      const double lim = __longlong_as_double(Q[(c * 2 + (s > 0.0 ? 0 : 1)) * n + N[a]]);
-      coef[c] = fmin(coef[c], lim);
+      const F lim = F(__longlong_as_double(Q[(c * 2 + (s > F(0.0) ? 0 : 1)) * n + N[a]]));
+      coef[c] = coef[c] < lim ? coef[c] : lim;
     }
   }
-  double cs = 1.0;
+  F cs = F(1.0);
   for (int c = 0; c < 5; ++c)
-    if (sysmask & (1 << c)) cs = fmin(cs, coef[c]);
+    if (sysmask & (1 << c)) cs = cs < coef[c] ? cs : coef[c];
   for (int c = 0; c < 5; ++c)
     if (sysmask & (1 << c)) coef[c] = cs;
   for (int c = 0; c < 5; ++c)
-    for (int a = 0; a < 4; ++a) atomicAdd(A + c * n + N[a], coef[c] * aec[c][a]);
+    for (int a = 0; a < 4; ++a) atomicAdd(A + c * n + N[a], double(coef[c] * aec[c][a]));
 }
 
 // KozCG::solve (KozCG.cpp:1144-1150): A = low-order + A/vol, then U = A and
@@ -493,6 +520,23 @@ int refresh_dt(xg_ctx* c, KozCGDev* d) {
   return XG_OK;
 }
 
+// Node primitives and the element Galerkin (+ antidiffusive) pass on state U,
+// in the context's precision.
+void galerkin(cudaStream_t s, KozCGDev* d, const double* U, int fct) {
+  const int64_t n = d->n, ne = d->ne;
+  if (d->prm.precision == XG_FP32_FLUX) {
+    float* V = reinterpret_cast<float*>(d->V);
+    k_node_prim<float><<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, U, d->prm.gamma, V);
+    k_elem_rhs_aec<float><<<blocks_for(ne, kBlock), kBlock, 0, s>>>(
+        n, ne, d->inpoel, d->xyz, U, V, d->scal, d->prm.gamma, d->prm.ctau, fct, d->R, d->P);
+  } else {
+    double* V = d->V;
+    k_node_prim<double><<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, U, d->prm.gamma, V);
+    k_elem_rhs_aec<double><<<blocks_for(ne, kBlock), kBlock, 0, s>>>(
+        n, ne, d->inpoel, d->xyz, U, V, d->scal, d->prm.gamma, d->prm.ctau, fct, d->R, d->P);
+  }
+}
+
 // One KozCG step with the dt already in the device scalars.
 int step(xg_ctx* c, KozCGDev* d) {
   cudaStream_t s = c->stream;
@@ -503,10 +547,7 @@ int step(xg_ctx* c, KozCGDev* d) {
     XG_CUDA(c, cudaMemsetAsync(d->P, 0, n * 10 * 8, s));
     XG_CUDA(c, cudaMemsetAsync(d->A, 0, n * 5 * 8, s));
   }
-  k_node_prim<<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, d->U, d->prm.gamma, d->V);
-  k_elem_rhs_aec<<<blocks_for(ne, kBlock), kBlock, 0, s>>>(n, ne, d->inpoel, d->xyz, d->U, d->V,
-                                                            d->scal, d->prm.gamma, d->prm.ctau,
-                                                            fct, d->R, d->P);
+  galerkin(s, d, d->U, fct);
   XG_CHECK_LAUNCH(c);
   if (fct && d->nbc) {
     k_bc_p<<<blocks_for(d->nbc, kBlock), kBlock, 0, s>>>(n, kbc_of(d), d->P);
@@ -521,8 +562,12 @@ int step(xg_ctx* c, KozCGDev* d) {
     XG_CHECK_LAUNCH(c);
     k_node_lim<<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, d->R, d->P, d->Q);
     XG_CHECK_LAUNCH(c);
-    k_elem_lim<<<blocks_for(ne, kBlock), kBlock, 0, s>>>(n, ne, d->inpoel, d->xyz, d->U, d->Q,
-                                                          d->prm.ctau, d->prm.fctsys, d->A);
+    if (d->prm.precision == XG_FP32_FLUX)
+      k_elem_lim<float><<<blocks_for(ne, kBlock), kBlock, 0, s>>>(
+          n, ne, d->inpoel, d->xyz, d->U, d->Q, d->prm.ctau, d->prm.fctsys, d->A);
+    else
+      k_elem_lim<double><<<blocks_for(ne, kBlock), kBlock, 0, s>>>(
+          n, ne, d->inpoel, d->xyz, d->U, d->Q, d->prm.ctau, d->prm.fctsys, d->A);
     XG_CHECK_LAUNCH(c);
   }
   k_node_solve<<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, d->vol, d->R, d->A, fct, d->isbc,
@@ -551,6 +596,8 @@ int xg_kozcg_setup(xg_ctx* c, const xg_kozcg_params* prm, int64_t npoin, const d
     return fail(c, XG_ERR_ARG, "kozcg_setup: bad mesh");
   if (npoin >= (int64_t(1) << 31) - 64) return fail(c, XG_ERR_ARG, "kozcg_setup: too many nodes");
   if (prm->fctsys & ~31) return fail(c, XG_ERR_ARG, "kozcg_setup: fctsys mask beyond 5 components");
+  if (prm->precision != XG_FP64 && prm->precision != XG_FP32_FLUX)
+    return fail(c, XG_ERR_ARG, "kozcg_setup: unknown precision");
   std::vector<int32_t> ip(nelem * 4);
   for (int64_t i = 0; i < nelem * 4; ++i) {
     if (inpoel[i] >= static_cast<uint64_t>(npoin))
@@ -717,10 +764,7 @@ int xg_kozcg_rhs(xg_ctx* c, const double* U, double dt, double* R) {
   k_set_dt<<<1, 1, 0, s>>>(d->scal, dt);
   XG_CHECK_LAUNCH(c);
   XG_CUDA(c, cudaMemsetAsync(d->R, 0, d->n * 5 * 8, s));
-  k_node_prim<<<blocks_for(d->n, kBlock), kBlock, 0, s>>>(d->n, d->A, d->prm.gamma, d->V);
-  k_elem_rhs_aec<<<blocks_for(d->ne, kBlock), kBlock, 0, s>>>(d->n, d->ne, d->inpoel, d->xyz, d->A,
-                                                               d->V, d->scal, d->prm.gamma,
-                                                               d->prm.ctau, 0, d->R, d->P);
+  galerkin(s, d, d->A, 0);
   XG_CHECK_LAUNCH(c);
   k_soa_to_aos<<<blocks_for(d->n * 5, kBlock), kBlock, 0, s>>>(d->n, 5, d->R, d->stage);
   XG_CHECK_LAUNCH(c);

@@ -14,8 +14,9 @@ from .lib import Context, KozcgParams, f64, i32, p, u64
 
 class KozCG:
     def __init__(self, ctx: Context, coord, vol, inpoel, gamma=1.4, cfl=0.5, const_dt=0.0,
-                 fct=True, ctau=1.0, fctclip=False, fctsys=()):
-        """fctsys: zero-based component ids limited as a system."""
+                 fct=True, ctau=1.0, fctclip=False, fctsys=(), precision="fp64"):
+        """fctsys: zero-based component ids limited as a system.  precision
+        "fp32" forms the element terms in FP32 and sums them into FP64 nodes."""
         self.ctx = ctx
         self.lib = ctx.lib
         coord = f64(coord)
@@ -23,7 +24,8 @@ class KozCG:
         mask = 0
         for c in fctsys:
             mask |= 1 << int(c)
-        prm = KozcgParams(gamma, cfl, const_dt, int(fct), ctau, int(fctclip), mask)
+        prec = {"fp64": 0, "fp32": 1}[precision]
+        prm = KozcgParams(gamma, cfl, const_dt, int(fct), ctau, int(fctclip), mask, prec)
         v = f64(vol)
         ip = u64(inpoel).reshape(-1)
         self._keep = (coord, v, ip)

@@ -38,7 +38,7 @@ class RiecgParams(C.Structure):
 
 class KozcgParams(C.Structure):
     _fields_ = [("gamma", _dbl), ("cfl", _dbl), ("const_dt", _dbl), ("fct", _int),
-                ("ctau", _dbl), ("fctclip", _int), ("fctsys", _int)]
+                ("ctau", _dbl), ("fctclip", _int), ("fctsys", _int), ("precision", _int)]
 
 
 class ChocgParams(C.Structure):
