@@ -83,6 +83,7 @@ struct CGDev {
   double *x = nullptr, *b = nullptr, *r = nullptr, *q = nullptr, *z = nullptr, *d = nullptr;
   double* p[2] = {nullptr, nullptr};
   float *r32 = nullptr, *q32 = nullptr, *z32 = nullptr, *d32 = nullptr, *e32 = nullptr;
+  float* r32b = nullptr;  // second FP32 residual (factored mixed iteration, alternating)
   float* p32[2] = {nullptr, nullptr};
   double* partial = nullptr;  // 3 * maxgrid
   CGScalars* scal = nullptr;
@@ -501,6 +502,37 @@ __global__ void __launch_bounds__(kBlock) k_pc_upper(int64_t n, const int32_t* _
   }
 }
 
+// The update of a factored FP32 iteration fused with the first factor pass:
+// r' = r - alpha q, e += alpha p', u = (I+N)^T S r', with the neighbours'
+// S r' formed from their r and q.  The residual alternates between ra and rb
+// with the count (the current one is ra at even counts): the pass reads one
+// and writes the other, so no row reads a residual that another row of the
+// same pass has replaced.
+template <class CI>
+__global__ void __launch_bounds__(kBlock) k_pc_upper_res(
+    int64_t n, const int32_t* __restrict__ soffU, const int32_t* __restrict__ swU, CI ci,
+    const __half* __restrict__ nvU, const float* __restrict__ srow, const float* __restrict__ q,
+    const float* p0, const float* p1, float* ra, float* rb, float* __restrict__ e,
+    float* __restrict__ u, const CGScalars* __restrict__ sc) {
+  if (sc->done) return;
+  const float alpha = float(sc->alpha);
+  const int64_t it = sc->it;
+  const float* __restrict__ p = (it & 1) ? p0 : p1;
+  const float* __restrict__ rold = (it & 1) ? rb : ra;
+  float* __restrict__ rnew = (it & 1) ? ra : rb;
+  XG_ROWS(i, n) {
+    const int lane = int(i & 31);
+    const float ri = rold[i] - alpha * q[i];
+    rnew[i] = ri;
+    e[i] += alpha * p[i];
+    u[i] = srow[i] * ri +
+           sell_row<4, float>(ci, nvU, soffU[i >> 5], swU[i >> 5], lane, int32_t(i),
+                              [&](int32_t c) {
+                                return __ldg(srow + c) * (__ldg(rold + c) - alpha * __ldg(q + c));
+                              });
+  }
+}
+
 // z = -S (I+N) u (Dirichlet rows: z = r), partial (r,z); the last block
 // stores rho = (r,z).  MODE 0 applies the preconditioner only; MODE 1 (FP64)
 // and MODE 2 (mixed) also close a CG iteration: partial (r,r), the count and
@@ -512,9 +544,14 @@ __global__ void __launch_bounds__(kBlock) k_pc_lower(int64_t n, const int32_t* _
                                                       const float* __restrict__ srow,
                                                       const uint8_t* __restrict__ mask,
                                                       const T* __restrict__ u,
-                                                      const T* __restrict__ r, T* __restrict__ z,
-                                                      double* partial, CGScalars* sc) {
+                                                      const T* r_even, const T* r_odd,
+                                                      T* __restrict__ z, double* partial,
+                                                      CGScalars* sc) {
   if (sc->done) return;
+  // the residual: r_even unless it alternates (r_odd given), then the one
+  // k_pc_upper_res wrote (MODE 2) or the current one (MODE 0)
+  const bool odd = r_odd && (((sc->it + (MODE == 2 ? 1 : 0)) & 1) != 0);
+  const T* __restrict__ r = odd ? r_odd : r_even;
   double v[2] = {0.0, 0.0};
   XG_ROWS(i, n) {
     const int lane = int(i & 31);
@@ -568,10 +605,12 @@ __global__ void __launch_bounds__(kBlock) k_outer_res(int64_t n, const int32_t* 
                                                        const double* __restrict__ b,
                                                        const float* __restrict__ d32,
                                                        const float* __restrict__ srow,
-                                                       float* __restrict__ r32,
+                                                       float* r32, float* r32b,
                                                        float* __restrict__ z32,
                                                        float* __restrict__ v32, int first,
                                                        double* partial, CGScalars* sc) {
+  // the current residual buffer (it alternates in the factored iteration)
+  float* __restrict__ rout = (r32b && !first && (sc->it & 1)) ? r32b : r32;
   double v[2] = {0.0, 0.0};
   XG_ROWS(i, n) {
     const int lane = int(i & 31);
@@ -579,7 +618,7 @@ __global__ void __launch_bounds__(kBlock) k_outer_res(int64_t n, const int32_t* 
                                          int32_t(i), [&](int32_t c) { return __ldg(x + c); });
     const double ri = b[i] - s;
     const float rf = float(ri);
-    r32[i] = rf;
+    rout[i] = rf;
     if (srow) {
       v32[i] = srow[i] * rf;
     } else {
@@ -778,24 +817,23 @@ int factor_apply64(xg_ctx* c, CGDev* d, const double* r, double* z) {
           n, d->soffU, d->swU, Cols32{d->colU}, d->nvU, d->v, d->u, d->scal);
   k_pc_lower<double, float, Cols32, 0>
       <<<pgrid<k_pc_lower<double, float, Cols32, 0>>(n), kBlock, 0, s>>>(
-          n, d->soffL, d->swL, Cols32{d->colL}, d->nvL, d->srow, d->bcmask, d->u, r, z,
+          n, d->soffL, d->swL, Cols32{d->colL}, d->nvL, d->srow, d->bcmask, d->u, r, nullptr, z,
           d->partial, d->scal);
   XG_CHECK_LAUNCH(c);
   return XG_OK;
 }
 
-// The FP32 factor passes on v32 = S r32 (already written): z32, rho; with
-// MODE 2 they also close a mixed iteration.
-template <class CI, int MODE>
-void factor_passes32(xg_ctx* c, CGDev* d, CI cu, CI cl) {
+// The FP32 factor passes on v32 = S r (already written, r the current
+// residual): z32 and rho = (r, z32).
+template <class CI>
+void factor_apply32(xg_ctx* c, CGDev* d, CI cu, CI cl) {
   cudaStream_t s = c->stream;
   const int64_t n = d->n;
   k_pc_upper<float, __half, CI><<<pgrid<k_pc_upper<float, __half, CI>>(n), kBlock, 0, s>>>(
       n, d->soffU, d->swU, cu, d->hvU, d->v32, d->u32, d->scal);
-  k_pc_lower<float, __half, CI, MODE>
-      <<<pgrid<k_pc_lower<float, __half, CI, MODE>>(n), kBlock, 0, s>>>(
-          n, d->soffL, d->swL, cl, d->hvL, d->srow, d->bcmask, d->u32, d->r32, d->z32,
-          d->partial, d->scal);
+  k_pc_lower<float, __half, CI, 0><<<pgrid<k_pc_lower<float, __half, CI, 0>>(n), kBlock, 0, s>>>(
+      n, d->soffL, d->swL, cl, d->hvL, d->srow, d->bcmask, d->u32, d->r32, d->r32b, d->z32,
+      d->partial, d->scal);
 }
 
 int cg_iterate(xg_ctx* c, CGDev* d, int64_t maxit, double tol, CGScalars* h) {
@@ -818,7 +856,7 @@ int cg_iterate(xg_ctx* c, CGDev* d, int64_t maxit, double tol, CGScalars* h) {
         k_pc_lower<double, float, Cols32, 1>
             <<<pgrid<k_pc_lower<double, float, Cols32, 1>>(n), kBlock, 0, s>>>(
                 n, d->soffL, d->swL, Cols32{d->colL}, d->nvL, d->srow, d->bcmask, d->u, d->r,
-                d->z, d->partial, d->scal);
+                nullptr, d->z, d->partial, d->scal);
       } else {
         k_cg_b<double, false, false><<<pgrid<k_cg_b<double, false, false>>(n), kBlock, 0, s>>>(
             n, d->q, d->d, p0, p1, d->srow, d->r, d->z, d->v, d->x, d->partial, d->scal);
@@ -832,7 +870,9 @@ int cg_iterate(xg_ctx* c, CGDev* d, int64_t maxit, double tol, CGScalars* h) {
   return XG_OK;
 }
 
-// A batch of FP32 iterations with column encoding CI.
+// A batch of FP32 iterations with column encoding CI.  Factored: q = A p'
+// (k_cg_a), the update with u = (I+N)^T S r' (k_pc_upper_res), then
+// z = -S (I+N) u closing the iteration (k_pc_lower); Jacobi: k_cg_a, k_cg_b.
 template <class CI>
 int mixed_batch(xg_ctx* c, CGDev* d, CI ca, CI cu, CI cl) {
   cudaStream_t s = c->stream;
@@ -842,10 +882,13 @@ int mixed_batch(xg_ctx* c, CGDev* d, CI ca, CI cu, CI cl) {
     k_cg_a<float, float, CI><<<pgrid<k_cg_a<float, float, CI>>(n), kBlock, 0, s>>>(
         n, d->soff, d->swidth, ca, d->a32, d->z32, p0, p1, d->q32, d->partial, d->scal);
     if (d->pc == 2) {
-      k_cg_b<float, true, true><<<pgrid<k_cg_b<float, true, true>>(n), kBlock, 0, s>>>(
-          n, d->q32, d->d32, p0, p1, d->srow, d->r32, d->z32, d->v32, d->e32, d->partial,
-          d->scal);
-      factor_passes32<CI, 2>(c, d, cu, cl);
+      k_pc_upper_res<CI><<<pgrid<k_pc_upper_res<CI>>(n), kBlock, 0, s>>>(
+          n, d->soffU, d->swU, cu, d->hvU, d->srow, d->q32, p0, p1, d->r32, d->r32b, d->e32,
+          d->u32, d->scal);
+      k_pc_lower<float, __half, CI, 2>
+          <<<pgrid<k_pc_lower<float, __half, CI, 2>>(n), kBlock, 0, s>>>(
+              n, d->soffL, d->swL, cl, d->hvL, d->srow, d->bcmask, d->u32, d->r32, d->r32b,
+              d->z32, d->partial, d->scal);
     } else {
       k_cg_b<float, false, true><<<pgrid<k_cg_b<float, false, true>>(n), kBlock, 0, s>>>(
           n, d->q32, d->d32, p0, p1, d->srow, d->r32, d->z32, d->v32, d->e32, d->partial,
@@ -862,13 +905,13 @@ int replace_residual(xg_ctx* c, CGDev* d, int first) {
   const int64_t n = d->n;
   k_outer_res<<<pgrid<k_outer_res>(n), kBlock, 0, s>>>(
       n, d->soff, d->swidth, d->col, d->a, d->x, d->b, d->d32, d->pc == 2 ? d->srow : nullptr,
-      d->r32, d->z32, d->v32, first, d->partial, d->scal);
+      d->r32, d->pc == 2 ? d->r32b : nullptr, d->z32, d->v32, first, d->partial, d->scal);
   XG_CHECK_LAUNCH(c);
   if (d->pc == 2) {
     if (d->use16)
-      factor_passes32<Cols16, 0>(c, d, Cols16{d->colU16}, Cols16{d->colL16});
+      factor_apply32(c, d, Cols16{d->colU16}, Cols16{d->colL16});
     else
-      factor_passes32<Cols32, 0>(c, d, Cols32{d->colU}, Cols32{d->colL});
+      factor_apply32(c, d, Cols32{d->colU}, Cols32{d->colL});
     XG_CHECK_LAUNCH(c);
   }
   return XG_OK;
@@ -1118,6 +1161,7 @@ int xg_cg_setup(xg_ctx* c, int64_t nrow, const uint64_t* ia, const uint64_t* ja,
     A.plan(d->p[0], nrow);
     A.plan(d->p[1], nrow);
     A.plan(d->r32, nrow);
+    A.plan(d->r32b, nrow);
     A.plan(d->q32, nrow);
     A.plan(d->z32, nrow);
     A.plan(d->d32, nrow);
