@@ -16,13 +16,17 @@
 // their diagonal), and the right-hand side correction sum_i a_ji * val_i is
 // summed per row in the reference's order (decreasing node id).
 //
-// One PCG iteration (the reference's FP64 algorithm) is two kernels:
-//   k_cg_a: p' = z + beta p (beta = rho/rho0), q = A p', partial (p', q)
-//   k_cg_b: alpha = rho/(p,q); r -= alpha q; x += alpha p'; z = r/d (Jacobi,
+// One PCG iteration (the reference's FP64 algorithm) is three kernels:
+//   k_cg_p: p = z + beta p (beta = rho/rho0)
+//   k_cg_a: q = A p, partial (p, q)
+//   k_cg_b: alpha = rho/(p,q); r -= alpha q; x += alpha p; z = r/d (Jacobi,
 //           as r times the stored inverse diagonal);
 //           partial (r,z), (r,r); convergence test
 // plus, for the factored preconditioner (pc 2, no reference counterpart),
 // z = -S (I+N)(I+N)^T S r in two passes over the lower and upper triangles.
+// GB300 runs FP64 arithmetic at a small fraction of its FP32 rate, so the
+// FP64 kernels keep FP64 operations per row to what the algorithm needs
+// (p is formed once per row, scalar divisions once per block).
 // Kernels loop over rows with a grid of one wave of resident blocks, so a
 // reduction has one partial per block; the last block to finish (an atomic
 // ticket, no spinning) adds them in block order, so every reduction is
@@ -37,7 +41,10 @@
 // residual b - A x whenever the recursive residual has fallen by the factor
 // `inner_tol` since the last replacement.  The search direction is kept
 // across replacements, so the FP32 iteration follows the FP64 one instead of
-// restarting.
+// restarting.  The FP32 iteration is three kernels: k_cg_a forms
+// p' = z + beta p per gathered entry (FP32 arithmetic is cheap; no p pass),
+// k_pc_upper_res updates r and e and applies (I+N)^T S, k_pc_lower applies
+// -S (I+N) and closes the iteration.
 
 #include <cuda_fp16.h>
 
@@ -124,13 +131,15 @@ namespace {
 
 // Sum of one value per thread into partial[k * gridDim.x + blockIdx.x];
 // returns true in the block that completes last (its threads then see every
-// partial).
-template <int K>
-__device__ __forceinline__ bool block_partials(const double (&v)[K], double* partial,
+// partial).  The warp sums run in A (FP32 for the FP32 solver, whose values
+// are FP32: FP64 shuffles and adds per thread load GB300's narrow FP64
+// pipe); the warp totals are summed in FP64.
+template <int K, class A>
+__device__ __forceinline__ bool block_partials(const A (&v)[K], double* partial,
                                                unsigned int* ticket) {
   __shared__ double sm[K][32];
   __shared__ bool last;
-  double s[K];
+  A s[K];
 #pragma unroll
   for (int k = 0; k < K; ++k) {
     s[k] = v[k];
@@ -140,7 +149,7 @@ __device__ __forceinline__ bool block_partials(const double (&v)[K], double* par
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   if (lane == 0)
 #pragma unroll
-    for (int k = 0; k < K; ++k) sm[k][wid] = s[k];
+    for (int k = 0; k < K; ++k) sm[k][wid] = double(s[k]);
   __syncthreads();
   if (threadIdx.x == 0) {
     const int nw = (blockDim.x + 31) >> 5;
@@ -364,12 +373,35 @@ __global__ void __launch_bounds__(kBlock) k_setup(int64_t n, const int32_t* __re
   }
 }
 
-// next + qAp + q (ConjugateGradients.cpp:584-669), fused: p' = z + beta p,
+// next + qAp + q (ConjugateGradients.cpp:584-669): p' = z + beta p,
 // q = A p', partial (p', q); the last block sets alpha = rho / (p', q).
 // T is the vector type, V the matrix value type, CI the column encoding.
-// The search direction ping-pongs between p0 and p1 by the parity of the
-// iteration count, which only the iterations that ran advance.
-template <class T, class V, class CI>
+//
+// beta = rho/rho0 (0 in the first iteration), formed once per block: an FP64
+// division per thread would load GB300's narrow FP64 pipe.
+template <class T>
+__device__ __forceinline__ T block_beta(const CGScalars* sc) {
+  __shared__ T beta_s;
+  if (threadIdx.x == 0) beta_s = sc->it == 0 ? T(0) : T(sc->rho / sc->rho0);
+  __syncthreads();
+  return beta_s;
+}
+
+// p = z + beta p in place (the FP64 solver; its SpMV then gathers p alone,
+// with half the FP64 operations of forming p per gathered entry).
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_cg_p(int64_t n, const T* __restrict__ z,
+                                                  T* __restrict__ p, const CGScalars* sc) {
+  if (sc->done) return;
+  const T beta = block_beta<T>(sc);
+  XG_ROWS(i, n) p[i] = z[i] + beta * p[i];
+}
+
+// q = A p', (p', q).  PF: p' = z + beta p formed per gathered entry and
+// stored for the row (the FP32 solver: two gathers, no extra pass; p0/p1
+// alternate with the count); otherwise p' = p0 = p1 (k_cg_p).  The FP32
+// solver sums (p', q) per thread in FP32 and widens once.
+template <class T, class V, class CI, bool PF>
 __global__ void __launch_bounds__(kBlock) k_cg_a(int64_t n, const int32_t* __restrict__ soff,
                                                   const int32_t* __restrict__ sw, CI ci,
                                                   const V* __restrict__ a,
@@ -378,19 +410,27 @@ __global__ void __launch_bounds__(kBlock) k_cg_a(int64_t n, const int32_t* __res
                                                   CGScalars* sc) {
   if (sc->done) return;
   const int64_t it = sc->it;
-  const T beta = it == 0 ? T(0) : T(sc->rho / sc->rho0);
+  const T beta = PF ? block_beta<T>(sc) : T(0);
   const T* __restrict__ pold = (it & 1) ? p1 : p0;
   T* __restrict__ pnew = (it & 1) ? p0 : p1;
-  double v[1] = {0.0};
+  T dot = T(0);
   XG_ROWS(i, n) {
     const int lane = int(i & 31);
-    const T s = sell_row<4, T>(ci, a, soff[i >> 5], sw[i >> 5], lane, int32_t(i),
-                               [&](int32_t c) { return __ldg(z + c) + beta * __ldg(pold + c); });
-    const T pi = z[i] + beta * pold[i];
-    pnew[i] = pi;
-    q[i] = s;
-    v[0] += double(pi) * double(s);
+    if (PF) {
+      const T s = sell_row<4, T>(ci, a, soff[i >> 5], sw[i >> 5], lane, int32_t(i),
+                                 [&](int32_t c) { return __ldg(z + c) + beta * __ldg(pold + c); });
+      const T pi = z[i] + beta * pold[i];
+      pnew[i] = pi;
+      q[i] = s;
+      dot += pi * s;
+    } else {
+      const T s = sell_row<4, T>(ci, a, soff[i >> 5], sw[i >> 5], lane, int32_t(i),
+                                 [&](int32_t c) { return __ldg(p0 + c); });
+      q[i] = s;
+      dot += p0[i] * s;
+    }
   }
+  T v[1] = {dot};
   if (block_partials<1>(v, partial, &sc->ticket[1])) {
     double pq = sum_partials(partial, 0);
     if (threadIdx.x == 0) {
@@ -463,16 +503,17 @@ __global__ void __launch_bounds__(kBlock) k_cg_b(int64_t n, const T* __restrict_
     }
     return;
   }
-  double v[2] = {0.0, 0.0};
+  T rz = T(0), rr = T(0);  // per thread in T, widened in block_partials
   XG_ROWS(i, n) {
     const T ri = r[i] - alpha * q[i];
     r[i] = ri;
     x[i] += alpha * p[i];
     const T zi = ri * d[i];
     z[i] = zi;
-    v[0] += double(ri) * double(zi);
-    v[1] += double(ri) * double(ri);
+    rz += ri * zi;
+    rr += ri * ri;
   }
+  const T v[2] = {rz, rr};
   if (block_partials<2>(v, partial, &sc->ticket[2])) {
     double rz = sum_partials(partial, 0);
     double rr = sum_partials(partial, 1);
@@ -552,7 +593,7 @@ __global__ void __launch_bounds__(kBlock) k_pc_lower(int64_t n, const int32_t* _
   // k_pc_upper_res wrote (MODE 2) or the current one (MODE 0)
   const bool odd = r_odd && (((sc->it + (MODE == 2 ? 1 : 0)) & 1) != 0);
   const T* __restrict__ r = odd ? r_odd : r_even;
-  double v[2] = {0.0, 0.0};
+  T rz = T(0), rr = T(0);  // per thread in T (FP32 for the mixed solver), widened once
   XG_ROWS(i, n) {
     const int lane = int(i & 31);
     const T acc = u[i] + sell_row<4, T>(ci, nvL, soffL[i >> 5], swL[i >> 5], lane, int32_t(i),
@@ -560,11 +601,12 @@ __global__ void __launch_bounds__(kBlock) k_pc_lower(int64_t n, const int32_t* _
     const T ri = r[i];
     const T zi = mask[i] ? ri : -T(srow[i]) * acc;
     z[i] = zi;
-    v[0] += double(ri) * double(zi);
-    if (MODE > 0) v[1] += double(ri) * double(ri);
+    rz += ri * zi;
+    if (MODE > 0) rr += ri * ri;
   }
+  T v[2] = {rz, rr};
   if (MODE == 0) {
-    double w[1] = {v[0]};
+    T w[1] = {v[0]};
     if (block_partials<1>(w, partial, &sc->ticket[3])) {
       double rz = sum_partials(partial, 0);
       if (threadIdx.x == 0) {
@@ -844,12 +886,15 @@ int cg_iterate(xg_ctx* c, CGDev* d, int64_t maxit, double tol, CGScalars* h) {
   const int64_t n = d->n;
   for (;;) {
     for (int k = 0; k < kBatch; ++k) {
-      double *p0 = d->p[0], *p1 = d->p[1];
-      k_cg_a<double, double, Cols32><<<pgrid<k_cg_a<double, double, Cols32>>(n), kBlock, 0, s>>>(
-          n, d->soff, d->swidth, Cols32{d->col}, d->a, d->z, p0, p1, d->q, d->partial, d->scal);
+      double* p0 = d->p[0];
+      k_cg_p<double><<<pgrid<k_cg_p<double>>(n), kBlock, 0, s>>>(n, d->z, p0, d->scal);
+      k_cg_a<double, double, Cols32, false>
+          <<<pgrid<k_cg_a<double, double, Cols32, false>>(n), kBlock, 0, s>>>(
+              n, d->soff, d->swidth, Cols32{d->col}, d->a, d->z, p0, p0, d->q, d->partial,
+              d->scal);
       if (d->pc == 2) {
         k_cg_b<double, true, false><<<pgrid<k_cg_b<double, true, false>>(n), kBlock, 0, s>>>(
-            n, d->q, d->d, p0, p1, d->srow, d->r, d->z, d->v, d->x, d->partial, d->scal);
+            n, d->q, d->d, p0, p0, d->srow, d->r, d->z, d->v, d->x, d->partial, d->scal);
         k_pc_upper<double, float, Cols32>
             <<<pgrid<k_pc_upper<double, float, Cols32>>(n), kBlock, 0, s>>>(
                 n, d->soffU, d->swU, Cols32{d->colU}, d->nvU, d->v, d->u, d->scal);
@@ -859,7 +904,7 @@ int cg_iterate(xg_ctx* c, CGDev* d, int64_t maxit, double tol, CGScalars* h) {
                 nullptr, d->z, d->partial, d->scal);
       } else {
         k_cg_b<double, false, false><<<pgrid<k_cg_b<double, false, false>>(n), kBlock, 0, s>>>(
-            n, d->q, d->d, p0, p1, d->srow, d->r, d->z, d->v, d->x, d->partial, d->scal);
+            n, d->q, d->d, p0, p0, d->srow, d->r, d->z, d->v, d->x, d->partial, d->scal);
       }
     }
     XG_CHECK_LAUNCH(c);
@@ -879,7 +924,7 @@ int mixed_batch(xg_ctx* c, CGDev* d, CI ca, CI cu, CI cl) {
   const int64_t n = d->n;
   for (int k = 0; k < kBatch; ++k) {
     float *p0 = d->p32[0], *p1 = d->p32[1];
-    k_cg_a<float, float, CI><<<pgrid<k_cg_a<float, float, CI>>(n), kBlock, 0, s>>>(
+    k_cg_a<float, float, CI, true><<<pgrid<k_cg_a<float, float, CI, true>>(n), kBlock, 0, s>>>(
         n, d->soff, d->swidth, ca, d->a32, d->z32, p0, p1, d->q32, d->partial, d->scal);
     if (d->pc == 2) {
       k_pc_upper_res<CI><<<pgrid<k_pc_upper_res<CI>>(n), kBlock, 0, s>>>(
