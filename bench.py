@@ -182,7 +182,7 @@ def run_chocg(n=129, steps=5, warm=2, tol=1e-8, train_steps=300, seed=0):
     for name, (pc, mdl, mixed) in modes.items():
         ctx = lib.Context(0)
         d = chocg.ChoCG(ctx, ops, mu=0.01, cfl=0.5, flux="damp2", pc=pc, ptol=tol,
-                        pmaxit=50000, mixed=mixed, inner_tol=1e-2, guard="underflow")
+                        pmaxit=50000, mixed=mixed, inner_tol=0.1, guard="underflow")
         if pc == "factor":
             d.cg.set_factor(None if mdl == "none" else mdl, 1.0)
         d.set_state(u0)

@@ -196,10 +196,13 @@ __device__ double sum_partials(const double* partial, int k) {
 // ---------------------------------------------------------------- row access
 
 // Column of SELL entry e of row i (or -1 for padding), from int32 columns or
-// 16-bit offsets.
+// 16-bit offsets.  The int32 columns and FP64 values (the FP64 solver's
+// matrix stream, larger than L2) are read with the evict-first hint so that
+// the gathered vectors stay in L2; the FP32 solver's narrower stream is read
+// through the non-coherent cache (measured faster for it).
 struct Cols32 {
   const int32_t* c;
-  __device__ __forceinline__ int32_t at(int32_t e, int32_t) const { return __ldg(c + e); }
+  __device__ __forceinline__ int32_t at(int32_t e, int32_t) const { return __ldcs(c + e); }
 };
 struct Cols16 {
   const int16_t* c;
@@ -211,7 +214,7 @@ struct Cols16 {
 
 __device__ __forceinline__ float ldv(const __half* p) { return __half2float(p[0]); }
 __device__ __forceinline__ float ldv(const float* p) { return __ldg(p); }
-__device__ __forceinline__ double ldv(const double* p) { return __ldg(p); }
+__device__ __forceinline__ double ldv(const double* p) { return __ldcs(p); }
 
 // sum_k val[e_k] * g(col[e_k]) over row i of a SELL-32 layout, in entry
 // order, issued in groups of U entries so that U column / value loads and
@@ -243,6 +246,52 @@ __device__ __forceinline__ T sell_row(CI ci, const V* __restrict__ val, int32_t 
   return s;
 }
 
+// The same sum with each round fully unrolled to the exact number of entries
+// left (at most XM): a row of w <= XM entries is one round, its column /
+// value loads and then its gathers all in flight at once, with no predicated
+// or sequential tail (the slice width is uniform across the warp, so the
+// dispatch does not diverge).  Wider rows take rounds of XM.  XM bounds the
+// registers of the kernel: 16 for whole rows (15 entries on a tetrahedral
+// mesh of a cube), 8 for the strict triangles (7).
+
+template <int W, class T, class CI, class V, class G>
+__device__ __forceinline__ T sell_fixed(CI ci, const V* __restrict__ val, int32_t off, int lane,
+                                        int32_t i, G g, T s) {
+  int32_t cc[W];
+  T vv[W];
+#pragma unroll
+  for (int u = 0; u < W; ++u) {
+    const int32_t e = off + u * kSlice + lane;
+    const int32_t c = ci.at(e, i);
+    vv[u] = c < 0 ? T(0) : T(ldv(val + e));
+    cc[u] = c < 0 ? i : c;
+  }
+#pragma unroll
+  for (int u = 0; u < W; ++u) s += vv[u] * g(cc[u]);
+  return s;
+}
+
+template <int W, int XM, class T, class CI, class V, class G>
+__device__ __forceinline__ T sell_tail(int r, CI ci, const V* __restrict__ val, int32_t off,
+                                       int lane, int32_t i, G g, T s) {
+  if constexpr (W <= XM) {
+    if (r == W) return sell_fixed<W, T>(ci, val, off, lane, i, g, s);
+    return sell_tail<W + 1, XM, T>(r, ci, val, off, lane, i, g, s);
+  } else {
+    return s;
+  }
+}
+
+template <class T, int XM = 16, class CI, class V, class G>
+__device__ __forceinline__ T sell_row_x(CI ci, const V* __restrict__ val, int32_t off, int w,
+                                        int lane, int32_t i, G g) {
+  T s = T(0);
+  int k = 0;
+  for (; w - k > XM; k += XM) s = sell_fixed<XM, T>(ci, val, off + k * kSlice, lane, i, g, s);
+  if (w > k) s = sell_tail<1, XM, T>(w - k, ci, val, off + k * kSlice, lane, i, g, s);
+  return s;
+}
+
 // One wave of resident blocks of kernel K for n rows.
 int g_nsm = 0;
 template <auto K>
@@ -271,7 +320,7 @@ __global__ void __launch_bounds__(kBlock) k_spmv(int64_t n, const int32_t* __res
                                                  double* __restrict__ y) {
   XG_ROWS(i, n) {
     const int lane = int(i & 31);
-    y[i] = sell_row<4, double>(Cols32{col}, a, soff[i >> 5], sw[i >> 5], lane, int32_t(i),
+    y[i] = sell_row_x<double>(Cols32{col}, a, soff[i >> 5], sw[i >> 5], lane, int32_t(i),
                                [&](int32_t c) { return __ldg(x + c); });
   }
 }
@@ -343,7 +392,7 @@ __global__ void __launch_bounds__(kBlock) k_setup(int64_t n, const int32_t* __re
   const int pc = sc->pc;
   XG_ROWS(i, n) {
     const int lane = int(i & 31);
-    const double s = sell_row<4, double>(Cols32{col}, a, soff[i >> 5], sw[i >> 5], lane,
+    const double s = sell_row_x<double>(Cols32{col}, a, soff[i >> 5], sw[i >> 5], lane,
                                          int32_t(i), [&](int32_t c) { return x[c]; });
     const double ri = b[i] - s;
     // the inverse Jacobi diagonal: one multiply per row and iteration in
@@ -417,14 +466,14 @@ __global__ void __launch_bounds__(kBlock) k_cg_a(int64_t n, const int32_t* __res
   XG_ROWS(i, n) {
     const int lane = int(i & 31);
     if (PF) {
-      const T s = sell_row<4, T>(ci, a, soff[i >> 5], sw[i >> 5], lane, int32_t(i),
+      const T s = sell_row_x<T>(ci, a, soff[i >> 5], sw[i >> 5], lane, int32_t(i),
                                  [&](int32_t c) { return __ldg(z + c) + beta * __ldg(pold + c); });
       const T pi = z[i] + beta * pold[i];
       pnew[i] = pi;
       q[i] = s;
       dot += pi * s;
     } else {
-      const T s = sell_row<4, T>(ci, a, soff[i >> 5], sw[i >> 5], lane, int32_t(i),
+      const T s = sell_row_x<T>(ci, a, soff[i >> 5], sw[i >> 5], lane, int32_t(i),
                                  [&](int32_t c) { return __ldg(p0 + c); });
       q[i] = s;
       dot += p0[i] * s;
@@ -538,7 +587,7 @@ __global__ void __launch_bounds__(kBlock) k_pc_upper(int64_t n, const int32_t* _
   if (sc->done) return;
   XG_ROWS(i, n) {
     const int lane = int(i & 31);
-    u[i] = vs[i] + sell_row<4, T>(ci, nvU, soffU[i >> 5], swU[i >> 5], lane, int32_t(i),
+    u[i] = vs[i] + sell_row_x<T, 8>(ci, nvU, soffU[i >> 5], swU[i >> 5], lane, int32_t(i),
                                   [&](int32_t c) { return __ldg(vs + c); });
   }
 }
@@ -567,7 +616,7 @@ __global__ void __launch_bounds__(kBlock) k_pc_upper_res(
     rnew[i] = ri;
     e[i] += alpha * p[i];
     u[i] = srow[i] * ri +
-           sell_row<4, float>(ci, nvU, soffU[i >> 5], swU[i >> 5], lane, int32_t(i),
+           sell_row_x<float, 8>(ci, nvU, soffU[i >> 5], swU[i >> 5], lane, int32_t(i),
                               [&](int32_t c) {
                                 return __ldg(srow + c) * (__ldg(rold + c) - alpha * __ldg(q + c));
                               });
@@ -596,7 +645,7 @@ __global__ void __launch_bounds__(kBlock) k_pc_lower(int64_t n, const int32_t* _
   T rz = T(0), rr = T(0);  // per thread in T (FP32 for the mixed solver), widened once
   XG_ROWS(i, n) {
     const int lane = int(i & 31);
-    const T acc = u[i] + sell_row<4, T>(ci, nvL, soffL[i >> 5], swL[i >> 5], lane, int32_t(i),
+    const T acc = u[i] + sell_row_x<T, 8>(ci, nvL, soffL[i >> 5], swL[i >> 5], lane, int32_t(i),
                                         [&](int32_t c) { return __ldg(u + c); });
     const T ri = r[i];
     const T zi = mask[i] ? ri : -T(srow[i]) * acc;
@@ -656,7 +705,7 @@ __global__ void __launch_bounds__(kBlock) k_outer_res(int64_t n, const int32_t* 
   double v[2] = {0.0, 0.0};
   XG_ROWS(i, n) {
     const int lane = int(i & 31);
-    const double s = sell_row<4, double>(Cols32{col}, a, soff[i >> 5], sw[i >> 5], lane,
+    const double s = sell_row_x<double>(Cols32{col}, a, soff[i >> 5], sw[i >> 5], lane,
                                          int32_t(i), [&](int32_t c) { return __ldg(x + c); });
     const double ri = b[i] - s;
     const float rf = float(ri);
