@@ -309,6 +309,42 @@ unsigned pgrid(int64_t n) {
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < (n); \
        i += int64_t(gridDim.x) * blockDim.x)
 
+// ---------------------------------------------------------------- launches
+
+// The iteration kernels are launched as programmatic dependents of the
+// kernel before them in the stream: their blocks may be scheduled while that
+// kernel drains (its blocks trigger after their row loop, before the
+// reduction tail) and wait in griddep_wait() until it has completed and its
+// writes are visible.  Every kernel launched with launch_dep() calls
+// griddep_wait() before it reads anything.
+__device__ __forceinline__ void griddep_wait() {
+  asm volatile("griddepcontrol.wait;\n" ::: "memory");
+}
+__device__ __forceinline__ void griddep_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+}
+
+template <class... P, class... A>
+void launch_dep_k(void (*k)(P...), unsigned grid, cudaStream_t s, A&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(kBlock);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  (void)cudaLaunchKernelEx(&cfg, k, std::forward<A>(args)...);  // errors: cudaGetLastError
+}
+
+// Kernel K over n rows, one wave of resident blocks, as a dependent launch.
+template <auto K, class... A>
+void launch_dep(int64_t n, cudaStream_t s, A&&... args) {
+  launch_dep_k(K, pgrid<K>(n), s, std::forward<A>(args)...);
+}
+
 // ---------------------------------------------------------------- kernels
 
 // CSR::mult on the original values: y = A x.
@@ -441,9 +477,11 @@ __device__ __forceinline__ T block_beta(const CGScalars* sc) {
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_cg_p(int64_t n, const T* __restrict__ z,
                                                   T* __restrict__ p, const CGScalars* sc) {
+  griddep_wait();
   if (sc->done) return;
   const T beta = block_beta<T>(sc);
   XG_ROWS(i, n) p[i] = z[i] + beta * p[i];
+  griddep_trigger();
 }
 
 // q = A p', (p', q).  PF: p' = z + beta p formed per gathered entry and
@@ -457,6 +495,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_a(int64_t n, const int32_t* __res
                                                   const T* __restrict__ z, T* p0, T* p1,
                                                   T* __restrict__ q, double* partial,
                                                   CGScalars* sc) {
+  griddep_wait();
   if (sc->done) return;
   const int64_t it = sc->it;
   const T beta = PF ? block_beta<T>(sc) : T(0);
@@ -479,6 +518,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_a(int64_t n, const int32_t* __res
       dot += p0[i] * s;
     }
   }
+  griddep_trigger();
   T v[1] = {dot};
   if (block_partials<1>(v, partial, &sc->ticket[1])) {
     double pq = sum_partials(partial, 0);
@@ -536,6 +576,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_b(int64_t n, const T* __restrict_
                                                   T* __restrict__ r, T* __restrict__ z,
                                                   T* __restrict__ vs, T* __restrict__ x,
                                                   double* partial, CGScalars* sc) {
+  griddep_wait();
   if (sc->done) return;
   const T alpha = T(sc->alpha);
   // the p' of this iteration (k_cg_a wrote it; the count advances below, or
@@ -550,6 +591,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_b(int64_t n, const T* __restrict_
       x[i] += alpha * p[i];
       vs[i] = T(srow[i]) * ri;
     }
+    griddep_trigger();
     return;
   }
   T rz = T(0), rr = T(0);  // per thread in T, widened in block_partials
@@ -562,6 +604,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_b(int64_t n, const T* __restrict_
     rz += ri * zi;
     rr += ri * ri;
   }
+  griddep_trigger();
   const T v[2] = {rz, rr};
   if (block_partials<2>(v, partial, &sc->ticket[2])) {
     double rz = sum_partials(partial, 0);
@@ -584,6 +627,7 @@ __global__ void __launch_bounds__(kBlock) k_pc_upper(int64_t n, const int32_t* _
                                                       const T* __restrict__ vs,
                                                       T* __restrict__ u,
                                                       const CGScalars* __restrict__ sc) {
+  griddep_wait();
   if (sc->done) return;
   XG_ROWS(i, n) {
     const int lane = int(i & 31);
@@ -604,6 +648,7 @@ __global__ void __launch_bounds__(kBlock) k_pc_upper_res(
     const __half* __restrict__ nvU, const float* __restrict__ srow, const float* __restrict__ q,
     const float* p0, const float* p1, float* ra, float* rb, float* __restrict__ e,
     float* __restrict__ u, const CGScalars* __restrict__ sc) {
+  griddep_wait();
   if (sc->done) return;
   const float alpha = float(sc->alpha);
   const int64_t it = sc->it;
@@ -637,6 +682,7 @@ __global__ void __launch_bounds__(kBlock) k_pc_lower(int64_t n, const int32_t* _
                                                       const T* r_even, const T* r_odd,
                                                       T* __restrict__ z, double* partial,
                                                       CGScalars* sc) {
+  griddep_wait();
   if (sc->done) return;
   // the residual: r_even unless it alternates (r_odd given), then the one
   // k_pc_upper_res wrote (MODE 2) or the current one (MODE 0)
@@ -653,6 +699,7 @@ __global__ void __launch_bounds__(kBlock) k_pc_lower(int64_t n, const int32_t* _
     rz += ri * zi;
     if (MODE > 0) rr += ri * ri;
   }
+  griddep_trigger();
   T v[2] = {rz, rr};
   if (MODE == 0) {
     T w[1] = {v[0]};
@@ -903,13 +950,10 @@ int factor_apply64(xg_ctx* c, CGDev* d, const double* r, double* z) {
   cudaStream_t s = c->stream;
   const int64_t n = d->n;
   k_scale<double><<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, d->srow, r, d->v);
-  k_pc_upper<double, float, Cols32>
-      <<<pgrid<k_pc_upper<double, float, Cols32>>(n), kBlock, 0, s>>>(
-          n, d->soffU, d->swU, Cols32{d->colU}, d->nvU, d->v, d->u, d->scal);
-  k_pc_lower<double, float, Cols32, 0>
-      <<<pgrid<k_pc_lower<double, float, Cols32, 0>>(n), kBlock, 0, s>>>(
-          n, d->soffL, d->swL, Cols32{d->colL}, d->nvL, d->srow, d->bcmask, d->u, r, nullptr, z,
-          d->partial, d->scal);
+  launch_dep<k_pc_upper<double, float, Cols32>>(n, s, n, d->soffU, d->swU, Cols32{d->colU}, d->nvU,
+      d->v, d->u, d->scal);
+  launch_dep<k_pc_lower<double, float, Cols32, 0>>(n, s, n, d->soffL, d->swL, Cols32{d->colL},
+      d->nvL, d->srow, d->bcmask, d->u, r, nullptr, z, d->partial, d->scal);
   XG_CHECK_LAUNCH(c);
   return XG_OK;
 }
@@ -920,11 +964,10 @@ template <class CI>
 void factor_apply32(xg_ctx* c, CGDev* d, CI cu, CI cl) {
   cudaStream_t s = c->stream;
   const int64_t n = d->n;
-  k_pc_upper<float, __half, CI><<<pgrid<k_pc_upper<float, __half, CI>>(n), kBlock, 0, s>>>(
-      n, d->soffU, d->swU, cu, d->hvU, d->v32, d->u32, d->scal);
-  k_pc_lower<float, __half, CI, 0><<<pgrid<k_pc_lower<float, __half, CI, 0>>(n), kBlock, 0, s>>>(
-      n, d->soffL, d->swL, cl, d->hvL, d->srow, d->bcmask, d->u32, d->r32, d->r32b, d->z32,
-      d->partial, d->scal);
+  launch_dep<k_pc_upper<float, __half, CI>>(n, s, n, d->soffU, d->swU, cu, d->hvU, d->v32, d->u32,
+      d->scal);
+  launch_dep<k_pc_lower<float, __half, CI, 0>>(n, s, n, d->soffL, d->swL, cl, d->hvL, d->srow,
+      d->bcmask, d->u32, d->r32, d->r32b, d->z32, d->partial, d->scal);
 }
 
 int cg_iterate(xg_ctx* c, CGDev* d, int64_t maxit, double tol, CGScalars* h) {
@@ -936,24 +979,19 @@ int cg_iterate(xg_ctx* c, CGDev* d, int64_t maxit, double tol, CGScalars* h) {
   for (;;) {
     for (int k = 0; k < kBatch; ++k) {
       double* p0 = d->p[0];
-      k_cg_p<double><<<pgrid<k_cg_p<double>>(n), kBlock, 0, s>>>(n, d->z, p0, d->scal);
-      k_cg_a<double, double, Cols32, false>
-          <<<pgrid<k_cg_a<double, double, Cols32, false>>(n), kBlock, 0, s>>>(
-              n, d->soff, d->swidth, Cols32{d->col}, d->a, d->z, p0, p0, d->q, d->partial,
-              d->scal);
+      launch_dep<k_cg_p<double>>(n, s, n, d->z, p0, d->scal);
+      launch_dep<k_cg_a<double, double, Cols32, false>>(n, s, n, d->soff, d->swidth, Cols32{d->col},
+          d->a, d->z, p0, p0, d->q, d->partial, d->scal);
       if (d->pc == 2) {
-        k_cg_b<double, true, false><<<pgrid<k_cg_b<double, true, false>>(n), kBlock, 0, s>>>(
-            n, d->q, d->d, p0, p0, d->srow, d->r, d->z, d->v, d->x, d->partial, d->scal);
-        k_pc_upper<double, float, Cols32>
-            <<<pgrid<k_pc_upper<double, float, Cols32>>(n), kBlock, 0, s>>>(
-                n, d->soffU, d->swU, Cols32{d->colU}, d->nvU, d->v, d->u, d->scal);
-        k_pc_lower<double, float, Cols32, 1>
-            <<<pgrid<k_pc_lower<double, float, Cols32, 1>>(n), kBlock, 0, s>>>(
-                n, d->soffL, d->swL, Cols32{d->colL}, d->nvL, d->srow, d->bcmask, d->u, d->r,
-                nullptr, d->z, d->partial, d->scal);
+        launch_dep<k_cg_b<double, true, false>>(n, s, n, d->q, d->d, p0, p0, d->srow, d->r, d->z,
+            d->v, d->x, d->partial, d->scal);
+        launch_dep<k_pc_upper<double, float, Cols32>>(n, s, n, d->soffU, d->swU, Cols32{d->colU},
+            d->nvU, d->v, d->u, d->scal);
+        launch_dep<k_pc_lower<double, float, Cols32, 1>>(n, s, n, d->soffL, d->swL, Cols32{d->colL},
+            d->nvL, d->srow, d->bcmask, d->u, d->r, nullptr, d->z, d->partial, d->scal);
       } else {
-        k_cg_b<double, false, false><<<pgrid<k_cg_b<double, false, false>>(n), kBlock, 0, s>>>(
-            n, d->q, d->d, p0, p0, d->srow, d->r, d->z, d->v, d->x, d->partial, d->scal);
+        launch_dep<k_cg_b<double, false, false>>(n, s, n, d->q, d->d, p0, p0, d->srow, d->r, d->z,
+            d->v, d->x, d->partial, d->scal);
       }
     }
     XG_CHECK_LAUNCH(c);
@@ -973,20 +1011,16 @@ int mixed_batch(xg_ctx* c, CGDev* d, CI ca, CI cu, CI cl) {
   const int64_t n = d->n;
   for (int k = 0; k < kBatch; ++k) {
     float *p0 = d->p32[0], *p1 = d->p32[1];
-    k_cg_a<float, float, CI, true><<<pgrid<k_cg_a<float, float, CI, true>>(n), kBlock, 0, s>>>(
-        n, d->soff, d->swidth, ca, d->a32, d->z32, p0, p1, d->q32, d->partial, d->scal);
+    launch_dep<k_cg_a<float, float, CI, true>>(n, s, n, d->soff, d->swidth, ca, d->a32, d->z32, p0,
+        p1, d->q32, d->partial, d->scal);
     if (d->pc == 2) {
-      k_pc_upper_res<CI><<<pgrid<k_pc_upper_res<CI>>(n), kBlock, 0, s>>>(
-          n, d->soffU, d->swU, cu, d->hvU, d->srow, d->q32, p0, p1, d->r32, d->r32b, d->e32,
-          d->u32, d->scal);
-      k_pc_lower<float, __half, CI, 2>
-          <<<pgrid<k_pc_lower<float, __half, CI, 2>>(n), kBlock, 0, s>>>(
-              n, d->soffL, d->swL, cl, d->hvL, d->srow, d->bcmask, d->u32, d->r32, d->r32b,
-              d->z32, d->partial, d->scal);
+      launch_dep<k_pc_upper_res<CI>>(n, s, n, d->soffU, d->swU, cu, d->hvU, d->srow, d->q32, p0, p1,
+          d->r32, d->r32b, d->e32, d->u32, d->scal);
+      launch_dep<k_pc_lower<float, __half, CI, 2>>(n, s, n, d->soffL, d->swL, cl, d->hvL, d->srow,
+          d->bcmask, d->u32, d->r32, d->r32b, d->z32, d->partial, d->scal);
     } else {
-      k_cg_b<float, false, true><<<pgrid<k_cg_b<float, false, true>>(n), kBlock, 0, s>>>(
-          n, d->q32, d->d32, p0, p1, d->srow, d->r32, d->z32, d->v32, d->e32, d->partial,
-          d->scal);
+      launch_dep<k_cg_b<float, false, true>>(n, s, n, d->q32, d->d32, p0, p1, d->srow, d->r32,
+          d->z32, d->v32, d->e32, d->partial, d->scal);
     }
   }
   XG_CHECK_LAUNCH(c);
