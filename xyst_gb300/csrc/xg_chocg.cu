@@ -58,7 +58,10 @@ struct ChoCGDev {
   xg_chocg_params prm{};
   int32_t *soff = nullptr, *swidth = nullptr, *nbr = nullptr;
   Coef4* dd = nullptr;
+  double* sdl = nullptr;  // per entry |d| / edge length (the pressure damping of chorin::div)
   int32_t *bidx = nullptr, *bptr = nullptr, *bent = nullptr, *btri = nullptr;
+  int32_t* bnode = nullptr;  // boundary index -> node
+  double* park = nullptr;    // [nbn][9] domain sums of boundary nodes between passes
   double *xyz = nullptr, *vol = nullptr;
   double *u = nullptr, *u2 = nullptr, *un = nullptr, *pr = nullptr, *pgrad = nullptr,
          *vgrad = nullptr, *div = nullptr, *flx = nullptr, *stage = nullptr;
@@ -84,6 +87,7 @@ struct ChoAdj {
   const int32_t* swidth;
   const int32_t* nbr;
   const Coef4* dd;
+  const double* sdl;
 };
 struct ChoBnd {
   const int32_t* bidx;
@@ -91,7 +95,31 @@ struct ChoBnd {
   const int32_t* bent;  // (triangle << 2) | position of the node in it
   const int32_t* btri;
   const double* xyz;    // SoA coordinates
+  const int32_t* bnode;  // boundary index -> node
+  double* park;          // [nb][9]: a boundary node's domain sum between the passes
+  int64_t nb;
 };
+
+// Every node kernel runs as two passes.  The domain pass (one thread per
+// node) sums the edge terms; a boundary node parks that sum and returns.  The
+// boundary pass (one thread per boundary node) adds the boundary-triangle
+// terms in the reference's order and applies the epilogue.  Folded into the
+// domain pass, the few boundary nodes of a warp held all 32 lanes for their
+// triangle loops.
+__device__ __forceinline__ bool node_of(bool bnd_pass, int64_t n, const ChoBnd& b, int64_t& p,
+                                        int32_t& bi) {
+  const int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (bnd_pass) {
+    if (t >= b.nb) return false;
+    bi = static_cast<int32_t>(t);
+    p = __ldg(b.bnode + t);
+  } else {
+    if (t >= n) return false;
+    p = t;
+    bi = -1;
+  }
+  return true;
+}
 
 __device__ __forceinline__ Coef4 ldd4(const Coef4* p) {
   const double2* q = reinterpret_cast<const double2*>(p);
@@ -146,6 +174,44 @@ __device__ __forceinline__ void block_min(double v, unsigned long long* dst) {
   }
 }
 
+// Calls f(e, q, first) for the adjacency entries of a node in entry order
+// (q the neighbour, first: the node is the edge's canonical first end), in
+// rounds fully unrolled to exactly the entries left, at most XM (the slice
+// width is uniform across the warp, so the dispatch does not diverge).  A
+// round loads its neighbour ids first, so that its gathers are in flight
+// together instead of one entry's load chain after another.
+template <int R, class F>
+__device__ __forceinline__ void adj_round(const int32_t* __restrict__ nbr, int32_t e0, F& f) {
+  int32_t qq[R];
+#pragma unroll
+  for (int u = 0; u < R; ++u) qq[u] = __ldg(nbr + e0 + u * kSlice);
+#pragma unroll
+  for (int u = 0; u < R; ++u) {
+    const int32_t q = qq[u];
+    if (q != kPad) f(e0 + u * kSlice, q >= 0 ? q : ~q, q >= 0);
+  }
+}
+
+template <int R, int XM, class F>
+__device__ __forceinline__ void adj_tail(int r, const int32_t* __restrict__ nbr, int32_t e0,
+                                         F& f) {
+  if constexpr (R <= XM) {
+    if (r == R) {
+      adj_round<R>(nbr, e0, f);
+      return;
+    }
+    adj_tail<R + 1, XM>(r, nbr, e0, f);
+  }
+}
+
+template <int XM, class F>
+__device__ __forceinline__ void for_adj(const ChoAdj& adj, int32_t off, int w, int lane, F f) {
+  const int32_t e0 = off + lane;
+  int k = 0;
+  for (; w - k > XM; k += XM) adj_round<XM>(adj.nbr, e0 + k * kSlice, f);
+  if (w > k) adj_tail<1, XM>(w - k, adj.nbr, e0 + k * kSlice, f);
+}
+
 // What the gradient kernel does with a node's gradient g of NC components.
 enum GradOut { GRAD_RAW = 0, GRAD_DIVIDE = 1, GRAD_PROJECT = 2 };
 
@@ -155,46 +221,50 @@ enum GradOut { GRAD_RAW = 0, GRAD_DIVIDE = 1, GRAD_PROJECT = 2 };
 // GRAD_PROJECT (NC = 1, the pressure increment) applies the projection of
 // ChoCG::psolved (src/Inciter/ChoCG.cpp:1204-1216): u -= dt G/vol, and with
 // addp the pressure update pr += increment (src/Inciter/ChoCG.cpp:1246-1250).
-template <int NC, int MODE>
+template <int NC, int MODE, bool BND>
 __global__ void __launch_bounds__(kBlock) k_cgrad(int64_t n, ChoAdj adj, const double* U,
                                                    ChoBnd bnd, const double* __restrict__ vol,
                                                    double* __restrict__ G, double dt, int addp,
                                                    double* u, double* pr) {
-  const int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  if (p >= n) return;
-  const int lane = static_cast<int>(p & (kSlice - 1));
-  const int64_t s = p >> 5;
-  const int32_t off = __ldg(adj.soff + s), w = __ldg(adj.swidth + s);
+  int64_t p;
+  int32_t bi;
+  if (!node_of(BND, n, bnd, p, bi)) return;
   double up[NC];
 #pragma unroll
   for (int i = 0; i < NC; ++i) up[i] = U[i * n + p];
   double g[3 * NC];
+  if (!BND) {
 #pragma unroll
-  for (int i = 0; i < 3 * NC; ++i) g[i] = 0.0;
-  for (int k = 0; k < w; ++k) {
-    const int32_t e = off + k * kSlice + lane;
-    int32_t q = __ldg(adj.nbr + e);
-    if (q == kPad) continue;
-    const bool first = q >= 0;
-    if (!first) q = ~q;
-    const Coef4 d = ldd4(adj.dd + e);
+    for (int i = 0; i < 3 * NC; ++i) g[i] = 0.0;
+    const int lane = static_cast<int>(p & (kSlice - 1));
+    const int64_t s = p >> 5;
+    const int32_t off = __ldg(adj.soff + s), w = __ldg(adj.swidth + s);
+    for_adj<NC == 1 ? 16 : 8>(adj, off, w, lane, [&](int32_t e, int32_t q, bool first) {
+      const Coef4 d = ldd4(adj.dd + e);
 #pragma unroll
-    for (int i = 0; i < NC; ++i) {
-      const double sum = U[i * n + q] + up[i];
-      const double f0 = d.x * sum, f1 = d.y * sum, f2 = d.z * sum;
-      if (first) {
-        g[i * 3 + 0] -= f0;
-        g[i * 3 + 1] -= f1;
-        g[i * 3 + 2] -= f2;
-      } else {
-        g[i * 3 + 0] += f0;
-        g[i * 3 + 1] += f1;
-        g[i * 3 + 2] += f2;
+      for (int i = 0; i < NC; ++i) {
+        const double sum = U[i * n + q] + up[i];
+        const double f0 = d.x * sum, f1 = d.y * sum, f2 = d.z * sum;
+        if (first) {
+          g[i * 3 + 0] -= f0;
+          g[i * 3 + 1] -= f1;
+          g[i * 3 + 2] -= f2;
+        } else {
+          g[i * 3 + 0] += f0;
+          g[i * 3 + 1] += f1;
+          g[i * 3 + 2] += f2;
+        }
       }
+    });
+    const int32_t b = __ldg(bnd.bidx + p);
+    if (b >= 0) {
+#pragma unroll
+      for (int i = 0; i < 3 * NC; ++i) bnd.park[b * 9 + i] = g[i];
+      return;
     }
-  }
-  const int32_t bi = __ldg(bnd.bidx + p);
-  if (bi >= 0) {
+  } else {
+#pragma unroll
+    for (int i = 0; i < 3 * NC; ++i) g[i] = bnd.park[bi * 9 + i];
     for (int32_t j = __ldg(bnd.bptr + bi); j < __ldg(bnd.bptr + bi + 1); ++j) {
       const int32_t ent = __ldg(bnd.bent + j);
       const int pos = ent & 3;
@@ -227,44 +297,48 @@ __global__ void __launch_bounds__(kBlock) k_cgrad(int64_t n, ChoAdj adj, const d
 // chorin::div (Chorin.cpp:34-209): divergence of the 3-component U with the
 // 4th-order pressure damping when stab, optionally divided by dt
 // (ChoCG::pinit, src/Inciter/ChoCG.cpp:1039).
+template <bool BND>
 __global__ void __launch_bounds__(kBlock) k_cdiv(int64_t n, ChoAdj adj, const double* U,
                                                   const double* __restrict__ P,
                                                   const double* __restrict__ PG, ChoBnd bnd,
                                                   double dt, int stab, int bydt,
                                                   double* __restrict__ D) {
-  const int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  if (p >= n) return;
-  const int lane = static_cast<int>(p & (kSlice - 1));
-  const int64_t s = p >> 5;
-  const int32_t off = __ldg(adj.soff + s), w = __ldg(adj.swidth + s);
-  const double* x = bnd.xyz;
-  const double* y = bnd.xyz + n;
-  const double* z = bnd.xyz + 2 * n;
+  int64_t p;
+  int32_t bi;
+  if (!node_of(BND, n, bnd, p, bi)) return;
   double acc = 0.0;
-  for (int k = 0; k < w; ++k) {
-    const int32_t e = off + k * kSlice + lane;
-    int32_t q = __ldg(adj.nbr + e);
-    if (q == kPad) continue;
-    const bool first = q >= 0;
-    if (!first) q = ~q;
-    const Coef4 d = ldd4(adj.dd + e);
-    const int64_t a = first ? p : q, b = first ? q : p;  // canonical ends
-    double f = d.x * (U[a] + U[b]) + d.y * (U[n + a] + U[n + b]) +
-               d.z * (U[2 * n + a] + U[2 * n + b]);
-    if (stab) {
-      const double dx = x[a] - x[b], dy = y[a] - y[b], dz = z[a] - z[b];
-      const double dl = sqrt(dx * dx + dy * dy + dz * dz);
-      const double p2 = P[b] - P[a];
-      const double Dn = sqrt(d.x * d.x + d.y * d.y + d.z * d.z);
-      const double dpx = PG[a] + PG[b], dpy = PG[n + a] + PG[n + b],
-                   dpz = PG[2 * n + a] + PG[2 * n + b];
-      const double p4 = 0.5 * (dx * dpx + dy * dpy + dz * dpz);
-      f += Dn * dt / dl * (p2 + p4);
+  if (!BND) {
+    const int lane = static_cast<int>(p & (kSlice - 1));
+    const int64_t s = p >> 5;
+    const int32_t off = __ldg(adj.soff + s), w = __ldg(adj.swidth + s);
+    const double* x = bnd.xyz;
+    const double* y = bnd.xyz + n;
+    const double* z = bnd.xyz + 2 * n;
+    for_adj<8>(adj, off, w, lane, [&](int32_t e, int32_t q, bool first) {
+      const Coef4 d = ldd4(adj.dd + e);
+      const int64_t a = first ? p : q, b = first ? q : p;  // canonical ends
+      double f = d.x * (U[a] + U[b]) + d.y * (U[n + a] + U[n + b]) +
+                 d.z * (U[2 * n + a] + U[2 * n + b]);
+      if (stab) {
+        // |d| / |x_a - x_b| is geometric: formed once at setup (two FP64
+        // square roots and a division per edge and call are expensive on
+        // GB300's FP64 pipe)
+        const double dx = x[a] - x[b], dy = y[a] - y[b], dz = z[a] - z[b];
+        const double p2 = P[b] - P[a];
+        const double dpx = PG[a] + PG[b], dpy = PG[n + a] + PG[n + b],
+                     dpz = PG[2 * n + a] + PG[2 * n + b];
+        const double p4 = 0.5 * (dx * dpx + dy * dpy + dz * dpz);
+        f += __ldg(adj.sdl + e) * dt * (p2 + p4);
+      }
+      acc = first ? acc - f : acc + f;
+    });
+    const int32_t b = __ldg(bnd.bidx + p);
+    if (b >= 0) {
+      bnd.park[b * 9] = acc;
+      return;
     }
-    acc = first ? acc - f : acc + f;
-  }
-  const int32_t bi = __ldg(bnd.bidx + p);
-  if (bi >= 0) {
+  } else {
+    acc = bnd.park[bi * 9];
     for (int32_t j = __ldg(bnd.bptr + bi); j < __ldg(bnd.bptr + bi + 1); ++j) {
       const int32_t ent = __ldg(bnd.bent + j);
       const int pos = ent & 3;
@@ -305,35 +379,40 @@ __device__ __forceinline__ double mflux_p(const double* U, const double* G, int6
 
 // chorin::flux (Chorin.cpp:509-638): F_i = d[s_ij - u_i u_j]/dx_j, raw or
 // divided by the volume (ChoCG::div at start-up, src/Inciter/ChoCG.cpp:877).
+template <bool BND>
 __global__ void __launch_bounds__(kBlock) k_cflux(int64_t n, ChoAdj adj, const double* U,
                                                    const double* G, ChoBnd bnd,
                                                    const double* __restrict__ vol, double mu,
                                                    int divide, double* __restrict__ F) {
-  const int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  if (p >= n) return;
-  const int lane = static_cast<int>(p & (kSlice - 1));
-  const int64_t s = p >> 5;
-  const int32_t off = __ldg(adj.soff + s), w = __ldg(adj.swidth + s);
+  int64_t p;
+  int32_t bi;
+  if (!node_of(BND, n, bnd, p, bi)) return;
   double acc[3] = {0.0, 0.0, 0.0};
-  for (int k = 0; k < w; ++k) {
-    const int32_t e = off + k * kSlice + lane;
-    int32_t q = __ldg(adj.nbr + e);
-    if (q == kPad) continue;
-    const bool first = q >= 0;
-    if (!first) q = ~q;
-    const Coef4 d = ldd4(adj.dd + e);
-    const int64_t a = first ? p : q, b = first ? q : p;
-    const double dj[3] = {d.x, d.y, d.z};
+  if (!BND) {
+    const int lane = static_cast<int>(p & (kSlice - 1));
+    const int64_t s = p >> 5;
+    const int32_t off = __ldg(adj.soff + s), w = __ldg(adj.swidth + s);
+    for_adj<4>(adj, off, w, lane, [&](int32_t e, int32_t q, bool first) {
+      const Coef4 d = ldd4(adj.dd + e);
+      const int64_t a = first ? p : q, b = first ? q : p;
+      const double dj[3] = {d.x, d.y, d.z};
 #pragma unroll
-    for (int i = 0; i < 3; ++i)
+      for (int i = 0; i < 3; ++i)
 #pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        const double f = dj[j] * mflux_e(U, G, n, i, j, b, a, mu);
-        acc[i] = first ? acc[i] - f : acc[i] + f;
-      }
-  }
-  const int32_t bi = __ldg(bnd.bidx + p);
-  if (bi >= 0) {
+        for (int j = 0; j < 3; ++j) {
+          const double f = dj[j] * mflux_e(U, G, n, i, j, b, a, mu);
+          acc[i] = first ? acc[i] - f : acc[i] + f;
+        }
+    });
+    const int32_t b = __ldg(bnd.bidx + p);
+    if (b >= 0) {
+#pragma unroll
+      for (int i = 0; i < 3; ++i) bnd.park[b * 9 + i] = acc[i];
+      return;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) acc[i] = bnd.park[bi * 9 + i];
     for (int32_t jb = __ldg(bnd.bptr + bi); jb < __ldg(bnd.bptr + bi + 1); ++jb) {
       const int32_t ent = __ldg(bnd.bent + jb);
       const int pos = ent & 3;
@@ -417,33 +496,37 @@ __device__ __forceinline__ void adv_edge(const double* U, const double* G, const
 // stage update of ChoCG::solve (src/Inciter/ChoCG.cpp:1550-1566):
 // u_out = un - dtk R / vol, where un is this stage's input at stage 0.
 // With dtk == 0 and a null u_out only R is written (drop-in).
-template <bool DAMP4>
+template <bool DAMP4, bool BND>
 __global__ void __launch_bounds__(kBlock) k_crhs(int64_t n, ChoAdj adj, const double* U,
                                                   const double* G, const double* P, ChoBnd bnd,
                                                   AdvPrm ap, const double* __restrict__ vol,
                                                   double dtk, int stage0, double* un,
                                                   double* __restrict__ uout,
                                                   double* __restrict__ R) {
-  const int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  if (p >= n) return;
-  const int lane = static_cast<int>(p & (kSlice - 1));
-  const int64_t s = p >> 5;
-  const int32_t off = __ldg(adj.soff + s), w = __ldg(adj.swidth + s);
+  int64_t p;
+  int32_t bi;
+  if (!node_of(BND, n, bnd, p, bi)) return;
   double acc[3] = {0.0, 0.0, 0.0};
-  for (int k = 0; k < w; ++k) {
-    const int32_t e = off + k * kSlice + lane;
-    int32_t q = __ldg(adj.nbr + e);
-    if (q == kPad) continue;
-    const bool first = q >= 0;
-    if (!first) q = ~q;
-    const Coef4 d = ldd4(adj.dd + e);
-    double f[3];
-    adv_edge<DAMP4>(U, G, P, bnd.xyz, n, d, first ? p : q, first ? q : p, ap, f);
+  if (!BND) {
+    const int lane = static_cast<int>(p & (kSlice - 1));
+    const int64_t s = p >> 5;
+    const int32_t off = __ldg(adj.soff + s), w = __ldg(adj.swidth + s);
+    for_adj<DAMP4 ? 4 : 8>(adj, off, w, lane, [&](int32_t e, int32_t q, bool first) {
+      const Coef4 d = ldd4(adj.dd + e);
+      double f[3];
+      adv_edge<DAMP4>(U, G, P, bnd.xyz, n, d, first ? p : q, first ? q : p, ap, f);
 #pragma unroll
-    for (int c = 0; c < 3; ++c) acc[c] = first ? acc[c] - f[c] : acc[c] + f[c];
-  }
-  const int32_t bi = __ldg(bnd.bidx + p);
-  if (bi >= 0) {
+      for (int c = 0; c < 3; ++c) acc[c] = first ? acc[c] - f[c] : acc[c] + f[c];
+    });
+    const int32_t b = __ldg(bnd.bidx + p);
+    if (b >= 0) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) bnd.park[b * 9 + c] = acc[c];
+      return;
+    }
+  } else {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) acc[c] = bnd.park[bi * 9 + c];
     for (int32_t j = __ldg(bnd.bptr + bi); j < __ldg(bnd.bptr + bi + 1); ++j) {
       const int32_t ent = __ldg(bnd.bent + j);
       const int pos = ent & 3;
@@ -549,8 +632,18 @@ __global__ void k_soa_aos(int64_t n, int nc, const double* __restrict__ s, doubl
 
 // ---------------------------------------------------------------- host side
 
-ChoAdj adj_of(ChoCGDev* d) { return ChoAdj{d->soff, d->swidth, d->nbr, d->dd}; }
-ChoBnd bnd_of(ChoCGDev* d) { return ChoBnd{d->bidx, d->bptr, d->bent, d->btri, d->xyz}; }
+ChoAdj adj_of(ChoCGDev* d) { return ChoAdj{d->soff, d->swidth, d->nbr, d->dd, d->sdl}; }
+ChoBnd bnd_of(ChoCGDev* d) {
+  return ChoBnd{d->bidx, d->bptr, d->bent, d->btri, d->xyz, d->bnode, d->park, d->nbn};
+}
+
+// Both passes of a node kernel (domain pass over the n nodes, then the
+// boundary pass over the boundary nodes), the same arguments to each.
+template <auto KD, auto KB, class... A>
+void two_pass(cudaStream_t s, int64_t n, int64_t nb, A... args) {
+  KD<<<blocks_for(n, kBlock), kBlock, 0, s>>>(args...);
+  if (nb > 0) KB<<<blocks_for(nb, kBlock), kBlock, 0, s>>>(args...);
+}
 AdvPrm adv_of(ChoCGDev* d) {
   return AdvPrm{d->prm.mu, d->prm.stab2coef, d->prm.stab != 0, d->prm.stab2 != 0};
 }
@@ -569,8 +662,8 @@ int get_ctx(xg_ctx* c, ChoCGDev** out, bool need_cg) {
 template <int NC, int MODE>
 int launch_grad(xg_ctx* c, ChoCGDev* d, const double* U, double* G, double dt = 0.0,
                 int addp = 0) {
-  k_cgrad<NC, MODE><<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(
-      d->n, adj_of(d), U, bnd_of(d), d->vol, G, dt, addp, d->u, d->pr);
+  two_pass<k_cgrad<NC, MODE, false>, k_cgrad<NC, MODE, true>>(
+      c->stream, d->n, d->nbn, d->n, adj_of(d), U, bnd_of(d), d->vol, G, dt, addp, d->u, d->pr);
   XG_CHECK_LAUNCH(c);
   return XG_OK;
 }
@@ -585,8 +678,8 @@ int launch_bc(xg_ctx* c, ChoCGDev* d, double* U, int sym_only) {
 }
 
 int launch_div(xg_ctx* c, ChoCGDev* d, const double* U, double dt, int stab, int bydt) {
-  k_cdiv<<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(
-      d->n, adj_of(d), U, d->pr, d->pgrad, bnd_of(d), dt, stab, bydt, d->div);
+  two_pass<k_cdiv<false>, k_cdiv<true>>(c->stream, d->n, d->nbn, d->n, adj_of(d), U, d->pr,
+                                        d->pgrad, bnd_of(d), dt, stab, bydt, d->div);
   XG_CHECK_LAUNCH(c);
   return XG_OK;
 }
@@ -595,11 +688,13 @@ int launch_rhs(xg_ctx* c, ChoCGDev* d, const double* U, double dtk, int stage0, 
                double* R) {
   const AdvPrm ap = adv_of(d);
   if (d->prm.flux == XG_DAMP4)
-    k_crhs<true><<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(
-        d->n, adj_of(d), U, d->vgrad, d->pr, bnd_of(d), ap, d->vol, dtk, stage0, d->un, uout, R);
+    two_pass<k_crhs<true, false>, k_crhs<true, true>>(c->stream, d->n, d->nbn, d->n, adj_of(d), U,
+                                                       d->vgrad, d->pr, bnd_of(d), ap, d->vol,
+                                                       dtk, stage0, d->un, uout, R);
   else
-    k_crhs<false><<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(
-        d->n, adj_of(d), U, d->vgrad, d->pr, bnd_of(d), ap, d->vol, dtk, stage0, d->un, uout, R);
+    two_pass<k_crhs<false, false>, k_crhs<false, true>>(c->stream, d->n, d->nbn, d->n, adj_of(d),
+                                                         U, d->vgrad, d->pr, bnd_of(d), ap, d->vol,
+                                                         dtk, stage0, d->un, uout, R);
   XG_CHECK_LAUNCH(c);
   return XG_OK;
 }
@@ -745,6 +840,7 @@ int xg_chocg_setup(xg_ctx* c, const xg_chocg_params* prm, int64_t npoin, const d
   soff[nslice] = static_cast<int32_t>(total);
   std::vector<int32_t> nbr(static_cast<size_t>(std::max<int64_t>(1, total)), kPad);
   std::vector<Coef4> dd(nbr.size(), Coef4{0.0, 0.0, 0.0, 0.0});
+  std::vector<double> sdl(nbr.size(), 0.0);
   for (int64_t p = 0; p < n; ++p) {
     const int64_t s = p / kSlice, lane = p % kSlice;
     for (int64_t k = 0; k < start[p + 1] - start[p]; ++k) {
@@ -753,6 +849,10 @@ int xg_chocg_setup(xg_ctx* c, const xg_chocg_params* prm, int64_t npoin, const d
       nbr[idx] = en.first ? static_cast<int32_t>(en.q) : ~static_cast<int32_t>(en.q);
       const double* r = E[en.eid].d;
       dd[idx] = Coef4{r[0], r[1], r[2], r[4]};
+      const double dx = coord[p] - coord[en.q], dy = coord[n + p] - coord[n + en.q],
+                   dz = coord[2 * n + p] - coord[2 * n + en.q];
+      sdl[idx] = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]) /
+                 std::sqrt(dx * dx + dy * dy + dz * dz);
     }
   }
   // boundary triangles, per boundary node the (triangle, position) pairs in
@@ -772,6 +872,9 @@ int xg_chocg_setup(xg_ctx* c, const xg_chocg_params* prm, int64_t npoin, const d
       ++bcount[bidx[p]];
     }
   std::vector<int32_t> bptr(nbn + 1, 0), bent(std::max<int64_t>(1, nbtri * 3));
+  std::vector<int32_t> bnode(std::max<int64_t>(1, nbn), 0);
+  for (int64_t p = 0; p < n; ++p)
+    if (bidx[p] >= 0) bnode[bidx[p]] = static_cast<int32_t>(p);
   for (int64_t i = 0; i < nbn; ++i) bptr[i + 1] = bptr[i] + bcount[i];
   {
     std::vector<int32_t> fill(bptr.begin(), bptr.end() - 1);
@@ -797,10 +900,13 @@ int xg_chocg_setup(xg_ctx* c, const xg_chocg_params* prm, int64_t npoin, const d
     A.plan(d->swidth, swidth.size());
     A.plan(d->nbr, nbr.size());
     A.plan(d->dd, dd.size());
+    A.plan(d->sdl, sdl.size());
     A.plan(d->bidx, n);
     A.plan(d->bptr, bptr.size());
     A.plan(d->bent, bent.size());
     A.plan(d->btri, btri.size());
+    A.plan(d->bnode, bnode.size());
+    A.plan(d->park, bnode.size() * 9);
     A.plan(d->xyz, 3 * n);
     A.plan(d->vol, n);
     A.plan(d->u, 3 * n);
@@ -829,10 +935,12 @@ int xg_chocg_setup(xg_ctx* c, const xg_chocg_params* prm, int64_t npoin, const d
   XG_CUDA(c, up(d->swidth, swidth.data(), swidth.size() * 4));
   XG_CUDA(c, up(d->nbr, nbr.data(), nbr.size() * 4));
   XG_CUDA(c, up(d->dd, dd.data(), dd.size() * sizeof(Coef4)));
+  XG_CUDA(c, up(d->sdl, sdl.data(), sdl.size() * 8));
   XG_CUDA(c, up(d->bidx, bidx.data(), n * 4));
   XG_CUDA(c, up(d->bptr, bptr.data(), bptr.size() * 4));
   XG_CUDA(c, up(d->bent, bent.data(), bent.size() * 4));
   XG_CUDA(c, up(d->btri, btri.data(), btri.size() * 4));
+  XG_CUDA(c, up(d->bnode, bnode.data(), bnode.size() * 4));
   XG_CUDA(c, up(d->xyz, coord, 3 * n * 8));
   XG_CUDA(c, up(d->vol, vol, n * 8));
   for (double* z : {d->u, d->u2, d->un, d->pr, d->pgrad, d->vgrad, d->div, d->flx})
@@ -981,8 +1089,8 @@ int xg_chocg_init(xg_ctx* c, int64_t* it) {
   // divergence of the volume-divided momentum flux with symmetry applied
   rc = launch_grad<3, GRAD_DIVIDE>(c, d, d->u, d->vgrad);
   if (rc) return rc;
-  k_cflux<<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(
-      d->n, adj_of(d), d->u, d->vgrad, bnd_of(d), d->vol, d->prm.mu, 1, d->flx);
+  two_pass<k_cflux<false>, k_cflux<true>>(c->stream, d->n, d->nbn, d->n, adj_of(d), d->u,
+                                          d->vgrad, bnd_of(d), d->vol, d->prm.mu, 1, d->flx);
   XG_CHECK_LAUNCH(c);
   rc = launch_bc(c, d, d->flx, 1);
   if (rc) return rc;
@@ -1116,8 +1224,8 @@ int xg_chorin_div(xg_ctx* c, const double* U, const double* P, const double* G, 
   XG_CUDA(c, cudaMemcpyAsync(out, G, n * 24, cudaMemcpyHostToDevice, s));
   k_aos_soa<<<blocks_for(n * 3, kBlock), kBlock, 0, s>>>(n, 3, out, g);
   XG_CUDA(c, cudaMemcpyAsync(p, P, n * 8, cudaMemcpyHostToDevice, s));
-  k_cdiv<<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, adj_of(d), u, p, g, bnd_of(d), dt, stab, 0,
-                                                   out);
+  two_pass<k_cdiv<false>, k_cdiv<true>>(s, n, d->nbn, n, adj_of(d), u, p, g, bnd_of(d), dt, stab,
+                                        0, out);
   XG_CHECK_LAUNCH(c);
   XG_CUDA(c, cudaMemcpyAsync(D, out, n * 8, cudaMemcpyDeviceToHost, s));
   XG_CUDA(c, cudaStreamSynchronize(s));
@@ -1140,9 +1248,8 @@ int xg_chorin_grad(xg_ctx* c, const double* S, double* Gout) {
   }
   cudaStream_t s = c->stream;
   XG_CUDA(c, cudaMemcpyAsync(sv, S, n * 8, cudaMemcpyHostToDevice, s));
-  k_cgrad<1, GRAD_RAW><<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, adj_of(d), sv, bnd_of(d),
-                                                                 d->vol, g, 0.0, 0, nullptr,
-                                                                 nullptr);
+  two_pass<k_cgrad<1, GRAD_RAW, false>, k_cgrad<1, GRAD_RAW, true>>(
+      s, n, d->nbn, n, adj_of(d), sv, bnd_of(d), d->vol, g, 0.0, 0, nullptr, nullptr);
   XG_CHECK_LAUNCH(c);
   k_soa_aos<<<blocks_for(n * 3, kBlock), kBlock, 0, s>>>(n, 3, g, out);
   XG_CUDA(c, cudaMemcpyAsync(Gout, out, n * 24, cudaMemcpyDeviceToHost, s));
@@ -1167,9 +1274,8 @@ int xg_chorin_vgrad(xg_ctx* c, const double* U, double* Gout) {
   cudaStream_t s = c->stream;
   XG_CUDA(c, cudaMemcpyAsync(out, U, n * 24, cudaMemcpyHostToDevice, s));
   k_aos_soa<<<blocks_for(n * 3, kBlock), kBlock, 0, s>>>(n, 3, out, u);
-  k_cgrad<3, GRAD_RAW><<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, adj_of(d), u, bnd_of(d),
-                                                                 d->vol, g, 0.0, 0, nullptr,
-                                                                 nullptr);
+  two_pass<k_cgrad<3, GRAD_RAW, false>, k_cgrad<3, GRAD_RAW, true>>(
+      s, n, d->nbn, n, adj_of(d), u, bnd_of(d), d->vol, g, 0.0, 0, nullptr, nullptr);
   XG_CHECK_LAUNCH(c);
   k_soa_aos<<<blocks_for(n * 9, kBlock), kBlock, 0, s>>>(n, 9, g, out);
   XG_CUDA(c, cudaMemcpyAsync(Gout, out, n * 72, cudaMemcpyDeviceToHost, s));
@@ -1197,8 +1303,8 @@ int xg_chorin_flux(xg_ctx* c, const double* U, const double* G, double* F) {
   k_aos_soa<<<blocks_for(n * 3, kBlock), kBlock, 0, s>>>(n, 3, tmp, u);
   XG_CUDA(c, cudaMemcpyAsync(tmp, G, n * 72, cudaMemcpyHostToDevice, s));
   k_aos_soa<<<blocks_for(n * 9, kBlock), kBlock, 0, s>>>(n, 9, tmp, g);
-  k_cflux<<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, adj_of(d), u, g, bnd_of(d), d->vol,
-                                                    d->prm.mu, 0, f);
+  two_pass<k_cflux<false>, k_cflux<true>>(s, n, d->nbn, n, adj_of(d), u, g, bnd_of(d), d->vol,
+                                          d->prm.mu, 0, f);
   XG_CHECK_LAUNCH(c);
   k_soa_aos<<<blocks_for(n * 3, kBlock), kBlock, 0, s>>>(n, 3, f, tmp);
   XG_CUDA(c, cudaMemcpyAsync(F, tmp, n * 24, cudaMemcpyDeviceToHost, s));
@@ -1230,11 +1336,13 @@ int xg_chorin_rhs(xg_ctx* c, const double* P, const double* U, const double* G, 
   XG_CUDA(c, cudaMemcpyAsync(p, P, n * 8, cudaMemcpyHostToDevice, s));
   const AdvPrm ap = adv_of(d);
   if (d->prm.flux == XG_DAMP4)
-    k_crhs<true><<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, adj_of(d), u, g, p, bnd_of(d), ap,
-                                                           d->vol, 0.0, 0, nullptr, nullptr, r);
+    two_pass<k_crhs<true, false>, k_crhs<true, true>>(s, n, d->nbn, n, adj_of(d), u, g, p,
+                                                       bnd_of(d), ap, d->vol, 0.0, 0, nullptr,
+                                                       nullptr, r);
   else
-    k_crhs<false><<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, adj_of(d), u, g, p, bnd_of(d), ap,
-                                                            d->vol, 0.0, 0, nullptr, nullptr, r);
+    two_pass<k_crhs<false, false>, k_crhs<false, true>>(s, n, d->nbn, n, adj_of(d), u, g, p,
+                                                         bnd_of(d), ap, d->vol, 0.0, 0, nullptr,
+                                                         nullptr, r);
   XG_CHECK_LAUNCH(c);
   k_soa_aos<<<blocks_for(n * 3, kBlock), kBlock, 0, s>>>(n, 3, r, tmp);
   XG_CUDA(c, cudaMemcpyAsync(R, tmp, n * 24, cudaMemcpyDeviceToHost, s));
