@@ -430,6 +430,66 @@ def barrier(world):
         _dist.barrier()
 
 
+def _cuda_profiler(on):
+    """cudaProfilerStart/Stop through the CUDA runtime, so that
+    `ncu --profile-from-start off` captures exactly the bracketed region."""
+    import ctypes
+    import glob
+    rt = None
+    for name in ["libcudart.so", "libcudart.so.13"] + sorted(
+            glob.glob("/usr/local/cuda/lib64/libcudart.so*")):
+        try:
+            rt = ctypes.CDLL(name)
+            break
+        except OSError:
+            continue
+    if rt is None:
+        raise RuntimeError("CUDA runtime library not found")
+    (rt.cudaProfilerStart if on else rt.cudaProfilerStop)()
+
+
+def profile_step(what, n):
+    """One warm step of a workload bracketed by the profiler range (for
+    `ncu --profile-from-start off`): chocg-fp64 (Jacobi PCG), chocg-mixed
+    (first-order factor, mixed solve), kozcg-fp64, kozcg-fp32."""
+    from xyst_gb300 import chocg, kozcg, lib, mesh, riecg
+
+    ctx = lib.Context(0)
+    if what.startswith("chocg"):
+        m = mesh.cube(n, jitter=0.2, seed=0, numbering="random", perm_seed=1)
+        ops = chocg.operators(m, sym_sets=[1, 2, 3, 4, 5, 6], hydrostat=0)
+        if what == "chocg-fp64":
+            d = chocg.ChoCG(ctx, ops, mu=0.01, cfl=0.5, flux="damp2", pc="jacobi", ptol=1e-8,
+                            pmaxit=50000, guard="underflow")
+        else:
+            d = chocg.ChoCG(ctx, ops, mu=0.01, cfl=0.5, flux="damp2", pc="factor", ptol=1e-8,
+                            pmaxit=50000, mixed=True, inner_tol=0.1, guard="underflow")
+            d.cg.set_factor(None, 1.0)
+        d.set_state(chocg.taylor_green(ops["coord"]))
+        d.init()
+        d.run(1)
+        _cuda_profiler(True)
+        _, its, ms, _ = d.run(1)
+        _cuda_profiler(False)
+        out = {"profile": what, "n": n, "iterations": [int(i) for i in its], "ms": ms}
+    else:
+        m = mesh.cube(n, jitter=0.2, seed=0, numbering="random", perm_seed=1)
+        m = mesh.relabel(m, riecg.rcm(m["inpoel"], m["coord"].shape[1]))
+        v = riecg.volumes(m["coord"], m["inpoel"])
+        ops = riecg.operators(m, sym_sets=[1, 2, 3, 4, 5, 6], renumber=False)
+        k = kozcg.KozCG(ctx, m["coord"], v, m["inpoel"],
+                        precision="fp32" if what == "kozcg-fp32" else "fp64")
+        k.set_bc(sym=ops["sym"])
+        k.set_state(wave_state(m["coord"]))
+        k.run(1)
+        _cuda_profiler(True)
+        _, ms = k.run(1)
+        _cuda_profiler(False)
+        out = {"profile": what, "n": n, "ms": ms}
+    ctx.close()
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -441,7 +501,14 @@ def main():
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-pcg", action="store_true", help="skip the ChoCG leg")
+    ap.add_argument("--profile-step", default=None,
+                    choices=["chocg-fp64", "chocg-mixed", "kozcg-fp64", "kozcg-fp32"],
+                    help="run one warm step of that workload (side --n) inside a profiler "
+                         "range and exit")
     args = ap.parse_args()
+    if args.profile_step:
+        profile_step(args.profile_step, args.n)
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     global _dist
