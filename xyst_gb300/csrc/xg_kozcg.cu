@@ -1,5 +1,5 @@
 // KozCG on one GB300: element Taylor-Galerkin residual and flux-corrected
-// transport, FP64.
+// transport, FP64, or with FP32 element arithmetic (XG_FP32_FLUX).
 //
 // Reference path (paths relative to the reference project root):
 //   kozak::rhs      src/Physics/Kozak.cpp:29-180
@@ -20,6 +20,14 @@
 // passes.  One step is:
 //   step_begin -> zero -> node_prim -> elem_rhs_aec -> bc_p -> node_lo -> elem_alw ->
 //   node_lim -> elem_lim -> node_solve -> bc (+ CFL minimum for the next step)
+//
+// FP32-element mode: the element passes read an FP32 copy of the state (made
+// by node_prim) and FP32 element geometry (made at setup), and add into FP32
+// node records [n][8] / [n][12] with vector atomics; the allowed limits are
+// 32-bit keys of floats.  The node passes (low-order solution, limit
+// coefficients, update, dt) stay FP64 on the FP64 state.  GB300's FP64 rate
+// is a small fraction of its FP32 rate, and FP32/FP64 conversions run at the
+// FP64 rate, so this mode converts per node, not per element.
 
 #include <algorithm>
 #include <cfloat>
@@ -54,6 +62,11 @@ struct KozCGDev {
   unsigned long long* Q = nullptr;
   double* stage = nullptr;
   double* V = nullptr;  // [n][4] velocity and pressure per node (FP32 packed in the first half)
+  // FP32-element mode: element sums, the FP32 state, the low-order solution
+  // as the allowed-limit pass reads it, 32-bit limit keys, element geometry
+  float *R32 = nullptr, *P32 = nullptr, *A32 = nullptr, *U32 = nullptr, *lo32 = nullptr;
+  unsigned int* Q32 = nullptr;
+  float* geo32 = nullptr;
   // BC program: one thread per BC node
   int64_t nbc = 0;
   int32_t *bcnode = nullptr, *bcdir = nullptr, *bcsymp = nullptr, *dirmask = nullptr;
@@ -150,13 +163,70 @@ __device__ __forceinline__ Geo<F> tetgeo(const double* xyz, int64_t n, const int
   return t;
 }
 
+// Types of a precision mode: F is the element arithmetic; FP64 mode sums in
+// FP64 and keeps the allowed limits as 64-bit keys of doubles, the
+// FP32-element mode sums in FP32 and keys floats in 32 bits.
+template <class F>
+struct KozT;
+template <>
+struct KozT<double> {
+  using Key = unsigned long long;
+};
+template <>
+struct KozT<float> {
+  using Key = unsigned int;
+};
+
+template <class F>
+__device__ __forceinline__ F big() {
+  return sizeof(F) == 8 ? F(DBL_MAX) : F(FLT_MAX);
+}
+__device__ __forceinline__ unsigned long long okey(double v) { return dkey(v); }
+__device__ __forceinline__ unsigned int okey(float v) {
+  const unsigned int b = __float_as_uint(v);
+  return (b >> 31) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ double oval(unsigned long long k) { return dval(k); }
+__device__ __forceinline__ float oval(unsigned int k) {
+  return __uint_as_float((k >> 31) ? (k & 0x7fffffffu) : ~k);
+}
+__device__ __forceinline__ double kbits(unsigned long long k) { return __longlong_as_double(k); }
+__device__ __forceinline__ float kbits(unsigned int k) { return __uint_as_float(k); }
+__device__ __forceinline__ unsigned long long tobits(double v) { return __double_as_longlong(v); }
+__device__ __forceinline__ unsigned int tobits(float v) { return __float_as_uint(v); }
+
+// Where component c of node i lives in the element sums: FP64 mode SoA
+// [5][n] (R, A) and [10][n] (P); FP32 mode node records [n][8] and [n][12],
+// so that one element adds a node's contribution with vector atomics
+// (red.global.add.v4/v2.f32) instead of one atomic per component.
+template <class F>
+__device__ __forceinline__ int64_t ridx(int64_t n, int c, int64_t i) {
+  return sizeof(F) == 4 ? i * 8 + c : c * n + i;
+}
+template <class F>
+__device__ __forceinline__ int64_t pidx(int64_t n, int cs, int64_t i) {
+  return sizeof(F) == 4 ? i * 12 + cs : cs * n + i;
+}
+
+// r[5] added to node i's record of R or A.
+__device__ __forceinline__ void add5(double* R, int64_t n, int64_t i, const double r[5]) {
+  for (int c = 0; c < 5; ++c) atomicAdd(R + c * n + i, r[c]);
+}
+__device__ __forceinline__ void add5(float* R, int64_t, int64_t i, const float r[5]) {
+  atomicAdd(reinterpret_cast<float4*>(R + i * 8), make_float4(r[0], r[1], r[2], r[3]));
+  atomicAdd(R + i * 8 + 4, r[4]);
+}
+
 // Per-node velocity and pressure (the node-wise quotients kozak::rhs forms
 // for every element holding the node, Kozak.cpp:93-118): computed once per
 // node, the same expressions, so the element pass gathers bit-identical
-// values instead of repeating the FP64 divisions per element.
+// values instead of repeating the FP64 divisions per element.  In FP32 mode
+// the state itself is also stored in FP32 (Uf), so that the element passes
+// read it without conversions.
 template <class F>
 __global__ void __launch_bounds__(kBlock) k_node_prim(int64_t n, const double* __restrict__ U,
-                                                       double gamma_d, F* __restrict__ V) {
+                                                       double gamma_d, F* __restrict__ V,
+                                                       F* __restrict__ Uf) {
   const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (i >= n) return;
   const F gamma = F(gamma_d);
@@ -169,6 +239,51 @@ __global__ void __launch_bounds__(kBlock) k_node_prim(int64_t n, const double* _
   o[3] = (gamma - F(1.0)) * (u[4] - F(0.5) * (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) / u[0]);
 #pragma unroll
   for (int k = 0; k < 4; ++k) V[i * 4 + k] = o[k];
+  if (Uf) {
+#pragma unroll
+    for (int c = 0; c < 5; ++c) Uf[c * n + i] = u[c];
+  }
+}
+
+// Element geometry in FP32 for the FP32 mode, formed once at setup from the
+// FP64 coordinates (tetgeo<double>, then rounded): J and g1, g2, g3 as
+// [10][T] (g0 = -g1 - g2 - g3 is re-formed in the element passes).
+__global__ void k_geo32(int64_t n, int64_t ne, const int32_t* __restrict__ inpoel,
+                        const double* __restrict__ xyz, float* __restrict__ geo) {
+  const int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (e >= ne) return;
+  int32_t N[4];
+  for (int a = 0; a < 4; ++a) N[a] = inpoel[e * 4 + a];
+  const Geo<double> t = tetgeo<double>(xyz, n, N);
+  geo[e] = float(t.J);
+  for (int a = 1; a < 4; ++a)
+    for (int j = 0; j < 3; ++j) geo[(1 + (a - 1) * 3 + j) * ne + e] = float(t.g[a][j]);
+}
+
+template <class F>
+__device__ __forceinline__ Geo<F> elem_geo(const double* __restrict__ xyz,
+                                           const float* __restrict__ geo, int64_t n, int64_t ne,
+                                           int64_t e, const int32_t N[4]) {
+  if constexpr (sizeof(F) == 8) {
+    return tetgeo<double>(xyz, n, N);
+  } else {
+    Geo<float> t;
+    t.J = __ldg(geo + e);
+    for (int a = 1; a < 4; ++a)
+      for (int j = 0; j < 3; ++j) t.g[a][j] = __ldg(geo + (1 + (a - 1) * 3 + j) * ne + e);
+    for (int j = 0; j < 3; ++j) t.g[0][j] = -t.g[1][j] - t.g[2][j] - t.g[3][j];
+    return t;
+  }
+}
+
+// Component c of the state at a node, as the element arithmetic reads it.
+template <class F>
+__device__ __forceinline__ F ust(const double* __restrict__ U, const F* __restrict__ Uf, int64_t n,
+                                 int c, int32_t node) {
+  if constexpr (sizeof(F) == 8)
+    return U[c * n + node];
+  else
+    return __ldg(Uf + c * n + node);
 }
 
 // kozak::rhs for one tet (Kozak.cpp:73-173) plus the antidiffusive element
@@ -196,20 +311,22 @@ template <class F>
 __global__ void __launch_bounds__(kBlock) k_elem_rhs_aec(int64_t n, int64_t ne,
                                                           const int32_t* __restrict__ inpoel,
                                                           const double* __restrict__ xyz,
+                                                          const float* __restrict__ geo,
                                                           const double* __restrict__ U,
+                                                          const F* __restrict__ Uf,
                                                           const F* __restrict__ V,
                                                           const KScalars* __restrict__ sc,
                                                           double gamma_d, double ctau_d, int fct,
-                                                          double* R, double* P) {
+                                                          F* R, F* P) {
   int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (e >= ne) return;
   const F gamma = F(gamma_d), ctau = F(ctau_d);
   int32_t N[4];
   for (int a = 0; a < 4; ++a) N[a] = inpoel[e * 4 + a];
-  const Geo<F> t = tetgeo<F>(xyz, n, N);
+  const Geo<F> t = elem_geo<F>(xyz, geo, n, ne, e, N);
   F u[4][5], vel[4][3], p[4];
   for (int a = 0; a < 4; ++a) {
-    for (int c = 0; c < 5; ++c) u[a][c] = F(U[c * n + N[a]]);
+    for (int c = 0; c < 5; ++c) u[a][c] = ust<F>(U, Uf, n, c, N[a]);
     F v4[4];
     load_v4(V, N[a], v4);
     vel[a][0] = v4[0];
@@ -250,21 +367,41 @@ __global__ void __launch_bounds__(kBlock) k_elem_rhs_aec(int64_t n, int64_t ne,
       r[a][4] += cg * (ue[4] + pr) * uj;
     }
   }
-  for (int a = 0; a < 4; ++a)
-    for (int c = 0; c < 5; ++c) atomicAdd(R + c * n + N[a], double(r[a][c]));
+  for (int a = 0; a < 4; ++a) add5(R, n, N[a], r[a]);
   if (!fct) return;
-  for (int c = 0; c < 5; ++c)
-    for (int a = 0; a < 4; ++a) {
-      F aec = F(0.0);
-      for (int b = 0; b < 4; ++b) {
-        const F m = t.J / F(120.0) * ((a == b) ? F(3.0) : F(-1.0));
-        aec += m * ctau * u[b][c];
+  if constexpr (sizeof(F) == 8) {
+    for (int c = 0; c < 5; ++c)
+      for (int a = 0; a < 4; ++a) {
+        F aec = F(0.0);
+        for (int b = 0; b < 4; ++b) {
+          const F m = t.J / F(120.0) * ((a == b) ? F(3.0) : F(-1.0));
+          aec += m * ctau * u[b][c];
+        }
+        if (aec > F(0.0))
+          atomicAdd(P + (c * 2 + 0) * n + N[a], aec);
+        else if (aec < F(0.0))
+          atomicAdd(P + (c * 2 + 1) * n + N[a], aec);
       }
-      if (aec > F(0.0))
-        atomicAdd(P + (c * 2 + 0) * n + N[a], double(aec));
-      else if (aec < F(0.0))
-        atomicAdd(P + (c * 2 + 1) * n + N[a], double(aec));
+  } else {
+    // per node the ten sums (+, - per component) in one record: the sign
+    // that does not apply adds 0
+    for (int a = 0; a < 4; ++a) {
+      F pa[10];
+      for (int c = 0; c < 5; ++c) {
+        F aec = F(0.0);
+        for (int b = 0; b < 4; ++b) {
+          const F m = t.J / F(120.0) * ((a == b) ? F(3.0) : F(-1.0));
+          aec += m * ctau * u[b][c];
+        }
+        pa[c * 2 + 0] = aec > F(0.0) ? aec : F(0.0);
+        pa[c * 2 + 1] = aec < F(0.0) ? aec : F(0.0);
+      }
+      float* q = P + int64_t(N[a]) * 12;
+      atomicAdd(reinterpret_cast<float4*>(q), make_float4(pa[0], pa[1], pa[2], pa[3]));
+      atomicAdd(reinterpret_cast<float4*>(q + 4), make_float4(pa[4], pa[5], pa[6], pa[7]));
+      atomicAdd(reinterpret_cast<float2*>(q + 8), make_float2(pa[8], pa[9]));
     }
+  }
 }
 
 struct KBC {
@@ -278,20 +415,21 @@ struct KBC {
 };
 
 // Symmetry projection of the momentum antidiffusive sums (KozCG.cpp:816-830).
-__global__ void k_bc_p(int64_t n, KBC bc, double* P) {
+template <class F>
+__global__ void k_bc_p(int64_t n, KBC bc, F* P) {
   int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (i >= bc.nbc) return;
   const int64_t p = bc.node[i];
   for (int32_t k = bc.symp[i]; k < bc.symp[i + 1]; ++k) {
-    const double nx = bc.symn[3 * k], ny = bc.symn[3 * k + 1], nz = bc.symn[3 * k + 2];
-    double* P2 = P + 2 * n + p;  // comp 1 (+)
-    double* P3 = P + 3 * n + p;  // comp 1 (-)
-    double* P4 = P + 4 * n + p;
-    double* P5 = P + 5 * n + p;
-    double* P6 = P + 6 * n + p;
-    double* P7 = P + 7 * n + p;
-    const double rvnp = *P2 * nx + *P4 * ny + *P6 * nz;
-    const double rvnn = *P3 * nx + *P5 * ny + *P7 * nz;
+    const F nx = F(bc.symn[3 * k]), ny = F(bc.symn[3 * k + 1]), nz = F(bc.symn[3 * k + 2]);
+    F* P2 = P + pidx<F>(n, 2, p);  // comp 1 (+)
+    F* P3 = P + pidx<F>(n, 3, p);  // comp 1 (-)
+    F* P4 = P + pidx<F>(n, 4, p);
+    F* P5 = P + pidx<F>(n, 5, p);
+    F* P6 = P + pidx<F>(n, 6, p);
+    F* P7 = P + pidx<F>(n, 7, p);
+    const F rvnp = *P2 * nx + *P4 * ny + *P6 * nz;
+    const F rvnn = *P3 * nx + *P5 * ny + *P7 * nz;
     *P2 -= rvnp * nx;
     *P3 -= rvnn * nx;
     *P4 -= rvnp * ny;
@@ -302,76 +440,96 @@ __global__ void k_bc_p(int64_t n, KBC bc, double* P) {
 }
 
 // KozCG::alw node part (KozCG.cpp:887-912): P /= vol, low-order solution
-// R <- U + dt R/vol - P+ - P-, Q keys reset to (-large, +large).  Without FCT
-// the update of KozCG::solve (KozCG.cpp:1151-1160) goes straight to A.
+// lo = U + dt R/vol - P+ - P-, the keys of Q reset to (-large, +large).
+// Without FCT the update of KozCG::solve (KozCG.cpp:1151-1160) goes straight
+// to A.  Racc/Pacc are the element sums (in F); lo and P/vol go to the FP64
+// arrays Rlo/Pout (the same arrays as Racc/Pacc in FP64 mode), and in FP32
+// mode lo also to lo32 for the element pass of the allowed limits.
+template <class F>
 __global__ void k_node_lo(int64_t n, const double* __restrict__ vol, const double* __restrict__ U,
-                          const KScalars* __restrict__ sc, int fct, double* R, double* P,
-                          unsigned long long* Q, double* A) {
+                          const KScalars* __restrict__ sc, int fct, const F* Racc, const F* Pacc,
+                          double* Rlo, double* Pout, F* lo32, typename KozT<F>::Key* Q,
+                          double* A) {
   int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (i >= n) return;
   const double dt = sc->dt;
   const double v = vol[i];
+  // FP32 mode: one FP64 division per node (GB300's FP64 divisions are slow);
+  // FP64 mode divides as the reference does
+  const double iv = sizeof(F) == 4 ? 1.0 / v : 0.0;
+  auto per_vol = [&](double x) { return sizeof(F) == 4 ? x * iv : x / v; };
   for (int c = 0; c < 5; ++c) {
     if (fct) {
-      double pp = P[(c * 2 + 0) * n + i] / v;
-      double pn = P[(c * 2 + 1) * n + i] / v;
-      P[(c * 2 + 0) * n + i] = pp;
-      P[(c * 2 + 1) * n + i] = pn;
-      R[c * n + i] = U[c * n + i] + dt * R[c * n + i] / v - pp - pn;
-      Q[(c * 2 + 0) * n + i] = dkey(-DBL_MAX);
-      Q[(c * 2 + 1) * n + i] = dkey(DBL_MAX);
+      double pp = per_vol(double(Pacc[pidx<F>(n, c * 2 + 0, i)]));
+      double pn = per_vol(double(Pacc[pidx<F>(n, c * 2 + 1, i)]));
+      Pout[(c * 2 + 0) * n + i] = pp;
+      Pout[(c * 2 + 1) * n + i] = pn;
+      const double lo = U[c * n + i] + per_vol(dt * double(Racc[ridx<F>(n, c, i)])) - pp - pn;
+      Rlo[c * n + i] = lo;
+      if (lo32) lo32[c * n + i] = F(lo);
+      Q[(c * 2 + 0) * n + i] = okey(-big<F>());
+      Q[(c * 2 + 1) * n + i] = okey(big<F>());
     } else {
-      A[c * n + i] = U[c * n + i] + dt * R[c * n + i] / v;
+      A[c * n + i] = U[c * n + i] + per_vol(dt * double(Racc[ridx<F>(n, c, i)]));
     }
   }
 }
 
-// KozCG::alw element part (KozCG.cpp:914-935): allowed limits.
+// KozCG::alw element part (KozCG.cpp:914-935): allowed limits, from the
+// low-order solution lo and the state U, as F.
+template <class F>
 __global__ void __launch_bounds__(kBlock) k_elem_alw(int64_t n, int64_t ne,
                                                       const int32_t* __restrict__ inpoel,
-                                                      const double* __restrict__ U,
-                                                      const double* __restrict__ R, int clip,
-                                                      unsigned long long* Q) {
+                                                      const F* __restrict__ U,
+                                                      const F* __restrict__ lo, int clip,
+                                                      typename KozT<F>::Key* Q) {
   int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (e >= ne) return;
   int32_t N[4];
   for (int a = 0; a < 4; ++a) N[a] = inpoel[e * 4 + a];
   for (int c = 0; c < 5; ++c) {
-    double alwp = -DBL_MAX, alwn = DBL_MAX;
+    F alwp = -big<F>(), alwn = big<F>();
     for (int a = 0; a < 4; ++a) {
-      const double lo = R[c * n + N[a]];
+      const F l = lo[c * n + N[a]];
       if (clip) {
-        alwp = fmax(alwp, lo);
-        alwn = fmin(alwn, lo);
+        alwp = fmax(alwp, l);
+        alwn = fmin(alwn, l);
       } else {
-        const double uo = U[c * n + N[a]];
-        alwp = fmax(alwp, fmax(lo, uo));
-        alwn = fmin(alwn, fmin(lo, uo));
+        const F uo = U[c * n + N[a]];
+        alwp = fmax(alwp, fmax(l, uo));
+        alwn = fmin(alwn, fmin(l, uo));
       }
     }
-    const unsigned long long kp = dkey(alwp), kn = dkey(alwn);
+    const auto kp = okey(alwp), kn = okey(alwn);
+    // a key only ever grows (shrinks): an element whose bound does not pass
+    // the one already stored (read through L2, possibly older) skips its
+    // atomic, which cannot change the result
     for (int a = 0; a < 4; ++a) {
-      atomicMax(Q + (c * 2 + 0) * n + N[a], kp);
-      atomicMin(Q + (c * 2 + 1) * n + N[a], kn);
+      auto* qp = Q + (c * 2 + 0) * n + N[a];
+      auto* qn = Q + (c * 2 + 1) * n + N[a];
+      if (kp > __ldcg(qp)) atomicMax(qp, kp);
+      if (kn < __ldcg(qn)) atomicMin(qn, kn);
     }
   }
 }
 
 // KozCG::lim node part (KozCG.cpp:1004-1024): Q -= low-order solution, limit
-// coefficients C+/- stored back into Q as plain doubles (reinterpreted).
+// coefficients C+/- stored back into Q as F values (reinterpreted).
+template <class F>
 __global__ void k_node_lim(int64_t n, const double* __restrict__ R, const double* __restrict__ P,
-                           unsigned long long* Q) {
+                           typename KozT<F>::Key* Q) {
   int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (i >= n) return;
   const double eps = DBL_EPSILON;
   for (int c = 0; c < 5; ++c) {
-    double qp = dval(Q[(c * 2 + 0) * n + i]) - R[c * n + i];
-    double qn = dval(Q[(c * 2 + 1) * n + i]) - R[c * n + i];
+    double qp = double(oval(Q[(c * 2 + 0) * n + i])) - R[c * n + i];
+    double qn = double(oval(Q[(c * 2 + 1) * n + i])) - R[c * n + i];
     const double pp = P[(c * 2 + 0) * n + i], pn = P[(c * 2 + 1) * n + i];
-    qp = pp < eps ? 0.0 : fmin(1.0, qp / pp);
-    qn = pn > -eps ? 0.0 : fmin(1.0, qn / pn);
-    Q[(c * 2 + 0) * n + i] = __double_as_longlong(qp);
-    Q[(c * 2 + 1) * n + i] = __double_as_longlong(qn);
+    // the coefficient's quotient in F (an FP32 division in FP32 mode)
+    const F cp = pp < eps ? F(0) : fmin(F(1), F(qp) / F(pp));
+    const F cn = pn > -eps ? F(0) : fmin(F(1), F(qn) / F(pn));
+    Q[(c * 2 + 0) * n + i] = tobits(cp);
+    Q[(c * 2 + 1) * n + i] = tobits(cn);
   }
 }
 
@@ -381,15 +539,17 @@ template <class F>
 __global__ void __launch_bounds__(kBlock) k_elem_lim(int64_t n, int64_t ne,
                                                       const int32_t* __restrict__ inpoel,
                                                       const double* __restrict__ xyz,
+                                                      const float* __restrict__ geo,
                                                       const double* __restrict__ U,
-                                                      const unsigned long long* __restrict__ Q,
-                                                      double ctau_d, int sysmask, double* A) {
+                                                      const F* __restrict__ Uf,
+                                                      const typename KozT<F>::Key* __restrict__ Q,
+                                                      double ctau_d, int sysmask, F* A) {
   int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (e >= ne) return;
   const F ctau = F(ctau_d);
   int32_t N[4];
   for (int a = 0; a < 4; ++a) N[a] = inpoel[e * 4 + a];
-  const Geo<F> t = tetgeo<F>(xyz, n, N);
+  const Geo<F> t = elem_geo<F>(xyz, geo, n, ne, e, N);
   F coef[5], aec[5][4];
   for (int c = 0; c < 5; ++c) {
     coef[c] = F(1.0);
@@ -397,10 +557,10 @@ __global__ void __launch_bounds__(kBlock) k_elem_lim(int64_t n, int64_t ne,
       F s = F(0.0);
       for (int b = 0; b < 4; ++b) {
         const F m = t.J / F(120.0) * ((a == b) ? F(3.0) : F(-1.0));
-        s += m * ctau * F(U[c * n + N[b]]);
+        s += m * ctau * ust<F>(U, Uf, n, c, N[b]);
       }
       aec[c][a] = s;
-      const F lim = F(__longlong_as_double(Q[(c * 2 + (s > F(0.0) ? 0 : 1)) * n + N[a]]));
+      const F lim = kbits(Q[(c * 2 + (s > F(0.0) ? 0 : 1)) * n + N[a]]);
       coef[c] = coef[c] < lim ? coef[c] : lim;
     }
   }
@@ -409,14 +569,20 @@ __global__ void __launch_bounds__(kBlock) k_elem_lim(int64_t n, int64_t ne,
     if (sysmask & (1 << c)) cs = cs < coef[c] ? cs : coef[c];
   for (int c = 0; c < 5; ++c)
     if (sysmask & (1 << c)) coef[c] = cs;
-  for (int c = 0; c < 5; ++c)
-    for (int a = 0; a < 4; ++a) atomicAdd(A + c * n + N[a], double(coef[c] * aec[c][a]));
+  for (int a = 0; a < 4; ++a) {
+    F ca[5];
+    for (int c = 0; c < 5; ++c) ca[c] = coef[c] * aec[c][a];
+    add5(A, n, N[a], ca);
+  }
 }
 
 // KozCG::solve (KozCG.cpp:1144-1150): A = low-order + A/vol, then U = A and
-// the CFL minimum of the new state for nodes without BCs.
+// the CFL minimum of the new state for nodes without BCs.  Aacc: the limited
+// sums (F, with FCT); A: the update itself (FP64, without FCT).
+template <class F>
 __global__ void __launch_bounds__(kBlock) k_node_solve(int64_t n, const double* __restrict__ vol,
                                                         const double* __restrict__ R,
+                                                        const F* __restrict__ Aacc,
                                                         const double* __restrict__ A, int fct,
                                                         const uint8_t* __restrict__ isbc,
                                                         double gamma, double* U,
@@ -425,8 +591,11 @@ __global__ void __launch_bounds__(kBlock) k_node_solve(int64_t n, const double* 
   double dtp = DBL_MAX;
   if (i < n) {
     double u[5];
+    const double v = vol[i];
+    const double iv = sizeof(F) == 4 ? 1.0 / v : 0.0;  // FP32 mode: one division
     for (int c = 0; c < 5; ++c) {
-      u[c] = fct ? R[c * n + i] + A[c * n + i] / vol[i] : A[c * n + i];
+      const double a = double(Aacc[ridx<F>(n, c, i)]);
+      u[c] = fct ? R[c * n + i] + (sizeof(F) == 4 ? a * iv : a / v) : A[c * n + i];
       U[c * n + i] = u[c];
     }
     if (!isbc[i]) dtp = node_dt(u, vol[i], gamma);
@@ -520,58 +689,73 @@ int refresh_dt(xg_ctx* c, KozCGDev* d) {
   return XG_OK;
 }
 
-// Node primitives and the element Galerkin (+ antidiffusive) pass on state U,
-// in the context's precision.
-void galerkin(cudaStream_t s, KozCGDev* d, const double* U, int fct) {
-  const int64_t n = d->n, ne = d->ne;
-  if (d->prm.precision == XG_FP32_FLUX) {
-    float* V = reinterpret_cast<float*>(d->V);
-    k_node_prim<float><<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, U, d->prm.gamma, V);
-    k_elem_rhs_aec<float><<<blocks_for(ne, kBlock), kBlock, 0, s>>>(
-        n, ne, d->inpoel, d->xyz, U, V, d->scal, d->prm.gamma, d->prm.ctau, fct, d->R, d->P);
-  } else {
-    double* V = d->V;
-    k_node_prim<double><<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, U, d->prm.gamma, V);
-    k_elem_rhs_aec<double><<<blocks_for(ne, kBlock), kBlock, 0, s>>>(
-        n, ne, d->inpoel, d->xyz, U, V, d->scal, d->prm.gamma, d->prm.ctau, fct, d->R, d->P);
-  }
+// The arrays of precision F: element sums (R, P, A accumulators), the state
+// the element passes read, the per-node primitives, the limit keys.
+template <class F>
+struct KArrays {
+  F *R, *P, *A, *Uf, *V, *lo;
+  typename KozT<F>::Key* Q;
+  const float* geo;
+};
+KArrays<double> arrays64(KozCGDev* d) {
+  return KArrays<double>{d->R, d->P, d->A, nullptr, d->V, d->R, d->Q, nullptr};
+}
+KArrays<float> arrays32(KozCGDev* d) {
+  return KArrays<float>{d->R32, d->P32, d->A32, d->U32, reinterpret_cast<float*>(d->V),
+                        d->lo32, d->Q32, d->geo32};
 }
 
-// One KozCG step with the dt already in the device scalars.
-int step(xg_ctx* c, KozCGDev* d) {
+// Node primitives and the element Galerkin (+ antidiffusive) pass on state U
+// into the accumulators k.R, k.P.
+template <class F>
+void galerkin(cudaStream_t s, KozCGDev* d, const KArrays<F>& k, const double* U, int fct) {
+  const int64_t n = d->n, ne = d->ne;
+  k_node_prim<F><<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, U, d->prm.gamma, k.V, k.Uf);
+  k_elem_rhs_aec<F><<<blocks_for(ne, kBlock), kBlock, 0, s>>>(n, ne, d->inpoel, d->xyz, k.geo, U,
+                                                               k.Uf, k.V, d->scal, d->prm.gamma,
+                                                               d->prm.ctau, fct, k.R, k.P);
+}
+
+// One KozCG step with the dt already in the device scalars, element
+// arithmetic in F.
+template <class F>
+int step_impl(xg_ctx* c, KozCGDev* d, const KArrays<F>& k) {
   cudaStream_t s = c->stream;
   const int64_t n = d->n, ne = d->ne;
   const int fct = d->prm.fct;
-  XG_CUDA(c, cudaMemsetAsync(d->R, 0, n * 5 * 8, s));
+  // FP64: R, A [5][n], P [10][n]; FP32: R, A [n][8], P [n][12]
+  const int64_t rb = sizeof(F) == 4 ? 8 * 4 : 5 * 8, pb = sizeof(F) == 4 ? 12 * 4 : 10 * 8;
+  XG_CUDA(c, cudaMemsetAsync(k.R, 0, n * rb, s));
   if (fct) {
-    XG_CUDA(c, cudaMemsetAsync(d->P, 0, n * 10 * 8, s));
-    XG_CUDA(c, cudaMemsetAsync(d->A, 0, n * 5 * 8, s));
+    XG_CUDA(c, cudaMemsetAsync(k.P, 0, n * pb, s));
+    XG_CUDA(c, cudaMemsetAsync(k.A, 0, n * rb, s));
   }
-  galerkin(s, d, d->U, fct);
+  galerkin<F>(s, d, k, d->U, fct);
   XG_CHECK_LAUNCH(c);
   if (fct && d->nbc) {
-    k_bc_p<<<blocks_for(d->nbc, kBlock), kBlock, 0, s>>>(n, kbc_of(d), d->P);
+    k_bc_p<F><<<blocks_for(d->nbc, kBlock), kBlock, 0, s>>>(n, kbc_of(d), k.P);
     XG_CHECK_LAUNCH(c);
   }
-  k_node_lo<<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, d->vol, d->U, d->scal, fct, d->R, d->P,
-                                                      d->Q, d->A);
+  const bool f32 = sizeof(F) == 4;
+  k_node_lo<F><<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, d->vol, d->U, d->scal, fct, k.R, k.P,
+                                                         d->R, d->P, f32 ? k.lo : nullptr, k.Q,
+                                                         d->A);
   XG_CHECK_LAUNCH(c);
   if (fct) {
-    k_elem_alw<<<blocks_for(ne, kBlock), kBlock, 0, s>>>(n, ne, d->inpoel, d->U, d->R,
-                                                          d->prm.fctclip, d->Q);
+    const F* Ust = f32 ? k.Uf : reinterpret_cast<const F*>(d->U);
+    k_elem_alw<F><<<blocks_for(ne, kBlock), kBlock, 0, s>>>(n, ne, d->inpoel, Ust, k.lo,
+                                                             d->prm.fctclip, k.Q);
     XG_CHECK_LAUNCH(c);
-    k_node_lim<<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, d->R, d->P, d->Q);
+    k_node_lim<F><<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, d->R, d->P, k.Q);
     XG_CHECK_LAUNCH(c);
-    if (d->prm.precision == XG_FP32_FLUX)
-      k_elem_lim<float><<<blocks_for(ne, kBlock), kBlock, 0, s>>>(
-          n, ne, d->inpoel, d->xyz, d->U, d->Q, d->prm.ctau, d->prm.fctsys, d->A);
-    else
-      k_elem_lim<double><<<blocks_for(ne, kBlock), kBlock, 0, s>>>(
-          n, ne, d->inpoel, d->xyz, d->U, d->Q, d->prm.ctau, d->prm.fctsys, d->A);
+    k_elem_lim<F><<<blocks_for(ne, kBlock), kBlock, 0, s>>>(n, ne, d->inpoel, d->xyz, k.geo,
+                                                             d->U, k.Uf, k.Q, d->prm.ctau,
+                                                             d->prm.fctsys, k.A);
     XG_CHECK_LAUNCH(c);
   }
-  k_node_solve<<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, d->vol, d->R, d->A, fct, d->isbc,
-                                                         d->prm.gamma, d->U, &d->scal->dtmin);
+  k_node_solve<F><<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, d->vol, d->R, k.A, d->A, fct,
+                                                            d->isbc, d->prm.gamma, d->U,
+                                                            &d->scal->dtmin);
   XG_CHECK_LAUNCH(c);
   if (d->nbc) {
     k_bc<<<blocks_for(d->nbc, kBlock), kBlock, 0, s>>>(n, kbc_of(d), d->prm.gamma, d->U, d->vol,
@@ -579,6 +763,19 @@ int step(xg_ctx* c, KozCGDev* d) {
     XG_CHECK_LAUNCH(c);
   }
   return XG_OK;
+}
+
+int step(xg_ctx* c, KozCGDev* d) {
+  if (d->prm.precision == XG_FP32_FLUX) return step_impl<float>(c, d, arrays32(d));
+  return step_impl<double>(c, d, arrays64(d));
+}
+
+// FP32 node records [n][8] to FP64 [5][n].
+__global__ void k_rec_to_soa(int64_t n, const float* __restrict__ a, double* __restrict__ b) {
+  const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= n * 5) return;
+  const int64_t c = i / n, p = i - c * n;
+  b[i] = double(a[p * 8 + c]);
 }
 
 }  // namespace
@@ -626,6 +823,15 @@ int xg_kozcg_setup(xg_ctx* c, const xg_kozcg_params* prm, int64_t npoin, const d
     A.plan(d->A, npoin * 5);
     A.plan(d->stage, npoin * 5);
     A.plan(d->V, npoin * 4);
+    if (prm->precision == XG_FP32_FLUX) {
+      A.plan(d->R32, npoin * 8);
+      A.plan(d->P32, npoin * 12);
+      A.plan(d->A32, npoin * 8);
+      A.plan(d->U32, npoin * 5);
+      A.plan(d->lo32, npoin * 5);
+      A.plan(d->Q32, npoin * 10);
+      A.plan(d->geo32, nelem * 10);
+    }
     A.plan(d->isbc, npoin);
     A.plan(d->scal, 1);
     if (pass == 0) {
@@ -643,6 +849,11 @@ int xg_kozcg_setup(xg_ctx* c, const xg_kozcg_params* prm, int64_t npoin, const d
   XG_CUDA(c, cudaMemcpy(d->vol, vol, npoin * 8, cudaMemcpyHostToDevice));
   XG_CUDA(c, cudaMemsetAsync(d->U, 0, npoin * 5 * 8, s));
   XG_CUDA(c, cudaMemsetAsync(d->isbc, 0, npoin, s));
+  if (d->geo32) {
+    k_geo32<<<blocks_for(nelem, kBlock), kBlock, 0, s>>>(npoin, nelem, d->inpoel, d->xyz,
+                                                          d->geo32);
+    XG_CHECK_LAUNCH(c);
+  }
   KScalars k0{0.0, 0ull, 0, 0};
   double big = DBL_MAX;
   std::memcpy(&k0.dtmin, &big, sizeof(double));
@@ -763,8 +974,15 @@ int xg_kozcg_rhs(xg_ctx* c, const double* U, double dt, double* R) {
   XG_CHECK_LAUNCH(c);
   k_set_dt<<<1, 1, 0, s>>>(d->scal, dt);
   XG_CHECK_LAUNCH(c);
-  XG_CUDA(c, cudaMemsetAsync(d->R, 0, d->n * 5 * 8, s));
-  galerkin(s, d, d->A, 0);
+  if (d->prm.precision == XG_FP32_FLUX) {
+    const KArrays<float> k = arrays32(d);
+    XG_CUDA(c, cudaMemsetAsync(k.R, 0, d->n * 8 * 4, s));
+    galerkin<float>(s, d, k, d->A, 0);
+    k_rec_to_soa<<<blocks_for(d->n * 5, kBlock), kBlock, 0, s>>>(d->n, k.R, d->R);
+  } else {
+    XG_CUDA(c, cudaMemsetAsync(d->R, 0, d->n * 5 * 8, s));
+    galerkin<double>(s, d, arrays64(d), d->A, 0);
+  }
   XG_CHECK_LAUNCH(c);
   k_soa_to_aos<<<blocks_for(d->n * 5, kBlock), kBlock, 0, s>>>(d->n, 5, d->R, d->stage);
   XG_CHECK_LAUNCH(c);
