@@ -67,6 +67,10 @@ struct KozCGDev {
   float *R32 = nullptr, *P32 = nullptr, *A32 = nullptr, *U32 = nullptr, *lo32 = nullptr;
   unsigned int* Q32 = nullptr;
   float* geo32 = nullptr;
+  // node adjacency (every pair of nodes sharing a tet) as SELL-32: slice s
+  // of 32 nodes, entry k of node i at aoff[s] + 32 k + lane, -1 padding
+  int64_t nslice = 0;
+  int32_t *aoff = nullptr, *aw = nullptr, *anbr = nullptr;
   // BC program: one thread per BC node
   int64_t nbc = 0;
   int32_t *bcnode = nullptr, *bcdir = nullptr, *bcsymp = nullptr, *dirmask = nullptr;
@@ -440,7 +444,7 @@ __global__ void k_bc_p(int64_t n, KBC bc, F* P) {
 }
 
 // KozCG::alw node part (KozCG.cpp:887-912): P /= vol, low-order solution
-// lo = U + dt R/vol - P+ - P-, the keys of Q reset to (-large, +large).
+// lo = U + dt R/vol - P+ - P-.
 // Without FCT the update of KozCG::solve (KozCG.cpp:1151-1160) goes straight
 // to A.  Racc/Pacc are the element sums (in F); lo and P/vol go to the FP64
 // arrays Rlo/Pout (the same arrays as Racc/Pacc in FP64 mode), and in FP32
@@ -448,8 +452,7 @@ __global__ void k_bc_p(int64_t n, KBC bc, F* P) {
 template <class F>
 __global__ void k_node_lo(int64_t n, const double* __restrict__ vol, const double* __restrict__ U,
                           const KScalars* __restrict__ sc, int fct, const F* Racc, const F* Pacc,
-                          double* Rlo, double* Pout, F* lo32, typename KozT<F>::Key* Q,
-                          double* A) {
+                          double* Rlo, double* Pout, F* lo32, double* A) {
   int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (i >= n) return;
   const double dt = sc->dt;
@@ -467,49 +470,63 @@ __global__ void k_node_lo(int64_t n, const double* __restrict__ vol, const doubl
       const double lo = U[c * n + i] + per_vol(dt * double(Racc[ridx<F>(n, c, i)])) - pp - pn;
       Rlo[c * n + i] = lo;
       if (lo32) lo32[c * n + i] = F(lo);
-      Q[(c * 2 + 0) * n + i] = okey(-big<F>());
-      Q[(c * 2 + 1) * n + i] = okey(big<F>());
     } else {
       A[c * n + i] = U[c * n + i] + per_vol(dt * double(Racc[ridx<F>(n, c, i)]));
     }
   }
 }
 
-// KozCG::alw element part (KozCG.cpp:914-935): allowed limits, from the
-// low-order solution lo and the state U, as F.
+// KozCG::alw element part (KozCG.cpp:914-935): the allowed limits of a node
+// are the maximum / minimum, over the elements holding it, of the element's
+// extremes of the low-order solution lo (and of the state U unless clip).
+// The nodes of those elements are the node and its adjacency, so the same
+// extremes are taken here per node over {i} and its neighbours: max and min
+// are exact, so the bounds are the element loop's, without atomics.  Stored
+// as order-preserving keys (the node pass of the limits reads keys).
 template <class F>
-__global__ void __launch_bounds__(kBlock) k_elem_alw(int64_t n, int64_t ne,
-                                                      const int32_t* __restrict__ inpoel,
+__global__ void __launch_bounds__(kBlock) k_node_alw(int64_t n, const int32_t* __restrict__ aoff,
+                                                      const int32_t* __restrict__ aw,
+                                                      const int32_t* __restrict__ nbr,
                                                       const F* __restrict__ U,
                                                       const F* __restrict__ lo, int clip,
-                                                      typename KozT<F>::Key* Q) {
-  int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  if (e >= ne) return;
-  int32_t N[4];
-  for (int a = 0; a < 4; ++a) N[a] = inpoel[e * 4 + a];
+                                                      typename KozT<F>::Key* __restrict__ Q) {
+  const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= n) return;
+  const int lane = static_cast<int>(i & 31);
+  const int64_t s = i >> 5;
+  const int32_t off = __ldg(aoff + s), w = __ldg(aw + s);
+  F mx[5], mn[5];
+#pragma unroll
   for (int c = 0; c < 5; ++c) {
-    F alwp = -big<F>(), alwn = big<F>();
-    for (int a = 0; a < 4; ++a) {
-      const F l = lo[c * n + N[a]];
-      if (clip) {
-        alwp = fmax(alwp, l);
-        alwn = fmin(alwn, l);
-      } else {
-        const F uo = U[c * n + N[a]];
-        alwp = fmax(alwp, fmax(l, uo));
-        alwn = fmin(alwn, fmin(l, uo));
+    const F l = lo[c * n + i];
+    mx[c] = l;
+    mn[c] = l;
+    if (!clip) {
+      const F u = U[c * n + i];
+      mx[c] = fmax(mx[c], u);
+      mn[c] = fmin(mn[c], u);
+    }
+  }
+#pragma unroll 4
+  for (int k = 0; k < w; ++k) {
+    const int32_t q = __ldg(nbr + off + k * 32 + lane);
+    if (q < 0) continue;
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      const F l = __ldg(lo + c * n + q);
+      mx[c] = fmax(mx[c], l);
+      mn[c] = fmin(mn[c], l);
+      if (!clip) {
+        const F u = __ldg(U + c * n + q);
+        mx[c] = fmax(mx[c], u);
+        mn[c] = fmin(mn[c], u);
       }
     }
-    const auto kp = okey(alwp), kn = okey(alwn);
-    // a key only ever grows (shrinks): an element whose bound does not pass
-    // the one already stored (read through L2, possibly older) skips its
-    // atomic, which cannot change the result
-    for (int a = 0; a < 4; ++a) {
-      auto* qp = Q + (c * 2 + 0) * n + N[a];
-      auto* qn = Q + (c * 2 + 1) * n + N[a];
-      if (kp > __ldcg(qp)) atomicMax(qp, kp);
-      if (kn < __ldcg(qn)) atomicMin(qn, kn);
-    }
+  }
+#pragma unroll
+  for (int c = 0; c < 5; ++c) {
+    Q[(c * 2 + 0) * n + i] = okey(mx[c]);
+    Q[(c * 2 + 1) * n + i] = okey(mn[c]);
   }
 }
 
@@ -738,13 +755,12 @@ int step_impl(xg_ctx* c, KozCGDev* d, const KArrays<F>& k) {
   }
   const bool f32 = sizeof(F) == 4;
   k_node_lo<F><<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, d->vol, d->U, d->scal, fct, k.R, k.P,
-                                                         d->R, d->P, f32 ? k.lo : nullptr, k.Q,
-                                                         d->A);
+                                                         d->R, d->P, f32 ? k.lo : nullptr, d->A);
   XG_CHECK_LAUNCH(c);
   if (fct) {
     const F* Ust = f32 ? k.Uf : reinterpret_cast<const F*>(d->U);
-    k_elem_alw<F><<<blocks_for(ne, kBlock), kBlock, 0, s>>>(n, ne, d->inpoel, Ust, k.lo,
-                                                             d->prm.fctclip, k.Q);
+    k_node_alw<F><<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, d->aoff, d->aw, d->anbr, Ust,
+                                                            k.lo, d->prm.fctclip, k.Q);
     XG_CHECK_LAUNCH(c);
     k_node_lim<F><<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, d->R, d->P, k.Q);
     XG_CHECK_LAUNCH(c);
@@ -801,6 +817,55 @@ int xg_kozcg_setup(xg_ctx* c, const xg_kozcg_params* prm, int64_t npoin, const d
       return fail(c, XG_ERR_ARG, "kozcg_setup: element node id out of range");
     ip[i] = static_cast<int32_t>(inpoel[i]);
   }
+  // node adjacency for the allowed limits: the elements of each node
+  // (counting sort), then each node's sorted distinct element neighbours,
+  // laid out as SELL-32
+  const int64_t nslice = (npoin + 31) / 32;
+  std::vector<int32_t> aoff(nslice + 1), aw(nslice), anbr;
+  {
+    std::vector<int64_t> eptr(npoin + 1, 0);
+    for (int64_t i = 0; i < nelem * 4; ++i) ++eptr[ip[i] + 1];
+    for (int64_t i = 0; i < npoin; ++i) eptr[i + 1] += eptr[i];
+    std::vector<int32_t> eln(nelem * 4);
+    {
+      std::vector<int64_t> fill(eptr.begin(), eptr.end() - 1);
+      for (int64_t e = 0; e < nelem; ++e)
+        for (int a = 0; a < 4; ++a) eln[fill[ip[e * 4 + a]]++] = static_cast<int32_t>(e);
+    }
+    std::vector<int64_t> nptr(npoin + 1, 0);
+    std::vector<int32_t> nb;
+    nb.reserve(static_cast<size_t>(npoin) * 16);
+    std::vector<int32_t> tmp;
+    for (int64_t i = 0; i < npoin; ++i) {
+      tmp.clear();
+      for (int64_t k = eptr[i]; k < eptr[i + 1]; ++k)
+        for (int a = 0; a < 4; ++a) {
+          const int32_t j = ip[int64_t(eln[k]) * 4 + a];
+          if (j != i) tmp.push_back(j);
+        }
+      std::sort(tmp.begin(), tmp.end());
+      tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
+      nb.insert(nb.end(), tmp.begin(), tmp.end());
+      nptr[i + 1] = static_cast<int64_t>(nb.size());
+    }
+    int64_t tot = 0;
+    for (int64_t sl = 0; sl < nslice; ++sl) {
+      int64_t w = 0;
+      for (int64_t i = sl * 32; i < std::min<int64_t>(npoin, sl * 32 + 32); ++i)
+        w = std::max(w, nptr[i + 1] - nptr[i]);
+      aoff[sl] = static_cast<int32_t>(tot);
+      aw[sl] = static_cast<int32_t>(w);
+      tot += 32 * w;
+      if (tot >= (int64_t(1) << 31)) return fail(c, XG_ERR_ARG, "kozcg_setup: adjacency too large");
+    }
+    aoff[nslice] = static_cast<int32_t>(tot);
+    anbr.assign(static_cast<size_t>(std::max<int64_t>(1, tot)), -1);
+    for (int64_t i = 0; i < npoin; ++i) {
+      const int64_t sl = i / 32, lane = i % 32;
+      for (int64_t k = nptr[i]; k < nptr[i + 1]; ++k)
+        anbr[aoff[sl] + (k - nptr[i]) * 32 + lane] = nb[k];
+    }
+  }
   if (c->kozcg) {
     XG_CUDA(c, cudaStreamSynchronize(c->stream));
     destroy_kozcg(c->kozcg);
@@ -811,6 +876,7 @@ int xg_kozcg_setup(xg_ctx* c, const xg_kozcg_params* prm, int64_t npoin, const d
   d->n = npoin;
   d->ne = nelem;
   d->prm = *prm;
+  d->nslice = nslice;
   for (int pass = 0; pass < 2; ++pass) {
     Arena& A = d->arena;
     A.plan(d->inpoel, nelem * 4);
@@ -823,6 +889,9 @@ int xg_kozcg_setup(xg_ctx* c, const xg_kozcg_params* prm, int64_t npoin, const d
     A.plan(d->A, npoin * 5);
     A.plan(d->stage, npoin * 5);
     A.plan(d->V, npoin * 4);
+    A.plan(d->aoff, aoff.size());
+    A.plan(d->aw, aw.size());
+    A.plan(d->anbr, anbr.size());
     if (prm->precision == XG_FP32_FLUX) {
       A.plan(d->R32, npoin * 8);
       A.plan(d->P32, npoin * 12);
@@ -847,6 +916,9 @@ int xg_kozcg_setup(xg_ctx* c, const xg_kozcg_params* prm, int64_t npoin, const d
   XG_CUDA(c, cudaMemcpy(d->inpoel, ip.data(), ip.size() * 4, cudaMemcpyHostToDevice));
   XG_CUDA(c, cudaMemcpy(d->xyz, coord, npoin * 3 * 8, cudaMemcpyHostToDevice));
   XG_CUDA(c, cudaMemcpy(d->vol, vol, npoin * 8, cudaMemcpyHostToDevice));
+  XG_CUDA(c, cudaMemcpy(d->aoff, aoff.data(), aoff.size() * 4, cudaMemcpyHostToDevice));
+  XG_CUDA(c, cudaMemcpy(d->aw, aw.data(), aw.size() * 4, cudaMemcpyHostToDevice));
+  XG_CUDA(c, cudaMemcpy(d->anbr, anbr.data(), anbr.size() * 4, cudaMemcpyHostToDevice));
   XG_CUDA(c, cudaMemsetAsync(d->U, 0, npoin * 5 * 8, s));
   XG_CUDA(c, cudaMemsetAsync(d->isbc, 0, npoin, s));
   if (d->geo32) {
