@@ -13,12 +13,12 @@
 // Layout: node arrays SoA [ncomp][n] (U, R = rhs then low-order solution,
 // P = antidiffusive sums +/- per component, A = limited contributions),
 // elements as int32 [T][4].  Element kernels (one thread per tet) scatter to
-// their four nodes with FP64 atomic adds; the allowed limits Q+/- are
-// maxima/minima kept as order-preserving 64-bit keys so that atomicMax /
-// atomicMin on integers implement them exactly and deterministically.  Node
+// their four nodes with atomic adds.  The allowed limits Q+/- (extremes over
+// the elements holding a node) are taken per node over the node adjacency,
+// which holds the same nodes, and kept as order-preserving keys.  Node
 // kernels (one thread per node) do the per-node algebra between the element
 // passes.  One step is:
-//   step_begin -> zero -> node_prim -> elem_rhs_aec -> bc_p -> node_lo -> elem_alw ->
+//   step_begin -> zero -> node_prim -> elem_rhs_aec -> bc_p -> node_lo -> node_alw ->
 //   node_lim -> elem_lim -> node_solve -> bc (+ CFL minimum for the next step)
 //
 // FP32-element mode: the element passes read an FP32 copy of the state (made
@@ -181,10 +181,6 @@ struct KozT<float> {
   using Key = unsigned int;
 };
 
-template <class F>
-__device__ __forceinline__ F big() {
-  return sizeof(F) == 8 ? F(DBL_MAX) : F(FLT_MAX);
-}
 __device__ __forceinline__ unsigned long long okey(double v) { return dkey(v); }
 __device__ __forceinline__ unsigned int okey(float v) {
   const unsigned int b = __float_as_uint(v);
