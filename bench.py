@@ -414,9 +414,9 @@ def e2e_run(r, U0, steps, world):
     barrier(world)
     t0 = time.perf_counter()
     for _ in range(steps):
-        r.set_state(host)  # H2D of the step's input state
+        r.set_state(host)  # H2D of the step's input state (pinned)
         r.run(1)
-        host[:] = r.state()[0]  # D2H of the step's result
+        r.state(out=host)  # D2H of the step's result into the same pinned buffer
     t1 = time.perf_counter()
     barrier(world)
     return (t1 - t0) * 1e3

@@ -245,8 +245,15 @@ class RieCG:
         assert U.shape == (self.n, 5)
         self.ctx.check(self.lib.xg_riecg_set_state(self.ctx.h, p(U), t))
 
-    def state(self):
-        U = np.zeros((self.n, 5))
+    def state(self, out=None):
+        """(U, t); U node-major (n, 5).  ``out``: a C-contiguous float64
+        (n, 5) array to download into (pinned host memory for a DMA copy)."""
+        if out is None:
+            U = np.zeros((self.n, 5))
+        else:
+            if out.shape != (self.n, 5) or out.dtype != np.float64 or not out.flags.c_contiguous:
+                raise ValueError("out must be a C-contiguous float64 (n, 5) array")
+            U = out
         t = C.c_double()
         self.ctx.check(self.lib.xg_riecg_get_state(self.ctx.h, p(U), C.byref(t)))
         return U, t.value
