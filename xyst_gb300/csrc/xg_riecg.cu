@@ -1182,6 +1182,23 @@ __global__ void __launch_bounds__(kBlock) k_dt(int64_t n, const double* __restri
   block_min_atomic(dtp, dtmin);
 }
 
+// The same minimum with the FP32-mode formula of the step epilogue
+// (node_dt_f: FP32 arithmetic on the FP64 state, cbrt(vol) given), so that
+// a state set from the host gets the dt the time loop itself would form.
+__global__ void __launch_bounds__(kBlock) k_dt_f(int64_t n, const double* __restrict__ U,
+                                                  const float* __restrict__ cbrtv, double gamma,
+                                                  unsigned long long* dtmin) {
+  int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  double dtp = DBL_MAX;
+  if (p < n) {
+    double u[5];
+#pragma unroll
+    for (int c = 0; c < 5; ++c) u[c] = U[c * n + p];
+    dtp = double(node_dt_f(u, cbrtv[p], float(gamma)));
+  }
+  block_min_atomic(dtp, dtmin);
+}
+
 // Step prologue (RieCG::dt reduction target + RieCG::advance,
 // src/Inciter/RieCG.cpp:839-869): dt = cfl * min, blowup when dt < eps; then
 // reset the running minimum for the next step.
@@ -1383,8 +1400,12 @@ int do_stage(xg_ctx* c, RieCGDev* d, int stage) {
 int refresh_dt(xg_ctx* c, RieCGDev* d) {
   k_reset_min<<<1, 1, 0, c->stream>>>(d->scal);
   XG_CHECK_LAUNCH(c);
-  k_dt<<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(d->n, d->U, d->vol, d->prm.gamma,
-                                                            &d->scal->dtmin);
+  if (d->fp32)
+    k_dt_f<<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(d->n, d->U, d->cbrtv,
+                                                                d->prm.gamma, &d->scal->dtmin);
+  else
+    k_dt<<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(d->n, d->U, d->vol, d->prm.gamma,
+                                                              &d->scal->dtmin);
   XG_CHECK_LAUNCH(c);
   d->dt_valid = true;
   return XG_OK;
