@@ -673,7 +673,7 @@ __global__ void __launch_bounds__(kBlock) k_pc_upper_res(
 // and MODE 2 (mixed) also close a CG iteration: partial (r,r), the count and
 // the stopping test.
 template <class T, class V, class CI, int MODE>
-__global__ void __launch_bounds__(kBlock) k_pc_lower(int64_t n, const int32_t* __restrict__ soffL,
+__global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? 6 : 1) k_pc_lower(int64_t n, const int32_t* __restrict__ soffL,
                                                       const int32_t* __restrict__ swL, CI ci,
                                                       const V* __restrict__ nvL,
                                                       const float* __restrict__ srow,
