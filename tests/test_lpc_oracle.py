@@ -125,3 +125,74 @@ def test_first_order_factor_beats_jacobi():
     itj = _pcg(A, b2, lambda r: lpc.precondition(g, np.zeros_like(g.le), r))
     itf = _pcg(A, b2, lambda r: lpc.precondition(g, g.le, r))
     assert itf < 0.7 * itj
+
+
+def _pcg_its(A, b, apply_m, tol=1e-8, maxit=5000):
+    """Iterations of a plain PCG (x0 = 0) to ||r|| < tol ||b||."""
+    x = np.zeros_like(b)
+    r = b.copy()
+    z = apply_m(r)
+    p = z.copy()
+    rz = r @ z
+    nb = np.linalg.norm(b)
+    for k in range(1, maxit + 1):
+        q = A @ p
+        al = rz / (p @ q)
+        x += al * p
+        r -= al * q
+        if np.linalg.norm(r) < tol * nb:
+            return k
+        z = apply_m(r)
+        rz_new = r @ z
+        p = z + (rz_new / rz) * p
+        rz = rz_new
+    return maxit
+
+
+def test_pattern_optimal_factor_bounds_the_learned_one():
+    """The trace loss the network is trained on, minimised exactly on the
+    factor's pattern (strictly lower part of A, column by column: the
+    factorised sparse approximate inverse), is the best a learned N of that
+    pattern can reach.  On a ChoCG pressure system (hydrostat node) it gains
+    only ~10 % of PCG iterations over the first-order factor N = E, which in
+    turn halves Jacobi's: the pattern, not the network, bounds the learned
+    preconditioner."""
+    m = mesh.cube(11, jitter=0.2, seed=3, numbering="rcm", perm_seed=10)
+    ia, ja, a = oracle.pressure_matrix(m["coord"], m["inpoel"])
+    A = _dense(ia, ja, a)
+    n = A.shape[0]
+    A[0, :] = 0.0
+    A[:, 0] = 0.0
+    A[0, 0] = A[1, 1]
+    A *= np.sign(A[1, 1])  # positive definite
+    s = 1.0 / np.sqrt(np.abs(np.diag(A)))
+    Ah = s[:, None] * A * s[None, :]
+    E = np.eye(n) - Ah
+    pattern = np.tril(A != 0.0, -1)
+    N1 = np.where(pattern, E, 0.0)
+    Nf = np.zeros((n, n))
+    for j in range(n):
+        P = np.nonzero(pattern[:, j])[0]
+        if P.size:
+            Nf[P, j] = np.linalg.solve(Ah[np.ix_(P, P)], -Ah[P, j])
+
+    def loss(N):
+        L = np.eye(n) + N
+        return (np.trace(L.T @ Ah @ L) - n) / n
+
+    assert loss(Nf) < loss(N1) < 0.0
+    rng = np.random.default_rng(1)
+    b = rng.standard_normal(n)
+    b[0] = 0.0
+    d = np.diag(A)
+
+    def factor(N):
+        L = np.eye(n) + N
+        return lambda r: s * (L @ (L.T @ (s * r)))
+
+    its_j = _pcg_its(A, b, lambda r: r / d)
+    its_1 = _pcg_its(A, b, factor(N1))
+    its_f = _pcg_its(A, b, factor(Nf))
+    assert its_1 < 0.7 * its_j
+    assert its_f < its_1
+    assert its_f > 0.8 * its_1
