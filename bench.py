@@ -430,6 +430,17 @@ def barrier(world):
         _dist.barrier()
 
 
+def max_over_ranks(vals, world):
+    """Element-wise maximum of a few floats over the replica ranks (the
+    slowest rank's times define the whole job's)."""
+    if world <= 1 or _dist is None:
+        return [float(v) for v in vals]
+    import torch
+    t = torch.tensor([float(v) for v in vals], dtype=torch.float64)
+    _dist.all_reduce(t, op=_dist.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
 def _cuda_profiler(on):
     """cudaProfilerStart/Stop through the CUDA runtime, so that
     `ncu --profile-from-start off` captures exactly the bracketed region."""
@@ -548,13 +559,7 @@ def main():
             cpu_cho = cpu_chocg()
     res = run_gpu(args, rank, world)
     # max over ranks
-    ms = res["ms"]
-    e2e_ms = res["e2e_ms"]
-    if world > 1:
-        import torch
-        t = torch.tensor([ms, e2e_ms], dtype=torch.float64)
-        _dist.all_reduce(t, op=_dist.ReduceOp.MAX)
-        ms, e2e_ms = float(t[0]), float(t[1])
+    ms, e2e_ms = max_over_ranks([res["ms"], res["e2e_ms"]], world)
     if rank != 0:
         return
     n = res["n"]
