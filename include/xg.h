@@ -169,7 +169,8 @@ typedef struct xg_kozcg_params {
   int fctsys;    /* bit c set: component c is limited as part of the system */
   int precision; /* enum xg_precision: XG_FP32_FLUX forms the element terms
                     (Galerkin residual, antidiffusive and limited element
-                    contributions) in FP32 and sums them into FP64 nodes */
+                    contributions) in FP32, sums them per node in FP32 and
+                    updates the FP64 state in FP64 */
 } xg_kozcg_params;
 
 /* Mesh of KozCG: coordinates, nodal volumes and tetrahedra (Discretization
