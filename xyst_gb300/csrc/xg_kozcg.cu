@@ -64,7 +64,7 @@ struct KozCGDev {
   double* V = nullptr;  // [n][4] velocity and pressure per node (FP32 packed in the first half)
   // FP32-element mode: element sums, the FP32 state, the low-order solution
   // as the allowed-limit pass reads it, 32-bit limit keys, element geometry
-  float *R32 = nullptr, *P32 = nullptr, *A32 = nullptr, *U32 = nullptr, *lo32 = nullptr;
+  float *R32 = nullptr, *A32 = nullptr, *U32 = nullptr, *lo32 = nullptr;
   unsigned int* Q32 = nullptr;
   float* geo32 = nullptr;
   // node adjacency (every pair of nodes sharing a tet) as SELL-32: slice s
@@ -196,25 +196,31 @@ __device__ __forceinline__ unsigned long long tobits(double v) { return __double
 __device__ __forceinline__ unsigned int tobits(float v) { return __float_as_uint(v); }
 
 // Where component c of node i lives in the element sums: FP64 mode SoA
-// [5][n] (R, A) and [10][n] (P); FP32 mode node records [n][8] and [n][12],
-// so that one element adds a node's contribution with vector atomics
-// (red.global.add.v4/v2.f32) instead of one atomic per component.
-template <class F>
+// [5][n] (R, A) and [10][n] (P); FP32 mode node records, so that one element
+// adds a node's contribution with 16-byte vector atomics
+// (red.global.add.v4.f32) instead of one atomic per component: R and P share
+// a [n][16] record (R at 0..4, P+/- at 5..14, P addressed from R + 5), A has
+// [n][8].
+constexpr int kRP = 16;  // FP32 R+P record
+constexpr int kAR = 8;   // FP32 A record
+template <class F, int S>
 __device__ __forceinline__ int64_t ridx(int64_t n, int c, int64_t i) {
-  return sizeof(F) == 4 ? i * 8 + c : c * n + i;
+  return sizeof(F) == 4 ? i * S + c : c * n + i;
 }
 template <class F>
 __device__ __forceinline__ int64_t pidx(int64_t n, int cs, int64_t i) {
-  return sizeof(F) == 4 ? i * 12 + cs : cs * n + i;
+  return sizeof(F) == 4 ? i * kRP + cs : cs * n + i;
 }
 
-// r[5] added to node i's record of R or A.
+// r[5] added to node i's record of R (S = kRP) or A (S = kAR).
+template <int S>
 __device__ __forceinline__ void add5(double* R, int64_t n, int64_t i, const double r[5]) {
   for (int c = 0; c < 5; ++c) atomicAdd(R + c * n + i, r[c]);
 }
+template <int S>
 __device__ __forceinline__ void add5(float* R, int64_t, int64_t i, const float r[5]) {
-  atomicAdd(reinterpret_cast<float4*>(R + i * 8), make_float4(r[0], r[1], r[2], r[3]));
-  atomicAdd(R + i * 8 + 4, r[4]);
+  atomicAdd(reinterpret_cast<float4*>(R + i * S), make_float4(r[0], r[1], r[2], r[3]));
+  atomicAdd(R + i * S + 4, r[4]);
 }
 
 // Per-node velocity and pressure (the node-wise quotients kozak::rhs forms
@@ -367,7 +373,8 @@ __global__ void __launch_bounds__(kBlock) k_elem_rhs_aec(int64_t n, int64_t ne,
       r[a][4] += cg * (ue[4] + pr) * uj;
     }
   }
-  for (int a = 0; a < 4; ++a) add5(R, n, N[a], r[a]);
+  if (!fct || sizeof(F) == 8)
+    for (int a = 0; a < 4; ++a) add5<kRP>(R, n, N[a], r[a]);
   if (!fct) return;
   if constexpr (sizeof(F) == 8) {
     for (int c = 0; c < 5; ++c)
@@ -383,23 +390,26 @@ __global__ void __launch_bounds__(kBlock) k_elem_rhs_aec(int64_t n, int64_t ne,
           atomicAdd(P + (c * 2 + 1) * n + N[a], aec);
       }
   } else {
-    // per node the ten sums (+, - per component) in one record: the sign
-    // that does not apply adds 0
+    // per node its residual and its ten antidiffusive sums (+, - per
+    // component; the sign that does not apply adds 0) in one [16] record:
+    // four vector atomics
     for (int a = 0; a < 4; ++a) {
-      F pa[10];
+      F v[16];
+      for (int c = 0; c < 5; ++c) v[c] = r[a][c];
       for (int c = 0; c < 5; ++c) {
         F aec = F(0.0);
         for (int b = 0; b < 4; ++b) {
           const F m = t.J / F(120.0) * ((a == b) ? F(3.0) : F(-1.0));
           aec += m * ctau * u[b][c];
         }
-        pa[c * 2 + 0] = aec > F(0.0) ? aec : F(0.0);
-        pa[c * 2 + 1] = aec < F(0.0) ? aec : F(0.0);
+        v[5 + c * 2 + 0] = aec > F(0.0) ? aec : F(0.0);
+        v[5 + c * 2 + 1] = aec < F(0.0) ? aec : F(0.0);
       }
-      float* q = P + int64_t(N[a]) * 12;
-      atomicAdd(reinterpret_cast<float4*>(q), make_float4(pa[0], pa[1], pa[2], pa[3]));
-      atomicAdd(reinterpret_cast<float4*>(q + 4), make_float4(pa[4], pa[5], pa[6], pa[7]));
-      atomicAdd(reinterpret_cast<float2*>(q + 8), make_float2(pa[8], pa[9]));
+      v[15] = F(0.0);
+      float* q = R + int64_t(N[a]) * kRP;
+      for (int k = 0; k < 4; ++k)
+        atomicAdd(reinterpret_cast<float4*>(q + 4 * k),
+                  make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]));
     }
   }
 }
@@ -463,11 +473,11 @@ __global__ void k_node_lo(int64_t n, const double* __restrict__ vol, const doubl
       double pn = per_vol(double(Pacc[pidx<F>(n, c * 2 + 1, i)]));
       Pout[(c * 2 + 0) * n + i] = pp;
       Pout[(c * 2 + 1) * n + i] = pn;
-      const double lo = U[c * n + i] + per_vol(dt * double(Racc[ridx<F>(n, c, i)])) - pp - pn;
+      const double lo = U[c * n + i] + per_vol(dt * double(Racc[ridx<F, kRP>(n, c, i)])) - pp - pn;
       Rlo[c * n + i] = lo;
       if (lo32) lo32[c * n + i] = F(lo);
     } else {
-      A[c * n + i] = U[c * n + i] + per_vol(dt * double(Racc[ridx<F>(n, c, i)]));
+      A[c * n + i] = U[c * n + i] + per_vol(dt * double(Racc[ridx<F, kRP>(n, c, i)]));
     }
   }
 }
@@ -585,7 +595,7 @@ __global__ void __launch_bounds__(kBlock) k_elem_lim(int64_t n, int64_t ne,
   for (int a = 0; a < 4; ++a) {
     F ca[5];
     for (int c = 0; c < 5; ++c) ca[c] = coef[c] * aec[c][a];
-    add5(A, n, N[a], ca);
+    add5<kAR>(A, n, N[a], ca);
   }
 }
 
@@ -607,7 +617,7 @@ __global__ void __launch_bounds__(kBlock) k_node_solve(int64_t n, const double* 
     const double v = vol[i];
     const double iv = sizeof(F) == 4 ? 1.0 / v : 0.0;  // FP32 mode: one division
     for (int c = 0; c < 5; ++c) {
-      const double a = double(Aacc[ridx<F>(n, c, i)]);
+      const double a = double(Aacc[ridx<F, kAR>(n, c, i)]);
       u[c] = fct ? R[c * n + i] + (sizeof(F) == 4 ? a * iv : a / v) : A[c * n + i];
       U[c * n + i] = u[c];
     }
@@ -714,7 +724,7 @@ KArrays<double> arrays64(KozCGDev* d) {
   return KArrays<double>{d->R, d->P, d->A, nullptr, d->V, d->R, d->Q, nullptr};
 }
 KArrays<float> arrays32(KozCGDev* d) {
-  return KArrays<float>{d->R32, d->P32, d->A32, d->U32, reinterpret_cast<float*>(d->V),
+  return KArrays<float>{d->R32, d->R32 + 5, d->A32, d->U32, reinterpret_cast<float*>(d->V),
                         d->lo32, d->Q32, d->geo32};
 }
 
@@ -736,12 +746,16 @@ int step_impl(xg_ctx* c, KozCGDev* d, const KArrays<F>& k) {
   cudaStream_t s = c->stream;
   const int64_t n = d->n, ne = d->ne;
   const int fct = d->prm.fct;
-  // FP64: R, A [5][n], P [10][n]; FP32: R, A [n][8], P [n][12]
-  const int64_t rb = sizeof(F) == 4 ? 8 * 4 : 5 * 8, pb = sizeof(F) == 4 ? 12 * 4 : 10 * 8;
-  XG_CUDA(c, cudaMemsetAsync(k.R, 0, n * rb, s));
-  if (fct) {
-    XG_CUDA(c, cudaMemsetAsync(k.P, 0, n * pb, s));
-    XG_CUDA(c, cudaMemsetAsync(k.A, 0, n * rb, s));
+  // FP64: R, A [5][n], P [10][n]; FP32: R with P [n][16], A [n][8]
+  if (sizeof(F) == 4) {
+    XG_CUDA(c, cudaMemsetAsync(k.R, 0, n * kRP * 4, s));
+    if (fct) XG_CUDA(c, cudaMemsetAsync(k.A, 0, n * kAR * 4, s));
+  } else {
+    XG_CUDA(c, cudaMemsetAsync(k.R, 0, n * 5 * 8, s));
+    if (fct) {
+      XG_CUDA(c, cudaMemsetAsync(k.P, 0, n * 10 * 8, s));
+      XG_CUDA(c, cudaMemsetAsync(k.A, 0, n * 5 * 8, s));
+    }
   }
   galerkin<F>(s, d, k, d->U, fct);
   XG_CHECK_LAUNCH(c);
@@ -782,12 +796,12 @@ int step(xg_ctx* c, KozCGDev* d) {
   return step_impl<double>(c, d, arrays64(d));
 }
 
-// FP32 node records [n][8] to FP64 [5][n].
+// The residual of FP32 node records [n][16] to FP64 [5][n].
 __global__ void k_rec_to_soa(int64_t n, const float* __restrict__ a, double* __restrict__ b) {
   const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (i >= n * 5) return;
   const int64_t c = i / n, p = i - c * n;
-  b[i] = double(a[p * 8 + c]);
+  b[i] = double(a[p * kRP + c]);
 }
 
 }  // namespace
@@ -889,8 +903,7 @@ int xg_kozcg_setup(xg_ctx* c, const xg_kozcg_params* prm, int64_t npoin, const d
     A.plan(d->aw, aw.size());
     A.plan(d->anbr, anbr.size());
     if (prm->precision == XG_FP32_FLUX) {
-      A.plan(d->R32, npoin * 8);
-      A.plan(d->P32, npoin * 12);
+      A.plan(d->R32, npoin * 16);  // R and P records
       A.plan(d->A32, npoin * 8);
       A.plan(d->U32, npoin * 5);
       A.plan(d->lo32, npoin * 5);
@@ -1044,7 +1057,7 @@ int xg_kozcg_rhs(xg_ctx* c, const double* U, double dt, double* R) {
   XG_CHECK_LAUNCH(c);
   if (d->prm.precision == XG_FP32_FLUX) {
     const KArrays<float> k = arrays32(d);
-    XG_CUDA(c, cudaMemsetAsync(k.R, 0, d->n * 8 * 4, s));
+    XG_CUDA(c, cudaMemsetAsync(k.R, 0, d->n * kRP * 4, s));
     galerkin<float>(s, d, k, d->A, 0);
     k_rec_to_soa<<<blocks_for(d->n * 5, kBlock), kBlock, 0, s>>>(d->n, k.R, d->R);
   } else {
