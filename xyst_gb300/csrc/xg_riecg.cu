@@ -443,23 +443,6 @@ struct EntOf<double> {
   using type = Ent64;
 };
 
-__device__ __forceinline__ void load_ent(const int4* ent, int32_t e, int32_t& q, float& d0,
-                                         float& d1, float& d2) {
-  const int4 v = __ldg(ent + e);
-  q = v.x;
-  d0 = __int_as_float(v.y);
-  d1 = __int_as_float(v.z);
-  d2 = __int_as_float(v.w);
-}
-__device__ __forceinline__ void load_ent(const Ent64* ent, int32_t e, int32_t& q, double& d0,
-                                         double& d1, double& d2) {
-  const double2* p = reinterpret_cast<const double2*>(ent + e);
-  const double2 a = __ldg(p), b = __ldg(p + 1);
-  d0 = a.x;
-  d1 = a.y;
-  d2 = b.x;
-  q = __double2loint(b.y);
-}
 
 // Ring entries: copy one entry into its shared-memory slot, decode a landed one.
 template <class E>
