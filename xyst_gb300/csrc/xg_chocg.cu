@@ -20,12 +20,16 @@
 //   adjacency     SELL-32 over both ends of every edge, entry (k, lane) of
 //                 slice s at off[s] + 32k + lane: the neighbour (~id when the
 //                 node is the canonical second end) and (d0, d1, d2, d4), the
-//                 dual-face normal and the viscous coefficient of the edge.
+//                 dual-face normal and the viscous coefficient of the edge,
+//                 plus |d| / |x_a - x_b| for the pressure damping
+//   bnode, park   boundary-node list and [nb][9] domain sums between passes
 // Every edge term is evaluated in the edge's canonical orientation at both
 // ends, so the two ends see bit-identical values and each node owns its
 // writes (no atomics except the scalar CFL minimum).  A node's neighbours are
 // visited in increasing id, which for an unrenumbered mesh is the order in
-// which the reference's edge loop reaches the node.
+// which the reference's edge loop reaches the node.  Each node kernel runs
+// as a domain pass over all nodes and a pass over the boundary nodes that
+// adds the boundary-triangle terms (see node_of).
 
 #include <algorithm>
 #include <cfloat>
