@@ -58,6 +58,17 @@ def test_host_setup_matches_oracle(numbering):
     assert np.array_equal(e5, o5) and np.array_equal(d5, od5)
 
 
+@pytest.mark.parametrize("ncoef", [3, 5])
+def test_threaded_edge_integrals_match_oracle(ncoef):
+    """Large enough (15,625 nodes) for the row-parallel edge integrals: still
+    the oracle's serial element-order sums, bit for bit."""
+    m = mesh.cube(25, jitter=0.2, seed=4, numbering="random", perm_seed=6)
+    ops = riecg.operators(m, sym_sets=[1, 2, 3, 4, 5, 6], renumber=True)
+    e, d = riecg.edges(ops["coord"], ops["inpoel"], gid=ops["gid"], ncoef=ncoef)
+    eo, do = oracle.domint(ops["coord"], ops["inpoel"], gid=ops["gid"], ncoef=ncoef)
+    assert np.array_equal(e, eo) and np.array_equal(d, do)
+
+
 def test_rcm_is_permutation_and_reduces_bandwidth():
     m = mesh.cube(9, numbering="random", perm_seed=1)
     perm = riecg.rcm(m["inpoel"], m["coord"].shape[1])

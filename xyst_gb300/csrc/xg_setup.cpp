@@ -1,7 +1,10 @@
 // Host-side operator setup: the caller side of xg_riecg_setup.  Builds, from
 // a tetrahedron mesh, the arrays RieCG computes once per mesh (nodal
 // volumes, domain edge integrals, boundary point normals) and a locality
-// renumbering.  Plain C++; linear or n log n in the mesh size.
+// renumbering.  Plain C++; linear or n log n in the mesh size.  The edge
+// integrals run on all host cores, each thread owning whole rows of the edge
+// table and summing every edge's element contributions in element order, so
+// the result is the serial one bit for bit.
 
 #include <algorithm>
 #include <cmath>
@@ -10,6 +13,7 @@
 #include <numeric>
 #include <queue>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/xg.h"
@@ -39,6 +43,28 @@ void psup(int64_t n, int64_t nelem, const uint64_t* inpoel, std::vector<int64_t>
     adj.insert(adj.end(), b, u);
     ptr[i + 1] = static_cast<int64_t>(adj.size());
   }
+}
+
+// fn(i) for i in [0, n) on the host's cores, in contiguous chunks.
+template <class Fn>
+void parallel_rows(int64_t n, Fn fn) {
+  unsigned hw = std::thread::hardware_concurrency();
+  int64_t nt = std::min<int64_t>(hw ? hw : 1, 64);
+  if (n < 8192) nt = 1;
+  if (nt <= 1) {
+    for (int64_t i = 0; i < n; ++i) fn(i);
+    return;
+  }
+  const int64_t chunk = (n + nt - 1) / nt;
+  std::vector<std::thread> th;
+  for (int64_t t = 0; t < nt; ++t) {
+    const int64_t b = t * chunk, e = std::min(n, b + chunk);
+    if (b >= e) break;
+    th.emplace_back([b, e, &fn] {
+      for (int64_t i = b; i < e; ++i) fn(i);
+    });
+  }
+  for (auto& x : th) x.join();
 }
 
 inline void cross(double ax, double ay, double az, double bx, double by, double bz, double& rx,
@@ -142,64 +168,88 @@ int xg_mesh_edges(int64_t npoin, const double* coord, int64_t nelem, const uint6
           col[fill[b]++] = a;
       }
   }
-  std::vector<int64_t> rptr(npoin + 1, 0);
-  std::vector<uint64_t> rcol;
-  rcol.reserve(col.size() / 4);
-  for (int64_t i = 0; i < npoin; ++i) {
+  // each row's distinct neighbours, sorted by gid (rows in parallel)
+  std::vector<int64_t> ucnt(npoin);
+  parallel_rows(npoin, [&](int64_t i) {
     auto b = col.begin() + cnt[i], en = col.begin() + cnt[i + 1];
     std::sort(b, en, [&](uint64_t p, uint64_t q) { return G(p) < G(q); });
-    auto u = std::unique(b, en);
-    rcol.insert(rcol.end(), b, u);
-    rptr[i + 1] = static_cast<int64_t>(rcol.size());
-  }
+    ucnt[i] = std::unique(b, en) - b;
+  });
+  std::vector<int64_t> rptr(npoin + 1, 0);
+  for (int64_t i = 0; i < npoin; ++i) rptr[i + 1] = rptr[i] + ucnt[i];
+  std::vector<uint64_t> rcol(rptr[npoin]);
+  parallel_rows(npoin, [&](int64_t i) {
+    std::copy(col.begin() + cnt[i], col.begin() + cnt[i] + ucnt[i], rcol.begin() + rptr[i]);
+  });
   const int64_t ne = static_cast<int64_t>(rcol.size());
   *nedge = ne;
   if (cap < ne) return XG_OK;
   if (!edges || !dint) return XG_ERR_ARG;
+  // the elements of every node in increasing element id
+  std::vector<int64_t> eptr(npoin + 1, 0);
+  for (int64_t e = 0; e < nelem; ++e)
+    for (int a = 0; a < 4; ++a) ++eptr[inpoel[e * 4 + a] + 1];
+  for (int64_t i = 0; i < npoin; ++i) eptr[i + 1] += eptr[i];
+  std::vector<int64_t> elist(eptr[npoin]);
+  {
+    std::vector<int64_t> fill(eptr.begin(), eptr.end() - 1);
+    for (int64_t e = 0; e < nelem; ++e)
+      for (int a = 0; a < 4; ++a) elist[fill[inpoel[e * 4 + a]]++] = e;
+  }
+  // row r sums, element by element in increasing id, the contributions of
+  // the edges it owns (its smaller-gid end): every edge's sum in the element
+  // order of the serial element loop
   std::vector<double> D(static_cast<size_t>(ne) * ncoef, 0.0);
-  for (int64_t e = 0; e < nelem; ++e) {
-    const uint64_t* N = inpoel + e * 4;
-    double ba[3] = {x[N[1]] - x[N[0]], y[N[1]] - y[N[0]], z[N[1]] - z[N[0]]};
-    double ca[3] = {x[N[2]] - x[N[0]], y[N[2]] - y[N[0]], z[N[2]] - z[N[0]]};
-    double da[3] = {x[N[3]] - x[N[0]], y[N[3]] - y[N[0]], z[N[3]] - z[N[0]]};
-    double g[4][3];
-    cross(ca[0], ca[1], ca[2], da[0], da[1], da[2], g[1][0], g[1][1], g[1][2]);
-    cross(da[0], da[1], da[2], ba[0], ba[1], ba[2], g[2][0], g[2][1], g[2][2]);
-    cross(ba[0], ba[1], ba[2], ca[0], ca[1], ca[2], g[3][0], g[3][1], g[3][2]);
-    for (int i = 0; i < 3; ++i) g[0][i] = -g[1][i] - g[2][i] - g[3][i];
-    double J = ba[0] * g[1][0] + ba[1] * g[1][1] + ba[2] * g[1][2];
-    for (int k = 0; k < 6; ++k) {
-      int p = lpoed[k][0], q = lpoed[k][1];
-      uint64_t a = N[p], b = N[q];
-      double sig = 1.0;
-      if (G(a) > G(b)) {
-        std::swap(a, b);
-        sig = -1.0;
-      }
-      auto beg = rcol.begin() + rptr[a], en = rcol.begin() + rptr[a + 1];
-      auto it = std::lower_bound(beg, en, b, [&](uint64_t u, uint64_t v) { return G(u) < G(v); });
-      double* n = &D[static_cast<size_t>(it - rcol.begin()) * ncoef];
-      n[0] += sig * (g[p][0] - g[q][0]) / 48.0;
-      n[1] += sig * (g[p][1] - g[q][1]) / 48.0;
-      n[2] += sig * (g[p][2] - g[q][2]) / 48.0;
-      if (ncoef == 5) {
-        n[3] += J / 120.0;
-        n[4] += (g[p][0] * g[q][0] + g[p][1] * g[q][1] + g[p][2] * g[q][2]) / J / 6.0;
+  parallel_rows(npoin, [&](int64_t r) {
+    for (int64_t k = eptr[r]; k < eptr[r + 1]; ++k) {
+      const uint64_t* N = inpoel + elist[k] * 4;
+      double ba[3] = {x[N[1]] - x[N[0]], y[N[1]] - y[N[0]], z[N[1]] - z[N[0]]};
+      double ca[3] = {x[N[2]] - x[N[0]], y[N[2]] - y[N[0]], z[N[2]] - z[N[0]]};
+      double da[3] = {x[N[3]] - x[N[0]], y[N[3]] - y[N[0]], z[N[3]] - z[N[0]]};
+      double g[4][3];
+      cross(ca[0], ca[1], ca[2], da[0], da[1], da[2], g[1][0], g[1][1], g[1][2]);
+      cross(da[0], da[1], da[2], ba[0], ba[1], ba[2], g[2][0], g[2][1], g[2][2]);
+      cross(ba[0], ba[1], ba[2], ca[0], ca[1], ca[2], g[3][0], g[3][1], g[3][2]);
+      for (int i = 0; i < 3; ++i) g[0][i] = -g[1][i] - g[2][i] - g[3][i];
+      double J = ba[0] * g[1][0] + ba[1] * g[1][1] + ba[2] * g[1][2];
+      for (int kk = 0; kk < 6; ++kk) {
+        int p = lpoed[kk][0], q = lpoed[kk][1];
+        uint64_t a = N[p], b = N[q];
+        double sig = 1.0;
+        if (G(a) > G(b)) {
+          std::swap(a, b);
+          sig = -1.0;
+        }
+        if (a != static_cast<uint64_t>(r)) continue;
+        auto beg = rcol.begin() + rptr[a], en = rcol.begin() + rptr[a + 1];
+        auto it =
+            std::lower_bound(beg, en, b, [&](uint64_t u, uint64_t v) { return G(u) < G(v); });
+        double* n = &D[static_cast<size_t>(it - rcol.begin()) * ncoef];
+        n[0] += sig * (g[p][0] - g[q][0]) / 48.0;
+        n[1] += sig * (g[p][1] - g[q][1]) / 48.0;
+        n[2] += sig * (g[p][2] - g[q][2]) / 48.0;
+        if (ncoef == 5) {
+          n[3] += J / 120.0;
+          n[4] += (g[p][0] * g[q][0] + g[p][1] * g[q][1] + g[p][2] * g[q][2]) / J / 6.0;
+        }
       }
     }
-  }
+  });
   // emit in (gid, gid) order
   std::vector<int64_t> rows(npoin);
   std::iota(rows.begin(), rows.end(), 0);
   if (gid) std::sort(rows.begin(), rows.end(), [&](int64_t a, int64_t b) { return gid[a] < gid[b]; });
-  int64_t k = 0;
-  for (int64_t a : rows)
-    for (int64_t j = rptr[a]; j < rptr[a + 1]; ++j) {
-      edges[k * 2 + 0] = static_cast<uint64_t>(a);
-      edges[k * 2 + 1] = rcol[j];
-      std::memcpy(dint + k * ncoef, &D[static_cast<size_t>(j) * ncoef], sizeof(double) * ncoef);
-      ++k;
+  std::vector<int64_t> opos(npoin + 1, 0);
+  for (int64_t k = 0; k < npoin; ++k) opos[k + 1] = opos[k] + (rptr[rows[k] + 1] - rptr[rows[k]]);
+  parallel_rows(npoin, [&](int64_t k) {
+    const int64_t a = rows[k];
+    int64_t o = opos[k];
+    for (int64_t j = rptr[a]; j < rptr[a + 1]; ++j, ++o) {
+      edges[o * 2 + 0] = static_cast<uint64_t>(a);
+      edges[o * 2 + 1] = rcol[j];
+      std::memcpy(dint + o * ncoef, &D[static_cast<size_t>(j) * ncoef], sizeof(double) * ncoef);
     }
+  });
   return XG_OK;
 }
 
