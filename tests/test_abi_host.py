@@ -69,6 +69,18 @@ def test_threaded_edge_integrals_match_oracle(ncoef):
     assert np.array_equal(e, eo) and np.array_equal(d, do)
 
 
+def test_threaded_pressure_matrix_matches_oracle():
+    """The row-parallel ChoCG::prelhs matrix (15,625 rows): the oracle's
+    serial element-order sums, bit for bit."""
+    from xyst_gb300 import cg
+    m = mesh.cube(25, jitter=0.2, seed=4, numbering="random", perm_seed=6)
+    ia, ja, a = cg.pressure_matrix(m["coord"], m["inpoel"])
+    io, jo, ao = oracle.pressure_matrix(m["coord"], m["inpoel"])
+    assert np.array_equal(np.asarray(ia, np.int64), np.asarray(io, np.int64))
+    assert np.array_equal(np.asarray(ja, np.int64), np.asarray(jo, np.int64))
+    assert np.array_equal(a, ao)
+
+
 def test_rcm_is_permutation_and_reduces_bandwidth():
     m = mesh.cube(9, numbering="random", perm_seed=1)
     perm = riecg.rcm(m["inpoel"], m["coord"].shape[1])

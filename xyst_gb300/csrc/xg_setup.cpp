@@ -20,31 +20,6 @@
 
 namespace {
 
-// Points surrounding points as CSR (sorted, unique, no self) from tets.
-void psup(int64_t n, int64_t nelem, const uint64_t* inpoel, std::vector<int64_t>& ptr,
-          std::vector<int64_t>& adj) {
-  std::vector<int64_t> cnt(n + 1, 0);
-  for (int64_t e = 0; e < nelem; ++e)
-    for (int a = 0; a < 4; ++a) cnt[inpoel[e * 4 + a] + 1] += 3;
-  for (int64_t i = 0; i < n; ++i) cnt[i + 1] += cnt[i];
-  std::vector<int64_t> tmp(cnt[n]);
-  std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
-  for (int64_t e = 0; e < nelem; ++e)
-    for (int a = 0; a < 4; ++a)
-      for (int b = 0; b < 4; ++b)
-        if (a != b) tmp[fill[inpoel[e * 4 + a]]++] = static_cast<int64_t>(inpoel[e * 4 + b]);
-  ptr.assign(n + 1, 0);
-  adj.clear();
-  adj.reserve(tmp.size() / 3);
-  for (int64_t i = 0; i < n; ++i) {
-    auto b = tmp.begin() + cnt[i], en = tmp.begin() + cnt[i + 1];
-    std::sort(b, en);
-    auto u = std::unique(b, en);
-    adj.insert(adj.end(), b, u);
-    ptr[i + 1] = static_cast<int64_t>(adj.size());
-  }
-}
-
 // fn(i) for i in [0, n) on the host's cores, in contiguous chunks.
 template <class Fn>
 void parallel_rows(int64_t n, Fn fn) {
@@ -65,6 +40,33 @@ void parallel_rows(int64_t n, Fn fn) {
     });
   }
   for (auto& x : th) x.join();
+}
+
+// Points surrounding points as CSR (sorted, unique, no self) from tets.
+void psup(int64_t n, int64_t nelem, const uint64_t* inpoel, std::vector<int64_t>& ptr,
+          std::vector<int64_t>& adj) {
+  std::vector<int64_t> cnt(n + 1, 0);
+  for (int64_t e = 0; e < nelem; ++e)
+    for (int a = 0; a < 4; ++a) cnt[inpoel[e * 4 + a] + 1] += 3;
+  for (int64_t i = 0; i < n; ++i) cnt[i + 1] += cnt[i];
+  std::vector<int64_t> tmp(cnt[n]);
+  std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
+  for (int64_t e = 0; e < nelem; ++e)
+    for (int a = 0; a < 4; ++a)
+      for (int b = 0; b < 4; ++b)
+        if (a != b) tmp[fill[inpoel[e * 4 + a]]++] = static_cast<int64_t>(inpoel[e * 4 + b]);
+  std::vector<int64_t> ucnt(n);
+  parallel_rows(n, [&](int64_t i) {
+    auto b = tmp.begin() + cnt[i], en = tmp.begin() + cnt[i + 1];
+    std::sort(b, en);
+    ucnt[i] = std::unique(b, en) - b;
+  });
+  ptr.assign(n + 1, 0);
+  for (int64_t i = 0; i < n; ++i) ptr[i + 1] = ptr[i] + ucnt[i];
+  adj.assign(ptr[n], 0);
+  parallel_rows(n, [&](int64_t i) {
+    std::copy(tmp.begin() + cnt[i], tmp.begin() + cnt[i] + ucnt[i], adj.begin() + ptr[i]);
+  });
 }
 
 inline void cross(double ax, double ay, double az, double bx, double by, double bz, double& rx,
@@ -326,25 +328,41 @@ int xg_mesh_pressure_matrix(int64_t npoin, const double* coord, int64_t nelem,
   }
   std::fill(a, a + total, 0.0);
   const double *x = coord, *y = coord + npoin, *z = coord + 2 * npoin;
-  for (int64_t e = 0; e < nelem; ++e) {
-    const uint64_t* N = inpoel + e * 4;
-    double ba[3] = {x[N[1]] - x[N[0]], y[N[1]] - y[N[0]], z[N[1]] - z[N[0]]};
-    double ca[3] = {x[N[2]] - x[N[0]], y[N[2]] - y[N[0]], z[N[2]] - z[N[0]]};
-    double da[3] = {x[N[3]] - x[N[0]], y[N[3]] - y[N[0]], z[N[3]] - z[N[0]]};
-    double g[4][3];
-    cross(ca[0], ca[1], ca[2], da[0], da[1], da[2], g[1][0], g[1][1], g[1][2]);
-    cross(da[0], da[1], da[2], ba[0], ba[1], ba[2], g[2][0], g[2][1], g[2][2]);
-    cross(ba[0], ba[1], ba[2], ca[0], ca[1], ca[2], g[3][0], g[3][1], g[3][2]);
-    for (int i = 0; i < 3; ++i) g[0][i] = -g[1][i] - g[2][i] - g[3][i];
-    const double J = (ba[0] * g[1][0] + ba[1] * g[1][1] + ba[2] * g[1][2]) * 6.0;
-    for (int p = 0; p < 4; ++p)
-      for (int q = 0; q < 4; ++q) {
-        const uint64_t* beg = ja + ia[N[p]];
-        const uint64_t* en = ja + ia[N[p] + 1];
-        const uint64_t* pos = std::lower_bound(beg, en, N[q]);
-        a[pos - ja] -= (g[p][0] * g[q][0] + g[p][1] * g[q][1] + g[p][2] * g[q][2]) / J;
-      }
+  // the elements of every node in increasing element id; row r then sums its
+  // entries element by element, the serial element loop's order
+  std::vector<int64_t> eptr(npoin + 1, 0);
+  for (int64_t e = 0; e < nelem; ++e)
+    for (int v = 0; v < 4; ++v) ++eptr[inpoel[e * 4 + v] + 1];
+  for (int64_t i = 0; i < npoin; ++i) eptr[i + 1] += eptr[i];
+  std::vector<int64_t> elist(eptr[npoin]);
+  {
+    std::vector<int64_t> fill(eptr.begin(), eptr.end() - 1);
+    for (int64_t e = 0; e < nelem; ++e)
+      for (int v = 0; v < 4; ++v) elist[fill[inpoel[e * 4 + v]]++] = e;
   }
+  parallel_rows(npoin, [&](int64_t r) {
+    for (int64_t k = eptr[r]; k < eptr[r + 1]; ++k) {
+      const uint64_t* N = inpoel + elist[k] * 4;
+      double ba[3] = {x[N[1]] - x[N[0]], y[N[1]] - y[N[0]], z[N[1]] - z[N[0]]};
+      double ca[3] = {x[N[2]] - x[N[0]], y[N[2]] - y[N[0]], z[N[2]] - z[N[0]]};
+      double da[3] = {x[N[3]] - x[N[0]], y[N[3]] - y[N[0]], z[N[3]] - z[N[0]]};
+      double g[4][3];
+      cross(ca[0], ca[1], ca[2], da[0], da[1], da[2], g[1][0], g[1][1], g[1][2]);
+      cross(da[0], da[1], da[2], ba[0], ba[1], ba[2], g[2][0], g[2][1], g[2][2]);
+      cross(ba[0], ba[1], ba[2], ca[0], ca[1], ca[2], g[3][0], g[3][1], g[3][2]);
+      for (int i = 0; i < 3; ++i) g[0][i] = -g[1][i] - g[2][i] - g[3][i];
+      const double J = (ba[0] * g[1][0] + ba[1] * g[1][1] + ba[2] * g[1][2]) * 6.0;
+      for (int p = 0; p < 4; ++p) {
+        if (N[p] != static_cast<uint64_t>(r)) continue;
+        for (int q = 0; q < 4; ++q) {
+          const uint64_t* beg = ja + ia[N[p]];
+          const uint64_t* en = ja + ia[N[p] + 1];
+          const uint64_t* pos = std::lower_bound(beg, en, N[q]);
+          a[pos - ja] -= (g[p][0] * g[q][0] + g[p][1] * g[q][1] + g[p][2] * g[q][2]) / J;
+        }
+      }
+    }
+  });
   return XG_OK;
 }
 
