@@ -111,3 +111,40 @@ def test_pressure_matrix_matches_oracle():
     ia, ja, a = cg.pressure_matrix(m["coord"], m["inpoel"])
     oia, oja, oa = oracle.pressure_matrix(m["coord"], m["inpoel"])
     assert np.array_equal(ia, oia) and np.array_equal(ja, oja) and np.array_equal(a, oa)
+
+
+def test_header_is_c_and_links_from_c(tmp_path):
+    """include/xg.h is plain C99: a C translation unit that includes it, links
+    against libxg and calls the host entry points (mesh volumes, the error
+    path of xg_create without a GPU) builds and runs."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    so = lib.load()._name
+    src = tmp_path / "c_abi.c"
+    src.write_text(r'''
+#include <stdio.h>
+#include "xg.h"
+int main(void) {
+  /* one right tetrahedron of volume 1/6 */
+  const double coord[12] = {0, 1, 0, 0,  0, 0, 1, 0,  0, 0, 0, 1};
+  const uint64_t inpoel[4] = {0, 1, 2, 3};
+  double vol[4] = {0, 0, 0, 0};
+  if (xg_mesh_vol(4, coord, 1, inpoel, vol) != XG_OK) return 1;
+  for (int i = 0; i < 4; ++i)
+    if (vol[i] < 1.0 / 24 - 1e-15 || vol[i] > 1.0 / 24 + 1e-15) return 2;
+  xg_ctx* ctx = 0;
+  if (xg_create(12345, &ctx) == XG_OK || ctx != 0) return 3;
+  printf("ok\n");
+  return 0;
+}
+''')
+    exe = tmp_path / "c_abi"
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                        str(src), so, "-Wl,-rpath," + os.path.dirname(so), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", (r.returncode, r.stdout, r.stderr)
