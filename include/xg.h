@@ -39,7 +39,8 @@ enum xg_status {
   XG_ERR_STATE = 3,    /* call out of order (e.g. no operators uploaded) */
   XG_ERR_BLOWUP = 4,   /* dt below machine epsilon (RieCG::advance blowup) */
   XG_ERR_NOTCONV = 5,  /* CG stopped without reaching the tolerance */
-  XG_ERR_DEVICE = 6    /* a kernel reported an error status */
+  XG_ERR_DEVICE = 6,   /* a kernel reported an error status */
+  XG_ERR_HOST = 7      /* host-side failure: out of host memory, threads refused */
 };
 
 enum xg_precision {
@@ -145,8 +146,11 @@ int xg_riecg_kernel_times(xg_ctx* ctx, int cap, const char** names, double* ms,
  * the device's memory, or they run where cudaMalloc is not allowed) and that
  * hold RieCG's state on the device themselves.  U (npoin x 5, node-major)
  * and vol (npoin) are device pointers; dt (host) receives cfl * min over
- * nodes of cbrt(vol)/max(|u|+c, 1e-8), as xg_riecg_dt, or const_dt when
- * |const_dt| > eps.  Work is issued on stream (a cudaStream_t, null for the
+ * nodes of cbrt(vol)/max(|u|+c, 1e-8) evaluated in FP64 arithmetic, or
+ * const_dt when |const_dt| > eps.  That is xg_riecg_dt's result for an FP64
+ * context; an XG_FP32_FLUX context's xg_riecg_dt evaluates the same formula
+ * in FP32 arithmetic, which can differ in the low bits (about 1e-7
+ * relative).  Work is issued on stream (a cudaStream_t, null for the
  * default stream) on the calling thread's current device, then synchronised.
  * The scratch is a fixed 512 KiB device array inside the library, shared by
  * all calls on a device: npoin is limited to 16,777,216 nodes (XG_ERR_ARG

@@ -40,11 +40,24 @@ def build(force: bool = False) -> str:
     return LIB
 
 
-def build_ref(reference_root: str = "/root/reference") -> str | None:
+def reference_root() -> str | None:
+    """Where the reference's sources are: $XYST_REFERENCE if set, else a
+    checkout named ``reference`` beside this repository; None when neither
+    holds the reference's src/Physics."""
+    cands = [os.environ.get("XYST_REFERENCE"),
+             os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")]
+    for c in cands:
+        if c and os.path.isdir(os.path.join(c, "src", "Physics")):
+            return c
+    return None
+
+
+def build_ref(root: str | None = None) -> str | None:
     """Build oracle/_ref from the reference sources when they are present."""
-    if not os.path.isdir(os.path.join(reference_root, "src", "Physics")):
+    src = root or reference_root()
+    if src is None or not os.path.isdir(os.path.join(src, "src", "Physics")):
         return None
-    subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"), reference_root])
+    subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"), src])
     return REF_LIB
 
 

@@ -3,10 +3,11 @@
 # physics sources where they lie, plus the stub headers in oracle/ref_stubs and
 # the shim oracle/ref_driver.cpp.  Test infrastructure only: the result pins the
 # C++ restatement in oracle/xg_oracle.cpp.  Outputs go to oracle/_ref/ only.
-#   usage: oracle/build_ref.sh [reference-root]   (default /root/reference)
+#   usage: oracle/build_ref.sh [reference-root]
+#   (default: $XYST_REFERENCE, else a checkout named "reference" beside this repository)
 set -e
-REF=${1:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
+REF=${1:-${XYST_REFERENCE:-$HERE/../../reference}}
 OUT="$HERE/_ref"
 if [ ! -d "$REF/src/Physics" ]; then
   echo "reference sources not found at $REF; skipping" >&2

@@ -1,7 +1,8 @@
 """Extract the reference's own golden vectors for the accelerated path into
 small committed fixtures (tests/golden/*.npz).
 
-Run in a checkout that has the reference sources (default /root/reference):
+Run where the reference sources are readable (the root given as the argument,
+else $XYST_REFERENCE, else a checkout named "reference" beside this repository):
 
     python tests/golden/make_golden.py [reference-root]
 
@@ -152,4 +153,6 @@ def main(ref: str):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    default = os.environ.get("XYST_REFERENCE") or os.path.join(
+        os.path.dirname(os.path.dirname(os.path.dirname(HERE))), "reference")
+    main(sys.argv[1] if len(sys.argv) > 1 else default)

@@ -1128,6 +1128,7 @@ extern "C" {
 
 int xg_cg_setup(xg_ctx* c, int64_t nrow, const uint64_t* ia, const uint64_t* ja, const double* a,
                 int base) {
+  XG_HOST_TRY
   int rc = use(c);
   if (rc) return rc;
   if (nrow <= 0 || !ia || !ja || !a || (base != 0 && base != 1))
@@ -1367,6 +1368,7 @@ int xg_cg_setup(xg_ctx* c, int64_t nrow, const uint64_t* ia, const uint64_t* ja,
   XG_CHECK_LAUNCH(c);
   XG_CUDA(c, cudaStreamSynchronize(s));
   return XG_OK;
+  XG_HOST_CATCH(c)
 }
 
 int xg_cg_mult(xg_ctx* c, const double* x, double* y) {
@@ -1386,6 +1388,7 @@ int xg_cg_mult(xg_ctx* c, const double* x, double* y) {
 
 int xg_cg_init(xg_ctx* c, const double* x, const double* b, const double* neubc, int64_t ndir,
                const uint64_t* dirnodes, const double* dirvals, int apply, int pc) {
+  XG_HOST_TRY
   int rc = use(c);
   if (rc) return rc;
   CGDev* d = c->cg;
@@ -1453,6 +1456,7 @@ int xg_cg_init(xg_ctx* c, const double* x, const double* b, const double* neubc,
   XG_CUDA(c, cudaStreamSynchronize(s));
   d->ready = true;
   return XG_OK;
+  XG_HOST_CATCH(c)
 }
 
 int xg_cg_solve(xg_ctx* c, int64_t maxit, double tol, int64_t* it, double* normr,

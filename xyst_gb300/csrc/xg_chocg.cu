@@ -764,6 +764,7 @@ int xg_chocg_setup(xg_ctx* c, const xg_chocg_params* prm, int64_t npoin, const d
                    const double* dsupint0, int64_t ntri, const uint64_t* dsupedge1,
                    const double* dsupint1, int64_t nedge, const uint64_t* dsupedge2,
                    const double* dsupint2, int64_t nbtri, const uint64_t* triinpoel) {
+  XG_HOST_TRY
   int rc = use(c);
   if (rc) return rc;
   if (!prm || npoin <= 0 || !coord || !vol) return fail(c, XG_ERR_ARG, "chocg_setup: bad mesh");
@@ -950,12 +951,14 @@ int xg_chocg_setup(xg_ctx* c, const xg_chocg_params* prm, int64_t npoin, const d
   for (double* z : {d->u, d->u2, d->un, d->pr, d->pgrad, d->vgrad, d->div, d->flx})
     XG_CUDA(c, cudaMemset(z, 0, (z == d->vgrad ? 9 : (z == d->pr || z == d->div ? 1 : 3)) * n * 8));
   return XG_OK;
+  XG_HOST_CATCH(c)
 }
 
 int xg_chocg_set_bc(xg_ctx* c, int64_t ndir, const uint64_t* dirnodes, const int32_t* dirmask,
                     const double* dirvals, int64_t nsym, const uint64_t* symnodes,
                     const double* symnorms, int64_t nnoslip, const uint64_t* noslipnodes,
                     int64_t npdir, const uint64_t* pdirnodes, const double* pdirvals) {
+  XG_HOST_TRY
   ChoCGDev* d = nullptr;
   int rc = get_ctx(c, &d, false);
   if (rc) return rc;
@@ -1032,6 +1035,7 @@ int xg_chocg_set_bc(xg_ctx* c, int64_t ndir, const uint64_t* dirnodes, const int
   if (rc) return rc;
   d->pdir_set = true;
   return XG_OK;
+  XG_HOST_CATCH(c)
 }
 
 int xg_chocg_set_state(xg_ctx* c, const double* u, const double* p, double t) {

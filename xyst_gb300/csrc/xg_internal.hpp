@@ -6,6 +6,8 @@
 
 #include <cstdint>
 #include <cstdio>
+#include <exception>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -130,6 +132,22 @@ inline int fail(xg_ctx* c, int code, const std::string& msg) {
   } while (0)
 
 #define XG_CHECK_LAUNCH(ctx) XG_CUDA(ctx, cudaGetLastError())
+
+// Host-side set-up bodies run inside XG_HOST_TRY ... XG_HOST_CATCH(ctx): an
+// exception (std::bad_alloc on a large mesh, std::system_error when threads
+// are refused) becomes XG_ERR_HOST instead of crossing the C ABI.
+#define XG_HOST_TRY try {
+#define XG_HOST_CATCH(ctx)                                                         \
+  }                                                                                \
+  catch (const std::bad_alloc&) {                                                  \
+    return ::xg::fail((ctx), XG_ERR_HOST, "out of host memory");                   \
+  }                                                                                \
+  catch (const std::exception& ex_) {                                              \
+    return ::xg::fail((ctx), XG_ERR_HOST, std::string("host: ") + ex_.what());     \
+  }                                                                                \
+  catch (...) {                                                                    \
+    return ::xg::fail((ctx), XG_ERR_HOST, "host-side exception");                  \
+  }
 
 // Grid size for n items at b threads per block, as a multiple of what one
 // wave needs is left to the hardware scheduler: every node kernel is a flat

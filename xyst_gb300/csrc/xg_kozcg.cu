@@ -813,6 +813,7 @@ extern "C" {
 
 int xg_kozcg_setup(xg_ctx* c, const xg_kozcg_params* prm, int64_t npoin, const double* coord,
                    const double* vol, int64_t nelem, const uint64_t* inpoel) {
+  XG_HOST_TRY
   int rc = use(c);
   if (rc) return rc;
   if (!prm || npoin <= 0 || nelem <= 0 || !coord || !vol || !inpoel)
@@ -941,11 +942,13 @@ int xg_kozcg_setup(xg_ctx* c, const xg_kozcg_params* prm, int64_t npoin, const d
   XG_CUDA(c, cudaMemcpyAsync(d->scal, &k0, sizeof(k0), cudaMemcpyHostToDevice, s));
   XG_CUDA(c, cudaStreamSynchronize(s));
   return XG_OK;
+  XG_HOST_CATCH(c)
 }
 
 int xg_kozcg_set_bc(xg_ctx* c, int64_t nsym, const uint64_t* symnodes, const double* symnorms,
                     int64_t ndir, const uint64_t* dirnodes, const int32_t* dirmask,
                     const double* dirvals) {
+  XG_HOST_TRY
   int rc = use(c);
   if (rc) return rc;
   KozCGDev* d = c->kozcg;
@@ -1009,6 +1012,7 @@ int xg_kozcg_set_bc(xg_ctx* c, int64_t nsym, const uint64_t* symnodes, const dou
   d->nbc = nbc;
   d->dt_valid = false;
   return XG_OK;
+  XG_HOST_CATCH(c)
 }
 
 int xg_kozcg_set_state(xg_ctx* c, const double* U, double t) {

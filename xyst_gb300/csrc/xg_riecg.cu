@@ -1564,6 +1564,7 @@ int xg_riecg_setup(xg_ctx* c, const xg_riecg_params* prm, int64_t npoin, const d
                    const double* dsupint1, int64_t nedge, const uint64_t* dsupedge2,
                    const double* dsupint2, int64_t nbtri, const uint64_t* triinpoel,
                    const uint8_t* besym) {
+  XG_HOST_TRY
   int rc = use(c);
   if (rc) return rc;
   if (!prm || npoin <= 0 || !coord || !vol) return fail(c, XG_ERR_ARG, "riecg_setup: bad mesh");
@@ -1793,6 +1794,7 @@ int xg_riecg_setup(xg_ctx* c, const xg_riecg_params* prm, int64_t npoin, const d
   }
   // bidx is also needed on the host to set BC flags later
   return XG_OK;
+  XG_HOST_CATCH(c)
 }
 
 int xg_riecg_set_bc(xg_ctx* c, int64_t nsym, const uint64_t* symnodes, const double* symnorms,
@@ -1800,6 +1802,7 @@ int xg_riecg_set_bc(xg_ctx* c, int64_t nsym, const uint64_t* symnodes, const dou
                     const double* far5, int64_t ndir, const uint64_t* dirnodes,
                     const int32_t* dirmask, const double* dirvals, int64_t npre,
                     const uint64_t* prenodes, const double* prevals) {
+  XG_HOST_TRY
   int rc = use(c);
   if (rc) return rc;
   RieCGDev* d = c->riecg;
@@ -1893,6 +1896,7 @@ int xg_riecg_set_bc(xg_ctx* c, int64_t nsym, const uint64_t* symnodes, const dou
     d->graph = nullptr;
   }
   return XG_OK;
+  XG_HOST_CATCH(c)
 }
 
 int xg_riecg_set_state(xg_ctx* c, const double* U, double t) {

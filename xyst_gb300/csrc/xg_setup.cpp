@@ -13,10 +13,21 @@
 #include <numeric>
 #include <queue>
 #include <string>
+#include <system_error>
 #include <thread>
 #include <vector>
 
 #include "../../include/xg.h"
+
+// Every entry point's body runs inside XG_HOST_TRY ... XG_HOST_CATCH, so an
+// exception (std::bad_alloc on a large mesh, std::system_error) becomes
+// XG_ERR_HOST instead of crossing the C ABI.
+#define XG_HOST_TRY try {
+#define XG_HOST_CATCH \
+  }                   \
+  catch (...) {       \
+    return XG_ERR_HOST; \
+  }
 
 namespace {
 
@@ -32,12 +43,23 @@ void parallel_rows(int64_t n, Fn fn) {
   }
   const int64_t chunk = (n + nt - 1) / nt;
   std::vector<std::thread> th;
-  for (int64_t t = 0; t < nt; ++t) {
-    const int64_t b = t * chunk, e = std::min(n, b + chunk);
-    if (b >= e) break;
-    th.emplace_back([b, e, &fn] {
+  th.reserve(static_cast<size_t>(nt));
+  int64_t t = 0;
+  try {
+    for (; t < nt; ++t) {
+      const int64_t b = t * chunk, e = std::min(n, b + chunk);
+      if (b >= e) break;
+      th.emplace_back([b, e, &fn] {
+        for (int64_t i = b; i < e; ++i) fn(i);
+      });
+    }
+  } catch (const std::system_error&) {
+    // thread creation refused (rlimits, containers): the chunks not yet
+    // handed out run on this thread
+    for (; t < nt; ++t) {
+      const int64_t b = t * chunk, e = std::min(n, b + chunk);
       for (int64_t i = b; i < e; ++i) fn(i);
-    });
+    }
   }
   for (auto& x : th) x.join();
 }
@@ -83,6 +105,7 @@ extern "C" {
 // Reverse Cuthill-McKee: BFS from a minimum-degree node of each connected
 // component, visiting neighbours in increasing degree, then reversed.
 int xg_mesh_rcm(int64_t npoin, int64_t nelem, const uint64_t* inpoel, uint64_t* new_of_old) {
+  XG_HOST_TRY
   if (npoin <= 0 || nelem < 0 || !inpoel || !new_of_old) return XG_ERR_ARG;
   for (int64_t i = 0; i < nelem * 4; ++i)
     if (inpoel[i] >= static_cast<uint64_t>(npoin)) return XG_ERR_ARG;
@@ -119,10 +142,12 @@ int xg_mesh_rcm(int64_t npoin, int64_t nelem, const uint64_t* inpoel, uint64_t* 
   for (int64_t k = 0; k < npoin; ++k)
     new_of_old[order[k]] = static_cast<uint64_t>(npoin - 1 - k);
   return XG_OK;
+  XG_HOST_CATCH
 }
 
 int xg_mesh_vol(int64_t npoin, const double* coord, int64_t nelem, const uint64_t* inpoel,
                 double* vol) {
+  XG_HOST_TRY
   if (npoin <= 0 || !coord || !inpoel || !vol) return XG_ERR_ARG;
   const double *x = coord, *y = coord + npoin, *z = coord + 2 * npoin;
   std::fill(vol, vol + npoin, 0.0);
@@ -140,11 +165,13 @@ int xg_mesh_vol(int64_t npoin, const double* coord, int64_t nelem, const uint64_
     for (int a = 0; a < 4; ++a) vol[N[a]] += J;
   }
   return XG_OK;
+  XG_HOST_CATCH
 }
 
 int xg_mesh_edges(int64_t npoin, const double* coord, int64_t nelem, const uint64_t* inpoel,
                   const uint64_t* gid, int ncoef, int64_t cap, int64_t* nedge, uint64_t* edges,
                   double* dint) {
+  XG_HOST_TRY
   if (npoin <= 0 || !coord || !inpoel || !nedge || (ncoef != 3 && ncoef != 5)) return XG_ERR_ARG;
   const double *x = coord, *y = coord + npoin, *z = coord + 2 * npoin;
   auto G = [&](uint64_t p) { return gid ? gid[p] : p; };
@@ -253,10 +280,12 @@ int xg_mesh_edges(int64_t npoin, const double* coord, int64_t nelem, const uint6
     }
   });
   return XG_OK;
+  XG_HOST_CATCH
 }
 
 int xg_mesh_bnorm(int64_t npoin, const double* coord, int64_t nface, const uint64_t* faces,
                   int64_t nnode, const uint64_t* nodes, double* norms) {
+  XG_HOST_TRY
   if (npoin <= 0 || !coord || (nface && !faces) || (nnode && (!nodes || !norms)))
     return XG_ERR_ARG;
   const double *x = coord, *y = coord + npoin, *z = coord + 2 * npoin;
@@ -294,6 +323,7 @@ int xg_mesh_bnorm(int64_t npoin, const double* coord, int64_t nface, const uint6
     for (int j = 0; j < 3; ++j) norms[i * 3 + j] = acc[p * 4 + j] / acc[p * 4 + 3];
   }
   return XG_OK;
+  XG_HOST_CATCH
 }
 
 // Pressure-Poisson matrix of ChoCG::prelhs (src/Inciter/ChoCG.cpp:146-188):
@@ -303,6 +333,7 @@ int xg_mesh_bnorm(int64_t npoin, const double* coord, int64_t nface, const uint6
 int xg_mesh_pressure_matrix(int64_t npoin, const double* coord, int64_t nelem,
                             const uint64_t* inpoel, int64_t cap, int64_t* nnz, uint64_t* ia,
                             uint64_t* ja, double* a) {
+  XG_HOST_TRY
   if (npoin <= 0 || !coord || !inpoel || !nnz) return XG_ERR_ARG;
   for (int64_t i = 0; i < nelem * 4; ++i)
     if (inpoel[i] >= static_cast<uint64_t>(npoin)) return XG_ERR_ARG;
@@ -364,6 +395,7 @@ int xg_mesh_pressure_matrix(int64_t npoin, const double* coord, int64_t nelem,
     }
   });
   return XG_OK;
+  XG_HOST_CATCH
 }
 
 }  // extern "C"
