@@ -15,15 +15,16 @@ all six faces, CFL 0.5.  Synthetic data: the mesh and state are generated.
          taken inside the timed region, against the measured HBM copy
          bandwidth
   cpu_baseline  the oracle (serial C++ restatement of the reference loops) on
-         host cores, on a bounded sample (a 49^3 cube, 30 steps; the per-node
-         work does not depend on the mesh size)
+         one host core, on a bounded sample of the same workload (eight cell
+         layers from the middle of the cube, ten steps)
   chocg  the metric's second half: ChoCG s/step on the same cube (Taylor-Green
          vortex, Re 100), every pressure solve to 1e-8 relative residual, FP64
          Jacobi PCG against the learned factor with mixed precision
 
 --impl reference runs the reference's CPU arithmetic (the oracle port; the
-reference itself needs Charm++ and cannot be built on the GPU machine) on all host
-cores, one independent mesh partition per core, and prints the same metric.
+reference itself needs Charm++ and cannot be built on the GPU machine) on the same
+n^3 workload: the cube cut into one z-slab per host core, one single-threaded
+process per slab, --warmup real warm-up steps and --steps timed steps.
 """
 
 from __future__ import annotations
@@ -214,41 +215,92 @@ def run_chocg(n=129, steps=5, warm=2, tol=1e-8, train_steps=300, seed=0):
 
 # ------------------------------------------------------------------ CPU leg
 
-def cpu_sample(n=41, steps=3, procs=1):
-    """Oracle node-updates/s on `procs` independent n^3 cubes, one per process."""
-    code = r"""
-import sys, time, json
-sys.path.insert(0, %r)
-import numpy as np, oracle
-from xyst_gb300 import mesh
-from bench import wave_state
-n, steps = %d, %d
-m = mesh.cube(n, jitter=0.2, seed=0)
-c, ip = m["coord"], m["inpoel"]
-v = oracle.vol(c, ip); e, d = oracle.domint(c, ip)
-tri = np.concatenate([m["bface"][s] for s in sorted(m["bface"])])
-nodes, norms, symset = oracle.sym_bc(c, m["bface"], [1,2,3,4,5,6])
-besym = np.isin(tri, list(symset)).astype(np.uint8)
-o = oracle.RieCG(c, v, e, d, tri, besym)
-o.set_sym(nodes, norms); o.set_state(wave_state(c)); o.bc()
-t0 = time.perf_counter(); o.run(steps); t1 = time.perf_counter()
-print(json.dumps({"n": c.shape[1], "steps": steps, "s": t1 - t0}))
-""" % (ROOT, n, steps)
+def _ref_partition(n, k0, k1, warmup, steps, barrier, queue):
+    """One reference-arm process: the oracle RieCG (FP64, the reference's
+    arithmetic, one thread) on the z-slab k0 <= k < k1 of the n^3 jittered
+    cube, as one partition of a domain-decomposed run without its halo
+    exchange: warmup untimed steps, then steps timed between two barriers
+    shared by all partitions."""
+    os.environ["OMP_NUM_THREADS"] = "1"
+    import oracle
+    from xyst_gb300 import mesh
+
+    m = mesh.cube_slab(n, k0, k1, jitter=0.2, seed=0)
+    c, ip = m["coord"], m["inpoel"]
+    v = oracle.vol(c, ip)
+    e, d = oracle.domint(c, ip)
+    tri = np.concatenate([m["bface"][s_] for s_ in sorted(m["bface"])])
+    nodes, norms, symset = oracle.sym_bc(c, m["bface"], [1, 2, 3, 4, 5, 6])
+    besym = np.isin(tri, list(symset)).astype(np.uint8)
+    o = oracle.RieCG(c, v, e, d, tri, besym)
+    o.set_sym(nodes, norms)
+    o.set_state(wave_state(c))
+    o.bc()
+    if warmup:
+        o.run(warmup)
+    barrier.wait()
+    t0 = time.perf_counter()
+    if steps:
+        o.run(steps)
+    t1 = time.perf_counter()
+    barrier.wait()
+    queue.put({"k0": k0, "k1": k1, "owned": int(m["owned"]), "nodes": int(c.shape[1]),
+               "s": t1 - t0})
+
+
+def reference_arm(n, steps, warmup, procs=None, one_slab=None):
+    """The reference's CPU arithmetic on the n^3 workload itself: the cube cut
+    into P z-slabs (P = host cores, at most n-1), one single-threaded oracle
+    process per slab, all timed over the same `steps` steps after `warmup`
+    real warm-up steps.  node-updates/s = n^3 * steps / the slowest slab's
+    time (an upper bound of the reference's parallel model: each slab does a
+    Charm++ chare's work without the halo exchange).
+
+    one_slab=(k0, k1): time only that slab, on one core (a bounded sample of
+    the same workload: node-updates/s per core)."""
+    import multiprocessing as mp
+
     import oracle
     oracle.build()
-    env = dict(os.environ, OMP_NUM_THREADS="1")
-    ps = [subprocess.Popen([sys.executable, "-c", code], stdout=subprocess.PIPE, text=True,
-                           env=env) for _ in range(procs)]
-    res = []
-    for p in ps:
-        out, _ = p.communicate()
-        res.append(json.loads(out.strip().splitlines()[-1]))
-    nodes = res[0]["n"]
+    if one_slab is None:
+        P = max(1, min(procs or os.cpu_count() or 1, n - 1))
+        cuts = np.linspace(0, n - 1, P + 1).round().astype(int)
+        slabs = [(int(cuts[j]), int(cuts[j + 1])) for j in range(P)]
+    else:
+        P, slabs = 1, [tuple(one_slab)]
+    ctx = mp.get_context("spawn")
+    barrier = ctx.Barrier(P)
+    queue = ctx.Queue()
+    ps = [ctx.Process(target=_ref_partition, args=(n, k0, k1, warmup, steps, barrier, queue))
+          for k0, k1 in slabs]
+    t0 = time.perf_counter()
+    for pr in ps:
+        pr.start()
+    res = [queue.get() for _ in range(P)]
+    for pr in ps:
+        pr.join()
+    wall = time.perf_counter() - t0
+    owned = sum(r["owned"] for r in res)
     worst = max(r["s"] for r in res)
-    value = procs * nodes * steps / worst
-    return {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
-            "sample": f"{procs}x independent {n}^3 cube ({nodes} nodes), {steps} steps each, "
-                      f"oracle C++ restatement, 1 thread per process, {worst:.2f} s"}
+    value = owned * steps / worst if steps and worst > 0 else 0.0
+    if one_slab is not None:
+        r = res[0]
+        return {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
+                "ms_per_step": worst / max(steps, 1) * 1e3,
+                "sample": f"z-slab layers {r['k0']}-{r['k1']} of the {n}^3 workload "
+                          f"({r['nodes']} nodes, {owned} owned), {warmup} warm-up + {steps} "
+                          f"timed steps, oracle C++ restatement (FP64), 1 thread, {worst:.2f} s",
+                "wall_s": wall}
+    assert owned == n ** 3
+    return {"value": value, "unit": UNIT, "cores": P, "kind": "port",
+            "ms_per_step": worst / max(steps, 1) * 1e3,
+            "sample": f"the whole {n}^3 workload ({owned} nodes) in {P} z-slab partitions "
+                      f"({min(r['nodes'] for r in res)}-{max(r['nodes'] for r in res)} nodes "
+                      f"each, shared planes duplicated), one single-threaded oracle (C++ "
+                      f"restatement, FP64) process per partition and core, {warmup} warm-up + "
+                      f"{steps} timed steps between barriers, no halo exchange (upper bound); "
+                      f"slowest partition {worst:.2f} s",
+            "wall_s": wall}
 
 
 def _oracle_proc(code):
@@ -392,13 +444,70 @@ def run_gpu(args, rank, world):
     # e2e through the C ABI with host buffers
     e2e = e2e_run(r, U0, args.steps, world)
     dev_bytes = ctx.device_bytes()
+    # the same workload in FP64 (the reference's arithmetic on the GPU), and
+    # every field of the benchmark's mode against it after the workload's
+    # 200 steps
+    fp64 = accuracy = None
+    if rank == 0 and not args.no_fp64:
+        fp64, accuracy = fp64_leg(ctx, ops, r, U0, prec, args)
     ctx.close()
     cho = run_chocg(n=args.n) if (rank == 0 and not args.no_pcg) else None
     koz = run_kozcg(n=args.n) if (rank == 0 and not args.no_pcg) else None
-    out = {"chocg": cho, "kozcg": koz, "n": n, "nedge": nedge, "ms": ms_plain, "ms_events": ms, "kt": kt,
+    out = {"chocg": cho, "kozcg": koz, "fp64": fp64, "accuracy": accuracy,
+           "n": n, "nedge": nedge, "ms": ms_plain, "ms_events": ms, "kt": kt,
            "clocks": ck.summary(), "e2e_ms": e2e, "setup_s": t_setup, "dts": dts2,
            "dev_bytes": dev_bytes}
     return out
+
+
+FIELDS = ("density", "x-momentum", "y-momentum", "z-momentum", "total energy")
+
+
+def fp64_leg(ctx, ops, r, U0, prec, args, acc_steps=200):
+    """RieCG in FP64 mode on the same workload (device-resident, per-kernel
+    events) and, for the FP32-flux mode, the error of every conserved field
+    after acc_steps steps against the FP64 run from the same initial state:
+    max |U32 - U64| / max |U64| per field, and the dt history's largest
+    relative difference."""
+    from xyst_gb300 import riecg
+
+    r64 = riecg.from_operators(ctx, ops, precision="fp64")
+    r64.set_state(U0)
+    r64.bc()
+    r64.run(2)
+    k64 = max(3, min(args.steps, 20))
+    r64.set_state(U0)
+    r64.bc()
+    r64.profile(True)
+    _, ms_ev = r64.run(k64)
+    r64.profile(False)
+    kt = r64.kernel_times()
+    r64.set_state(U0)
+    r64.bc()
+    _, ms = r64.run(k64)
+    n = U0.shape[0]
+    out = {"workload": "the same cube, state and steps in FP64 mode (gradients, fluxes and "
+                       "update in FP64, the reference's operation order)",
+           "steps": k64, "ms_per_step": ms / k64, "value": n * k64 / (ms / 1e3), "unit": UNIT,
+           "kernels": {k: {"ms_total": v[0], "launches": v[1]} for k, v in kt.items()}}
+    acc = None
+    if prec == "fp32":
+        r64.set_state(U0)
+        r64.bc()
+        d64, _ = r64.run(acc_steps)
+        U64 = r64.state()[0]
+        r.set_state(U0)
+        r.bc()
+        d32, _ = r.run(acc_steps)
+        U32 = r.state()[0]
+        acc = {"steps": acc_steps, "reference": "FP64 mode on the GPU (equal to the oracle to "
+                                                "1e-12 on the same mesh)",
+               "max_rel_dev_vs_fp64": {f: float(np.abs(U32[:, k] - U64[:, k]).max() /
+                                               np.abs(U64[:, k]).max())
+                                       for k, f in enumerate(FIELDS)},
+               "dt_max_rel_dev": float(np.abs(d32 / d64 - 1).max())}
+    del r64
+    return out, acc
 
 
 def e2e_run(r, U0, steps, world):
@@ -512,6 +621,7 @@ def main():
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-pcg", action="store_true", help="skip the ChoCG leg")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-mode RieCG leg")
     ap.add_argument("--profile-step", default=None,
                     choices=["chocg-fp64", "chocg-mixed", "kozcg-fp64", "kozcg-fp32"],
                     help="run one warm step of that workload (side --n) inside a profiler "
@@ -536,24 +646,28 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        procs = os.cpu_count() or 1
-        t0 = time.perf_counter()
-        for _ in range(args.warmup):
-            pass
-        cb = cpu_sample(n=49, steps=10, procs=procs)
+        cb = reference_arm(args.n, args.steps, args.warmup)
+        ms_step = cb.pop("ms_per_step")
+        wall = cb.pop("wall_s")
+        rconfig = dict(config, precision="FP64 (the reference's arithmetic)")
         line = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup,
-                "ms_per_step": args.n ** 3 / cb["value"] * 1e3, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": config, "impl": "reference", "cpu_baseline": cb,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64", "data": "synthetic", "config": rconfig, "impl": "reference",
+                "cpu_baseline": cb,
                 "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0},
-                "wall_s": time.perf_counter() - t0}
+                "wall_s": wall}
         print(json.dumps(line))
         return
     cpu = cpu_koz = cpu_cho = None
     if rank == 0 and not args.no_cpu:
-        cpu = cpu_sample(n=49, steps=30, procs=1)  # before any GPU work in this process
+        # before any GPU work in this process: one slab of eight cell layers
+        # from the middle of the same cube, ten steps on one core
+        mid = (args.n - 1) // 2
+        cpu = reference_arm(args.n, 10, 1, one_slab=(max(0, mid - 4), min(args.n - 1, mid + 4)))
+        cpu.pop("ms_per_step")
+        cpu.pop("wall_s")
         if not args.no_pcg:
             cpu_koz = cpu_kozcg()
             cpu_cho = cpu_chocg()
@@ -595,6 +709,7 @@ def main():
             "cpu_baseline": cpu,
             "setup_s": res["setup_s"], "device_bytes": res["dev_bytes"],
             "dt_first_last": [float(res["dts"][0]), float(res["dts"][-1])],
+            "riecg_fp64": res["fp64"], "accuracy": res["accuracy"],
             "chocg": res["chocg"], "kozcg": res["kozcg"]}
     if line["chocg"] is not None:
         line["chocg"]["cpu_baseline"] = cpu_cho

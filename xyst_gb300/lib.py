@@ -22,7 +22,7 @@ _int = C.c_int
 
 XG_OK = 0
 STATUS = {0: "XG_OK", 1: "XG_ERR_ARG", 2: "XG_ERR_CUDA", 3: "XG_ERR_STATE", 4: "XG_ERR_BLOWUP",
-          5: "XG_ERR_NOTCONV", 6: "XG_ERR_DEVICE"}
+          5: "XG_ERR_NOTCONV", 6: "XG_ERR_DEVICE", 7: "XG_ERR_HOST"}
 
 
 class XgError(RuntimeError):

@@ -29,10 +29,12 @@ import numpy as np
 _EXO_TET_SIDE = np.array([[0, 1, 3], [1, 2, 3], [0, 3, 2], [0, 2, 1]], dtype=np.int64)
 
 
-def _kuhn_cells(m: int) -> np.ndarray:
-    """Six tets per cell, ids in the lexicographic (i fastest) numbering."""
+def _kuhn_cells(m: int, k0: int = 0, k1: int | None = None) -> np.ndarray:
+    """Six tets per cell, ids in the lexicographic (i fastest) numbering;
+    only the cell layers k0 <= k < k1 (all by default)."""
     n = m + 1
-    i, j, k = np.meshgrid(np.arange(m), np.arange(m), np.arange(m), indexing="ij")
+    k1 = m if k1 is None else k1
+    i, j, k = np.meshgrid(np.arange(m), np.arange(m), np.arange(k0, k1), indexing="ij")
     base = (i + n * j + n * n * k).transpose(2, 1, 0).reshape(-1)  # i fastest
     step = {0: 1, 1: n, 2: n * n}
     tets = []
@@ -101,17 +103,9 @@ def _cube_faces(n: int) -> dict[int, np.ndarray]:
     return faces
 
 
-def cube(n: int, jitter: float = 0.0, seed: int = 0, numbering: str = "lex",
-         perm_seed: int | None = None) -> dict:
-    """Unit cube [0,1]^3 with n**3 nodes, Kuhn-split into 6 (n-1)**3 tets.
-
-    jitter: interior nodes move by U(-jitter*h, +jitter*h) per coordinate
-    (seeded by ``seed``); boundary nodes stay on the cube faces.
-    numbering: "lex" (i fastest), "random" (seeded permutation, ``perm_seed``)
-    or "rcm" (reverse Cuthill-McKee of the lexicographic graph).
-    """
-    if n < 2:
-        raise ValueError("cube needs at least 2 nodes per side")
+def _cube_coord(n: int, jitter: float, seed: int) -> np.ndarray:
+    """Node coordinates of the n**3 cube (lexicographic ids), interior nodes
+    jittered by U(-jitter*h, +jitter*h) per coordinate (seeded)."""
     m = n - 1
     h = 1.0 / m
     g = np.arange(n, dtype=np.float64) * h
@@ -126,6 +120,48 @@ def cube(n: int, jitter: float = 0.0, seed: int = 0, numbering: str = "lex",
         interior = interior.transpose(2, 1, 0).reshape(-1)
         d = rng.uniform(-jitter * h, jitter * h, size=(3, int(interior.sum())))
         coord[:, interior] += d
+    return coord
+
+
+def cube_slab(n: int, k0: int, k1: int, jitter: float = 0.0, seed: int = 0) -> dict:
+    """The part of ``cube(n, jitter, seed)`` (lexicographic numbering) made of
+    the cell layers k0 <= k < k1 along z: a partition of the cube as a
+    domain-decomposed solver holds it (the node planes k0..k1, the shared
+    planes duplicated in the neighbouring slabs), with the cube's own
+    boundary triangles that lie in it.  Node ids are local (global id minus
+    k0 * n**2); ``owned`` counts the nodes the slab owns when every shared
+    plane belongs to the slab below it (the slabs' counts sum to n**3)."""
+    m = n - 1
+    if not (0 <= k0 < k1 <= m):
+        raise ValueError("slab layers out of range")
+    coord = _cube_coord(n, jitter, seed)
+    lo, hi = k0 * n * n, (k1 + 1) * n * n
+    coord = coord[:, lo:hi].copy()
+    inpoel = _orient_positive(coord, _kuhn_cells(m, k0, k1) - lo)
+    faces = {}
+    for sid, tri in _cube_faces(n).items():
+        keep = np.all((tri >= lo) & (tri < hi), axis=1)
+        if keep.any():
+            faces[sid] = tri[keep] - lo
+    bface = faces_from_tets(inpoel, faces)
+    owned = (k1 - k0) * n * n + (n * n if k1 == m else 0)
+    return {"coord": coord, "inpoel": inpoel, "bface": bface, "h": 1.0 / m, "owned": owned}
+
+
+def cube(n: int, jitter: float = 0.0, seed: int = 0, numbering: str = "lex",
+         perm_seed: int | None = None) -> dict:
+    """Unit cube [0,1]^3 with n**3 nodes, Kuhn-split into 6 (n-1)**3 tets.
+
+    jitter: interior nodes move by U(-jitter*h, +jitter*h) per coordinate
+    (seeded by ``seed``); boundary nodes stay on the cube faces.
+    numbering: "lex" (i fastest), "random" (seeded permutation, ``perm_seed``)
+    or "rcm" (reverse Cuthill-McKee of the lexicographic graph).
+    """
+    if n < 2:
+        raise ValueError("cube needs at least 2 nodes per side")
+    m = n - 1
+    h = 1.0 / m
+    coord = _cube_coord(n, jitter, seed)
     inpoel = _orient_positive(coord, _kuhn_cells(m))
     bface = faces_from_tets(inpoel, _cube_faces(n))
     mesh = {"coord": coord, "inpoel": inpoel, "bface": bface, "h": h}
