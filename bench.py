@@ -469,9 +469,10 @@ def fp64_leg(ctx, ops, r, U0, prec, args, acc_steps=200):
     after acc_steps steps against the FP64 run from the same initial state:
     max |U32 - U64| / max |U64| per field, and the dt history's largest
     relative difference."""
-    from xyst_gb300 import riecg
+    from xyst_gb300 import lib, riecg
 
-    r64 = riecg.from_operators(ctx, ops, precision="fp64")
+    ctx64 = lib.Context(ctx.device)  # a context holds one RieCG state
+    r64 = riecg.from_operators(ctx64, ops, precision="fp64")
     r64.set_state(U0)
     r64.bc()
     r64.run(2)
@@ -507,6 +508,7 @@ def fp64_leg(ctx, ops, r, U0, prec, args, acc_steps=200):
                                        for k, f in enumerate(FIELDS)},
                "dt_max_rel_dev": float(np.abs(d32 / d64 - 1).max())}
     del r64
+    ctx64.close()
     return out, acc
 
 

@@ -8,7 +8,12 @@ on the same mesh and inputs and compares every field:
   symmetry on all faces, RK3 at CFL 0.5, 100 steps (RieCG::solve,
   src/Inciter/RieCG.cpp:992-1057): dt history and fields within 1e-12.
 * RieCG smooth density wave on the 129^3-node jittered cube (2,146,689
-  nodes), FP64, one full 3-stage step: fields within 1e-12.
+  nodes), FP64, one full 3-stage step.  At this size the reference
+  arithmetic itself is order-sensitive at a few nodes: the oracle run with
+  its edges in reverse order differs from the oracle by up to 7.7e-12 in
+  the max norm (9e-15 in the L2 norm) after one step.  The GPU must be as
+  close to the oracle as that (max norm within twice the oracle's own
+  reordering difference, or 1e-12) and within 1e-13 in the L2 norm.
 * KozCG smooth density wave on the same 129^3 cube, FP64 Taylor-Galerkin +
   FCT, one step (KozCG.cpp:613-1197): fields within 1e-12.
 * ChoCG Taylor-Green vortex on the 65^3-node cube (1,572,864 tets), Re 100,
@@ -63,6 +68,11 @@ def _wave_129():
     return riecg.operators(m, sym_sets=[1, 2, 3, 4, 5, 6], renumber=True)
 
 
+def _l2(a, b):
+    return {f: float(np.linalg.norm(a[:, k] - b[:, k]) / np.linalg.norm(b[:, k]))
+            for k, f in enumerate(FIELDS)}
+
+
 def test_riecg_wave_129cube_fp64_one_step():
     ops = _wave_129()
     assert ops["coord"].shape[1] == 2146689
@@ -75,8 +85,20 @@ def test_riecg_wave_129cube_fp64_one_step():
     dts, _ = d.run(1)
     dto = o.run(1)
     assert np.allclose(dts, dto, rtol=1e-12, atol=0)
-    errs = _per_field(d.state()[0], o.state())
-    assert max(errs.values()) < 1e-12, errs
+    Ud, Uo = d.state()[0], o.state()
+    # the oracle against itself with the edges summed in reverse order
+    rev = oracle.RieCG(ops["coord"], ops["vol"], ops["edges"][::-1].copy(),
+                       ops["dint"][::-1].copy(), ops["tri"], ops["besym"])
+    rev.set_sym(*ops["sym"])
+    rev.set_state(U0)
+    rev.bc()
+    rev.run(1)
+    own = _per_field(rev.state(), Uo)
+    errs = _per_field(Ud, Uo)
+    for f in FIELDS:
+        assert errs[f] <= max(1e-12, 2.0 * own[f]), (f, errs[f], own[f])
+    l2 = _l2(Ud, Uo)
+    assert max(l2.values()) < 1e-13, l2
 
 
 def test_kozcg_wave_129cube_fp64_one_step():
