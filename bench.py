@@ -131,19 +131,30 @@ def build_ops(n, seed=0):
     return riecg.operators(m, sym_sets=[1, 2, 3, 4, 5, 6], renumber=True)
 
 
-def kernel_bytes(n, nedge, fp32):
-    """Algorithmic (compulsory) bytes per launch: every array the kernel must
-    read or write once; gathered neighbour records are re-reads and excluded.
-    nedge edges, each stored once per end in the gradient adjacency and once
-    in the owner's half-edge list (neighbour, D and the slot of the edge in
-    the other end's list, where the owner deposits that end's flux)."""
-    F = 4 if fp32 else 8
-    Wb, Gb, Db = 8 * F, 16 * F, 4 + 3 * F
-    grad = n * (Wb + 8 + 4 + Gb) + 2 * nedge * Db
-    flux = n * (Wb + Gb + 5 * F) + nedge * (Db + 4 + 5 * F)
-    rhs12 = n * (5 * F + Wb + 8 + 4 + 40 + 40 + Wb) + nedge * 5 * F
-    rhs0 = rhs12 + n * 80  # stage 0 also reads U and writes Un
-    return {"riecg_grad": grad, "riecg_flux": flux, "riecg_rhs_update": (rhs0 + 2 * rhs12) / 3.0}
+def kernel_bytes(n, nedge, nbtri, fp32):
+    """Algorithmic bytes per launch of the time loop's kernels, by the
+    reference's dataflow per RK stage (each array read or written once per
+    pass; node arrays 8 B per value, halved for the G, D and coordinate terms
+    in FP32-flux mode; int32 ids): riemann::grad, riemann::rhs and the update
+    read U, write and read G, read coordinates, write and read R, read Un,
+    Vol and write U -- 512 N + 64 E (FP64) or 380 N + 40 E (FP32) for the
+    fused stage kernel -- and the boundary integrals 30 B for the boundary
+    kernel.  The step adds a dt pass and the Un copy (128 N).
+
+    `own` is what the fused kernel itself must move per launch (both ends of
+    every edge in the adjacency, the owned entries' deposit slots, the
+    primitive records in and out, U, 1/vol, the node's degree and boundary
+    index; U written and cbrt(vol) read by the last stage only), averaged
+    over the three stages."""
+    if fp32:
+        stage = 380 * n + 40 * nedge
+        own = 2 * nedge * 16 + nedge * 4 + n * (2 + 4 + 32 + 32 + 40 + 8) + n * 44 / 3.0
+    else:
+        stage = 512 * n + 64 * nedge
+        own = 2 * nedge * 32 + nedge * 4 + n * (2 + 4 + 64 + 64 + 40 + 8) + n * 40 / 3.0
+    bnd = 30 * nbtri
+    return {"riecg_stage": stage, "riecg_bnd": bnd,
+            "step": 3 * (stage + bnd) + 128 * n, "own": {"riecg_stage": own}}
 
 
 def run_chocg(n=129, steps=5, warm=2, tol=1e-8, train_steps=300, seed=0):
@@ -420,6 +431,7 @@ def run_gpu(args, rank, world):
     r = riecg.from_operators(ctx, ops, precision=prec)
     t_setup = time.perf_counter() - t_setup
     nedge = ops["edges"].shape[0]
+    nbtri = ops["tri"].shape[0]
     r.set_state(U0)
     r.bc()
     # warm-up
@@ -454,7 +466,7 @@ def run_gpu(args, rank, world):
     cho = run_chocg(n=args.n) if (rank == 0 and not args.no_pcg) else None
     koz = run_kozcg(n=args.n) if (rank == 0 and not args.no_pcg) else None
     out = {"chocg": cho, "kozcg": koz, "fp64": fp64, "accuracy": accuracy,
-           "n": n, "nedge": nedge, "ms": ms_plain, "ms_events": ms, "kt": kt,
+           "n": n, "nedge": nedge, "nbtri": nbtri, "ms": ms_plain, "ms_events": ms, "kt": kt,
            "clocks": ck.summary(), "e2e_ms": e2e, "setup_s": t_setup, "dts": dts2,
            "dev_bytes": dev_bytes}
     return out
@@ -681,12 +693,13 @@ def main():
     n = res["n"]
     value = world * n * args.steps / (ms / 1e3)
     e2e_val = world * n * args.steps / (e2e_ms / 1e3)
-    kb = kernel_bytes(n, res["nedge"], args.precision == "fp32")
+    kb = kernel_bytes(n, res["nedge"], res["nbtri"], args.precision == "fp32")
     kt = res["kt"]
     dom = max((k for k in kt if k in kb), key=lambda k: kt[k][0])
     avg_ms = kt[dom][0] / kt[dom][1]
     peak, kind = peaks()
     achieved = kb[dom] / (avg_ms / 1e3) / 1e9
+    own = kb["own"].get(dom)
     traffic = None
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
@@ -702,7 +715,12 @@ def main():
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                          "peak_kind": kind, "algorithmic_bytes_per_launch": kb[dom],
-                         "mean_launch_ms": avg_ms},
+                         "mean_launch_ms": avg_ms,
+                         "own_bytes_per_launch": own,
+                         "own_frac": None if own is None else own / (avg_ms / 1e3) / 1e9 / peak},
+            "step_roofline": {"algorithmic_bytes_per_step": kb["step"],
+                              "achieved": kb["step"] / (ms / args.steps / 1e3) / 1e9,
+                              "frac": kb["step"] / (ms / args.steps / 1e3) / 1e9 / peak},
             "kernels": {k: {"ms_total": v[0], "launches": v[1]} for k, v in kt.items()},
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": n * 5 * 8,
                     "d2h_bytes_per_step": n * 5 * 8},
