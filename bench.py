@@ -135,26 +135,36 @@ def kernel_bytes(n, nedge, nbtri, fp32):
     """Algorithmic bytes per launch of the time loop's kernels, by the
     reference's dataflow per RK stage (each array read or written once per
     pass; node arrays 8 B per value, halved for the G, D and coordinate terms
-    in FP32-flux mode; int32 ids): riemann::grad, riemann::rhs and the update
-    read U, write and read G, read coordinates, write and read R, read Un,
-    Vol and write U -- 512 N + 64 E (FP64) or 380 N + 40 E (FP32) for the
-    fused stage kernel -- and the boundary integrals 30 B for the boundary
-    kernel.  The step adds a dt pass and the Un copy (128 N).
+    in FP32-flux mode; int32 ids): riemann::grad reads U and writes G, with
+    the edge ids and D (160 N + 32 E in FP64, 100 N + 20 E in FP32);
+    riemann::rhs reads U, G and coordinates and writes R, with the edge ids
+    and D (224 N + 32 E, or 152 N + 20 E) -- the flux kernel; the update
+    reads R, Un and Vol and writes U (128 N) -- the residual-and-update
+    kernel; each boundary integral 15 B per boundary triangle.  Per stage
+    that is 512 N + 64 E + 30 B (FP64) or 380 N + 40 E + 30 B (FP32), and
+    the step adds a dt pass and the Un copy (128 N).
 
-    `own` is what the fused kernel itself must move per launch (both ends of
-    every edge in the adjacency, the owned entries' deposit slots, the
-    primitive records in and out, U, 1/vol, the node's degree and boundary
-    index; U written and cbrt(vol) read by the last stage only), averaged
-    over the three stages."""
+    `own` is what each kernel itself must move per launch (each array it
+    reads or writes once; gathered neighbour records excluded): the
+    gradient pass both ends of every edge in the adjacency; the flux pass
+    the owned half (neighbour, D and the slot of the edge in the other end's
+    list, where it deposits that end's flux) and the deposits; the
+    residual-and-update pass the deposits and the node state."""
+    F = 4 if fp32 else 8
+    Wb, Gb, Db = 8 * F, 16 * F, 4 + 3 * F
     if fp32:
-        stage = 380 * n + 40 * nedge
-        own = 2 * nedge * 16 + nedge * 4 + n * (2 + 4 + 32 + 32 + 40 + 8) + n * 44 / 3.0
+        grad, flux = 100 * n + 20 * nedge, 152 * n + 20 * nedge
     else:
-        stage = 512 * n + 64 * nedge
-        own = 2 * nedge * 32 + nedge * 4 + n * (2 + 4 + 64 + 64 + 40 + 8) + n * 40 / 3.0
-    bnd = 30 * nbtri
-    return {"riecg_stage": stage, "riecg_bnd": bnd,
-            "step": 3 * (stage + bnd) + 128 * n, "own": {"riecg_stage": own}}
+        grad, flux = 160 * n + 32 * nedge, 224 * n + 32 * nedge
+    upd = 128 * n
+    bnd = 15 * nbtri
+    own_rhs = n * (5 * F + Wb + 8 + 4 + 40 + Wb) + nedge * 5 * F
+    own = {"riecg_grad": n * (Wb + 8 + 4 + Gb) + 2 * nedge * Db,
+           "riecg_flux": n * (Wb + Gb + 5 * F) + nedge * (Db + 4 + 5 * F),
+           "riecg_rhs_update": own_rhs + n * 40 / 3.0}
+    return {"riecg_grad": grad, "riecg_flux": flux, "riecg_rhs_update": upd,
+            "riecg_grad_bnd": bnd, "riecg_rhs_bnd": bnd,
+            "step": 3 * (grad + flux + upd + 2 * bnd) + 128 * n, "own": own}
 
 
 def run_chocg(n=129, steps=5, warm=2, tol=1e-8, train_steps=300, seed=0):

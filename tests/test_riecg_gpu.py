@@ -173,7 +173,8 @@ def test_profile_counts_launches():
     d.profile(True)
     d.run(3)
     kt = d.kernel_times()
-    assert kt["riecg_stage"][1] == 9 and kt["riecg_bnd"][1] == 9
+    assert kt["riecg_grad"][1] == 9 and kt["riecg_rhs_update"][1] == 9
+    assert kt["riecg_flux"][1] == 9
     assert kt["riecg_step_begin"][1] == 3
     d.profile(False)
 

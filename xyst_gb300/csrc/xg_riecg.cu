@@ -21,10 +21,10 @@
 //             canonical edge, PAD for padding) and the canonical edge
 //             integral D (16 bytes in FP32 mode, 32 in FP64 mode).
 //   ivol, cbrtv  1/vol (double) and cbrt(vol) (float) for the FP32 epilogue
-// Every edge flux is evaluated with the canonical orientation (left = first
-// end), so both ends compute bit-identical fluxes and the sum is the
-// reference's up to summation order.  Each node owns its writes: no atomics
-// except the scalar CFL minimum.
+// In FP64 mode every edge flux is evaluated with the canonical orientation
+// (left = first end), so the sum is the reference's up to summation order;
+// FP32 mode evaluates it in the owner's orientation.  Each node owns its
+// writes: no atomics except the scalar CFL minimum.
 
 #include <algorithm>
 #include <cfloat>
@@ -49,10 +49,8 @@ struct Scalars {
   double dt;                  // current step size
   unsigned long long dtmin;   // running minimum of the per-node CFL dt (bits)
   int32_t blowup;             // set when a dt fell below eps
-  int32_t err;                // nonzero: a fused-stage wait timed out (error code)
+  int32_t pad;
   long long step;             // steps taken in the current run (dt history index)
-  int32_t epoch;              // fused stages launched so far (tile flag value)
-  uint32_t ticket;            // next tile ticket of the running fused stage
 };
 
 }  // namespace
@@ -68,6 +66,7 @@ struct RieCGDev {
   double *U = nullptr, *Un = nullptr, *vol = nullptr;
   int32_t* bidx = nullptr;  // per node: index into boundary lists or -1
   void* W[2] = {nullptr, nullptr};
+  void* G = nullptr;
   // adjacency
   int32_t *soff = nullptr, *swidth = nullptr;
   void* ent = nullptr;  // int4 (FP32 mode) or Ent64 (FP64 mode) per entry
@@ -81,17 +80,6 @@ struct RieCGDev {
   void* Rp = nullptr;    // F [5][n] first-end partial residuals
   double* ivol = nullptr;
   float* cbrtv = nullptr;
-  // fused stage (k_stage): tiles of kTile nodes, rings and tile flags
-  int32_t ntiles = 0, lag = 0, rg_mask = 0, rf = 0, smax = 0;
-  int32_t* posr = nullptr;      // per owned entry: deposit ring slot
-  int32_t* dsoff = nullptr;     // per slice: offset of its deposit slots
-  uint16_t* odeg = nullptr;     // per node: owned count | degree << 8
-  int32_t *tmaxref = nullptr, *tminown = nullptr;
-  void* Gring = nullptr;
-  void* fring = nullptr;
-  void* bG = nullptr;
-  void* bR = nullptr;
-  int32_t *gdone = nullptr, *fdone = nullptr, *cdone = nullptr;
   // boundary triangles, per boundary node lists of (tri << 2 | position)
   int32_t *bptr = nullptr, *bnode = nullptr;
   int4* bent4 = nullptr;  // per boundary entry: the triangle's 3 nodes, pos | sym flags << 2
@@ -775,12 +763,13 @@ __device__ __forceinline__ float node_dt_f(const double ud[5], float L, float g)
   return __fdividef(L, fmaxf(vel + c, 1.0e-8f));
 }
 
-// Half-edge residual, pass 1: every edge flux once, at the edge's owner end,
-// in the edge's canonical orientation (riemann::rhs advdom,
-// src/Physics/Riemann.cpp:695-759): -f (owner is the first end) or +f is
-// summed into the owner's partial residual and the other end's contribution
-// (+f or -f) is stored into that end's list-2 slot (pos1), so the second pass
-// reads its fluxes as a coalesced stream.
+// Half-edge residual, pass 1: every edge flux once, at the edge's owner end
+// (riemann::rhs advdom, src/Physics/Riemann.cpp:695-759), in the edge's
+// canonical orientation in FP64 mode (-f summed into the owner's partial
+// residual when the owner is the first end, +f otherwise) and in the owner's
+// orientation in FP32 mode; the other end's contribution is stored into
+// that end's list-2 slot (pos1), so the second pass reads its fluxes as a
+// coalesced stream.
 template <class F>
 struct Half {
   const int32_t* soff1;
@@ -835,27 +824,54 @@ __global__ void __launch_bounds__(kBlock, sizeof(F) == 4 ? 3 : 1)
     load8(W + int64_t(q) * 8, wq);
     load16(G + int64_t(q) * 16, gq);
     const F v0 = wq[5] - wp[5], v1 = wq[6] - wp[6], v2 = wq[7] - wp[7];
-    F wl[5], wr[5], g1[5], g2[5];
+    F f[5], fo[5];
+    if constexpr (sizeof(F) == 4) {
+      // FP32: the flux in the owner's orientation (p -> q, the edge integral
+      // signed accordingly), with no per-component orientation selects; it
+      // differs from the canonical-orientation flux only through the
+      // limiter's 1e-9 regularisation, far below FP32 rounding of the sums
+      F g1[5], g2[5];
 #pragma unroll
-    for (int c = 0; c < 5; ++c) {
-      const F A = proj(gp + 3 * c, v0, v1, v2);
-      const F B = proj(gq + 3 * c, v0, v1, v2);
-      g1[c] = first ? A : -B;
-      g2[c] = first ? B : -A;
-      wl[c] = first ? wp[c] : wq[c];
-      wr[c] = first ? wq[c] : wp[c];
-    }
-    F f[5];
-    if (FLUX == XG_HLLC)
-      hllc(wl, wr, g1, g2, d0, d1, d2, gamma, stab2 != 0, stab2coef, f);
-    else
-      rusanov(wl, wr, g1, g2, d0, d1, d2, gamma, stab2 != 0, stab2coef, f);
-    const F sg = first ? F(-1) : F(1);
-    F fo[5];
+      for (int c = 0; c < 5; ++c) {
+        g1[c] = proj(gp + 3 * c, v0, v1, v2);
+        g2[c] = proj(gq + 3 * c, v0, v1, v2);
+      }
+      if (!first) {
+        d0 = -d0;
+        d1 = -d1;
+        d2 = -d2;
+      }
+      if (FLUX == XG_HLLC)
+        hllc(wp, wq, g1, g2, d0, d1, d2, gamma, stab2 != 0, stab2coef, f);
+      else
+        rusanov(wp, wq, g1, g2, d0, d1, d2, gamma, stab2 != 0, stab2coef, f);
 #pragma unroll
-    for (int c = 0; c < 5; ++c) {
-      R[c] += sg * f[c];
-      fo[c] = -sg * f[c];
+      for (int c = 0; c < 5; ++c) {
+        R[c] -= f[c];
+        fo[c] = f[c];
+      }
+    } else {
+      // FP64: the canonical orientation (left = first end), as the reference
+      F wl[5], wr[5], g1[5], g2[5];
+#pragma unroll
+      for (int c = 0; c < 5; ++c) {
+        const F A = proj(gp + 3 * c, v0, v1, v2);
+        const F B = proj(gq + 3 * c, v0, v1, v2);
+        g1[c] = first ? A : -B;
+        g2[c] = first ? B : -A;
+        wl[c] = first ? wp[c] : wq[c];
+        wr[c] = first ? wq[c] : wp[c];
+      }
+      if (FLUX == XG_HLLC)
+        hllc(wl, wr, g1, g2, d0, d1, d2, gamma, stab2 != 0, stab2coef, f);
+      else
+        rusanov(wl, wr, g1, g2, d0, d1, d2, gamma, stab2 != 0, stab2coef, f);
+      const F sg = first ? F(-1) : F(1);
+#pragma unroll
+      for (int c = 0; c < 5; ++c) {
+        R[c] += sg * f[c];
+        fo[c] = -sg * f[c];
+      }
     }
     store_f4(fbuf, dst, fo);
     fbuf[4 * h.nent2 + dst] = fo[4];
@@ -978,9 +994,10 @@ __device__ __forceinline__ void apply_bc(const BCProg& bc, int64_t i, double gam
 
 // One node's stage state (RieCG::solve, src/Inciter/RieCG.cpp:1010-1021):
 // un = Un - rkcoef*dt*R/vol from uo (U at stage 0, copied to Un, and Un
-// after).  The FP64 mode keeps the reference's expression; FP32 mode uses
-// 1/vol (no FP64 division per node).
-template <class F, int STAGE>
+// after; in the time loop's lean form uo is U, the state at the start of the
+// step, at every stage and nothing is copied).  The FP64 mode keeps the
+// reference's expression; FP32 mode uses 1/vol (no FP64 division per node).
+template <class F, int STAGE, bool LEAN = false>
 __device__ __forceinline__ void stage_state(int64_t n, int64_t p, const F R[5],
                                             const double uo[5],
                                             const double* __restrict__ vol, NodeAux aux,
@@ -990,14 +1007,14 @@ __device__ __forceinline__ void stage_state(int64_t n, int64_t p, const F R[5],
     const double v = vol[p];
 #pragma unroll
     for (int c = 0; c < 5; ++c) {
-      if (STAGE == 0) Un[c * n + p] = uo[c];
+      if (STAGE == 0 && !LEAN) Un[c * n + p] = uo[c];
       un[c] = uo[c] - rk * dt * double(R[c]) / v;
     }
   } else {
     const double cf = rk * dt * aux.ivol[p];
 #pragma unroll
     for (int c = 0; c < 5; ++c) {
-      if (STAGE == 0) Un[c * n + p] = uo[c];
+      if (STAGE == 0 && !LEAN) Un[c * n + p] = uo[c];
       un[c] = uo[c] - cf * double(R[c]);
     }
   }
@@ -1032,12 +1049,40 @@ __device__ __forceinline__ double store_node(int64_t n, int64_t p, const double 
   return dtp;
 }
 
+// Store a node's stage state: in the time loop's lean form the inner stages
+// write only the primitive record (the FP64 state of an inner stage is not
+// read again: every stage updates from the state at the start of the step);
+// otherwise as store_node.
+template <class F, int STAGE, bool LEAN>
+__device__ __forceinline__ double store_stage(int64_t n, int64_t p, const double u[5],
+                                              const F wp[8], const double* __restrict__ vol,
+                                              NodeAux aux, double gamma_d, double* U,
+                                              F* __restrict__ Wout) {
+  if (LEAN && STAGE != 2) {
+    if constexpr (sizeof(F) == 8) {
+      double pw[5];
+      prim5(u, pw);
+      F o[8] = {F(pw[0]), F(pw[1]), F(pw[2]), F(pw[3]), F(pw[4]), wp[5], wp[6], wp[7]};
+      store8(Wout + p * 8, o);
+    } else {
+      const float r = float(u[0]);
+      const float ir = __frcp_rn(r);
+      const float uu = float(u[1]) * ir, vv = float(u[2]) * ir, ww = float(u[3]) * ir;
+      const float ie = float(u[4]) * ir - 0.5f * (uu * uu + vv * vv + ww * ww);
+      F o[8] = {r, uu, vv, ww, ie, wp[5], wp[6], wp[7]};
+      store8(Wout + p * 8, o);
+    }
+    return DBL_MAX;
+  }
+  return store_node<F>(n, p, u, wp, STAGE == 2, vol, aux, gamma_d, U, Wout);
+}
+
 // Half-edge residual, pass 2: the fluxes of the edges the other end owns and
 // (optionally) the RK update of one stage with the new primitive records and,
 // on the last stage, the CFL minimum.  Boundary nodes only park their domain
 // residual in Rb: k_rhs_bnd adds their boundary integral and updates them,
 // so no warp here waits on the triangle gathers.
-template <class F, int STAGE, bool UPDATE>
+template <class F, int STAGE, bool UPDATE, bool LEAN>
 __global__ void __launch_bounds__(kBlock, sizeof(F) == 4 ? 4 : 1)
     k_rhs2(int64_t n, Half<F> h, const F* __restrict__ fbuf, const F* __restrict__ Rp,
            const F* __restrict__ W, Bnd bnd, int64_t nbn, F* __restrict__ Rb,
@@ -1059,7 +1104,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(F) == 4 ? 4 : 1)
     double uo[5];
     if (UPDATE && bi < 0) {
 #pragma unroll
-      for (int c = 0; c < 5; ++c) uo[c] = STAGE == 0 ? U[c * n + p] : Un[c * n + p];
+      for (int c = 0; c < 5; ++c) uo[c] = (STAGE == 0 || LEAN) ? U[c * n + p] : Un[c * n + p];
     }
     F wp[8];
     if (UPDATE && bi < 0) load8(W + p * 8, wp);
@@ -1092,8 +1137,8 @@ __global__ void __launch_bounds__(kBlock, sizeof(F) == 4 ? 4 : 1)
       for (int c = 0; c < 5; ++c) Rout[p * 5 + c] = double(R[c]);
     } else {
       double un[5];
-      stage_state<F, STAGE>(n, p, R, uo, vol, aux, scal->dt, Un, un);
-      dtp = store_node<F>(n, p, un, wp, STAGE == 2, vol, aux, gamma_d, U, Wout);
+      stage_state<F, STAGE, LEAN>(n, p, R, uo, vol, aux, scal->dt, Un, un);
+      dtp = store_stage<F, STAGE, LEAN>(n, p, un, wp, vol, aux, gamma_d, U, Wout);
     }
   }
   if (UPDATE && STAGE == 2) block_min_atomic(dtp, dtmin);
@@ -1104,7 +1149,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(F) == 4 ? 4 : 1)
 // update, then the node's nodal BCs (RieCG::BC after RieCG::solve's update,
 // src/Inciter/RieCG.cpp:1010-1030; every BC node lies on a boundary
 // triangle) and, on the last stage, the CFL time step of the final state.
-template <class F, int STAGE, bool UPDATE>
+template <class F, int STAGE, bool UPDATE, bool LEAN>
 __global__ void __launch_bounds__(kBlock)
     k_rhs_bnd(int64_t n, int64_t nbn, Bnd bnd, const F* __restrict__ Rb,
               const F* __restrict__ W, const int32_t* __restrict__ bcof, BCProg bc,
@@ -1121,7 +1166,7 @@ __global__ void __launch_bounds__(kBlock)
     double uo[5];
     if (UPDATE) {
 #pragma unroll
-      for (int c = 0; c < 5; ++c) uo[c] = STAGE == 0 ? U[c * n + p] : Un[c * n + p];
+      for (int c = 0; c < 5; ++c) uo[c] = (STAGE == 0 || LEAN) ? U[c * n + p] : Un[c * n + p];
     }
     F wp[8];
     load8(W + p * 8, wp);
@@ -1132,442 +1177,12 @@ __global__ void __launch_bounds__(kBlock)
       for (int c = 0; c < 5; ++c) Rout[p * 5 + c] = double(R[c]);
     } else {
       double un[5];
-      stage_state<F, STAGE>(n, p, R, uo, vol, aux, scal->dt, Un, un);
+      stage_state<F, STAGE, LEAN>(n, p, R, uo, vol, aux, scal->dt, Un, un);
       if (b >= 0) apply_bc(bc, b, gamma_d, un);
-      dtp = store_node<F>(n, p, un, wp, STAGE == 2, vol, aux, gamma_d, U, Wout);
+      dtp = store_stage<F, STAGE, LEAN>(n, p, un, wp, vol, aux, gamma_d, U, Wout);
     }
   }
   if (UPDATE && STAGE == 2) block_min_atomic(dtp, dtmin);
-}
-
-// ---------------------------------------------------------------------------
-// Fused stage: one launch per RK stage runs the gradient pass, the edge-flux
-// pass and the node update as a wavefront over tiles of 256 consecutive
-// (RCM-ordered) nodes.  Each block takes the next ticket t from a counter and
-// runs
-//   phase A  gradients of tile t into a ring of G records,
-//   phase B  the fluxes of the edges owned by tile b = t - lag (owner = the
-//            smaller id), summed into the owners' residuals in registers and
-//            deposited, signed, into the other ends' deposit slots of a ring,
-//   phase C  tile b's residual (own sum + deposits + boundary terms), the
-//            stage update, the nodal BCs and the new primitive records.
-// Phase B of tile b needs the G records of tiles b..maxref(b) (its edges'
-// other ends) and phase C the deposits of the owner tiles minown(b)..b-1;
-// both come from lower tickets.  Tickets are taken in order by running
-// blocks, so every wait is on a block that is running or done: the lowest
-// unfinished ticket never waits on anything unfinished.  A ring slot is only
-// rewritten after the flags of the phase that read its last contents say so.
-// G records and deposits live only in these rings (sized to the blocks
-// resident at once, tens of MB, L2-resident); they never make the round trip
-// to HBM.  Every wait is bounded: after kSpinLimit polls the block records an
-// error status and returns, and the other blocks return at their next wait.
-
-constexpr int kTile = 256;              // nodes per tile (8 SELL slices)
-constexpr int kSpinLimit = 1 << 22;     // polls per flag (about a second)
-constexpr int32_t kErrStageWait = 101;  // Scalars::err: a stage wait timed out
-
-__device__ __forceinline__ int ld_acquire(const int32_t* p) {
-  int v;
-  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ __forceinline__ void st_release(int32_t* p, int v) {
-  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-
-// Loads of records written by other blocks during the same launch: through
-// L2 only (ld.cg), never from a possibly stale L1 line of an earlier use of
-// the same ring slot.
-__device__ __forceinline__ void load8_cg(const float* p, float o[8]) {
-  asm volatile("ld.global.cg.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-               : "=f"(o[0]), "=f"(o[1]), "=f"(o[2]), "=f"(o[3]), "=f"(o[4]), "=f"(o[5]),
-                 "=f"(o[6]), "=f"(o[7])
-               : "l"(p));
-}
-__device__ __forceinline__ void load8_cg(const double* p, double o[8]) {
-  asm volatile("ld.global.cg.v4.f64 {%0,%1,%2,%3}, [%4];"
-               : "=d"(o[0]), "=d"(o[1]), "=d"(o[2]), "=d"(o[3])
-               : "l"(p));
-  asm volatile("ld.global.cg.v4.f64 {%0,%1,%2,%3}, [%4];"
-               : "=d"(o[4]), "=d"(o[5]), "=d"(o[6]), "=d"(o[7])
-               : "l"(p + 4));
-}
-template <class F>
-__device__ __forceinline__ void load16_cg(const F* p, F o[16]) {
-  load8_cg(p, o);
-  load8_cg(p + 8, o + 8);
-}
-__device__ __forceinline__ void load_f4_cg(const float* a, int64_t i, float f[4]) {
-  const float4 v = __ldcg(reinterpret_cast<const float4*>(a) + i);
-  f[0] = v.x;
-  f[1] = v.y;
-  f[2] = v.z;
-  f[3] = v.w;
-}
-__device__ __forceinline__ void load_f4_cg(const double* a, int64_t i, double f[4]) {
-  const double2* q = reinterpret_cast<const double2*>(a) + 2 * i;
-  const double2 u = __ldcg(q), v = __ldcg(q + 1);
-  f[0] = u.x;
-  f[1] = u.y;
-  f[2] = v.x;
-  f[3] = v.y;
-}
-
-// Poll one flag until it holds ep; false on timeout or when another block
-// has recorded an error.
-__device__ __forceinline__ bool spin_until(const int32_t* f, int ep, int32_t* err) {
-  for (int it = 0; it < kSpinLimit; ++it) {
-    if (ld_acquire(f) == ep) return true;
-    if (*reinterpret_cast<volatile int32_t*>(err) != 0) return false;
-    __nanosleep(it < 8 ? 32 : 256);
-  }
-  atomicCAS(err, 0, kErrStageWait);
-  return false;
-}
-
-// Wait until flags f1[lo1 .. lo1+n1) and f2[lo2 .. lo2+n2) all hold ep, the
-// threads of the block polling in parallel (acquire loads), then a block
-// barrier, after which every thread may read what the flagged phases wrote.
-// Returns false (in every thread) when any wait failed.  n1 + n2 is uniform
-// over the block.
-__device__ __forceinline__ bool wait_flags(const int32_t* f1, int lo1, int n1, const int32_t* f2,
-                                           int lo2, int n2, int ep, int32_t* err) {
-  if (n1 + n2 <= 0) return true;
-  bool ok = true;
-  for (int i = threadIdx.x; i < n1 + n2; i += blockDim.x) {
-    const int32_t* f = i < n1 ? f1 + lo1 + i : f2 + lo2 + (i - n1);
-    ok = ok && spin_until(f, ep, err);
-  }
-  return __syncthreads_or(!ok) == 0;
-}
-
-// Publish a phase of a tile: a block barrier orders every thread's writes
-// before thread 0's device-scope fence and release store of the flag (the
-// pattern of a grid-wide barrier's arrival).
-__device__ __forceinline__ void publish(int32_t* flag, int ep) {
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    st_release(flag, ep);
-  }
-}
-
-template <class F>
-struct StageArgs {
-  int64_t n;
-  int32_t ntiles, lag, rg_mask, rf, smax;  // rg_mask = G ring nodes - 1 (power of two);
-                                           // rf deposit ring tiles of smax slots
-  Adj<F> adj;                              // both ends of every edge, owned entries first
-  const int32_t* posr;       // per owned entry: the deposit ring slot of the other end
-  const int32_t* dsoff;      // per slice: offset of its deposit slots (SELL-32)
-  const uint16_t* odeg;      // per node: owned count | degree << 8
-  const int32_t* tmaxref;    // per tile: largest tile its owned edges reach
-  const int32_t* tminown;    // per tile: smallest tile owning an edge into it
-  const F* Win;
-  F* Wout;
-  F* Gring;                  // [ring nodes][16]
-  F* fring;                  // [rf * smax][4], then [rf * smax]
-  const int32_t* bidx;
-  const F* bG;               // [nbn][16] boundary-triangle gradient terms
-  const F* bR;               // [nbn][8] boundary-triangle residual terms
-  const int32_t* bcof;
-  BCProg bc;
-  const double* vol;
-  NodeAux aux;
-  double gamma;
-  int stab2;
-  double stab2coef;
-  Scalars* scal;
-  double* U;
-  double* Un;
-  int32_t *gdone, *fdone, *cdone;
-};
-
-// Boundary-triangle terms of both passes for every boundary node, from the
-// stage's input records (the boundary integrals of riemann::grad,
-// src/Physics/Riemann.cpp:329-364, and of advbnd, :768-878, each summed over
-// the node's triangles in order); block 0 also opens the stage: a new epoch
-// for the tile flags and a reset ticket counter.
-template <class F>
-__global__ void __launch_bounds__(kBlock) k_bnd_terms(int64_t nbn, Bnd bnd,
-                                                       const F* __restrict__ W, double gamma_d,
-                                                       F* __restrict__ bG, F* __restrict__ bR,
-                                                       Scalars* scal) {
-  const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    scal->ticket = 0;
-    scal->epoch = scal->epoch + 1;
-  }
-  if (i >= nbn) return;
-  F g[16];
-#pragma unroll
-  for (int k = 0; k < 16; ++k) g[k] = F(0);
-  grad_bnd_term(bnd, static_cast<int32_t>(i), W, g);
-  store16(bG + i * 16, g);
-  F R[8] = {F(0), F(0), F(0), F(0), F(0), F(0), F(0), F(0)};
-  rhs_bnd_term(bnd, static_cast<int32_t>(i), W, F(gamma_d), R);
-  store8(bR + i * 8, R);
-}
-
-// One RK stage as a tile wavefront (see above).  LEAN: U holds the state at
-// the start of the step and is only written by the last stage (the time
-// loop); otherwise every stage writes U, stage 0 copying it to Un first (the
-// single-stage entry point, which exposes every stage's state).
-template <class F, int FLUX, int STAGE, bool LEAN>
-__global__ void __launch_bounds__(kTile, sizeof(F) == 4 ? 4 : 1) k_stage(StageArgs<F> A) {
-  using EntT = typename EntOf<F>::type;
-  constexpr int RL = ring_len<EntT>();
-  __shared__ EntT ring[RL][kTile];
-  __shared__ int s_ticket;
-  const int tid = threadIdx.x;
-  if (tid == 0) s_ticket = static_cast<int>(atomicAdd(&A.scal->ticket, 1u));
-  __syncthreads();
-  const int t = s_ticket;
-  const int ep = *reinterpret_cast<volatile int32_t*>(&A.scal->epoch);
-  int32_t* err = &A.scal->err;
-  const int64_t n = A.n;
-  const int rg_tiles = (A.rg_mask + 1) / kTile;
-
-  // ---------------- phase A: gradients of tile t
-  if (t < A.ntiles) {
-    const int a = t;
-    const int old = a - rg_tiles;  // the tile whose G records this ring slot held
-    if (old >= 0) {
-      const int lo = __ldg(A.tminown + old);
-      if (!wait_flags(A.fdone, lo, old - lo + 1, A.fdone, 0, 0, ep, err)) return;
-    }
-    const int64_t p = int64_t(a) * kTile + tid;
-    if (p < n) {
-      const int lane = static_cast<int>(p & (kSlice - 1));
-      const int64_t s = p >> 5;
-      const int32_t off = __ldg(A.adj.soff + s), w = __ldg(A.adj.swidth + s);
-      const EntT* src = A.adj.ent + off + lane;
-      // entries 0..RL-2 requested up front, entry k+RL-1 while entry k is
-      // summed, into the slot entry k-1 freed
-#pragma unroll
-      for (int j = 0; j < RL - 1; ++j) {
-        if (j < w) fetch_ent(&ring[j][tid], src + j * kSlice);
-        cp_async_commit();
-      }
-      F wp[5];
-      load5(A.Win + p * 8, wp);
-      F g[15];
-#pragma unroll
-      for (int i = 0; i < 15; ++i) g[i] = F(0);
-      for (int k = 0; k < w; ++k) {
-        cp_async_wait<RL - 2>();
-        int32_t q;
-        F d0, d1, d2;
-        dec_ent(&ring[k & (RL - 1)][tid], q, d0, d1, d2);
-        if (k + RL - 1 < w)
-          fetch_ent(&ring[(k + RL - 1) & (RL - 1)][tid], src + (k + RL - 1) * kSlice);
-        cp_async_commit();
-        if (q == kPad) continue;
-        if (q >= 0) {  // this node is the first end: G -= f
-          d0 = -d0;
-          d1 = -d1;
-          d2 = -d2;
-        } else {
-          q = ~q;
-        }
-        F wq[5];
-        load5(A.Win + int64_t(q) * 8, wq);
-#pragma unroll
-        for (int c = 0; c < 5; ++c) {
-          const F sum = wq[c] + wp[c];
-          g[c * 3 + 0] += d0 * sum;
-          g[c * 3 + 1] += d1 * sum;
-          g[c * 3 + 2] += d2 * sum;
-        }
-      }
-      cp_async_wait<0>();
-      const int32_t bi = __ldg(A.bidx + p);
-      if (bi >= 0) {
-        F gb[16];
-        load16(A.bG + int64_t(bi) * 16, gb);
-#pragma unroll
-        for (int i = 0; i < 15; ++i) g[i] += gb[i];
-      }
-      F o[16];
-      finish_grad(g, 1, A.vol, A.aux, p, o);
-      o[15] = F(0);
-      store16(A.Gring + (p & A.rg_mask) * 16, o);
-    }
-    publish(A.gdone + a, ep);  // its barrier also frees the entry ring for phase B
-  }
-
-  // ---------------- phase B: fluxes of the edges tile b owns
-  const int b = t - A.lag;
-  if (b < 0 || b >= A.ntiles) return;
-  {
-    const int hi = __ldg(A.tmaxref + b);
-    const int lo2 = max(0, b - A.rf), hi2 = hi - A.rf;
-    if (!wait_flags(A.gdone, b, hi - b + 1, A.cdone, lo2, max(0, hi2 - lo2 + 1), ep, err))
-      return;
-  }
-  const int64_t p = int64_t(b) * kTile + tid;
-  const bool active = p < n;
-  const F gamma = F(A.gamma), stab2coef = F(A.stab2coef);
-  // deposit ring index of slot j of this node: rbase + dsoff[slice] + 32 j + lane
-  const int64_t rbase =
-      int64_t(b % A.rf) * A.smax - __ldg(A.dsoff + int64_t(b) * (kTile / kSlice));
-  F* fr4 = A.fring;
-  F* fr1 = A.fring + int64_t(4) * A.rf * A.smax;
-  F R[5] = {F(0), F(0), F(0), F(0), F(0)};
-  int32_t off = 0, doff = 0, own = 0, deg = 0;
-  int lane = 0;
-  F wp[8];
-  if (active) {
-    lane = static_cast<int>(p & (kSlice - 1));
-    const int64_t s = p >> 5;
-    off = __ldg(A.adj.soff + s);
-    doff = __ldg(A.dsoff + s);
-    const uint16_t od = __ldg(A.odeg + p);
-    own = od & 0xff;
-    deg = od >> 8;
-  }
-  const int wown = __reduce_max_sync(0xffffffffu, own);  // owned entries of the warp's slice
-  if (active) {
-    const EntT* src = A.adj.ent + off + lane;
-#pragma unroll
-    for (int j = 0; j < RL - 1; ++j) {
-      if (j < wown) fetch_ent(&ring[j][tid], src + j * kSlice);
-      cp_async_commit();
-    }
-    F gp[16];
-    load8(A.Win + p * 8, wp);
-    load16_cg(A.Gring + (p & A.rg_mask) * 16, gp);
-    for (int k = 0; k < wown; ++k) {
-      const int32_t e = off + k * kSlice + lane;
-      cp_async_wait<RL - 2>();
-      int32_t q;
-      F d0, d1, d2;
-      dec_ent(&ring[k & (RL - 1)][tid], q, d0, d1, d2);
-      if (k + RL - 1 < wown)
-        fetch_ent(&ring[(k + RL - 1) & (RL - 1)][tid], src + (k + RL - 1) * kSlice);
-      cp_async_commit();
-      if (k >= own) continue;
-      const int32_t dst = __ldg(A.posr + e);
-      const bool first = q >= 0;
-      if (!first) q = ~q;
-      F wq[8], gq[16];
-      load8(A.Win + int64_t(q) * 8, wq);
-      load16_cg(A.Gring + (int64_t(q) & A.rg_mask) * 16, gq);
-      const F v0 = wq[5] - wp[5], v1 = wq[6] - wp[6], v2 = wq[7] - wp[7];
-      F wl[5], wr[5], g1[5], g2[5];
-#pragma unroll
-      for (int c = 0; c < 5; ++c) {
-        const F Ap = proj(gp + 3 * c, v0, v1, v2);
-        const F Bq = proj(gq + 3 * c, v0, v1, v2);
-        g1[c] = first ? Ap : -Bq;
-        g2[c] = first ? Bq : -Ap;
-        wl[c] = first ? wp[c] : wq[c];
-        wr[c] = first ? wq[c] : wp[c];
-      }
-      F f[5];
-      if (FLUX == XG_HLLC)
-        hllc(wl, wr, g1, g2, d0, d1, d2, gamma, A.stab2 != 0, stab2coef, f);
-      else
-        rusanov(wl, wr, g1, g2, d0, d1, d2, gamma, A.stab2 != 0, stab2coef, f);
-      const F sg = first ? F(-1) : F(1);
-      F fo[5];
-#pragma unroll
-      for (int c = 0; c < 5; ++c) {
-        R[c] += sg * f[c];
-        fo[c] = -sg * f[c];
-      }
-      store_f4(fr4, dst, fo);
-      fr1[dst] = fo[4];
-    }
-    cp_async_wait<0>();
-  }
-  publish(A.fdone + b, ep);
-
-  // ---------------- phase C: residual, update and BCs of tile b
-  {
-    const int lo = __ldg(A.tminown + b);
-    if (!wait_flags(A.fdone, lo, b - lo, A.fdone, 0, 0, ep, err)) return;
-  }
-  double dtp = DBL_MAX;
-  // the deposits of the edges this node's lower neighbours own (its entries
-  // own..deg-1, entries ordered by decreasing neighbour): deg - own slots,
-  // visited in warp-uniform rounds so that each round's loads coalesce
-  const int nd = deg - own;
-  const int ndw = __reduce_max_sync(0xffffffffu, nd);
-  if (active) {
-    for (int k0 = 0; k0 < ndw; k0 += 4) {
-      F f[4][4], f4[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        if (k0 + u < nd) {
-          const int64_t e = rbase + doff + (k0 + u) * kSlice + lane;
-          load_f4_cg(fr4, e, f[u]);
-          f4[u] = __ldcg(fr1 + e);
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        if (k0 + u < nd) {
-#pragma unroll
-          for (int c = 0; c < 4; ++c) R[c] += f[u][c];
-          R[4] += f4[u];
-        }
-      }
-    }
-    const int32_t bi = __ldg(A.bidx + p);
-    if (bi >= 0) {
-      F rb[8];
-      load8(A.bR + int64_t(bi) * 8, rb);
-#pragma unroll
-      for (int c = 0; c < 5; ++c) R[c] += rb[c];
-    }
-    // the stage update (RieCG::solve, src/Inciter/RieCG.cpp:1010-1021), the
-    // same arithmetic as stage_state
-    double uo[5];
-#pragma unroll
-    for (int c = 0; c < 5; ++c) uo[c] = (LEAN || STAGE == 0) ? A.U[c * n + p] : A.Un[c * n + p];
-    if (!LEAN && STAGE == 0) {
-#pragma unroll
-      for (int c = 0; c < 5; ++c) A.Un[c * n + p] = uo[c];
-    }
-    constexpr double rk = STAGE == 0 ? 1.0 / 3.0 : (STAGE == 1 ? 0.5 : 1.0);
-    const double dt = A.scal->dt;
-    double un[5];
-    if constexpr (sizeof(F) == 8) {
-      const double v = A.vol[p];
-#pragma unroll
-      for (int c = 0; c < 5; ++c) un[c] = uo[c] - rk * dt * double(R[c]) / v;
-    } else {
-      const double cf = rk * dt * A.aux.ivol[p];
-#pragma unroll
-      for (int c = 0; c < 5; ++c) un[c] = uo[c] - cf * double(R[c]);
-    }
-    if (bi >= 0) {
-      const int32_t bcix = __ldg(A.bcof + bi);
-      if (bcix >= 0) apply_bc(A.bc, bcix, A.gamma, un);
-    }
-    if (LEAN && STAGE != 2) {
-      // only the primitive record: the FP64 state of an inner stage is not
-      // needed after it
-      if constexpr (sizeof(F) == 8) {
-        double pw[5];
-        prim5(un, pw);
-        F o[8] = {F(pw[0]), F(pw[1]), F(pw[2]), F(pw[3]), F(pw[4]), wp[5], wp[6], wp[7]};
-        store8(A.Wout + p * 8, o);
-      } else {
-        const float r = float(un[0]);
-        const float ir = __frcp_rn(r);
-        const float uu = float(un[1]) * ir, vv = float(un[2]) * ir, ww = float(un[3]) * ir;
-        const float ie = float(un[4]) * ir - 0.5f * (uu * uu + vv * vv + ww * ww);
-        F o[8] = {r, uu, vv, ww, ie, wp[5], wp[6], wp[7]};
-        store8(A.Wout + p * 8, o);
-      }
-    } else {
-      dtp = store_node<F>(n, p, un, wp, STAGE == 2, A.vol, A.aux, A.gamma, A.U, A.Wout);
-    }
-  }
-  if (STAGE == 2) block_min_atomic(dtp, &A.scal->dtmin);
-  publish(A.cdone + b, ep);
 }
 
 // Nodal BCs on the device state (RieCG::BC), one thread per BC node; refreshes
@@ -1660,14 +1275,6 @@ struct HalfLists {
   std::vector<int32_t> soff1, sw1, soff2, sw2, q1, pos1;
   std::vector<double> d1;
   int64_t nent1 = 0, nent2 = 0;
-};
-
-// Host plan of the fused stage (k_stage).
-struct FusedPlan {
-  int32_t ntiles = 0, lag = 0, rf = 0, smax = 0;
-  int64_t rg_nodes = 0;
-  std::vector<int32_t> tmaxref, tminown, posr, dsoff;
-  std::vector<uint16_t> odeg;
 };
 
 int launch_done(xg_ctx* c, RieCGDev* d, int slot, cudaEvent_t e0) {
@@ -1764,7 +1371,7 @@ Half<F> half_of(RieCGDev* d) {
                  d->pos1, d->soff2, d->sw2, d->nent2};
 }
 
-template <class F, int FLUX, int STAGE, bool UPDATE>
+template <class F, int FLUX, int STAGE, bool UPDATE, bool LEAN>
 int launch_rhs_t(xg_ctx* c, RieCGDev* d, const F* W, const F* G, F* Wout, double* Rout) {
   F* fbuf = static_cast<F*>(d->fbuf);
   F* Rp = static_cast<F*>(d->Rp);
@@ -1773,14 +1380,14 @@ int launch_rhs_t(xg_ctx* c, RieCGDev* d, const F* W, const F* G, F* Wout, double
                      d->n, half_of<F>(d), W, G, d->prm.gamma, d->prm.stab2, d->prm.stab2coef,
                      fbuf, Rp)));
   XG_PROF_LAUNCH(c, d, "riecg_rhs_update",
-                 (k_rhs2<F, STAGE, UPDATE><<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(
+                 (k_rhs2<F, STAGE, UPDATE, LEAN><<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(
                      d->n, half_of<F>(d), fbuf, Rp, W, bnd_of(d), d->nbn,
                      static_cast<F*>(d->Rb), d->vol, aux_of(d), d->prm.gamma, d->scal, d->U,
                      d->Un, Wout, Rout, &d->scal->dtmin)));
   if (d->nbn > 0)
     XG_PROF_LAUNCH(c, d, "riecg_rhs_bnd",
-                   (k_rhs_bnd<F, STAGE, UPDATE><<<blocks_for(d->nbn, kBlock), kBlock, 0,
-                                                  c->stream>>>(
+                   (k_rhs_bnd<F, STAGE, UPDATE, LEAN><<<blocks_for(d->nbn, kBlock), kBlock, 0,
+                                                        c->stream>>>(
                        d->n, d->nbn, bnd_of(d), static_cast<const F*>(d->Rb), W, d->bcof,
                        bcprog_of(d), d->vol, aux_of(d), d->prm.gamma, d->scal, d->U, d->Un,
                        Wout, Rout, &d->scal->dtmin)));
@@ -1788,20 +1395,27 @@ int launch_rhs_t(xg_ctx* c, RieCGDev* d, const F* W, const F* G, F* Wout, double
 }
 
 template <class F, int FLUX>
-int launch_rhs_f(xg_ctx* c, RieCGDev* d, int stage, bool update, const F* W, const F* G, F* Wout,
-                 double* Rout) {
-  if (!update) return launch_rhs_t<F, FLUX, 0, false>(c, d, W, G, Wout, Rout);
-  if (stage == 0) return launch_rhs_t<F, FLUX, 0, true>(c, d, W, G, Wout, Rout);
-  if (stage == 1) return launch_rhs_t<F, FLUX, 1, true>(c, d, W, G, Wout, Rout);
-  return launch_rhs_t<F, FLUX, 2, true>(c, d, W, G, Wout, Rout);
+int launch_rhs_f(xg_ctx* c, RieCGDev* d, int stage, bool update, bool lean, const F* W,
+                 const F* G, F* Wout, double* Rout) {
+  if (!update) return launch_rhs_t<F, FLUX, 0, false, false>(c, d, W, G, Wout, Rout);
+  if (lean) {
+    if (stage == 0) return launch_rhs_t<F, FLUX, 0, true, true>(c, d, W, G, Wout, Rout);
+    if (stage == 1) return launch_rhs_t<F, FLUX, 1, true, true>(c, d, W, G, Wout, Rout);
+    return launch_rhs_t<F, FLUX, 2, true, true>(c, d, W, G, Wout, Rout);
+  }
+  if (stage == 0) return launch_rhs_t<F, FLUX, 0, true, false>(c, d, W, G, Wout, Rout);
+  if (stage == 1) return launch_rhs_t<F, FLUX, 1, true, false>(c, d, W, G, Wout, Rout);
+  return launch_rhs_t<F, FLUX, 2, true, false>(c, d, W, G, Wout, Rout);
 }
 
+// The residual pass; with update, also the stage update (lean: the time
+// loop's form, see store_stage).
 template <class F>
-int launch_rhs(xg_ctx* c, RieCGDev* d, int stage, bool update, const F* W, const F* G, F* Wout,
-               double* Rout) {
+int launch_rhs(xg_ctx* c, RieCGDev* d, int stage, bool update, bool lean, const F* W, const F* G,
+               F* Wout, double* Rout) {
   if (d->prm.flux == XG_HLLC)
-    return launch_rhs_f<F, XG_HLLC>(c, d, stage, update, W, G, Wout, Rout);
-  return launch_rhs_f<F, XG_RUSANOV>(c, d, stage, update, W, G, Wout, Rout);
+    return launch_rhs_f<F, XG_HLLC>(c, d, stage, update, lean, W, G, Wout, Rout);
+  return launch_rhs_f<F, XG_RUSANOV>(c, d, stage, update, lean, W, G, Wout, Rout);
 }
 
 template <class F>
@@ -1814,85 +1428,21 @@ int launch_bc(xg_ctx* c, RieCGDev* d, F* W, int want_dt) {
   return XG_OK;
 }
 
-template <class F>
-StageArgs<F> stage_args(RieCGDev* d) {
-  StageArgs<F> a;
-  a.n = d->n;
-  a.ntiles = d->ntiles;
-  a.lag = d->lag;
-  a.rg_mask = d->rg_mask;
-  a.rf = d->rf;
-  a.smax = d->smax;
-  a.adj = adj_of<F>(d);
-  a.posr = d->posr;
-  a.dsoff = d->dsoff;
-  a.odeg = d->odeg;
-  a.tmaxref = d->tmaxref;
-  a.tminown = d->tminown;
-  a.Win = static_cast<const F*>(d->W[d->cur]);
-  a.Wout = static_cast<F*>(d->W[d->cur ^ 1]);
-  a.Gring = static_cast<F*>(d->Gring);
-  a.fring = static_cast<F*>(d->fring);
-  a.bidx = d->bidx;
-  a.bG = static_cast<const F*>(d->bG);
-  a.bR = static_cast<const F*>(d->bR);
-  a.bcof = d->bcof;
-  a.bc = bcprog_of(d);
-  a.vol = d->vol;
-  a.aux = aux_of(d);
-  a.gamma = d->prm.gamma;
-  a.stab2 = d->prm.stab2;
-  a.stab2coef = d->prm.stab2coef;
-  a.scal = d->scal;
-  a.U = d->U;
-  a.Un = d->Un;
-  a.gdone = d->gdone;
-  a.fdone = d->fdone;
-  a.cdone = d->cdone;
-  return a;
-}
-
-template <class F, int FLUX, int STAGE, bool LEAN>
-int launch_stage_t(xg_ctx* c, RieCGDev* d) {
-  XG_PROF_LAUNCH(c, d, "riecg_stage",
-                 (k_stage<F, FLUX, STAGE, LEAN><<<static_cast<unsigned>(d->ntiles + d->lag), kTile,
-                                                  0, c->stream>>>(stage_args<F>(d))));
-  return XG_OK;
-}
-
-template <class F, int FLUX>
-int launch_stage_f(xg_ctx* c, RieCGDev* d, int stage, bool lean) {
-  if (lean) {
-    if (stage == 0) return launch_stage_t<F, FLUX, 0, true>(c, d);
-    if (stage == 1) return launch_stage_t<F, FLUX, 1, true>(c, d);
-    return launch_stage_t<F, FLUX, 2, true>(c, d);
-  }
-  if (stage == 0) return launch_stage_t<F, FLUX, 0, false>(c, d);
-  if (stage == 1) return launch_stage_t<F, FLUX, 1, false>(c, d);
-  return launch_stage_t<F, FLUX, 2, false>(c, d);
-}
-
-// One stage on the device state: the boundary-triangle terms of the input
-// records, then the fused stage.  lean: the time loop's form (U written by
-// the last stage only); otherwise every stage's state lands in U.
+// One stage on the device state.  lean: the time loop's form (U holds the
+// state at the start of the step and only the last stage writes it);
+// otherwise every stage's state lands in U (stage 0 copying U to Un first).
 template <class F>
 int do_stage(xg_ctx* c, RieCGDev* d, int stage, bool lean) {
-  const F* Win = static_cast<const F*>(d->W[d->cur]);
-  XG_PROF_LAUNCH(c, d, "riecg_bnd",
-                 (k_bnd_terms<F><<<std::max(1u, blocks_for(d->nbn, kBlock)), kBlock, 0,
-                                   c->stream>>>(d->nbn, bnd_of(d), Win, d->prm.gamma,
-                                                static_cast<F*>(d->bG), static_cast<F*>(d->bR),
-                                                d->scal)));
-  int rc = d->prm.flux == XG_HLLC ? launch_stage_f<F, XG_HLLC>(c, d, stage, lean)
-                                  : launch_stage_f<F, XG_RUSANOV>(c, d, stage, lean);
+  F* Win = static_cast<F*>(d->W[d->cur]);
+  F* Wout = static_cast<F*>(d->W[d->cur ^ 1]);
+  F* G = static_cast<F*>(d->G);
+  int rc = launch_grad<F>(c, d, Win, G, 1);
+  if (rc) return rc;
+  // the residual pass updates every node and applies the nodal BCs of the
+  // boundary nodes (all BC nodes) after their update
+  rc = launch_rhs<F>(c, d, stage, true, lean, Win, G, Wout, nullptr);
   if (rc) return rc;
   d->cur ^= 1;
-  return XG_OK;
-}
-
-// The status the fused stages leave in the scalars (after a synchronise).
-int stage_status(xg_ctx* c, const Scalars& s) {
-  if (s.err) return fail(c, XG_ERR_DEVICE, "fused stage: a tile wait timed out");
   return XG_OK;
 }
 
@@ -1916,10 +1466,10 @@ int alloc_and_upload(xg_ctx* c, RieCGDev* d, const double* coord, const double* 
                      const std::vector<int32_t>& nbr, const std::vector<double>& ddx,
                      const std::vector<double>& ddy, const std::vector<double>& ddz,
                      const std::vector<int32_t>& bidx, const std::vector<int32_t>& bptr,
-                     const std::vector<int4>& bent4, const HalfLists& hl, const FusedPlan& fp) {
+                     const std::vector<int4>& bent4, const HalfLists& hl) {
   const int64_t n = d->n;
   using EntT = typename EntOf<F>::type;
-  F *W0, *W1, *fbuf, *Rp, *Rb, *Gring, *fring, *bG, *bR;
+  F *W0, *W1, *G, *fbuf, *Rp, *Rb;
   EntT *ent, *ent1;
   for (int pass = 0; pass < 2; ++pass) {
     Arena& A = d->arena;
@@ -1929,6 +1479,7 @@ int alloc_and_upload(xg_ctx* c, RieCGDev* d, const double* coord, const double* 
     A.plan(d->bidx, n);
     A.plan(W0, n * 8);
     A.plan(W1, n * 8);
+    A.plan(G, n * 16);
     A.plan(d->soff, soff.size());
     A.plan(d->swidth, swidth.size());
     A.plan(ent, nbr.size());
@@ -1947,18 +1498,6 @@ int alloc_and_upload(xg_ctx* c, RieCGDev* d, const double* coord, const double* 
     A.plan(d->bcof, std::max<int64_t>(1, d->nbn));
     A.plan(d->bnode, std::max<int64_t>(1, d->nbn));
     A.plan(Rb, std::max<int64_t>(1, d->nbn) * 5);
-    A.plan(d->posr, fp.posr.size());
-    A.plan(d->dsoff, fp.dsoff.size());
-    A.plan(d->odeg, n);
-    A.plan(d->tmaxref, fp.ntiles);
-    A.plan(d->tminown, fp.ntiles);
-    A.plan(Gring, fp.rg_nodes * 16);
-    A.plan(fring, int64_t(fp.rf) * fp.smax * 5);
-    A.plan(bG, std::max<int64_t>(1, d->nbn) * 16);
-    A.plan(bR, std::max<int64_t>(1, d->nbn) * 8);
-    A.plan(d->gdone, fp.ntiles);
-    A.plan(d->fdone, fp.ntiles);
-    A.plan(d->cdone, fp.ntiles);
     A.plan(d->scal, 1);
     if (pass == 0) XG_CUDA(c, A.reserve());
   }
@@ -1976,15 +1515,7 @@ int alloc_and_upload(xg_ctx* c, RieCGDev* d, const double* coord, const double* 
   }
   d->W[0] = W0;
   d->W[1] = W1;
-  d->Gring = Gring;
-  d->fring = fring;
-  d->bG = bG;
-  d->bR = bR;
-  d->ntiles = fp.ntiles;
-  d->lag = fp.lag;
-  d->rg_mask = static_cast<int32_t>(fp.rg_nodes - 1);
-  d->rf = fp.rf;
-  d->smax = fp.smax;
+  d->G = G;
   d->ent = ent;
   d->ent1 = ent1;
   d->fbuf = fbuf;
@@ -2064,14 +1595,7 @@ int alloc_and_upload(xg_ctx* c, RieCGDev* d, const double* coord, const double* 
   XG_CUDA(c, cudaMemsetAsync(d->bcof, 0xff, std::max<int64_t>(1, d->nbn) * 4, s));  // -1
   XG_CUDA(c, cudaMemsetAsync(d->U, 0, n * 5 * sizeof(double), s));
   XG_CUDA(c, cudaMemsetAsync(d->Un, 0, n * 5 * sizeof(double), s));
-  XG_CUDA(c, up(d->posr, fp.posr.data(), fp.posr.size() * 4));
-  XG_CUDA(c, up(d->dsoff, fp.dsoff.data(), fp.dsoff.size() * 4));
-  XG_CUDA(c, up(d->odeg, fp.odeg.data(), fp.odeg.size() * 2));
-  XG_CUDA(c, up(d->tmaxref, fp.tmaxref.data(), fp.tmaxref.size() * 4));
-  XG_CUDA(c, up(d->tminown, fp.tminown.data(), fp.tminown.size() * 4));
-  XG_CUDA(c, cudaMemsetAsync(d->gdone, 0, fp.ntiles * 4, s));
-  XG_CUDA(c, cudaMemsetAsync(d->fdone, 0, fp.ntiles * 4, s));
-  XG_CUDA(c, cudaMemsetAsync(d->cdone, 0, fp.ntiles * 4, s));
+  XG_CUDA(c, cudaMemsetAsync(G, 0, n * 16 * sizeof(F), s));
   {
     // W records: zero primitives, coordinates in slots 5..7
     std::vector<F> w(n * 8, F(0));
@@ -2084,7 +1608,7 @@ int alloc_and_upload(xg_ctx* c, RieCGDev* d, const double* coord, const double* 
     XG_CUDA(c, cudaMemcpy(W1, w.data(), w.size() * sizeof(F), cudaMemcpyHostToDevice));
     XG_CUDA(c, cudaMemcpy(d->stage_W, w.data(), w.size() * sizeof(F), cudaMemcpyHostToDevice));
   }
-  Scalars s0{};
+  Scalars s0{0.0, 0ull, 0, 0};
   double big = DBL_MAX;
   std::memcpy(&s0.dtmin, &big, sizeof(double));
   XG_CUDA(c, cudaMemcpy(d->scal, &s0, sizeof(s0), cudaMemcpyHostToDevice));
@@ -2171,11 +1695,9 @@ int xg_riecg_setup(xg_ctx* c, const xg_riecg_params* prm, int64_t npoin, const d
       ent[fill[E[k].b]++] = {E[k].a, int64_t(k), false};
     }
   }
-  // each node's entries by decreasing neighbour id: the edges the node owns
-  // (other end larger) come first, so the flux pass reads a prefix
   for (int64_t p = 0; p < n; ++p)
     std::sort(ent.begin() + start[p], ent.begin() + start[p + 1],
-              [](const Ent& x, const Ent& y) { return x.q > y.q || (x.q == y.q && x.eid < y.eid); });
+              [](const Ent& x, const Ent& y) { return x.q < y.q || (x.q == y.q && x.eid < y.eid); });
   // SELL-32 slices
   const int64_t nslice = (n + kSlice - 1) / kSlice;
   std::vector<int32_t> soff(nslice + 1), swidth(nslice);
@@ -2192,7 +1714,6 @@ int xg_riecg_setup(xg_ctx* c, const xg_riecg_params* prm, int64_t npoin, const d
   soff[nslice] = static_cast<int32_t>(total);
   std::vector<int32_t> nbr(static_cast<size_t>(total), kPad);
   std::vector<double> ddx(nbr.size(), 0.0), ddy(nbr.size(), 0.0), ddz(nbr.size(), 0.0);
-  std::vector<int32_t> at_a(E.size()), at_b(E.size());  // entry index of each edge at each end
   for (int64_t p = 0; p < n; ++p) {
     const int64_t s = p / kSlice, lane = p % kSlice;
     for (int64_t k = 0; k < start[p + 1] - start[p]; ++k) {
@@ -2202,89 +1723,6 @@ int xg_riecg_setup(xg_ctx* c, const xg_riecg_params* prm, int64_t npoin, const d
       ddx[idx] = E[en.eid].d[0];
       ddy[idx] = E[en.eid].d[1];
       ddz[idx] = E[en.eid].d[2];
-      (en.first ? at_a : at_b)[en.eid] = static_cast<int32_t>(idx);
-    }
-  }
-  // fused-stage tiles: the reach of each tile's owned edges and of the
-  // owners depositing into it, the lag between a tile's gradient and flux
-  // phases, ring sizes and, per owned entry, its deposit slot in the ring
-  FusedPlan fp;
-  {
-    const int64_t nt = (n + kTile - 1) / kTile;
-    fp.ntiles = static_cast<int32_t>(nt);
-    fp.tmaxref.resize(nt);
-    fp.tminown.resize(nt);
-    for (int64_t t = 0; t < nt; ++t) fp.tmaxref[t] = fp.tminown[t] = static_cast<int32_t>(t);
-    fp.odeg.assign(n, 0);
-    for (int64_t p = 0; p < n; ++p) {
-      const int64_t dg = start[p + 1] - start[p];
-      int64_t own = 0;
-      for (int64_t k = 0; k < dg; ++k) own += ent[start[p] + k].q > p ? 1 : 0;
-      if (dg > 255) return fail(c, XG_ERR_ARG, "riecg_setup: node degree above 255");
-      fp.odeg[p] = static_cast<uint16_t>(own | (dg << 8));
-    }
-    for (auto& e : E) {
-      const int64_t lo = std::min(e.a, e.b), hi = std::max(e.a, e.b);
-      const int32_t tl = static_cast<int32_t>(lo / kTile), th = static_cast<int32_t>(hi / kTile);
-      fp.tmaxref[tl] = std::max(fp.tmaxref[tl], th);
-      fp.tminown[th] = std::min(fp.tminown[th], tl);
-    }
-    int32_t reach = 0;
-    for (int64_t t = 0; t < nt; ++t)
-      reach = std::max({reach, fp.tmaxref[t] - static_cast<int32_t>(t),
-                        static_cast<int32_t>(t) - fp.tminown[t]});
-    auto pow2 = [](int64_t x) {
-      int64_t r = 1;
-      while (r < x) r <<= 1;
-      return r;
-    };
-    // Rings: a slot is rewritten only after the blocks that read its last
-    // contents are done, so a ring shorter than the window of blocks
-    // resident at once (plus the lag) makes new blocks wait for old ones.
-    // The window comes from the occupancy of the kernel on this device.
-    int nsm = 0, per_sm = 0;
-    XG_CUDA(c, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
-    if (prm->precision == XG_FP32_FLUX)
-      XG_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                     &per_sm, k_stage<float, XG_RUSANOV, 0, true>, kTile, 0));
-    else
-      XG_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                     &per_sm, k_stage<double, XG_RUSANOV, 0, true>, kTile, 0));
-    const int64_t window = int64_t(std::max(nsm, 1)) * std::max(per_sm, 1);
-    fp.lag = 2 * reach + 2;
-    const int64_t rg = std::min<int64_t>(pow2(fp.lag + window + 32), pow2(nt));
-    fp.rg_nodes = rg * kTile;
-    fp.rf = static_cast<int32_t>(std::min<int64_t>(reach + window + 32, nt));
-    // deposit slots: per node its entries own..deg-1 (the edges its lower
-    // neighbours own), SELL-32 over slices of their own width
-    constexpr int64_t spt = kTile / kSlice;  // slices per tile
-    fp.dsoff.assign(nslice + 1, 0);
-    for (int64_t s2 = 0; s2 < nslice; ++s2) {
-      int64_t w2 = 0;
-      for (int64_t p = s2 * kSlice; p < std::min(n, (s2 + 1) * kSlice); ++p)
-        w2 = std::max<int64_t>(w2, (fp.odeg[p] >> 8) - (fp.odeg[p] & 0xff));
-      if (fp.dsoff[s2] + w2 * kSlice >= (int64_t(1) << 31))
-        return fail(c, XG_ERR_ARG, "adjacency too large");
-      fp.dsoff[s2 + 1] = static_cast<int32_t>(fp.dsoff[s2] + w2 * kSlice);
-    }
-    int64_t smax = 0;
-    for (int64_t t = 0; t < nt; ++t)
-      smax = std::max<int64_t>(smax, fp.dsoff[std::min(nslice, (t + 1) * spt)] - fp.dsoff[t * spt]);
-    fp.smax = static_cast<int32_t>(std::max<int64_t>(smax, 1));
-    if (int64_t(fp.rf) * fp.smax >= (int64_t(1) << 31))
-      return fail(c, XG_ERR_ARG, "riecg_setup: deposit ring too large");
-    fp.posr.assign(nbr.size(), 0);
-    for (size_t k = 0; k < E.size(); ++k) {
-      const bool a_owns = E[k].a < E[k].b;
-      const int64_t oth = a_owns ? E[k].b : E[k].a;
-      const int32_t own_idx = a_owns ? at_a[k] : at_b[k];
-      const int32_t oth_idx = a_owns ? at_b[k] : at_a[k];
-      const int64_t tq = oth / kTile, sq = oth / kSlice, lq = oth % kSlice;
-      const int64_t kq = (oth_idx - soff[sq] - lq) / kSlice;  // entry position in oth's row
-      const int64_t j = kq - (fp.odeg[oth] & 0xff);           // among its deposit slots
-      fp.posr[own_idx] = static_cast<int32_t>((tq % fp.rf) * fp.smax +
-                                              (fp.dsoff[sq] - fp.dsoff[tq * spt]) +
-                                              j * kSlice + lq);
     }
   }
   // half-edge lists: every edge is owned by its end with the smaller local
@@ -2364,9 +1802,9 @@ int xg_riecg_setup(xg_ctx* c, const xg_riecg_params* prm, int64_t npoin, const d
     }
   }
   // boundary triangles: per boundary node, the (tri, position) pairs
-  // boundary nodes are indexed in node order
   std::vector<int32_t> bidx(n, -1), btri(nbtri * 3);
   std::vector<uint8_t> bsym(nbtri * 3);
+  std::vector<int64_t> bcount;
   int64_t nbn = 0;
   for (int64_t t = 0; t < nbtri; ++t)
     for (int a = 0; a < 3; ++a) {
@@ -2374,12 +1812,12 @@ int xg_riecg_setup(xg_ctx* c, const xg_riecg_params* prm, int64_t npoin, const d
       if (bad(p)) return fail(c, XG_ERR_ARG, "triinpoel id");
       btri[t * 3 + a] = static_cast<int32_t>(p);
       bsym[t * 3 + a] = besym[t * 3 + a] ? 1 : 0;
-      bidx[p] = 0;
+      if (bidx[p] < 0) {
+        bidx[p] = static_cast<int32_t>(nbn++);
+        bcount.push_back(0);
+      }
+      ++bcount[bidx[p]];
     }
-  for (int64_t p = 0; p < n; ++p)
-    if (bidx[p] == 0) bidx[p] = static_cast<int32_t>(nbn++);
-  std::vector<int64_t> bcount(nbn, 0);
-  for (int64_t t = 0; t < nbtri * 3; ++t) ++bcount[bidx[btri[t]]];
   std::vector<int32_t> bptr(nbn + 1, 0);
   std::vector<int4> bent4(nbtri * 3);
   for (int64_t i = 0; i < nbn; ++i) bptr[i + 1] = bptr[i] + static_cast<int32_t>(bcount[i]);
@@ -2411,10 +1849,10 @@ int xg_riecg_setup(xg_ctx* c, const xg_riecg_params* prm, int64_t npoin, const d
   d->nbent = nbtri * 3;
   if (d->fp32)
     rc = alloc_and_upload<float>(c, d, coord, vol, soff, swidth, nbr, ddx, ddy, ddz, bidx, bptr,
-                                 bent4, hl, fp);
+                                 bent4, hl);
   else
     rc = alloc_and_upload<double>(c, d, coord, vol, soff, swidth, nbr, ddx, ddy, ddz, bidx, bptr,
-                                  bent4, hl, fp);
+                                  bent4, hl);
   if (rc) {
     destroy_riecg(d);
     c->riecg = nullptr;
@@ -2603,7 +2041,7 @@ int rhs_dropin(xg_ctx* c, RieCGDev* d, const double* G, const double* U, double*
                              c->stream));
   k_prim_aos<F><<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(d->n, d->stage_buf, W, W);
   XG_CHECK_LAUNCH(c);
-  int rc = launch_rhs<F>(c, d, 0, false, W, Gr, nullptr, d->stage_buf);
+  int rc = launch_rhs<F>(c, d, 0, false, false, W, Gr, nullptr, d->stage_buf);
   if (rc) return rc;
   XG_CUDA(c, cudaMemcpyAsync(R, d->stage_buf, d->n * 5 * sizeof(double), cudaMemcpyDeviceToHost,
                              c->stream));
@@ -2687,10 +2125,8 @@ int xg_riecg_stage(xg_ctx* c, int stage, double dt) {
   d->dt_valid = stage == 2;
   rc = flush_profile(c, d);
   if (rc) return rc;
-  Scalars sc;
-  XG_CUDA(c, cudaMemcpyAsync(&sc, d->scal, sizeof(sc), cudaMemcpyDeviceToHost, c->stream));
   XG_CUDA(c, cudaStreamSynchronize(c->stream));
-  return stage_status(c, sc);
+  return XG_OK;
 }
 
 int xg_riecg_run(xg_ctx* c, int64_t nstep, double* dts, float* ms) {
@@ -2792,8 +2228,6 @@ int xg_riecg_run(xg_ctx* c, int64_t nstep, double* dts, float* ms) {
   d->dt_valid = true;
   Scalars s;
   XG_CUDA(c, cudaMemcpy(&s, d->scal, sizeof(s), cudaMemcpyDeviceToHost));
-  rc = stage_status(c, s);
-  if (rc) return rc;
   if (s.blowup) return fail(c, XG_ERR_BLOWUP, "dt below machine epsilon");
   return XG_OK;
 }
