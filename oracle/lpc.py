@@ -215,3 +215,15 @@ def loss_grad(theta, g):
     grads["W0"] = cache["x"].T @ du
     grads["b0"] = du.sum(0)
     return loss, flatten(grads), nval
+
+
+def adam(theta, grad, m, v, step, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
+    """One Adam step (Kingma and Ba, "Adam: A Method for Stochastic
+    Optimization", ICLR 2015, Algorithm 1) in FP64: the first and second
+    moment estimates, their bias corrections 1 - beta^step, and
+    theta -= lr * m_hat / (sqrt(v_hat) + eps).  Returns (theta, m, v)."""
+    m = beta1 * m + (1.0 - beta1) * grad
+    v = beta2 * v + (1.0 - beta2) * grad * grad
+    mh = m / (1.0 - beta1 ** step)
+    vh = v / (1.0 - beta2 ** step)
+    return theta - lr * mh / (np.sqrt(vh) + eps), m, v

@@ -112,6 +112,59 @@ def test_network_gradient_matches_oracle():
     model.close()
 
 
+def test_network_gradient_tensor_cores_matches_oracle():
+    """The BF16 path: forward layers, the backward data products dY W^T and
+    the weight gradients X^T dY on the 5th-generation tensor cores
+    (tcgen05.mma, BF16 operands, FP32 accumulation in TMEM).  Against the
+    FP64 oracle: loss within 1e-2 relative; every parameter group's
+    gradient within 3e-2 of the largest oracle gradient entry (BF16 rounds
+    each operand to 8 significant bits); the whole gradient vector's cosine
+    similarity above 0.999; the second call doubles the gradient bit for
+    bit (fixed-order partials)."""
+    S = _system(n=13, seed=8)
+    s = _cg(S, "jacobi")
+    theta = _random_params(9)
+    model = lpc.LearnedPreconditioner(ctx(), precision="bf16", params=theta)
+    model.zero_grads()
+    loss = model.grad(s)
+    gg = model.grads().astype(np.float64)
+    g = olpc.Graph(S["ia"], S["ja"], S["a2"], S["mask"])
+    lo, go, _ = olpc.loss_grad(theta.astype(np.float64), g)
+    assert abs(loss - lo) < 1e-2 * abs(lo)
+    scale = np.abs(go).max()
+    k = 0
+    for name, shp in olpc.SHAPES:
+        m = int(np.prod(shp))
+        assert np.abs(gg[k:k + m] - go[k:k + m]).max() <= 3e-2 * scale, name
+        k += m
+    cos = gg @ go / (np.linalg.norm(gg) * np.linalg.norm(go))
+    assert cos > 0.999, cos
+    model.grad(s)
+    assert np.array_equal(model.grads().astype(np.float64), 2 * gg)
+    model.close()
+
+
+def test_adam_matches_oracle():
+    """Two device Adam steps against the oracle's FP64 Adam (Kingma and Ba,
+    Algorithm 1) on the same gradient: parameters within FP32 rounding."""
+    S = _system(n=7, seed=8)
+    s = _cg(S, "jacobi")
+    theta = _random_params(11)
+    model = lpc.LearnedPreconditioner(ctx(), precision="fp32", params=theta)
+    t = theta.astype(np.float64)
+    m = np.zeros_like(t)
+    v = np.zeros_like(t)
+    for step in (1, 2):
+        model.zero_grads()
+        model.grad(s)
+        grad = model.grads().astype(np.float64)
+        model.adam(lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8)
+        t, m, v = olpc.adam(t, grad, m, v, step, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8)
+        got = model.params().astype(np.float64)
+        assert np.abs(got - t).max() <= 1e-6 * np.abs(t).max() + 2e-6
+    model.close()
+
+
 def test_training_lowers_loss_and_beats_first_order():
     c = ctx()
     train = [lpc.training_system(c, lpc.pressure_system(c, n, seed))

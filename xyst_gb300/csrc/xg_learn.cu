@@ -15,10 +15,12 @@
 //   [a|b] = h3 Wo
 //   o_ij = w . relu(a_i + b_j + c e_ij + d) + ob          every lower edge i > j
 //   N_ij = e_ij (1 + tanh o_ij)
-// The dense layers run as BF16 tensor-core GEMMs with FP32 accumulation
-// (precision 1) or in FP32 (precision 0); the backward pass is FP32 and
-// every reduction over nodes or edges goes through fixed-order block
-// partials, so a gradient is bit-reproducible.
+// The dense layers -- forward, the backward data products dY W^T and the
+// weight gradients X^T dY -- run as BF16 GEMMs with FP32 accumulation on the
+// 5th-generation tensor cores (tcgen05.mma, accumulators in TMEM; precision
+// 1), or in FP32 on the CUDA cores (precision 0, the reference the tensor-core
+// path is tested against).  Every reduction over nodes or edges goes
+// through fixed-order block partials, so a gradient is bit-reproducible.
 //
 // Loss: Kaporin's trace functional of the factorised approximate inverse.
 // With unit-diagonal L = I + N, det(L^T A^ L) = det(A^) is fixed (A^ = I - E),
@@ -66,9 +68,6 @@ constexpr int64_t kNParams = oob + 1;
 constexpr int64_t kLayerW[3] = {oW1, oW2, oW3};
 constexpr int64_t kLayerB[3] = {ob1, ob2, ob3};
 
-// BF16 B-fragment images of the tensor-core layers: W1..W3 (K 128, N 64) and
-// Wo (K 64, N 128); K * N / 2 32-bit words each.
-constexpr int64_t kFragWords = 2 * H * H / 2;
 
 // ---------------------------------------------------------------- helpers
 
@@ -80,12 +79,6 @@ __device__ __forceinline__ float warp_sum(float v) {
   return v;
 }
 
-__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
-  __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
-  uint32_t u;
-  memcpy(&u, &v, 4);
-  return u;
-}
 
 // Fixed-order block sum of one double per thread; thread 0 gets the total.
 __device__ double block_sum(double v) {
@@ -235,85 +228,340 @@ __global__ void __launch_bounds__(kThreads) k_dense_f32(int64_t n, const float* 
   }
 }
 
-// BF16 tensor-core version of the forward layers (mma.sync m16n8k16, FP32
-// accumulation): each warp owns 16-row tiles, its A fragments come straight
-// from the FP32 activations (one 32-byte sector per row and k-step), the
-// B fragments from a shared-memory copy of the packed weight image.
-template <int K, int N>
-__global__ void __launch_bounds__(kThreads) k_dense_tc(int64_t n, const float* __restrict__ X1,
-                                                       const float* __restrict__ X2,
-                                                       const uint32_t* __restrict__ wfrag,
-                                                       const float* __restrict__ bias, int act,
-                                                       float* __restrict__ Y1,
-                                                       float* __restrict__ Y2) {
-  constexpr int KS = K / 16, NT = N / 8;
-  __shared__ uint2 Bs[KS * NT * 32];
-  for (int t = threadIdx.x; t < KS * NT * 32; t += kThreads)
-    Bs[t] = reinterpret_cast<const uint2*>(wfrag)[t];
-  __syncthreads();
-  const int lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
-  const int64_t ntile = (n + 15) / 16;
-  const int64_t wstride = int64_t(gridDim.x) * (kThreads / 32);
-  for (int64_t tile = blockIdx.x * int64_t(kThreads / 32) + (threadIdx.x >> 5); tile < ntile;
-       tile += wstride) {
-    const int64_t ra = tile * 16 + g, rb = ra + 8;
-    float acc[NT][4];
-#pragma unroll
-    for (int nt = 0; nt < NT; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
-#pragma unroll
-    for (int ks = 0; ks < KS; ++ks) {
-      const float* X = (ks * 16 < H) ? X1 : X2;
-      const int c0 = (ks * 16) % H + 2 * tq;
-      float2 v00 = make_float2(0.f, 0.f), v10 = v00, v01 = v00, v11 = v00;
-      if (ra < n) {
-        v00 = __ldg(reinterpret_cast<const float2*>(X + ra * H + c0));
-        v01 = __ldg(reinterpret_cast<const float2*>(X + ra * H + c0 + 8));
-      }
-      if (rb < n) {
-        v10 = __ldg(reinterpret_cast<const float2*>(X + rb * H + c0));
-        v11 = __ldg(reinterpret_cast<const float2*>(X + rb * H + c0 + 8));
-      }
-      const uint32_t a0 = pack_bf16(v00.x, v00.y), a1 = pack_bf16(v10.x, v10.y);
-      const uint32_t a2 = pack_bf16(v01.x, v01.y), a3 = pack_bf16(v11.x, v11.y);
-#pragma unroll
-      for (int nt = 0; nt < NT; ++nt) {
-        const uint2 b = Bs[(ks * NT + nt) * 32 + lane];
-        asm volatile(
-            "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
-            "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
-            : "+f"(acc[nt][0]), "+f"(acc[nt][1]), "+f"(acc[nt][2]), "+f"(acc[nt][3])
-            : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b.x), "r"(b.y));
-      }
-    }
-#pragma unroll
-    for (int nt = 0; nt < NT; ++nt) {
-      const int cc = nt * 8 + 2 * tq;
-      const float b0 = bias ? bias[cc] : 0.f, b1 = bias ? bias[cc + 1] : 0.f;
-      float2 ya = make_float2(acc[nt][0] + b0, acc[nt][1] + b1);
-      float2 yb = make_float2(acc[nt][2] + b0, acc[nt][3] + b1);
-      if (act) {
-        ya.x = relu(ya.x), ya.y = relu(ya.y), yb.x = relu(yb.x), yb.y = relu(yb.y);
-      }
-      float* Y = cc < H ? Y1 : Y2;
-      const int cy = cc % H;
-      if (ra < n) *reinterpret_cast<float2*>(Y + ra * H + cy) = ya;
-      if (rb < n) *reinterpret_cast<float2*>(Y + rb * H + cy) = yb;
-    }
-  }
+// ---------------------------------------------------------------- tcgen05 (5th-gen tensor cores)
+//
+// BF16 GEMMs on sm_103a tensor cores: operands in shared memory, the FP32
+// accumulator in tensor memory (TMEM).  One thread of the CTA issues
+// tcgen05.mma; its completion arrives on an mbarrier (tcgen05.commit); the
+// epilogue reads the accumulator back with tcgen05.ld.  Operand layout: the
+// canonical K-major layout without swizzle -- 8 x 8 BF16 "core matrices"
+// (8 rows of 16 contiguous bytes, 128 bytes each), adjacent core matrices
+// along K kLbo bytes apart and along M (or N) sbo = K * 16 bytes apart.
+// The element (row r, k) of an R x K operand therefore sits at byte
+//   (r / 8) * (K * 16) + (k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2.
+// Every wait on the mbarrier is bounded: after kUmmaSpin polls the CTA
+// records an error status, frees its TMEM and returns.
+
+constexpr int kUmmaThreads = 128;  // one thread per accumulator row (TMEM lane)
+constexpr int kUmmaM = 128;        // rows per MMA tile
+constexpr uint32_t kLbo = 128;     // bytes between core matrices along K
+constexpr int kUmmaSpin = 1 << 20;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
-// Packed BF16 B fragments of a K x N row-major FP32 weight: word pair
-// ((ks * N/8 + nt) * 32 + lane) holds W[k0..k0+1][col] and W[k0+8..k0+9][col]
-// with col = nt * 8 + lane / 4, k0 = ks * 16 + 2 (lane % 4).
-__global__ void k_pack_frag(const float* __restrict__ W, int K, int N, uint32_t* __restrict__ out) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int NT = N / 8;
-  if (t >= (K / 16) * NT * 32) return;
-  const int lane = t & 31, blk = t >> 5;
-  const int ks = blk / NT, nt = blk % NT;
-  const int colw = nt * 8 + (lane >> 2), k0 = ks * 16 + 2 * (lane & 3);
-  out[2 * t + 0] = pack_bf16(W[k0 * N + colw], W[(k0 + 1) * N + colw]);
-  out[2 * t + 1] = pack_bf16(W[(k0 + 8) * N + colw], W[(k0 + 9) * N + colw]);
+// byte offset of element (r, k) in an R x K K-major core-matrix operand
+__device__ __forceinline__ uint32_t umma_off(int r, int k, int K) {
+  return uint32_t((r >> 3) * (K * 16) + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+// Shared-memory matrix descriptor (no swizzle): start address, LBO and SBO
+// in 16-byte units, descriptor version 1.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= uint64_t((saddr >> 4) & 0x3FFF);
+  d |= uint64_t((lbo >> 4) & 0x3FFF) << 16;
+  d |= uint64_t((sbo >> 4) & 0x3FFF) << 32;
+  d |= uint64_t(1) << 46;  // version
+  return d;                // base offset 0, layout type 0 (no swizzle)
+}
+
+// Instruction descriptor of kind::f16: BF16 A and B (K-major), FP32 D, M x N.
+__host__ __device__ constexpr uint32_t umma_idesc_bf16(int M, int N) {
+  return (1u << 4)       // D format FP32
+         | (1u << 7)     // A format BF16
+         | (1u << 10)    // B format BF16
+         | (uint32_t(N >> 3) << 17) | (uint32_t(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc,
+                                          uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t* mbar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(mbar))
+      : "memory");
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* mbar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mbar)), "r"(count)
+               : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Bounded wait for the mbarrier phase with the given parity; false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity) {
+  const uint32_t a = smem_u32(mbar);
+  for (int it = 0; it < kUmmaSpin; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst_smem, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                   smem_u32(dst_smem)),
+               "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_free(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+// generic-proxy shared-memory writes made visible to the tensor cores
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// 32 consecutive FP32 accumulator columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float v[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+      "%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ uint16_t bf16_bits(float f) {
+  return __bfloat16_as_ushort(__float2bfloat16_rn(f));
+}
+
+// Y = act([X1 | X2] Bt^T + bias) (o [maskY > 0]) on the tensor cores, for
+// rows 0..n-1: X1, X2 n x 64 FP32 (X2 null: KIN = 64); Bt NOUT x KIN
+// (FROM_W: built from a KIN x NOUT row-major weight W, Bt[o][k] = W[k][o] --
+// the forward layer; otherwise Bt = W, NOUT x KIN row-major -- dX = dY W^T
+// of the backward pass); Y split into Y1 (columns 0..63) and Y2 (64..127).
+// Operands are rounded to BF16, products accumulated in FP32.  Each CTA
+// takes 128-row tiles in turn; one TMEM accumulator of NOUT columns.
+template <int KIN, int NOUT, bool FROM_W>
+__global__ void __launch_bounds__(kUmmaThreads, 1)
+    k_dense_umma(int64_t n, const float* __restrict__ X1, const float* __restrict__ X2,
+                 const float* __restrict__ W, const float* __restrict__ bias, int act,
+                 const float* __restrict__ maskY, float* __restrict__ Y1, float* __restrict__ Y2,
+                 int32_t* __restrict__ err) {
+  static_assert(KIN % 16 == 0 && NOUT % 32 == 0 && NOUT >= 32 && NOUT <= 256, "UMMA shape");
+  extern __shared__ __align__(1024) uint8_t umma_smem[];
+  uint8_t* sA = umma_smem;                     // kUmmaM x KIN BF16
+  uint8_t* sB = umma_smem + kUmmaM * KIN * 2;  // NOUT x KIN BF16
+  __shared__ uint64_t mbar;
+  __shared__ uint32_t taddr_s;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  // the weight operand, once per CTA
+  for (int t = tid; t < NOUT * KIN; t += kUmmaThreads) {
+    const int o = t / KIN, k = t % KIN;
+    const float v = FROM_W ? W[k * NOUT + o] : W[o * KIN + k];
+    *reinterpret_cast<uint16_t*>(sB + umma_off(o, k, KIN)) = bf16_bits(v);
+  }
+  if (tid == 0) mbar_init(&mbar, 1);
+  if (warp == 0) tmem_alloc(&taddr_s, NOUT);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = taddr_s;
+  constexpr uint32_t idesc = umma_idesc_bf16(kUmmaM, NOUT);
+  const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+  const int64_t ntile = (n + kUmmaM - 1) / kUmmaM;
+  uint32_t phase = 0;
+  bool ok = true;
+  for (int64_t tile = blockIdx.x; tile < ntile && ok; tile += gridDim.x) {
+    // A tile: row tid of the tile, KIN values rounded to BF16, 16 bytes at a time
+    const int64_t i = tile * kUmmaM + tid;
+#pragma unroll
+    for (int k0 = 0; k0 < KIN; k0 += 8) {
+      const float* X = k0 < H ? X1 : X2;
+      const int c = k0 % H;
+      float v[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      if (i < n) {
+        const float4 lo = __ldg(reinterpret_cast<const float4*>(X + i * H + c));
+        const float4 hi = __ldg(reinterpret_cast<const float4*>(X + i * H + c + 4));
+        v[0] = lo.x, v[1] = lo.y, v[2] = lo.z, v[3] = lo.w;
+        v[4] = hi.x, v[5] = hi.y, v[6] = hi.z, v[7] = hi.w;
+      }
+      uint4 pk;
+      pk.x = uint32_t(bf16_bits(v[0])) | (uint32_t(bf16_bits(v[1])) << 16);
+      pk.y = uint32_t(bf16_bits(v[2])) | (uint32_t(bf16_bits(v[3])) << 16);
+      pk.z = uint32_t(bf16_bits(v[4])) | (uint32_t(bf16_bits(v[5])) << 16);
+      pk.w = uint32_t(bf16_bits(v[6])) | (uint32_t(bf16_bits(v[7])) << 16);
+      *reinterpret_cast<uint4*>(sA + umma_off(tid, k0, KIN)) = pk;
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (tid == 0) {
+#pragma unroll
+      for (int ks = 0; ks < KIN / 16; ++ks)
+        umma_bf16(tmem, umma_desc(a0 + ks * 2 * kLbo, kLbo, KIN * 16),
+                  umma_desc(b0 + ks * 2 * kLbo, kLbo, KIN * 16), idesc, ks > 0 ? 1u : 0u);
+      umma_commit(&mbar);
+    }
+    ok = mbar_wait(&mbar, phase);
+    phase ^= 1;
+    ok = __syncthreads_and(ok) != 0;  // block-uniform before the warp-collective TMEM reads
+    tc_fence_after();
+    if (ok) {
+      // accumulator row tid (TMEM lane 32 warp + lane): NOUT columns
+#pragma unroll
+      for (int c0 = 0; c0 < NOUT; c0 += 32) {
+        float v[32];
+        tmem_ld32(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c0), v);
+        if (i < n) {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const int o = c0 + j;
+            float y = v[j] + (bias ? bias[o] : 0.f);
+            if (act) y = relu(y);
+            if (maskY && !(maskY[i * NOUT + o] > 0.f)) y = 0.f;
+            v[j] = y;
+          }
+          float* Y = c0 < H ? Y1 : Y2;
+          float* dst = Y + i * H + (c0 % H);
+#pragma unroll
+          for (int j = 0; j < 32; j += 4)
+            *reinterpret_cast<float4*>(dst + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+        }
+      }
+    }
+    // every lane's reads of this accumulator and of the A tile are done
+    // before the next tile's MMAs overwrite them
+    tc_fence_before();
+    ok = __syncthreads_and(ok) != 0;
+    tc_fence_after();
+  }
+  if (!ok) {
+    // a timed-out wait: give the MMAs in flight one more bounded wait before
+    // the accumulator is freed
+    mbar_wait(&mbar, phase ^ 1);
+    if (tid == 0) atomicCAS(err, 0, 1);
+  }
+  __syncthreads();
+  if (warp == 0) tmem_free(tmem, NOUT);
+}
+
+// Per-CTA partials of dW = X^T dY (KIN x NOUT, KIN = 64 or 128 from X1 | X2)
+// on the tensor cores and, with BIAS, db = sum dY (FP32 on the CUDA cores):
+// the CTA accumulates its 128-row tiles in TMEM (rows as the reduction
+// dimension: the A operand is X^T -- KIN rows padded to 128, the rows of
+// the tile along K -- and the B operand dY^T) and writes its partial to
+// part[blockIdx.x] (KIN*NOUT weights, then NOUT biases), summed over CTAs
+// in a fixed order afterwards.
+template <int KIN, int NOUT, bool BIAS>
+__global__ void __launch_bounds__(kUmmaThreads, 1)
+    k_wgrad_umma(int64_t n, const float* __restrict__ X1, const float* __restrict__ X2,
+                 const float* __restrict__ dY1, const float* __restrict__ dY2,
+                 float* __restrict__ part, int32_t* __restrict__ err) {
+  static_assert((KIN == 64 || KIN == 128) && NOUT % 32 == 0 && NOUT <= 256, "UMMA shape");
+  constexpr int KR = kUmmaM;  // reduction rows per tile (the MMA's K)
+  extern __shared__ __align__(1024) uint8_t umma_smem[];
+  uint8_t* sA = umma_smem;                    // (X^T) 128 x 128 BF16, rows >= KIN zero
+  uint8_t* sB = umma_smem + kUmmaM * KR * 2;  // (dY^T) NOUT x 128 BF16
+  __shared__ uint64_t mbar;
+  __shared__ uint32_t taddr_s;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  for (int t = tid; t < (kUmmaM - KIN) * KR; t += kUmmaThreads) {
+    const int r = KIN + t / KR, k = t % KR;
+    *reinterpret_cast<uint16_t*>(sA + umma_off(r, k, KR)) = 0;
+  }
+  if (tid == 0) mbar_init(&mbar, 1);
+  if (warp == 0) tmem_alloc(&taddr_s, NOUT);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = taddr_s;
+  constexpr uint32_t idesc = umma_idesc_bf16(kUmmaM, NOUT);
+  const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+  const int64_t ntile = (n + KR - 1) / KR;
+  uint32_t phase = 0, acc = 0;
+  bool ok = true;
+  float dbias = 0.f;  // thread tid < NOUT: column tid of dY summed over this CTA's rows
+  for (int64_t tile = blockIdx.x; tile < ntile && ok; tile += gridDim.x) {
+    // row tid of the tile: its KIN inputs as column tid of A, its NOUT
+    // output gradients as column tid of B
+    const int64_t i = tile * KR + tid;
+    for (int k = 0; k < KIN; ++k) {
+      const float v = i < n ? (k < H ? X1[i * H + k] : X2[i * H + (k - H)]) : 0.f;
+      *reinterpret_cast<uint16_t*>(sA + umma_off(k, tid, KR)) = bf16_bits(v);
+    }
+    for (int o = 0; o < NOUT; ++o) {
+      const float v = i < n ? (o < H ? dY1[i * H + o] : dY2[i * H + (o - H)]) : 0.f;
+      *reinterpret_cast<uint16_t*>(sB + umma_off(o, tid, KR)) = bf16_bits(v);
+    }
+    if (BIAS && tid < NOUT) {
+      for (int r = 0; r < KR; ++r) {
+        const int64_t ir = tile * KR + r;
+        if (ir < n) dbias += tid < H ? dY1[ir * H + tid] : dY2[ir * H + (tid - H)];
+      }
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (tid == 0) {
+#pragma unroll
+      for (int ks = 0; ks < KR / 16; ++ks)
+        umma_bf16(tmem, umma_desc(a0 + ks * 2 * kLbo, kLbo, KR * 16),
+                  umma_desc(b0 + ks * 2 * kLbo, kLbo, KR * 16), idesc, (acc | ks) ? 1u : 0u);
+      umma_commit(&mbar);
+    }
+    acc = 1;
+    // the operand tiles are rewritten only after these MMAs have read them
+    ok = mbar_wait(&mbar, phase);
+    phase ^= 1;
+    tc_fence_after();
+    ok = __syncthreads_and(ok) != 0;
+  }
+  constexpr int NW = KIN * NOUT;
+  float* out = part + int64_t(blockIdx.x) * (NW + (BIAS ? NOUT : 0));
+  if (ok) {
+    // accumulator row tid = input unit tid (< KIN), NOUT columns; a CTA with
+    // no tile writes zeros
+    if (tid < KIN) {  // warp-uniform: KIN is a multiple of 32
+#pragma unroll
+      for (int c0 = 0; c0 < NOUT; c0 += 32) {
+        float v[32];
+        tmem_ld32(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c0), v);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) out[tid * NOUT + c0 + j] = acc ? v[j] : 0.f;
+      }
+    }
+    if (BIAS && tid < NOUT) out[NW + tid] = dbias;
+  } else {
+    // a timed-out wait: one more bounded wait for the MMAs in flight
+    mbar_wait(&mbar, phase ^ 1);
+    if (tid == 0) atomicCAS(err, 0, 1);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tmem_free(tmem, NOUT);
 }
 
 // ---------------------------------------------------------------- weight gradients
@@ -668,8 +916,8 @@ struct xg_lpc {
   int64_t step = 0;
   xg::Arena params;  // theta, grad, Adam moments, BF16 fragments, partials
   float *theta = nullptr, *grad = nullptr, *m1 = nullptr, *m2 = nullptr, *wpart = nullptr;
-  uint32_t* frag = nullptr;  // 4 x kFragWords: W1, W2, W3, Wo
   double* lossv = nullptr;   // [x^.b^, e.g]
+  int32_t* uerr = nullptr;   // nonzero: a tensor-core GEMM's mbarrier wait timed out
   // workspace, sized for the largest graph seen
   xg::Arena work;
   int64_t cap_n = 0, cap_l = 0, cap_u = 0;
@@ -729,16 +977,59 @@ int ensure_work(xg_ctx* c, xg_lpc* m, int64_t n, int64_t nl, int64_t nu) {
   return XG_OK;
 }
 
-int refresh_frag(xg_ctx* c, xg_lpc* m) {
-  cudaStream_t s = c->stream;
-  for (int l = 0; l < 3; ++l) {
-    k_pack_frag<<<(kFragWords / 2 + 255) / 256, 256, 0, s>>>(m->theta + kLayerW[l], 2 * H, H,
-                                                             m->frag + l * kFragWords);
-  }
-  k_pack_frag<<<(kFragWords / 2 + 255) / 256, 256, 0, s>>>(m->theta + oWo, H, 2 * H,
-                                                           m->frag + 3 * kFragWords);
+// The tensor-core GEMMs: dense layer (forward or backward data) and weight
+// gradient partials, on one CTA per SM at most (each holds up to 128 TMEM
+// columns and 64 KB of operand tiles).
+int umma_grid(int64_t n) {
+  static int nsm = [] {
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      v = 1;
+    return v < 1 ? 1 : v;
+  }();
+  return static_cast<int>(std::max<int64_t>(1, std::min<int64_t>((n + kUmmaM - 1) / kUmmaM, nsm)));
+}
+
+template <int KIN, int NOUT, bool FROM_W>
+int dense_umma(xg_ctx* c, xg_lpc* m, int64_t n, const float* X1, const float* X2, const float* W,
+               const float* bias, int act, const float* maskY, float* Y1, float* Y2) {
+  constexpr int smem = (kUmmaM * KIN + NOUT * KIN) * 2;
+  static const cudaError_t attr = cudaFuncSetAttribute(
+      k_dense_umma<KIN, NOUT, FROM_W>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  XG_CUDA(c, attr);
+  k_dense_umma<KIN, NOUT, FROM_W><<<umma_grid(n), kUmmaThreads, smem, c->stream>>>(
+      n, X1, X2, W, bias, act, maskY, Y1, Y2, m->uerr);
   XG_CHECK_LAUNCH(c);
   return XG_OK;
+}
+
+template <int KIN, int NOUT, bool BIAS>
+int wgrad_umma(xg_ctx* c, xg_lpc* m, int64_t n, const float* X1, const float* X2,
+               const float* dY1, const float* dY2, int64_t wofs, int64_t bofs) {
+  constexpr int smem = (kUmmaM * kUmmaM + NOUT * kUmmaM) * 2;
+  constexpr int NW = KIN * NOUT, NOUTP = NW + (BIAS ? NOUT : 0);
+  static const cudaError_t attr = cudaFuncSetAttribute(
+      k_wgrad_umma<KIN, NOUT, BIAS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  XG_CUDA(c, attr);
+  const int grid = umma_grid(n);
+  k_wgrad_umma<KIN, NOUT, BIAS><<<grid, kUmmaThreads, smem, c->stream>>>(n, X1, X2, dY1, dY2,
+                                                                          m->wpart, m->uerr);
+  k_reduce_parts<<<(NOUTP + 255) / 256, 256, 0, c->stream>>>(m->wpart, grid, NOUTP, NW, wofs,
+                                                             bofs, m->grad);
+  XG_CHECK_LAUNCH(c);
+  return XG_OK;
+}
+
+// The tensor-core GEMMs' error word (after a synchronise), reset when set.
+int umma_status(xg_ctx* c, xg_lpc* m) {
+  int32_t e = 0;
+  XG_CUDA(c, cudaMemcpyAsync(&e, m->uerr, sizeof(e), cudaMemcpyDeviceToHost, c->stream));
+  XG_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (!e) return XG_OK;
+  XG_CUDA(c, cudaMemsetAsync(m->uerr, 0, sizeof(e), c->stream));
+  XG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return fail(c, XG_ERR_DEVICE, "tensor-core GEMM: an mbarrier wait timed out");
 }
 
 // Network forward on g up to a and b (m->A, m->B).
@@ -755,23 +1046,26 @@ int forward_nodes(xg_ctx* c, xg_lpc* m, const LpcGraph& g) {
   for (int l = 1; l <= 3; ++l) {
     k_spmm<<<nrb, kThreads, 0, s>>>(n, g.soff, g.sw, g.col, g.eF, m->h[l - 1], nullptr, nullptr,
                                     m->mh[l]);
+    XG_CHECK_LAUNCH(c);
+    int rc = XG_OK;
     if (m->precision == 1)
-      k_dense_tc<2 * H, H><<<ngemm, kThreads, 0, s>>>(n, m->h[l - 1], m->mh[l],
-                                                      m->frag + (l - 1) * kFragWords,
-                                                      m->theta + kLayerB[l - 1], 1, m->h[l],
-                                                      nullptr);
+      rc = dense_umma<2 * H, H, true>(c, m, n, m->h[l - 1], m->mh[l], m->theta + kLayerW[l - 1],
+                                      m->theta + kLayerB[l - 1], 1, nullptr, m->h[l], nullptr);
     else
       k_dense_f32<2 * H, H, false><<<ngemm, kThreads, 0, s>>>(
           n, m->h[l - 1], m->mh[l], m->theta + kLayerW[l - 1], m->theta + kLayerB[l - 1], 1,
           nullptr, m->h[l], nullptr);
+    if (rc) return rc;
     XG_CHECK_LAUNCH(c);
   }
-  if (m->precision == 1)
-    k_dense_tc<H, 2 * H><<<ngemm, kThreads, 0, s>>>(n, m->h[3], nullptr, m->frag + 3 * kFragWords,
-                                                    nullptr, 0, m->A, m->B);
-  else
+  if (m->precision == 1) {
+    int rc = dense_umma<H, 2 * H, true>(c, m, n, m->h[3], nullptr, m->theta + oWo, nullptr, 0,
+                                        nullptr, m->A, m->B);
+    if (rc) return rc;
+  } else {
     k_dense_f32<H, 2 * H, false><<<ngemm, kThreads, 0, s>>>(n, m->h[3], nullptr, m->theta + oWo,
                                                             nullptr, 0, nullptr, m->A, m->B);
+  }
   XG_CHECK_LAUNCH(c);
   return XG_OK;
 }
@@ -812,7 +1106,7 @@ int lpc_factor(xg_ctx* c, xg_lpc* m, const LpcGraph& g, float* nvL, float* nvU) 
       g.n, g.soffL, g.swL, g.colL, g.eL, g.tposU, m->tU, m->A, m->B, edge_params(m->theta), nvL,
       nvU, nullptr);
   XG_CHECK_LAUNCH(c);
-  return XG_OK;
+  return m->precision == 1 ? umma_status(c, m) : XG_OK;
 }
 
 }  // namespace xg
@@ -841,8 +1135,8 @@ int xg_lpc_create(xg_ctx* c, int precision, xg_lpc** out) {
     P.plan(m->grad, kNParams);
     P.plan(m->m1, kNParams);
     P.plan(m->m2, kNParams);
-    P.plan(m->frag, 4 * kFragWords);
     P.plan(m->lossv, 4);
+    P.plan(m->uerr, 1);
     P.plan(m->wpart, int64_t(kWgradBlocks) * (2 * H * 2 * H + 2 * H));
     if (pass == 0 && P.reserve() != cudaSuccess) {
       xg_lpc_destroy(m);
@@ -854,7 +1148,7 @@ int xg_lpc_create(xg_ctx* c, int precision, xg_lpc** out) {
   if (e == cudaSuccess) e = cudaMemsetAsync(m->grad, 0, kNParams * 4, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(m->m1, 0, kNParams * 4, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(m->m2, 0, kNParams * 4, s);
-  if (e == cudaSuccess && refresh_frag(&m->own, m) != XG_OK) e = cudaErrorUnknown;
+  if (e == cudaSuccess) e = cudaMemsetAsync(m->uerr, 0, sizeof(int32_t), s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) {
     xg_lpc_destroy(m);
@@ -886,8 +1180,6 @@ int xg_lpc_set_params(xg_lpc* m, const float* theta) {
   XG_CUDA(c, cudaMemsetAsync(m->m1, 0, kNParams * 4, c->stream));
   XG_CUDA(c, cudaMemsetAsync(m->m2, 0, kNParams * 4, c->stream));
   m->step = 0;
-  rc = refresh_frag(c, m);
-  if (rc) return rc;
   XG_CUDA(c, cudaStreamSynchronize(c->stream));
   return XG_OK;
 }
@@ -962,21 +1254,37 @@ int xg_lpc_grad(xg_lpc* m, xg_ctx* c, double* loss) {
   XG_CHECK_LAUNCH(c);
   // output layer: dWo = h3^T [da | db]; du3 = ([da | db] Wo^T) o [h3 > 0]
   const unsigned ngemm = static_cast<unsigned>(std::min<int64_t>(blocks_for(n, 32), 4 * 148));
-  rc = wgrad<H, 0, 2 * H, false>(c, m, n, m->h[3], nullptr, m->da, m->db, oWo, 0);
+  const bool tc = m->precision == 1;
+  rc = tc ? wgrad_umma<H, 2 * H, false>(c, m, n, m->h[3], nullptr, m->da, m->db, oWo, 0)
+          : wgrad<H, 0, 2 * H, false>(c, m, n, m->h[3], nullptr, m->da, m->db, oWo, 0);
   if (rc) return rc;
-  k_dense_f32<2 * H, H, true><<<ngemm, kThreads, 0, s>>>(n, m->da, m->db, m->theta + oWo, nullptr,
-                                                         0, m->h[3], m->du, nullptr);
+  if (tc) {
+    rc = dense_umma<2 * H, H, false>(c, m, n, m->da, m->db, m->theta + oWo, nullptr, 0, m->h[3],
+                                     m->du, nullptr);
+    if (rc) return rc;
+  } else {
+    k_dense_f32<2 * H, H, true><<<ngemm, kThreads, 0, s>>>(n, m->da, m->db, m->theta + oWo,
+                                                           nullptr, 0, m->h[3], m->du, nullptr);
+  }
   XG_CHECK_LAUNCH(c);
   float* du = m->du;
   float* dnext = m->du2;
   for (int l = 3; l >= 1; --l) {
-    rc = wgrad<H, H, H, true>(c, m, n, m->h[l - 1], m->mh[l], du, nullptr, kLayerW[l - 1],
-                              kLayerB[l - 1]);
+    rc = tc ? wgrad_umma<2 * H, H, true>(c, m, n, m->h[l - 1], m->mh[l], du, nullptr,
+                                         kLayerW[l - 1], kLayerB[l - 1])
+            : wgrad<H, H, H, true>(c, m, n, m->h[l - 1], m->mh[l], du, nullptr, kLayerW[l - 1],
+                                   kLayerB[l - 1]);
     if (rc) return rc;
     // [dih | dim] = du W_l^T
-    k_dense_f32<H, 2 * H, true><<<ngemm, kThreads, 0, s>>>(n, du, nullptr,
-                                                           m->theta + kLayerW[l - 1], nullptr, 0,
-                                                           nullptr, m->dih, m->dim);
+    if (tc) {
+      rc = dense_umma<H, 2 * H, false>(c, m, n, du, nullptr, m->theta + kLayerW[l - 1], nullptr,
+                                       0, nullptr, m->dih, m->dim);
+      if (rc) return rc;
+    } else {
+      k_dense_f32<H, 2 * H, true><<<ngemm, kThreads, 0, s>>>(n, du, nullptr,
+                                                             m->theta + kLayerW[l - 1], nullptr,
+                                                             0, nullptr, m->dih, m->dim);
+    }
     // du_{l-1} = (dih + E dim) o [h_{l-1} > 0]   (E symmetric)
     k_spmm<<<nrb, kThreads, 0, s>>>(n, g.soff, g.sw, g.col, g.eF, m->dim, m->dih, m->h[l - 1],
                                     dnext);
@@ -988,6 +1296,10 @@ int xg_lpc_grad(xg_lpc* m, xg_ctx* c, double* loss) {
   double lv = 0.0;
   XG_CUDA(c, cudaMemcpyAsync(&lv, m->lossv, sizeof(lv), cudaMemcpyDeviceToHost, s));
   XG_CUDA(c, cudaStreamSynchronize(s));
+  if (tc) {
+    rc = umma_status(c, m);
+    if (rc) return rc;
+  }
   if (loss) *loss = lv / double(n);
   return XG_OK;
 }
@@ -1005,8 +1317,6 @@ int xg_lpc_adam(xg_lpc* m, double lr, double beta1, double beta2, double eps) {
                                                           float(beta2), float(eps), float(c1),
                                                           float(c2));
   XG_CHECK_LAUNCH(c);
-  rc = refresh_frag(c, m);
-  if (rc) return rc;
   XG_CUDA(c, cudaStreamSynchronize(c->stream));
   return XG_OK;
 }
