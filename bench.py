@@ -167,6 +167,51 @@ def kernel_bytes(n, nedge, nbtri, fp32):
             "step": 3 * (grad + flux + upd + 2 * bnd) + 128 * n, "own": own}
 
 
+# the learned preconditioner's training corpus (cube size, jitter seed) and
+# its evaluation systems (unseen seeds)
+CORPUS = ([(33, s) for s in range(10, 16)] + [(49, s) for s in range(20, 24)] +
+          [(65, s) for s in range(30, 33)] + [(81, 40), (97, 50)])
+EVAL = [(129, 98), (193, 99)]
+
+
+def lpc_eval(model, n, seed, tol=1e-8):
+    """One ChoCG pressure system (n^3 jittered cube, unseen jitter seed,
+    hydrostat node, smooth right-hand side) solved to tol relative residual
+    by FP64 Jacobi PCG (the reference's algorithm, underflow guard) and by
+    the mixed-precision solve with the first-order and the learned factor:
+    iterations and wall seconds per solve (x0 = 0, device sync included)."""
+    from xyst_gb300 import cg, lib, lpc
+
+    t0 = time.perf_counter()
+    sysd = lpc.chocg_system(None, n, seed, rhs="smooth")
+    ctx = lib.Context(0)
+    s = cg.ConjugateGradients(ctx, sysd["ia"], sysd["ja"], sysd["a"])
+    s.set_guard("underflow")
+    out = {"nodes": int(n ** 3), "jitter_seed": seed, "tol": tol,
+           "setup_s": time.perf_counter() - t0}
+    dirbc = (sysd["dirnodes"], sysd["dirvals"])
+    for name, pc, mdl in (("fp64_jacobi", "jacobi", None), ("mixed_first_order", "factor", "none"),
+                          ("mixed_learned", "factor", model)):
+        if pc == "factor":
+            s.set_factor(None if mdl == "none" else mdl, 1.0)
+        runs = []
+        for rep in range(2):  # the first solve also builds the factor
+            s.init(x=np.zeros(s.n), b=sysd["b"], dirbc=dirbc, apply=True, pc=pc)
+            t1 = time.perf_counter()
+            if pc == "jacobi":
+                s.solve(50000, tol)
+            else:
+                s.solve_mixed(1000, tol, inner_tol=0.1, inner_maxit=50000)
+            runs.append(time.perf_counter() - t1)
+        out[name] = {"iterations": int(s.it()), "converged": bool(s.converged()),
+                     "s_per_solve": runs[-1],
+                     "rel_residual": float(s.normr / max(s.normb, 1e-300))}
+    out["speedup_learned_mixed_vs_fp64_jacobi"] = (out["fp64_jacobi"]["s_per_solve"] /
+                                                   out["mixed_learned"]["s_per_solve"])
+    ctx.close()
+    return out
+
+
 def run_chocg(n=129, steps=5, warm=2, tol=1e-8, train_steps=300, seed=0):
     """ChoCG s/step on the n^3 jittered cube (Taylor-Green vortex on
     [0, 2 pi]^3 mapped to the unit cube, mu = 1/Re = 0.01, damp2, CFL 0.5,
@@ -186,17 +231,23 @@ def run_chocg(n=129, steps=5, warm=2, tol=1e-8, train_steps=300, seed=0):
     t_setup = time.perf_counter() - t_setup
     tctx = lib.Context(0)
     t0 = time.perf_counter()
-    systems = [lpc.training_system(tctx, lpc.chocg_system(tctx, k, sd))
-               for k, sd in ((13, 1), (17, 2), (21, 3), (25, 4))]
+    systems = [lpc.training_system(tctx, lpc.chocg_system(tctx, k, sd)) for k, sd in CORPUS]
+    t_corpus = time.perf_counter() - t0
     model = lpc.LearnedPreconditioner(tctx, precision="bf16", seed=0)
+    t0 = time.perf_counter()
     hist = model.train(systems, train_steps, lr=1e-3)
+    t_train = time.perf_counter() - t0
     out = {"workload": f"ChoCG Taylor-Green, {n}^3 jittered cube, Re 100, damp2, CFL 0.5, "
                        "symmetry on all faces, hydrostat node",
            "nodes": int(ops["coord"].shape[1]), "tol": tol, "steps_timed": steps,
            "setup_s": t_setup,
-           "training": {"s": time.perf_counter() - t0, "steps": train_steps,
+           "training": {"s": t_train, "corpus_setup_s": t_corpus, "steps": train_steps,
                         "loss_first_last": [hist[0], hist[-1]],
-                        "systems": "ChoCG pressure matrices (hydrostat) of 13^3-25^3 cubes"}}
+                        "systems": f"{len(CORPUS)} ChoCG pressure matrices (hydrostat) of "
+                                   f"33^3-97^3 jittered cubes, jitter seeds 10-50 (the matrix, "
+                                   f"not the Reynolds number, is all the trace loss reads); "
+                                   f"{sum(k ** 3 for k, _ in CORPUS)} rows in all",
+                        "dense_layers": "BF16 tcgen05 tensor-core GEMMs, forward and backward"}}
     modes = {"fp64_jacobi": ("jacobi", None, False),
              "mixed_first_order": ("factor", "none", True),
              "mixed_learned": ("factor", model, True)}
@@ -227,6 +278,7 @@ def run_chocg(n=129, steps=5, warm=2, tol=1e-8, train_steps=300, seed=0):
                                                max(np.linalg.norm(ref_p), 1e-300))
     out["speedup_learned_mixed_vs_fp64_jacobi"] = (out["fp64_jacobi"]["s_per_step"] /
                                                    out["mixed_learned"]["s_per_step"])
+    out["pressure_solve_eval"] = [lpc_eval(model, k, sd, tol) for k, sd in EVAL]
     model.close()
     for s_ in systems:
         s_.ctx.close()

@@ -165,6 +165,31 @@ def test_adam_matches_oracle():
     model.close()
 
 
+def test_mixed_solve_smooth_rhs_tracks_fp64():
+    """The mixed-precision solve on a ChoCG pressure system with a smooth
+    right-hand side (its solution dominated by A's smoothest modes): the FP32
+    inner iteration forms A p' as sum a_ij (p'_j - p'_i) + rowsum p'_i and
+    accumulates the correction in FP64, so it converges like the FP64 PCG
+    with the same factor (at most 30 % more iterations) to the same
+    solution.  A plain FP32 row sum or an FP32 correction made the solve
+    stall on such systems."""
+    c = ctx()
+    sysd = lpc.chocg_system(None, 49, 5, rhs="smooth")
+    s = cg.ConjugateGradients(c, sysd["ia"], sysd["ja"], sysd["a"])
+    s.set_guard("underflow")
+    dirbc = (sysd["dirnodes"], sysd["dirvals"])
+    s.set_factor(None, 1.0)
+    s.init(x=np.zeros(s.n), b=sysd["b"], dirbc=dirbc, apply=True, pc="factor")
+    s.solve(20000, 1e-10)
+    it64, x64 = s.it(), s.solution()
+    assert s.converged()
+    s.init(x=np.zeros(s.n), b=sysd["b"], dirbc=dirbc, apply=True, pc="factor")
+    s.solve_mixed(1000, 1e-10, inner_tol=0.1, inner_maxit=20000)
+    assert s.converged()
+    assert s.it() <= 1.3 * it64, (s.it(), it64)
+    assert relerr(s.solution(), x64) < 1e-7
+
+
 def test_training_lowers_loss_and_beats_first_order():
     c = ctx()
     train = [lpc.training_system(c, lpc.pressure_system(c, n, seed))

@@ -84,12 +84,14 @@ struct CGDev {
   double* a0 = nullptr;                // original values (SELL order)
   double* a = nullptr;                 // working values (after Dirichlet elimination)
   float* a32 = nullptr;
+  float* rs32 = nullptr;               // per row: exact (FP64) working row sum, in FP32
   int32_t* diagpos = nullptr;          // SELL index of each row's diagonal
   uint8_t* bcmask = nullptr;
   double* bcval = nullptr;
   double *x = nullptr, *b = nullptr, *r = nullptr, *q = nullptr, *z = nullptr, *d = nullptr;
   double* p[2] = {nullptr, nullptr};
-  float *r32 = nullptr, *q32 = nullptr, *z32 = nullptr, *d32 = nullptr, *e32 = nullptr;
+  float *r32 = nullptr, *q32 = nullptr, *z32 = nullptr, *d32 = nullptr;
+  double* e64 = nullptr;  // the mixed solve's correction sum alpha p', accumulated in FP64
   float* r32b = nullptr;  // second FP32 residual (factored mixed iteration, alternating)
   float* p32[2] = {nullptr, nullptr};
   double* partial = nullptr;  // 3 * maxgrid
@@ -402,6 +404,22 @@ __global__ void k_apply_bc(int64_t n, const int32_t* __restrict__ soff,
   b[i] = bi;
 }
 
+// rs_i = sum_j a_ij of the working matrix (FP64), stored in FP32.
+__global__ void k_row_sums(int64_t n, const int32_t* __restrict__ soff,
+                           const int32_t* __restrict__ sw, const int32_t* __restrict__ col,
+                           const double* __restrict__ a, float* __restrict__ rs) {
+  int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= n) return;
+  const int lane = int(i & 31);
+  const int32_t off = soff[i >> 5], w = sw[i >> 5];
+  double sum = 0.0;
+  for (int k = 0; k < w; ++k) {
+    const int32_t e = off + k * kSlice + lane;
+    if (col[e] >= 0) sum += a[e];
+  }
+  rs[i] = float(sum);
+}
+
 __global__ void k_copy_values(int64_t nent, const double* __restrict__ a0, double* __restrict__ a,
                               float* __restrict__ a32) {
   int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
@@ -487,14 +505,19 @@ __global__ void __launch_bounds__(kBlock) k_cg_p(int64_t n, const T* __restrict_
 // q = A p', (p', q).  PF: p' = z + beta p formed per gathered entry and
 // stored for the row (the FP32 solver: two gathers, no extra pass; p0/p1
 // alternate with the count); otherwise p' = p0 = p1 (k_cg_p).  The FP32
-// solver sums (p', q) per thread in FP32 and widens once.
+// solver sums (p', q) per thread in FP32 and widens once, and forms each row
+// as sum_j a_ij (p'_j - p'_i) + rs_i p'_i (rs: the row's exact sum, zero for
+// an interior row of the pressure Laplacian): on a smooth p' the terms
+// a_ij p'_j of the plain sum cancel to a result about 1/kappa(A) of their
+// size, which FP32 cannot hold, while the differences p'_j - p'_i are
+// formed exactly and nothing large cancels.
 template <class T, class V, class CI, bool PF>
 __global__ void __launch_bounds__(kBlock) k_cg_a(int64_t n, const int32_t* __restrict__ soff,
                                                   const int32_t* __restrict__ sw, CI ci,
                                                   const V* __restrict__ a,
                                                   const T* __restrict__ z, T* p0, T* p1,
                                                   T* __restrict__ q, double* partial,
-                                                  CGScalars* sc) {
+                                                  CGScalars* sc, const float* __restrict__ rs) {
   griddep_wait();
   if (sc->done) return;
   const int64_t it = sc->it;
@@ -505,9 +528,12 @@ __global__ void __launch_bounds__(kBlock) k_cg_a(int64_t n, const int32_t* __res
   XG_ROWS(i, n) {
     const int lane = int(i & 31);
     if (PF) {
-      const T s = sell_row_x<T>(ci, a, soff[i >> 5], sw[i >> 5], lane, int32_t(i),
-                                 [&](int32_t c) { return __ldg(z + c) + beta * __ldg(pold + c); });
       const T pi = z[i] + beta * pold[i];
+      const T s = sell_row_x<T>(ci, a, soff[i >> 5], sw[i >> 5], lane, int32_t(i),
+                                 [&](int32_t c) {
+                                   return (__ldg(z + c) + beta * __ldg(pold + c)) - pi;
+                                 }) +
+                  T(rs[i]) * pi;
       pnew[i] = pi;
       q[i] = s;
       dot += pi * s;
@@ -569,12 +595,14 @@ __device__ __forceinline__ void end_iteration(double rr, CGScalars* sc) {
 //   FP64: ||r|| < tol ||b||, or maxit iterations (the reference's test);
 //   MIXED: ||r|| < max(tol ||b||, delta * rlast) asks for a residual
 //   replacement (rlast: the last true residual norm), as does maxit.
+// x is the FP64 solution (FP64 solver) or the mixed solver's FP64 correction
+// e, summed with exact FP64 products alpha p'.
 template <class T, bool FACTOR, bool MIXED>
 __global__ void __launch_bounds__(kBlock) k_cg_b(int64_t n, const T* __restrict__ q,
                                                   const T* __restrict__ d, const T* p0,
                                                   const T* p1, const float* __restrict__ srow,
                                                   T* __restrict__ r, T* __restrict__ z,
-                                                  T* __restrict__ vs, T* __restrict__ x,
+                                                  T* __restrict__ vs, double* __restrict__ x,
                                                   double* partial, CGScalars* sc) {
   griddep_wait();
   if (sc->done) return;
@@ -588,7 +616,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_b(int64_t n, const T* __restrict_
     XG_ROWS(i, n) {
       const T ri = r[i] - alpha * q[i];
       r[i] = ri;
-      x[i] += alpha * p[i];
+      x[i] += double(alpha) * double(p[i]);
       vs[i] = T(srow[i]) * ri;
     }
     griddep_trigger();
@@ -598,7 +626,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_b(int64_t n, const T* __restrict_
   XG_ROWS(i, n) {
     const T ri = r[i] - alpha * q[i];
     r[i] = ri;
-    x[i] += alpha * p[i];
+    x[i] += double(alpha) * double(p[i]);
     const T zi = ri * d[i];
     z[i] = zi;
     rz += ri * zi;
@@ -637,7 +665,9 @@ __global__ void __launch_bounds__(kBlock) k_pc_upper(int64_t n, const int32_t* _
 }
 
 // The update of a factored FP32 iteration fused with the first factor pass:
-// r' = r - alpha q, e += alpha p', u = (I+N)^T S r', with the neighbours'
+// r' = r - alpha q, e += alpha p' (in FP64: FP32 rounding noise in the
+// correction would be amplified by A's largest eigenvalues into the residual
+// the outer loop replaces), u = (I+N)^T S r', with the neighbours'
 // S r' formed from their r and q.  The residual alternates between ra and rb
 // with the count (the current one is ra at even counts): the pass reads one
 // and writes the other, so no row reads a residual that another row of the
@@ -646,7 +676,7 @@ template <class CI>
 __global__ void __launch_bounds__(kBlock) k_pc_upper_res(
     int64_t n, const int32_t* __restrict__ soffU, const int32_t* __restrict__ swU, CI ci,
     const __half* __restrict__ nvU, const float* __restrict__ srow, const float* __restrict__ q,
-    const float* p0, const float* p1, float* ra, float* rb, float* __restrict__ e,
+    const float* p0, const float* p1, float* ra, float* rb, double* __restrict__ e,
     float* __restrict__ u, const CGScalars* __restrict__ sc) {
   griddep_wait();
   if (sc->done) return;
@@ -659,7 +689,7 @@ __global__ void __launch_bounds__(kBlock) k_pc_upper_res(
     const int lane = int(i & 31);
     const float ri = rold[i] - alpha * q[i];
     rnew[i] = ri;
-    e[i] += alpha * p[i];
+    e[i] += double(alpha) * double(p[i]);
     u[i] = srow[i] * ri +
            sell_row_x<float, 8>(ci, nvU, soffU[i >> 5], swU[i >> 5], lane, int32_t(i),
                               [&](int32_t c) {
@@ -781,11 +811,11 @@ __global__ void __launch_bounds__(kBlock) k_outer_res(int64_t n, const int32_t* 
 }
 
 // x += e, e = 0
-__global__ void k_add_correction(int64_t n, float* __restrict__ e, double* __restrict__ x) {
+__global__ void k_add_correction(int64_t n, double* __restrict__ e, double* __restrict__ x) {
   int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (i < n) {
-    x[i] += double(e[i]);
-    e[i] = 0.f;
+    x[i] += e[i];
+    e[i] = 0.0;
   }
 }
 
@@ -981,7 +1011,7 @@ int cg_iterate(xg_ctx* c, CGDev* d, int64_t maxit, double tol, CGScalars* h) {
       double* p0 = d->p[0];
       launch_dep<k_cg_p<double>>(n, s, n, d->z, p0, d->scal);
       launch_dep<k_cg_a<double, double, Cols32, false>>(n, s, n, d->soff, d->swidth, Cols32{d->col},
-          d->a, d->z, p0, p0, d->q, d->partial, d->scal);
+          d->a, d->z, p0, p0, d->q, d->partial, d->scal, static_cast<const float*>(nullptr));
       if (d->pc == 2) {
         launch_dep<k_cg_b<double, true, false>>(n, s, n, d->q, d->d, p0, p0, d->srow, d->r, d->z,
             d->v, d->x, d->partial, d->scal);
@@ -1012,15 +1042,15 @@ int mixed_batch(xg_ctx* c, CGDev* d, CI ca, CI cu, CI cl) {
   for (int k = 0; k < kBatch; ++k) {
     float *p0 = d->p32[0], *p1 = d->p32[1];
     launch_dep<k_cg_a<float, float, CI, true>>(n, s, n, d->soff, d->swidth, ca, d->a32, d->z32, p0,
-        p1, d->q32, d->partial, d->scal);
+        p1, d->q32, d->partial, d->scal, static_cast<const float*>(d->rs32));
     if (d->pc == 2) {
       launch_dep<k_pc_upper_res<CI>>(n, s, n, d->soffU, d->swU, cu, d->hvU, d->srow, d->q32, p0, p1,
-          d->r32, d->r32b, d->e32, d->u32, d->scal);
+          d->r32, d->r32b, d->e64, d->u32, d->scal);
       launch_dep<k_pc_lower<float, __half, CI, 2>>(n, s, n, d->soffL, d->swL, cl, d->hvL, d->srow,
           d->bcmask, d->u32, d->r32, d->r32b, d->z32, d->partial, d->scal);
     } else {
       launch_dep<k_cg_b<float, false, true>>(n, s, n, d->q32, d->d32, p0, p1, d->srow, d->r32,
-          d->z32, d->v32, d->e32, d->partial, d->scal);
+          d->z32, d->v32, d->e64, d->partial, d->scal);
     }
   }
   XG_CHECK_LAUNCH(c);
@@ -1098,6 +1128,9 @@ int cg_init_device(xg_ctx* c, const double* b_dev, int zero_values, int pc) {
   d->apply = true;
   k_apply_bc<<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, d->soff, d->swidth, d->col, d->a0, d->a,
                                                        d->a32, d->bcmask, val, nullptr, d->b);
+  XG_CHECK_LAUNCH(c);
+  k_row_sums<<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, d->soff, d->swidth, d->col, d->a,
+                                                      d->rs32);
   XG_CHECK_LAUNCH(c);
   CGScalars h{};
   h.pc = pc;
@@ -1278,6 +1311,7 @@ int xg_cg_setup(xg_ctx* c, int64_t nrow, const uint64_t* ia, const uint64_t* ja,
     A.plan(d->a0, tot);
     A.plan(d->a, tot);
     A.plan(d->a32, tot);
+    A.plan(d->rs32, nrow);
     A.plan(d->diagpos, nrow);
     A.plan(d->bcmask, nrow);
     A.plan(d->bcval, nrow);
@@ -1294,7 +1328,7 @@ int xg_cg_setup(xg_ctx* c, int64_t nrow, const uint64_t* ia, const uint64_t* ja,
     A.plan(d->q32, nrow);
     A.plan(d->z32, nrow);
     A.plan(d->d32, nrow);
-    A.plan(d->e32, nrow);
+    A.plan(d->e64, nrow);
     A.plan(d->p32[0], nrow);
     A.plan(d->p32[1], nrow);
     A.plan(d->partial, 3 * d->maxgrid);
@@ -1366,6 +1400,9 @@ int xg_cg_setup(xg_ctx* c, int64_t nrow, const uint64_t* ia, const uint64_t* ja,
   XG_CUDA(c, cudaMemsetAsync(d->scal, 0, sizeof(CGScalars), s));
   k_copy_values<<<blocks_for(tot, kBlock), kBlock, 0, s>>>(tot, d->a0, d->a, d->a32);
   XG_CHECK_LAUNCH(c);
+  k_row_sums<<<blocks_for(nrow, kBlock), kBlock, 0, s>>>(nrow, d->soff, d->swidth, d->col, d->a,
+                                                         d->rs32);
+  XG_CHECK_LAUNCH(c);
   XG_CUDA(c, cudaStreamSynchronize(s));
   return XG_OK;
   XG_HOST_CATCH(c)
@@ -1434,6 +1471,9 @@ int xg_cg_init(xg_ctx* c, const double* x, const double* b, const double* neubc,
     k_copy_values<<<blocks_for(d->nent, kBlock), kBlock, 0, s>>>(d->nent, d->a0, d->a, d->a32);
     XG_CHECK_LAUNCH(c);
   }
+  k_row_sums<<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, d->soff, d->swidth, d->col, d->a,
+                                                      d->rs32);
+  XG_CHECK_LAUNCH(c);
   if (key != d->bc_key || !d->ready) {
     d->geom_set = false;
     d->factor_set = false;
@@ -1494,7 +1534,7 @@ int xg_cg_solve_mixed(xg_ctx* c, int64_t maxit, double tol, double inner_tol,
   rc = read_scal(c, d, &h);
   if (rc) return rc;
   const double nb0 = h.normb > 1.0e-14 ? h.normb : 1.0;
-  XG_CUDA(c, cudaMemsetAsync(d->e32, 0, d->n * 4, s));
+  XG_CUDA(c, cudaMemsetAsync(d->e64, 0, d->n * 8, s));
   // the first FP32 iteration reads p with weight beta = 0: make it finite
   XG_CUDA(c, cudaMemsetAsync(d->p32[0], 0, d->n * 4, s));
   XG_CUDA(c, cudaMemsetAsync(d->p32[1], 0, d->n * 4, s));
@@ -1524,7 +1564,7 @@ int xg_cg_solve_mixed(xg_ctx* c, int64_t maxit, double tol, double inner_tol,
       if (h.done) break;
     }
     breakdown = h.finished;
-    k_add_correction<<<blocks_for(d->n, kBlock), kBlock, 0, s>>>(d->n, d->e32, d->x);
+    k_add_correction<<<blocks_for(d->n, kBlock), kBlock, 0, s>>>(d->n, d->e64, d->x);
     XG_CHECK_LAUNCH(c);
     rc = replace_residual(c, d, 0);
     if (rc) return rc;

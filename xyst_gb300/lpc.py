@@ -143,15 +143,33 @@ def pressure_system(ctx: Context, n: int, seed: int, jitter: float = 0.2, dir_se
     return dict(mesh=m, ia=ia, ja=ja, a=a, dirnodes=dn, dirvals=np.zeros(dn.size), b=b)
 
 
-def chocg_system(ctx: Context, n: int, seed: int, jitter: float = 0.2):
+def chocg_system(ctx: Context, n: int, seed: int, jitter: float = 0.2, rhs: str = "random"):
     """The pressure system ChoCG assembles for the Taylor-Green setup on an
-    n^3 jittered cube (symmetry on every face): the ChoCG::prelhs matrix with
-    the hydrostat node as its only Dirichlet row.  The trace loss reads the
-    matrix only; b is a random right-hand side for iteration counts."""
-    m = mesh.cube(n, jitter=jitter, seed=seed, numbering="rcm", perm_seed=seed + 7)
+    n^3 jittered cube (symmetry on every face), nodes in reverse
+    Cuthill-McKee order: the ChoCG::prelhs matrix with the hydrostat node as
+    its only Dirichlet row.  The trace loss reads the matrix only; b is a
+    right-hand side for iteration counts: "random" (white noise) or
+    "smooth" (a few low Fourier modes plus 10 % noise, the character of a
+    pressure increment's divergence source), scaled like ChoCG's."""
+    from . import riecg
+    m = mesh.cube(n, jitter=jitter, seed=seed, numbering="lex", faces=False)
+    m = mesh.relabel(m, riecg.rcm(m["inpoel"], m["coord"].shape[1]))
     ia, ja, a = cg.pressure_matrix(m["coord"], m["inpoel"])
     rng = np.random.default_rng(seed + 1000)
-    b = rng.standard_normal(ia.size - 1) * np.abs(a).max() * 1e2
+    if rhs == "smooth":
+        x, y, z = m["coord"]
+        b = np.zeros(x.size)
+        for _ in range(4):
+            k = rng.integers(1, 4, size=3)
+            ph = rng.uniform(0, 2 * np.pi, size=3)
+            b += rng.standard_normal() * (np.sin(np.pi * k[0] * x + ph[0]) *
+                                          np.sin(np.pi * k[1] * y + ph[1]) *
+                                          np.sin(np.pi * k[2] * z + ph[2]))
+        b += 0.1 * rng.standard_normal(x.size)
+    else:
+        b = rng.standard_normal(ia.size - 1)
+    b *= np.abs(a).max() * 1e2
+    b[0] = 0.0  # the hydrostat row
     return dict(mesh=m, ia=ia, ja=ja, a=a, dirnodes=np.array([0]), dirvals=np.zeros(1), b=b)
 
 

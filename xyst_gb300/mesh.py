@@ -149,13 +149,15 @@ def cube_slab(n: int, k0: int, k1: int, jitter: float = 0.0, seed: int = 0) -> d
 
 
 def cube(n: int, jitter: float = 0.0, seed: int = 0, numbering: str = "lex",
-         perm_seed: int | None = None) -> dict:
+         perm_seed: int | None = None, faces: bool = True) -> dict:
     """Unit cube [0,1]^3 with n**3 nodes, Kuhn-split into 6 (n-1)**3 tets.
 
     jitter: interior nodes move by U(-jitter*h, +jitter*h) per coordinate
     (seeded by ``seed``); boundary nodes stay on the cube faces.
     numbering: "lex" (i fastest), "random" (seeded permutation, ``perm_seed``)
     or "rcm" (reverse Cuthill-McKee of the lexicographic graph).
+    faces: False leaves the side sets out (bface empty), for uses that need
+    the volume mesh only.
     """
     if n < 2:
         raise ValueError("cube needs at least 2 nodes per side")
@@ -163,7 +165,7 @@ def cube(n: int, jitter: float = 0.0, seed: int = 0, numbering: str = "lex",
     h = 1.0 / m
     coord = _cube_coord(n, jitter, seed)
     inpoel = _orient_positive(coord, _kuhn_cells(m))
-    bface = faces_from_tets(inpoel, _cube_faces(n))
+    bface = faces_from_tets(inpoel, _cube_faces(n)) if faces else {}
     mesh = {"coord": coord, "inpoel": inpoel, "bface": bface, "h": h}
     if numbering == "lex":
         return mesh
