@@ -561,10 +561,31 @@ def fp64_leg(ctx, ops, r, U0, prec, args, acc_steps=200):
     r64.bc()
     _, ms = r64.run(k64)
     n = U0.shape[0]
+    nedge = ops["edges"].shape[0]
     out = {"workload": "the same cube, state and steps in FP64 mode (gradients, fluxes and "
-                       "update in FP64, the reference's operation order)",
+                       "update in FP64, the reference's operation order apart from the van "
+                       "Leer pair's one division per side)",
            "steps": k64, "ms_per_step": ms / k64, "value": n * k64 / (ms / 1e3), "unit": UNIT,
            "kernels": {k: {"ms_total": v[0], "launches": v[1]} for k, v in kt.items()}}
+    # FP64 roofline of the flux kernel: its operation count per edge from the
+    # source (10 three-term projections 50, MUSCL 5 x 34 with one division per
+    # component, Rusanov 94 with 3 square roots, the two residual shares 15:
+    # 329 FP64 operations, each division or square root counted once) against
+    # the FP64 peak measured here (cuBLAS DGEMM), and its bytes against HBM
+    if "riecg_flux" in kt:
+        fl_ms = kt["riecg_flux"][0] / kt["riecg_flux"][1]
+        peak64 = fp64_peak_tflops()
+        flops = 329.0 * nedge
+        kb = kernel_bytes(n, nedge, ops["tri"].shape[0], False)
+        hbm, kind = peaks()
+        out["flux_roofline"] = {
+            "kernel": "riecg_flux (FP64)", "mean_launch_ms": fl_ms,
+            "flops_per_launch": flops, "achieved_tflops": flops / (fl_ms / 1e3) / 1e12,
+            "fp64_peak_tflops": peak64, "fp64_peak_kind": "measured: cuBLAS DGEMM 4096^3",
+            "frac_fp64": flops / (fl_ms / 1e3) / 1e12 / peak64 if peak64 else None,
+            "algorithmic_bytes_per_launch": kb["riecg_flux"],
+            "frac_hbm": kb["riecg_flux"] / (fl_ms / 1e3) / 1e9 / hbm,
+            "bound": "fp64"}
     acc = None
     if prec == "fp32":
         r64.set_state(U0)
@@ -584,6 +605,29 @@ def fp64_leg(ctx, ops, r, U0, prec, args, acc_steps=200):
     del r64
     ctx64.close()
     return out, acc
+
+
+def fp64_peak_tflops(m=4096, reps=5):
+    """FP64 throughput of a cuBLAS DGEMM (m^3, best of reps, CUDA events):
+    the measured FP64 roof of this GPU."""
+    try:
+        import torch
+        a = torch.randn(m, m, dtype=torch.float64, device="cuda")
+        b = torch.randn(m, m, dtype=torch.float64, device="cuda")
+        torch.matmul(a, b)
+        best = None
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b)
+            e1.record()
+            torch.cuda.synchronize()
+            t = e0.elapsed_time(e1) / 1e3
+            best = t if best is None else min(best, t)
+        del a, b
+        return 2.0 * m ** 3 / best / 1e12
+    except Exception:
+        return None
 
 
 def e2e_run(r, U0, steps, world):

@@ -256,11 +256,12 @@ __device__ __forceinline__ void block_min_atomic(double v, unsigned long long* d
 
 // MUSCL reconstruction of the five flow variables on edge L->R
 // (muscl(), src/Physics/Riemann.cpp:34-143) from the edge-end primitives and
-// the projections g1 = G_L.(x_R - x_L), g2 = G_R.(x_R - x_L).  The double
-// instantiation keeps the reference's operation order; the float one
-// evaluates the same van Leer pair phi(a/b), phi(b/a) = 2|a|/(|a|+|b|),
-// 2|b|/(|a|+|b|) (zero for opposite signs) with one reciprocal instead of four
-// divisions.
+// the projections g1 = G_L.(x_R - x_L), g2 = G_R.(x_R - x_L).  The van Leer
+// limiter of a pair, phi(r) = (|r| + r)/(|r| + 1) at r = a/b and at 1/r, is
+// the same pair of numbers as 2|a|/(|a|+|b|), 2|b|/(|a|+|b|) for a b > 0 and
+// 0, 0 otherwise: both precisions evaluate that form, with one division (FP64)
+// or one reciprocal (FP32) per side instead of the reference's four
+// divisions per side (the difference is rounding, ~1e-16 relative).
 template <class F>
 __device__ __forceinline__ void muscl(const F wl[5], const F wr[5], const F g1[5],
                                       const F g2[5], F l[5], F r[5]) {
@@ -273,14 +274,14 @@ __device__ __forceinline__ void muscl(const F wl[5], const F wr[5], const F g1[5
     d1[c] = F(2.0) * g1[c] - d2;
     d3[c] = F(2.0) * g2[c] - d2;
     if constexpr (sizeof(F) == 8) {
-      F rcL = (d2 + eps) / (d1[c] + eps);
-      F rcR = (d2 + eps) / (d3[c] + eps);
-      F rLinv = (d1[c] + eps) / (d2 + eps);
-      F rRinv = (d3[c] + eps) / (d2 + eps);
-      F phiL = (fabs(rcL) + rcL) / (fabs(rcL) + F(1.0));
-      F phiR = (fabs(rcR) + rcR) / (fabs(rcR) + F(1.0));
-      F phiLi = (fabs(rLinv) + rLinv) / (fabs(rLinv) + F(1.0));
-      F phiRi = (fabs(rRinv) + rRinv) / (fabs(rRinv) + F(1.0));
+      const F a = d2 + eps, b = d1[c] + eps, e3 = d3[c] + eps;
+      const F aa = fabs(a), ab = fabs(b), ae = fabs(e3);
+      // both sides' 2/(|a|+|b|) from one division: 2/((|a|+|b|)(|a|+|e|))
+      const F sL = aa + ab, sR = aa + ae;
+      const F q2 = F(2.0) / (sL * sR);
+      const F iL = (a * b > F(0)) ? q2 * sR : F(0);
+      const F iR = (a * e3 > F(0)) ? q2 * sL : F(0);
+      const F phiL = aa * iL, phiLi = ab * iL, phiR = aa * iR, phiRi = ae * iR;
       l[c] = wl[c] + F(0.25) * (d1[c] * (F(1.0) - k) * phiL + d2 * (F(1.0) + k) * phiLi);
       r[c] = wr[c] - F(0.25) * (d3[c] * (F(1.0) - k) * phiR + d2 * (F(1.0) + k) * phiRi);
     } else {
@@ -305,8 +306,6 @@ __device__ __forceinline__ void muscl(const F wl[5], const F wr[5], const F g1[5
 // sqrt: IEEE in double; x * rsqrt(x) in float (x >= 0).
 __device__ __forceinline__ double xsqrt(double x) { return sqrt(x); }
 __device__ __forceinline__ float xsqrt(float x) { return x > 0.f ? x * rsqrtf(x) : 0.f; }
-__device__ __forceinline__ double xdiv(double a, double b) { return a / b; }
-__device__ __forceinline__ float xdiv(float a, float b) { return __fdividef(a, b); }
 
 // Rusanov edge flux (rusanov(), src/Physics/Riemann.cpp:369-478).
 template <class F>
@@ -317,6 +316,7 @@ __device__ __forceinline__ void rusanov(const F wl[5], const F wr[5], const F g1
   muscl(wl, wr, g1, g2, l, r);
   F pL = l[0] * l[4] * (gamma - F(1.0));
   F pR = r[0] * r[4] * (gamma - F(1.0));
+  const F cLe = l[4], cRe = r[4];
   F vnL = l[1] * nx + l[2] * ny + l[3] * nz;
   F vnR = r[1] * nx + r[2] * ny + r[3] * nz;
   l[4] = (l[4] + F(0.5) * (l[1] * l[1] + l[2] * l[2] + l[3] * l[3])) * l[0];
@@ -328,8 +328,12 @@ __device__ __forceinline__ void rusanov(const F wl[5], const F wr[5], const F g1
   r[2] *= r[0];
   r[3] *= r[0];
   F len = xsqrt(nx * nx + ny * ny + nz * nz);
-  F sl = fabs(vnL) + xsqrt(xdiv(gamma * pL, l[0])) * len;
-  F sr = fabs(vnR) + xsqrt(xdiv(gamma * pR, r[0])) * len;
+  // sound speed^2 = gamma p / rho with p = rho e (gamma - 1): gamma (gamma - 1) e
+  // (the reference divides p by rho; the same value up to rounding); e is
+  // the reconstructed internal energy, kept in cLe / cRe before the
+  // conversion to total energy below
+  F sl = fabs(vnL) + xsqrt(gamma * (gamma - F(1.0)) * cLe) * len;
+  F sr = fabs(vnR) + xsqrt(gamma * (gamma - F(1.0)) * cRe) * len;
   F fw = sl > sr ? sl : sr;
   f[0] = l[0] * vnL + r[0] * vnR + fw * (r[0] - l[0]);
   f[1] = l[1] * vnL + r[1] * vnR + (pL + pR) * nx + fw * (r[1] - l[1]);
