@@ -1,8 +1,10 @@
 """KozCG (Taylor-Galerkin + FCT) on the GPU against the oracle and the
-reference's KozCG Sod baseline.  In FP64 the element scatter uses atomic adds,
-so results agree with the oracle up to summation order (1e-12 relative).  The
-FP32 element path (element terms in FP32, nodal sums and update in FP64) is
-held to stated error bounds against the same FP64 oracle."""
+reference's KozCG Sod baseline.  In FP64 each node sums its element
+contributions in ascending element order (the oracle's order), with no
+atomics, so a run gives the same bits every time; it agrees with the oracle
+to 1e-12 relative (contracted multiply-adds round differently).  The FP32
+element path (element terms in FP32, nodal sums and update in FP64) is held
+to stated error bounds against the same FP64 oracle."""
 
 import numpy as np
 import pytest
@@ -58,6 +60,30 @@ def test_run_fp32_bound(fct):
     dto = o.run(8)
     assert np.allclose(dts, dto, rtol=1e-6)
     assert relerr(d.state()[0], o.state()) < 1e-5
+
+
+def test_fp64_runs_are_bit_identical():
+    """FP64 with FCT on a 17^3 cube in random node order (many elements per
+    node, every order of arrival possible): two set-ups, the same state and
+    steps, give bit-identical states, time steps and right-hand sides."""
+    m, v = _cube(17, seed=3)
+    sym = oracle.sym_bc(m["coord"], m["bface"], [1, 2, 3, 4, 5, 6])
+    U0 = wave_ic(m["coord"])
+    out = []
+    for _ in range(2):
+        d = kozcg.KozCG(ctx(), m["coord"], v, m["inpoel"], fct=True)
+        d.set_bc(sym=sym[:2])
+        rhs = d.rhs(U0, 1.0e-3)
+        d.set_state(U0)
+        dts, _ = d.run(10)
+        out.append((rhs, dts, d.state()[0]))
+    for a, b in zip(out[0], out[1]):
+        assert np.array_equal(a, b)
+    o = oracle.KozCG(m["coord"], v, m["inpoel"], fct=True)
+    o.set_sym(*sym[:2])
+    o.set_state(U0)
+    o.run(10)
+    assert relerr(out[0][2], o.state()) < 1e-12
 
 
 def test_bad_precision_rejected():

@@ -12,18 +12,22 @@
 //
 // Layout: node arrays SoA [ncomp][n] (U, R = rhs then low-order solution,
 // P = antidiffusive sums +/- per component, A = limited contributions),
-// elements as int32 [T][4].  Element kernels (one thread per tet) scatter to
-// their four nodes with atomic adds.  The allowed limits Q+/- (extremes over
+// elements as int32 [T][4].  Element kernels (one thread per tet) hand their
+// four nodes' contributions on: in FP64 as plain stores into element-major
+// slots that k_node_gather sums per node in ascending element order (the
+// reference's order, the same bits on every run), in FP32 as vector atomic
+// adds into node records.  The allowed limits Q+/- (extremes over
 // the elements holding a node) are taken per node over the node adjacency,
 // which holds the same nodes, and kept as order-preserving keys.  Node
 // kernels (one thread per node) do the per-node algebra between the element
 // passes.  One step is:
-//   step_begin -> zero -> node_prim -> elem_rhs_aec -> bc_p -> node_lo -> node_alw ->
-//   node_lim -> elem_lim -> node_solve -> bc (+ CFL minimum for the next step)
+//   step_begin -> node_prim -> elem_rhs_aec -> [gather] -> bc_p -> node_lo -> node_alw ->
+//   node_lim -> elem_lim -> [gather] -> node_solve -> bc (+ CFL minimum for the next step)
+// ([gather]: FP64; FP32 zeroes its records first instead)
 //
 // FP32-element mode: the element passes read an FP32 copy of the state (made
 // by node_prim) and FP32 element geometry (made at setup), and add into FP32
-// node records [n][8] / [n][12] with vector atomics; the allowed limits are
+// node records [n][16] / [n][8] with vector atomics; the allowed limits are
 // 32-bit keys of floats.  The node passes (low-order solution, limit
 // coefficients, update, dt) stay FP64 on the FP64 state.  GB300's FP64 rate
 // is a small fraction of its FP32 rate, and FP32/FP64 conversions run at the
@@ -67,6 +71,11 @@ struct KozCGDev {
   float *R32 = nullptr, *A32 = nullptr, *U32 = nullptr, *lo32 = nullptr;
   unsigned int* Q32 = nullptr;
   float* geo32 = nullptr;
+  // FP64 mode: residual and limited slot records (10 and 6 doubles per
+  // (element, local node) slot) and each node's slots in element order,
+  // SELL-32 like the adjacency
+  double *E = nullptr, *L = nullptr;
+  int32_t *soff = nullptr, *sw = nullptr, *sslot = nullptr;
   // node adjacency (every pair of nodes sharing a tet) as SELL-32: slice s
   // of 32 nodes, entry k of node i at aoff[s] + 32 k + lane, -1 padding
   int64_t nslice = 0;
@@ -201,8 +210,9 @@ __device__ __forceinline__ unsigned int tobits(float v) { return __float_as_uint
 // (red.global.add.v4.f32) instead of one atomic per component: R and P share
 // a [n][16] record (R at 0..4, P+/- at 5..14, P addressed from R + 5), A has
 // [n][8].
-constexpr int kRP = 16;  // FP32 R+P record
-constexpr int kAR = 8;   // FP32 A record
+constexpr int kRP = 16;   // FP32 R+P record
+constexpr int kAR = 8;    // FP32 A record
+constexpr int kGB = 4;    // FP64 node gather: slots loaded together
 template <class F, int S>
 __device__ __forceinline__ int64_t ridx(int64_t n, int c, int64_t i) {
   return sizeof(F) == 4 ? i * S + c : c * n + i;
@@ -212,11 +222,7 @@ __device__ __forceinline__ int64_t pidx(int64_t n, int cs, int64_t i) {
   return sizeof(F) == 4 ? i * kRP + cs : cs * n + i;
 }
 
-// r[5] added to node i's record of R (S = kRP) or A (S = kAR).
-template <int S>
-__device__ __forceinline__ void add5(double* R, int64_t n, int64_t i, const double r[5]) {
-  for (int c = 0; c < 5; ++c) atomicAdd(R + c * n + i, r[c]);
-}
+// FP32 mode: r[5] added to node i's record of R (S = kRP) or A (S = kAR).
 template <int S>
 __device__ __forceinline__ void add5(float* R, int64_t, int64_t i, const float r[5]) {
   atomicAdd(reinterpret_cast<float4*>(R + i * S), make_float4(r[0], r[1], r[2], r[3]));
@@ -313,21 +319,19 @@ __device__ __forceinline__ void load_v4(const F* V, int64_t i, F o[4]) {
   }
 }
 
+// kozak::rhs for one tet (Kozak.cpp:73-173): the residual r[a][c] of its
+// four nodes, and with fct the antidiffusive element contributions of
+// KozCG::aec (KozCG.cpp:794-814) aec[a][c] (zero without).  V holds each
+// node's velocity and pressure (k_node_prim).
 template <class F>
-__global__ void __launch_bounds__(kBlock) k_elem_rhs_aec(int64_t n, int64_t ne,
-                                                          const int32_t* __restrict__ inpoel,
-                                                          const double* __restrict__ xyz,
-                                                          const float* __restrict__ geo,
-                                                          const double* __restrict__ U,
-                                                          const F* __restrict__ Uf,
-                                                          const F* __restrict__ V,
-                                                          const KScalars* __restrict__ sc,
-                                                          double gamma_d, double ctau_d, int fct,
-                                                          F* R, F* P) {
-  int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  if (e >= ne) return;
-  const F gamma = F(gamma_d), ctau = F(ctau_d);
-  int32_t N[4];
+__device__ __forceinline__ void elem_terms(int64_t n, int64_t ne, int64_t e,
+                                           const int32_t* __restrict__ inpoel,
+                                           const double* __restrict__ xyz,
+                                           const float* __restrict__ geo,
+                                           const double* __restrict__ U, const F* __restrict__ Uf,
+                                           const F* __restrict__ V,
+                                           const KScalars* __restrict__ sc, F gamma, F ctau,
+                                           int fct, int32_t N[4], F r[4][5], F aec[4][5]) {
   for (int a = 0; a < 4; ++a) N[a] = inpoel[e * 4 + a];
   const Geo<F> t = elem_geo<F>(xyz, geo, n, ne, e, N);
   F u[4][5], vel[4][3], p[4];
@@ -357,7 +361,6 @@ __global__ void __launch_bounds__(kBlock) k_elem_rhs_aec(int64_t n, int64_t ne,
     }
   const F pr =
       (gamma - F(1.0)) * (ue[4] - F(0.5) * (ue[1] * ue[1] + ue[2] * ue[2] + ue[3] * ue[3]) / ue[0]);
-  F r[4][5];
   for (int a = 0; a < 4; ++a)
     for (int c = 0; c < 5; ++c) r[a][c] = F(0.0);
   coef = F(1.0) / F(6.0);
@@ -373,45 +376,110 @@ __global__ void __launch_bounds__(kBlock) k_elem_rhs_aec(int64_t n, int64_t ne,
       r[a][4] += cg * (ue[4] + pr) * uj;
     }
   }
-  if (!fct || sizeof(F) == 8)
-    for (int a = 0; a < 4; ++a) add5<kRP>(R, n, N[a], r[a]);
-  if (!fct) return;
-  if constexpr (sizeof(F) == 8) {
-    for (int c = 0; c < 5; ++c)
-      for (int a = 0; a < 4; ++a) {
-        F aec = F(0.0);
-        for (int b = 0; b < 4; ++b) {
-          const F m = t.J / F(120.0) * ((a == b) ? F(3.0) : F(-1.0));
-          aec += m * ctau * u[b][c];
-        }
-        if (aec > F(0.0))
-          atomicAdd(P + (c * 2 + 0) * n + N[a], aec);
-        else if (aec < F(0.0))
-          atomicAdd(P + (c * 2 + 1) * n + N[a], aec);
-      }
-  } else {
-    // per node its residual and its ten antidiffusive sums (+, - per
-    // component; the sign that does not apply adds 0) in one [16] record:
-    // four vector atomics
+  for (int c = 0; c < 5; ++c)
     for (int a = 0; a < 4; ++a) {
-      F v[16];
-      for (int c = 0; c < 5; ++c) v[c] = r[a][c];
-      for (int c = 0; c < 5; ++c) {
-        F aec = F(0.0);
+      F s = F(0.0);
+      if (fct)
         for (int b = 0; b < 4; ++b) {
           const F m = t.J / F(120.0) * ((a == b) ? F(3.0) : F(-1.0));
-          aec += m * ctau * u[b][c];
+          s += m * ctau * u[b][c];
         }
-        v[5 + c * 2 + 0] = aec > F(0.0) ? aec : F(0.0);
-        v[5 + c * 2 + 1] = aec < F(0.0) ? aec : F(0.0);
-      }
-      v[15] = F(0.0);
-      float* q = R + int64_t(N[a]) * kRP;
-      for (int k = 0; k < 4; ++k)
-        atomicAdd(reinterpret_cast<float4*>(q + 4 * k),
-                  make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]));
+      aec[a][c] = s;
+    }
+}
+
+// FP32 element pass: per node its residual and its ten antidiffusive sums
+// (+, - per component; the sign that does not apply adds 0) in one [16]
+// record, four vector atomics (one per 4 floats); without FCT the residual
+// alone.
+__global__ void __launch_bounds__(kBlock) k_elem_rhs_aec32(int64_t n, int64_t ne,
+                                                            const int32_t* __restrict__ inpoel,
+                                                            const float* __restrict__ geo,
+                                                            const float* __restrict__ Uf,
+                                                            const float* __restrict__ V,
+                                                            const KScalars* __restrict__ sc,
+                                                            double gamma, double ctau, int fct,
+                                                            float* R) {
+  const int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (e >= ne) return;
+  int32_t N[4];
+  float r[4][5], aec[4][5];
+  elem_terms<float>(n, ne, e, inpoel, nullptr, geo, nullptr, Uf, V, sc, float(gamma),
+                    float(ctau), fct, N, r, aec);
+  if (!fct) {
+    for (int a = 0; a < 4; ++a) add5<kRP>(R, n, N[a], r[a]);
+    return;
+  }
+  for (int a = 0; a < 4; ++a) {
+    float v[16];
+    for (int c = 0; c < 5; ++c) v[c] = r[a][c];
+    for (int c = 0; c < 5; ++c) {
+      v[5 + c * 2 + 0] = aec[a][c] > 0.f ? aec[a][c] : 0.f;
+      v[5 + c * 2 + 1] = aec[a][c] < 0.f ? aec[a][c] : 0.f;
+    }
+    v[15] = 0.f;
+    float* q = R + int64_t(N[a]) * kRP;
+    for (int k = 0; k < 4; ++k)
+      atomicAdd(reinterpret_cast<float4*>(q + 4 * k),
+                make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]));
+  }
+}
+
+// FP64 element passes hand their node contributions to k_node_gather through
+// slot records, one per (element e, local node a), slot q = 4 e + a: the
+// residual pass writes 10 doubles (the five contributions, then the five
+// antidiffusive ones), the limiting pass 6 (the five limited contributions
+// and a zero).  A warp's 32 elements own 128 consecutive records; each lane
+// builds its four in shared memory (kStW double2 per lane: 16-byte stores
+// of 8 lanes fall in distinct banks) and the warp moves the run to or from
+// global memory with contiguous 512-byte accesses.
+constexpr int kEB = 128;   // FP64 element-pass block: 4 warps
+constexpr int kStW = 21;   // staged double2 per lane
+constexpr int kRecD2 = 5;  // residual slot record, double2
+constexpr int kLimD2 = 3;  // limited slot record, double2
+
+template <int D2>  // double2 per element
+__device__ __forceinline__ void warp_put(double2* __restrict__ g, const double2* buf, int nv,
+                                         int lane) {
+  for (int k = lane; k < nv * D2; k += 32) g[k] = buf[(k / D2) * kStW + k % D2];
+}
+template <int D2>
+__device__ __forceinline__ void warp_get(const double2* __restrict__ g, double2* buf, int nv,
+                                         int lane) {
+  for (int k = lane; k < nv * D2; k += 32) buf[(k / D2) * kStW + k % D2] = __ldg(g + k);
+}
+
+__global__ void __launch_bounds__(kEB) k_elem_rhs64(int64_t n, int64_t ne,
+                                                     const int32_t* __restrict__ inpoel,
+                                                     const double* __restrict__ xyz,
+                                                     const double* __restrict__ U,
+                                                     const double* __restrict__ V,
+                                                     const KScalars* __restrict__ sc,
+                                                     double gamma, double ctau, int fct,
+                                                     double* __restrict__ E) {
+  __shared__ double2 st[kEB / 32][32 * kStW];
+  const int lane = threadIdx.x & 31;
+  const int64_t e = blockIdx.x * int64_t(kEB) + threadIdx.x;
+  const int64_t e0 = e - lane;
+  if (e0 >= ne) return;  // the whole warp is past the last element
+  double2* buf = st[threadIdx.x >> 5];
+  if (e < ne) {
+    int32_t N[4];
+    double r[4][5], aec[4][5];
+    elem_terms<double>(n, ne, e, inpoel, xyz, nullptr, U, nullptr, V, sc, gamma, ctau, fct, N, r,
+                       aec);
+    for (int a = 0; a < 4; ++a) {
+      double2* b = buf + lane * kStW + a * kRecD2;
+      b[0] = make_double2(r[a][0], r[a][1]);
+      b[1] = make_double2(r[a][2], r[a][3]);
+      b[2] = make_double2(r[a][4], aec[a][0]);
+      b[3] = make_double2(aec[a][1], aec[a][2]);
+      b[4] = make_double2(aec[a][3], aec[a][4]);
     }
   }
+  __syncwarp();
+  const int nv = static_cast<int>(ne - e0 < 32 ? ne - e0 : 32);
+  warp_put<4 * kRecD2>(reinterpret_cast<double2*>(E) + e0 * 4 * kRecD2, buf, nv, lane);
 }
 
 struct KBC {
@@ -558,31 +626,17 @@ __global__ void k_node_lim(int64_t n, const double* __restrict__ R, const double
 
 // KozCG::lim element part (KozCG.cpp:1049-1078): limited antidiffusive
 // element contributions, system-limited over the components in sysmask.
+// Limit coefficients of one element from its antidiffusive contributions
+// aec[a][c] and the nodes' C+/- (Q, as F bits); ca = the limited ones.
 template <class F>
-__global__ void __launch_bounds__(kBlock) k_elem_lim(int64_t n, int64_t ne,
-                                                      const int32_t* __restrict__ inpoel,
-                                                      const double* __restrict__ xyz,
-                                                      const float* __restrict__ geo,
-                                                      const double* __restrict__ U,
-                                                      const F* __restrict__ Uf,
-                                                      const typename KozT<F>::Key* __restrict__ Q,
-                                                      double ctau_d, int sysmask, F* A) {
-  int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  if (e >= ne) return;
-  const F ctau = F(ctau_d);
-  int32_t N[4];
-  for (int a = 0; a < 4; ++a) N[a] = inpoel[e * 4 + a];
-  const Geo<F> t = elem_geo<F>(xyz, geo, n, ne, e, N);
-  F coef[5], aec[5][4];
+__device__ __forceinline__ void elem_limit(int64_t n, const int32_t N[4],
+                                           const typename KozT<F>::Key* __restrict__ Q,
+                                           int sysmask, const F aec[4][5], F ca[4][5]) {
+  F coef[5];
   for (int c = 0; c < 5; ++c) {
     coef[c] = F(1.0);
     for (int a = 0; a < 4; ++a) {
-      F s = F(0.0);
-      for (int b = 0; b < 4; ++b) {
-        const F m = t.J / F(120.0) * ((a == b) ? F(3.0) : F(-1.0));
-        s += m * ctau * ust<F>(U, Uf, n, c, N[b]);
-      }
-      aec[c][a] = s;
+      const F s = aec[a][c];
       const F lim = kbits(Q[(c * 2 + (s > F(0.0) ? 0 : 1)) * n + N[a]]);
       coef[c] = coef[c] < lim ? coef[c] : lim;
     }
@@ -592,10 +646,156 @@ __global__ void __launch_bounds__(kBlock) k_elem_lim(int64_t n, int64_t ne,
     if (sysmask & (1 << c)) cs = cs < coef[c] ? cs : coef[c];
   for (int c = 0; c < 5; ++c)
     if (sysmask & (1 << c)) coef[c] = cs;
-  for (int a = 0; a < 4; ++a) {
-    F ca[5];
-    for (int c = 0; c < 5; ++c) ca[c] = coef[c] * aec[c][a];
-    add5<kAR>(A, n, N[a], ca);
+  for (int a = 0; a < 4; ++a)
+    for (int c = 0; c < 5; ++c) ca[a][c] = coef[c] * aec[a][c];
+}
+
+// FP32: the antidiffusive contributions formed again from the FP32 state and
+// geometry (as KozCG::lim does), the limited ones added atomically.
+__global__ void __launch_bounds__(kBlock) k_elem_lim32(int64_t n, int64_t ne,
+                                                        const int32_t* __restrict__ inpoel,
+                                                        const float* __restrict__ geo,
+                                                        const float* __restrict__ Uf,
+                                                        const unsigned int* __restrict__ Q,
+                                                        double ctau_d, int sysmask, float* A) {
+  const int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (e >= ne) return;
+  const float ctau = float(ctau_d);
+  int32_t N[4];
+  for (int a = 0; a < 4; ++a) N[a] = inpoel[e * 4 + a];
+  const Geo<float> t = elem_geo<float>(nullptr, geo, n, ne, e, N);
+  float aec[4][5], ca[4][5];
+  for (int c = 0; c < 5; ++c)
+    for (int a = 0; a < 4; ++a) {
+      float s = 0.f;
+      for (int b = 0; b < 4; ++b) {
+        const float m = t.J / 120.f * ((a == b) ? 3.f : -1.f);
+        s += m * ctau * ust<float>(nullptr, Uf, n, c, N[b]);
+      }
+      aec[a][c] = s;
+    }
+  elem_limit<float>(n, N, Q, sysmask, aec, ca);
+  for (int a = 0; a < 4; ++a) add5<kAR>(A, n, N[a], ca[a]);
+}
+
+// FP64: the antidiffusive contributions are the ones the residual pass
+// stored in the residual slot records E (the values KozCG::lim forms again
+// from the same state and geometry); the limited ones go to the limited slot
+// records L.
+__global__ void __launch_bounds__(kEB) k_elem_lim64(int64_t n, int64_t ne,
+                                                     const int32_t* __restrict__ inpoel,
+                                                     const double* __restrict__ E,
+                                                     const unsigned long long* __restrict__ Q,
+                                                     int sysmask, double* __restrict__ L) {
+  __shared__ double2 st[kEB / 32][32 * kStW];
+  const int lane = threadIdx.x & 31;
+  const int64_t e = blockIdx.x * int64_t(kEB) + threadIdx.x;
+  const int64_t e0 = e - lane;
+  if (e0 >= ne) return;  // the whole warp is past the last element
+  double2* buf = st[threadIdx.x >> 5];
+  const int nv = static_cast<int>(ne - e0 < 32 ? ne - e0 : 32);
+  warp_get<4 * kRecD2>(reinterpret_cast<const double2*>(E) + e0 * 4 * kRecD2, buf, nv, lane);
+  __syncwarp();
+  double ca[4][5];
+  const bool live = e < ne;
+  if (live) {
+    int32_t N[4];
+    for (int a = 0; a < 4; ++a) N[a] = inpoel[e * 4 + a];
+    double aec[4][5];
+    for (int a = 0; a < 4; ++a) {
+      const double* rec = reinterpret_cast<const double*>(buf + lane * kStW + a * kRecD2);
+      for (int c = 0; c < 5; ++c) aec[a][c] = rec[5 + c];
+    }
+    elem_limit<double>(n, N, Q, sysmask, aec, ca);
+  }
+  __syncwarp();
+  if (live)
+    for (int a = 0; a < 4; ++a) {
+      double2* b = buf + lane * kStW + a * kLimD2;
+      b[0] = make_double2(ca[a][0], ca[a][1]);
+      b[1] = make_double2(ca[a][2], ca[a][3]);
+      b[2] = make_double2(ca[a][4], 0.0);
+    }
+  __syncwarp();
+  warp_put<4 * kLimD2>(reinterpret_cast<double2*>(L) + e0 * 4 * kLimD2, buf, nv, lane);
+}
+
+// FP64 node sums of the element contributions, in a fixed order: node i
+// adds the slots (element e, local node a) of the elements holding it in
+// ascending e -- the order of the reference's serial element loop
+// (Kozak.cpp:73-173 adds R[N[a]] per element, KozCG.cpp:794-814 and
+// 1049-1078 likewise P and A) -- so the sums are the same on every run, with
+// no atomics.  Slot q's record is RD2 double2 at E + q * RD2: entries 0..4
+// the contributions to the node's five components, and with WP entries
+// 5..9 the antidiffusive ones, summed by sign into P+ / P- (zero goes to
+// neither).  Slots as SELL-32: slice s of 32 nodes, entry k of node i at
+// soff[s] + 32 k + lane, value q, -1 padding.  The slots are taken kGB at a
+// time, their loads issued together before the adds (in slot order), so
+// that a node's loads overlap.
+template <int RD2, bool WP>
+__global__ void __launch_bounds__(kBlock) k_node_gather(int64_t n,
+                                                         const int32_t* __restrict__ soff,
+                                                         const int32_t* __restrict__ sw,
+                                                         const int32_t* __restrict__ slot,
+                                                         const double* __restrict__ E,
+                                                         double* __restrict__ R,
+                                                         double* __restrict__ P) {
+  constexpr int LD2 = WP ? 5 : 3;  // double2 read per slot
+  const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= n) return;
+  const int lane = static_cast<int>(i & 31);
+  const int64_t s = i >> 5;
+  const int32_t off = __ldg(soff + s), w = __ldg(sw + s);
+  const double2* E2 = reinterpret_cast<const double2*>(E);
+  double r[5], pp[5], pn[5];
+#pragma unroll
+  for (int c = 0; c < 5; ++c) r[c] = pp[c] = pn[c] = 0.0;
+  for (int k0 = 0; k0 < w; k0 += kGB) {
+    int32_t q[kGB];
+#pragma unroll
+    for (int j = 0; j < kGB; ++j) q[j] = k0 + j < w ? __ldg(slot + off + (k0 + j) * 32 + lane) : -1;
+    double x[kGB][2 * LD2];
+#pragma unroll
+    for (int j = 0; j < kGB; ++j) {
+      const int64_t qq = q[j] >= 0 ? q[j] : 0;  // padding reads slot 0, unused
+#pragma unroll
+      for (int k = 0; k < LD2; ++k) {
+        const double2 t = __ldg(E2 + qq * RD2 + k);
+        x[j][2 * k] = t.x;
+        x[j][2 * k + 1] = t.y;
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < kGB; ++j) {
+      if (q[j] < 0) break;  // padding only after a node's last slot
+#pragma unroll
+      for (int c = 0; c < 5; ++c) r[c] += x[j][c];
+      if constexpr (WP) {
+#pragma unroll
+        for (int c = 0; c < 5; ++c) {
+          // v > 0 and v < 0 as integer tests of the bits (NaN and -0 in
+          // neither), off GB300's narrow FP64 pipe
+          const double v = x[j][5 + c];
+          const long long b = __double_as_longlong(v);
+          const long long mag = b & 0x7fffffffffffffffll;
+          if (mag != 0 && mag <= 0x7ff0000000000000ll) {
+            if (b > 0)
+              pp[c] += v;
+            else
+              pn[c] += v;
+          }
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 5; ++c) R[c * n + i] = r[c];
+  if constexpr (WP) {
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      P[(c * 2 + 0) * n + i] = pp[c];
+      P[(c * 2 + 1) * n + i] = pn[c];
+    }
   }
 }
 
@@ -729,14 +929,27 @@ KArrays<float> arrays32(KozCGDev* d) {
 }
 
 // Node primitives and the element Galerkin (+ antidiffusive) pass on state U
-// into the accumulators k.R, k.P.
+// into the node sums R, P: in FP64 the element pass fills the residual slot
+// records and k_node_gather forms R (and P with FCT) in the FP64 arrays; in
+// FP32 it adds into the zeroed node records k.R directly.
 template <class F>
 void galerkin(cudaStream_t s, KozCGDev* d, const KArrays<F>& k, const double* U, int fct) {
   const int64_t n = d->n, ne = d->ne;
   k_node_prim<F><<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, U, d->prm.gamma, k.V, k.Uf);
-  k_elem_rhs_aec<F><<<blocks_for(ne, kBlock), kBlock, 0, s>>>(n, ne, d->inpoel, d->xyz, k.geo, U,
-                                                               k.Uf, k.V, d->scal, d->prm.gamma,
-                                                               d->prm.ctau, fct, k.R, k.P);
+  if constexpr (sizeof(F) == 8) {
+    k_elem_rhs64<<<blocks_for(ne, kEB), kEB, 0, s>>>(n, ne, d->inpoel, d->xyz, U, k.V, d->scal,
+                                                     d->prm.gamma, d->prm.ctau, fct, d->E);
+    if (fct)
+      k_node_gather<kRecD2, true><<<blocks_for(n, kBlock), kBlock, 0, s>>>(
+          n, d->soff, d->sw, d->sslot, d->E, d->R, d->P);
+    else
+      k_node_gather<kRecD2, false><<<blocks_for(n, kBlock), kBlock, 0, s>>>(
+          n, d->soff, d->sw, d->sslot, d->E, d->R, nullptr);
+  } else {
+    k_elem_rhs_aec32<<<blocks_for(ne, kBlock), kBlock, 0, s>>>(n, ne, d->inpoel, k.geo, k.Uf, k.V,
+                                                                d->scal, d->prm.gamma,
+                                                                d->prm.ctau, fct, k.R);
+  }
 }
 
 // One KozCG step with the dt already in the device scalars, element
@@ -746,16 +959,11 @@ int step_impl(xg_ctx* c, KozCGDev* d, const KArrays<F>& k) {
   cudaStream_t s = c->stream;
   const int64_t n = d->n, ne = d->ne;
   const int fct = d->prm.fct;
-  // FP64: R, A [5][n], P [10][n]; FP32: R with P [n][16], A [n][8]
+  // FP32: R with P [n][16], A [n][8] accumulate atomically from zero; FP64:
+  // R, A [5][n], P [10][n] are written whole by k_node_gather
   if (sizeof(F) == 4) {
     XG_CUDA(c, cudaMemsetAsync(k.R, 0, n * kRP * 4, s));
     if (fct) XG_CUDA(c, cudaMemsetAsync(k.A, 0, n * kAR * 4, s));
-  } else {
-    XG_CUDA(c, cudaMemsetAsync(k.R, 0, n * 5 * 8, s));
-    if (fct) {
-      XG_CUDA(c, cudaMemsetAsync(k.P, 0, n * 10 * 8, s));
-      XG_CUDA(c, cudaMemsetAsync(k.A, 0, n * 5 * 8, s));
-    }
   }
   galerkin<F>(s, d, k, d->U, fct);
   XG_CHECK_LAUNCH(c);
@@ -774,10 +982,18 @@ int step_impl(xg_ctx* c, KozCGDev* d, const KArrays<F>& k) {
     XG_CHECK_LAUNCH(c);
     k_node_lim<F><<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, d->R, d->P, k.Q);
     XG_CHECK_LAUNCH(c);
-    k_elem_lim<F><<<blocks_for(ne, kBlock), kBlock, 0, s>>>(n, ne, d->inpoel, d->xyz, k.geo,
-                                                             d->U, k.Uf, k.Q, d->prm.ctau,
-                                                             d->prm.fctsys, k.A);
-    XG_CHECK_LAUNCH(c);
+    if constexpr (sizeof(F) == 4) {
+      k_elem_lim32<<<blocks_for(ne, kBlock), kBlock, 0, s>>>(n, ne, d->inpoel, k.geo, k.Uf, k.Q,
+                                                              d->prm.ctau, d->prm.fctsys, k.A);
+      XG_CHECK_LAUNCH(c);
+    } else {
+      k_elem_lim64<<<blocks_for(ne, kEB), kEB, 0, s>>>(n, ne, d->inpoel, d->E, k.Q,
+                                                       d->prm.fctsys, d->L);
+      XG_CHECK_LAUNCH(c);
+      k_node_gather<kLimD2, false><<<blocks_for(n, kBlock), kBlock, 0, s>>>(
+          n, d->soff, d->sw, d->sslot, d->L, d->A, nullptr);
+      XG_CHECK_LAUNCH(c);
+    }
   }
   k_node_solve<F><<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, d->vol, d->R, k.A, d->A, fct,
                                                             d->isbc, d->prm.gamma, d->U,
@@ -822,26 +1038,75 @@ int xg_kozcg_setup(xg_ctx* c, const xg_kozcg_params* prm, int64_t npoin, const d
   if (prm->fctsys & ~31) return fail(c, XG_ERR_ARG, "kozcg_setup: fctsys mask beyond 5 components");
   if (prm->precision != XG_FP64 && prm->precision != XG_FP32_FLUX)
     return fail(c, XG_ERR_ARG, "kozcg_setup: unknown precision");
-  std::vector<int32_t> ip(nelem * 4);
-  for (int64_t i = 0; i < nelem * 4; ++i) {
+  for (int64_t i = 0; i < nelem * 4; ++i)
     if (inpoel[i] >= static_cast<uint64_t>(npoin))
       return fail(c, XG_ERR_ARG, "kozcg_setup: element node id out of range");
-    ip[i] = static_cast<int32_t>(inpoel[i]);
+  // Elements in the order of their smallest node id (stable counting sort),
+  // so that consecutive elements share nearby nodes: the element passes then
+  // read nearby node data, and the elements holding a run of nodes (the
+  // slots one warp of k_node_gather reads) lie in a window of the slot
+  // records about the mesh's node bandwidth wide, instead of across the
+  // whole array.  Results do not depend on the element order beyond the
+  // order of each node's sums, which stays fixed.
+  std::vector<int32_t> ip(nelem * 4);
+  {
+    std::vector<int64_t> cnt(npoin + 1, 0);
+    std::vector<int32_t> key(nelem);
+    for (int64_t e = 0; e < nelem; ++e) {
+      uint64_t m = inpoel[e * 4];
+      for (int a = 1; a < 4; ++a) m = std::min(m, inpoel[e * 4 + a]);
+      key[e] = static_cast<int32_t>(m);
+      ++cnt[m + 1];
+    }
+    for (int64_t i = 0; i < npoin; ++i) cnt[i + 1] += cnt[i];
+    for (int64_t e = 0; e < nelem; ++e) {
+      const int64_t to = cnt[key[e]]++;
+      for (int a = 0; a < 4; ++a) ip[to * 4 + a] = static_cast<int32_t>(inpoel[e * 4 + a]);
+    }
   }
   // node adjacency for the allowed limits: the elements of each node
   // (counting sort), then each node's sorted distinct element neighbours,
   // laid out as SELL-32
   const int64_t nslice = (npoin + 31) / 32;
+  const bool f64 = prm->precision == XG_FP64;
+  if (f64 && nelem * 4 >= (int64_t(1) << 31))
+    return fail(c, XG_ERR_ARG, "kozcg_setup: too many elements for FP64 slots");
   std::vector<int32_t> aoff(nslice + 1), aw(nslice), anbr;
+  // FP64 node sums: per node its (element, local node) slots e * 4 + a in
+  // ascending e, SELL-32 (slice offsets soff, widths sw, -1 padding)
+  std::vector<int32_t> soff(nslice + 1), sw(nslice), sslot;
   {
     std::vector<int64_t> eptr(npoin + 1, 0);
     for (int64_t i = 0; i < nelem * 4; ++i) ++eptr[ip[i] + 1];
     for (int64_t i = 0; i < npoin; ++i) eptr[i + 1] += eptr[i];
-    std::vector<int32_t> eln(nelem * 4);
+    std::vector<int32_t> eln(nelem * 4), els(f64 ? nelem * 4 : 0);
     {
       std::vector<int64_t> fill(eptr.begin(), eptr.end() - 1);
       for (int64_t e = 0; e < nelem; ++e)
-        for (int a = 0; a < 4; ++a) eln[fill[ip[e * 4 + a]]++] = static_cast<int32_t>(e);
+        for (int a = 0; a < 4; ++a) {
+          const int64_t k = fill[ip[e * 4 + a]]++;
+          eln[k] = static_cast<int32_t>(e);
+          if (f64) els[k] = static_cast<int32_t>(e * 4 + a);
+        }
+    }
+    if (f64) {
+      int64_t tot = 0;
+      for (int64_t sl = 0; sl < nslice; ++sl) {
+        int64_t w = 0;
+        for (int64_t i = sl * 32; i < std::min<int64_t>(npoin, sl * 32 + 32); ++i)
+          w = std::max(w, eptr[i + 1] - eptr[i]);
+        soff[sl] = static_cast<int32_t>(tot);
+        sw[sl] = static_cast<int32_t>(w);
+        tot += 32 * w;
+        if (tot >= (int64_t(1) << 31)) return fail(c, XG_ERR_ARG, "kozcg_setup: slots too many");
+      }
+      soff[nslice] = static_cast<int32_t>(tot);
+      sslot.assign(static_cast<size_t>(std::max<int64_t>(1, tot)), -1);
+      for (int64_t i = 0; i < npoin; ++i) {
+        const int64_t sl = i / 32, lane = i % 32;
+        for (int64_t k = eptr[i]; k < eptr[i + 1]; ++k)
+          sslot[soff[sl] + (k - eptr[i]) * 32 + lane] = els[k];
+      }
     }
     std::vector<int64_t> nptr(npoin + 1, 0);
     std::vector<int32_t> nb;
@@ -910,6 +1175,12 @@ int xg_kozcg_setup(xg_ctx* c, const xg_kozcg_params* prm, int64_t npoin, const d
       A.plan(d->lo32, npoin * 5);
       A.plan(d->Q32, npoin * 10);
       A.plan(d->geo32, nelem * 10);
+    } else {
+      A.plan(d->E, nelem * 4 * kRecD2 * 2);
+      if (prm->fct) A.plan(d->L, nelem * 4 * kLimD2 * 2);
+      A.plan(d->soff, soff.size());
+      A.plan(d->sw, sw.size());
+      A.plan(d->sslot, sslot.size());
     }
     A.plan(d->isbc, npoin);
     A.plan(d->scal, 1);
@@ -929,6 +1200,11 @@ int xg_kozcg_setup(xg_ctx* c, const xg_kozcg_params* prm, int64_t npoin, const d
   XG_CUDA(c, cudaMemcpy(d->aoff, aoff.data(), aoff.size() * 4, cudaMemcpyHostToDevice));
   XG_CUDA(c, cudaMemcpy(d->aw, aw.data(), aw.size() * 4, cudaMemcpyHostToDevice));
   XG_CUDA(c, cudaMemcpy(d->anbr, anbr.data(), anbr.size() * 4, cudaMemcpyHostToDevice));
+  if (f64) {
+    XG_CUDA(c, cudaMemcpy(d->soff, soff.data(), soff.size() * 4, cudaMemcpyHostToDevice));
+    XG_CUDA(c, cudaMemcpy(d->sw, sw.data(), sw.size() * 4, cudaMemcpyHostToDevice));
+    XG_CUDA(c, cudaMemcpy(d->sslot, sslot.data(), sslot.size() * 4, cudaMemcpyHostToDevice));
+  }
   XG_CUDA(c, cudaMemsetAsync(d->U, 0, npoin * 5 * 8, s));
   XG_CUDA(c, cudaMemsetAsync(d->isbc, 0, npoin, s));
   if (d->geo32) {
@@ -1065,7 +1341,6 @@ int xg_kozcg_rhs(xg_ctx* c, const double* U, double dt, double* R) {
     galerkin<float>(s, d, k, d->A, 0);
     k_rec_to_soa<<<blocks_for(d->n * 5, kBlock), kBlock, 0, s>>>(d->n, k.R, d->R);
   } else {
-    XG_CUDA(c, cudaMemsetAsync(d->R, 0, d->n * 5 * 8, s));
     galerkin<double>(s, d, arrays64(d), d->A, 0);
   }
   XG_CHECK_LAUNCH(c);
