@@ -694,14 +694,58 @@ def _cuda_profiler(on):
     (rt.cudaProfilerStart if on else rt.cudaProfilerStop)()
 
 
+def scatter_designs(n=81, reps=20):
+    """The two scatters of the RieCG edge fluxes on the same n^3 FP32 Rusanov
+    residual (drop-in riemann::rhs with host G and U): owner half-edges with
+    deposit slots (k_flux1 + k_rhs2 + k_rhs_bnd) against edge colouring (one
+    k_flux_colour launch per class of node-disjoint edges + the node
+    epilogue).  Per-kernel CUDA-event times over reps calls of each."""
+    from xyst_gb300 import lib, riecg
+
+    ops = build_ops(n, seed=0)
+    ctx = lib.Context(0)
+    r = riecg.from_operators(ctx, ops, precision="fp32")
+    U = wave_state(ops["coord"])
+    Gv = r.grad(U) / ops["vol"][:, None]
+    R0 = r.rhs(Gv, U)
+    Rc, ncol = r.rhs_coloured(Gv, U)
+    out = {"n": n, "nodes": int(ops["coord"].shape[1]), "edges": int(ops["edges"].shape[0]),
+           "colours": ncol, "reps": reps,
+           "max_rel_diff": float(np.abs(Rc - R0).max() / np.abs(R0).max())}
+    for name, call in (("owner_deposit", r.rhs), ("edge_colouring", r.rhs_coloured)):
+        r.profile(True)
+        for _ in range(reps):
+            call(Gv, U)
+        r.profile(False)
+        kt = r.kernel_times()
+        out[name] = {k: {"ms_per_call": v[0] / reps, "launches_per_call": v[1] / reps}
+                     for k, v in kt.items()}
+        out[name]["total_ms_per_call"] = sum(v[0] for v in kt.values()) / reps
+    ctx.close()
+    return out
+
+
 def profile_step(what, n):
     """One warm step of a workload bracketed by the profiler range (for
     `ncu --profile-from-start off`): chocg-fp64 (Jacobi PCG), chocg-mixed
-    (first-order factor, mixed solve), kozcg-fp64, kozcg-fp32."""
+    (first-order factor, mixed solve), kozcg-fp64, kozcg-fp32, and one FP32
+    RieCG residual by each flux scatter, riecg-rhs-owner and
+    riecg-rhs-colour."""
     from xyst_gb300 import chocg, kozcg, lib, mesh, riecg
 
     ctx = lib.Context(0)
-    if what.startswith("chocg"):
+    if what.startswith("riecg-rhs"):
+        ops = build_ops(n, seed=0)
+        r = riecg.from_operators(ctx, ops, precision="fp32")
+        U = wave_state(ops["coord"])
+        Gv = r.grad(U) / ops["vol"][:, None]
+        call = r.rhs if what == "riecg-rhs-owner" else (lambda g, u: r.rhs_coloured(g, u)[0])
+        call(Gv, U)
+        _cuda_profiler(True)
+        call(Gv, U)
+        _cuda_profiler(False)
+        out = {"profile": what, "n": n}
+    elif what.startswith("chocg"):
         m = mesh.cube(n, jitter=0.2, seed=0, numbering="random", perm_seed=1)
         ops = chocg.operators(m, sym_sets=[1, 2, 3, 4, 5, 6], hydrostat=0)
         if what == "chocg-fp64":
@@ -749,12 +793,19 @@ def main():
     ap.add_argument("--no-pcg", action="store_true", help="skip the ChoCG leg")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-mode RieCG leg")
     ap.add_argument("--profile-step", default=None,
-                    choices=["chocg-fp64", "chocg-mixed", "kozcg-fp64", "kozcg-fp32"],
+                    choices=["chocg-fp64", "chocg-mixed", "kozcg-fp64", "kozcg-fp32",
+                             "riecg-rhs-owner", "riecg-rhs-colour"],
                     help="run one warm step of that workload (side --n) inside a profiler "
                          "range and exit")
+    ap.add_argument("--scatter-designs", action="store_true",
+                    help="time the owner/deposit and edge-colouring flux scatters on the "
+                         "--n cube and exit")
     args = ap.parse_args()
     if args.profile_step:
         profile_step(args.profile_step, args.n)
+        return
+    if args.scatter_designs:
+        print(json.dumps(scatter_designs(args.n)))
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

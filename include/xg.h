@@ -117,6 +117,16 @@ int xg_riecg_grad(xg_ctx* ctx, const double* U, double* G);
  * side R (npoin x 5) from host G (volume-divided, npoin x 15) and U. */
 int xg_riecg_rhs(xg_ctx* ctx, const double* G, const double* U, double* R);
 
+/* xg_riecg_rhs computed with the edge-coloured scatter instead of owner
+ * half-edges with deposits (FP32 mode only): the edges are split into
+ * classes with no shared node (greedy colouring, built on the first call),
+ * and one launch per class updates both ends of each edge in place.  The
+ * same residual (riemann::rhs advdom, src/Physics/Riemann.cpp:652-766, adds
+ * -f and +f per edge), summed in another order.  *ncolours (may be NULL)
+ * receives the number of classes. */
+int xg_riecg_rhs_coloured(xg_ctx* ctx, const double* G, const double* U, double* R,
+                          int* ncolours);
+
 /* Apply the boundary conditions to the device state (RieCG::BC). */
 int xg_riecg_bc(xg_ctx* ctx);
 

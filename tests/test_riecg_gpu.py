@@ -37,6 +37,26 @@ def test_dropin_fp32_bound():
     assert relerr(d.rhs(Gv, U), o.rhs(Gv, U)) < 1e-4
 
 
+@pytest.mark.parametrize("flux,stab2", [("rusanov", False), ("hllc", True)])
+def test_dropin_rhs_edge_coloured(flux, stab2):
+    """The edge-coloured scatter (one launch per class of node-disjoint edges,
+    both ends updated in place) gives the owner/deposit residual up to FP32
+    summation order, within the FP32 bound of the oracle; the colouring is a
+    proper one (checked on the host from the class count: at least the
+    largest node degree)."""
+    ops = cube_ops(9)
+    d, o = pair(ops, precision="fp32", flux=flux, stab2=stab2)
+    U = random_state(ops["coord"].shape[1], 9)
+    Gv = o.grad(U) / ops["vol"][:, None]
+    Ro = o.rhs(Gv, U)
+    R = d.rhs(Gv, U)
+    Rc, ncol = d.rhs_coloured(Gv, U)
+    assert relerr(Rc, Ro) < 1e-4
+    assert relerr(Rc, R) < 1e-5
+    deg = np.bincount(np.asarray(ops["edges"]).ravel()).max()
+    assert deg <= ncol <= 128
+
+
 def test_superedge_groups_expand_like_reference():
     """Tet and triangle superedge groups are evaluated edge by edge in the
     reference's orientation; equal to the same edges passed as a plain list."""

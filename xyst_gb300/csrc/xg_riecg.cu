@@ -100,6 +100,14 @@ struct RieCGDev {
   bool dt_valid = false;
   // two whole time steps captured once and replayed (launch overhead)
   cudaGraphExec_t graph = nullptr;
+  // edge-coloured residual (xg_riecg_rhs_coloured), built on first use:
+  // colour c holds edges coff[c] .. coff[c+1] - 1 as (owner, other end) and
+  // the edge integral in the owner's orientation; cR: F [n][8] records
+  Arena colarena;
+  std::vector<int64_t> coff;
+  int2* cpq = nullptr;
+  float4* cd = nullptr;
+  float* cR = nullptr;
   // staging for the drop-in entry points
   double* stage_buf = nullptr;
   void* stage_W = nullptr;
@@ -127,7 +135,8 @@ void destroy_riecg(RieCGDev* d) {
 }
 
 size_t bytes_riecg(const RieCGDev* d) {
-  return d ? d->arena.bytes() + d->bcarena.bytes() + d->scratch.bytes() : 0;
+  return d ? d->arena.bytes() + d->bcarena.bytes() + d->scratch.bytes() + d->colarena.bytes()
+           : 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -1189,6 +1198,70 @@ __global__ void __launch_bounds__(kBlock)
   if (UPDATE && STAGE == 2) block_min_atomic(dtp, dtmin);
 }
 
+// Edge-coloured residual, the comparison design for the scatter of the
+// edge fluxes (xg_riecg_rhs_coloured, FP32 mode): the owned edges split into
+// colour classes in which no two edges share a node; one launch per class,
+// one thread per edge, evaluates the flux once (in the owner's orientation,
+// as k_flux1 does in FP32) and updates both ends' residual records in
+// place, R_p -= f and R_q += f, with plain loads and stores: no atomics and
+// no deposit slots, at the cost of one launch per colour and of scattered
+// read-modify-writes of both ends' records (riemann::rhs advdom,
+// src/Physics/Riemann.cpp:695-759, adds -f and +f the same way).
+template <int FLUX>
+__global__ void __launch_bounds__(kBlock)
+    k_flux_colour(int64_t m, const int2* __restrict__ pq, const float4* __restrict__ dd,
+                  const float* __restrict__ W, const float* __restrict__ G, double gamma_d,
+                  int stab2, double stab2coef_d, float* R) {
+  const int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (e >= m) return;
+  const float gamma = float(gamma_d), stab2coef = float(stab2coef_d);
+  const int2 ends = __ldg(pq + e);
+  const float4 d = __ldg(dd + e);
+  float wp[8], wq[8], gp[16], gq[16];
+  load8(W + int64_t(ends.x) * 8, wp);
+  load8(W + int64_t(ends.y) * 8, wq);
+  load16(G + int64_t(ends.x) * 16, gp);
+  load16(G + int64_t(ends.y) * 16, gq);
+  const float v0 = wq[5] - wp[5], v1 = wq[6] - wp[6], v2 = wq[7] - wp[7];
+  float g1[5], g2[5], f[5];
+#pragma unroll
+  for (int c = 0; c < 5; ++c) {
+    g1[c] = proj(gp + 3 * c, v0, v1, v2);
+    g2[c] = proj(gq + 3 * c, v0, v1, v2);
+  }
+  if (FLUX == XG_HLLC)
+    hllc(wp, wq, g1, g2, d.x, d.y, d.z, gamma, stab2 != 0, stab2coef, f);
+  else
+    rusanov(wp, wq, g1, g2, d.x, d.y, d.z, gamma, stab2 != 0, stab2coef, f);
+  // each record is read and written by this thread alone in this launch
+  float rp[8], rq[8];
+  load8(R + int64_t(ends.x) * 8, rp);
+  load8(R + int64_t(ends.y) * 8, rq);
+#pragma unroll
+  for (int c = 0; c < 5; ++c) {
+    rp[c] -= f[c];
+    rq[c] += f[c];
+  }
+  store8(R + int64_t(ends.x) * 8, rp);
+  store8(R + int64_t(ends.y) * 8, rq);
+}
+
+// The coloured residual's node epilogue: the domain sums plus, at boundary
+// nodes, the boundary integral (in the reference's order), as FP64
+// node-major output.
+__global__ void __launch_bounds__(kBlock)
+    k_colour_out(int64_t n, const float* __restrict__ R, Bnd bnd, const float* __restrict__ W,
+                 double gamma, double* __restrict__ Rout) {
+  const int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (p >= n) return;
+  float r[8];
+  load8(R + p * 8, r);
+  const int32_t bi = __ldg(bnd.bidx + p);
+  if (bi >= 0) rhs_bnd_term(bnd, bi, W, float(gamma), r);
+#pragma unroll
+  for (int c = 0; c < 5; ++c) Rout[p * 5 + c] = double(r[c]);
+}
+
 // Nodal BCs on the device state (RieCG::BC), one thread per BC node; refreshes
 // the node's primitive record and, when asked, its CFL dt.
 template <class F>
@@ -2052,6 +2125,121 @@ int rhs_dropin(xg_ctx* c, RieCGDev* d, const double* G, const double* U, double*
   XG_CUDA(c, cudaStreamSynchronize(c->stream));
   return XG_OK;
 }
+
+// Greedy colouring of the owned edges (list 1, read back from the device):
+// each edge, in owner order, takes the lowest colour neither end uses yet
+// (at most 2 x max degree - 1 colours; 128 supported), then the edges are
+// grouped by colour, owner order kept within a colour.
+int build_colours(xg_ctx* c, RieCGDev* d) {
+  if (!d->coff.empty()) return XG_OK;
+  const int64_t n = d->n, nslice = (n + kSlice - 1) / kSlice;
+  std::vector<int32_t> soff1(nslice + 1), sw1(nslice);
+  std::vector<int4> e1(std::max<int64_t>(1, d->nent1));
+  XG_CUDA(c, cudaStreamSynchronize(c->stream));
+  XG_CUDA(c, cudaMemcpy(soff1.data(), d->soff1, soff1.size() * 4, cudaMemcpyDeviceToHost));
+  XG_CUDA(c, cudaMemcpy(sw1.data(), d->sw1, sw1.size() * 4, cudaMemcpyDeviceToHost));
+  if (d->nent1)
+    XG_CUDA(c, cudaMemcpy(e1.data(), d->ent1, d->nent1 * sizeof(int4), cudaMemcpyDeviceToHost));
+  std::vector<int2> pq;
+  std::vector<float4> dd;
+  for (int64_t p = 0; p < n; ++p) {
+    const int64_t s2 = p / kSlice, lane = p % kSlice;
+    for (int64_t k = 0; k < sw1[s2]; ++k) {
+      const int4 v = e1[soff1[s2] + k * kSlice + lane];
+      if (v.x == kPad) continue;
+      float x, y, z;
+      std::memcpy(&x, &v.y, 4);
+      std::memcpy(&y, &v.z, 4);
+      std::memcpy(&z, &v.w, 4);
+      const float sg = v.x >= 0 ? 1.f : -1.f;  // owner's orientation
+      pq.push_back(make_int2(static_cast<int>(p), v.x >= 0 ? v.x : ~v.x));
+      dd.push_back(make_float4(sg * x, sg * y, sg * z, 0.f));
+    }
+  }
+  const int64_t m = static_cast<int64_t>(pq.size());
+  std::vector<uint64_t> used(2 * n, 0);
+  std::vector<int32_t> col(m);
+  int ncol = 0;
+  for (int64_t e = 0; e < m; ++e) {
+    const int64_t a = pq[e].x, b = pq[e].y;
+    int k = -1;
+    for (int w = 0; w < 2 && k < 0; ++w) {
+      const uint64_t busy = used[2 * a + w] | used[2 * b + w];
+      if (~busy) k = 64 * w + __builtin_ctzll(~busy);
+    }
+    if (k < 0) return fail(c, XG_ERR_ARG, "rhs_coloured: more than 128 edge colours");
+    used[2 * a + k / 64] |= uint64_t(1) << (k % 64);
+    used[2 * b + k / 64] |= uint64_t(1) << (k % 64);
+    col[e] = k;
+    ncol = std::max(ncol, k + 1);
+  }
+  std::vector<int64_t> off(ncol + 1, 0);
+  for (int64_t e = 0; e < m; ++e) ++off[col[e] + 1];
+  for (int k = 0; k < ncol; ++k) off[k + 1] += off[k];
+  std::vector<int2> spq(std::max<int64_t>(1, m));
+  std::vector<float4> sdd(std::max<int64_t>(1, m));
+  {
+    std::vector<int64_t> fill(off.begin(), off.end() - 1);
+    for (int64_t e = 0; e < m; ++e) {
+      const int64_t to = fill[col[e]]++;
+      spq[to] = pq[e];
+      sdd[to] = dd[e];
+    }
+  }
+  d->colarena.release();
+  for (int pass = 0; pass < 2; ++pass) {
+    Arena& A = d->colarena;
+    A.plan(d->cpq, spq.size());
+    A.plan(d->cd, sdd.size());
+    A.plan(d->cR, n * 8);
+    if (pass == 0) XG_CUDA(c, A.reserve());
+  }
+  XG_CUDA(c, cudaMemcpy(d->cpq, spq.data(), spq.size() * sizeof(int2), cudaMemcpyHostToDevice));
+  XG_CUDA(c, cudaMemcpy(d->cd, sdd.data(), sdd.size() * sizeof(float4), cudaMemcpyHostToDevice));
+  d->coff = off;
+  return XG_OK;
+}
+
+template <int FLUX>
+int launch_colours(xg_ctx* c, RieCGDev* d, const float* W, const float* G) {
+  for (size_t k = 0; k + 1 < d->coff.size(); ++k) {
+    const int64_t m = d->coff[k + 1] - d->coff[k];
+    if (m == 0) continue;
+    XG_PROF_LAUNCH(c, d, "riecg_flux_colour",
+                   (k_flux_colour<FLUX><<<blocks_for(m, kBlock), kBlock, 0, c->stream>>>(
+                       m, d->cpq + d->coff[k], d->cd + d->coff[k], W, G, d->prm.gamma,
+                       d->prm.stab2, d->prm.stab2coef, d->cR)));
+  }
+  return XG_OK;
+}
+
+// xg_riecg_rhs with the edge-coloured scatter (FP32 mode).
+int rhs_dropin_coloured(xg_ctx* c, RieCGDev* d, const double* G, const double* U, double* R) {
+  int rc = build_colours(c, d);
+  if (rc) return rc;
+  float* W = static_cast<float*>(d->stage_W);
+  float* Gr = static_cast<float*>(d->stage_G);
+  XG_CUDA(c, cudaMemcpyAsync(d->stage_buf, G, d->n * 15 * sizeof(double), cudaMemcpyHostToDevice,
+                             c->stream));
+  k_aos_to_grec<float><<<blocks_for(d->n * 16, kBlock), kBlock, 0, c->stream>>>(d->n, d->stage_buf,
+                                                                                 Gr);
+  XG_CHECK_LAUNCH(c);
+  XG_CUDA(c, cudaMemcpyAsync(d->stage_buf, U, d->n * 5 * sizeof(double), cudaMemcpyHostToDevice,
+                             c->stream));
+  k_prim_aos<float><<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(d->n, d->stage_buf, W, W);
+  XG_CHECK_LAUNCH(c);
+  XG_CUDA(c, cudaMemsetAsync(d->cR, 0, d->n * 8 * sizeof(float), c->stream));
+  rc = d->prm.flux == XG_HLLC ? launch_colours<XG_HLLC>(c, d, W, Gr)
+                              : launch_colours<XG_RUSANOV>(c, d, W, Gr);
+  if (rc) return rc;
+  XG_PROF_LAUNCH(c, d, "riecg_colour_out",
+                 (k_colour_out<<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(
+                     d->n, d->cR, bnd_of(d), W, d->prm.gamma, d->stage_buf)));
+  XG_CUDA(c, cudaMemcpyAsync(R, d->stage_buf, d->n * 5 * sizeof(double), cudaMemcpyDeviceToHost,
+                             c->stream));
+  XG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return XG_OK;
+}
 }  // namespace
 
 extern "C" {
@@ -2072,6 +2260,21 @@ int xg_riecg_rhs(xg_ctx* c, const double* G, const double* U, double* R) {
   if (!d) return fail(c, XG_ERR_STATE, "riecg_rhs before riecg_setup");
   if (!U || !G || !R) return fail(c, XG_ERR_ARG, "riecg_rhs: null array");
   return d->fp32 ? rhs_dropin<float>(c, d, G, U, R) : rhs_dropin<double>(c, d, G, U, R);
+}
+
+int xg_riecg_rhs_coloured(xg_ctx* c, const double* G, const double* U, double* R, int* ncolours) {
+  XG_HOST_TRY
+  int rc = use(c);
+  if (rc) return rc;
+  RieCGDev* d = c->riecg;
+  if (!d) return fail(c, XG_ERR_STATE, "riecg_rhs_coloured before riecg_setup");
+  if (!d->fp32) return fail(c, XG_ERR_STATE, "riecg_rhs_coloured: FP32 mode only");
+  if (!U || !G || !R) return fail(c, XG_ERR_ARG, "riecg_rhs_coloured: null array");
+  rc = rhs_dropin_coloured(c, d, G, U, R);
+  if (rc) return rc;
+  if (ncolours) *ncolours = static_cast<int>(d->coff.size()) - 1;
+  return XG_OK;
+  XG_HOST_CATCH(c)
 }
 
 int xg_riecg_bc(xg_ctx* c) {
@@ -2238,14 +2441,27 @@ int xg_riecg_run(xg_ctx* c, int64_t nstep, double* dts, float* ms) {
 
 int xg_riecg_profile(xg_ctx* c, int enable) {
   if (!c || !c->riecg) return fail(c, XG_ERR_STATE, "riecg_profile before riecg_setup");
-  c->riecg->prof = enable != 0;
-  if (enable) c->riecg->ktimes.clear();
+  RieCGDev* d = c->riecg;
+  if (enable) {
+    // a fresh record: launches still pending from an earlier one are dropped
+    XG_CUDA(c, cudaStreamSynchronize(c->stream));
+    for (auto& p : d->pending) {
+      cudaEventDestroy(p.second.first);
+      cudaEventDestroy(p.second.second);
+    }
+    d->pending.clear();
+    d->ktimes.clear();
+  }
+  d->prof = enable != 0;
   return XG_OK;
 }
 
 int xg_riecg_kernel_times(xg_ctx* c, int cap, const char** names, double* ms, int64_t* launches,
                           int* n) {
   if (!c || !c->riecg) return fail(c, XG_ERR_STATE, "riecg_kernel_times before riecg_setup");
+  // launches of the drop-in entry points are still pending here
+  const int rc = flush_profile(c, c->riecg);
+  if (rc) return rc;
   auto& kt = c->riecg->ktimes;
   if (n) *n = static_cast<int>(kt.size());
   for (int i = 0; i < cap && i < static_cast<int>(kt.size()); ++i) {

@@ -240,6 +240,15 @@ class RieCG:
         self.ctx.check(self.lib.xg_riecg_rhs(self.ctx.h, p(G), p(U), p(R)))
         return R
 
+    def rhs_coloured(self, G, U):
+        """rhs() by the edge-coloured scatter (FP32 mode): (R, colours)."""
+        G = f64(G)
+        U = f64(U)
+        R = np.zeros((self.n, 5))
+        k = C.c_int(0)
+        self.ctx.check(self.lib.xg_riecg_rhs_coloured(self.ctx.h, p(G), p(U), p(R), C.byref(k)))
+        return R, k.value
+
     def set_state(self, U, t=0.0):
         U = f64(U)
         assert U.shape == (self.n, 5)
