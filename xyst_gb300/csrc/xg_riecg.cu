@@ -268,9 +268,9 @@ __device__ __forceinline__ void block_min_atomic(double v, unsigned long long* d
 // the projections g1 = G_L.(x_R - x_L), g2 = G_R.(x_R - x_L).  The van Leer
 // limiter of a pair, phi(r) = (|r| + r)/(|r| + 1) at r = a/b and at 1/r, is
 // the same pair of numbers as 2|a|/(|a|+|b|), 2|b|/(|a|+|b|) for a b > 0 and
-// 0, 0 otherwise: both precisions evaluate that form, with one division (FP64)
-// or one reciprocal (FP32) per side instead of the reference's four
-// divisions per side (the difference is rounding, ~1e-16 relative).
+// 0, 0 otherwise: FP64 evaluates that form, with one division per side
+// instead of the reference's four (the difference is rounding, ~1e-16
+// relative); FP32 goes on to the harmonic slope it amounts to (below).
 template <class F>
 __device__ __forceinline__ void muscl(const F wl[5], const F wr[5], const F g1[5],
                                       const F g2[5], F l[5], F r[5]) {
@@ -294,12 +294,17 @@ __device__ __forceinline__ void muscl(const F wl[5], const F wr[5], const F g1[5
       l[c] = wl[c] + F(0.25) * (d1[c] * (F(1.0) - k) * phiL + d2 * (F(1.0) + k) * phiLi);
       r[c] = wr[c] - F(0.25) * (d3[c] * (F(1.0) - k) * phiR + d2 * (F(1.0) + k) * phiRi);
     } else {
-      float a = d2 + eps, b = d1[c] + eps, e3 = d3[c] + eps;
-      float aa = fabsf(a), ab = fabsf(b), ae = fabsf(e3);
-      float iL = (a * b > 0.f) ? __fdividef(0.5f, aa + ab) : 0.f;
-      float iR = (a * e3 > 0.f) ? __fdividef(0.5f, aa + ae) : 0.f;
-      l[c] = wl[c] + iL * (d1[c] * (1.f - k) * aa + d2 * (1.f + k) * ab);
-      r[c] = wr[c] - iR * (d3[c] * (1.f - k) * aa + d2 * (1.f + k) * ae);
+      // FP32: with a = d2 + eps, b = d1 + eps of one sign s, the limited
+      // slope (1-k) d1 phiL + (1+k) d2 phiLi = ((1-k) d1 |a| + (1+k) d2 |b|)
+      // 2/(|a|+|b|) is 4 s|a||b|/(|a|+|b|) - 4 eps w, w in [1-k, 1+k]/2, so
+      // the reconstruction (a quarter of it) is the harmonic slope
+      // a b/(a + b) shifted by eps w (at most 7e-10, far below FP32
+      // rounding): one product, one sum and one quotient per side
+      (void)k;
+      const float a = d2 + eps, b = d1[c] + eps, e3 = d3[c] + eps;
+      const float pl = a * b, pr = a * e3;
+      l[c] = wl[c] + (pl > 0.f ? __fdividef(pl, a + b) : 0.f);
+      r[c] = wr[c] - (pr > 0.f ? __fdividef(pr, a + e3) : 0.f);
     }
   }
   if (wl[0] < d1[0] || wl[4] < d1[4]) {
