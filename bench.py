@@ -570,18 +570,20 @@ def fp64_leg(ctx, ops, r, U0, prec, args, acc_steps=200):
     nedge = ops["edges"].shape[0]
     out = {"workload": "the same cube, state and steps in FP64 mode (gradients, fluxes and "
                        "update in FP64, the reference's operation order apart from the van "
-                       "Leer pair's one division per side)",
+                       "Leer limiter in an algebraically equal form with one division for its "
+                       "ten quotients, and the sound speed times |D| as one root)",
            "steps": k64, "ms_per_step": ms / k64, "value": n * k64 / (ms / 1e3), "unit": UNIT,
            "kernels": {k: {"ms_total": v[0], "launches": v[1]} for k, v in kt.items()}}
     # FP64 roofline of the flux kernel: its operation count per edge from the
-    # source (10 three-term projections 50, MUSCL 5 x 34 with one division per
-    # component, Rusanov 94 with 3 square roots, the two residual shares 15:
-    # 329 FP64 operations, each division or square root counted once) against
-    # the FP64 peak measured here (cuBLAS DGEMM), and its bytes against HBM
+    # source (10 three-term projections 50; MUSCL 5 x 25 + 28, the ten
+    # quotients from one division by batch inversion; Rusanov 93 with 2 square
+    # roots; the two residual shares 15: 311 FP64 operations, a multiply-add
+    # counted as two, each division or square root once) against the FP64
+    # peak measured here (cuBLAS DGEMM), and its bytes against HBM
     if "riecg_flux" in kt:
         fl_ms = kt["riecg_flux"][0] / kt["riecg_flux"][1]
         peak64 = fp64_peak_tflops()
-        flops = 329.0 * nedge
+        flops = 311.0 * nedge
         kb = kernel_bytes(n, nedge, ops["tri"].shape[0], False)
         hbm, kind = peaks()
         out["flux_roofline"] = {

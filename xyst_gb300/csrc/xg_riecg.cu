@@ -268,32 +268,69 @@ __device__ __forceinline__ void block_min_atomic(double v, unsigned long long* d
 // the projections g1 = G_L.(x_R - x_L), g2 = G_R.(x_R - x_L).  The van Leer
 // limiter of a pair, phi(r) = (|r| + r)/(|r| + 1) at r = a/b and at 1/r, is
 // the same pair of numbers as 2|a|/(|a|+|b|), 2|b|/(|a|+|b|) for a b > 0 and
-// 0, 0 otherwise: FP64 evaluates that form, with one division per side
-// instead of the reference's four (the difference is rounding, ~1e-16
-// relative); FP32 goes on to the harmonic slope it amounts to (below).
+// 0, 0 otherwise.  Both precisions reduce the limited reconstruction
+// algebraically (below): FP64 exactly, with one division for all ten
+// quotients instead of the reference's four per side (the difference is
+// rounding, a few 1e-16 of the increment); FP32 to the harmonic slope.
 template <class F>
 __device__ __forceinline__ void muscl(const F wl[5], const F wr[5], const F g1[5],
                                       const F g2[5], F l[5], F r[5]) {
   const F eps = F(1.0e-9);
   const F k = F(1.0) / F(3.0);
   F d1[5], d3[5];
+  if constexpr (sizeof(F) == 8) {
+    // FP64: with a = d2 + eps, b = d1 + eps of one sign s (a b > 0), the
+    // reconstruction wl + ((1-k) d1 phiL + (1+k) d2 phiLi) / 4 is, exactly,
+    // wl + (a b - s (eps/2) ((1-k)|a| + (1+k)|b|)) / (a + b), and the right
+    // state likewise with e = d3 + eps (the reference's form up to rounding,
+    // a few 1e-16 of the increment).  The ten quotients come from one
+    // division (batch inversion: prefix products, one reciprocal,
+    // back-substitution); an unused denominator (a b <= 0) counts as 1, and
+    // a product outside [1e-290, 1e290] falls back to ten divisions.
+    const F h = F(0.5) * eps;
+    F d2[5], num[10], den[10], pre[10];
 #pragma unroll
-  for (int c = 0; c < 5; ++c) {
-    F d2 = wr[c] - wl[c];
-    d1[c] = F(2.0) * g1[c] - d2;
-    d3[c] = F(2.0) * g2[c] - d2;
-    if constexpr (sizeof(F) == 8) {
-      const F a = d2 + eps, b = d1[c] + eps, e3 = d3[c] + eps;
-      const F aa = fabs(a), ab = fabs(b), ae = fabs(e3);
-      // both sides' 2/(|a|+|b|) from one division: 2/((|a|+|b|)(|a|+|e|))
-      const F sL = aa + ab, sR = aa + ae;
-      const F q2 = F(2.0) / (sL * sR);
-      const F iL = (a * b > F(0)) ? q2 * sR : F(0);
-      const F iR = (a * e3 > F(0)) ? q2 * sL : F(0);
-      const F phiL = aa * iL, phiLi = ab * iL, phiR = aa * iR, phiRi = ae * iR;
-      l[c] = wl[c] + F(0.25) * (d1[c] * (F(1.0) - k) * phiL + d2 * (F(1.0) + k) * phiLi);
-      r[c] = wr[c] - F(0.25) * (d3[c] * (F(1.0) - k) * phiR + d2 * (F(1.0) + k) * phiRi);
+    for (int c = 0; c < 5; ++c) {
+      d2[c] = wr[c] - wl[c];
+      d1[c] = F(2.0) * g1[c] - d2[c];
+      d3[c] = F(2.0) * g2[c] - d2[c];
+      const F a = d2[c] + eps, b = d1[c] + eps, e3 = d3[c] + eps;
+      const F pl = a * b, pr = a * e3;
+      const F sh = copysign(h, a);
+      const F ka = (F(1.0) - k) * fabs(a);
+      num[2 * c] = pl > F(0) ? pl - sh * (ka + (F(1.0) + k) * fabs(b)) : F(0);
+      num[2 * c + 1] = pr > F(0) ? pr - sh * (ka + (F(1.0) + k) * fabs(e3)) : F(0);
+      den[2 * c] = pl > F(0) ? a + b : F(1);
+      den[2 * c + 1] = pr > F(0) ? a + e3 : F(1);
+    }
+    pre[0] = den[0];
+#pragma unroll
+    for (int m = 1; m < 10; ++m) pre[m] = pre[m - 1] * den[m];
+    F q[10];
+    const F ap = fabs(pre[9]);
+    if (ap > F(1e-290) && ap < F(1e290)) {
+      F inv = F(1.0) / pre[9];
+#pragma unroll
+      for (int m = 9; m > 0; --m) {
+        q[m] = inv * pre[m - 1];
+        inv *= den[m];
+      }
+      q[0] = inv;
     } else {
+#pragma unroll
+      for (int m = 0; m < 10; ++m) q[m] = F(1.0) / den[m];
+    }
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      l[c] = wl[c] + num[2 * c] * q[2 * c];
+      r[c] = wr[c] - num[2 * c + 1] * q[2 * c + 1];
+    }
+  } else {
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      const float d2 = wr[c] - wl[c];
+      d1[c] = 2.f * g1[c] - d2;
+      d3[c] = 2.f * g2[c] - d2;
       // FP32: with a = d2 + eps, b = d1 + eps of one sign s, the limited
       // slope (1-k) d1 phiL + (1+k) d2 phiLi = ((1-k) d1 |a| + (1+k) d2 |b|)
       // 2/(|a|+|b|) is 4 s|a||b|/(|a|+|b|) - 4 eps w, w in [1-k, 1+k]/2, so
@@ -341,13 +378,15 @@ __device__ __forceinline__ void rusanov(const F wl[5], const F wr[5], const F g1
   r[1] *= r[0];
   r[2] *= r[0];
   r[3] *= r[0];
-  F len = xsqrt(nx * nx + ny * ny + nz * nz);
   // sound speed^2 = gamma p / rho with p = rho e (gamma - 1): gamma (gamma - 1) e
   // (the reference divides p by rho; the same value up to rounding); e is
   // the reconstructed internal energy, kept in cLe / cRe before the
-  // conversion to total energy below
-  F sl = fabs(vnL) + xsqrt(gamma * (gamma - F(1.0)) * cLe) * len;
-  F sr = fabs(vnR) + xsqrt(gamma * (gamma - F(1.0)) * cRe) * len;
+  // conversion to total energy below.  c |D| is taken as one root,
+  // sqrt(gamma (gamma - 1) e |D|^2), where the reference multiplies the
+  // roots of the two (the same value up to rounding; one square root fewer)
+  const F gl = gamma * (gamma - F(1.0)) * (nx * nx + ny * ny + nz * nz);
+  F sl = fabs(vnL) + xsqrt(gl * cLe);
+  F sr = fabs(vnR) + xsqrt(gl * cRe);
   F fw = sl > sr ? sl : sr;
   f[0] = l[0] * vnL + r[0] * vnR + fw * (r[0] - l[0]);
   f[1] = l[1] * vnL + r[1] * vnR + (pL + pR) * nx + fw * (r[1] - l[1]);
