@@ -326,22 +326,50 @@ __device__ __forceinline__ void muscl(const F wl[5], const F wr[5], const F g1[5
       r[c] = wr[c] - num[2 * c + 1] * q[2 * c + 1];
     }
   } else {
+    // FP32: with a = d2 + eps, b = d1 + eps of one sign s, the limited
+    // slope (1-k) d1 phiL + (1+k) d2 phiLi = ((1-k) d1 |a| + (1+k) d2 |b|)
+    // 2/(|a|+|b|) is 4 s|a||b|/(|a|+|b|) - 4 eps w, w in [1-k, 1+k]/2, so
+    // the reconstruction (a quarter of it) is the harmonic slope
+    // a b/(a + b) shifted by eps w (at most 7e-10, far below FP32
+    // rounding): one product, one sum and one quotient per side.
+    // Components 0-1 and 2-3 go through the packed FP32x2 pipe (two
+    // components per instruction, each rounded as its scalar FMA), 4 alone.
+    (void)k;
 #pragma unroll
-    for (int c = 0; c < 5; ++c) {
-      const float d2 = wr[c] - wl[c];
-      d1[c] = 2.f * g1[c] - d2;
-      d3[c] = 2.f * g2[c] - d2;
-      // FP32: with a = d2 + eps, b = d1 + eps of one sign s, the limited
-      // slope (1-k) d1 phiL + (1+k) d2 phiLi = ((1-k) d1 |a| + (1+k) d2 |b|)
-      // 2/(|a|+|b|) is 4 s|a||b|/(|a|+|b|) - 4 eps w, w in [1-k, 1+k]/2, so
-      // the reconstruction (a quarter of it) is the harmonic slope
-      // a b/(a + b) shifted by eps w (at most 7e-10, far below FP32
-      // rounding): one product, one sum and one quotient per side
-      (void)k;
-      const float a = d2 + eps, b = d1[c] + eps, e3 = d3[c] + eps;
+    for (int c = 0; c < 4; c += 2) {
+      const float2 m1 = make_float2(-1.f, -1.f), two = make_float2(2.f, 2.f),
+                   e2 = make_float2(eps, eps);
+      const float2 wl2 = make_float2(wl[c], wl[c + 1]), wr2 = make_float2(wr[c], wr[c + 1]);
+      const float2 nd2 = __ffma2_rn(wr2, m1, wl2);  // -(wr - wl)
+      const float2 dd1 = __ffma2_rn(make_float2(g1[c], g1[c + 1]), two, nd2);
+      const float2 dd3 = __ffma2_rn(make_float2(g2[c], g2[c + 1]), two, nd2);
+      const float2 a = __ffma2_rn(nd2, m1, e2);
+      const float2 b = __fadd2_rn(dd1, e2), e3 = __fadd2_rn(dd3, e2);
+      const float2 pl = __fmul2_rn(a, b), pr = __fmul2_rn(a, e3);
+      const float2 sl = __fadd2_rn(a, b), sr = __fadd2_rn(a, e3);
+      const float2 isl = make_float2(__fdividef(1.f, sl.x), __fdividef(1.f, sl.y));
+      const float2 isr = make_float2(__fdividef(1.f, sr.x), __fdividef(1.f, sr.y));
+      const float2 ql = __fmul2_rn(pl, isl), qr = __fmul2_rn(pr, isr);
+      const float2 lz = make_float2(pl.x > 0.f ? ql.x : 0.f, pl.y > 0.f ? ql.y : 0.f);
+      const float2 rz = make_float2(pr.x > 0.f ? qr.x : 0.f, pr.y > 0.f ? qr.y : 0.f);
+      const float2 l2 = __fadd2_rn(wl2, lz), r2 = __ffma2_rn(rz, m1, wr2);
+      d1[c] = dd1.x;
+      d1[c + 1] = dd1.y;
+      d3[c] = dd3.x;
+      d3[c + 1] = dd3.y;
+      l[c] = l2.x;
+      l[c + 1] = l2.y;
+      r[c] = r2.x;
+      r[c + 1] = r2.y;
+    }
+    {
+      const float d2 = wr[4] - wl[4];
+      d1[4] = 2.f * g1[4] - d2;
+      d3[4] = 2.f * g2[4] - d2;
+      const float a = d2 + eps, b = d1[4] + eps, e3 = d3[4] + eps;
       const float pl = a * b, pr = a * e3;
-      l[c] = wl[c] + (pl > 0.f ? __fdividef(pl, a + b) : 0.f);
-      r[c] = wr[c] - (pr > 0.f ? __fdividef(pr, a + e3) : 0.f);
+      l[4] = wl[4] + (pl > 0.f ? __fdividef(pl, a + b) : 0.f);
+      r[4] = wr[4] - (pr > 0.f ? __fdividef(pr, a + e3) : 0.f);
     }
   }
   if (wl[0] < d1[0] || wl[4] < d1[4]) {
@@ -565,6 +593,50 @@ __device__ __forceinline__ F proj(const F* g, F v0, F v1, F v2) {
   return g[0] * v0 + g[1] * v1 + g[2] * v2;
 }
 
+// Slot of gradient component c, direction j in a G record.  FP64: 3c + j.
+// FP32 pairs components for the packed FP32x2 pipe:
+//   [c0x c1x | c0y c1y | c0z c1z | c2x c3x | c2y c3y | c2z c3z | c4x c4y | c4z pad]
+template <class F>
+__host__ __device__ constexpr int gslot(int c, int j) {
+  return sizeof(F) == 8 ? 3 * c + j : c < 2 ? 2 * j + c : c < 4 ? 6 + 2 * j + (c - 2) : 12 + j;
+}
+// Canonical gradients g[3c + j] to a record and back (register renaming).
+template <class F>
+__device__ __forceinline__ void to_rec(const F g[16], F o[16]) {
+#pragma unroll
+  for (int c = 0; c < 5; ++c)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) o[gslot<F>(c, j)] = g[3 * c + j];
+  o[15] = F(0);
+}
+template <class F>
+__device__ __forceinline__ void from_rec(const F o[16], F g[16]) {
+#pragma unroll
+  for (int c = 0; c < 5; ++c)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) g[3 * c + j] = o[gslot<F>(c, j)];
+  g[15] = F(0);
+}
+
+// The five projections G.v at one end from an FP32 record (paired layout):
+// components 0-1 and 2-3 two per packed FP32x2 instruction, 4 alone; the
+// same expression at both ends, as proj.
+__device__ __forceinline__ void proj5(const float g[16], float v0, float v1, float v2,
+                                      float o[5]) {
+  const float2 V0 = make_float2(v0, v0), V1 = make_float2(v1, v1), V2 = make_float2(v2, v2);
+  float2 t = __fmul2_rn(make_float2(g[0], g[1]), V0);
+  t = __ffma2_rn(make_float2(g[2], g[3]), V1, t);
+  t = __ffma2_rn(make_float2(g[4], g[5]), V2, t);
+  float2 u = __fmul2_rn(make_float2(g[6], g[7]), V0);
+  u = __ffma2_rn(make_float2(g[8], g[9]), V1, u);
+  u = __ffma2_rn(make_float2(g[10], g[11]), V2, u);
+  o[0] = t.x;
+  o[1] = t.y;
+  o[2] = u.x;
+  o[3] = u.y;
+  o[4] = fmaf(g[14], v2, fmaf(g[13], v1, g[12] * v0));
+}
+
 // Node-major (host layout) <-> SoA.
 __global__ void k_aos_to_soa(int64_t n, int nc, const double* __restrict__ a,
                              double* __restrict__ s) {
@@ -607,7 +679,7 @@ __global__ void k_grec_to_aos(int64_t n, const F* __restrict__ G, double* __rest
   if (i >= n * 15) return;
   int64_t p = i / 15;
   int c = static_cast<int>(i - p * 15);
-  a[i] = double(G[p * 16 + c]);
+  a[i] = double(G[p * 16 + gslot<F>(c / 3, c % 3)]);
 }
 template <class F>
 __global__ void k_aos_to_grec(int64_t n, const double* __restrict__ a, F* __restrict__ G) {
@@ -615,7 +687,16 @@ __global__ void k_aos_to_grec(int64_t n, const double* __restrict__ a, F* __rest
   if (i >= n * 16) return;
   int64_t p = i / 16;
   int c = static_cast<int>(i - p * 16);
-  G[i] = c < 15 ? F(a[p * 15 + c]) : F(0);
+  if (c == 15) {
+    G[i] = F(0);
+    return;
+  }
+  // the canonical index held by slot c
+  int k = c;
+  for (int cc = 0; cc < 5; ++cc)
+    for (int j = 0; j < 3; ++j)
+      if (gslot<F>(cc, j) == c) k = 3 * cc + j;
+  G[i] = F(a[p * 15 + k]);
 }
 
 template <class F>
@@ -759,7 +840,9 @@ __global__ void __launch_bounds__(GradShape<F>::BLOCK)
     finish_grad(g, divide, vol, aux, p, o);
   }
   o[15] = F(0);
-  store16(G + p * 16, o);
+  F rec[16];
+  to_rec(o, rec);
+  store16(G + p * 16, rec);
 }
 
 // Boundary-triangle term of riemann::grad (src/Physics/Riemann.cpp:329-364)
@@ -798,13 +881,15 @@ __global__ void __launch_bounds__(kBlock) k_grad_bnd(int64_t nbn, Bnd bnd,
   const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (i >= nbn) return;
   const int64_t p = __ldg(bnd.bnode + i);
-  F g[16];
-  load16(G + p * 16, g);
+  F rec[16], g[16];
+  load16(G + p * 16, rec);
+  from_rec(rec, g);
   grad_bnd_term(bnd, static_cast<int32_t>(i), W, g);
   F o[16];
   finish_grad(g, divide, vol, aux, p, o);
   o[15] = F(0);
-  store16(G + p * 16, o);
+  to_rec(o, rec);
+  store16(G + p * 16, rec);
 }
 
 // FP32-mode per-node CFL time step from the FP64 state (the formula of
@@ -888,11 +973,8 @@ __global__ void __launch_bounds__(kBlock, sizeof(F) == 4 ? 3 : 1)
       // differs from the canonical-orientation flux only through the
       // limiter's 1e-9 regularisation, far below FP32 rounding of the sums
       F g1[5], g2[5];
-#pragma unroll
-      for (int c = 0; c < 5; ++c) {
-        g1[c] = proj(gp + 3 * c, v0, v1, v2);
-        g2[c] = proj(gq + 3 * c, v0, v1, v2);
-      }
+      proj5(gp, v0, v1, v2, g1);
+      proj5(gq, v0, v1, v2, g2);
       if (!first) {
         d0 = -d0;
         d1 = -d1;
@@ -1268,11 +1350,8 @@ __global__ void __launch_bounds__(kBlock)
   load16(G + int64_t(ends.y) * 16, gq);
   const float v0 = wq[5] - wp[5], v1 = wq[6] - wp[6], v2 = wq[7] - wp[7];
   float g1[5], g2[5], f[5];
-#pragma unroll
-  for (int c = 0; c < 5; ++c) {
-    g1[c] = proj(gp + 3 * c, v0, v1, v2);
-    g2[c] = proj(gq + 3 * c, v0, v1, v2);
-  }
+  proj5(gp, v0, v1, v2, g1);
+  proj5(gq, v0, v1, v2, g2);
   if (FLUX == XG_HLLC)
     hllc(wp, wq, g1, g2, d.x, d.y, d.z, gamma, stab2 != 0, stab2coef, f);
   else
