@@ -50,6 +50,18 @@ enum xg_precision {
 
 enum xg_flux { XG_RUSANOV = 0, XG_HLLC = 1 };
 
+/* Problems with a manufactured source term in riemann::rhs (riemann::src,
+ * src/Physics/Riemann.cpp:880-907, the src functions of
+ * src/Physics/Problems.cpp).  The scalar-transport problems (slot_cyl,
+ * sheardiff) carry more than five components and are not offered. */
+enum xg_source {
+  XG_SRC_NONE = 0,
+  XG_SRC_TAYLOR_GREEN = 1,
+  XG_SRC_VORTICAL_FLOW = 2,
+  XG_SRC_NONLINEAR_ENERGY_GROWTH = 3,
+  XG_SRC_RAYLEIGH_TAYLOR = 4
+};
+
 /* Physics and numerics settings the reference reads from its global config
  * (mat.spec_heat_ratio, flux, stab2, stab2coef, cfl, dt). */
 typedef struct xg_riecg_params {
@@ -116,6 +128,16 @@ int xg_riecg_grad(xg_ctx* ctx, const double* U, double* G);
 /* Drop-in for riemann::rhs (src/Physics/Riemann.cpp:909-946): right-hand
  * side R (npoin x 5) from host G (volume-divided, npoin x 15) and U. */
 int xg_riecg_rhs(xg_ctx* ctx, const double* G, const double* U, double* R);
+
+/* The manufactured source of riemann::rhs: R -= s(x, t) V per node, with
+ * s the problem's source (enum xg_source) and prm its control-file
+ * parameters problem_alpha, problem_beta[3], problem_kappa, problem_r0,
+ * problem_p0, problem_ce (8 doubles; may be NULL for taylor_green).  The
+ * source is evaluated at the context's time: the time given to
+ * xg_riecg_set_state, advanced by xg_riecg_run; every stage of a step uses
+ * the time at the start of the step, as RieCG::rhs passes it
+ * (src/Inciter/RieCG.cpp:948-949).  XG_SRC_NONE switches it off. */
+int xg_riecg_set_source(xg_ctx* ctx, int problem, const double* prm);
 
 /* xg_riecg_rhs computed with the edge-coloured scatter instead of owner
  * half-edges with deposits (FP32 mode only): the edges are split into

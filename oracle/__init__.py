@@ -94,6 +94,7 @@ def lib():
         L.orc_riecg_run.argtypes = [_vp, _i64, _vp]
         L.orc_riecg_run.restype = _dbl
         L.orc_riecg_stage.argtypes = [_vp, C.c_int, _dbl]
+        L.orc_riecg_set_source.argtypes = [_vp, C.c_int, _vp]
         L.orc_kozcg_create.restype = _vp
         L.orc_kozcg_create.argtypes = [_i64, _vp, _vp, _i64, _vp, _dbl, _dbl, _dbl, C.c_int,
                                        _dbl, C.c_int, C.c_int, _vp]
@@ -206,6 +207,11 @@ def sym_bc(coord, bface, sym_sets, far_sets=()):
 
 # ---------------------------------------------------------------- RieCG
 
+# problems with a manufactured source term in riemann::rhs (codes of the C ABI)
+SOURCES = {"none": 0, "taylor_green": 1, "vortical_flow": 2, "nonlinear_energy_growth": 3,
+           "rayleigh_taylor": 4}
+
+
 class RieCG:
     """Serial RieCG restatement over a plain edge list (canonical orientation)."""
 
@@ -272,6 +278,14 @@ class RieCG:
         R = np.zeros((self.n, 5))
         lib().orc_riecg_rhs(self.h, _p(G), _p(U), _p(R))
         return R
+
+    def set_source(self, problem, prm=None):
+        """The manufactured source of riemann::rhs (SOURCES names the
+        problems), evaluated at the state's time; prm = alpha, beta[3], kappa,
+        r0, p0, ce."""
+        self._src = None if prm is None else _c(np.asarray(prm, dtype=np.float64), np.float64)
+        lib().orc_riecg_set_source(self.h, SOURCES[problem],
+                                   None if self._src is None else _p(self._src))
 
     def bc(self):
         lib().orc_riecg_bc(self.h)

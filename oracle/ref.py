@@ -31,6 +31,7 @@ def lib():
         _lib = C.CDLL(REF_LIB)
         _lib.ref_last_error.restype = C.c_char_p
         _lib.ref_set_config.argtypes = [_dbl, C.c_char_p, C.c_int, _dbl, C.c_char_p, C.c_int]
+        _lib.ref_set_problem_params.argtypes = [_dbl] * 8
         _lib.ref_riemann_grad.argtypes = [_i64, _vp, _i64] + [_i64, _vp, _vp] * 3 + [_i64, _vp, _vp, _vp]
         _lib.ref_riemann_rhs.argtypes = ([_i64, _vp, _i64] + [_i64, _vp, _vp] * 3 +
                                          [_i64, _vp, _vp, _vp, _vp, _vp, _dbl, _vp])
@@ -57,6 +58,11 @@ def _check(rc):
 def set_config(gamma=1.4, flux="rusanov", stab2=False, stab2coef=0.2, problem="userdef",
                ncomp=5):
     lib().ref_set_config(gamma, flux.encode(), int(stab2), stab2coef, problem.encode(), ncomp)
+
+
+def set_problem_params(alpha=0.0, beta=(0.0, 0.0, 0.0), kappa=0.0, r0=0.0, p0=0.0, ce=0.0):
+    """The manufactured-solution parameters of the control file."""
+    lib().ref_set_problem_params(alpha, beta[0], beta[1], beta[2], kappa, r0, p0, ce)
 
 
 def _sup(sup):

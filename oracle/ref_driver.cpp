@@ -81,6 +81,20 @@ int ref_set_config(double gamma, const char* flux, int stab2, double stab2coef,
   return 0;
 }
 
+// The manufactured-solution parameters the problems' source terms read
+// (problem_alpha, problem_beta[3], problem_kappa, problem_r0, problem_p0,
+// problem_ce of the control file).
+int ref_set_problem_params(double alpha, double b0, double b1, double b2, double kappa,
+                           double r0, double p0, double ce) {
+  g_cfg.get<tag::problem_alpha>() = alpha;
+  g_cfg.get<tag::problem_beta>() = std::vector<double>{b0, b1, b2};
+  g_cfg.get<tag::problem_kappa>() = kappa;
+  g_cfg.get<tag::problem_r0>() = r0;
+  g_cfg.get<tag::problem_p0>() = p0;
+  g_cfg.get<tag::problem_ce>() = ce;
+  return 0;
+}
+
 // riemann::grad (src/Physics/Riemann.cpp:229-367).  Superedge counts are in
 // groups (tets: 4 ids + 18 reals, tris: 3 ids + 9 reals, edges: 2 ids + 3).
 int ref_riemann_grad(int64_t npoin, const double* xyz, int64_t ncomp,

@@ -107,6 +107,11 @@ struct RieCG {
   real t = 0, dt = 0;
   int stage = 0;
   int64_t it = 0;
+  // manufactured source (riemann::src): problem 0 none, 1 taylor_green,
+  // 2 vortical_flow, 3 nonlinear_energy_growth, 4 rayleigh_taylor; prm =
+  // alpha, beta[3], kappa, r0, p0, ce
+  int src = 0;
+  real sprm[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 };
 
 // EOS (src/Physics/EOS.hpp:29-56)
@@ -327,8 +332,80 @@ void riecg_grad(const RieCG& s, const real* U, real* G) {
   }
 }
 
-// riemann::rhs = advdom + advbnd (src/Physics/Riemann.cpp:652-878, 909-946);
-// the manufactured source term is off for the configured problems.
+// Source terms of the manufactured-solution problems at (x, y, z, t), the
+// problems' src functions (src/Physics/Problems.cpp: nonlinear_energy_growth
+// 163-220, rayleigh_taylor 261-332, taylor_green 433-449, vortical_flow
+// 481-508), restated from their formulas.
+void problem_source(const RieCG& s, real x, real y, real z, real t, real o[5]) {
+  const real pi = M_PI, g = s.gamma;
+  const real a = s.sprm[0], b0 = s.sprm[1], b1 = s.sprm[2], b2 = s.sprm[3];
+  const real kap = s.sprm[4], r0 = s.sprm[5], p0 = s.sprm[6], ce = s.sprm[7];
+  for (int c = 0; c < 5; ++c) o[c] = 0.0;
+  if (s.src == 1) {  // taylor_green: energy only
+    o[4] = 3.0 * pi / 8.0 *
+           (std::cos(3.0 * pi * x) * std::cos(pi * y) - std::cos(3.0 * pi * y) * std::cos(pi * x));
+  } else if (s.src == 2) {  // vortical_flow: rho = 1, linear velocity field
+    const real rho = 1.0;
+    const real mx = a * x - kap * y, my = kap * x + a * y;
+    o[1] = a * mx / rho - kap * my / rho;
+    o[2] = kap * mx / rho + a * my / rho;
+    o[4] = (o[1] * mx + o[2] * my) / rho + 8.0 * a * a * a * z * z / (g - 1.0);
+  } else if (s.src == 3) {  // nonlinear_energy_growth
+    const real gx = 1.0 - x * x - y * y - z * z;
+    const real dg[3] = {-2.0 * x, -2.0 * y, -2.0 * z};
+    const real cx = std::cos(b0 * pi * x), cy = std::cos(b1 * pi * y), cz = std::cos(b2 * pi * z);
+    const real h = cx * cy * cz;
+    const real dh[3] = {-b0 * pi * std::sin(b0 * pi * x) * cy * cz,
+                        -b1 * pi * cx * std::sin(b1 * pi * y) * cz,
+                        -b2 * pi * cx * cy * std::sin(b2 * pi * z)};
+    const real ft = std::exp(-a * t), dfdt = -a * ft;
+    const real rho = r0 + ft * gx, drdt = gx * dfdt;
+    const real ie = std::pow(-3.0 * (ce + kap * h * h * t), -1.0 / 3.0);
+    const real ie4 = std::pow(ie, 4.0);
+    o[0] = drdt;
+    for (int j = 0; j < 3; ++j) {
+      const real dedx = 2.0 * ie4 * kap * h * dh[j] * t, drdx = ft * dg[j];
+      o[1 + j] = (g - 1.0) * (rho * dedx + ie * drdx);
+    }
+    o[4] = rho * (kap * h * h * ie4) + ie * drdt;
+  } else if (s.src == 4) {  // rayleigh_taylor
+    const real gx = b0 * x * x + b1 * y * y + b2 * z * z;
+    const real ft = std::cos(kap * pi * t), st = std::sin(kap * pi * t);
+    const real sx = std::sin(pi * x), cx = std::cos(pi * x);
+    const real sy = std::sin(pi * y), cy = std::cos(pi * y);
+    // the solution as the problem's initial condition forms it, conserved
+    const real r = r0 - gx;
+    const real u0 = ft * z * sx, v0 = ft * z * cy, w0 = ft * (-0.5 * pi * z * z * (cx - sy));
+    const real rE = (p0 + a * gx) / (g - 1.0) + 0.5 * r * (u0 * u0 + v0 * v0 + w0 * w0);
+    const real m[3] = {r * u0, r * v0, r * w0};
+    // and back to primitives
+    const real rho = r, u = m[0] / rho, v = m[1] / rho, w = m[2] / rho, E = rE / rho;
+    const real p = p0 + a * (b0 * x * x + b1 * y * y + b2 * z * z);
+    const real drdx[3] = {-2.0 * b0 * x, -2.0 * b1 * y, -2.0 * b2 * z};
+    const real dpdx[3] = {2.0 * a * b0 * x, 2.0 * a * b1 * y, 2.0 * a * b2 * z};
+    const real dudx[3] = {ft * pi * z * cx, 0.0, ft * sx};
+    const real dvdx[3] = {0.0, -ft * pi * z * sy, ft * cy};
+    const real dwdx[3] = {ft * pi * 0.5 * pi * z * z * sx, ft * pi * 0.5 * pi * z * z * cy,
+                          -ft * pi * z * (cx - sy)};
+    real dedx[3];
+    for (int j = 0; j < 3; ++j)
+      dedx[j] = dpdx[j] / rho / (g - 1.0) - p / (g - 1.0) / rho / rho * drdx[j] + u * dudx[j] +
+                v * dvdx[j] + w * dwdx[j];
+    const real dudt = -kap * pi * st * z * sx, dvdt = -kap * pi * st * z * cy;
+    const real dwdt = kap * pi * st / 2.0 * pi * z * z * (cx - sy);
+    const real dedt = u * dudt + v * dvdt + w * dwdt;
+    o[0] = u * drdx[0] + v * drdx[1] + w * drdx[2];
+    o[1] = rho * dudt + u * o[0] + dpdx[0] + m[0] * dudx[0] + m[1] * dudx[1] + m[2] * dudx[2];
+    o[2] = rho * dvdt + v * o[0] + dpdx[1] + m[0] * dvdx[0] + m[1] * dvdx[1] + m[2] * dvdx[2];
+    o[3] = rho * dwdt + w * o[0] + dpdx[2] + m[0] * dwdx[0] + m[1] * dwdx[1] + m[2] * dwdx[2];
+    o[4] = rho * dedt + E * o[0] + m[0] * dedx[0] + m[1] * dedx[1] + m[2] * dedx[2] +
+           u * dpdx[0] + v * dpdx[1] + w * dpdx[2];
+  }
+}
+
+// riemann::rhs = advdom + advbnd + src (src/Physics/Riemann.cpp:652-946),
+// the source at the state's time t (RieCG::rhs passes the time at the start
+// of the step to every stage, RieCG.cpp:948-949).
 void riecg_rhs(const RieCG& s, const real* G, const real* U, real* R) {
   const int64_t n = s.npoin;
   std::fill(R, R + n * 5, 0.0);
@@ -378,6 +455,12 @@ void riecg_rhs(const RieCG& s, const real* G, const real* U, real* R) {
       R[N[2] * 5 + c] += fbc + fca + f[c][2];
     }
   }
+  if (s.src)
+    for (int64_t p = 0; p < n; ++p) {
+      real so[5];
+      problem_source(s, s.x[p], s.y[p], s.z[p], s.t, so);
+      for (int c = 0; c < 5; ++c) R[p * 5 + c] -= so[c] * s.vol[p];
+    }
 }
 
 // RieCG::BC (src/Inciter/RieCG.cpp:764-785) -> physics::dirbc, symbc, farbc,
@@ -1341,6 +1424,15 @@ void orc_riecg_grad(void* h, const double* U, double* G) {
 // Right-hand side from volume-divided gradients, like riemann::rhs.
 void orc_riecg_rhs(void* h, const double* G, const double* U, double* R) {
   riecg_rhs(*static_cast<RieCG*>(h), G, U, R);
+}
+
+// The manufactured source of riemann::rhs: problem (0 none, 1 taylor_green,
+// 2 vortical_flow, 3 nonlinear_energy_growth, 4 rayleigh_taylor) and its
+// parameters alpha, beta[3], kappa, r0, p0, ce (prm may be null).
+void orc_riecg_set_source(void* h, int problem, const double* prm) {
+  auto* s = static_cast<RieCG*>(h);
+  s->src = problem;
+  for (int k = 0; k < 8; ++k) s->sprm[k] = prm ? prm[k] : 0.0;
 }
 
 void orc_riecg_bc(void* h) {

@@ -44,6 +44,46 @@ def test_riemann_grad_rhs_bitexact(flux, stab2):
     assert np.array_equal(R, ref.riemann_rhs(coord, [None, None, (e, d)], tri, besym, Gv, U, v))
 
 
+# manufactured-solution problems with a source in riemann::rhs, with
+# parameters that keep their states physical on the unit cube:
+# (alpha, beta, kappa, r0, p0, ce)
+SOURCE_CASES = {
+    "taylor_green": (0.0, (0.0, 0.0, 0.0), 0.0, 0.0, 0.0, 0.0),
+    "vortical_flow": (0.1, (0.0, 0.0, 0.0), 1.0, 0.0, 10.0, 0.0),
+    "nonlinear_energy_growth": (0.25, (1.0, 0.75, 0.5), 0.8, 2.0, 0.0, -1.0),
+    "rayleigh_taylor": (1.0, (1.0, 1.0, 1.0), 1.0, 4.0, 1.0, 0.0),
+}
+
+
+def source_prm(name):
+    a, b, k, r0, p0, ce = SOURCE_CASES[name]
+    return [a, b[0], b[1], b[2], k, r0, p0, ce]
+
+
+@needs_ref
+@pytest.mark.parametrize("problem", sorted(SOURCE_CASES))
+def test_riemann_rhs_source_matches_reference(problem):
+    """riemann::rhs with a problem's manufactured source (riemann::src,
+    src/Physics/Riemann.cpp:880-907) at t = 0.3: the oracle's restatement of
+    the source formulas against the reference's Problems.cpp, bit for bit."""
+    m, coord, inpoel, v, e, d, tri, besym, *_ = _cube_ops()
+    U = random_state(coord.shape[1], 5)
+    a, b, k, r0, p0, ce = SOURCE_CASES[problem]
+    ref.set_config(problem=problem)
+    ref.set_problem_params(a, b, k, r0, p0, ce)
+    o = oracle.RieCG(coord, v, e, d, tri, besym)
+    o.set_source(problem, source_prm(problem))
+    o.set_state(U, 0.3)
+    Gv = o.grad(U) / v[:, None]
+    R = o.rhs(Gv, U)
+    Rr = ref.riemann_rhs(coord, [None, None, (e, d)], tri, besym, Gv, U, v, t=0.3)
+    o.set_source("none")
+    R0 = o.rhs(Gv, U)
+    assert np.abs(R - R0).max() > 1e-6 * np.abs(R0).max()  # the source is on
+    assert np.array_equal(R, Rr)
+    ref.set_config()
+
+
 @needs_ref
 def test_kozak_rhs_bitexact():
     m, coord, inpoel, v, *_ = _cube_ops(5)

@@ -51,6 +51,16 @@ struct Scalars {
   int32_t blowup;             // set when a dt fell below eps
   int32_t pad;
   long long step;             // steps taken in the current run (dt history index)
+  double t;                   // time at the start of the current step
+  double tnext;               // time at the start of the next step
+};
+
+// A manufactured source (enum xg_source) and its parameters alpha,
+// beta[3], kappa, r0, p0, ce.
+struct SrcPrm {
+  int problem;
+  double p[8];
+  double gamma;
 };
 
 }  // namespace
@@ -108,6 +118,11 @@ struct RieCGDev {
   int2* cpq = nullptr;
   float4* cd = nullptr;
   float* cR = nullptr;
+  // manufactured source: problem, parameters, and s V per node at the time
+  // of the current step (F [5][n], its own arena)
+  SrcPrm src{};
+  Arena srcarena;
+  void* Sv = nullptr;
   // staging for the drop-in entry points
   double* stage_buf = nullptr;
   void* stage_W = nullptr;
@@ -135,7 +150,8 @@ void destroy_riecg(RieCGDev* d) {
 }
 
 size_t bytes_riecg(const RieCGDev* d) {
-  return d ? d->arena.bytes() + d->bcarena.bytes() + d->scratch.bytes() + d->colarena.bytes()
+  return d ? d->arena.bytes() + d->bcarena.bytes() + d->scratch.bytes() + d->colarena.bytes() +
+                 d->srcarena.bytes()
            : 0;
 }
 
@@ -1216,6 +1232,98 @@ __device__ __forceinline__ double store_stage(int64_t n, int64_t p, const double
   return store_node<F>(n, p, u, wp, STAGE == 2, vol, aux, gamma_d, U, Wout);
 }
 
+// Manufactured source s(x, y, z, t) of a problem (riemann::src,
+// src/Physics/Riemann.cpp:880-907, with the problems' src functions of
+// src/Physics/Problems.cpp: nonlinear_energy_growth 163-220, rayleigh_taylor
+// 261-332, taylor_green 433-449, vortical_flow 481-508), in FP64.
+__device__ void problem_source(const SrcPrm& q, double x, double y, double z, double t,
+                               double o[5]) {
+  const double pi = 3.14159265358979323846, g = q.gamma;
+  const double a = q.p[0], b0 = q.p[1], b1 = q.p[2], b2 = q.p[3];
+  const double kap = q.p[4], r0 = q.p[5], p0 = q.p[6], ce = q.p[7];
+#pragma unroll
+  for (int c = 0; c < 5; ++c) o[c] = 0.0;
+  if (q.problem == XG_SRC_TAYLOR_GREEN) {
+    // energy only: 3 pi/8 (cos 3 pi x cos pi y - cos 3 pi y cos pi x)
+    o[4] = 3.0 * pi / 8.0 * (cos(3.0 * pi * x) * cos(pi * y) - cos(3.0 * pi * y) * cos(pi * x));
+  } else if (q.problem == XG_SRC_VORTICAL_FLOW) {
+    // unit density, momentum (a x - k y, k x + a y, -2 a z)
+    const double rho = 1.0, mx = a * x - kap * y, my = kap * x + a * y;
+    o[1] = a * mx / rho - kap * my / rho;
+    o[2] = kap * mx / rho + a * my / rho;
+    o[4] = (o[1] * mx + o[2] * my) / rho + 8.0 * a * a * a * z * z / (g - 1.0);
+  } else if (q.problem == XG_SRC_NONLINEAR_ENERGY_GROWTH) {
+    // rho = r0 + exp(-a t)(1 - |x|^2), e = (-3 (ce + k h^2 t))^(-1/3),
+    // h = cos(b0 pi x) cos(b1 pi y) cos(b2 pi z)
+    const double gx = 1.0 - x * x - y * y - z * z;
+    const double dg[3] = {-2.0 * x, -2.0 * y, -2.0 * z};
+    const double cx = cos(b0 * pi * x), cy = cos(b1 * pi * y), cz = cos(b2 * pi * z);
+    const double h = cx * cy * cz;
+    const double dh[3] = {-b0 * pi * sin(b0 * pi * x) * cy * cz, -b1 * pi * cx * sin(b1 * pi * y) * cz,
+                          -b2 * pi * cx * cy * sin(b2 * pi * z)};
+    const double ft = exp(-a * t), dfdt = -a * ft;
+    const double rho = r0 + ft * gx, drdt = gx * dfdt;
+    const double ie = pow(-3.0 * (ce + kap * h * h * t), -1.0 / 3.0);
+    const double ie4 = pow(ie, 4.0);
+    o[0] = drdt;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const double dedx = 2.0 * ie4 * kap * h * dh[j] * t, drdx = ft * dg[j];
+      o[1 + j] = (g - 1.0) * (rho * dedx + ie * drdx);
+    }
+    o[4] = rho * (kap * h * h * ie4) + ie * drdt;
+  } else if (q.problem == XG_SRC_RAYLEIGH_TAYLOR) {
+    // rho = r0 - |b x^2|, p = p0 + a |b x^2|, velocity cos(k pi t) times
+    // (z sin pi x, z cos pi y, -pi z^2 (cos pi x - sin pi y) / 2); the
+    // conserved solution formed first and the primitives taken from it
+    const double gx = b0 * x * x + b1 * y * y + b2 * z * z;
+    const double ft = cos(kap * pi * t), st = sin(kap * pi * t);
+    const double sx = sin(pi * x), cx = cos(pi * x), sy = sin(pi * y), cy = cos(pi * y);
+    const double r = r0 - gx;
+    const double u0 = ft * z * sx, v0 = ft * z * cy, w0 = ft * (-0.5 * pi * z * z * (cx - sy));
+    const double rE = (p0 + a * gx) / (g - 1.0) + 0.5 * r * (u0 * u0 + v0 * v0 + w0 * w0);
+    const double m[3] = {r * u0, r * v0, r * w0};
+    const double rho = r, u = m[0] / rho, v = m[1] / rho, w = m[2] / rho, E = rE / rho;
+    const double p = p0 + a * (b0 * x * x + b1 * y * y + b2 * z * z);
+    const double drdx[3] = {-2.0 * b0 * x, -2.0 * b1 * y, -2.0 * b2 * z};
+    const double dpdx[3] = {2.0 * a * b0 * x, 2.0 * a * b1 * y, 2.0 * a * b2 * z};
+    const double dudx[3] = {ft * pi * z * cx, 0.0, ft * sx};
+    const double dvdx[3] = {0.0, -ft * pi * z * sy, ft * cy};
+    const double dwdx[3] = {ft * pi * 0.5 * pi * z * z * sx, ft * pi * 0.5 * pi * z * z * cy,
+                            -ft * pi * z * (cx - sy)};
+    double dedx[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      dedx[j] = dpdx[j] / rho / (g - 1.0) - p / (g - 1.0) / rho / rho * drdx[j] + u * dudx[j] +
+                v * dvdx[j] + w * dwdx[j];
+    const double dudt = -kap * pi * st * z * sx, dvdt = -kap * pi * st * z * cy;
+    const double dwdt = kap * pi * st / 2.0 * pi * z * z * (cx - sy);
+    const double dedt = u * dudt + v * dvdt + w * dwdt;
+    o[0] = u * drdx[0] + v * drdx[1] + w * drdx[2];
+    o[1] = rho * dudt + u * o[0] + dpdx[0] + m[0] * dudx[0] + m[1] * dudx[1] + m[2] * dudx[2];
+    o[2] = rho * dvdt + v * o[0] + dpdx[1] + m[0] * dvdx[0] + m[1] * dvdx[1] + m[2] * dvdx[2];
+    o[3] = rho * dwdt + w * o[0] + dpdx[2] + m[0] * dwdx[0] + m[1] * dwdx[1] + m[2] * dwdx[2];
+    o[4] = rho * dedt + E * o[0] + m[0] * dedx[0] + m[1] * dedx[1] + m[2] * dedx[2] +
+           u * dpdx[0] + v * dpdx[1] + w * dpdx[2];
+  }
+}
+
+// s V per node at the time of the current step (coordinates from the
+// primitive records), once per step: every stage subtracts it.
+template <class F>
+__global__ void __launch_bounds__(kBlock)
+    k_src(int64_t n, SrcPrm q, const Scalars* __restrict__ sc, const F* __restrict__ W,
+          const double* __restrict__ vol, F* __restrict__ Sv) {
+  const int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (p >= n) return;
+  const F* w = W + p * 8;
+  double o[5];
+  problem_source(q, double(w[5]), double(w[6]), double(w[7]), sc->t, o);
+  const double v = vol[p];
+#pragma unroll
+  for (int c = 0; c < 5; ++c) Sv[c * n + p] = F(o[c] * v);
+}
+
 // Half-edge residual, pass 2: the fluxes of the edges the other end owns and
 // (optionally) the RK update of one stage with the new primitive records and,
 // on the last stage, the CFL minimum.  Boundary nodes only park their domain
@@ -1227,7 +1335,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(F) == 4 ? 4 : 1)
            const F* __restrict__ W, Bnd bnd, int64_t nbn, F* __restrict__ Rb,
            const double* __restrict__ vol, NodeAux aux, double gamma_d,
            const Scalars* __restrict__ scal, double* U, double* Un, F* __restrict__ Wout,
-           double* __restrict__ Rout, unsigned long long* dtmin) {
+           double* __restrict__ Rout, unsigned long long* dtmin, const F* __restrict__ Sv) {
   int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   const bool active = p < n;
   double dtp = DBL_MAX;
@@ -1268,6 +1376,12 @@ __global__ void __launch_bounds__(kBlock, sizeof(F) == 4 ? 4 : 1)
         }
       }
     }
+    // the manufactured source after the domain (and, in k_rhs_bnd, the
+    // boundary) sums, as riemann::rhs adds it last
+    if (Sv && bi < 0) {
+#pragma unroll
+      for (int c = 0; c < 5; ++c) R[c] -= Sv[c * n + p];
+    }
     if (bi >= 0) {
 #pragma unroll
       for (int c = 0; c < 5; ++c) Rb[c * nbn + bi] = R[c];
@@ -1294,7 +1408,7 @@ __global__ void __launch_bounds__(kBlock)
               const F* __restrict__ W, const int32_t* __restrict__ bcof, BCProg bc,
               const double* __restrict__ vol, NodeAux aux, double gamma_d,
               const Scalars* __restrict__ scal, double* U, double* Un, F* __restrict__ Wout,
-              double* __restrict__ Rout, unsigned long long* dtmin) {
+              double* __restrict__ Rout, unsigned long long* dtmin, const F* __restrict__ Sv) {
   const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   double dtp = DBL_MAX;
   if (i < nbn) {
@@ -1311,6 +1425,10 @@ __global__ void __launch_bounds__(kBlock)
     load8(W + p * 8, wp);
     const int32_t b = UPDATE ? __ldg(bcof + i) : -1;
     rhs_bnd_term(bnd, static_cast<int32_t>(i), W, F(gamma_d), R);
+    if (Sv) {
+#pragma unroll
+      for (int c = 0; c < 5; ++c) R[c] -= Sv[c * n + p];
+    }
     if (!UPDATE) {
 #pragma unroll
       for (int c = 0; c < 5; ++c) Rout[p * 5 + c] = double(R[c]);
@@ -1374,13 +1492,17 @@ __global__ void __launch_bounds__(kBlock)
 // node-major output.
 __global__ void __launch_bounds__(kBlock)
     k_colour_out(int64_t n, const float* __restrict__ R, Bnd bnd, const float* __restrict__ W,
-                 double gamma, double* __restrict__ Rout) {
+                 double gamma, const float* __restrict__ Sv, double* __restrict__ Rout) {
   const int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (p >= n) return;
   float r[8];
   load8(R + p * 8, r);
   const int32_t bi = __ldg(bnd.bidx + p);
   if (bi >= 0) rhs_bnd_term(bnd, bi, W, float(gamma), r);
+  if (Sv) {
+#pragma unroll
+    for (int c = 0; c < 5; ++c) r[c] -= Sv[c * n + p];
+  }
 #pragma unroll
   for (int c = 0; c < 5; ++c) Rout[p * 5 + c] = double(r[c]);
 }
@@ -1445,6 +1567,7 @@ __global__ void __launch_bounds__(kBlock) k_dt_f(int64_t n, const double* __rest
 __global__ void k_step_begin(Scalars* s, double cfl, double const_dt, double* hist) {
   const long long k = s->step;
   s->step = k + 1;
+  s->t = s->tnext;
   double dt;
   if (fabs(const_dt) > DBL_EPSILON)
     dt = const_dt;
@@ -1452,11 +1575,17 @@ __global__ void k_step_begin(Scalars* s, double cfl, double const_dt, double* hi
     dt = __longlong_as_double(s->dtmin) * cfl;
   if (dt < DBL_EPSILON) s->blowup = 1;
   s->dt = dt;
+  s->tnext = s->t + dt;
   s->dtmin = __double_as_longlong(DBL_MAX);
   if (hist) hist[k] = dt;
 }
 
 __global__ void k_set_dt(Scalars* s, double dt) { s->dt = dt; }
+// The time of the next step to start (and of drop-in residuals): t.
+__global__ void k_set_time(Scalars* s, double t) {
+  s->t = t;
+  s->tnext = t;
+}
 __global__ void k_reset_min(Scalars* s) { s->dtmin = __double_as_longlong(DBL_MAX); }
 
 }  // namespace
@@ -1533,6 +1662,20 @@ Adj<F> adj_of(RieCGDev* d) {
   return Adj<F>{d->soff, d->swidth, static_cast<const typename EntOf<F>::type*>(d->ent)};
 }
 NodeAux aux_of(RieCGDev* d) { return NodeAux{d->ivol, d->cbrtv}; }
+// s V per node when a manufactured source is on, else null
+template <class F>
+const F* src_of(RieCGDev* d) {
+  return d->src.problem != XG_SRC_NONE ? static_cast<const F*>(d->Sv) : nullptr;
+}
+// Evaluate s V at the device's current step time (scal->t) from records W.
+template <class F>
+int launch_src(xg_ctx* c, RieCGDev* d, const F* W) {
+  if (d->src.problem == XG_SRC_NONE) return XG_OK;
+  XG_PROF_LAUNCH(c, d, "riecg_src",
+                 (k_src<F><<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(
+                     d->n, d->src, d->scal, W, d->vol, static_cast<F*>(d->Sv))));
+  return XG_OK;
+}
 Bnd bnd_of(RieCGDev* d) { return Bnd{d->bnode, d->bidx, d->bptr, d->bent4}; }
 
 BCProg bcprog_of(RieCGDev* d) {
@@ -1583,14 +1726,14 @@ int launch_rhs_t(xg_ctx* c, RieCGDev* d, const F* W, const F* G, F* Wout, double
                  (k_rhs2<F, STAGE, UPDATE, LEAN><<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(
                      d->n, half_of<F>(d), fbuf, Rp, W, bnd_of(d), d->nbn,
                      static_cast<F*>(d->Rb), d->vol, aux_of(d), d->prm.gamma, d->scal, d->U,
-                     d->Un, Wout, Rout, &d->scal->dtmin)));
+                     d->Un, Wout, Rout, &d->scal->dtmin, src_of<F>(d))));
   if (d->nbn > 0)
     XG_PROF_LAUNCH(c, d, "riecg_rhs_bnd",
                    (k_rhs_bnd<F, STAGE, UPDATE, LEAN><<<blocks_for(d->nbn, kBlock), kBlock, 0,
                                                         c->stream>>>(
                        d->n, d->nbn, bnd_of(d), static_cast<const F*>(d->Rb), W, d->bcof,
                        bcprog_of(d), d->vol, aux_of(d), d->prm.gamma, d->scal, d->U, d->Un,
-                       Wout, Rout, &d->scal->dtmin)));
+                       Wout, Rout, &d->scal->dtmin, src_of<F>(d))));
   return XG_OK;
 }
 
@@ -2241,7 +2384,11 @@ int rhs_dropin(xg_ctx* c, RieCGDev* d, const double* G, const double* U, double*
                              c->stream));
   k_prim_aos<F><<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(d->n, d->stage_buf, W, W);
   XG_CHECK_LAUNCH(c);
-  int rc = launch_rhs<F>(c, d, 0, false, false, W, Gr, nullptr, d->stage_buf);
+  k_set_time<<<1, 1, 0, c->stream>>>(d->scal, d->t);
+  XG_CHECK_LAUNCH(c);
+  int rc = launch_src<F>(c, d, W);
+  if (rc) return rc;
+  rc = launch_rhs<F>(c, d, 0, false, false, W, Gr, nullptr, d->stage_buf);
   if (rc) return rc;
   XG_CUDA(c, cudaMemcpyAsync(R, d->stage_buf, d->n * 5 * sizeof(double), cudaMemcpyDeviceToHost,
                              c->stream));
@@ -2352,12 +2499,16 @@ int rhs_dropin_coloured(xg_ctx* c, RieCGDev* d, const double* G, const double* U
   k_prim_aos<float><<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(d->n, d->stage_buf, W, W);
   XG_CHECK_LAUNCH(c);
   XG_CUDA(c, cudaMemsetAsync(d->cR, 0, d->n * 8 * sizeof(float), c->stream));
+  k_set_time<<<1, 1, 0, c->stream>>>(d->scal, d->t);
+  XG_CHECK_LAUNCH(c);
+  rc = launch_src<float>(c, d, W);
+  if (rc) return rc;
   rc = d->prm.flux == XG_HLLC ? launch_colours<XG_HLLC>(c, d, W, Gr)
                               : launch_colours<XG_RUSANOV>(c, d, W, Gr);
   if (rc) return rc;
   XG_PROF_LAUNCH(c, d, "riecg_colour_out",
                  (k_colour_out<<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(
-                     d->n, d->cR, bnd_of(d), W, d->prm.gamma, d->stage_buf)));
+                     d->n, d->cR, bnd_of(d), W, d->prm.gamma, src_of<float>(d), d->stage_buf)));
   XG_CUDA(c, cudaMemcpyAsync(R, d->stage_buf, d->n * 5 * sizeof(double), cudaMemcpyDeviceToHost,
                              c->stream));
   XG_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -2396,6 +2547,40 @@ int xg_riecg_rhs_coloured(xg_ctx* c, const double* G, const double* U, double* R
   rc = rhs_dropin_coloured(c, d, G, U, R);
   if (rc) return rc;
   if (ncolours) *ncolours = static_cast<int>(d->coff.size()) - 1;
+  return XG_OK;
+  XG_HOST_CATCH(c)
+}
+
+int xg_riecg_set_source(xg_ctx* c, int problem, const double* prm) {
+  XG_HOST_TRY
+  int rc = use(c);
+  if (rc) return rc;
+  RieCGDev* d = c->riecg;
+  if (!d) return fail(c, XG_ERR_STATE, "riecg_set_source before riecg_setup");
+  if (problem < XG_SRC_NONE || problem > XG_SRC_RAYLEIGH_TAYLOR)
+    return fail(c, XG_ERR_ARG, "riecg_set_source: unknown problem");
+  if (problem != XG_SRC_NONE && !d->Sv) {
+    XG_CUDA(c, cudaStreamSynchronize(c->stream));
+    for (int pass = 0; pass < 2; ++pass) {
+      double* p64 = nullptr;
+      float* p32 = nullptr;
+      if (d->fp32)
+        d->srcarena.plan(p32, d->n * 5);
+      else
+        d->srcarena.plan(p64, d->n * 5);
+      if (pass == 0) XG_CUDA(c, d->srcarena.reserve());
+      d->Sv = d->fp32 ? static_cast<void*>(p32) : static_cast<void*>(p64);
+    }
+  }
+  d->src.problem = problem;
+  for (int k = 0; k < 8; ++k) d->src.p[k] = prm ? prm[k] : 0.0;
+  d->src.gamma = d->prm.gamma;
+  // the captured time loop holds the source launch or not: capture again
+  if (d->graph) {
+    XG_CUDA(c, cudaStreamSynchronize(c->stream));
+    cudaGraphExecDestroy(d->graph);
+    d->graph = nullptr;
+  }
   return XG_OK;
   XG_HOST_CATCH(c)
 }
@@ -2450,6 +2635,12 @@ int xg_riecg_stage(xg_ctx* c, int stage, double dt) {
     k_reset_min<<<1, 1, 0, c->stream>>>(d->scal);
     XG_CHECK_LAUNCH(c);
   }
+  // every stage's source at the context's time (the start of the step)
+  k_set_time<<<1, 1, 0, c->stream>>>(d->scal, d->t);
+  XG_CHECK_LAUNCH(c);
+  rc = d->fp32 ? launch_src<float>(c, d, static_cast<const float*>(d->W[d->cur]))
+               : launch_src<double>(c, d, static_cast<const double*>(d->W[d->cur]));
+  if (rc) return rc;
   rc = d->fp32 ? do_stage<float>(c, d, stage, false) : do_stage<double>(c, d, stage, false);
   if (rc) return rc;
   d->dt_valid = stage == 2;
@@ -2486,10 +2677,16 @@ int xg_riecg_run(xg_ctx* c, int64_t nstep, double* dts, float* ms) {
     }
   }
   XG_CUDA(c, cudaMemsetAsync(&d->scal->step, 0, sizeof(long long), c->stream));
+  k_set_time<<<1, 1, 0, c->stream>>>(d->scal, d->t);
+  XG_CHECK_LAUNCH(c);
   auto one_step = [&]() -> int {
     XG_PROF_LAUNCH(c, d, "riecg_step_begin",
                    (k_step_begin<<<1, 1, 0, c->stream>>>(d->scal, d->prm.cfl, d->prm.const_dt,
                                                          d->dthist)));
+    // the source of the whole step at its start time (RieCG::rhs)
+    const int r1 = d->fp32 ? launch_src<float>(c, d, static_cast<const float*>(d->W[d->cur]))
+                           : launch_src<double>(c, d, static_cast<const double*>(d->W[d->cur]));
+    if (r1) return r1;
     for (int st = 0; st < 3; ++st) {
       int r2 = d->fp32 ? do_stage<float>(c, d, st, true) : do_stage<double>(c, d, st, true);
       if (r2) return r2;

@@ -63,6 +63,7 @@ SIGNATURES = {
     "xg_riecg_grad": (_int, [_vp, _vp, _vp]),
     "xg_riecg_rhs": (_int, [_vp, _vp, _vp, _vp]),
     "xg_riecg_rhs_coloured": (_int, [_vp, _vp, _vp, _vp, _vp]),
+    "xg_riecg_set_source": (_int, [_vp, _int, _vp]),
     "xg_riecg_bc": (_int, [_vp]),
     "xg_riecg_dt": (_int, [_vp, _vp]),
     "xg_riecg_stage": (_int, [_vp, _int, _dbl]),

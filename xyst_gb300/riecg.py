@@ -21,6 +21,10 @@ import numpy as np
 
 from .lib import Context, RiecgParams, f64, i32, load, p, u64, u8
 
+# problems with a manufactured source term (enum xg_source)
+SOURCES = {"none": 0, "taylor_green": 1, "vortical_flow": 2, "nonlinear_energy_growth": 3,
+           "rayleigh_taylor": 4}
+
 FLUX = {"rusanov": 0, "hllc": 1}
 PRECISION = {"fp64": 0, "fp32": 1}
 
@@ -239,6 +243,15 @@ class RieCG:
         R = np.zeros((self.n, 5))
         self.ctx.check(self.lib.xg_riecg_rhs(self.ctx.h, p(G), p(U), p(R)))
         return R
+
+    def set_source(self, problem, prm=None):
+        """The manufactured source of riemann::rhs (SOURCES names the
+        problems; src/Physics/Riemann.cpp:880-907) with the control-file
+        parameters prm = alpha, beta[3], kappa, r0, p0, ce, evaluated at the
+        context's time (the start of each step)."""
+        self._src = None if prm is None else f64(np.asarray(prm, dtype=np.float64).reshape(8))
+        self.ctx.check(self.lib.xg_riecg_set_source(self.ctx.h, SOURCES[problem],
+                                                    None if self._src is None else p(self._src)))
 
     def rhs_coloured(self, G, U):
         """rhs() by the edge-coloured scatter (FP32 mode): (R, colours)."""
