@@ -276,6 +276,21 @@ int xg_chocg_setup(xg_ctx* ctx, const xg_chocg_params* prm, int64_t npoin, const
                    const double* dsupint1, int64_t nedge, const uint64_t* dsupedge2,
                    const double* dsupint2, int64_t nbtri, const uint64_t* triinpoel);
 
+/* The theta-implicit momentum prediction of ChoCG (theta > 0; 0 switches
+ * back to the explicit one): the last Runge-Kutta stage solves
+ * A du = R with A = -(M / dt + theta mu K), M the consistent mass and K the
+ * stiffness matrix of the tetrahedra (ChoCG::lhs, src/Inciter/ChoCG.cpp:
+ * 1433-1477), the velocity Dirichlet components and noslip nodes as zero
+ * rows, warm-started from the previous increment, at most mom_iter
+ * iterations to mom_tol with mom_pc (0 none, 1 jacobi), and sets
+ * u = un + du (ChoCG::solve/msolve/msolved, ChoCG.cpp:1529-1645).  inpoel:
+ * the tetrahedra, 4 node ids each.  The control file's theta, and the
+ * momentum solver's iter, tol and pc. */
+int xg_chocg_set_theta(xg_ctx* ctx, double theta, int64_t ntet, const uint64_t* inpoel,
+                       int mom_pc, int64_t mom_iter, double mom_tol);
+/* Iterations of the last momentum solve (negative: stopped short of mom_tol). */
+int xg_chocg_momentum_its(xg_ctx* ctx, int64_t* it);
+
 /* Boundary conditions as ChoCG::setupDirBC/streamable store them and
  * ChoCG::BC applies them (src/Inciter/ChoCG.cpp:207-275, 1333-1354):
  *   velocity Dirichlet: nodes, 3 mask ints per node (nonzero: set) and 3

@@ -124,6 +124,9 @@ def lib():
         L.orc_chocg_init.restype = _i64
         L.orc_chocg_step.argtypes = [_vp, _vp]
         L.orc_chocg_step.restype = _dbl
+        L.orc_chocg_set_theta.argtypes = [_vp, _dbl, _i64, _vp, C.c_int, _i64, _dbl]
+        L.orc_chocg_momentum_its.argtypes = [_vp]
+        L.orc_chocg_momentum_its.restype = _i64
         L.orc_chocg_div.argtypes = [_vp, _vp, _vp, _vp, _dbl, C.c_int, _vp]
         L.orc_chocg_vgrad.argtypes = [_vp, _vp, C.c_int, _vp]
         L.orc_chocg_flux.argtypes = [_vp, _vp, _vp, _vp]
@@ -461,6 +464,15 @@ class ChoCG:
 
     def init(self):
         return int(lib().orc_chocg_init(self.h))
+
+    def set_theta(self, theta, inpoel, mom_pc="none", mom_iter=10, mom_tol=1e-3):
+        """theta-implicit momentum prediction on the tetrahedra inpoel."""
+        self._tets = _c(inpoel, np.int64)
+        lib().orc_chocg_set_theta(self.h, theta, self._tets.size // 4, _p(self._tets),
+                                  1 if mom_pc == "jacobi" else 0, mom_iter, mom_tol)
+
+    def momentum_its(self):
+        return int(lib().orc_chocg_momentum_its(self.h))
 
     def step(self):
         it = np.zeros(1, np.int64)

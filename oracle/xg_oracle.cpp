@@ -835,6 +835,16 @@ struct ChoCG {
   int np = 0;
   int64_t last_it = 0;
   real last_normr = 0, last_normb = 0;
+  // theta-implicit momentum prediction: tetrahedra, the momentum system's
+  // pattern (3 rows per node, row 3i + c), its warm-start solution and the
+  // solver settings (mom_pc 0 none, 1 jacobi)
+  real theta = 0;
+  std::vector<int64_t> inpoel, mia, mja;
+  std::vector<real> momx;
+  int mom_pc = 0;
+  int64_t mom_iter = 10;
+  real mom_tol = 1e-3;
+  int64_t last_mit = 0;
 };
 
 inline real cx(const ChoCG& s, int64_t p) { return s.xyz[p]; }
@@ -1181,6 +1191,62 @@ void cho_init(ChoCG& s) {
 // (stabilised) / dt -> pressure-increment solve (Dirichlet values 0) ->
 // sgrad -> projection and BC -> pressure update and pgrad -> t += dt
 // (src/Inciter/ChoCG.cpp:1356-1695, 868-1281).
+// The semi-implicit last stage (ChoCG::lhs, src/Inciter/ChoCG.cpp:1433-1477,
+// then ChoCG::solve's implicit branch 1576-1606 and msolved 1626-1645): A is
+// assembled per element, A(a,b,c) -= J/dt/120 (2 or 1) + theta mu
+// grad_a.grad_b/J/6, the velocity Dirichlet components and noslip nodes are
+// zero rows (CSR::dirichlet with value 0), the PCG starts from the previous
+// increment, and u = un + du.
+void cho_momentum(ChoCG& s) {
+  const int64_t n = s.n, n3 = 3 * n;
+  std::vector<real> a(s.mja.size(), 0.0), b(s.rhs);
+  auto pos = [&](int64_t r, int64_t col) {
+    return static_cast<int64_t>(
+        std::lower_bound(s.mja.begin() + s.mia[r], s.mja.begin() + s.mia[r + 1], col) -
+        s.mja.begin());
+  };
+  for (int64_t e = 0; e < static_cast<int64_t>(s.inpoel.size() / 4); ++e) {
+    const int64_t* N = &s.inpoel[e * 4];
+    const real ba[3] = {cx(s, N[1]) - cx(s, N[0]), cy(s, N[1]) - cy(s, N[0]),
+                        cz(s, N[1]) - cz(s, N[0])};
+    const real ca[3] = {cx(s, N[2]) - cx(s, N[0]), cy(s, N[2]) - cy(s, N[0]),
+                        cz(s, N[2]) - cz(s, N[0])};
+    const real da[3] = {cx(s, N[3]) - cx(s, N[0]), cy(s, N[3]) - cy(s, N[0]),
+                        cz(s, N[3]) - cz(s, N[0])};
+    real g[4][3];
+    cross(ca[0], ca[1], ca[2], da[0], da[1], da[2], g[1][0], g[1][1], g[1][2]);
+    cross(da[0], da[1], da[2], ba[0], ba[1], ba[2], g[2][0], g[2][1], g[2][2]);
+    cross(ba[0], ba[1], ba[2], ca[0], ca[1], ca[2], g[3][0], g[3][1], g[3][2]);
+    for (int k = 0; k < 3; ++k) g[0][k] = -g[1][k] - g[2][k] - g[3][k];
+    const real J = ba[0] * g[1][0] + ba[1] * g[1][1] + ba[2] * g[1][2];
+    for (int p = 0; p < 4; ++p)
+      for (int q = 0; q < 4; ++q) {
+        real v = J / s.dt / 120.0 * ((p == q) ? 2.0 : 1.0);
+        v += s.theta * s.mu * (g[p][0] * g[q][0] + g[p][1] * g[q][1] + g[p][2] * g[q][2]) / J / 6.0;
+        for (int c = 0; c < 3; ++c) a[pos(N[p] * 3 + c, N[q] * 3 + c)] -= v;
+      }
+  }
+  std::vector<uint8_t> mask(n3, 0);
+  for (size_t k = 0; k < s.dirn.size(); ++k)
+    for (int c = 0; c < 3; ++c)
+      if (s.dirmask[k * 3 + c]) mask[s.dirn[k] * 3 + c] = 1;
+  for (int64_t p : s.noslip)
+    for (int c = 0; c < 3; ++c) mask[p * 3 + c] = 1;
+  std::vector<int64_t> rows;
+  for (int64_t r = n3 - 1; r >= 0; --r)
+    if (mask[r]) rows.push_back(r);
+  std::vector<real> zero(rows.size(), 0.0);
+  orc_csr_dirichlet(n3, s.mia.data(), s.mja.data(), a.data(), b.data(),
+                    static_cast<int64_t>(rows.size()), rows.data(), zero.data());
+  real nr = 0, nb = 0;
+  int conv = 0;
+  s.last_mit = orc_pcg(n3, s.mia.data(), s.mja.data(), a.data(), b.data(), s.momx.data(),
+                       s.mom_iter, s.mom_tol, s.mom_pc, &nr, &nb, &conv);
+  if (!conv) s.last_mit = -s.last_mit;
+  for (int64_t i = 0; i < n; ++i)
+    for (int c = 0; c < 3; ++c) s.u[i * 3 + c] = s.un[i * 3 + c] + s.momx[i * 3 + c];
+}
+
 real cho_step(ChoCG& s) {
   static const real rkc[4][4] = {{1.0, 0, 0, 0},
                                  {1.0 / 2.0, 1.0, 0, 0},
@@ -1191,10 +1257,14 @@ real cho_step(ChoCG& s) {
   for (int st = 0; st < s.rk; ++st) {
     cho_rhs(s, s.u.data(), s.vgrad.data(), s.pr.data(), s.rhs.data());
     if (st == 0) s.un = s.u;
-    const real dtk = rkc[s.rk - 1][st] * s.dt;
-    for (int64_t i = 0; i < n; ++i)
-      for (int c = 0; c < 3; ++c)
-        s.u[i * 3 + c] = s.un[i * 3 + c] - dtk * s.rhs[i * 3 + c] / s.vol[i];
+    if (s.theta > std::numeric_limits<real>::epsilon() && st + 1 == s.rk) {
+      cho_momentum(s);
+    } else {
+      const real dtk = rkc[s.rk - 1][st] * s.dt;
+      for (int64_t i = 0; i < n; ++i)
+        for (int c = 0; c < 3; ++c)
+          s.u[i * 3 + c] = s.un[i * 3 + c] - dtk * s.rhs[i * 3 + c] / s.vol[i];
+    }
     cho_bc(s, s.u.data());
     if (s.damp4) {
       std::fill(s.vgrad.begin(), s.vgrad.end(), 0.0);
@@ -1789,6 +1859,39 @@ int64_t orc_chocg_init(void* h) {
 }
 
 // One time step; returns dt and writes the pressure-solve iterations.
+// theta-implicit momentum prediction: tetrahedra (4 ids each) and the
+// momentum solver's settings; the pattern: nodes sharing a tetrahedron and
+// the diagonal, 3 rows per node
+void orc_chocg_set_theta(void* h, double theta, int64_t ntet, const int64_t* inpoel, int mom_pc,
+                         int64_t mom_iter, double mom_tol) {
+  auto* s = static_cast<ChoCG*>(h);
+  s->theta = theta;
+  s->inpoel.assign(inpoel, inpoel + ntet * 4);
+  s->mom_pc = mom_pc;
+  s->mom_iter = mom_iter;
+  s->mom_tol = mom_tol;
+  const int64_t n = s->n;
+  std::vector<std::vector<int64_t>> nb(n);
+  for (int64_t e = 0; e < ntet; ++e)
+    for (int a = 0; a < 4; ++a)
+      for (int b = 0; b < 4; ++b) nb[inpoel[e * 4 + a]].push_back(inpoel[e * 4 + b]);
+  s->mia.assign(3 * n + 1, 0);
+  s->mja.clear();
+  for (int64_t i = 0; i < n; ++i) {
+    auto& v = nb[i];
+    v.push_back(i);
+    std::sort(v.begin(), v.end());
+    v.erase(std::unique(v.begin(), v.end()), v.end());
+    for (int c = 0; c < 3; ++c) {
+      for (int64_t j : v) s->mja.push_back(j * 3 + c);
+      s->mia[i * 3 + c + 1] = static_cast<int64_t>(s->mja.size());
+    }
+  }
+  s->momx.assign(3 * n, 0.0);
+}
+
+int64_t orc_chocg_momentum_its(void* h) { return static_cast<ChoCG*>(h)->last_mit; }
+
 double orc_chocg_step(void* h, int64_t* it) {
   auto* s = static_cast<ChoCG*>(h);
   double dt = cho_step(*s);

@@ -75,6 +75,60 @@ def test_run_matches_oracle(flux, rk):
     assert relerr(d.field(4), o.get(6)) < 1e-8
 
 
+@pytest.mark.parametrize("mom_pc,mom_iter,mom_tol,rk", [("jacobi", 200, 1e-10, 1),
+                                                          ("none", 10, 1e-3, 3)])
+def test_theta_implicit_matches_oracle(mom_pc, mom_iter, mom_tol, rk):
+    """theta-implicit momentum prediction (theta = 0.5): the last stage
+    solves -(M/dt + theta mu K) du = R on a second CG system of 3n rows,
+    warm-started from the previous increment; converged (Jacobi, 1e-10) and
+    with the reference's defaults (no preconditioner, 10 iterations, 1e-3,
+    stopping at the limit).  Four steps against the oracle: dt, pressure and
+    momentum iteration counts, fields."""
+    ops = _cube_ops(9)
+    kw = dict(mu=0.05, cfl=0.5, flux="damp2", rk=rk, pc="jacobi", ptol=1e-10, pmaxit=2000)
+    d = chocg.ChoCG(ctx(), ops, **kw)
+    o = _oracle(ops, **kw)
+    for s in (d, o):
+        s.set_theta(0.5, ops["inpoel"], mom_pc=mom_pc, mom_iter=mom_iter, mom_tol=mom_tol)
+    u0 = chocg.taylor_green(ops["coord"])
+    d.set_state(u0)
+    o.set_state(u0, np.zeros(u0.shape[0]))
+    assert same_its(d.init(), o.init())
+    dts, its, _, _ = d.run(4)
+    for k in range(4):
+        dto, ito = o.step()
+        assert abs(dts[k] / dto - 1) < 1e-12
+        assert same_its(its[k], ito)
+    assert same_its(d.momentum_its(), o.momentum_its())
+    u, p, _ = d.state()
+    assert relerr(u, o.get(0)) < 1e-9
+    assert relerr(p, o.get(2)) < 1e-9
+
+
+def test_theta_implicit_lid_dirichlet_rows():
+    """The lid-driven cavity (noslip walls, lid velocity Dirichlet) with the
+    theta-implicit prediction: the momentum system's zero rows at the noslip
+    and Dirichlet components; three steps against the oracle."""
+    m, data, ops, kw, nstep = _regression_ops("lid")
+    kw = dict(kw, ptol=1e-8)
+    d = chocg.ChoCG(ctx(), ops, **kw)
+    o = _oracle(ops, **kw)
+    for s in (d, o):
+        s.set_theta(1.0, ops["inpoel"], mom_pc="jacobi", mom_iter=100, mom_tol=1e-8)
+    n = ops["coord"].shape[1]
+    d.set_state(np.zeros((n, 3)))
+    o.set_state(np.zeros((n, 3)), np.zeros(n))
+    assert same_its(d.init(), o.init())
+    dts, its, _, _ = d.run(3)
+    for k in range(3):
+        dto, ito = o.step()
+        assert abs(dts[k] / dto - 1) < 1e-12
+        assert same_its(its[k], ito)
+    u, p, _ = d.state()
+    assert relerr(u, o.get(0)) < 1e-9
+    assert relerr(p, o.get(2)) < 1e-9
+
+
 def _regression_ops(name):
     m, data = chocg_mesh(name)
     if name == "lid":

@@ -174,6 +174,19 @@ class ChoCG:
         self.ctx.check(self.lib.xg_chocg_init(self.ctx.h, C.byref(it)))
         return it.value
 
+    def set_theta(self, theta, inpoel, mom_pc="none", mom_iter=10, mom_tol=1e-3):
+        """theta-implicit momentum prediction (the control file's theta and
+        momentum solver iter / tol / pc) on the tetrahedra inpoel (ntet, 4)."""
+        self._tets = u64(inpoel).reshape(-1)
+        self.ctx.check(self.lib.xg_chocg_set_theta(self.ctx.h, float(theta), self._tets.size // 4,
+                                                   p(self._tets), 1 if mom_pc == "jacobi" else 0,
+                                                   int(mom_iter), float(mom_tol)))
+
+    def momentum_its(self):
+        it = C.c_int64()
+        self.ctx.check(self.lib.xg_chocg_momentum_its(self.ctx.h, C.byref(it)))
+        return it.value
+
     def run(self, nstep, check=True):
         """Returns (dts, pressure iterations per step, device ms, status)."""
         dts = np.zeros(nstep)

@@ -1153,6 +1153,35 @@ int cg_init_device(xg_ctx* c, const double* b_dev, int zero_values, int pc) {
 const double* cg_solution_device(xg_ctx* c) { return c->cg ? c->cg->x : nullptr; }
 int64_t cg_rows(xg_ctx* c) { return c->cg ? c->cg->n : 0; }
 
+// Values in CSR order, on the row pattern ia (zero-based, the pattern the
+// context's system was set up with), into that system's SELL-32 layout: entry
+// j of row i at soff[i / 32] + (j - ia[i]) 32 + i % 32, with the slice widths
+// xg_cg_setup forms; padding entries 0.  dev_out holds nent() doubles.
+int cg_to_sell(xg_ctx* c, const uint64_t* ia, const double* csr, double* dev_out) {
+  CGDev* d = c->cg;
+  if (!d) return fail(c, XG_ERR_STATE, "cg_to_sell before cg_setup");
+  const int64_t nrow = d->n, nslice = (nrow + kSlice - 1) / kSlice;
+  std::vector<int64_t> soff(nslice + 1, 0);
+  for (int64_t s = 0; s < nslice; ++s) {
+    uint64_t w = 0;
+    for (int64_t i = s * kSlice; i < std::min(nrow, (s + 1) * kSlice); ++i)
+      w = std::max<uint64_t>(w, ia[i + 1] - ia[i]);
+    soff[s + 1] = soff[s] + int64_t(w) * kSlice;
+  }
+  if (soff[nslice] != d->nent) return fail(c, XG_ERR_ARG, "cg_to_sell: pattern mismatch");
+  std::vector<double> v(static_cast<size_t>(d->nent), 0.0);
+  for (int64_t i = 0; i < nrow; ++i) {
+    const int64_t s = i / kSlice, lane = i % kSlice;
+    for (uint64_t j = ia[i]; j < ia[i + 1]; ++j)
+      v[soff[s] + int64_t(j - ia[i]) * kSlice + lane] = csr[j];
+  }
+  XG_CUDA(c, cudaMemcpy(dev_out, v.data(), v.size() * 8, cudaMemcpyHostToDevice));
+  return XG_OK;
+}
+int64_t cg_nent(xg_ctx* c) { return c->cg ? c->cg->nent : 0; }
+// The working values the solves read are formed from these originals.
+double* cg_values_device(xg_ctx* c) { return c->cg ? c->cg->a0 : nullptr; }
+
 }  // namespace xg
 
 using namespace xg;

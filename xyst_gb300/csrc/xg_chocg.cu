@@ -79,10 +79,31 @@ struct ChoCGDev {
   double t = 0.0;
   bool ready = false;  // start-up done
   int64_t last_it = 0;
+  std::vector<double> xyz_host;  // [3][n], for the momentum matrix
+  // theta-implicit momentum prediction (ChoCG::lhs/solve/msolve/msolved):
+  // its own CG system of 3n rows (row 3i + c), the stiffness and consistent
+  // mass values on its pattern (SELL order), the rhs of the last stage
+  // ([3][n]) and as the system's right-hand side (row order), and the
+  // Dirichlet rows (velocity Dirichlet components and noslip nodes)
+  double theta = 0.0;
+  int mom_pc = 0;
+  int64_t mom_iter = 10;
+  double mom_tol = 1.0e-3;
+  CGDev* mom = nullptr;
+  Arena momarena;
+  double *baseK = nullptr, *baseM = nullptr, *R3 = nullptr, *b3 = nullptr;
+  std::vector<uint8_t> mommask;
+  bool mommask_up = false;
+  int64_t last_mit = 0;
 };
 
-void destroy_chocg(ChoCGDev* d) { delete d; }
-size_t bytes_chocg(const ChoCGDev* d) { return d ? d->arena.bytes() + d->bcarena.bytes() : 0; }
+void destroy_chocg(ChoCGDev* d) {
+  if (d && d->mom) destroy_cg(d->mom);
+  delete d;
+}
+size_t bytes_chocg(const ChoCGDev* d) {
+  return d ? d->arena.bytes() + d->bcarena.bytes() + d->momarena.bytes() : 0;
+}
 
 namespace {
 
@@ -703,6 +724,74 @@ int launch_rhs(xg_ctx* c, ChoCGDev* d, const double* U, double dtk, int stage0, 
   return XG_OK;
 }
 
+// theta-implicit momentum system, per step (ChoCG::lhs, ChoCG.cpp:1433-1477):
+// A = -(M / dt + theta mu K) with M the consistent mass sum_e J/120 (1 + d_ab)
+// and K the stiffness sum_e grad_a.grad_b / J / 6, both on A's pattern.
+__global__ void k_mom_values(int64_t nent, const double* __restrict__ K,
+                             const double* __restrict__ M, double thmu, double dt,
+                             double* __restrict__ a) {
+  const int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (e >= nent) return;
+  a[e] = -(M[e] / dt + thmu * K[e]);
+}
+// [3][n] -> row order 3i + c, and the update u = un + du of ChoCG::msolved
+// (ChoCG.cpp:1626-1645).
+__global__ void k_to_rows3(int64_t n, const double* __restrict__ R, double* __restrict__ b) {
+  const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= n) return;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) b[i * 3 + c] = R[c * n + i];
+}
+__global__ void k_mom_update(int64_t n, const double* __restrict__ un,
+                             const double* __restrict__ du, double* __restrict__ u) {
+  const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= n) return;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) u[c * n + i] = un[c * n + i] + du[i * 3 + c];
+}
+
+// The semi-implicit last stage of ChoCG::solve (ChoCG.cpp:1576-1606): the
+// momentum system A du = R (R the stage's rhs, [3][n] in d->R3) with the
+// Dirichlet rows at zero increment, warm-started from the previous
+// increment, mom_iter iterations at most to mom_tol, then u = un + du.  The
+// momentum system is the context's CG system while it solves.
+int momentum_solve(xg_ctx* c, ChoCGDev* d, double dt) {
+  const int64_t n = d->n;
+  cudaStream_t s = c->stream;
+  CGDev* const saved = c->cg;
+  c->cg = d->mom;
+  int rc = XG_OK;
+  do {
+    const int64_t nent = cg_nent(c);
+    k_mom_values<<<blocks_for(nent, kBlock), kBlock, 0, s>>>(
+        nent, d->baseK, d->baseM, d->theta * d->prm.mu, dt, cg_values_device(c));
+    XG_CHECK_LAUNCH(c);
+    k_to_rows3<<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, d->R3, d->b3);
+    XG_CHECK_LAUNCH(c);
+    if (!d->mommask_up) {
+      std::vector<uint8_t> mask = d->mommask;
+      mask.resize(n * 3, 0);
+      std::vector<double> zero(n * 3, 0.0);
+      rc = cg_set_dirichlet(c, mask.data(), zero.data());
+      if (rc) break;
+      d->mommask_up = true;
+    }
+    rc = cg_init_device(c, d->b3, 1, d->mom_pc);
+    if (rc) break;
+    int64_t it = 0;
+    double normr = 0, normb = 0;
+    int conv = 0;
+    rc = xg_cg_solve(c, d->mom_iter, d->mom_tol, &it, &normr, &normb, &conv);
+    if (rc == XG_ERR_NOTCONV) rc = XG_OK;  // the reference carries on
+    if (rc) break;
+    d->last_mit = conv ? it : -it;
+    k_mom_update<<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, d->un, cg_solution_device(c), d->u);
+    XG_CHECK_LAUNCH(c);
+  } while (false);
+  c->cg = saved;
+  return rc;
+}
+
 // One pressure solve of ChoCG::pinit/psolve on the context's CG system with
 // the device right-hand side d->div: Dirichlet values of the first solves or
 // zero, warm start from the previous solution.  As in the reference, a solve
@@ -947,11 +1036,148 @@ int xg_chocg_setup(xg_ctx* c, const xg_chocg_params* prm, int64_t npoin, const d
   XG_CUDA(c, up(d->btri, btri.data(), btri.size() * 4));
   XG_CUDA(c, up(d->bnode, bnode.data(), bnode.size() * 4));
   XG_CUDA(c, up(d->xyz, coord, 3 * n * 8));
+  d->xyz_host.assign(coord, coord + 3 * n);
   XG_CUDA(c, up(d->vol, vol, n * 8));
   for (double* z : {d->u, d->u2, d->un, d->pr, d->pgrad, d->vgrad, d->div, d->flx})
     XG_CUDA(c, cudaMemset(z, 0, (z == d->vgrad ? 9 : (z == d->pr || z == d->div ? 1 : 3)) * n * 8));
   return XG_OK;
   XG_HOST_CATCH(c)
+}
+
+int xg_chocg_set_theta(xg_ctx* c, double theta, int64_t ntet, const uint64_t* inpoel, int mom_pc,
+                       int64_t mom_iter, double mom_tol) {
+  XG_HOST_TRY
+  ChoCGDev* d = nullptr;
+  int rc = get_ctx(c, &d, false);
+  if (rc) return rc;
+  if (!(theta >= 0.0) || mom_iter < 0 || !(mom_tol > 0.0) || (mom_pc != 0 && mom_pc != 1))
+    return fail(c, XG_ERR_ARG, "chocg_set_theta: bad theta, iteration limit, tolerance or pc");
+  XG_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (d->mom) {
+    destroy_cg(d->mom);
+    d->mom = nullptr;
+  }
+  d->momarena.release();
+  d->theta = 0.0;
+  if (theta < std::numeric_limits<double>::epsilon()) return XG_OK;  // explicit prediction
+  const int64_t n = d->n;
+  if (ntet <= 0 || !inpoel) return fail(c, XG_ERR_ARG, "chocg_set_theta: no tetrahedra");
+  for (int64_t k = 0; k < ntet * 4; ++k)
+    if (inpoel[k] >= static_cast<uint64_t>(n))
+      return fail(c, XG_ERR_ARG, "chocg_set_theta: tetrahedron node out of range");
+  // the node pattern (every pair of nodes sharing a tetrahedron, and the
+  // diagonal), columns sorted
+  std::vector<std::vector<int64_t>> nb(n);
+  for (int64_t e = 0; e < ntet; ++e)
+    for (int a = 0; a < 4; ++a)
+      for (int b = 0; b < 4; ++b) nb[inpoel[e * 4 + a]].push_back(int64_t(inpoel[e * 4 + b]));
+  std::vector<uint64_t> ia(n + 1, 0);
+  std::vector<int64_t> ja;
+  for (int64_t i = 0; i < n; ++i) {
+    auto& v = nb[i];
+    v.push_back(i);
+    std::sort(v.begin(), v.end());
+    v.erase(std::unique(v.begin(), v.end()), v.end());
+    ia[i + 1] = ia[i] + v.size();
+    ja.insert(ja.end(), v.begin(), v.end());
+    std::vector<int64_t>().swap(v);
+  }
+  // stiffness grad_a.grad_b / J / 6 and consistent mass J/120 (1 + d_ab),
+  // summed over the elements in element order (ChoCG::lhs)
+  std::vector<double> K(ja.size(), 0.0), M(ja.size(), 0.0);
+  const double* X = d->xyz_host.data();
+  const double* Y = X + n;
+  const double* Z = Y + n;
+  auto pos = [&](int64_t i, int64_t j) {
+    return static_cast<int64_t>(std::lower_bound(ja.begin() + ia[i], ja.begin() + ia[i + 1], j) -
+                                ja.begin());
+  };
+  for (int64_t e = 0; e < ntet; ++e) {
+    const uint64_t* N = inpoel + e * 4;
+    const double ba[3] = {X[N[1]] - X[N[0]], Y[N[1]] - Y[N[0]], Z[N[1]] - Z[N[0]]};
+    const double ca[3] = {X[N[2]] - X[N[0]], Y[N[2]] - Y[N[0]], Z[N[2]] - Z[N[0]]};
+    const double da[3] = {X[N[3]] - X[N[0]], Y[N[3]] - Y[N[0]], Z[N[3]] - Z[N[0]]};
+    auto cross = [](const double u[3], const double v[3], double w[3]) {
+      w[0] = u[1] * v[2] - v[1] * u[2];
+      w[1] = u[2] * v[0] - v[2] * u[0];
+      w[2] = u[0] * v[1] - v[0] * u[1];
+    };
+    double g[4][3];
+    cross(ca, da, g[1]);
+    cross(da, ba, g[2]);
+    cross(ba, ca, g[3]);
+    for (int k = 0; k < 3; ++k) g[0][k] = -g[1][k] - g[2][k] - g[3][k];
+    const double J = ba[0] * g[1][0] + ba[1] * g[1][1] + ba[2] * g[1][2];
+    if (!(J > 0.0)) return fail(c, XG_ERR_ARG, "chocg_set_theta: element Jacobian non-positive");
+    for (int a = 0; a < 4; ++a)
+      for (int b = 0; b < 4; ++b) {
+        const int64_t q = pos(int64_t(N[a]), int64_t(N[b]));
+        M[q] += J / 120.0 * ((a == b) ? 2.0 : 1.0);
+        K[q] += (g[a][0] * g[b][0] + g[a][1] * g[b][1] + g[a][2] * g[b][2]) / J / 6.0;
+      }
+  }
+  // three components per node: row 3i + c, columns 3j + c
+  std::vector<uint64_t> ia3(n * 3 + 1, 0), ja3;
+  std::vector<double> K3, M3;
+  ja3.reserve(ja.size() * 3);
+  K3.reserve(ja.size() * 3);
+  M3.reserve(ja.size() * 3);
+  for (int64_t i = 0; i < n; ++i)
+    for (int cc = 0; cc < 3; ++cc) {
+      for (uint64_t k = ia[i]; k < ia[i + 1]; ++k) {
+        ja3.push_back(uint64_t(ja[k]) * 3 + cc);
+        K3.push_back(K[k]);
+        M3.push_back(M[k]);
+      }
+      ia3[i * 3 + cc + 1] = ja3.size();
+    }
+  // the momentum CG system, set up while it stands in for the context's
+  CGDev* const saved = c->cg;
+  c->cg = nullptr;
+  rc = xg_cg_setup(c, n * 3, ia3.data(), ja3.data(), K3.data(), 0);
+  d->mom = c->cg;
+  if (rc == XG_OK) {
+    const int64_t nent = cg_nent(c);
+    for (int pass = 0; pass < 2; ++pass) {
+      Arena& A = d->momarena;
+      A.plan(d->baseK, nent);
+      A.plan(d->baseM, nent);
+      A.plan(d->R3, n * 3);
+      A.plan(d->b3, n * 3);
+      if (pass == 0) {
+        const cudaError_t ce = A.reserve();
+        if (ce != cudaSuccess) {
+          rc = fail(c, XG_ERR_CUDA, std::string("chocg_set_theta: ") + cudaGetErrorString(ce));
+          break;
+        }
+      }
+    }
+    if (rc == XG_OK) rc = cg_to_sell(c, ia3.data(), K3.data(), d->baseK);
+    if (rc == XG_OK) rc = cg_to_sell(c, ia3.data(), M3.data(), d->baseM);
+  }
+  c->cg = saved;
+  if (rc) {
+    if (d->mom) destroy_cg(d->mom);
+    d->mom = nullptr;
+    d->momarena.release();
+    return rc;
+  }
+  d->theta = theta;
+  d->mom_pc = mom_pc;
+  d->mom_iter = mom_iter;
+  d->mom_tol = mom_tol;
+  d->mommask_up = false;
+  d->last_mit = 0;
+  return XG_OK;
+  XG_HOST_CATCH(c)
+}
+
+int xg_chocg_momentum_its(xg_ctx* c, int64_t* it) {
+  ChoCGDev* d = nullptr;
+  int rc = get_ctx(c, &d, false);
+  if (rc) return rc;
+  if (it) *it = d->last_mit;
+  return XG_OK;
 }
 
 int xg_chocg_set_bc(xg_ctx* c, int64_t ndir, const uint64_t* dirnodes, const int32_t* dirmask,
@@ -1020,6 +1246,16 @@ int xg_chocg_set_bc(xg_ctx* c, int64_t ndir, const uint64_t* dirnodes, const int
   XG_CUDA(c, up(d->symn, symn.data(), symn.size() * 8));
   XG_CUDA(c, up(d->dirmask, dirmask, ndir * 3 * 4));
   XG_CUDA(c, up(d->dirval, dirvals, ndir * 3 * 8));
+  // Dirichlet rows of the theta-implicit momentum system (ChoCG::solve,
+  // ChoCG.cpp:1580-1600): the masked velocity components of the Dirichlet
+  // nodes and all three of the noslip nodes, increment 0
+  d->mommask.assign(n * 3, 0);
+  for (int64_t k = 0; k < ndir; ++k)
+    for (int cc = 0; cc < 3; ++cc)
+      if (dirmask[k * 3 + cc]) d->mommask[dirnodes[k] * 3 + cc] = 1;
+  for (int64_t k = 0; k < nnoslip; ++k)
+    for (int cc = 0; cc < 3; ++cc) d->mommask[noslipnodes[k] * 3 + cc] = 1;
+  d->mommask_up = false;
   // pressure Dirichlet nodes on the context's CG system
   if (cg_rows(c) != n)
     return fail(c, XG_ERR_STATE, "chocg_set_bc: set up the pressure matrix (xg_cg_setup) first");
@@ -1122,6 +1358,7 @@ int xg_chocg_run(xg_ctx* c, int64_t nstep, double* dts, int64_t* its, float* ms)
   int rc = get_ctx(c, &d, true);
   if (rc) return rc;
   if (!d->ready) return fail(c, XG_ERR_STATE, "chocg_run before chocg_init");
+  const int64_t n = d->n;
   static const double rkc[4][4] = {{1.0, 0, 0, 0},
                                    {1.0 / 2.0, 1.0, 0, 0},
                                    {1.0 / 3.0, 1.0 / 2.0, 1.0, 0},
@@ -1144,9 +1381,19 @@ int xg_chocg_run(xg_ctx* c, int64_t nstep, double* dts, int64_t* its, float* ms)
     }
     // momentum prediction (ChoCG::rhs -> solve -> pred -> corr, per stage)
     for (int k = 0; k < d->prm.rk; ++k) {
-      rc = launch_rhs(c, d, d->u, rkc[d->prm.rk - 1][k] * dt, k == 0, d->u2, nullptr);
-      if (rc) return rc;
-      std::swap(d->u, d->u2);
+      if (d->mom && k + 1 == d->prm.rk) {
+        // semi-implicit last stage: the stage rhs, then the momentum solve
+        rc = launch_rhs(c, d, d->u, 0.0, 0, nullptr, d->R3);
+        if (rc) return rc;
+        if (k == 0) XG_CUDA(c, cudaMemcpyAsync(d->un, d->u, n * 3 * 8, cudaMemcpyDeviceToDevice,
+                                              c->stream));
+        rc = momentum_solve(c, d, dt);
+        if (rc) return rc;
+      } else {
+        rc = launch_rhs(c, d, d->u, rkc[d->prm.rk - 1][k] * dt, k == 0, d->u2, nullptr);
+        if (rc) return rc;
+        std::swap(d->u, d->u2);
+      }
       rc = launch_bc(c, d, d->u, 0);
       if (rc) return rc;
       if (d->prm.flux == XG_DAMP4) {

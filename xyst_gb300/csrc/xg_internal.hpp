@@ -92,6 +92,9 @@ int lpc_factor(xg_ctx* c, xg_lpc* m, const LpcGraph& g, float* nvL, float* nvU);
 int cg_set_dirichlet(xg_ctx* c, const uint8_t* mask, const double* val);
 int cg_zero_solution(xg_ctx* c);
 int cg_init_device(xg_ctx* c, const double* b_dev, int zero_values, int pc);
+int cg_to_sell(xg_ctx* c, const uint64_t* ia, const double* csr, double* dev_out);
+int64_t cg_nent(xg_ctx* c);
+double* cg_values_device(xg_ctx* c);
 const double* cg_solution_device(xg_ctx* c);
 int64_t cg_rows(xg_ctx* c);
 

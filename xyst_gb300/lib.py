@@ -87,6 +87,8 @@ SIGNATURES = {
     "xg_chocg_get_state": (_int, [_vp, _vp, _vp, _vp]),
     "xg_chocg_init": (_int, [_vp, _vp]),
     "xg_chocg_run": (_int, [_vp, _i64, _vp, _vp, _vp]),
+    "xg_chocg_set_theta": (_int, [_vp, _dbl, _i64, _vp, _int, _i64, _dbl]),
+    "xg_chocg_momentum_its": (_int, [_vp, _vp]),
     "xg_chocg_fields": (_int, [_vp, _int, _vp]),
     "xg_chorin_div": (_int, [_vp, _vp, _vp, _vp, _dbl, _int, _vp]),
     "xg_chorin_grad": (_int, [_vp, _vp, _vp]),
