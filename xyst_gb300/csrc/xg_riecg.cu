@@ -110,6 +110,8 @@ struct RieCGDev {
   bool dt_valid = false;
   // two whole time steps captured once and replayed (launch overhead)
   cudaGraphExec_t graph = nullptr;
+  // and one step from either primitive-buffer parity (single-step runs)
+  cudaGraphExec_t graph1[2] = {nullptr, nullptr};
   // edge-coloured residual (xg_riecg_rhs_coloured), built on first use:
   // colour c holds edges coff[c] .. coff[c+1] - 1 as (owner, other end) and
   // the edge integral in the owner's orientation; cR: F [n][8] records
@@ -138,9 +140,20 @@ struct RieCGDev {
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
 };
 
+// Captured time-loop graphs are dropped whenever what they captured changes
+// (BCs, the source, the dt history buffer).
+void drop_graphs(RieCGDev* d) {
+  if (d->graph) cudaGraphExecDestroy(d->graph);
+  d->graph = nullptr;
+  for (auto& g : d->graph1) {
+    if (g) cudaGraphExecDestroy(g);
+    g = nullptr;
+  }
+}
+
 void destroy_riecg(RieCGDev* d) {
   if (!d) return;
-  if (d->graph) cudaGraphExecDestroy(d->graph);
+  drop_graphs(d);
   if (d->dthist) cudaFree(d->dthist);
   for (auto& p : d->pending) {
     cudaEventDestroy(p.second.first);
@@ -240,6 +253,28 @@ __device__ __forceinline__ void prim5(const double u[5], double w[5]) {
   w[2] = u[2] / w[0];
   w[3] = u[3] / w[0];
   w[4] = u[4] / w[0] - 0.5 * (w[1] * w[1] + w[2] * w[2] + w[3] * w[3]);
+}
+
+// The five primitives of a W record from a node's FP64 state: FP64 mode
+// the reference's expressions (primitive(), src/Physics/Riemann.cpp:211-227);
+// FP32 mode FP32 arithmetic with one reciprocal (the records are FP32).
+template <class F>
+__device__ __forceinline__ void prim_record(const double u[5], F o[5]) {
+  if constexpr (sizeof(F) == 8) {
+    double pw[5];
+    prim5(u, pw);
+#pragma unroll
+    for (int c = 0; c < 5; ++c) o[c] = pw[c];
+  } else {
+    const float r = float(u[0]);
+    const float ir = __frcp_rn(r);
+    const float uu = float(u[1]) * ir, vv = float(u[2]) * ir, ww = float(u[3]) * ir;
+    o[0] = r;
+    o[1] = uu;
+    o[2] = vv;
+    o[3] = ww;
+    o[4] = float(u[4]) * ir - 0.5f * (uu * uu + vv * vv + ww * ww);
+  }
 }
 
 // Per-node CFL time step (src/Inciter/RieCG.cpp:827-838), before the CFL factor.
@@ -677,14 +712,12 @@ __global__ void k_prim_aos(int64_t n, const double* __restrict__ Ua, const F* __
                            F* __restrict__ W) {
   int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (p >= n) return;
-  double u[5], w[5];
+  double u[5];
 #pragma unroll
   for (int c = 0; c < 5; ++c) u[c] = Ua[p * 5 + c];
-  prim5(u, w);
   F o[8];
   load8(Wsrc + p * 8, o);
-#pragma unroll
-  for (int c = 0; c < 5; ++c) o[c] = F(w[c]);
+  prim_record<F>(u, o);
   store8(W + p * 8, o);
 }
 
@@ -1186,22 +1219,35 @@ __device__ __forceinline__ double store_node(int64_t n, int64_t p, const double 
   double dtp = DBL_MAX;
 #pragma unroll
   for (int c = 0; c < 5; ++c) U[c * n + p] = u[c];
-  if constexpr (sizeof(F) == 8) {
-    double pw[5];
-    prim5(u, pw);
-    F o[8] = {F(pw[0]), F(pw[1]), F(pw[2]), F(pw[3]), F(pw[4]), wp[5], wp[6], wp[7]};
-    store8(Wout + p * 8, o);
-    if (want_dt) dtp = node_dt(u, vol[p], gamma_d);
-  } else {
-    const float r = float(u[0]);
-    const float ir = __frcp_rn(r);
-    const float uu = float(u[1]) * ir, vv = float(u[2]) * ir, ww = float(u[3]) * ir;
-    const float ie = float(u[4]) * ir - 0.5f * (uu * uu + vv * vv + ww * ww);
-    F o[8] = {r, uu, vv, ww, ie, wp[5], wp[6], wp[7]};
-    store8(Wout + p * 8, o);
-    if (want_dt) dtp = double(node_dt_f(u, aux.cbrtv[p], float(gamma_d)));
-  }
+  F o[8] = {F(0), F(0), F(0), F(0), F(0), wp[5], wp[6], wp[7]};
+  prim_record<F>(u, o);
+  store8(Wout + p * 8, o);
+  if (want_dt)
+    dtp = sizeof(F) == 8 ? node_dt(u, vol[p], gamma_d)
+                         : double(node_dt_f(u, aux.cbrtv[p], float(gamma_d)));
   return dtp;
+}
+
+// A host-layout (node-major) state as the context's state in one pass: the
+// FP64 SoA state, the primitive records (coordinates kept) and the CFL
+// minimum of the new state (RieCG::dt's formula, the FP32 estimate in FP32
+// mode) -- what xg_riecg_set_state needs, reading the upload once.
+template <class F>
+__global__ void __launch_bounds__(kBlock)
+    k_state_in(int64_t n, const double* __restrict__ Ua, const double* __restrict__ vol,
+               NodeAux aux, double gamma_d, double* __restrict__ U, F* __restrict__ W,
+               unsigned long long* dtmin) {
+  const int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  double dtp = DBL_MAX;
+  if (p < n) {
+    double u[5];
+#pragma unroll
+    for (int c = 0; c < 5; ++c) u[c] = Ua[p * 5 + c];
+    F o[8];
+    load8(W + p * 8, o);  // coordinates
+    dtp = store_node<F>(n, p, u, o, true, vol, aux, gamma_d, U, W);
+  }
+  block_min_atomic(dtp, dtmin);
 }
 
 // Store a node's stage state: in the time loop's lean form the inner stages
@@ -2300,10 +2346,7 @@ int xg_riecg_set_bc(xg_ctx* c, int64_t nsym, const uint64_t* symnodes, const dou
     for (int i = 0; i < 5; ++i) d->far5[i] = far5[i];
   d->nbc = nbc;
   d->dt_valid = false;
-  if (d->graph) {
-    cudaGraphExecDestroy(d->graph);
-    d->graph = nullptr;
-  }
+  drop_graphs(d);
   return XG_OK;
   XG_HOST_CATCH(c)
 }
@@ -2316,20 +2359,20 @@ int xg_riecg_set_state(xg_ctx* c, const double* U, double t) {
   if (!U) return fail(c, XG_ERR_ARG, "riecg_set_state: null U");
   XG_CUDA(c, cudaMemcpyAsync(d->stage_buf, U, d->n * 5 * sizeof(double), cudaMemcpyHostToDevice,
                              c->stream));
-  k_aos_to_soa<<<blocks_for(d->n * 5, kBlock), kBlock, 0, c->stream>>>(d->n, 5, d->stage_buf,
-                                                                        d->U);
+  // the state, its primitive records and its CFL minimum in one pass
+  k_reset_min<<<1, 1, 0, c->stream>>>(d->scal);
   XG_CHECK_LAUNCH(c);
-  if (d->fp32) {
-    float* W = static_cast<float*>(d->W[d->cur]);
-    k_prim_aos<float><<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(d->n, d->stage_buf, W, W);
-  } else {
-    double* W = static_cast<double*>(d->W[d->cur]);
-    k_prim_aos<double><<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(d->n, d->stage_buf, W, W);
-  }
+  if (d->fp32)
+    k_state_in<float><<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(
+        d->n, d->stage_buf, d->vol, aux_of(d), d->prm.gamma, d->U,
+        static_cast<float*>(d->W[d->cur]), &d->scal->dtmin);
+  else
+    k_state_in<double><<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(
+        d->n, d->stage_buf, d->vol, aux_of(d), d->prm.gamma, d->U,
+        static_cast<double*>(d->W[d->cur]), &d->scal->dtmin);
   XG_CHECK_LAUNCH(c);
   d->t = t;
-  rc = refresh_dt(c, d);
-  if (rc) return rc;
+  d->dt_valid = true;
   XG_CUDA(c, cudaStreamSynchronize(c->stream));
   return XG_OK;
 }
@@ -2576,11 +2619,8 @@ int xg_riecg_set_source(xg_ctx* c, int problem, const double* prm) {
   for (int k = 0; k < 8; ++k) d->src.p[k] = prm ? prm[k] : 0.0;
   d->src.gamma = d->prm.gamma;
   // the captured time loop holds the source launch or not: capture again
-  if (d->graph) {
-    XG_CUDA(c, cudaStreamSynchronize(c->stream));
-    cudaGraphExecDestroy(d->graph);
-    d->graph = nullptr;
-  }
+  XG_CUDA(c, cudaStreamSynchronize(c->stream));
+  drop_graphs(d);
   return XG_OK;
   XG_HOST_CATCH(c)
 }
@@ -2671,10 +2711,7 @@ int xg_riecg_run(xg_ctx* c, int64_t nstep, double* dts, float* ms) {
     const int64_t cap = std::max<int64_t>(nstep, 1024);
     XG_CUDA(c, cudaMalloc(&d->dthist, cap * sizeof(double)));
     d->dthist_cap = cap;
-    if (d->graph) {
-      cudaGraphExecDestroy(d->graph);
-      d->graph = nullptr;
-    }
+    drop_graphs(d);
   }
   XG_CUDA(c, cudaMemsetAsync(&d->scal->step, 0, sizeof(long long), c->stream));
   k_set_time<<<1, 1, 0, c->stream>>>(d->scal, d->t);
@@ -2694,31 +2731,47 @@ int xg_riecg_run(xg_ctx* c, int64_t nstep, double* dts, float* ms) {
     return XG_OK;
   };
   // replay two whole steps at a time from a captured graph (the primitive
-  // buffers swap once per stage, so two steps return to the same buffer);
+  // buffers swap once per stage, so two steps return to the same buffer),
+  // and single steps from a one-step graph of the current parity;
   // profiling runs launch kernel by kernel
+  auto capture = [&](int steps, int parity, cudaGraphExec_t* out) -> int {
+    const int saved = d->cur;
+    d->cur = parity;
+    cudaGraph_t g = nullptr;
+    XG_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    int r = XG_OK;
+    for (int k = 0; k < steps && !r; ++k) r = one_step();
+    cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+    d->cur = saved;
+    if (r) {
+      if (g) cudaGraphDestroy(g);
+      return r;
+    }
+    if (ce != cudaSuccess) return fail(c, XG_ERR_CUDA, cudaGetErrorString(ce));
+    ce = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) {
+      *out = nullptr;
+      return fail(c, XG_ERR_CUDA, cudaGetErrorString(ce));
+    }
+    return XG_OK;
+  };
+  auto single = [&]() -> int {
+    if (d->prof) return one_step();
+    const int par = d->cur;
+    if (!d->graph1[par]) {
+      const int r = capture(1, par, &d->graph1[par]);
+      if (r) return r;
+    }
+    XG_CUDA(c, cudaGraphLaunch(d->graph1[par], c->stream));
+    d->cur ^= 1;  // three buffer swaps
+    return XG_OK;
+  };
   const bool use_graph = !d->prof && nstep >= 2;
   int64_t done = 0;
   if (use_graph && !d->graph) {
-    // capture (not run) two steps from the cur == 0 buffer parity
-    const int saved = d->cur;
-    d->cur = 0;
-    cudaGraph_t g = nullptr;
-    XG_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    int r1 = one_step();
-    int r2 = r1 ? r1 : one_step();
-    cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
-    d->cur = saved;
-    if (r2) {
-      if (g) cudaGraphDestroy(g);
-      return r2;
-    }
-    if (ce != cudaSuccess) return fail(c, XG_ERR_CUDA, cudaGetErrorString(ce));
-    ce = cudaGraphInstantiate(&d->graph, g, 0);
-    cudaGraphDestroy(g);
-    if (ce != cudaSuccess) {
-      d->graph = nullptr;
-      return fail(c, XG_ERR_CUDA, cudaGetErrorString(ce));
-    }
+    rc = capture(2, 0, &d->graph);
+    if (rc) return rc;
   }
   cudaEvent_t e0, e1;
   XG_CUDA(c, cudaEventCreate(&e0));
@@ -2726,7 +2779,7 @@ int xg_riecg_run(xg_ctx* c, int64_t nstep, double* dts, float* ms) {
   XG_CUDA(c, cudaEventRecord(e0, c->stream));
   if (use_graph) {
     if (d->cur != 0) {
-      rc = one_step();  // three buffer swaps bring cur back to 0
+      rc = single();  // three buffer swaps bring cur back to 0
       if (rc) return rc;
       ++done;
     }
@@ -2736,7 +2789,7 @@ int xg_riecg_run(xg_ctx* c, int64_t nstep, double* dts, float* ms) {
     }
   }
   for (; done < nstep; ++done) {
-    rc = one_step();
+    rc = single();
     if (rc) return rc;
   }
   XG_CUDA(c, cudaEventRecord(e1, c->stream));
