@@ -205,7 +205,8 @@ __device__ __forceinline__ unsigned long long tobits(double v) { return __double
 __device__ __forceinline__ unsigned int tobits(float v) { return __float_as_uint(v); }
 
 // Where component c of node i lives in the element sums: FP64 mode SoA
-// [5][n] (R, A) and [10][n] (P); FP32 mode node records, so that one element
+// [5][n] (R, A) and [10][n] (P), written whole by k_node_gather from the
+// slot records; FP32 mode node records, so that one element
 // adds a node's contribution with 16-byte vector atomics
 // (red.global.add.v4.f32) instead of one atomic per component: R and P share
 // a [n][16] record (R at 0..4, P+/- at 5..14, P addressed from R + 5), A has

@@ -9,11 +9,14 @@
 //   RieCG::solve    src/Inciter/RieCG.cpp:992-1057 (rkcoef :41)
 //   RieCG::BC       src/Inciter/RieCG.cpp:764-785 -> src/Physics/BC.cpp
 //   RieCG::dt       src/Inciter/RieCG.cpp:787-852
+//   riemann::src    src/Physics/Riemann.cpp:880-907 (manufactured sources)
 //
 // Data layout in HBM (n nodes):
 //   U, Un     double SoA [5][n]  conserved state and stage-0 copy
 //   W[0..1]   F [n][8]           (rho, u, v, w, e, x, y, z) records, ping-pong
-//   G         F [n][16]          15 volume-divided gradients + pad
+//   G         F [n][16]          15 volume-divided gradients + pad (FP32: the
+//                                component-paired order of gslot, for the
+//                                packed FP32x2 pipe)
 //   vol       double [n]
 //   adjacency SELL-32: slice s of 32 consecutive nodes holds width[s] entries
 //             per node at off[s] + k*32 + lane, each one packed record: the
