@@ -271,6 +271,31 @@ def test_profile_counts_launches():
     d.profile(False)
 
 
+def test_fp32_graph_profile_and_stage_paths_agree():
+    """FP32 steps through the captured graphs and through the kernel-by-
+    kernel profiling path give the same bits, and so do single stages."""
+    ops = cube_ops(7)
+    a, _ = pair(ops, precision="fp32")
+    b, _ = pair(ops, precision="fp32")
+    for d in (a, b):
+        d.set_state(wave_ic(ops["coord"]))
+    a.run(4)
+    b.run(2)
+    b.profile(True)
+    b.run(1)
+    b.profile(False)
+    b.run(1)
+    assert np.array_equal(a.state()[0], b.state()[0])
+    dt = a.dt()
+    assert dt == b.dt()
+    b.profile(True)
+    for st in range(3):
+        a.stage(st, dt)
+        b.stage(st, dt)
+    assert np.array_equal(a.state()[0], b.state()[0])
+    b.profile(False)
+
+
 def test_errors_are_status_codes():
     ops = cube_ops(4)
     d, _ = pair(ops)
