@@ -673,7 +673,7 @@ __global__ void __launch_bounds__(kBlock) k_pc_upper(int64_t n, const int32_t* _
 // and writes the other, so no row reads a residual that another row of the
 // same pass has replaced.
 template <class CI>
-__global__ void __launch_bounds__(kBlock) k_pc_upper_res(
+__global__ void __launch_bounds__(kBlock, 5) k_pc_upper_res(
     int64_t n, const int32_t* __restrict__ soffU, const int32_t* __restrict__ swU, CI ci,
     const __half* __restrict__ nvU, const float* __restrict__ srow, const float* __restrict__ q,
     const float* p0, const float* p1, float* ra, float* rb, double* __restrict__ e,
