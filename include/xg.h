@@ -116,7 +116,9 @@ int xg_riecg_set_bc(xg_ctx* ctx,
                     const double* dirvals,
                     int64_t npre, const uint64_t* prenodes, const double* prevals);
 
-/* Device-resident state U (npoin x 5, node-major), time t. */
+/* Device-resident state U (npoin x 5, node-major), time t.  U in pinned
+ * (page-locked) host memory is read / written by the kernels directly over
+ * the host link; other host memory goes through a staging copy. */
 int xg_riecg_set_state(xg_ctx* ctx, const double* U, double t);
 int xg_riecg_get_state(xg_ctx* ctx, double* U, double* t);
 

@@ -25,9 +25,10 @@ def cube_ops(n, jitter=0.2, seed=1, sym=(1, 2, 3, 4, 5, 6), far=(), dirs=(), pre
 
 
 def pair(ops, precision="fp64", flux="rusanov", stab2=False, cfl=0.5, const_dt=0.0,
-         far_state=None, dir_vals=None, pre_vals=None):
-    """(device RieCG, oracle RieCG) on the same operators and BCs."""
-    d = riecg.RieCG(ctx(), ops["coord"], ops["vol"], [None, None, ops["edges"]],
+         far_state=None, dir_vals=None, pre_vals=None, context=None):
+    """(device RieCG, oracle RieCG) on the same operators and BCs.  A context
+    holds one RieCG: two device solvers alive at once need two contexts."""
+    d = riecg.RieCG(context or ctx(), ops["coord"], ops["vol"], [None, None, ops["edges"]],
                     [None, None, ops["dint"]], ops["tri"], ops["besym"], flux=flux, stab2=stab2,
                     cfl=cfl, const_dt=const_dt, precision=precision)
     o = oracle.RieCG(ops["coord"], ops["vol"], ops["edges"], ops["dint"], ops["tri"],

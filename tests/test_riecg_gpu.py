@@ -10,7 +10,7 @@ import pytest
 from common import random_state, sod_ic, sod_mesh, wave_ic
 from gpu_util import cube_ops, ctx, pair, relerr
 from test_oracle_pins import SOURCE_CASES, source_prm
-from xyst_gb300 import riecg
+from xyst_gb300 import lib, riecg
 
 pytestmark = pytest.mark.gpu
 
@@ -258,6 +258,34 @@ def test_sod_reference_baseline_on_gpu():
             assert np.all(np.abs(f[i] - ref_f[i])[big] <= 1e-7 * np.abs(ref_f[i][big]))
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_pinned_host_buffers_match_pageable(precision):
+    """set_state / state with a pinned host buffer (read and written by the
+    kernels over the host link) give the same bits as with pageable memory,
+    on a node count that is not a multiple of the block size."""
+    torch = pytest.importorskip("torch")
+    ops = cube_ops(10)
+    n = ops["coord"].shape[1]
+    assert n % 256 != 0
+    a, _ = pair(ops, precision=precision)
+    b, _ = pair(ops, precision=precision, context=lib.Context(0))
+    U0 = wave_ic(ops["coord"])
+    pinned = torch.empty(U0.shape, dtype=torch.float64, pin_memory=True).numpy()
+    assert pinned.ctypes.data % 8 == 0
+    pinned[:] = U0
+    a.set_state(U0.copy())
+    b.set_state(pinned)
+    assert a.dt() == b.dt()
+    a.run(2)
+    b.run(2)
+    out = torch.empty(U0.shape, dtype=torch.float64, pin_memory=True).numpy()
+    out[:] = np.nan
+    Ua, ta = a.state()
+    Ub, tb = b.state(out=out)
+    assert Ub is out
+    assert np.array_equal(Ua, Ub) and ta == tb
+
+
 def test_profile_counts_launches():
     ops = cube_ops(6)
     d, _ = pair(ops)
@@ -276,7 +304,7 @@ def test_fp32_graph_profile_and_stage_paths_agree():
     kernel profiling path give the same bits, and so do single stages."""
     ops = cube_ops(7)
     a, _ = pair(ops, precision="fp32")
-    b, _ = pair(ops, precision="fp32")
+    b, _ = pair(ops, precision="fp32", context=lib.Context(0))
     for d in (a, b):
         d.set_state(wave_ic(ops["coord"]))
     a.run(4)

@@ -171,6 +171,19 @@ size_t bytes_riecg(const RieCGDev* d) {
            : 0;
 }
 
+// The device address of a caller's pinned (page-locked) host buffer, which
+// kernels may read and write over the host link, or nullptr for any other
+// memory (pageable host memory, 8-byte misaligned pointers).
+void* pinned_view(const void* p) {
+  if (reinterpret_cast<uintptr_t>(p) % alignof(double) != 0) return nullptr;
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    (void)cudaGetLastError();  // clear the query's error: the buffer is not one of CUDA's
+    return nullptr;
+  }
+  return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 // ---------------------------------------------------------------------------
 // device code
 
@@ -1235,17 +1248,28 @@ __device__ __forceinline__ double store_node(int64_t n, int64_t p, const double 
 // FP64 SoA state, the primitive records (coordinates kept) and the CFL
 // minimum of the new state (RieCG::dt's formula, the FP32 estimate in FP32
 // mode) -- what xg_riecg_set_state needs, reading the upload once.
+// The block's nodes are read as one contiguous run of node-major doubles
+// (coalesced: Ua may be the caller's pinned host buffer, read over the host
+// link) and staged in shared memory.
 template <class F>
 __global__ void __launch_bounds__(kBlock)
     k_state_in(int64_t n, const double* __restrict__ Ua, const double* __restrict__ vol,
                NodeAux aux, double gamma_d, double* __restrict__ U, F* __restrict__ W,
                unsigned long long* dtmin) {
-  const int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  __shared__ double su[kBlock * 5];
+  const int64_t p0 = blockIdx.x * int64_t(kBlock);
+  const int64_t p = p0 + threadIdx.x;
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const int64_t e = p0 * 5 + threadIdx.x + k * kBlock;
+    if (e < n * 5) su[threadIdx.x + k * kBlock] = Ua[e];
+  }
+  __syncthreads();
   double dtp = DBL_MAX;
   if (p < n) {
     double u[5];
 #pragma unroll
-    for (int c = 0; c < 5; ++c) u[c] = Ua[p * 5 + c];
+    for (int c = 0; c < 5; ++c) u[c] = su[threadIdx.x * 5 + c];
     F o[8];
     load8(W + p * 8, o);  // coordinates
     dtp = store_node<F>(n, p, u, o, true, vol, aux, gamma_d, U, W);
@@ -2360,19 +2384,25 @@ int xg_riecg_set_state(xg_ctx* c, const double* U, double t) {
   RieCGDev* d = c->riecg;
   if (!d) return fail(c, XG_ERR_STATE, "riecg_set_state before riecg_setup");
   if (!U) return fail(c, XG_ERR_ARG, "riecg_set_state: null U");
-  XG_CUDA(c, cudaMemcpyAsync(d->stage_buf, U, d->n * 5 * sizeof(double), cudaMemcpyHostToDevice,
-                             c->stream));
+  // a pinned host buffer is read by k_state_in itself over the host link;
+  // other memory goes through a staging copy
+  const double* src = static_cast<const double*>(pinned_view(U));
+  if (!src) {
+    XG_CUDA(c, cudaMemcpyAsync(d->stage_buf, U, d->n * 5 * sizeof(double),
+                               cudaMemcpyHostToDevice, c->stream));
+    src = d->stage_buf;
+  }
   // the state, its primitive records and its CFL minimum in one pass
   k_reset_min<<<1, 1, 0, c->stream>>>(d->scal);
   XG_CHECK_LAUNCH(c);
   if (d->fp32)
     k_state_in<float><<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(
-        d->n, d->stage_buf, d->vol, aux_of(d), d->prm.gamma, d->U,
-        static_cast<float*>(d->W[d->cur]), &d->scal->dtmin);
+        d->n, src, d->vol, aux_of(d), d->prm.gamma, d->U, static_cast<float*>(d->W[d->cur]),
+        &d->scal->dtmin);
   else
     k_state_in<double><<<blocks_for(d->n, kBlock), kBlock, 0, c->stream>>>(
-        d->n, d->stage_buf, d->vol, aux_of(d), d->prm.gamma, d->U,
-        static_cast<double*>(d->W[d->cur]), &d->scal->dtmin);
+        d->n, src, d->vol, aux_of(d), d->prm.gamma, d->U, static_cast<double*>(d->W[d->cur]),
+        &d->scal->dtmin);
   XG_CHECK_LAUNCH(c);
   d->t = t;
   d->dt_valid = true;
@@ -2386,11 +2416,15 @@ int xg_riecg_get_state(xg_ctx* c, double* U, double* t) {
   RieCGDev* d = c->riecg;
   if (!d) return fail(c, XG_ERR_STATE, "riecg_get_state before riecg_setup");
   if (U) {
-    k_soa_to_aos<<<blocks_for(d->n * 5, kBlock), kBlock, 0, c->stream>>>(d->n, 5, d->U,
-                                                                          d->stage_buf);
+    // into a pinned host buffer directly (coalesced stores over the host
+    // link), otherwise through a staging copy
+    double* dst = static_cast<double*>(pinned_view(U));
+    k_soa_to_aos<<<blocks_for(d->n * 5, kBlock), kBlock, 0, c->stream>>>(
+        d->n, 5, d->U, dst ? dst : d->stage_buf);
     XG_CHECK_LAUNCH(c);
-    XG_CUDA(c, cudaMemcpyAsync(U, d->stage_buf, d->n * 5 * sizeof(double), cudaMemcpyDeviceToHost,
-                               c->stream));
+    if (!dst)
+      XG_CUDA(c, cudaMemcpyAsync(U, d->stage_buf, d->n * 5 * sizeof(double),
+                                 cudaMemcpyDeviceToHost, c->stream));
   }
   XG_CUDA(c, cudaStreamSynchronize(c->stream));
   if (t) *t = d->t;
