@@ -30,6 +30,23 @@ def sod_ic(coord, gamma=1.4):
     return U
 
 
+def taylor_green_state(coord, gamma=5.0 / 3.0):
+    """The stationary Taylor-Green vortex (problems::taylor_green::ic,
+    src/Physics/Problems.cpp:409-428): rho = 1, p = 10 + (cos 2 pi x +
+    cos 2 pi y) / 4, u = sin pi x cos pi y, v = -cos pi x sin pi y, w = 0."""
+    x, y = coord[0], coord[1]
+    r = np.ones_like(x)
+    p = 10.0 + r / 4.0 * (np.cos(2.0 * np.pi * x) + np.cos(2.0 * np.pi * y))
+    u = np.sin(np.pi * x) * np.cos(np.pi * y)
+    v = -np.cos(np.pi * x) * np.sin(np.pi * y)
+    U = np.zeros((coord.shape[1], 5))
+    U[:, 0] = r
+    U[:, 1] = r * u
+    U[:, 2] = r * v
+    U[:, 4] = p / (gamma - 1.0) + 0.5 * r * (u * u + v * v)
+    return U
+
+
 def wave_ic(coord, gamma=1.4):
     """Smooth density wave rho = 1 + 0.2 sin(2 pi x) sin(2 pi y) sin(2 pi z),
     u = (1, 0.5, 0.25), p = 1."""

@@ -22,7 +22,13 @@ Sources, all read as data (nothing is executed):
     final nodal fields (ldc.std.exo) and per-step diagnostics (diag_ldc.std);
   * tests/regression/inciter/ChoCG/Poiseuille: the damp2 Poiseuille flow
     (CFL 0.05, mu 0.01, pressure 2.4 / 0 on side sets 1 / 2, noslip on 3,4,
-    v = w = 0 on 1 and 5, 20 steps): the same three files.
+    v = w = 0 on 1 and 5, 20 steps): the same three files;
+  * tests/regression/inciter/RieCG/TaylorGreen: the stationary Taylor-Green
+    vortex with its manufactured energy source (gamma 5/3, CFL 0.8, the
+    analytic state as Dirichlet values on all six side sets, to t = 1 in 68
+    steps): input mesh, nodal fields at every output time
+    (taylor_green.std.exo) and the diagnostics of every second step
+    (diag.std).
 """
 
 from __future__ import annotations
@@ -115,26 +121,36 @@ def sod_fixture(ref: str, scheme: str):
     return out
 
 
-def chocg_fixture(ref: str, case: str, meshfile: str, outfile: str, diagfile: str):
+def regression_fixture(ref: str, scheme: str, case: str, meshfile: str, outfile: str,
+                       diagfile: str, all_times: bool = False):
+    """Input mesh, output fields (the last time, or every time) and
+    diagnostics of one regression case of a scheme."""
     from xyst_gb300 import mesh as M
     from scipy.io import netcdf_file
 
-    base = os.path.join(ref, "tests/regression/inciter/ChoCG", case)
+    base = os.path.join(ref, "tests/regression/inciter", scheme, case)
     m = M.read_exo(os.path.join(base, meshfile))
     f = netcdf_file(os.path.join(base, outfile), "r", mmap=False)
     names = ["".join(c.decode() for c in row if c) for row in f.variables["name_nod_var"][:]]
     times = np.array(f.variables["time_whole"][:], dtype=np.float64)
-    fields = np.array([np.array(f.variables[f"vals_nod_var{i + 1}"][:][-1], dtype=np.float64)
-                       for i in range(len(names))])
+    allf = np.array([np.array(f.variables[f"vals_nod_var{i + 1}"][:], dtype=np.float64)
+                     for i in range(len(names))])  # [field][time][node]
     ocoord = np.stack([np.asarray(f.variables[k][:], dtype=np.float64)
                        for k in ("coordx", "coordy", "coordz")])
     f.close()
     out = {"coord": m["coord"], "inpoel": m["inpoel"], "final_time": times[-1],
-           "out_coord": ocoord, "out_fields": fields, "out_names": np.array(names),
+           "out_coord": ocoord, "out_fields": allf[:, -1], "out_names": np.array(names),
            "diag": _diag(os.path.join(base, diagfile))}
+    if all_times:
+        out["out_times"] = times
+        out["out_fields_all"] = allf
     for s, tri in m["bface"].items():
         out[f"bface{s}"] = tri
     return out
+
+
+def chocg_fixture(ref: str, case: str, meshfile: str, outfile: str, diagfile: str):
+    return regression_fixture(ref, "ChoCG", case, meshfile, outfile, diagfile)
 
 
 def main(ref: str):
@@ -149,6 +165,9 @@ def main(ref: str):
                         **chocg_fixture(ref, "Poiseuille", "poiseuille1tetz.exo",
                                         "poiseuille_damp2.std.exo",
                                         "diag_poiseuille_damp2.std"))
+    np.savez_compressed(os.path.join(HERE, "riecg_taylor_green.npz"),
+                        **regression_fixture(ref, "RieCG", "TaylorGreen", "unitcube_1k.exo",
+                                             "taylor_green.std.exo", "diag.std", all_times=True))
     print("wrote fixtures to", HERE)
 
 

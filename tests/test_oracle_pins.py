@@ -12,7 +12,8 @@ import pytest
 
 import oracle
 import oracle.ref as ref
-from common import dirichlet_matrix_only, golden, laplacian_14, random_state, sod_ic, sod_mesh
+from common import (dirichlet_matrix_only, golden, laplacian_14, random_state, sod_ic, sod_mesh,
+                    taylor_green_state)
 from xyst_gb300 import mesh
 
 needs_ref = pytest.mark.skipif(not ref.available(), reason="reference sources not built here")
@@ -221,6 +222,95 @@ def test_riecg_sod_golden():
             big = np.abs(ref_f[i]) > 1e-8
             assert np.all(np.abs(f[i] - ref_f[i])[big] <= 1e-7 * np.abs(ref_f[i][big]))
     assert abs(t - float(d["final_time"])) < 1e-8
+
+
+def taylor_green_steps(solver, term, vol, steps_out):
+    """Steps of the reference's Taylor-Green regression on solver (an oracle
+    or device RieCG): the CFL step of each step's start state, the last one
+    cut to end at term (Discretization::setdt, src/Inciter/
+    Discretization.cpp:926-939), stages driven one by one.  Returns the
+    diagnostics rows (t, dt, L2 of U, L2 of the step's change; NodeDiagnostics
+    norms) and the states after the steps listed in steps_out."""
+    def state():
+        s = solver.state()
+        return s[0] if isinstance(s, tuple) else s  # the device's (U, t)
+
+    Vt = vol.sum()
+    t, k, rows, states = 0.0, 0, [], {}
+    while abs(t - term) >= np.finfo(float).eps:
+        Uo = state()
+        dt = solver.dt()
+        if t + dt > term:
+            dt = term - t
+        for st in range(3):
+            solver.stage(st, dt)
+        t += dt
+        k += 1
+        U = state()
+        l2 = np.sqrt((U ** 2 * vol[:, None]).sum(0) / Vt)
+        l2r = np.sqrt(((U - Uo) ** 2 * vol[:, None]).sum(0) / Vt)
+        rows.append(np.concatenate([[k, t, dt], l2, l2r]))
+        if k in steps_out:
+            states[k] = U.copy()
+        assert k < 1000
+    return np.array(rows), states
+
+
+def check_taylor_green_golden(rows, states, coord, d, gamma=5.0 / 3.0):
+    """Against the reference's diag.std (every second step; numdiff: t, dt and
+    L2 of U abs 5e-4 or rel 1e-4, L2 of the change abs 5e-4 or rel 1e-7) and
+    taylor_green.std.exo (exodiff: relative 1e-7, floor 1e-8; x / y / z
+    velocity relative 2e-7 / 4e-7 / 3e-5)."""
+    diag = d["diag"]
+    assert rows.shape[0] == int(diag[-1, 0])
+    for ref in diag:
+        row = rows[int(ref[0]) - 1]
+        exp = ref[1:13]
+        got = row[1:13]
+        tol = np.where(np.arange(12) < 7, np.maximum(5e-4, 1e-4 * np.abs(exp)),
+                       np.maximum(5e-4, 1e-7 * np.abs(exp)))
+        assert np.all(np.abs(got - exp) <= tol), (ref[0], got, exp)
+        assert abs(got[1] / exp[1] - 1) < 1e-8  # dt, printed to 9 digits
+    idx = _by_coord(coord, d["out_coord"])
+    rel = [1e-7, 2e-7, 4e-7, 3e-5, 1e-7, 1e-7]
+    out_steps = sorted(states)
+    for j, k in enumerate(out_steps):
+        f = _fields(states[k], gamma)[:, idx]
+        ref_f = d["out_fields_all"][:6, j + 1]
+        for i in range(6):
+            m = np.maximum(np.abs(f[i]), np.abs(ref_f[i]))
+            big = m > 1e-8
+            assert np.all(np.abs(f[i] - ref_f[i])[big] <= rel[i] * m[big]), (k, i)
+
+
+def taylor_green_case():
+    d = golden("riecg_taylor_green")
+    bface = {int(k[5:]): d[k] for k in d.files if k.startswith("bface")}
+    return {"coord": d["coord"], "inpoel": d["inpoel"], "bface": bface}, d
+
+
+def test_riecg_taylor_green_golden():
+    """The reference's RieCG Taylor-Green regression (tests/regression/
+    inciter/RieCG/TaylorGreen/taylor_green.q): gamma 5/3, CFL 0.8, the
+    taylor_green manufactured energy source, the analytic state as Dirichlet
+    values on all six side sets, to t = 1 (68 steps, the last cut); the
+    oracle against the reference's diagnostics and its fields at steps 20,
+    40, 60 and 68."""
+    m, d = taylor_green_case()
+    coord, inpoel = m["coord"], m["inpoel"]
+    tri = np.concatenate([m["bface"][s] for s in sorted(m["bface"])])
+    v = oracle.vol(coord, inpoel)
+    e, de = oracle.domint(coord, inpoel)
+    o = oracle.RieCG(coord, v, e, de, tri, np.zeros(tri.shape, np.uint8), gamma=5.0 / 3.0,
+                     cfl=0.8)
+    U0 = taylor_green_state(coord)
+    dn = np.unique(tri)
+    o.set_dir(dn, np.ones((dn.size, 5), np.int32), U0[dn])
+    o.set_source("taylor_green", source_prm("taylor_green"))
+    o.set_state(U0, 0.0)
+    o.bc()
+    rows, states = taylor_green_steps(o, 1.0, v, {20, 40, 60, 68})
+    check_taylor_green_golden(rows, states, coord, d)
 
 
 def kozcg_sod_setup(m):
