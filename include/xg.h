@@ -239,6 +239,20 @@ int xg_kozcg_dt(xg_ctx* ctx, double* dt);
  * BCs; src/Inciter/KozCG.cpp:613-1197); dts and ms as in xg_riecg_run. */
 int xg_kozcg_run(xg_ctx* ctx, int64_t nstep, double* dts, float* ms);
 
+/* One KozCG step of the caller's dt (> 0) from the context's time, which
+ * then advances by dt: the step Discretization::setdt cuts to end at the
+ * final time (src/Inciter/Discretization.cpp:926-939). */
+int xg_kozcg_step(xg_ctx* ctx, double dt);
+
+/* The manufactured source of kozak::rhs (src/Physics/Kozak.cpp:125-132,
+ * 161-170): dt/8 of each node's source at the step's start time in the
+ * element's half step, and J/24 of the source at its centroid half a step
+ * later in each node's residual; problem and prm as for
+ * xg_riecg_set_source.  The time is the context's: set by
+ * xg_kozcg_set_state, advanced by xg_kozcg_run and xg_kozcg_step;
+ * xg_kozcg_rhs evaluates the sources at it.  XG_SRC_NONE switches it off. */
+int xg_kozcg_set_source(xg_ctx* ctx, int problem, const double* prm);
+
 /* ---- ChoCG ---------------------------------------------------------------- */
 
 enum xg_chorin_flux { XG_DAMP2 = 0, XG_DAMP4 = 1 };

@@ -101,7 +101,11 @@ def lib():
         L.orc_kozcg_destroy.argtypes = [_vp]
         L.orc_kozcg_set_sym.argtypes = [_vp, _i64, _vp, _vp]
         L.orc_kozcg_set_dir.argtypes = [_vp, _i64, _vp, _vp, _vp]
-        L.orc_kozcg_set_state.argtypes = [_vp, _vp]
+        L.orc_kozcg_set_state.argtypes = [_vp, _vp, _dbl]
+        L.orc_kozcg_set_source.argtypes = [_vp, C.c_int, _vp]
+        L.orc_kozcg_step.argtypes = [_vp, _dbl]
+        L.orc_kozcg_dt.argtypes = [_vp]
+        L.orc_kozcg_dt.restype = _dbl
         L.orc_kozcg_get_state.argtypes = [_vp, _vp]
         L.orc_kozcg_rhs.argtypes = [_vp, _vp, _dbl, _vp]
         L.orc_kozcg_run.argtypes = [_vp, _i64, _vp]
@@ -336,9 +340,24 @@ class KozCG:
         self._dir = (nodes, mask, vals)
         lib().orc_kozcg_set_dir(self.h, nodes.size, _p(nodes), _p(mask), _p(vals))
 
-    def set_state(self, U):
+    def set_state(self, U, t=0.0):
         U = _c(U, np.float64)
-        lib().orc_kozcg_set_state(self.h, _p(U))
+        lib().orc_kozcg_set_state(self.h, _p(U), t)
+
+    def set_source(self, problem, prm=None):
+        """The manufactured source of kozak::rhs (SOURCES names the problems;
+        prm: alpha, beta[3], kappa, r0, p0, ce)."""
+        self._src = None if prm is None else _c(np.asarray(prm, dtype=np.float64).reshape(8),
+                                                  np.float64)
+        lib().orc_kozcg_set_source(self.h, SOURCES[problem],
+                                   None if self._src is None else _p(self._src))
+
+    def dt(self):
+        return lib().orc_kozcg_dt(self.h)
+
+    def step(self, dt):
+        """One step of the given dt."""
+        lib().orc_kozcg_step(self.h, dt)
 
     def state(self):
         U = np.zeros((self.n, 5))

@@ -336,21 +336,24 @@ void riecg_grad(const RieCG& s, const real* U, real* G) {
 // problems' src functions (src/Physics/Problems.cpp: nonlinear_energy_growth
 // 163-220, rayleigh_taylor 261-332, taylor_green 433-449, vortical_flow
 // 481-508), restated from their formulas.
-void problem_source(const RieCG& s, real x, real y, real z, real t, real o[5]) {
-  const real pi = M_PI, g = s.gamma;
-  const real a = s.sprm[0], b0 = s.sprm[1], b1 = s.sprm[2], b2 = s.sprm[3];
-  const real kap = s.sprm[4], r0 = s.sprm[5], p0 = s.sprm[6], ce = s.sprm[7];
+// src: 0 none, 1 taylor_green, 2 vortical_flow, 3 nonlinear_energy_growth,
+// 4 rayleigh_taylor; sprm: alpha, beta[3], kappa, r0, p0, ce.
+void problem_source(int src, const real* sprm, real gamma, real x, real y, real z, real t,
+                    real o[5]) {
+  const real pi = M_PI, g = gamma;
+  const real a = sprm[0], b0 = sprm[1], b1 = sprm[2], b2 = sprm[3];
+  const real kap = sprm[4], r0 = sprm[5], p0 = sprm[6], ce = sprm[7];
   for (int c = 0; c < 5; ++c) o[c] = 0.0;
-  if (s.src == 1) {  // taylor_green: energy only
+  if (src == 1) {  // taylor_green: energy only
     o[4] = 3.0 * pi / 8.0 *
            (std::cos(3.0 * pi * x) * std::cos(pi * y) - std::cos(3.0 * pi * y) * std::cos(pi * x));
-  } else if (s.src == 2) {  // vortical_flow: rho = 1, linear velocity field
+  } else if (src == 2) {  // vortical_flow: rho = 1, linear velocity field
     const real rho = 1.0;
     const real mx = a * x - kap * y, my = kap * x + a * y;
     o[1] = a * mx / rho - kap * my / rho;
     o[2] = kap * mx / rho + a * my / rho;
     o[4] = (o[1] * mx + o[2] * my) / rho + 8.0 * a * a * a * z * z / (g - 1.0);
-  } else if (s.src == 3) {  // nonlinear_energy_growth
+  } else if (src == 3) {  // nonlinear_energy_growth
     const real gx = 1.0 - x * x - y * y - z * z;
     const real dg[3] = {-2.0 * x, -2.0 * y, -2.0 * z};
     const real cx = std::cos(b0 * pi * x), cy = std::cos(b1 * pi * y), cz = std::cos(b2 * pi * z);
@@ -368,7 +371,7 @@ void problem_source(const RieCG& s, real x, real y, real z, real t, real o[5]) {
       o[1 + j] = (g - 1.0) * (rho * dedx + ie * drdx);
     }
     o[4] = rho * (kap * h * h * ie4) + ie * drdt;
-  } else if (s.src == 4) {  // rayleigh_taylor
+  } else if (src == 4) {  // rayleigh_taylor
     const real gx = b0 * x * x + b1 * y * y + b2 * z * z;
     const real ft = std::cos(kap * pi * t), st = std::sin(kap * pi * t);
     const real sx = std::sin(pi * x), cx = std::cos(pi * x);
@@ -458,7 +461,7 @@ void riecg_rhs(const RieCG& s, const real* G, const real* U, real* R) {
   if (s.src)
     for (int64_t p = 0; p < n; ++p) {
       real so[5];
-      problem_source(s, s.x[p], s.y[p], s.z[p], s.t, so);
+      problem_source(s.src, s.sprm, s.gamma, s.x[p], s.y[p], s.z[p], s.t, so);
       for (int c = 0; c < 5; ++c) R[p * 5 + c] -= so[c] * s.vol[p];
     }
 }
@@ -572,12 +575,15 @@ struct KozCG {
   std::vector<real> U, R, P, Q, A;
   real t = 0, dt = 0;
   int64_t it = 0;
+  int src = 0;  // manufactured source, as RieCG's
+  real sprm[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 };
 
 inline real kpressure(const KozCG& s, real re) { return re * (s.gamma - 1.0); }
 
-// kozak::rhs (src/Physics/Kozak.cpp:29-180), no source term.
-void kozak_rhs(const KozCG& s, const real* U, real dt, real* R) {
+// kozak::rhs (src/Physics/Kozak.cpp:29-180) at time t, with the problem's
+// source when one is set (Kozak.cpp:125-132, 161-170).
+void kozak_rhs(const KozCG& s, const real* U, real t, real dt, real* R) {
   std::fill(R, R + s.npoin * 5, 0.0);
   for (int64_t e = 0; e < s.nelem; ++e) {
     const int64_t* N = &s.inpoel[e * 4];
@@ -603,6 +609,14 @@ void kozak_rhs(const KozCG& s, const real* U, real dt, real* R) {
         ue[j + 1] -= cg * p[a];
         ue[4] -= cg * (u[4] + p[a]) * uj;
       }
+    if (s.src) {  // dt/8 of each node's source at t
+      coef = dt / 8.0;
+      for (int a = 0; a < 4; ++a) {
+        real so[5];
+        problem_source(s.src, s.sprm, s.gamma, s.x[N[a]], s.y[N[a]], s.z[N[a]], t, so);
+        for (int c = 0; c < 5; ++c) ue[c] += coef * so[c];
+      }
+    }
     real r = ue[0], ru = ue[1], rv = ue[2], rw = ue[3];
     real pr = kpressure(s, ue[4] - 0.5 * (ru * ru + rv * rv + rw * rw) / r);
     coef = 1.0 / 6.0;
@@ -618,6 +632,16 @@ void kozak_rhs(const KozCG& s, const real* U, real dt, real* R) {
         Ra[j + 1] += cg * pr;
         Ra[4] += cg * (ue[4] + pr) * uj;
       }
+    }
+    if (s.src) {  // J/24 of the centroid's source at t + dt/2 to each node
+      const real xe = (s.x[N[0]] + s.x[N[1]] + s.x[N[2]] + s.x[N[3]]) / 4.0;
+      const real ye = (s.y[N[0]] + s.y[N[1]] + s.y[N[2]] + s.y[N[3]]) / 4.0;
+      const real ze = (s.z[N[0]] + s.z[N[1]] + s.z[N[2]] + s.z[N[3]]) / 4.0;
+      real se[5];
+      problem_source(s.src, s.sprm, s.gamma, xe, ye, ze, t + dt / 2.0, se);
+      coef = g.J / 24.0;
+      for (int a = 0; a < 4; ++a)
+        for (int c = 0; c < 5; ++c) R[N[a] * 5 + c] += coef * se[c];
     }
   }
 }
@@ -664,7 +688,7 @@ real kozcg_dt(const KozCG& s) {
 void kozcg_step(KozCG& s) {
   const int64_t n = s.npoin;
   const real* U = s.U.data();
-  kozak_rhs(s, U, s.dt, s.R.data());
+  kozak_rhs(s, U, s.t, s.dt, s.R.data());
   std::vector<real>& R = s.R;
   if (!s.fct) {
     for (int64_t i = 0; i < n; ++i)
@@ -1580,10 +1604,28 @@ void orc_kozcg_set_dir(void* h, int64_t n, const int64_t* nodes, const int32_t* 
   s->dirval.assign(vals, vals + n * 5);
 }
 
-void orc_kozcg_set_state(void* h, const double* U) {
+void orc_kozcg_set_state(void* h, const double* U, double t) {
   auto* s = static_cast<KozCG*>(h);
   s->U.assign(U, U + s->npoin * 5);
+  s->t = t;
 }
+
+void orc_kozcg_set_source(void* h, int problem, const double* prm) {
+  auto* s = static_cast<KozCG*>(h);
+  s->src = problem;
+  for (int k = 0; k < 8; ++k) s->sprm[k] = prm ? prm[k] : 0.0;
+}
+
+// One step of the given dt (Discretization::setdt's cut last step).
+void orc_kozcg_step(void* h, double dt) {
+  auto* s = static_cast<KozCG*>(h);
+  s->dt = dt;
+  kozcg_step(*s);
+  s->t += s->dt;
+  ++s->it;
+}
+
+double orc_kozcg_dt(void* h) { return kozcg_dt(*static_cast<KozCG*>(h)); }
 
 void orc_kozcg_get_state(void* h, double* U) {
   auto* s = static_cast<KozCG*>(h);
@@ -1591,7 +1633,8 @@ void orc_kozcg_get_state(void* h, double* U) {
 }
 
 void orc_kozcg_rhs(void* h, const double* U, double dt, double* R) {
-  kozak_rhs(*static_cast<KozCG*>(h), U, dt, R);
+  const auto* s = static_cast<KozCG*>(h);
+  kozak_rhs(*s, U, s->t, dt, R);
 }
 
 double orc_kozcg_run(void* h, int64_t nstep, double* dts) {

@@ -28,7 +28,9 @@ Sources, all read as data (nothing is executed):
     analytic state as Dirichlet values on all six side sets, to t = 1 in 68
     steps): input mesh, nodal fields at every output time
     (taylor_green.std.exo) and the diagnostics of every second step
-    (diag.std).
+    (diag.std);
+  * tests/regression/inciter/KozCG/TaylorGreen: the same problem with KozCG
+    (no FCT), the same three files.
 """
 
 from __future__ import annotations
@@ -167,6 +169,9 @@ def main(ref: str):
                                         "diag_poiseuille_damp2.std"))
     np.savez_compressed(os.path.join(HERE, "riecg_taylor_green.npz"),
                         **regression_fixture(ref, "RieCG", "TaylorGreen", "unitcube_1k.exo",
+                                             "taylor_green.std.exo", "diag.std", all_times=True))
+    np.savez_compressed(os.path.join(HERE, "kozcg_taylor_green.npz"),
+                        **regression_fixture(ref, "KozCG", "TaylorGreen", "unitcube_1k.exo",
                                              "taylor_green.std.exo", "diag.std", all_times=True))
     print("wrote fixtures to", HERE)
 

@@ -10,9 +10,11 @@ import numpy as np
 import pytest
 
 import oracle
-from common import random_state, sod_mesh, wave_ic
+from common import random_state, sod_mesh, taylor_green_state, wave_ic
 from gpu_util import ctx, relerr
-from test_oracle_pins import _by_coord, _fields, kozcg_sod_setup
+from test_oracle_pins import (SOURCE_CASES, _by_coord, _fields, check_taylor_green_golden,
+                              kozcg_sod_setup, source_prm, taylor_green_case_kozcg,
+                              taylor_green_steps)
 from xyst_gb300 import kozcg, mesh, riecg
 
 pytestmark = pytest.mark.gpu
@@ -30,6 +32,45 @@ def test_dropin_rhs():
     d = kozcg.KozCG(ctx(), m["coord"], v, m["inpoel"])
     o = oracle.KozCG(m["coord"], v, m["inpoel"])
     assert relerr(d.rhs(U, 2.5e-3), o.rhs(U, 2.5e-3)) < 1e-12
+
+
+@pytest.mark.parametrize("problem", sorted(SOURCE_CASES))
+def test_dropin_rhs_with_source(problem):
+    """kozak::rhs with a manufactured source at the context's time t = 0.3
+    (nodes' sources at t, centroids' at t + dt/2): FP64 against the oracle,
+    itself pinned bit for bit to the reference's compiled function."""
+    m, v = _cube()
+    U = random_state(m["coord"].shape[1], 6)
+    d = kozcg.KozCG(ctx(), m["coord"], v, m["inpoel"])
+    o = oracle.KozCG(m["coord"], v, m["inpoel"])
+    for s in (d, o):
+        s.set_source(problem, source_prm(problem))
+        s.set_state(U, 0.3)
+    R = d.rhs(U, 2.5e-3)
+    Ro = o.rhs(U, 2.5e-3)
+    assert relerr(R, Ro) < 1e-12
+    d.set_source("none")
+    assert relerr(d.rhs(U, 2.5e-3), Ro) > 1e-10  # the source was on
+
+
+def test_taylor_green_reference_baseline_on_gpu():
+    """The reference's KozCG Taylor-Green regression on the GPU in FP64 (no
+    FCT, the taylor_green source, Dirichlet on all six side sets, 68 steps
+    to t = 1 with the last one cut by xg_kozcg_step): every second step's
+    diagnostics within 1e-7 relative and the fields at steps 20, 40, 60 and
+    68 within the reference's exodiff tolerances."""
+    m, dd = taylor_green_case_kozcg()
+    coord, inpoel = m["coord"], m["inpoel"]
+    v = riecg.volumes(coord, inpoel)
+    d = kozcg.KozCG(ctx(), coord, v, inpoel, gamma=5.0 / 3.0, cfl=0.8, fct=False)
+    U0 = taylor_green_state(coord)
+    dn = np.unique(np.concatenate([m["bface"][s] for s in sorted(m["bface"])]))
+    d.set_bc(dir=(dn, np.ones((dn.size, 5), np.int32), U0[dn]))
+    d.set_source("taylor_green", source_prm("taylor_green"))
+    d.set_state(U0, 0.0)
+    rows, states = taylor_green_steps(d, 1.0, v, {20, 40, 60, 68})
+    check_taylor_green_golden(rows, states, coord, dd, kozcg=True)
+    assert abs(d.state()[1] - 1.0) < 1e-15
 
 
 def test_dropin_rhs_fp32_bound():

@@ -41,6 +41,7 @@
 #include <vector>
 
 #include "xg_internal.hpp"
+#include "xg_source.cuh"
 
 namespace xg {
 
@@ -52,6 +53,7 @@ struct KScalars {
   unsigned long long dtmin;
   int32_t blowup;
   int32_t pad;
+  double t, tnext;  // the current step's start time, the next step's
 };
 }  // namespace
 
@@ -90,11 +92,18 @@ struct KozCGDev {
   int64_t dthist_cap = 0;
   double t = 0.0;
   bool dt_valid = false;
+  // manufactured source (kozak::rhs with problems::SRC): per step the
+  // sources at the nodes at the step's start time S [5][n] and at the
+  // element centroids half a step later Se [ne][5]
+  SrcPrm src{};
+  double *S = nullptr, *Se = nullptr;
 };
 
 void destroy_kozcg(KozCGDev* d) {
   if (!d) return;
   if (d->dthist) cudaFree(d->dthist);
+  if (d->S) cudaFree(d->S);
+  if (d->Se) cudaFree(d->Se);
   delete d;
 }
 size_t bytes_kozcg(const KozCGDev* d) { return d ? d->arena.bytes() + d->bcarena.bytes() : 0; }
@@ -332,7 +341,9 @@ __device__ __forceinline__ void elem_terms(int64_t n, int64_t ne, int64_t e,
                                            const double* __restrict__ U, const F* __restrict__ Uf,
                                            const F* __restrict__ V,
                                            const KScalars* __restrict__ sc, F gamma, F ctau,
-                                           int fct, int32_t N[4], F r[4][5], F aec[4][5]) {
+                                           int fct, const double* __restrict__ S,
+                                           const double* __restrict__ Se, int32_t N[4],
+                                           F r[4][5], F aec[4][5]) {
   for (int a = 0; a < 4; ++a) N[a] = inpoel[e * 4 + a];
   const Geo<F> t = elem_geo<F>(xyz, geo, n, ne, e, N);
   F u[4][5], vel[4][3], p[4];
@@ -360,6 +371,11 @@ __device__ __forceinline__ void elem_terms(int64_t n, int64_t ne, int64_t e,
       ue[j + 1] -= cg * p[a];
       ue[4] -= cg * (u[a][4] + p[a]) * uj;
     }
+  if (S) {  // the nodes' sources at the step's start time, dt/8 each
+    const F c8 = dt / F(8.0);
+    for (int a = 0; a < 4; ++a)
+      for (int c = 0; c < 5; ++c) ue[c] += c8 * F(__ldg(S + c * n + N[a]));
+  }
   const F pr =
       (gamma - F(1.0)) * (ue[4] - F(0.5) * (ue[1] * ue[1] + ue[2] * ue[2] + ue[3] * ue[3]) / ue[0]);
   for (int a = 0; a < 4; ++a)
@@ -376,6 +392,13 @@ __device__ __forceinline__ void elem_terms(int64_t n, int64_t ne, int64_t e,
       r[a][j + 1] += cg * pr;
       r[a][4] += cg * (ue[4] + pr) * uj;
     }
+  }
+  if (Se) {  // the centroid's source half a step later, J/24 to each node
+    const F cj = t.J / F(24.0);
+    F se[5];
+    for (int c = 0; c < 5; ++c) se[c] = F(__ldg(Se + e * 5 + c));
+    for (int a = 0; a < 4; ++a)
+      for (int c = 0; c < 5; ++c) r[a][c] += cj * se[c];
   }
   for (int c = 0; c < 5; ++c)
     for (int a = 0; a < 4; ++a) {
@@ -400,13 +423,15 @@ __global__ void __launch_bounds__(kBlock) k_elem_rhs_aec32(int64_t n, int64_t ne
                                                             const float* __restrict__ V,
                                                             const KScalars* __restrict__ sc,
                                                             double gamma, double ctau, int fct,
+                                                            const double* __restrict__ S,
+                                                            const double* __restrict__ Se,
                                                             float* R) {
   const int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (e >= ne) return;
   int32_t N[4];
   float r[4][5], aec[4][5];
   elem_terms<float>(n, ne, e, inpoel, nullptr, geo, nullptr, Uf, V, sc, float(gamma),
-                    float(ctau), fct, N, r, aec);
+                    float(ctau), fct, S, Se, N, r, aec);
   if (!fct) {
     for (int a = 0; a < 4; ++a) add5<kRP>(R, n, N[a], r[a]);
     return;
@@ -457,6 +482,8 @@ __global__ void __launch_bounds__(kEB) k_elem_rhs64(int64_t n, int64_t ne,
                                                      const double* __restrict__ V,
                                                      const KScalars* __restrict__ sc,
                                                      double gamma, double ctau, int fct,
+                                                     const double* __restrict__ S,
+                                                     const double* __restrict__ Se,
                                                      double* __restrict__ E) {
   __shared__ double2 st[kEB / 32][32 * kStW];
   const int lane = threadIdx.x & 31;
@@ -467,8 +494,8 @@ __global__ void __launch_bounds__(kEB) k_elem_rhs64(int64_t n, int64_t ne,
   if (e < ne) {
     int32_t N[4];
     double r[4][5], aec[4][5];
-    elem_terms<double>(n, ne, e, inpoel, xyz, nullptr, U, nullptr, V, sc, gamma, ctau, fct, N, r,
-                       aec);
+    elem_terms<double>(n, ne, e, inpoel, xyz, nullptr, U, nullptr, V, sc, gamma, ctau, fct, S, Se,
+                       N, r, aec);
     for (int a = 0; a < 4; ++a) {
       double2* b = buf + lane * kStW + a * kRecD2;
       b[0] = make_double2(r[a][0], r[a][1]);
@@ -875,12 +902,51 @@ __global__ void k_step_begin(KScalars* s, double cfl, double const_dt, double* h
     dt = __longlong_as_double(s->dtmin) * cfl;
   if (dt < DBL_EPSILON) s->blowup = 1;
   s->dt = dt;
+  s->t = s->tnext;
+  s->tnext = s->t + dt;
   s->dtmin = __double_as_longlong(DBL_MAX);
   if (hist) hist[k] = dt;
 }
+// A step of the caller's dt from time t (its CFL minimum starts afresh).
+__global__ void k_set_step(KScalars* s, double t, double dt) {
+  s->t = t;
+  s->dt = dt;
+  s->tnext = t + dt;
+  s->dtmin = __double_as_longlong(DBL_MAX);
+}
+__global__ void k_set_time(KScalars* s, double t) {
+  s->t = t;
+  s->tnext = t;
+}
+
+// The sources kozak::rhs adds (src/Physics/Kozak.cpp:125-132, 161-170): at
+// every node at the step's start time, S [5][n], and at every element's
+// centroid (the mean of its nodes' coordinates) half a step later, Se [ne][5].
+__global__ void k_src_nodes(int64_t n, SrcPrm q, const KScalars* __restrict__ sc,
+                            const double* __restrict__ xyz, double* __restrict__ S) {
+  const int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (p >= n) return;
+  double o[5];
+  problem_source(q, xyz[p], xyz[n + p], xyz[2 * n + p], sc->t, o);
+  for (int c = 0; c < 5; ++c) S[c * n + p] = o[c];
+}
+__global__ void k_src_elems(int64_t n, int64_t ne, SrcPrm q, const KScalars* __restrict__ sc,
+                            const int32_t* __restrict__ inpoel, const double* __restrict__ xyz,
+                            double* __restrict__ Se) {
+  const int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (e >= ne) return;
+  const int32_t* N = inpoel + e * 4;
+  double c3[3];
+  for (int j = 0; j < 3; ++j) {
+    const double* x = xyz + j * n;
+    c3[j] = (x[N[0]] + x[N[1]] + x[N[2]] + x[N[3]]) / 4.0;
+  }
+  double o[5];
+  problem_source(q, c3[0], c3[1], c3[2], sc->t + sc->dt / 2.0, o);
+  for (int c = 0; c < 5; ++c) Se[e * 5 + c] = o[c];
+}
 
 __global__ void k_reset_min(KScalars* s) { s->dtmin = __double_as_longlong(DBL_MAX); }
-__global__ void k_set_dt(KScalars* s, double dt) { s->dt = dt; }
 
 __global__ void k_aos_to_soa(int64_t n, int nc, const double* __restrict__ a,
                              double* __restrict__ s) {
@@ -936,10 +1002,19 @@ KArrays<float> arrays32(KozCGDev* d) {
 template <class F>
 void galerkin(cudaStream_t s, KozCGDev* d, const KArrays<F>& k, const double* U, int fct) {
   const int64_t n = d->n, ne = d->ne;
+  const double *S = nullptr, *Se = nullptr;
+  if (d->src.problem != XG_SRC_NONE) {
+    k_src_nodes<<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, d->src, d->scal, d->xyz, d->S);
+    k_src_elems<<<blocks_for(ne, kBlock), kBlock, 0, s>>>(n, ne, d->src, d->scal, d->inpoel,
+                                                          d->xyz, d->Se);
+    S = d->S;
+    Se = d->Se;
+  }
   k_node_prim<F><<<blocks_for(n, kBlock), kBlock, 0, s>>>(n, U, d->prm.gamma, k.V, k.Uf);
   if constexpr (sizeof(F) == 8) {
     k_elem_rhs64<<<blocks_for(ne, kEB), kEB, 0, s>>>(n, ne, d->inpoel, d->xyz, U, k.V, d->scal,
-                                                     d->prm.gamma, d->prm.ctau, fct, d->E);
+                                                     d->prm.gamma, d->prm.ctau, fct, S, Se,
+                                                     d->E);
     if (fct)
       k_node_gather<kRecD2, true><<<blocks_for(n, kBlock), kBlock, 0, s>>>(
           n, d->soff, d->sw, d->sslot, d->E, d->R, d->P);
@@ -949,7 +1024,7 @@ void galerkin(cudaStream_t s, KozCGDev* d, const KArrays<F>& k, const double* U,
   } else {
     k_elem_rhs_aec32<<<blocks_for(ne, kBlock), kBlock, 0, s>>>(n, ne, d->inpoel, k.geo, k.Uf, k.V,
                                                                 d->scal, d->prm.gamma,
-                                                                d->prm.ctau, fct, k.R);
+                                                                d->prm.ctau, fct, S, Se, k.R);
   }
 }
 
@@ -1334,7 +1409,7 @@ int xg_kozcg_rhs(xg_ctx* c, const double* U, double dt, double* R) {
   XG_CUDA(c, cudaMemcpyAsync(d->stage, U, d->n * 5 * 8, cudaMemcpyHostToDevice, s));
   k_aos_to_soa<<<blocks_for(d->n * 5, kBlock), kBlock, 0, s>>>(d->n, 5, d->stage, d->A);
   XG_CHECK_LAUNCH(c);
-  k_set_dt<<<1, 1, 0, s>>>(d->scal, dt);
+  k_set_step<<<1, 1, 0, s>>>(d->scal, d->t, dt);  // the sources at the context's time
   XG_CHECK_LAUNCH(c);
   if (d->prm.precision == XG_FP32_FLUX) {
     const KArrays<float> k = arrays32(d);
@@ -1410,6 +1485,8 @@ int xg_kozcg_run(xg_ctx* c, int64_t nstep, double* dts, float* ms) {
     XG_CUDA(c, cudaMalloc(&d->dthist, nstep * sizeof(double)));
     d->dthist_cap = nstep;
   }
+  k_set_time<<<1, 1, 0, c->stream>>>(d->scal, d->t);
+  XG_CHECK_LAUNCH(c);
   cudaEvent_t e0, e1;
   XG_CUDA(c, cudaEventCreate(&e0));
   XG_CUDA(c, cudaEventCreate(&e1));
@@ -1435,6 +1512,42 @@ int xg_kozcg_run(xg_ctx* c, int64_t nstep, double* dts, float* ms) {
   KScalars s;
   XG_CUDA(c, cudaMemcpy(&s, d->scal, sizeof(s), cudaMemcpyDeviceToHost));
   if (s.blowup) return fail(c, XG_ERR_BLOWUP, "dt below machine epsilon");
+  return XG_OK;
+}
+
+int xg_kozcg_step(xg_ctx* c, double dt) {
+  int rc = use(c);
+  if (rc) return rc;
+  KozCGDev* d = c->kozcg;
+  if (!d) return fail(c, XG_ERR_STATE, "kozcg_step before kozcg_setup");
+  if (!(dt > 0.0) || !std::isfinite(dt)) return fail(c, XG_ERR_ARG, "kozcg_step: dt must be > 0");
+  k_set_step<<<1, 1, 0, c->stream>>>(d->scal, d->t, dt);
+  XG_CHECK_LAUNCH(c);
+  rc = step(c, d);
+  if (rc) return rc;
+  XG_CUDA(c, cudaStreamSynchronize(c->stream));
+  d->t += dt;
+  d->dt_valid = true;  // the step's solve formed the next CFL minimum
+  return XG_OK;
+}
+
+int xg_kozcg_set_source(xg_ctx* c, int problem, const double* prm) {
+  int rc = use(c);
+  if (rc) return rc;
+  KozCGDev* d = c->kozcg;
+  if (!d) return fail(c, XG_ERR_STATE, "kozcg_set_source before kozcg_setup");
+  if (problem < XG_SRC_NONE || problem > XG_SRC_RAYLEIGH_TAYLOR)
+    return fail(c, XG_ERR_ARG, "kozcg_set_source: unknown problem");
+  if (problem != XG_SRC_NONE && problem != XG_SRC_TAYLOR_GREEN && !prm)
+    return fail(c, XG_ERR_ARG, "kozcg_set_source: this problem needs its parameters");
+  XG_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (problem != XG_SRC_NONE && !d->S) {
+    XG_CUDA(c, cudaMalloc(&d->S, d->n * 5 * sizeof(double)));
+    XG_CUDA(c, cudaMalloc(&d->Se, std::max<int64_t>(1, d->ne) * 5 * sizeof(double)));
+  }
+  d->src.problem = problem;
+  for (int k = 0; k < 8; ++k) d->src.p[k] = prm ? prm[k] : 0.0;
+  d->src.gamma = d->prm.gamma;
   return XG_OK;
 }
 

@@ -74,3 +74,16 @@ class KozCG:
         ms = C.c_float()
         self.ctx.check(self.lib.xg_kozcg_run(self.ctx.h, nstep, p(dts), C.byref(ms)))
         return dts, ms.value
+
+    def step(self, dt):
+        """One step of the given dt (the last step cut to the final time)."""
+        self.ctx.check(self.lib.xg_kozcg_step(self.ctx.h, float(dt)))
+
+    def set_source(self, problem, prm=None):
+        """The manufactured source of kozak::rhs (riecg.SOURCES names the
+        problems; src/Physics/Kozak.cpp:125-132, 161-170) with the
+        control-file parameters prm = alpha, beta[3], kappa, r0, p0, ce."""
+        from .riecg import SOURCES
+        self._src = None if prm is None else f64(np.asarray(prm, dtype=np.float64).reshape(8))
+        self.ctx.check(self.lib.xg_kozcg_set_source(self.ctx.h, SOURCES[problem],
+                                                    None if self._src is None else p(self._src)))

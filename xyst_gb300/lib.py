@@ -79,6 +79,8 @@ SIGNATURES = {
     "xg_kozcg_bc": (_int, [_vp]),
     "xg_kozcg_dt": (_int, [_vp, _vp]),
     "xg_kozcg_run": (_int, [_vp, _i64, _vp, _vp]),
+    "xg_kozcg_step": (_int, [_vp, _dbl]),
+    "xg_kozcg_set_source": (_int, [_vp, _int, _vp]),
     "xg_chocg_setup": (_int, [_vp, C.POINTER(ChocgParams), _i64, _vp, _vp, _i64, _vp, _vp,
                               _i64, _vp, _vp, _i64, _vp, _vp, _i64, _vp]),
     "xg_chocg_set_bc": (_int, [_vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp, _i64, _vp, _i64, _vp,
