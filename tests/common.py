@@ -47,6 +47,21 @@ def taylor_green_state(coord, gamma=5.0 / 3.0):
     return U
 
 
+def vortical_flow_state(coord, a=0.1, k=1.0, p0=10.0, gamma=5.0 / 3.0):
+    """The vortical flow (problems::vortical_flow::ic, src/Physics/
+    Problems.cpp:453-478): rho = 1, momentum (a x - k y, k x + a y, -2 a z),
+    p = p0 - 2 a^2 z^2."""
+    x, y, z = coord
+    U = np.zeros((coord.shape[1], 5))
+    U[:, 0] = 1.0
+    U[:, 1] = a * x - k * y
+    U[:, 2] = k * x + a * y
+    U[:, 3] = -2.0 * a * z
+    U[:, 4] = (U[:, 1] ** 2 + U[:, 2] ** 2 + U[:, 3] ** 2) / 2.0 + (p0 - 2.0 * a * a * z * z) / (
+        gamma - 1.0)
+    return U
+
+
 def wave_ic(coord, gamma=1.4):
     """Smooth density wave rho = 1 + 0.2 sin(2 pi x) sin(2 pi y) sin(2 pi z),
     u = (1, 0.5, 0.25), p = 1."""

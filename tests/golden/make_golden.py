@@ -30,7 +30,12 @@ Sources, all read as data (nothing is executed):
     (taylor_green.std.exo) and the diagnostics of every second step
     (diag.std);
   * tests/regression/inciter/KozCG/TaylorGreen: the same problem with KozCG
-    (no FCT), the same three files.
+    (no FCT), the same three files;
+  * tests/regression/inciter/{RieCG,KozCG}/VorticalFlow: the vortical flow
+    with its manufactured source (alpha 0.1, kappa 1, p0 10, gamma 5/3, CFL
+    0.8, the analytic state as Dirichlet values on all six side sets, to
+    t = 1), RieCG with and without stab2 and KozCG without FCT: the same
+    three files each.
 """
 
 from __future__ import annotations
@@ -173,6 +178,15 @@ def main(ref: str):
     np.savez_compressed(os.path.join(HERE, "kozcg_taylor_green.npz"),
                         **regression_fixture(ref, "KozCG", "TaylorGreen", "unitcube_1k.exo",
                                              "taylor_green.std.exo", "diag.std", all_times=True))
+    for scheme, name, out, diag in (("RieCG", "riecg_vortical_flow", "vortical_flow.std.exo",
+                                     "diag.std"),
+                                    ("RieCG", "riecg_vortical_flow_stab2",
+                                     "vortical_flow_stab2.std.exo", "diag_stab2.std"),
+                                    ("KozCG", "kozcg_vortical_flow", "vortical_flow.std.exo",
+                                     "diag.std")):
+        np.savez_compressed(os.path.join(HERE, name + ".npz"),
+                            **regression_fixture(ref, scheme, "VorticalFlow", "unitcube_1k.exo",
+                                                 out, diag, all_times=True))
     print("wrote fixtures to", HERE)
 
 

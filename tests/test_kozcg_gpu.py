@@ -10,11 +10,11 @@ import numpy as np
 import pytest
 
 import oracle
-from common import random_state, sod_mesh, taylor_green_state, wave_ic
+from common import random_state, sod_mesh, wave_ic
 from gpu_util import ctx, relerr
-from test_oracle_pins import (SOURCE_CASES, _by_coord, _fields, check_taylor_green_golden,
-                              kozcg_sod_setup, source_prm, taylor_green_case_kozcg,
-                              taylor_green_steps)
+from test_oracle_pins import (GOLDEN_CASES, KOZCG_GOLDEN, SOURCE_CASES, _by_coord, _fields,
+                              check_golden, golden_case, golden_run, kozcg_sod_setup,
+                              source_prm)
 from xyst_gb300 import kozcg, mesh, riecg
 
 pytestmark = pytest.mark.gpu
@@ -53,23 +53,25 @@ def test_dropin_rhs_with_source(problem):
     assert relerr(d.rhs(U, 2.5e-3), Ro) > 1e-10  # the source was on
 
 
-def test_taylor_green_reference_baseline_on_gpu():
-    """The reference's KozCG Taylor-Green regression on the GPU in FP64 (no
-    FCT, the taylor_green source, Dirichlet on all six side sets, 68 steps
-    to t = 1 with the last one cut by xg_kozcg_step): every second step's
-    diagnostics within 1e-7 relative and the fields at steps 20, 40, 60 and
-    68 within the reference's exodiff tolerances."""
-    m, dd = taylor_green_case_kozcg()
+@pytest.mark.parametrize("name", KOZCG_GOLDEN)
+def test_manufactured_solution_baselines_on_gpu(name):
+    """The reference's KozCG Taylor-Green and vortical-flow regressions on
+    the GPU in FP64 (no FCT, the problem's source, Dirichlet on all six side
+    sets, to t = 1 with the last step cut by xg_kozcg_step): every
+    diagnostics row within 1e-7 relative and the fields at every output time
+    within the reference's exodiff tolerances."""
+    m, dd, state = golden_case(name)
+    problem = GOLDEN_CASES[name][0]
     coord, inpoel = m["coord"], m["inpoel"]
     v = riecg.volumes(coord, inpoel)
     d = kozcg.KozCG(ctx(), coord, v, inpoel, gamma=5.0 / 3.0, cfl=0.8, fct=False)
-    U0 = taylor_green_state(coord)
+    U0 = state(coord)
     dn = np.unique(np.concatenate([m["bface"][s] for s in sorted(m["bface"])]))
     d.set_bc(dir=(dn, np.ones((dn.size, 5), np.int32), U0[dn]))
-    d.set_source("taylor_green", source_prm("taylor_green"))
+    d.set_source(problem, source_prm(problem))
     d.set_state(U0, 0.0)
-    rows, states = taylor_green_steps(d, 1.0, v, {20, 40, 60, 68})
-    check_taylor_green_golden(rows, states, coord, dd, kozcg=True)
+    rows, states = golden_run(d, 1.0, v)
+    check_golden(name, rows, states, coord, dd)
     assert abs(d.state()[1] - 1.0) < 1e-15
 
 

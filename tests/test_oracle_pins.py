@@ -13,7 +13,7 @@ import pytest
 import oracle
 import oracle.ref as ref
 from common import (dirichlet_matrix_only, golden, laplacian_14, random_state, sod_ic, sod_mesh,
-                    taylor_green_state)
+                    taylor_green_state, vortical_flow_state)
 from xyst_gb300 import mesh
 
 needs_ref = pytest.mark.skipif(not ref.available(), reason="reference sources not built here")
@@ -248,20 +248,53 @@ def test_riecg_sod_golden():
     assert abs(t - float(d["final_time"])) < 1e-8
 
 
-def taylor_green_steps(solver, term, vol, steps_out):
-    """Steps of the reference's Taylor-Green regression on solver (an oracle
-    or device RieCG or KozCG): the CFL step of each step's start state, the
-    last one cut to end at term (Discretization::setdt, src/Inciter/
-    Discretization.cpp:926-939); RieCG's stages driven one by one, KozCG's
-    steps given their dt.  Returns the diagnostics rows (t, dt, L2 of U, L2
-    of the step's change; NodeDiagnostics norms) and the states after the
-    steps listed in steps_out."""
+# The reference's manufactured-solution regressions (tests/regression/
+# inciter/{RieCG,KozCG}/{TaylorGreen,VorticalFlow}): gamma 5/3, CFL 0.8, the
+# problem's source, its analytic state as Dirichlet values on all six side
+# sets, to t = 1 with the last step cut.  Per case: the problem, its state,
+# RieCG's stab2, the numdiff tolerances (abs, rel; either suffices) of the
+# diagnostics columns t .. L2(rE) and L2(dr) .. L2(drE), and the exodiff
+# relative tolerances (floor 1e-8) of density, x/y/z velocity, energy and
+# pressure (each case's diag.ndiff.cfg and exodiff.cfg).
+GOLDEN_CASES = {
+    "riecg_taylor_green": ("taylor_green", False, ((5e-4, 1e-4), (5e-4, 1e-7)),
+                           (1e-7, 2e-7, 4e-7, 3e-5, 1e-7, 1e-7)),
+    "riecg_vortical_flow": ("vortical_flow", False, ((3e-5, 2e-5), (1e-2, 1e-7)),
+                            (1e-7, 7e-6, 4e-6, 2e-5, 1e-7, 1e-7)),
+    "riecg_vortical_flow_stab2": ("vortical_flow", True, ((3e-5, 2e-5), (1e-2, 1e-7)),
+                                  (1e-7, 7e-6, 4e-6, 2e-5, 1e-7, 1e-7)),
+    "kozcg_taylor_green": ("taylor_green", False, ((0.0, 1e-7), (0.0, 1e-7)),
+                           (1e-7, 2e-7, 4e-7, 3e-5, 1e-7, 1e-7)),
+    "kozcg_vortical_flow": ("vortical_flow", False, ((0.0, 1e-7), (0.0, 1e-7)),
+                            (1e-7, 7e-6, 4e-6, 7e-6, 1e-7, 1e-7)),
+}
+RIECG_GOLDEN = sorted(k for k in GOLDEN_CASES if k.startswith("riecg"))
+KOZCG_GOLDEN = sorted(k for k in GOLDEN_CASES if k.startswith("kozcg"))
+
+
+def golden_case(name):
+    """(mesh, fixture, analytic state on the mesh) of a regression case."""
+    d = golden(name)
+    bface = {int(k[5:]): d[k] for k in d.files if k.startswith("bface")}
+    m = {"coord": d["coord"], "inpoel": d["inpoel"], "bface": bface}
+    problem = GOLDEN_CASES[name][0]
+    state = taylor_green_state if problem == "taylor_green" else vortical_flow_state
+    return m, d, state
+
+
+def golden_run(solver, term, vol):
+    """Steps of a regression case on solver (an oracle or device RieCG or
+    KozCG): the CFL step of each step's start state, the last one cut to end
+    at term (Discretization::setdt, src/Inciter/Discretization.cpp:926-939);
+    RieCG's stages driven one by one, KozCG's steps given their dt.  Returns
+    the diagnostics rows (step, t, dt, L2 of U, L2 of the step's change:
+    NodeDiagnostics norms) and the state after every step."""
     def state():
         s = solver.state()
         return s[0] if isinstance(s, tuple) else s  # the device's (U, t)
 
     Vt = vol.sum()
-    t, k, rows, states = 0.0, 0, [], {}
+    t, k, rows, states = 0.0, 0, [], []
     while abs(t - term) >= np.finfo(float).eps:
         Uo = state()
         dt = solver.dt()
@@ -278,97 +311,68 @@ def taylor_green_steps(solver, term, vol, steps_out):
         l2 = np.sqrt((U ** 2 * vol[:, None]).sum(0) / Vt)
         l2r = np.sqrt(((U - Uo) ** 2 * vol[:, None]).sum(0) / Vt)
         rows.append(np.concatenate([[k, t, dt], l2, l2r]))
-        if k in steps_out:
-            states[k] = U.copy()
+        states.append(U.copy())
         assert k < 1000
     return np.array(rows), states
 
 
-def check_taylor_green_golden(rows, states, coord, d, gamma=5.0 / 3.0, kozcg=False):
-    """Against the reference's diag.std (every second step; numdiff for
-    RieCG: t, dt and L2 of U abs 5e-4 or rel 1e-4, L2 of the change abs 5e-4
-    or rel 1e-7; for KozCG rel 1e-7 throughout) and taylor_green.std.exo
-    (exodiff: relative 1e-7, floor 1e-8; x / y / z velocity relative 2e-7 /
-    4e-7 / 3e-5)."""
+def check_golden(name, rows, states, coord, d, gamma=5.0 / 3.0):
+    """A run against the case's diag.std (every row it holds) and its fields
+    at every output time after the first, within the case's tolerances."""
+    _, _, (t1, t2), frel = GOLDEN_CASES[name]
     diag = d["diag"]
     assert rows.shape[0] == int(diag[-1, 0])
     for ref in diag:
-        row = rows[int(ref[0]) - 1]
+        got = rows[int(ref[0]) - 1, 1:13]
         exp = ref[1:13]
-        got = row[1:13]
-        if kozcg:
-            tol = 1e-7 * np.abs(exp)
-        else:
-            tol = np.where(np.arange(12) < 7, np.maximum(5e-4, 1e-4 * np.abs(exp)),
-                           np.maximum(5e-4, 1e-7 * np.abs(exp)))
+        tol = np.where(np.arange(12) < 7, np.maximum(t1[0], t1[1] * np.abs(exp)),
+                       np.maximum(t2[0], t2[1] * np.abs(exp)))
         assert np.all(np.abs(got - exp) <= tol), (ref[0], got, exp)
         assert abs(got[1] / exp[1] - 1) < 1e-8  # dt, printed to 9 digits
     idx = _by_coord(coord, d["out_coord"])
-    rel = [1e-7, 2e-7, 4e-7, 3e-5, 1e-7, 1e-7]
-    out_steps = sorted(states)
-    for j, k in enumerate(out_steps):
+    for j, tau in enumerate(d["out_times"][1:]):
+        k = int(np.argmin(np.abs(rows[:, 1] - tau)))
+        assert abs(rows[k, 1] - tau) < 1e-9, (tau, rows[k, 1])
         f = _fields(states[k], gamma)[:, idx]
         ref_f = d["out_fields_all"][:6, j + 1]
         for i in range(6):
             m = np.maximum(np.abs(f[i]), np.abs(ref_f[i]))
             big = m > 1e-8
-            assert np.all(np.abs(f[i] - ref_f[i])[big] <= rel[i] * m[big]), (k, i)
+            assert np.all(np.abs(f[i] - ref_f[i])[big] <= frel[i] * m[big]), (tau, i)
 
 
-def taylor_green_case():
-    d = golden("riecg_taylor_green")
-    bface = {int(k[5:]): d[k] for k in d.files if k.startswith("bface")}
-    return {"coord": d["coord"], "inpoel": d["inpoel"], "bface": bface}, d
-
-
-def test_riecg_taylor_green_golden():
-    """The reference's RieCG Taylor-Green regression (tests/regression/
-    inciter/RieCG/TaylorGreen/taylor_green.q): gamma 5/3, CFL 0.8, the
-    taylor_green manufactured energy source, the analytic state as Dirichlet
-    values on all six side sets, to t = 1 (68 steps, the last cut); the
-    oracle against the reference's diagnostics and its fields at steps 20,
-    40, 60 and 68."""
-    m, d = taylor_green_case()
+def oracle_golden_solver(name):
+    """The oracle on a regression case, set up as its control file says."""
+    m, d, state = golden_case(name)
+    problem, stab2 = GOLDEN_CASES[name][:2]
     coord, inpoel = m["coord"], m["inpoel"]
     tri = np.concatenate([m["bface"][s] for s in sorted(m["bface"])])
     v = oracle.vol(coord, inpoel)
-    e, de = oracle.domint(coord, inpoel)
-    o = oracle.RieCG(coord, v, e, de, tri, np.zeros(tri.shape, np.uint8), gamma=5.0 / 3.0,
-                     cfl=0.8)
-    U0 = taylor_green_state(coord)
+    U0 = state(coord)
     dn = np.unique(tri)
+    if name.startswith("riecg"):
+        e, de = oracle.domint(coord, inpoel)
+        o = oracle.RieCG(coord, v, e, de, tri, np.zeros(tri.shape, np.uint8), gamma=5.0 / 3.0,
+                         cfl=0.8, stab2=stab2)
+    else:
+        o = oracle.KozCG(coord, v, inpoel, gamma=5.0 / 3.0, cfl=0.8, fct=False)
     o.set_dir(dn, np.ones((dn.size, 5), np.int32), U0[dn])
-    o.set_source("taylor_green", source_prm("taylor_green"))
+    o.set_source(problem, source_prm(problem))
     o.set_state(U0, 0.0)
-    o.bc()
-    rows, states = taylor_green_steps(o, 1.0, v, {20, 40, 60, 68})
-    check_taylor_green_golden(rows, states, coord, d)
+    if name.startswith("riecg"):
+        o.bc()
+    return o, m, d, v
 
 
-def taylor_green_case_kozcg():
-    d = golden("kozcg_taylor_green")
-    bface = {int(k[5:]): d[k] for k in d.files if k.startswith("bface")}
-    return {"coord": d["coord"], "inpoel": d["inpoel"], "bface": bface}, d
-
-
-def test_kozcg_taylor_green_golden():
-    """The reference's KozCG Taylor-Green regression (tests/regression/
-    inciter/KozCG/TaylorGreen/taylor_green.q): no FCT, gamma 5/3, CFL 0.8,
-    the taylor_green source in kozak::rhs, the analytic state as Dirichlet
-    values on all six side sets, to t = 1 (68 steps, the last cut); the
-    oracle against the reference's diagnostics and its fields at steps 20,
-    40, 60 and 68."""
-    m, d = taylor_green_case_kozcg()
-    coord, inpoel = m["coord"], m["inpoel"]
-    v = oracle.vol(coord, inpoel)
-    k = oracle.KozCG(coord, v, inpoel, gamma=5.0 / 3.0, cfl=0.8, fct=False)
-    U0 = taylor_green_state(coord)
-    dn = np.unique(np.concatenate([m["bface"][s] for s in sorted(m["bface"])]))
-    k.set_dir(dn, np.ones((dn.size, 5), np.int32), U0[dn])
-    k.set_source("taylor_green", source_prm("taylor_green"))
-    k.set_state(U0, 0.0)
-    rows, states = taylor_green_steps(k, 1.0, v, {20, 40, 60, 68})
-    check_taylor_green_golden(rows, states, coord, d, kozcg=True)
+@pytest.mark.parametrize("name", sorted(GOLDEN_CASES))
+def test_manufactured_solution_golden(name):
+    """The oracle on the reference's Taylor-Green and vortical-flow
+    regressions of RieCG (with and without stab2) and KozCG (no FCT): every
+    diagnostics row and the fields at every output time within the
+    reference's own numdiff and exodiff tolerances."""
+    o, m, d, v = oracle_golden_solver(name)
+    rows, states = golden_run(o, 1.0, v)
+    check_golden(name, rows, states, m["coord"], d)
 
 
 def kozcg_sod_setup(m):

@@ -7,9 +7,10 @@ fluxes, FP64 state and update) is held to the bound stated in each test."""
 import numpy as np
 import pytest
 
-from common import random_state, sod_ic, sod_mesh, taylor_green_state, wave_ic
+from common import random_state, sod_ic, sod_mesh, wave_ic
 from gpu_util import cube_ops, ctx, pair, relerr
-from test_oracle_pins import SOURCE_CASES, source_prm
+from test_oracle_pins import (GOLDEN_CASES, RIECG_GOLDEN, SOURCE_CASES, check_golden,
+                              golden_case, golden_run, source_prm)
 from xyst_gb300 import lib, riecg
 
 pytestmark = pytest.mark.gpu
@@ -258,28 +259,28 @@ def test_sod_reference_baseline_on_gpu():
             assert np.all(np.abs(f[i] - ref_f[i])[big] <= 1e-7 * np.abs(ref_f[i][big]))
 
 
-def test_taylor_green_reference_baseline_on_gpu():
-    """The reference's RieCG Taylor-Green regression on the GPU in FP64 mode:
-    the taylor_green manufactured energy source, the analytic state as
-    Dirichlet values on all six side sets, gamma 5/3, CFL 0.8, to t = 1 (68
-    steps, the last one cut); the diagnostics of every second step and the
-    fields at steps 20, 40, 60 and 68 within the reference's numdiff and
-    exodiff tolerances."""
-    from test_oracle_pins import (check_taylor_green_golden, taylor_green_case,
-                                  taylor_green_steps)
-    m, dd = taylor_green_case()
+@pytest.mark.parametrize("name", RIECG_GOLDEN)
+def test_manufactured_solution_baselines_on_gpu(name):
+    """The reference's RieCG Taylor-Green and vortical-flow regressions (the
+    latter also with stab2) on the GPU in FP64 mode: the problem's source,
+    its analytic state as Dirichlet values on all six side sets, gamma 5/3,
+    CFL 0.8, to t = 1 with the last step cut; every diagnostics row and the
+    fields at every output time within the reference's numdiff and exodiff
+    tolerances."""
+    m, dd, state = golden_case(name)
+    problem, stab2 = GOLDEN_CASES[name][:2]
     ops = riecg.operators(m, dir_sets=[1, 2, 3, 4, 5, 6], renumber=True)
     d = riecg.RieCG(ctx(), ops["coord"], ops["vol"], [None, None, ops["edges"]],
                     [None, None, ops["dint"]], ops["tri"], ops["besym"], gamma=5.0 / 3.0,
-                    cfl=0.8)
-    U0 = taylor_green_state(ops["coord"])
+                    cfl=0.8, stab2=stab2)
+    U0 = state(ops["coord"])
     dn = ops["dirnodes"]
     d.set_bc(dir=(dn, np.ones((dn.size, 5), np.int32), U0[dn]))
-    d.set_source("taylor_green", source_prm("taylor_green"))
+    d.set_source(problem, source_prm(problem))
     d.set_state(U0, 0.0)
     d.bc()
-    rows, states = taylor_green_steps(d, 1.0, ops["vol"], {20, 40, 60, 68})
-    check_taylor_green_golden(rows, states, ops["coord"], dd)
+    rows, states = golden_run(d, 1.0, ops["vol"])
+    check_golden(name, rows, states, ops["coord"], dd)
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
