@@ -104,8 +104,12 @@ int xg_riecg_setup(xg_ctx* ctx, const xg_riecg_params* prm, int64_t npoin,
  *   sym:  m_symbcnodes / m_symbcnorms (a node may repeat, once per set);
  *   far:  m_farbcnodes / m_farbcnorms and the farfield state far5 =
  *         {density, u, v, w, pressure};
- *   dir:  node ids, 5 mask ints per node (nonzero: component is set) and
- *         5 values per node (time independent Dirichlet data);
+ *   dir:  node ids, 5 mask ints per node and 5 values per node
+ *         (physics::dirbc, src/Physics/BC.cpp:30-71): with a problem set
+ *         (xg_riecg_set_source) a component of mask 1 takes the problem's
+ *         analytic state at the BC's time (t + dt/3, t + dt/2, t + dt in the
+ *         stages, RieCG.cpp:1028; t in xg_riecg_bc); any other nonzero mask
+ *         sets the given value;
  *   pre:  m_prebcnodes / m_prebcvals (density, pressure per node).
  * Any count may be zero. */
 int xg_riecg_set_bc(xg_ctx* ctx,
@@ -159,7 +163,8 @@ int xg_riecg_dt(xg_ctx* ctx, double* dt);
 
 /* One RK stage on the device state with a given dt: grad, rhs, update
  * U = Un - rkcoef[stage]*dt*R/V, BCs (RieCG::grad/rhs/solve,
- * src/Inciter/RieCG.cpp:871-1057). */
+ * src/Inciter/RieCG.cpp:871-1057).  Stage 2 completes the step: the
+ * context's time advances by dt. */
 int xg_riecg_stage(xg_ctx* ctx, int stage, double dt);
 
 /* Advance nstep full time steps (CFL dt, 3 stages) on the device without
@@ -217,7 +222,9 @@ int xg_kozcg_setup(xg_ctx* ctx, const xg_kozcg_params* prm, int64_t npoin, const
                    const double* vol, int64_t nelem, const uint64_t* inpoel);
 
 /* Symmetry (m_symbcnodes / m_symbcnorms) and Dirichlet (nodes, 5 mask ints,
- * 5 values per node) BCs applied by KozCG::BC (src/Inciter/KozCG.cpp:590-611). */
+ * 5 values per node) BCs applied by KozCG::BC (src/Inciter/KozCG.cpp:590-611):
+ * masks as for xg_riecg_set_bc, the BC's time the end of the step
+ * (KozCG.cpp:1167; the context's time in xg_kozcg_bc). */
 int xg_kozcg_set_bc(xg_ctx* ctx, int64_t nsym, const uint64_t* symnodes, const double* symnorms,
                     int64_t ndir, const uint64_t* dirnodes, const int32_t* dirmask,
                     const double* dirvals);

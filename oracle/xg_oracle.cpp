@@ -406,6 +406,63 @@ void problem_source(int src, const real* sprm, real gamma, real x, real y, real 
   }
 }
 
+// The problems' analytic states at (x, y, z, t), conserved variables (the
+// problems' ic functions, src/Physics/Problems.cpp: nonlinear_energy_growth
+// 117-151, rayleigh_taylor 226-258, taylor_green 409-428, vortical_flow
+// 453-478, with eos::totalenergy, src/Physics/EOS.hpp:53-56): what
+// physics::dirbc sets where a Dirichlet mask is 1.
+void problem_ic(int src, const real* sprm, real gamma, real x, real y, real z, real t,
+                real o[5]) {
+  const real g = gamma;
+  const real a = sprm[0], b0 = sprm[1], b1 = sprm[2], b2 = sprm[3];
+  const real kap = sprm[4], r0 = sprm[5], p0 = sprm[6], ce = sprm[7];
+  auto energy = [g](real r, real u, real v, real w, real p) {
+    return p / (g - 1.0) + 0.5 * r * (u * u + v * v + w * w);
+  };
+  if (src == 1) {  // taylor_green
+    const real r = 1.0;
+    const real p = 10.0 + r / 4.0 * (std::cos(2.0 * M_PI * x) + std::cos(2.0 * M_PI * y));
+    const real u = std::sin(M_PI * x) * std::cos(M_PI * y);
+    const real v = -std::cos(M_PI * x) * std::sin(M_PI * y);
+    const real w = 0.0;
+    const real rE = energy(r, u, v, w, p);
+    o[0] = r, o[1] = r * u, o[2] = r * v, o[3] = r * w, o[4] = rE;
+  } else if (src == 2) {  // vortical_flow
+    const real ru = a * x - kap * y, rv = kap * x + a * y, rw = -2.0 * a * z;
+    const real rE = (ru * ru + rv * rv + rw * rw) / 2.0 + (p0 - 2.0 * a * a * z * z) / (g - 1.0);
+    o[0] = 1.0, o[1] = ru, o[2] = rv, o[3] = rw, o[4] = rE;
+  } else if (src == 3) {  // nonlinear_energy_growth
+    const real h = std::cos(b0 * M_PI * x) * std::cos(b1 * M_PI * y) * std::cos(b2 * M_PI * z);
+    const real r = r0 + std::exp(-a * t) * (1.0 - x * x - y * y - z * z);
+    const real re = r * std::pow(-3.0 * (ce + kap * h * h * t), -1.0 / 3.0);
+    o[0] = r, o[1] = 0.0, o[2] = 0.0, o[3] = 0.0, o[4] = re;
+  } else {  // rayleigh_taylor
+    const real gx = b0 * x * x + b1 * y * y + b2 * z * z;
+    const real r = r0 - gx;
+    const real ft = std::cos(kap * M_PI * t);
+    const real u = ft * z * std::sin(M_PI * x);
+    const real v = ft * z * std::cos(M_PI * y);
+    const real w = ft * (-0.5 * M_PI * z * z * (std::cos(M_PI * x) - std::sin(M_PI * y)));
+    const real rE = energy(r, u, v, w, p0 + a * gx);
+    o[0] = r, o[1] = r * u, o[2] = r * v, o[3] = r * w, o[4] = rE;
+  }
+}
+
+// Dirichlet values of node p at time t (physics::dirbc, src/Physics/
+// BC.cpp:30-71): with a problem set, components of mask 1 take its analytic
+// state at t; any other set component its given value.
+void dirichlet(int src, const real* sprm, real gamma, real x, real y, real z, real t,
+               const int32_t* mask, const real* val, real* u) {
+  real ic[5];
+  if (src) problem_ic(src, sprm, gamma, x, y, z, t, ic);
+  for (int c = 0; c < 5; ++c) {
+    if (mask[c] == 1 && src)
+      u[c] = ic[c];
+    else if (mask[c])
+      u[c] = val[c];
+  }
+}
+
 // riemann::rhs = advdom + advbnd + src (src/Physics/Riemann.cpp:652-946),
 // the source at the state's time t (RieCG::rhs passes the time at the start
 // of the step to every stage, RieCG.cpp:948-949).
@@ -469,11 +526,11 @@ void riecg_rhs(const RieCG& s, const real* G, const real* U, real* R) {
 // RieCG::BC (src/Inciter/RieCG.cpp:764-785) -> physics::dirbc, symbc, farbc,
 // prebc (src/Physics/BC.cpp:29-72, 110-136, 152-220, 222-241).  Dirichlet
 // values are given per node (time independent).
-void riecg_bc(RieCG& s, real* U) {
+void riecg_bc(RieCG& s, real* U, real t) {
   for (size_t i = 0; i < s.dirnode.size(); ++i) {
     int64_t p = s.dirnode[i];
-    for (int c = 0; c < 5; ++c)
-      if (s.dirmask[i * 5 + c]) U[p * 5 + c] = s.dirval[i * 5 + c];
+    dirichlet(s.src, s.sprm, s.gamma, s.x[p], s.y[p], s.z[p], t, &s.dirmask[i * 5],
+              &s.dirval[i * 5], &U[p * 5]);
   }
   for (size_t i = 0; i < s.symnode.size(); ++i) {
     int64_t p = s.symnode[i];
@@ -555,7 +612,7 @@ void riecg_stage(RieCG& s, int stage) {
   for (int64_t i = 0; i < n; ++i)
     for (int c = 0; c < 5; ++c)
       s.U[i * 5 + c] = s.Un[i * 5 + c] - rkcoef[stage] * s.dt * s.R[i * 5 + c] / s.vol[i];
-  riecg_bc(s, s.U.data());
+  riecg_bc(s, s.U.data(), s.t + rkcoef[stage] * s.dt);  // RieCG.cpp:1028
 }
 
 // --------------------------------------------------------------------------
@@ -647,11 +704,11 @@ void kozak_rhs(const KozCG& s, const real* U, real t, real dt, real* R) {
 }
 
 // KozCG::BC for the configured BC kinds (src/Inciter/KozCG.cpp:590-611).
-void kozcg_bc(KozCG& s, real* U) {
+void kozcg_bc(KozCG& s, real* U, real t) {
   for (size_t i = 0; i < s.dirnode.size(); ++i) {
     int64_t p = s.dirnode[i];
-    for (int c = 0; c < 5; ++c)
-      if (s.dirmask[i * 5 + c]) U[p * 5 + c] = s.dirval[i * 5 + c];
+    dirichlet(s.src, s.sprm, s.gamma, s.x[p], s.y[p], s.z[p], t, &s.dirmask[i * 5],
+              &s.dirval[i * 5], &U[p * 5]);
   }
   for (size_t i = 0; i < s.symnode.size(); ++i) {
     int64_t p = s.symnode[i];
@@ -801,7 +858,7 @@ void kozcg_step(KozCG& s) {
     for (int64_t i = 0; i < n; ++i)
       for (int c = 0; c < 5; ++c) s.A[i * 5 + c] = R[i * 5 + c] + s.A[i * 5 + c] / s.vol[i];
   }
-  kozcg_bc(s, s.A.data());
+  kozcg_bc(s, s.A.data(), s.t + s.dt);  // KozCG.cpp:1167
   s.U = s.A;
 }
 
@@ -1531,7 +1588,7 @@ void orc_riecg_set_source(void* h, int problem, const double* prm) {
 
 void orc_riecg_bc(void* h) {
   auto* s = static_cast<RieCG*>(h);
-  riecg_bc(*s, s->U.data());
+  riecg_bc(*s, s->U.data(), s->t);
 }
 
 double orc_riecg_dt(void* h) {
@@ -1554,10 +1611,16 @@ double orc_riecg_run(void* h, int64_t nstep, double* dts) {
 }
 
 // Single stage with a given dt (for stage-level parity tests).
+// One stage of the given dt; the last stage completes the step and advances
+// the time.
 void orc_riecg_stage(void* h, int stage, double dt) {
   auto* s = static_cast<RieCG*>(h);
   s->dt = dt;
   riecg_stage(*s, stage);
+  if (stage == 2) {
+    s->t += dt;
+    ++s->it;
+  }
 }
 
 // ---------------------------------------------------------------- KozCG

@@ -30,36 +30,39 @@ def sod_ic(coord, gamma=1.4):
     return U
 
 
-def taylor_green_state(coord, gamma=5.0 / 3.0):
-    """The stationary Taylor-Green vortex (problems::taylor_green::ic,
-    src/Physics/Problems.cpp:409-428): rho = 1, p = 10 + (cos 2 pi x +
-    cos 2 pi y) / 4, u = sin pi x cos pi y, v = -cos pi x sin pi y, w = 0."""
-    x, y = coord[0], coord[1]
-    r = np.ones_like(x)
-    p = 10.0 + r / 4.0 * (np.cos(2.0 * np.pi * x) + np.cos(2.0 * np.pi * y))
-    u = np.sin(np.pi * x) * np.cos(np.pi * y)
-    v = -np.cos(np.pi * x) * np.sin(np.pi * y)
-    U = np.zeros((coord.shape[1], 5))
-    U[:, 0] = r
-    U[:, 1] = r * u
-    U[:, 2] = r * v
-    U[:, 4] = p / (gamma - 1.0) + 0.5 * r * (u * u + v * v)
-    return U
-
-
-def vortical_flow_state(coord, a=0.1, k=1.0, p0=10.0, gamma=5.0 / 3.0):
-    """The vortical flow (problems::vortical_flow::ic, src/Physics/
-    Problems.cpp:453-478): rho = 1, momentum (a x - k y, k x + a y, -2 a z),
-    p = p0 - 2 a^2 z^2."""
+def problem_state(problem, prm, coord, t=0.0, gamma=5.0 / 3.0):
+    """A manufactured-solution problem's analytic state at time t, conserved
+    variables (the problems' ic functions, src/Physics/Problems.cpp:
+    nonlinear_energy_growth 117-151, rayleigh_taylor 226-258, taylor_green
+    409-428, vortical_flow 453-478); prm = alpha, beta[3], kappa, r0, p0, ce."""
+    a, b0, b1, b2, k, r0, p0, ce = prm
     x, y, z = coord
-    U = np.zeros((coord.shape[1], 5))
-    U[:, 0] = 1.0
-    U[:, 1] = a * x - k * y
-    U[:, 2] = k * x + a * y
-    U[:, 3] = -2.0 * a * z
-    U[:, 4] = (U[:, 1] ** 2 + U[:, 2] ** 2 + U[:, 3] ** 2) / 2.0 + (p0 - 2.0 * a * a * z * z) / (
-        gamma - 1.0)
-    return U
+    n = x.size
+    r = np.ones(n)
+    u = np.zeros(n)
+    v = np.zeros(n)
+    w = np.zeros(n)
+    if problem == "taylor_green":
+        p = 10.0 + r / 4.0 * (np.cos(2.0 * np.pi * x) + np.cos(2.0 * np.pi * y))
+        u = np.sin(np.pi * x) * np.cos(np.pi * y)
+        v = -np.cos(np.pi * x) * np.sin(np.pi * y)
+        rE = p / (gamma - 1.0) + 0.5 * r * (u * u + v * v)
+    elif problem == "vortical_flow":
+        u, v, w = a * x - k * y, k * x + a * y, -2.0 * a * z
+        rE = (u * u + v * v + w * w) / 2.0 + (p0 - 2.0 * a * a * z * z) / (gamma - 1.0)
+    elif problem == "nonlinear_energy_growth":
+        h = np.cos(b0 * np.pi * x) * np.cos(b1 * np.pi * y) * np.cos(b2 * np.pi * z)
+        r = r0 + np.exp(-a * t) * (1.0 - x * x - y * y - z * z)
+        rE = r * (-3.0 * (ce + k * h * h * t)) ** (-1.0 / 3.0)
+    else:  # rayleigh_taylor
+        gx = b0 * x * x + b1 * y * y + b2 * z * z
+        r = r0 - gx
+        ft = np.cos(k * np.pi * t)
+        u = ft * z * np.sin(np.pi * x)
+        v = ft * z * np.cos(np.pi * y)
+        w = ft * (-0.5 * np.pi * z * z * (np.cos(np.pi * x) - np.sin(np.pi * y)))
+        rE = (p0 + a * gx) / (gamma - 1.0) + 0.5 * r * (u * u + v * v + w * w)
+    return np.stack([r, r * u, r * v, r * w, rE], axis=1)
 
 
 def wave_ic(coord, gamma=1.4):

@@ -35,7 +35,11 @@ Sources, all read as data (nothing is executed):
     with its manufactured source (alpha 0.1, kappa 1, p0 10, gamma 5/3, CFL
     0.8, the analytic state as Dirichlet values on all six side sets, to
     t = 1), RieCG with and without stab2 and KozCG without FCT: the same
-    three files each.
+    three files each;
+  * tests/regression/inciter/{RieCG,KozCG}/{NonlinearEnergyGrowth,
+    RayleighTaylor}: the time-dependent manufactured solutions (Dirichlet
+    values of the analytic state at each BC's time; nleg.q to t = 1 at CFL
+    0.8, rayleigh_taylor.q 50 steps at CFL 0.5): the same three files each.
 """
 
 from __future__ import annotations
@@ -187,6 +191,16 @@ def main(ref: str):
         np.savez_compressed(os.path.join(HERE, name + ".npz"),
                             **regression_fixture(ref, scheme, "VorticalFlow", "unitcube_1k.exo",
                                                  out, diag, all_times=True))
+    for scheme in ("RieCG", "KozCG"):
+        low = scheme.lower()
+        np.savez_compressed(os.path.join(HERE, low + "_nonlinear_energy_growth.npz"),
+                            **regression_fixture(ref, scheme, "NonlinearEnergyGrowth",
+                                                 "unitcube_1k.exo", "nleg.std.exo", "diag.std",
+                                                 all_times=True))
+        np.savez_compressed(os.path.join(HERE, low + "_rayleigh_taylor.npz"),
+                            **regression_fixture(ref, scheme, "RayleighTaylor", "unitcube_1k.exo",
+                                                 "rayleigh_taylor.std.exo", "diag.std",
+                                                 all_times=True))
     print("wrote fixtures to", HERE)
 
 

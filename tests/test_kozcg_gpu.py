@@ -12,7 +12,7 @@ import pytest
 import oracle
 from common import random_state, sod_mesh, wave_ic
 from gpu_util import ctx, relerr
-from test_oracle_pins import (GOLDEN_CASES, KOZCG_GOLDEN, SOURCE_CASES, _by_coord, _fields,
+from test_oracle_pins import (KOZCG_GOLDEN, SOURCE_CASES, _by_coord, _fields,
                               check_golden, golden_case, golden_run, kozcg_sod_setup,
                               source_prm)
 from xyst_gb300 import kozcg, mesh, riecg
@@ -55,24 +55,24 @@ def test_dropin_rhs_with_source(problem):
 
 @pytest.mark.parametrize("name", KOZCG_GOLDEN)
 def test_manufactured_solution_baselines_on_gpu(name):
-    """The reference's KozCG Taylor-Green and vortical-flow regressions on
-    the GPU in FP64 (no FCT, the problem's source, Dirichlet on all six side
-    sets, to t = 1 with the last step cut by xg_kozcg_step): every
-    diagnostics row within 1e-7 relative and the fields at every output time
-    within the reference's exodiff tolerances."""
-    m, dd, state = golden_case(name)
-    problem = GOLDEN_CASES[name][0]
+    """The reference's KozCG manufactured-solution regressions (Taylor-Green,
+    vortical flow, nonlinear energy growth, Rayleigh-Taylor) on the GPU in
+    FP64 (no FCT, the problem's source, its analytic state as Dirichlet
+    values at each step's end time, steps given their dt by xg_kozcg_step):
+    every diagnostics row and the fields at every output time within the
+    reference's numdiff and exodiff tolerances."""
+    m, dd, case, state = golden_case(name)
     coord, inpoel = m["coord"], m["inpoel"]
     v = riecg.volumes(coord, inpoel)
-    d = kozcg.KozCG(ctx(), coord, v, inpoel, gamma=5.0 / 3.0, cfl=0.8, fct=False)
+    d = kozcg.KozCG(ctx(), coord, v, inpoel, gamma=5.0 / 3.0, cfl=case["cfl"], fct=False)
     U0 = state(coord)
     dn = np.unique(np.concatenate([m["bface"][s] for s in sorted(m["bface"])]))
     d.set_bc(dir=(dn, np.ones((dn.size, 5), np.int32), U0[dn]))
-    d.set_source(problem, source_prm(problem))
+    d.set_source(case["problem"], case["prm"])
     d.set_state(U0, 0.0)
-    rows, states = golden_run(d, 1.0, v)
+    rows, states = golden_run(d, case, v)
     check_golden(name, rows, states, coord, dd)
-    assert abs(d.state()[1] - 1.0) < 1e-15
+    assert abs(d.state()[1] - rows[-1, 1]) < 1e-15
 
 
 def test_dropin_rhs_fp32_bound():

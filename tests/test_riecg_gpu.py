@@ -7,9 +7,9 @@ fluxes, FP64 state and update) is held to the bound stated in each test."""
 import numpy as np
 import pytest
 
-from common import random_state, sod_ic, sod_mesh, wave_ic
+from common import problem_state, random_state, sod_ic, sod_mesh, wave_ic
 from gpu_util import cube_ops, ctx, pair, relerr
-from test_oracle_pins import (GOLDEN_CASES, RIECG_GOLDEN, SOURCE_CASES, check_golden,
+from test_oracle_pins import (RIECG_GOLDEN, SOURCE_CASES, check_golden,
                               golden_case, golden_run, source_prm)
 from xyst_gb300 import lib, riecg
 
@@ -79,21 +79,6 @@ def test_dropin_rhs_with_source_fp64(problem):
     assert relerr(d.rhs(Gv, U), Ro) > 1e-8  # the source was on
 
 
-def _rayleigh_taylor_state(coord, t, a=1.0, b=(1.0, 1.0, 1.0), k=1.0, r0=4.0, p0=1.0,
-                           g=1.4):
-    """The rayleigh_taylor manufactured solution at time t (its initial
-    condition, src/Physics/Problems.cpp:226-258), conserved variables."""
-    x, y, z = coord
-    gx = b[0] * x * x + b[1] * y * y + b[2] * z * z
-    r = r0 - gx
-    ft = np.cos(k * np.pi * t)
-    u = ft * z * np.sin(np.pi * x)
-    v = ft * z * np.cos(np.pi * y)
-    w = ft * (-0.5 * np.pi * z * z * (np.cos(np.pi * x) - np.sin(np.pi * y)))
-    rE = (p0 + a * gx) / (g - 1.0) + 0.5 * r * (u * u + v * v + w * w)
-    return np.stack([r, r * u, r * v, r * w, rE], axis=1)
-
-
 @pytest.mark.parametrize("problem", ["taylor_green", "rayleigh_taylor"])
 def test_run_with_source_fp64(problem):
     """Whole RK3 steps with a source, time-dependent for rayleigh_taylor:
@@ -105,7 +90,7 @@ def test_run_with_source_fp64(problem):
     ops = cube_ops(9)
     d, o = pair(ops)
     if problem == "rayleigh_taylor":
-        U0 = _rayleigh_taylor_state(ops["coord"], 0.1)
+        U0 = problem_state(problem, source_prm(problem), ops["coord"], 0.1, gamma=1.4)
     else:
         U0 = wave_ic(ops["coord"])
     for s in (d, o):
@@ -261,25 +246,24 @@ def test_sod_reference_baseline_on_gpu():
 
 @pytest.mark.parametrize("name", RIECG_GOLDEN)
 def test_manufactured_solution_baselines_on_gpu(name):
-    """The reference's RieCG Taylor-Green and vortical-flow regressions (the
-    latter also with stab2) on the GPU in FP64 mode: the problem's source,
-    its analytic state as Dirichlet values on all six side sets, gamma 5/3,
-    CFL 0.8, to t = 1 with the last step cut; every diagnostics row and the
-    fields at every output time within the reference's numdiff and exodiff
-    tolerances."""
-    m, dd, state = golden_case(name)
-    problem, stab2 = GOLDEN_CASES[name][:2]
+    """The reference's RieCG manufactured-solution regressions (Taylor-Green,
+    vortical flow with and without stab2, nonlinear energy growth,
+    Rayleigh-Taylor) on the GPU in FP64 mode: the problem's source, its
+    analytic state as Dirichlet values on all six side sets at each stage's
+    time, gamma 5/3; every diagnostics row and the fields at every output
+    time within the reference's numdiff and exodiff tolerances."""
+    m, dd, case, state = golden_case(name)
     ops = riecg.operators(m, dir_sets=[1, 2, 3, 4, 5, 6], renumber=True)
     d = riecg.RieCG(ctx(), ops["coord"], ops["vol"], [None, None, ops["edges"]],
                     [None, None, ops["dint"]], ops["tri"], ops["besym"], gamma=5.0 / 3.0,
-                    cfl=0.8, stab2=stab2)
+                    cfl=case["cfl"], stab2=case.get("stab2", False))
     U0 = state(ops["coord"])
     dn = ops["dirnodes"]
     d.set_bc(dir=(dn, np.ones((dn.size, 5), np.int32), U0[dn]))
-    d.set_source(problem, source_prm(problem))
+    d.set_source(case["problem"], case["prm"])
     d.set_state(U0, 0.0)
     d.bc()
-    rows, states = golden_run(d, 1.0, ops["vol"])
+    rows, states = golden_run(d, case, ops["vol"])
     check_golden(name, rows, states, ops["coord"], dd)
 
 

@@ -518,6 +518,8 @@ struct KBC {
   const int32_t* dirmask;
   const double* dirval;
   const double* symn;
+  SrcPrm prob;         // the problem whose analytic state mask-1 Dirichlet values take
+  const double* xyz;   // [3][n] node coordinates
 };
 
 // Symmetry projection of the momentum antidiffusive sums (KozCG.cpp:816-830).
@@ -856,9 +858,12 @@ __global__ void __launch_bounds__(kBlock) k_node_solve(int64_t n, const double* 
 
 // KozCG::BC: Dirichlet then symmetry (physics::dirbc/symbc), one thread per
 // BC node, with the node's CFL dt.
+// Nodal BCs (KozCG::BC) at time t: after a step t + dt (sc->tnext,
+// KozCG.cpp:1167), otherwise the caller's t_host (sc null).
 __global__ void __launch_bounds__(kBlock) k_bc(int64_t n, KBC bc, double gamma, double* U,
                                                 const double* __restrict__ vol, int want_dt,
-                                                unsigned long long* dtmin) {
+                                                unsigned long long* dtmin,
+                                                const KScalars* __restrict__ sc, double t_host) {
   int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   double dtp = DBL_MAX;
   if (i < bc.nbc) {
@@ -867,8 +872,8 @@ __global__ void __launch_bounds__(kBlock) k_bc(int64_t n, KBC bc, double gamma, 
     for (int c = 0; c < 5; ++c) u[c] = U[c * n + p];
     const int32_t d = bc.dir[i];
     if (d >= 0)
-      for (int c = 0; c < 5; ++c)
-        if (bc.dirmask[d * 5 + c]) u[c] = bc.dirval[d * 5 + c];
+      dirichlet(bc.prob, bc.xyz[p], bc.xyz[n + p], bc.xyz[2 * n + p], sc ? sc->tnext : t_host,
+                bc.dirmask + d * 5, bc.dirval + d * 5, u);
     for (int32_t k = bc.symp[i]; k < bc.symp[i + 1]; ++k) {
       const double* nn = bc.symn + 3 * k;
       double vn = u[1] * nn[0] + u[2] * nn[1] + u[3] * nn[2];
@@ -966,7 +971,8 @@ __global__ void k_soa_to_aos(int64_t n, int nc, const double* __restrict__ s,
 }
 
 KBC kbc_of(KozCGDev* d) {
-  return KBC{d->nbc, d->bcnode, d->bcdir, d->bcsymp, d->dirmask, d->dirval, d->symn};
+  return KBC{d->nbc,   d->bcnode, d->bcdir, d->bcsymp, d->dirmask,
+             d->dirval, d->symn,  d->src,   d->xyz};
 }
 
 int refresh_dt(xg_ctx* c, KozCGDev* d) {
@@ -1077,7 +1083,7 @@ int step_impl(xg_ctx* c, KozCGDev* d, const KArrays<F>& k) {
   XG_CHECK_LAUNCH(c);
   if (d->nbc) {
     k_bc<<<blocks_for(d->nbc, kBlock), kBlock, 0, s>>>(n, kbc_of(d), d->prm.gamma, d->U, d->vol,
-                                                        1, &d->scal->dtmin);
+                                                        1, &d->scal->dtmin, d->scal, 0.0);
     XG_CHECK_LAUNCH(c);
   }
   return XG_OK;
@@ -1454,8 +1460,8 @@ int xg_kozcg_bc(xg_ctx* c) {
   KozCGDev* d = c->kozcg;
   if (!d) return fail(c, XG_ERR_STATE, "kozcg_bc before kozcg_setup");
   if (d->nbc) {
-    k_bc<<<blocks_for(d->nbc, kBlock), kBlock, 0, c->stream>>>(d->n, kbc_of(d), d->prm.gamma,
-                                                                d->U, d->vol, 0, &d->scal->dtmin);
+    k_bc<<<blocks_for(d->nbc, kBlock), kBlock, 0, c->stream>>>(
+        d->n, kbc_of(d), d->prm.gamma, d->U, d->vol, 0, &d->scal->dtmin, nullptr, d->t);
     XG_CHECK_LAUNCH(c);
   }
   rc = refresh_dt(c, d);

@@ -99,6 +99,8 @@ struct RieCGDev {
   int32_t *bcnode = nullptr, *bcdir = nullptr, *bcsymp = nullptr, *bcfar = nullptr,
           *bcpre = nullptr, *dirmask = nullptr;
   double *symn = nullptr, *dirval = nullptr, *farn = nullptr, *preval = nullptr;
+  double* dirxyz = nullptr;       // [ndir][3] Dirichlet node coordinates
+  std::vector<double> xyz_host;  // [3][n] node coordinates (for dirxyz)
   double far5[5] = {1, 0, 0, 0, 1};
   // scalars and run bookkeeping
   Scalars* scal = nullptr;
@@ -1131,16 +1133,17 @@ struct BCProg {
   const double* farn;
   const double* preval;
   double far5[5];
+  SrcPrm prob;           // the problem whose analytic state mask-1 Dirichlet values take
+  const double* dirxyz;  // [ndir][3] coordinates of the Dirichlet nodes
 };
 
-// BC program entry i applied to the conserved state u of its node.
-__device__ __forceinline__ void apply_bc(const BCProg& bc, int64_t i, double gamma,
+// BC program entry i applied to the conserved state u of its node at time t.
+__device__ __forceinline__ void apply_bc(const BCProg& bc, int64_t i, double gamma, double t,
                                          double u[5]) {
   const int32_t d = bc.dir[i];
   if (d >= 0) {
-#pragma unroll
-    for (int c = 0; c < 5; ++c)
-      if (bc.dirmask[d * 5 + c]) u[c] = bc.dirval[d * 5 + c];
+    const double* x = bc.dirxyz + d * 3;
+    dirichlet(bc.prob, x[0], x[1], x[2], t, bc.dirmask + d * 5, bc.dirval + d * 5, u);
   }
   for (int32_t k = bc.symp[i]; k < bc.symp[i + 1]; ++k) {
     const double* nn = bc.symn + 3 * k;
@@ -1421,7 +1424,9 @@ __global__ void __launch_bounds__(kBlock)
     } else {
       double un[5];
       stage_state<F, STAGE, LEAN>(n, p, R, uo, vol, aux, scal->dt, Un, un);
-      if (b >= 0) apply_bc(bc, b, gamma_d, un);
+      // at the stage's time, t + c dt with c = 1/3, 1/2, 1 (RieCG.cpp:1028)
+      constexpr double rkc = STAGE == 0 ? 1.0 / 3.0 : (STAGE == 1 ? 1.0 / 2.0 : 1.0);
+      if (b >= 0) apply_bc(bc, b, gamma_d, scal->t + rkc * scal->dt, un);
       dtp = store_stage<F, STAGE, LEAN>(n, p, un, wp, vol, aux, gamma_d, U, Wout);
     }
   }
@@ -1498,7 +1503,7 @@ __global__ void __launch_bounds__(kBlock)
 template <class F>
 __global__ void __launch_bounds__(kBlock) k_bc(int64_t n, BCProg bc, double gamma, double* U,
                                                 F* __restrict__ W, const double* __restrict__ vol,
-                                                NodeAux aux, int want_dt,
+                                                NodeAux aux, double t, int want_dt,
                                                 unsigned long long* dtmin) {
   int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   double dtp = DBL_MAX;
@@ -1507,7 +1512,7 @@ __global__ void __launch_bounds__(kBlock) k_bc(int64_t n, BCProg bc, double gamm
     double u[5];
 #pragma unroll
     for (int c = 0; c < 5; ++c) u[c] = U[c * n + p];
-    apply_bc(bc, i, gamma, u);
+    apply_bc(bc, i, gamma, t, u);
     F o[8];
     load8(W + p * 8, o);
     dtp = store_node<F>(n, p, u, o, want_dt != 0, vol, aux, gamma, U, W);
@@ -1678,6 +1683,8 @@ BCProg bcprog_of(RieCGDev* d) {
   b.farn = d->farn;
   b.preval = d->preval;
   for (int i = 0; i < 5; ++i) b.far5[i] = d->far5[i];
+  b.prob = d->src;
+  b.dirxyz = d->dirxyz;
   return b;
 }
 
@@ -1752,7 +1759,7 @@ int launch_bc(xg_ctx* c, RieCGDev* d, F* W, int want_dt) {
   if (d->nbc == 0) return XG_OK;
   XG_PROF_LAUNCH(c, d, "riecg_bc",
                  (k_bc<F><<<blocks_for(d->nbc, kBlock), kBlock, 0, c->stream>>>(
-                     d->n, bcprog_of(d), d->prm.gamma, d->U, W, d->vol, aux_of(d), want_dt,
+                     d->n, bcprog_of(d), d->prm.gamma, d->U, W, d->vol, aux_of(d), d->t, want_dt,
                      &d->scal->dtmin)));
   return XG_OK;
 }
@@ -2176,6 +2183,7 @@ int xg_riecg_setup(xg_ctx* c, const xg_riecg_params* prm, int64_t npoin, const d
   d->nbn = nbn;
   d->nbt = nbtri;
   d->nbent = nbtri * 3;
+  d->xyz_host.assign(coord, coord + 3 * n);
   if (d->fp32)
     rc = alloc_and_upload<float>(c, d, coord, vol, soff, swidth, nbr, ddx, ddy, ddz, bidx, bptr,
                                  bent4, hl);
@@ -2264,6 +2272,7 @@ int xg_riecg_set_bc(xg_ctx* c, int64_t nsym, const uint64_t* symnodes, const dou
     A.plan(d->symn, symn.size());
     A.plan(d->dirmask, std::max<int64_t>(1, ndir) * 5);
     A.plan(d->dirval, std::max<int64_t>(1, ndir) * 5);
+    A.plan(d->dirxyz, std::max<int64_t>(1, ndir) * 3);
     A.plan(d->farn, std::max<int64_t>(1, nfar) * 3);
     A.plan(d->preval, std::max<int64_t>(1, npre) * 2);
     if (pass == 0) XG_CUDA(c, A.reserve());
@@ -2279,6 +2288,12 @@ int xg_riecg_set_bc(xg_ctx* c, int64_t nsym, const uint64_t* symnodes, const dou
   XG_CUDA(c, up(d->symn, symn.data(), symn.size() * 8));
   XG_CUDA(c, up(d->dirmask, dirmask, ndir * 5 * 4));
   XG_CUDA(c, up(d->dirval, dirvals, ndir * 5 * 8));
+  {
+    std::vector<double> dx(std::max<int64_t>(1, ndir) * 3, 0.0);
+    for (int64_t k = 0; k < ndir; ++k)
+      for (int j = 0; j < 3; ++j) dx[k * 3 + j] = d->xyz_host[j * d->n + dirnodes[k]];
+    XG_CUDA(c, up(d->dirxyz, dx.data(), ndir * 3 * 8));
+  }
   XG_CUDA(c, up(d->farn, farnorms, nfar * 3 * 8));
   XG_CUDA(c, up(d->preval, prevals, npre * 2 * 8));
   XG_CUDA(c, up(d->bcof, bcof.data(), bcof.size() * 4));
@@ -2634,6 +2649,7 @@ int xg_riecg_stage(xg_ctx* c, int stage, double dt) {
   rc = d->fp32 ? do_stage<float>(c, d, stage, false) : do_stage<double>(c, d, stage, false);
   if (rc) return rc;
   d->dt_valid = stage == 2;
+  if (stage == 2) d->t += dt;  // the step is complete
   rc = flush_profile(c, d);
   if (rc) return rc;
   XG_CUDA(c, cudaStreamSynchronize(c->stream));

@@ -89,4 +89,69 @@ __device__ inline void problem_source(const SrcPrm& q, double x, double y, doubl
   }
 }
 
+
+// The problems' analytic states at (x, y, z, t), conserved variables (the
+// problems' ic functions, src/Physics/Problems.cpp: nonlinear_energy_growth
+// 117-151, rayleigh_taylor 226-258, taylor_green 409-428, vortical_flow
+// 453-478, total energy as eos::totalenergy, src/Physics/EOS.hpp:53-56).
+__device__ inline void problem_ic(const SrcPrm& q, double x, double y, double z, double t,
+                                  double o[5]) {
+  const double pi = 3.14159265358979323846, g = q.gamma;
+  const double a = q.p[0], b0 = q.p[1], b1 = q.p[2], b2 = q.p[3];
+  const double kap = q.p[4], r0 = q.p[5], p0 = q.p[6], ce = q.p[7];
+  if (q.problem == XG_SRC_TAYLOR_GREEN) {
+    const double r = 1.0;
+    const double p = 10.0 + r / 4.0 * (cos(2.0 * pi * x) + cos(2.0 * pi * y));
+    const double u = sin(pi * x) * cos(pi * y), v = -cos(pi * x) * sin(pi * y), w = 0.0;
+    o[0] = r;
+    o[1] = r * u;
+    o[2] = r * v;
+    o[3] = r * w;
+    o[4] = p / (g - 1.0) + 0.5 * r * (u * u + v * v + w * w);
+  } else if (q.problem == XG_SRC_VORTICAL_FLOW) {
+    const double ru = a * x - kap * y, rv = kap * x + a * y, rw = -2.0 * a * z;
+    o[0] = 1.0;
+    o[1] = ru;
+    o[2] = rv;
+    o[3] = rw;
+    o[4] = (ru * ru + rv * rv + rw * rw) / 2.0 + (p0 - 2.0 * a * a * z * z) / (g - 1.0);
+  } else if (q.problem == XG_SRC_NONLINEAR_ENERGY_GROWTH) {
+    const double h = cos(b0 * pi * x) * cos(b1 * pi * y) * cos(b2 * pi * z);
+    const double r = r0 + exp(-a * t) * (1.0 - x * x - y * y - z * z);
+    o[0] = r;
+    o[1] = 0.0;
+    o[2] = 0.0;
+    o[3] = 0.0;
+    o[4] = r * pow(-3.0 * (ce + kap * h * h * t), -1.0 / 3.0);
+  } else {  // rayleigh_taylor
+    const double gx = b0 * x * x + b1 * y * y + b2 * z * z;
+    const double r = r0 - gx;
+    const double ft = cos(kap * pi * t);
+    const double u = ft * z * sin(pi * x), v = ft * z * cos(pi * y);
+    const double w = ft * (-0.5 * pi * z * z * (cos(pi * x) - sin(pi * y)));
+    o[0] = r;
+    o[1] = r * u;
+    o[2] = r * v;
+    o[3] = r * w;
+    o[4] = (p0 + a * gx) / (g - 1.0) + 0.5 * r * (u * u + v * v + w * w);
+  }
+}
+
+// Dirichlet values of a node at time t (physics::dirbc, src/Physics/
+// BC.cpp:30-71): with a problem set, components of mask 1 take its analytic
+// state at t; any other set component its given value.
+__device__ inline void dirichlet(const SrcPrm& q, double x, double y, double z, double t,
+                                 const int32_t* mask, const double* val, double u[5]) {
+  double ic[5];
+  const bool prob = q.problem != XG_SRC_NONE;
+  if (prob) problem_ic(q, x, y, z, t, ic);
+#pragma unroll
+  for (int c = 0; c < 5; ++c) {
+    if (mask[c] == 1 && prob)
+      u[c] = ic[c];
+    else if (mask[c])
+      u[c] = val[c];
+  }
+}
+
 }  // namespace xg
