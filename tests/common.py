@@ -174,3 +174,52 @@ def chocg_regression_setup(name, m):
         prm = dict(mu=0.01, cfl=0.05, flux="damp2", pc="jacobi", ptol=1e-3, pmaxit=500)
         nstep = 20
     return dirbc, noslip, pdir, prm, nstep
+
+
+# The ChoCG Poisson problems' right-hand sides and solutions (poisson_const,
+# poisson_sine, poisson_sine3: src/Physics/Problems.cpp:841-954).
+POISSON_PROBLEMS = {
+    "const": (lambda x, y, z: 6.0 + 0.0 * x, lambda x, y, z: x * x + y * y + z * z),
+    "sine": (lambda x, y, z: -np.pi * np.pi * x * y * np.sin(np.pi * z),
+             lambda x, y, z: x * y * np.sin(np.pi * z)),
+    "sine3": (lambda x, y, z: -3.0 * np.pi * np.pi * np.sin(np.pi * x) * np.sin(np.pi * y) *
+              np.sin(np.pi * z),
+              lambda x, y, z: np.sin(np.pi * x) * np.sin(np.pi * y) * np.sin(np.pi * z)),
+}
+
+
+def poisson_case(name, vol_of):
+    """A Poisson regression's system as ChoCG's start-up sets it up
+    (ChoCG.cpp:1046-1118): the pressure matrix's right-hand side pr V, the
+    solution's values as Dirichlet data on all six side sets.  Returns the
+    fixture, coordinates, tetrahedra, volumes, b, Dirichlet nodes and values
+    and the exact solution at the nodes."""
+    d = golden("chocg_poisson")
+    coord, inpoel = d["coord"], d["inpoel"]
+    x, y, z = coord
+    v = vol_of(coord, inpoel)
+    pr, sol = POISSON_PROBLEMS[name]
+    tri = np.concatenate([d[k] for k in sorted(d.files) if k.startswith("bface")])
+    dn = np.unique(tri.ravel())
+    return d, coord, inpoel, v, pr(x, y, z) * v, dn, sol(x[dn], y[dn], z[dn]), sol(x, y, z)
+
+
+def check_poisson(name, p, v, exact, d, coord):
+    """L2(p), L2(dp) (the change from zero), L2 and L1 of the error against
+    diag_poisson_<name>.std within its numdiff tolerance (abs or rel 1e-8),
+    and for poisson_const the pressure field against poisson_const.std.exo
+    (exodiff: relative 1e-7, floor 1e-8)."""
+    V = v.sum()
+    l2 = np.sqrt((p * p * v).sum() / V)
+    got = np.array([l2, l2, np.sqrt(((p - exact) ** 2 * v).sum() / V),
+                    (np.abs(p - exact) * v).sum() / V])
+    exp = d["diag_" + name][0, 3:7]
+    assert np.all(np.abs(got - exp) <= np.maximum(1e-8, 1e-8 * np.abs(exp))), (got, exp)
+    if name == "const":
+        from scipy.spatial import cKDTree
+        dist, idx = cKDTree(coord.T).query(d["out_coord"].T)
+        assert dist.max() < 1e-12
+        ref = d["const_pressure"]
+        m = np.maximum(np.abs(p[idx]), np.abs(ref))
+        big = m > 1e-8
+        assert np.all(np.abs(p[idx] - ref)[big] <= 1e-7 * m[big])

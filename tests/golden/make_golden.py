@@ -39,7 +39,12 @@ Sources, all read as data (nothing is executed):
   * tests/regression/inciter/{RieCG,KozCG}/{NonlinearEnergyGrowth,
     RayleighTaylor}: the time-dependent manufactured solutions (Dirichlet
     values of the analytic state at each BC's time; nleg.q to t = 1 at CFL
-    0.8, rayleigh_taylor.q 50 steps at CFL 0.5): the same three files each.
+    0.8, rayleigh_taylor.q 50 steps at CFL 0.5): the same three files each;
+  * tests/regression/inciter/ChoCG/Poisson: the pressure Poisson problems
+    poisson_const, poisson_sine and poisson_sine3 (right-hand side and
+    Dirichlet values from the problem's formulas on all six side sets, PCG
+    without preconditioner to 1e-6, at most 100 iterations): the mesh, the
+    three diagnostics files and the poisson_const pressure field.
 """
 
 from __future__ import annotations
@@ -160,6 +165,30 @@ def regression_fixture(ref: str, scheme: str, case: str, meshfile: str, outfile:
     return out
 
 
+def poisson_fixture(ref: str):
+    """The ChoCG Poisson regressions' mesh, the diagnostics of the
+    poisson_const, poisson_sine and poisson_sine3 runs, and the pressure of
+    the single-process poisson_const run (poisson_const.std.exo)."""
+    from xyst_gb300 import mesh as M
+    from scipy.io import netcdf_file
+
+    base = os.path.join(ref, "tests/regression/inciter/ChoCG/Poisson")
+    m = M.read_exo(os.path.join(base, "unitcube_01_1k.exo"))
+    out = {"coord": m["coord"], "inpoel": m["inpoel"]}
+    for s, tri in m["bface"].items():
+        out[f"bface{s}"] = tri
+    for name in ("const", "sine", "sine3"):
+        out["diag_" + name] = _diag(os.path.join(base, f"diag_poisson_{name}.std"))
+    f = netcdf_file(os.path.join(base, "poisson_const.std.exo"), "r", mmap=False)
+    names = ["".join(c.decode() for c in row if c) for row in f.variables["name_nod_var"][:]]
+    k = names.index("pressure")
+    out["const_pressure"] = np.array(f.variables[f"vals_nod_var{k + 1}"][:][-1], dtype=np.float64)
+    out["out_coord"] = np.stack([np.asarray(f.variables[c][:], dtype=np.float64)
+                                 for c in ("coordx", "coordy", "coordz")])
+    f.close()
+    return out
+
+
 def chocg_fixture(ref: str, case: str, meshfile: str, outfile: str, diagfile: str):
     return regression_fixture(ref, "ChoCG", case, meshfile, outfile, diagfile)
 
@@ -201,6 +230,7 @@ def main(ref: str):
                             **regression_fixture(ref, scheme, "RayleighTaylor", "unitcube_1k.exo",
                                                  "rayleigh_taylor.std.exo", "diag.std",
                                                  all_times=True))
+    np.savez_compressed(os.path.join(HERE, "chocg_poisson.npz"), **poisson_fixture(ref))
     print("wrote fixtures to", HERE)
 
 

@@ -5,7 +5,8 @@ import numpy as np
 import pytest
 
 import oracle
-from common import dirichlet_matrix_only, golden, laplacian_14
+from common import (POISSON_PROBLEMS, check_poisson, dirichlet_matrix_only, golden, laplacian_14,
+                    poisson_case)
 from gpu_util import ctx, relerr
 from xyst_gb300 import cg, mesh
 
@@ -79,6 +80,22 @@ def test_pcg_dirichlet_matches_oracle(pc):
     assert np.linalg.norm(res) < 1e-10 * nbo
     # the stored matrix is restored: plain products are unaffected
     assert relerr(s.mult(x), oracle.csr_mult(ia, ja, a, x)) < 1e-14
+
+
+@pytest.mark.parametrize("name", sorted(POISSON_PROBLEMS))
+def test_poisson_reference_baselines_on_gpu(name):
+    """The reference's ChoCG Poisson regressions through the ConjugateGradients
+    drop-in on the GPU: ChoCG::prelhs's matrix, the problem's right-hand
+    side pr V and Dirichlet values, FP64 PCG without preconditioner to 1e-6
+    (at most 100 iterations): the reference's diagnostics within 1e-8 and,
+    for poisson_const, its pressure field."""
+    d, coord, inpoel, v, b, dn, dv, exact = poisson_case(name, oracle.vol)
+    ia, ja, a = oracle.pressure_matrix(coord, inpoel)
+    s = cg.ConjugateGradients(ctx(), ia, ja, a)
+    s.init(x=np.zeros(coord.shape[1]), b=b, dirbc=(dn, dv), apply=True, pc="none")
+    s.solve(100, 1e-6)
+    assert s.converged()
+    check_poisson(name, s.solution(), v, exact, d, coord)
 
 
 def test_warm_start_and_maxit():

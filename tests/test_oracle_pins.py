@@ -12,8 +12,8 @@ import pytest
 
 import oracle
 import oracle.ref as ref
-from common import (dirichlet_matrix_only, golden, laplacian_14, problem_state, random_state,
-                    sod_ic, sod_mesh)
+from common import (POISSON_PROBLEMS, check_poisson, dirichlet_matrix_only, golden, laplacian_14,
+                    poisson_case, problem_state, random_state, sod_ic, sod_mesh)
 from xyst_gb300 import mesh
 
 needs_ref = pytest.mark.skipif(not ref.available(), reason="reference sources not built here")
@@ -452,6 +452,23 @@ def test_stages_and_steps_agree_with_time_dependent_data():
                 k.run(1)
         out.append(k.state())
     assert np.array_equal(out[0], out[1])
+
+
+@pytest.mark.parametrize("name", sorted(POISSON_PROBLEMS))
+def test_poisson_golden(name):
+    """The reference's ChoCG Poisson regressions (tests/regression/inciter/
+    ChoCG/Poisson, poisson_<name>.q): the start-up pressure solve of
+    ChoCG::prelhs's matrix with the problem's right-hand side and Dirichlet
+    values, PCG without preconditioner (the default) to 1e-6: the oracle's
+    restated CSR::dirichlet and ConjugateGradients against the reference's
+    diagnostics and, for poisson_const, its pressure field."""
+    d, coord, inpoel, v, b, dn, dv, exact = poisson_case(name, oracle.vol)
+    ia, ja, a = oracle.pressure_matrix(coord, inpoel)
+    a2, b2 = oracle.csr_dirichlet(ia, ja, a, b, dn, dv)
+    p, it, nr, nb, conv = oracle.pcg(ia, ja, a2, b2, np.zeros(coord.shape[1]), 100, 1e-6,
+                                     pc="none")
+    assert conv
+    check_poisson(name, p, v, exact, d, coord)
 
 
 @pytest.mark.parametrize("name", sorted(GOLDEN_CASES))
