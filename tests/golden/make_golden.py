@@ -44,7 +44,15 @@ Sources, all read as data (nothing is executed):
     poisson_const, poisson_sine and poisson_sine3 (right-hand side and
     Dirichlet values from the problem's formulas on all six side sets, PCG
     without preconditioner to 1e-6, at most 100 iterations): the mesh, the
-    three diagnostics files and the poisson_const pressure field.
+    three diagnostics files and the poisson_const pressure field;
+  * tests/regression/inciter/RieCG/Sedov: the Sedov blast on sedov_coarse.exo
+    (p0 4.86e3 at the origin node, gamma 5/3, CFL 0.5, symmetry on side sets
+    1-3, 10 steps): the mesh and the diagnostics (the checkout holds no
+    single-process field baseline);
+  * tests/regression/inciter/RieCG/Pipe: flow between pressure boundaries
+    (1e5 at side set 1, 99900 at 3, density 1, symmetry on 2, 4, 5, 6,
+    CFL 0.5, 20 steps): the mesh, the fields (pipe.std.exo) and the
+    diagnostics.
 """
 
 from __future__ import annotations
@@ -146,6 +154,12 @@ def regression_fixture(ref: str, scheme: str, case: str, meshfile: str, outfile:
 
     base = os.path.join(ref, "tests/regression/inciter", scheme, case)
     m = M.read_exo(os.path.join(base, meshfile))
+    if outfile is None:  # diagnostics only
+        out = {"coord": m["coord"], "inpoel": m["inpoel"],
+               "diag": _diag(os.path.join(base, diagfile))}
+        for s, tri in m["bface"].items():
+            out[f"bface{s}"] = tri
+        return out
     f = netcdf_file(os.path.join(base, outfile), "r", mmap=False)
     names = ["".join(c.decode() for c in row if c) for row in f.variables["name_nod_var"][:]]
     times = np.array(f.variables["time_whole"][:], dtype=np.float64)
@@ -231,6 +245,12 @@ def main(ref: str):
                                                  "rayleigh_taylor.std.exo", "diag.std",
                                                  all_times=True))
     np.savez_compressed(os.path.join(HERE, "chocg_poisson.npz"), **poisson_fixture(ref))
+    np.savez_compressed(os.path.join(HERE, "riecg_sedov.npz"),
+                        **regression_fixture(ref, "RieCG", "Sedov", "sedov_coarse.exo", None,
+                                             "diag.std"))
+    np.savez_compressed(os.path.join(HERE, "riecg_pipe.npz"),
+                        **regression_fixture(ref, "RieCG", "Pipe", "rectangle_01_1.5k.exo",
+                                             "pipe.std.exo", "diag.std", all_times=True))
     print("wrote fixtures to", HERE)
 
 

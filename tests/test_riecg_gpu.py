@@ -7,10 +7,10 @@ fluxes, FP64 state and update) is held to the bound stated in each test."""
 import numpy as np
 import pytest
 
-from common import problem_state, random_state, sod_ic, sod_mesh, wave_ic
+from common import golden, problem_state, random_state, sod_ic, sod_mesh, wave_ic
 from gpu_util import cube_ops, ctx, pair, relerr
-from test_oracle_pins import (RIECG_GOLDEN, SOURCE_CASES, check_golden,
-                              golden_case, golden_run, source_prm)
+from test_oracle_pins import (FLOW_CASES, RIECG_GOLDEN, SOURCE_CASES, check_golden,
+                              golden_case, golden_run, pressure_bc, source_prm)
 from xyst_gb300 import lib, riecg
 
 pytestmark = pytest.mark.gpu
@@ -265,6 +265,29 @@ def test_manufactured_solution_baselines_on_gpu(name):
     d.bc()
     rows, states = golden_run(d, case, ops["vol"])
     check_golden(name, rows, states, ops["coord"], dd)
+
+
+@pytest.mark.parametrize("name", sorted(FLOW_CASES))
+def test_flow_baselines_on_gpu(name):
+    """The reference's RieCG Sedov and Pipe regressions on the GPU in FP64
+    mode (symmetry and pressure side sets as their control files set them):
+    every diagnostics row and (Pipe) the fields at every output time within
+    the tolerances the oracle meets."""
+    case = FLOW_CASES[name]
+    d = golden(name)
+    m = {"coord": d["coord"], "inpoel": d["inpoel"],
+         "bface": {int(k[5:]): d[k] for k in d.files if k.startswith("bface")}}
+    ops = riecg.operators(m, sym_sets=list(case["sym"]), pre_sets=list(case["pre"]),
+                          renumber=True)
+    dev = riecg.RieCG(ctx(), ops["coord"], ops["vol"], [None, None, ops["edges"]],
+                      [None, None, ops["dint"]], ops["tri"], ops["besym"], gamma=case["gamma"],
+                      cfl=case["cfl"])
+    pn, pv = pressure_bc(ops["bface"], case["pre"])
+    dev.set_bc(sym=ops["sym"], pre=(pn, pv) if pn.size else None)
+    dev.set_state(case["state"](ops["coord"]), 0.0)
+    dev.bc()
+    rows, states = golden_run(dev, case, ops["vol"])
+    check_golden(name, rows, states, ops["coord"], d)
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
