@@ -149,11 +149,14 @@ def nodes_of(bface, sets):
 
 def chocg_regression_setup(name, m):
     """Boundary conditions and settings of the reference's ChoCG regressions
-    (tests/regression/inciter/ChoCG/Lid/ldc.q and Poiseuille/poiseuille_damp2.q)
-    as per-node lists in the mesh file's numbering: velocity Dirichlet
-    (nodes, mask, values), noslip nodes, pressure Dirichlet (nodes, values of
-    the initial solves), and the solver settings."""
+    (tests/regression/inciter/ChoCG/Lid/ldc.q, Poiseuille/poiseuille_damp2.q
+    and Sphere/inviscid_sphere.q) as per-node lists in the mesh file's
+    numbering: velocity Dirichlet (nodes, mask, values), noslip nodes,
+    pressure Dirichlet (nodes, values of the initial solves), the solver
+    settings, the step count, the symmetry side sets and the initial
+    velocity."""
     bf = m["bface"]
+    sym, u0 = (), (0.0, 0.0, 0.0)
     if name == "lid":
         dn = nodes_of(bf, [4])
         dirbc = (dn, np.ones((dn.size, 3), np.int32), np.tile([1.0, 0.0, 0.0], (dn.size, 1)))
@@ -161,6 +164,16 @@ def chocg_regression_setup(name, m):
         pdir = (np.array([0]), np.array([0.0]))  # hydrostat = 0, userdef pressure IC 0
         prm = dict(mu=0.01, cfl=0.9, flux="damp4", pc="jacobi", ptol=1e-3, pmaxit=500)
         nstep = 10
+    elif name == "inviscid_sphere":
+        dn = nodes_of(bf, [2])
+        dirbc = (dn, np.tile([1, 0, 0], (dn.size, 1)).astype(np.int32),
+                 np.tile([1.0, 0.0, 0.0], (dn.size, 1)))  # mask 1: the IC value u = 1
+        noslip = np.zeros(0, np.int64)
+        p3 = nodes_of(bf, [3])
+        pdir = (p3, np.zeros(p3.size))
+        prm = dict(mu=0.0, cfl=0.5, flux="damp2", pc="jacobi", ptol=1e-3, pmaxit=300)
+        nstep = 10
+        sym, u0 = (1, 4), (1.0, 0.0, 0.0)
     else:
         dn = nodes_of(bf, [1, 5])
         mask = np.tile([0, 1, 1], (dn.size, 1)).astype(np.int32)
@@ -173,7 +186,7 @@ def chocg_regression_setup(name, m):
         pdir = (pn[order], pv[order])
         prm = dict(mu=0.01, cfl=0.05, flux="damp2", pc="jacobi", ptol=1e-3, pmaxit=500)
         nstep = 20
-    return dirbc, noslip, pdir, prm, nstep
+    return dirbc, noslip, pdir, prm, nstep, sym, u0
 
 
 # The ChoCG Poisson problems' right-hand sides and solutions (poisson_const,

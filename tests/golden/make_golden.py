@@ -52,7 +52,11 @@ Sources, all read as data (nothing is executed):
   * tests/regression/inciter/RieCG/Pipe: flow between pressure boundaries
     (1e5 at side set 1, 99900 at 3, density 1, symmetry on 2, 4, 5, 6,
     CFL 0.5, 20 steps): the mesh, the fields (pipe.std.exo) and the
-    diagnostics.
+    diagnostics;
+  * tests/regression/inciter/ChoCG/Sphere: the inviscid flow past a sphere
+    (inviscid_sphere.q on sphere2_5K.exo: damp2, CFL 0.5, velocity (1, 0, 0)
+    held in x on side set 2, symmetry on 1 and 4, pressure 0 on 3, Jacobi
+    PCG to 1e-3, 10 steps): the mesh, the final fields and the diagnostics.
 """
 
 from __future__ import annotations
@@ -245,6 +249,9 @@ def main(ref: str):
                                                  "rayleigh_taylor.std.exo", "diag.std",
                                                  all_times=True))
     np.savez_compressed(os.path.join(HERE, "chocg_poisson.npz"), **poisson_fixture(ref))
+    np.savez_compressed(os.path.join(HERE, "chocg_inviscid_sphere.npz"),
+                        **chocg_fixture(ref, "Sphere", "sphere2_5K.exo", "inviscid_sphere.std.exo",
+                                        "diag_inviscid_sphere.std"))
     np.savez_compressed(os.path.join(HERE, "riecg_sedov.npz"),
                         **regression_fixture(ref, "RieCG", "Sedov", "sedov_coarse.exo", None,
                                              "diag.std"))

@@ -109,7 +109,7 @@ def test_theta_implicit_lid_dirichlet_rows():
     """The lid-driven cavity (noslip walls, lid velocity Dirichlet) with the
     theta-implicit prediction: the momentum system's zero rows at the noslip
     and Dirichlet components; three steps against the oracle."""
-    m, data, ops, kw, nstep = _regression_ops("lid")
+    m, data, ops, kw, nstep, _ = _regression_ops("lid")
     kw = dict(kw, ptol=1e-8)
     d = chocg.ChoCG(ctx(), ops, **kw)
     o = _oracle(ops, **kw)
@@ -131,11 +131,18 @@ def test_theta_implicit_lid_dirichlet_rows():
 
 def _regression_ops(name):
     m, data = chocg_mesh(name)
+    u0 = (0.0, 0.0, 0.0)
     if name == "lid":
         ops = chocg.operators(m, noslip_sets=[1, 2, 3, 5, 6],
                               dir_bcs=[(4, (1, 1, 1), (1.0, 0.0, 0.0))], hydrostat=0)
         kw = dict(mu=0.01, cfl=0.9, flux="damp4", pc="jacobi", ptol=1e-3, pmaxit=500)
         nstep = 10
+    elif name == "inviscid_sphere":
+        ops = chocg.operators(m, sym_sets=[1, 4], dir_bcs=[(2, (1, 0, 0), (1.0, 0.0, 0.0))],
+                              pdir_bcs=[(3, 0.0)])
+        kw = dict(mu=0.0, cfl=0.5, flux="damp2", pc="jacobi", ptol=1e-3, pmaxit=300)
+        nstep = 10
+        u0 = (1.0, 0.0, 0.0)
     else:
         ops = chocg.operators(m, noslip_sets=[3, 4],
                               dir_bcs=[(1, (0, 1, 1), (0.0, 0.0, 0.0)),
@@ -143,19 +150,20 @@ def _regression_ops(name):
                               pdir_bcs=[(1, 2.4), (2, 0.0)])
         kw = dict(mu=0.01, cfl=0.05, flux="damp2", pc="jacobi", ptol=1e-3, pmaxit=500)
         nstep = 20
-    return m, data, ops, kw, nstep
+    return m, data, ops, kw, nstep, u0
 
 
-@pytest.mark.parametrize("name", ["lid", "poiseuille"])
+@pytest.mark.parametrize("name", ["lid", "poiseuille", "inviscid_sphere"])
 def test_reference_regression_on_gpu(name, tmp_path):
-    """The reference's lid-driven cavity and Poiseuille regressions run
-    through the C ABI on renumbered (RCM) meshes: the diag file written by
-    DiagWriter matches the reference's diag baseline within its numdiff
-    tolerances, and the final fields match its exodiff tolerances."""
-    m, data, ops, kw, nstep = _regression_ops(name)
+    """The reference's lid-driven cavity, Poiseuille and inviscid sphere
+    regressions run through the C ABI on renumbered (RCM) meshes: the diag
+    file written by DiagWriter matches the reference's diag baseline within
+    its numdiff tolerances, and the final fields match its exodiff
+    tolerances."""
+    m, data, ops, kw, nstep, u0 = _regression_ops(name)
     d = chocg.ChoCG(ctx(), ops, **kw)
     n = ops["coord"].shape[1]
-    d.set_state(np.zeros((n, 3)))
+    d.set_state(np.tile(np.asarray(u0), (n, 1)))
     d.init()
     v = ops["vol"]
     t = 0.0

@@ -6,9 +6,11 @@
 * the whole restated ChoCG driver (initial projection, time steps, pressure
   PCG) against the reference's regression baselines committed in
   tests/golden/: the lid-driven cavity (damp4, hydrostat, noslip, lid
-  Dirichlet) and the damp2 Poiseuille flow (pressure Dirichlet sets), final
-  fields within the reference's exodiff tolerances and every per-step
-  diagnostic row within its numdiff tolerances.
+  Dirichlet), the damp2 Poiseuille flow (pressure Dirichlet sets) and the
+  inviscid flow past a sphere (symmetry, a velocity Dirichlet mask,
+  pressure Dirichlet), final fields within the reference's exodiff
+  tolerances and every per-step diagnostic row within its numdiff
+  tolerances.
 """
 
 import numpy as np
@@ -62,10 +64,14 @@ def chocg_oracle(name):
     e, de = oracle.domint(coord, inpoel, ncoef=5)
     tri = np.concatenate([m["bface"][s] for s in sorted(m["bface"])])  # all side sets
     ia, ja, a = oracle.pressure_matrix(coord, inpoel)
-    dirbc, noslip, pdir, prm, nstep = chocg_regression_setup(name, m)
+    dirbc, noslip, pdir, prm, nstep, sym_sets, u0 = chocg_regression_setup(name, m)
     o = oracle.ChoCG(coord, v, e, de, tri, ia, ja, a, **prm)
-    o.set_bc(dir=dirbc, noslip=noslip, pdir=pdir)
-    o.set_state(np.zeros((coord.shape[1], 3)), np.zeros(coord.shape[1]))
+    sym = None
+    if sym_sets:
+        sn, sv, _ = oracle.sym_bc(coord, m["bface"], list(sym_sets))
+        sym = (sn, sv)
+    o.set_bc(dir=dirbc, sym=sym, noslip=noslip, pdir=pdir)
+    o.set_state(np.tile(np.asarray(u0), (coord.shape[1], 1)), np.zeros(coord.shape[1]))
     return o, m, d, v, nstep
 
 
@@ -95,7 +101,7 @@ FIELD_TOL = {"lid": {"velocityx": 3e-7, "velocityy": 2e-6, "velocityz": 3e-7,
                      "pressure": 1e-7, "divergence": 1e-7}}
 
 
-@pytest.mark.parametrize("name", ["lid", "poiseuille"])
+@pytest.mark.parametrize("name", ["lid", "poiseuille", "inviscid_sphere"])
 def test_chocg_regression_golden(name):
     o, m, d, v, nstep = chocg_oracle(name)
     o.init()
