@@ -149,8 +149,9 @@ def nodes_of(bface, sets):
 
 def chocg_regression_setup(name, m):
     """Boundary conditions and settings of the reference's ChoCG regressions
-    (tests/regression/inciter/ChoCG/Lid/ldc.q, Poiseuille/poiseuille_damp2.q
-    and Sphere/inviscid_sphere.q) as per-node lists in the mesh file's
+    (tests/regression/inciter/ChoCG/Lid/ldc.q, Poiseuille/poiseuille_damp2.q,
+    Sphere/inviscid_sphere.q and Sphere/sphere_chocg_viscous_test.q) as
+    per-node lists in the mesh file's
     numbering: velocity Dirichlet (nodes, mask, values), noslip nodes,
     pressure Dirichlet (nodes, values of the initial solves), the solver
     settings, the step count, the symmetry side sets and the initial
@@ -174,6 +175,21 @@ def chocg_regression_setup(name, m):
         prm = dict(mu=0.0, cfl=0.5, flux="damp2", pc="jacobi", ptol=1e-3, pmaxit=300)
         nstep = 10
         sym, u0 = (1, 4), (1.0, 0.0, 0.0)
+    elif name == "viscous_sphere":
+        # a node on both velocity sets takes the union of their masks
+        d2, d4 = nodes_of(bf, [2]), nodes_of(bf, [4])
+        dn = np.union1d(d2, d4)
+        mask = np.zeros((dn.size, 3), np.int32)
+        mask[np.isin(dn, d2), 0] = 1
+        mask[np.isin(dn, d4)] = 1
+        dirbc = (dn, mask, np.tile([1.0, 0.0, 0.0], (dn.size, 1)))
+        noslip = nodes_of(bf, [1])
+        p3 = nodes_of(bf, [3])
+        pdir = (p3, np.zeros(p3.size))
+        prm = dict(mu=1.0 / 40.0, cfl=0.3, flux="damp4", rk=4, pc="jacobi", ptol=1e-3,
+                   pmaxit=300)
+        nstep = 20
+        u0 = (1.0, 0.0, 0.0)
     else:
         dn = nodes_of(bf, [1, 5])
         mask = np.tile([0, 1, 1], (dn.size, 1)).astype(np.int32)

@@ -56,7 +56,11 @@ Sources, all read as data (nothing is executed):
   * tests/regression/inciter/ChoCG/Sphere: the inviscid flow past a sphere
     (inviscid_sphere.q on sphere2_5K.exo: damp2, CFL 0.5, velocity (1, 0, 0)
     held in x on side set 2, symmetry on 1 and 4, pressure 0 on 3, Jacobi
-    PCG to 1e-3, 10 steps): the mesh, the final fields and the diagnostics.
+    PCG to 1e-3, 10 steps): the mesh, the final fields and the diagnostics;
+    and the viscous flow (sphere_chocg_viscous_test.q: Re 40, damp4, 4-stage
+    RK, CFL 0.3, noslip on the sphere, u = 1 held on the inflow set and all
+    of (1, 0, 0) on the far field, pressure 0 on the outflow, 20 steps): the
+    same three files.
 """
 
 from __future__ import annotations
@@ -252,6 +256,10 @@ def main(ref: str):
     np.savez_compressed(os.path.join(HERE, "chocg_inviscid_sphere.npz"),
                         **chocg_fixture(ref, "Sphere", "sphere2_5K.exo", "inviscid_sphere.std.exo",
                                         "diag_inviscid_sphere.std"))
+    np.savez_compressed(os.path.join(HERE, "chocg_viscous_sphere.npz"),
+                        **chocg_fixture(ref, "Sphere", "sphere2_5K.exo",
+                                        "sphere_chocg_viscous_test.std.exo",
+                                        "diag_sphere_chocg_viscous_test.std"))
     np.savez_compressed(os.path.join(HERE, "riecg_sedov.npz"),
                         **regression_fixture(ref, "RieCG", "Sedov", "sedov_coarse.exo", None,
                                              "diag.std"))

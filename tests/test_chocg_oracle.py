@@ -98,10 +98,16 @@ def chocg_diag_row(o, v, t, dt):
 # exodiff.cfg of both regressions: velocity x/y/z relative 3e-7 / 2e-6 / 3e-7
 # (Lid; Poiseuille uses its own file), others relative 1e-7 floor 1e-8
 FIELD_TOL = {"lid": {"velocityx": 3e-7, "velocityy": 2e-6, "velocityz": 3e-7,
-                     "pressure": 1e-7, "divergence": 1e-7}}
+                     "pressure": 1e-7, "divergence": 1e-7},
+             # the viscous sphere's exodiff is relative 1e-7 (floor 1e-8) for
+             # every field; the runs differ by at most 4e-10 in velocity and
+             # 1.1e-9 in pressure (1e-9 of their scale), which is more than
+             # 1e-7 of the values within about 1e-4 of zero, so an absolute
+             # 3e-9 is allowed besides
+             "viscous_sphere": {"abs": 3e-9}}
 
 
-@pytest.mark.parametrize("name", ["lid", "poiseuille", "inviscid_sphere"])
+@pytest.mark.parametrize("name", ["lid", "poiseuille", "inviscid_sphere", "viscous_sphere"])
 def test_chocg_regression_golden(name):
     o, m, d, v, nstep = chocg_oracle(name)
     o.init()
@@ -125,5 +131,6 @@ def test_chocg_regression_golden(name):
         rel = tol.get(fname, 1e-7)
         big = np.abs(exp) > 1e-8
         err = np.abs(val - exp)
-        assert np.all(err[big] <= rel * np.abs(exp[big]) + 1e-12), (fname, err.max())
+        assert np.all(err[big] <= rel * np.abs(exp[big]) + tol.get("abs", 1e-12)), (
+            fname, err.max())
         assert np.all(err[~big] <= 1e-8), fname
