@@ -214,23 +214,43 @@ POISSON_PROBLEMS = {
     "sine3": (lambda x, y, z: -3.0 * np.pi * np.pi * np.sin(np.pi * x) * np.sin(np.pi * y) *
               np.sin(np.pi * z),
               lambda x, y, z: np.sin(np.pi * x) * np.sin(np.pi * y) * np.sin(np.pi * z)),
+    "neumann": (lambda x, y, z: -3.0 * np.cos(2.0 * x) * np.exp(y),
+                lambda x, y, z: np.cos(2.0 * x) * np.exp(y)),
 }
+
+
+def _neumann_gradient(x, y, z):
+    """poisson_neumann's pressure gradient (Problems.cpp:966-972)."""
+    return np.array([-2.0 * np.sin(2.0 * x) * np.exp(y), np.cos(2.0 * x) * np.exp(y), 0.0 * x])
 
 
 def poisson_case(name, vol_of):
     """A Poisson regression's system as ChoCG's start-up sets it up
     (ChoCG.cpp:1046-1118): the pressure matrix's right-hand side pr V, the
-    solution's values as Dirichlet data on all six side sets.  Returns the
-    fixture, coordinates, tetrahedra, volumes, b, Dirichlet nodes and values
-    and the exact solution at the nodes."""
+    solution's values as Dirichlet data (on all six side sets; for
+    poisson_neumann on 1-3, with Neumann data on 4-6).  Returns the fixture,
+    coordinates, tetrahedra, volumes, b, Dirichlet nodes and values, the
+    exact solution at the nodes and the Neumann data."""
     d = golden("chocg_poisson")
-    coord, inpoel = d["coord"], d["inpoel"]
+    pre = "neumann_" if name == "neumann" else ""
+    coord, inpoel = d[pre + "coord"], d[pre + "inpoel"]
     x, y, z = coord
     v = vol_of(coord, inpoel)
     pr, sol = POISSON_PROBLEMS[name]
-    tri = np.concatenate([d[k] for k in sorted(d.files) if k.startswith("bface")])
-    dn = np.unique(tri.ravel())
-    return d, coord, inpoel, v, pr(x, y, z) * v, dn, sol(x[dn], y[dn], z[dn]), sol(x, y, z)
+    bface = {int(k[len(pre) + 5:]): d[k] for k in d.files
+             if k.startswith(pre + "bface") and k[len(pre) + 5:].isdigit()}
+    dirsets, neusets = ((1, 2, 3), (4, 5, 6)) if name == "neumann" else ((1, 2, 3, 4, 5, 6), ())
+    dn = np.unique(np.concatenate([bface[s] for s in dirsets]).ravel())
+    # Neumann data of the symmetry sets (ChoCG.cpp:1071-1092): each triangle
+    # takes n . grad p at its nodes off them, n = (b - a) x (c - a) / 6
+    neu = np.zeros(x.size)
+    for s in neusets:
+        for N in bface[s]:
+            n = np.cross(coord[:, N[1]] - coord[:, N[0]], coord[:, N[2]] - coord[:, N[0]]) / 6.0
+            for p in N:
+                neu[p] -= n @ _neumann_gradient(x[p], y[p], z[p])
+    return (d, coord, inpoel, v, pr(x, y, z) * v, dn, sol(x[dn], y[dn], z[dn]), sol(x, y, z),
+            neu)
 
 
 def check_poisson(name, p, v, exact, d, coord):

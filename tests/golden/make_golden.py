@@ -43,8 +43,10 @@ Sources, all read as data (nothing is executed):
   * tests/regression/inciter/ChoCG/Poisson: the pressure Poisson problems
     poisson_const, poisson_sine and poisson_sine3 (right-hand side and
     Dirichlet values from the problem's formulas on all six side sets, PCG
-    without preconditioner to 1e-6, at most 100 iterations): the mesh, the
-    three diagnostics files and the poisson_const pressure field;
+    without preconditioner to 1e-6, at most 100 iterations) and
+    poisson_neumann (Dirichlet on side sets 1-3, the solution's gradient as
+    Neumann data on 4-6): the meshes, the four diagnostics files and the
+    poisson_const pressure field;
   * tests/regression/inciter/RieCG/Sedov: the Sedov blast on sedov_coarse.exo
     (p0 4.86e3 at the origin node, gamma 5/3, CFL 0.5, symmetry on side sets
     1-3, 10 steps): the mesh and the diagnostics (the checkout holds no
@@ -188,9 +190,10 @@ def regression_fixture(ref: str, scheme: str, case: str, meshfile: str, outfile:
 
 
 def poisson_fixture(ref: str):
-    """The ChoCG Poisson regressions' mesh, the diagnostics of the
-    poisson_const, poisson_sine and poisson_sine3 runs, and the pressure of
-    the single-process poisson_const run (poisson_const.std.exo)."""
+    """The ChoCG Poisson regressions' meshes, the diagnostics of the
+    poisson_const, poisson_sine, poisson_sine3 and poisson_neumann runs, and
+    the pressure of the single-process poisson_const run
+    (poisson_const.std.exo)."""
     from xyst_gb300 import mesh as M
     from scipy.io import netcdf_file
 
@@ -201,6 +204,12 @@ def poisson_fixture(ref: str):
         out[f"bface{s}"] = tri
     for name in ("const", "sine", "sine3"):
         out["diag_" + name] = _diag(os.path.join(base, f"diag_poisson_{name}.std"))
+    out["diag_neumann"] = _diag(os.path.join(base, "diag_poisson_neumann.std"))
+    m2 = M.read_exo(os.path.join(base, "unitcube_0pidiv4_1k.exo"))
+    out["neumann_coord"] = m2["coord"]
+    out["neumann_inpoel"] = m2["inpoel"]
+    for s, tri in m2["bface"].items():
+        out[f"neumann_bface{s}"] = tri
     f = netcdf_file(os.path.join(base, "poisson_const.std.exo"), "r", mmap=False)
     names = ["".join(c.decode() for c in row if c) for row in f.variables["name_nod_var"][:]]
     k = names.index("pressure")

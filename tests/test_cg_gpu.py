@@ -89,10 +89,10 @@ def test_poisson_reference_baselines_on_gpu(name):
     side pr V and Dirichlet values, FP64 PCG without preconditioner to 1e-6
     (at most 100 iterations): the reference's diagnostics within 1e-8 and,
     for poisson_const, its pressure field."""
-    d, coord, inpoel, v, b, dn, dv, exact = poisson_case(name, oracle.vol)
+    d, coord, inpoel, v, b, dn, dv, exact, neu = poisson_case(name, oracle.vol)
     ia, ja, a = oracle.pressure_matrix(coord, inpoel)
     s = cg.ConjugateGradients(ctx(), ia, ja, a)
-    s.init(x=np.zeros(coord.shape[1]), b=b, dirbc=(dn, dv), apply=True, pc="none")
+    s.init(x=np.zeros(coord.shape[1]), b=b, neubc=neu, dirbc=(dn, dv), apply=True, pc="none")
     s.solve(100, 1e-6)
     assert s.converged()
     check_poisson(name, s.solution(), v, exact, d, coord)

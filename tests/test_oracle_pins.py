@@ -469,9 +469,9 @@ def test_poisson_golden(name):
     values, PCG without preconditioner (the default) to 1e-6: the oracle's
     restated CSR::dirichlet and ConjugateGradients against the reference's
     diagnostics and, for poisson_const, its pressure field."""
-    d, coord, inpoel, v, b, dn, dv, exact = poisson_case(name, oracle.vol)
+    d, coord, inpoel, v, b, dn, dv, exact, neu = poisson_case(name, oracle.vol)
     ia, ja, a = oracle.pressure_matrix(coord, inpoel)
-    a2, b2 = oracle.csr_dirichlet(ia, ja, a, b, dn, dv)
+    a2, b2 = oracle.csr_dirichlet(ia, ja, a, b + neu, dn, dv)
     p, it, nr, nb, conv = oracle.pcg(ia, ja, a2, b2, np.zeros(coord.shape[1]), 100, 1e-6,
                                      pc="none")
     assert conv
