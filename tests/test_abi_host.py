@@ -148,3 +148,70 @@ int main(void) {
     assert r.returncode == 0, r.stderr
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0 and r.stdout.strip() == "ok", (r.returncode, r.stdout, r.stderr)
+
+
+# ---------------------------------------------------------------- edge cases
+
+# one tetrahedron with unit legs along the axes (J = 1, volume 1/6)
+TET_COORD = np.array([[0.0, 1.0, 0.0, 0.0], [0.0, 0.0, 1.0, 0.0], [0.0, 0.0, 0.0, 1.0]])
+TET = np.array([[0, 1, 2, 3]])
+
+
+def test_host_setup_rejects_bad_input():
+    """Node ids past the node count, an empty node set and a degenerate tet
+    come back as status codes (the wrappers raise), never as a crash."""
+    bad = np.array([[0, 1, 2, 4]])
+    with pytest.raises(RuntimeError):
+        riecg.rcm(bad, 4)
+    with pytest.raises(ValueError):
+        riecg.volumes(TET_COORD, bad)
+    with pytest.raises(RuntimeError):
+        riecg.edges(TET_COORD, bad)
+    with pytest.raises(RuntimeError):
+        riecg.rcm(TET, 0)
+    flat = TET_COORD.copy()
+    flat[2, 3] = 0.0  # all four nodes in one plane: J = 0
+    with pytest.raises(ValueError):
+        riecg.volumes(flat, TET)
+    from xyst_gb300 import cg
+    with pytest.raises(ValueError):
+        cg.pressure_matrix(TET_COORD, bad)
+
+
+def test_single_tet_operators():
+    """The operators of one tetrahedron against their closed forms: nodal
+    volumes J/24 each, six edges oriented from the smaller id, and the
+    pressure matrix -grad_a.grad_b V (symmetric, zero row sums)."""
+    v = riecg.volumes(TET_COORD, TET)
+    assert np.allclose(v, 1.0 / 24.0, rtol=0, atol=1e-16)
+    e, d = riecg.edges(TET_COORD, TET)
+    assert e.shape == (6, 2) and d.shape == (6, 3)
+    assert np.all(e[:, 0] < e[:, 1])
+    from xyst_gb300 import cg
+    ia, ja, a = cg.pressure_matrix(TET_COORD, TET)
+    A = np.zeros((4, 4))
+    for i in range(4):
+        A[i, ja[ia[i]:ia[i + 1]]] = a[ia[i]:ia[i + 1]]
+    grads = np.array([[-1.0, -1.0, -1.0], [1.0, 0.0, 0.0], [0.0, 1.0, 0.0], [0.0, 0.0, 1.0]])
+    assert np.allclose(A, -grads @ grads.T / 6.0, rtol=0, atol=1e-15)
+    assert np.allclose(A.sum(1), 0.0, atol=1e-15)
+
+
+def test_rcm_disconnected_and_isolated_nodes():
+    """Two separate tetrahedra and a node that no element uses: the
+    renumbering is still a permutation of all nine nodes, and each connected
+    piece takes consecutive numbers."""
+    ip = np.array([[0, 1, 2, 3], [4, 5, 6, 7]])
+    r = riecg.rcm(ip, 9)
+    assert sorted(r) == list(range(9))
+    for piece in ([0, 1, 2, 3], [4, 5, 6, 7]):
+        nums = np.sort(r[piece])
+        assert nums[-1] - nums[0] == 3
+
+
+def test_bnorm_rejects_nodes_off_the_faces():
+    faces = np.array([[0, 2, 1]])  # the z = 0 face of the tetrahedron
+    n = riecg.bnorm(TET_COORD, faces, np.array([0, 1, 2]))
+    assert np.allclose(np.abs(n[:, 2]), 1.0) and np.allclose(n[:, :2], 0.0)
+    with pytest.raises(RuntimeError):
+        riecg.bnorm(TET_COORD, faces, np.array([3]))
