@@ -1294,7 +1294,7 @@ int xg_kozcg_setup(xg_ctx* c, const xg_kozcg_params* prm, int64_t npoin, const d
                                                           d->geo32);
     XG_CHECK_LAUNCH(c);
   }
-  KScalars k0{0.0, 0ull, 0, 0};
+  KScalars k0{};  // every member zero
   double big = DBL_MAX;
   std::memcpy(&k0.dtmin, &big, sizeof(double));
   XG_CUDA(c, cudaMemcpyAsync(d->scal, &k0, sizeof(k0), cudaMemcpyHostToDevice, s));

@@ -1944,7 +1944,7 @@ int alloc_and_upload(xg_ctx* c, RieCGDev* d, const double* coord, const double* 
     XG_CUDA(c, cudaMemcpy(W1, w.data(), w.size() * sizeof(F), cudaMemcpyHostToDevice));
     XG_CUDA(c, cudaMemcpy(d->stage_W, w.data(), w.size() * sizeof(F), cudaMemcpyHostToDevice));
   }
-  Scalars s0{0.0, 0ull, 0, 0};
+  Scalars s0{};  // every member zero
   double big = DBL_MAX;
   std::memcpy(&s0.dtmin, &big, sizeof(double));
   XG_CUDA(c, cudaMemcpy(d->scal, &s0, sizeof(s0), cudaMemcpyHostToDevice));
